@@ -1,0 +1,248 @@
+/*
+ * lmgpu -- GB300-native ray traversal and path tracing behind Lightmetrica v3's Accel and
+ * Renderer interfaces. C ABI: plain pointers, sizes and status codes; no C++ or torch types.
+ *
+ * Every entry point returns LMGPU_OK (0) or an LMGPU_ERR_* code; the message of the last failure
+ * on the calling thread is lmgpu_last_error(). No exception crosses this boundary.
+ *
+ * Conventions shared with the reference (include/lm/math.h:54-56): Inf = 1e10, Eps = 1e-3 (an
+ * absolute ray offset). Ray tests follow src/accel/accel_sahbvh.cpp:58-75 (Moller-Trumbore with
+ * the reference's operation order) in fp32 with IEEE rounding and no fused multiply-add.
+ */
+#ifndef LMGPU_H
+#define LMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LMGPU_OK 0
+#define LMGPU_ERR_INVALID_ARGUMENT 1 /* lm::Error::InvalidArgument (include/lm/exception.h) */
+#define LMGPU_ERR_UNSUPPORTED 2      /* lm::Error::Unsupported */
+#define LMGPU_ERR_UNINITIALIZED 3    /* lm::Error::Uninitialized: e.g. render before build */
+#define LMGPU_ERR_CUDA 4             /* a CUDA runtime call failed */
+#define LMGPU_ERR_OUT_OF_MEMORY 5    /* device allocation failed or the HBM budget is exceeded */
+#define LMGPU_ERR_TIMEOUT 6          /* a bounded device-side wait gave up */
+#define LMGPU_ERR_INTERNAL 7         /* a device-side consistency check failed */
+
+typedef struct lmgpu_accel lmgpu_accel;
+typedef struct lmgpu_scene lmgpu_scene;
+typedef struct lmgpu_film lmgpu_film;
+
+/* Closest-hit record. Replaces Accel::Hit (include/lm/accel.h:49-55): `prim` is the flattened
+ * triangle index (the order in which Accel::build visits primitives and faces), which the caller
+ * maps to (primitive node, face) exactly as accel_sahbvh.cpp:296-298 maps indices_[mi].
+ * prim == -1 means no hit. t is the ray parameter, (u, v) the barycentrics of p2 and p3. */
+typedef struct lmgpu_hit {
+    float t, u, v;
+    int32_t prim;
+} lmgpu_hit;
+
+/* Accel statistics for reports (not part of the reference interface). */
+typedef struct lmgpu_accel_stats {
+    int64_t num_tris;
+    int64_t num_nodes;       /* 8-wide nodes, 80 bytes each */
+    int32_t max_depth;       /* 8-wide levels, root = 1 */
+    int32_t reserved;
+    double build_seconds;    /* host SAH build + collapse + upload */
+    double sah_cost;         /* SAH cost of the binary tree before collapsing */
+    int64_t device_bytes;    /* nodes + triangles resident on the device */
+} lmgpu_accel_stats;
+
+/* ---------------------------------------------------------------------------------------------
+ * Library
+ */
+const char* lmgpu_last_error(void);
+int lmgpu_version(void);
+/* Selects the CUDA device used by every later call on this thread's handles (default 0). */
+int lmgpu_set_device(int device);
+
+/* ---------------------------------------------------------------------------------------------
+ * Accel. Replaces the accel::sahbvh / accel::nanort / accel::embree slot.
+ */
+
+/* Accel construction; the accel's Json props (embree_params.h:105-115 for accel::embree) have no
+ * counterpart: the builder is fixed (binned SAH, collapsed to 8-wide quantized nodes). */
+int lmgpu_accel_create(lmgpu_accel** out);
+int lmgpu_accel_destroy(lmgpu_accel* accel);
+
+/* Accel::build(const Scene&) (include/lm/accel.h:38; accel_sahbvh.cpp:127-151 flattens the scene
+ * graph first). The caller passes the flattened triangles: tri_p holds num_tris x 9 floats, the
+ * world-space p1, p2, p3 of each triangle in flattening order. The data is copied. */
+int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris);
+
+/* Accel::intersect(Ray, tmin, tmax) (include/lm/accel.h:70; accel_sahbvh.cpp:269-299) over a
+ * batch. Host buffers: rays is n x 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax); hits receives n
+ * records. Copies in, traces, copies out, synchronously. */
+int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgpu_hit* hits);
+
+/* Same, device-resident: d_rays (n x 8 floats, 16-byte aligned) and d_hits (n records) are
+ * device pointers; the trace is enqueued on `stream` (a cudaStream_t, 0 = legacy default stream)
+ * and the call returns without synchronizing. */
+int lmgpu_accel_intersect_device(lmgpu_accel* accel, const void* d_rays, int64_t n, void* d_hits, void* stream);
+
+/* Scene::visible (include/lm/scene.h:343-364) is a closest-hit query whose result is only tested
+ * for existence; this any-hit form returns the same boolean per ray: d_occluded[i] = 1 if any
+ * triangle is hit in [tmin, tmax]. Device pointers, enqueued on `stream`. */
+int lmgpu_accel_occluded_device(lmgpu_accel* accel, const void* d_rays, int64_t n, uint8_t* d_occluded, void* stream);
+
+int lmgpu_accel_get_stats(const lmgpu_accel* accel, lmgpu_accel_stats* out);
+
+/* Host-only build (no device needed; no reference counterpart): fills the 8-wide node words (20
+ * per node) and triangle records (12 floats per triangle) exactly as lmgpu_accel_build uploads
+ * them. `nodes` must hold 20 * max(num_tris, 1) words and `tris` 12 * num_tris floats. */
+int lmgpu_bvh8_build_host(const float* tri_p, int64_t num_tris, uint32_t* nodes, float* tris, int64_t* num_nodes,
+                          int32_t* max_depth);
+
+/* Instrumented trace (no reference counterpart; feeds the roofline's algorithmic byte count):
+ * over every `sample`-th ray of the device batch, the mean number of 8-wide nodes visited and
+ * of triangles tested, for closest-hit (any_hit = 0) or any-hit traversal. Synchronous. */
+int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, int32_t any_hit, int32_t sample,
+                             double* mean_nodes, double* mean_tris);
+
+/* ---------------------------------------------------------------------------------------------
+ * Scene description for rendering. Replaces the state that renderer::pt / renderer::raycast read
+ * through Scene_ (src/scene.cpp): flattened geometry with shading data, the primitive table, the
+ * materials (material_{diffuse,glossy,glass,mirror}.cpp), the light list in scene-graph traversal
+ * order (scene.cpp:279-286), and the camera (camera_pinhole.cpp).
+ */
+#define LMGPU_MAT_DIFFUSE 0
+#define LMGPU_MAT_GLOSSY 1
+#define LMGPU_MAT_GLASS 2
+#define LMGPU_MAT_MIRROR 3
+
+typedef struct lmgpu_material {
+    int32_t type;       /* LMGPU_MAT_* */
+    float color[3];     /* diffuse: Kd; glossy: Ks; otherwise unused */
+    float ax, ay;       /* glossy GGX roughness */
+    float ni;           /* glass index of refraction */
+} lmgpu_material;
+
+#define LMGPU_LIGHT_AREA 0
+#define LMGPU_LIGHT_ENVCONST 1
+#define LMGPU_LIGHT_ENV 2
+
+typedef struct lmgpu_light {
+    int32_t type;       /* LMGPU_LIGHT_* */
+    float ke[3];        /* area: Ke; envconst: Le */
+    /* area: a range of the light-triangle arrays below. The sampling CDF is built from the
+     * untransformed (mesh-local) triangle areas, as light_area.cpp:68-80 does. */
+    int64_t tri_offset, tri_count;
+    float transform_j;  /* |det| of the light primitive's linear transform (math.h:742-745) */
+    /* env: a w x h x 3 fp32 texel block at env_offset in env_texels; rot in degrees. */
+    int32_t env_w, env_h;
+    int64_t env_offset;
+    float rot_deg, scale;
+} lmgpu_light;
+
+typedef struct lmgpu_camera {
+    /* camera::pinhole props (camera_pinhole.cpp:76-97) */
+    float position[3], center[3], up[3];
+    float vfov, aspect;
+} lmgpu_camera;
+
+typedef struct lmgpu_scene_desc {
+    /* Flattened triangles in accel-build order (the same order as lmgpu_accel_build's input). */
+    int64_t num_tris;
+    const float* positions;      /* num_tris x 9: world-space p1, p2, p3 (the accel-build input) */
+    const float* normals;        /* num_tris x 9: per-corner normals transformed by normal_M */
+    const float* geo_normals;    /* num_tris x 3: normalize(normal_M * geometry_normal(local)) */
+    const int32_t* tri_prim;     /* num_tris: index into the primitive table */
+    /* Primitive table: one row per flattened primitive node that carries a mesh. */
+    int32_t num_prims;
+    const int32_t* prim_material; /* index into materials */
+    const int32_t* prim_light;    /* index into lights, or -1 */
+    int32_t num_materials;
+    const lmgpu_material* materials;
+    /* Lights in traversal order (uniform selection, scene.cpp:374-382). At most one env light. */
+    int32_t num_lights;
+    const lmgpu_light* lights;
+    int64_t num_light_tris;
+    const float* light_tri_p;      /* num_light_tris x 9: world-space p1, p2, p3 */
+    const float* light_tri_gn;     /* num_light_tris x 3: world-space geometry normal */
+    const float* light_tri_area;   /* num_light_tris: mesh-local triangle area */
+    int64_t num_env_texels;        /* floats in env_texels */
+    const float* env_texels;
+    int32_t has_camera;
+    lmgpu_camera camera;
+} lmgpu_scene_desc;
+
+/* Scene::build (src/scene.cpp:274-317) for the GPU renderers: uploads the description and binds
+ * the accel, which must already be built over the same flattened triangles. */
+int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_desc* desc);
+int lmgpu_scene_destroy(lmgpu_scene* scene);
+/* Device bytes the scene holds (geometry, shading data, tables), excluding the accel. */
+int lmgpu_scene_device_bytes(const lmgpu_scene* scene, int64_t* out);
+
+/* ---------------------------------------------------------------------------------------------
+ * Film. Replaces film::bitmap (src/film/film_bitmap.cpp): an fp32 RGB accumulator on the device.
+ * Pixel (x, y) is element y*w + x; row 0 is the bottom of the image (rp.y grows upward), as in
+ * the reference's raster_to_pixel (include/lm/film.h:166-171).
+ */
+int lmgpu_film_create(lmgpu_film** out, int32_t w, int32_t h);
+int lmgpu_film_destroy(lmgpu_film* film);
+int lmgpu_film_clear(lmgpu_film* film);
+/* Film::buffer (film_bitmap.cpp:202-208): copies h x w x 3 floats to host memory. */
+int lmgpu_film_read(lmgpu_film* film, float* out_rgb);
+/* Device pointer to the h x w x 3 fp32 pixels (valid until the film is destroyed). */
+int lmgpu_film_device_ptr(lmgpu_film* film, void** out);
+
+/* ---------------------------------------------------------------------------------------------
+ * Renderers.
+ */
+
+/* renderer::raycast (src/renderer/renderer_raycast.cpp:48-101). color may be NULL. */
+typedef struct lmgpu_raycast_params {
+    float bg_color[3];
+    int32_t use_constant_color;
+    int32_t visualize_normal;
+    int32_t has_color;
+    float color[3];
+} lmgpu_raycast_params;
+
+int lmgpu_render_raycast(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_raycast_params* params, void* stream);
+
+#define LMGPU_SAMPLING_NAIVE 0
+#define LMGPU_SAMPLING_NEE 1
+#define LMGPU_SAMPLING_MIS 2
+#define LMGPU_PRIMARY_PIXEL 0
+#define LMGPU_PRIMARY_IMAGE 1
+
+/* renderer::pt (src/renderer/renderer_pt.cpp:51-315) with scheduler::spp::sample
+ * (src/scheduler.cpp:17-50). max_verts counts path vertices including the camera vertex, so a
+ * maximum path length of L edges is max_verts = L + 1. Random numbers come from a Philox4x32-10
+ * stream keyed by (seed, pixel * spp + sample, vertex), independent of launch shape. */
+typedef struct lmgpu_pt_params {
+    int64_t spp;
+    int32_t max_verts;
+    uint32_t seed;
+    int32_t sampling_mode;      /* LMGPU_SAMPLING_* ("mis" is the reference default) */
+    int32_t primary_mode;       /* LMGPU_PRIMARY_* ("pixel" is the reference default) */
+    int64_t wave_paths;         /* paths in flight per wave; 0 = library default */
+    int32_t accumulate;         /* 1: add to the film without clearing or rescaling */
+    int32_t reserved;
+} lmgpu_pt_params;
+
+typedef struct lmgpu_render_stats {
+    int64_t paths;
+    int64_t rays;               /* every traced segment: extension + shadow */
+    int64_t extension_rays;
+    int64_t shadow_rays;
+    double elapsed_ms;          /* device time of the render (CUDA events) */
+    double trace_ms;            /* device time inside the extension + shadow trace kernels */
+} lmgpu_render_stats;
+
+/* Renders into `film` (cleared first unless params->accumulate) on `stream` and waits for it.
+ * stats may be NULL. The film holds the estimate scaled by 1/spp (pixel mode) or w*h/spp (image
+ * mode), as renderer_pt.cpp:307-312 rescales it. */
+int lmgpu_render_pt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params, void* stream,
+                    lmgpu_render_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LMGPU_H */

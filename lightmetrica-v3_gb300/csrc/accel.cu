@@ -1,0 +1,271 @@
+// Accel C-ABI (include/lmgpu.h): build the 8-wide BVH on the host, keep it resident on the
+// device, and trace batches of rays with one thread per ray.
+#include <chrono>
+#include <cstring>
+#include <mutex>
+
+#include "lmgpu_dev.cuh"
+#include "runtime.h"
+
+namespace lmgpu {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+DeviceInfo& current_device() {
+    thread_local DeviceInfo info;
+    thread_local bool init = false;
+    if (!init) {
+        LMGPU_CUDA(cudaGetDevice(&info.device));
+        LMGPU_CUDA(cudaDeviceGetAttribute(&info.num_sms, cudaDevAttrMultiProcessorCount, info.device));
+        init = true;
+    }
+    return info;
+}
+
+constexpr int kTraceBlock = 128;
+
+// One thread per ray, grid-stride. rays: 2 float4 per ray (o, tmin) (d, tmax).
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const float4* __restrict__ rays, int64_t n,
+                                                            lmgpu_hit* __restrict__ hits, uint8_t* __restrict__ occluded,
+                                                            int* __restrict__ err) {
+    extern __shared__ uint32_t smem[];
+    const int stride = blockDim.x;
+    uint32_t* sb = smem + threadIdx.x;
+    uint32_t* sbits = smem + stride * bvh.depth + threadIdx.x;
+    int lerr = 0;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const float4 a = rays[2 * i], b = rays[2 * i + 1];
+        const TraceHit h = trace_bvh8<kAnyHit, false>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits,
+                                                      stride, nullptr, nullptr, &lerr);
+        if (kAnyHit) {
+            occluded[i] = h.id >= 0 ? 1 : 0;
+        } else {
+            lmgpu_hit r;
+            r.t = h.id >= 0 ? h.t : 0.f;
+            r.u = h.u;
+            r.v = h.v;
+            r.prim = h.id;
+            hits[i] = r;
+        }
+    }
+    if (lerr) atomicOr(err, lerr);
+}
+
+// Instrumented pass: node visits and triangle tests summed over every `sample`-th ray.
+template <bool kAnyHit>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_count(Bvh8 bvh, const float4* __restrict__ rays, int64_t n,
+                                                            int sample, unsigned long long* sums, int* err) {
+    extern __shared__ uint32_t smem[];
+    const int stride = blockDim.x;
+    uint32_t* sb = smem + threadIdx.x;
+    uint32_t* sbits = smem + stride * bvh.depth + threadIdx.x;
+    int lerr = 0;
+    uint32_t nodes = 0, tris = 0, cnt = 0;
+    for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j * sample < n; j += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = j * sample;
+        const float4 a = rays[2 * i], b = rays[2 * i + 1];
+        trace_bvh8<kAnyHit, true>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits, stride, &nodes, &tris,
+                                  &lerr);
+        cnt++;
+    }
+    atomicAdd(&sums[0], (unsigned long long)nodes);
+    atomicAdd(&sums[1], (unsigned long long)tris);
+    atomicAdd(&sums[2], (unsigned long long)cnt);
+    if (lerr) atomicOr(err, lerr);
+}
+
+template <typename K>
+int trace_grid(K kernel, size_t smem, int64_t n) {
+    int per_sm = 0;
+    LMGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceBlock, smem));
+    per_sm = per_sm < 1 ? 1 : per_sm;
+    const int64_t need = (n + kTraceBlock - 1) / kTraceBlock;
+    int64_t g = int64_t(per_sm) * current_device().num_sms;
+    if (need < g) g = need;
+    return int(g < 1 ? 1 : g);
+}
+
+Bvh8 device_view(const lmgpu_accel* a) {
+    Bvh8 b;
+    b.nodes = a->nodes.as<const uint4>();
+    b.tris = a->tris.as<const float4>();
+    b.depth = a->depth;
+    b.num_nodes = uint32_t(a->num_nodes);
+    return b;
+}
+
+size_t trace_smem(const lmgpu_accel* a) { return size_t(2) * 4 * kTraceBlock * size_t(a->depth); }
+
+void check_built(const lmgpu_accel* a) {
+    if (!a) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "accel is null");
+    if (a->num_nodes == 0) throw Error(LMGPU_ERR_UNINITIALIZED, "accel is not built (call lmgpu_accel_build)");
+    if (a->depth > 96) throw Error(LMGPU_ERR_UNSUPPORTED, "BVH deeper than the traversal stack supports");
+}
+
+void launch_trace(const lmgpu_accel* a, const void* d_rays, int64_t n, void* d_hits, uint8_t* d_occ, cudaStream_t st,
+                  int* d_err) {
+    if (n <= 0) return;
+    if ((reinterpret_cast<uintptr_t>(d_rays) & 15u) != 0)
+        throw Error(LMGPU_ERR_INVALID_ARGUMENT, "ray buffer must be 16-byte aligned");
+    const Bvh8 b = device_view(a);
+    const size_t smem = trace_smem(a);
+    if (d_occ) {
+        const int g = trace_grid(k_trace_batch<true>, smem, n);
+        k_trace_batch<true><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n, nullptr, d_occ, d_err);
+    } else {
+        const int g = trace_grid(k_trace_batch<false>, smem, n);
+        k_trace_batch<false><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n,
+                                                           static_cast<lmgpu_hit*>(d_hits), nullptr, d_err);
+    }
+    LMGPU_CUDA(cudaGetLastError());
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+extern "C" {
+
+const char* lmgpu_last_error(void) { return g_last_error.c_str(); }
+
+int lmgpu_version(void) { return 1; }
+
+int lmgpu_set_device(int device) {
+    return guarded([&] {
+        LMGPU_CUDA(cudaSetDevice(device));
+        DeviceInfo& d = current_device();
+        d.device = device;
+        LMGPU_CUDA(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device));
+    });
+}
+
+int lmgpu_accel_create(lmgpu_accel** out) {
+    return guarded([&] {
+        if (!out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "out is null");
+        *out = new lmgpu_accel();  // device memory is allocated by lmgpu_accel_build
+    });
+}
+
+int lmgpu_accel_destroy(lmgpu_accel* accel) {
+    return guarded([&] { delete accel; });
+}
+
+int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris) {
+    return guarded([&] {
+        if (!accel || (!tri_p && num_tris > 0)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "accel or triangles null");
+        const auto t0 = std::chrono::steady_clock::now();
+        Bvh8Host h;
+        std::string err;
+        if (!build_bvh8(tri_p, num_tris, h, &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+        accel->nodes.upload(h.nodes.data(), h.nodes.size());
+        accel->tris.upload(h.tris.data(), h.tris.size());
+        accel->err.alloc(sizeof(int));
+        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
+        accel->num_tris = num_tris;
+        accel->num_nodes = int64_t(h.nodes.size() / 20);
+        accel->depth = h.max_depth;
+        accel->sah_cost = h.sah_cost;
+        LMGPU_CUDA(cudaDeviceSynchronize());
+        accel->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
+int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgpu_hit* hits) {
+    return guarded([&] {
+        check_built(accel);
+        if (n < 0 || (n > 0 && (!rays || !hits))) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "rays or hits null");
+        if (n == 0) return;
+        accel->scratch_rays.alloc(size_t(n) * 32);
+        accel->scratch_hits.alloc(size_t(n) * sizeof(lmgpu_hit));
+        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
+        LMGPU_CUDA(cudaMemcpy(accel->scratch_rays.p, rays, size_t(n) * 32, cudaMemcpyHostToDevice));
+        launch_trace(accel, accel->scratch_rays.p, n, accel->scratch_hits.p, nullptr, 0, accel->err.as<int>());
+        LMGPU_CUDA(cudaMemcpy(hits, accel->scratch_hits.p, size_t(n) * sizeof(lmgpu_hit), cudaMemcpyDeviceToHost));
+        int herr = 0;
+        LMGPU_CUDA(cudaMemcpy(&herr, accel->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed (code " + std::to_string(herr) + ")");
+    });
+}
+
+int lmgpu_accel_intersect_device(lmgpu_accel* accel, const void* d_rays, int64_t n, void* d_hits, void* stream) {
+    return guarded([&] {
+        check_built(accel);
+        if (n < 0 || (n > 0 && (!d_rays || !d_hits))) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "rays or hits null");
+        launch_trace(accel, d_rays, n, d_hits, nullptr, static_cast<cudaStream_t>(stream), accel->err.as<int>());
+    });
+}
+
+int lmgpu_accel_occluded_device(lmgpu_accel* accel, const void* d_rays, int64_t n, uint8_t* d_occluded, void* stream) {
+    return guarded([&] {
+        check_built(accel);
+        if (n < 0 || (n > 0 && (!d_rays || !d_occluded))) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "rays or output null");
+        launch_trace(accel, d_rays, n, nullptr, d_occluded, static_cast<cudaStream_t>(stream), accel->err.as<int>());
+    });
+}
+
+int lmgpu_accel_get_stats(const lmgpu_accel* accel, lmgpu_accel_stats* out) {
+    return guarded([&] {
+        if (!accel || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        std::memset(out, 0, sizeof(*out));
+        out->num_tris = accel->num_tris;
+        out->num_nodes = accel->num_nodes;
+        out->max_depth = accel->depth;
+        out->build_seconds = accel->build_seconds;
+        out->sah_cost = accel->sah_cost;
+        out->device_bytes = int64_t(accel->nodes.bytes + accel->tris.bytes);
+    });
+}
+
+int lmgpu_bvh8_build_host(const float* tri_p, int64_t num_tris, uint32_t* nodes, float* tris, int64_t* num_nodes,
+                          int32_t* max_depth) {
+    return guarded([&] {
+        if (!tri_p || !nodes || !tris || !num_nodes || !max_depth) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        Bvh8Host h;
+        std::string err;
+        if (!build_bvh8(tri_p, num_tris, h, &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+        if (h.nodes.size() > size_t(20) * size_t(num_tris > 0 ? num_tris : 1))
+            throw Error(LMGPU_ERR_INTERNAL, "node count above the documented bound");
+        std::memcpy(nodes, h.nodes.data(), h.nodes.size() * 4);
+        std::memcpy(tris, h.tris.data(), h.tris.size() * 4);
+        *num_nodes = int64_t(h.nodes.size() / 20);
+        *max_depth = h.max_depth;
+    });
+}
+
+int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, int32_t any_hit, int32_t sample,
+                             double* mean_nodes, double* mean_tris) {
+    return guarded([&] {
+        check_built(accel);
+        if (!d_rays || n <= 0 || sample <= 0 || !mean_nodes || !mean_tris)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid argument");
+        DevBuf sums;
+        sums.alloc(3 * sizeof(unsigned long long));
+        LMGPU_CUDA(cudaMemset(sums.p, 0, 3 * sizeof(unsigned long long)));
+        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
+        const Bvh8 b = device_view(accel);
+        const size_t smem = trace_smem(accel);
+        const int64_t m = (n + sample - 1) / sample;
+        if (any_hit) {
+            const int g = trace_grid(k_trace_count<true>, smem, m);
+            k_trace_count<true><<<g, kTraceBlock, smem>>>(b, static_cast<const float4*>(d_rays), n, sample,
+                                                          sums.as<unsigned long long>(), accel->err.as<int>());
+        } else {
+            const int g = trace_grid(k_trace_count<false>, smem, m);
+            k_trace_count<false><<<g, kTraceBlock, smem>>>(b, static_cast<const float4*>(d_rays), n, sample,
+                                                           sums.as<unsigned long long>(), accel->err.as<int>());
+        }
+        LMGPU_CUDA(cudaGetLastError());
+        unsigned long long h[3];
+        LMGPU_CUDA(cudaMemcpy(h, sums.p, sizeof(h), cudaMemcpyDeviceToHost));
+        const double c = h[2] ? double(h[2]) : 1.0;
+        *mean_nodes = double(h[0]) / c;
+        *mean_tris = double(h[1]) / c;
+    });
+}
+
+}  // extern "C"

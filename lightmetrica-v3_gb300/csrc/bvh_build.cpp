@@ -1,0 +1,399 @@
+// Host-side binned-SAH build and collapse to the 8-wide quantized layout (see bvh_build.h).
+// Compiled by the host compiler with OpenMP; the binary build recurses as OpenMP tasks.
+#include "bvh_build.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <omp.h>
+
+namespace lmgpu {
+
+namespace {
+
+constexpr int kMaxLeaf = 3;     // triangles per leaf child (3 bits of meta hold the count)
+constexpr int kBins = 32;
+constexpr int kTaskGrain = 8192;
+constexpr int kMedianDepth = 64;  // below this depth a degenerate split falls back to the median
+
+struct AABB {
+    float lo[3], hi[3];
+    void reset() {
+        for (int a = 0; a < 3; a++) { lo[a] = std::numeric_limits<float>::infinity(); hi[a] = -std::numeric_limits<float>::infinity(); }
+    }
+    void grow(const AABB& b) {
+        for (int a = 0; a < 3; a++) { lo[a] = std::min(lo[a], b.lo[a]); hi[a] = std::max(hi[a], b.hi[a]); }
+    }
+    void grow(const float* p) {
+        for (int a = 0; a < 3; a++) { lo[a] = std::min(lo[a], p[a]); hi[a] = std::max(hi[a], p[a]); }
+    }
+    double area() const {
+        if (!(hi[0] >= lo[0])) return 0.0;
+        const double dx = double(hi[0]) - lo[0], dy = double(hi[1]) - lo[1], dz = double(hi[2]) - lo[2];
+        return 2.0 * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct BinNode {
+    AABB box;
+    int32_t left = -1, right = -1;
+    int32_t start = 0, count = 0;
+};
+
+struct Builder {
+    const float* P = nullptr;
+    int64_t n = 0;
+    std::vector<AABB> tb;
+    std::vector<float> cen;  // 3 per triangle
+    std::vector<int32_t> idx;
+    std::vector<BinNode> nodes;
+    std::atomic<int32_t> next{1};
+
+    void split_median(int start, int count, int axis, int& mid) {
+        mid = start + count / 2;
+        std::nth_element(idx.begin() + start, idx.begin() + mid, idx.begin() + start + count,
+                         [&](int32_t a, int32_t b) { return cen[3 * a + axis] < cen[3 * b + axis]; });
+    }
+
+    void build(int32_t ni, int start, int count, int depth) {
+        BinNode& node = nodes[ni];
+        node.start = start;
+        node.count = count;
+        AABB box, cb;
+        box.reset(); cb.reset();
+        for (int i = start; i < start + count; i++) {
+            box.grow(tb[idx[i]]);
+            cb.grow(&cen[3 * idx[i]]);
+        }
+        node.box = box;
+        if (count == 1) return;
+
+        // Binned SAH over centroid bounds (C_trav = 1, C_tri = 1, costs relative to node area).
+        int best_axis = -1, best_split = -1;
+        double best_cost = std::numeric_limits<double>::infinity();
+        const double parea = box.area();
+        for (int a = 0; a < 3; a++) {
+            const float ext = cb.hi[a] - cb.lo[a];
+            if (!(ext > 0.f)) continue;
+            AABB bb[kBins];
+            int bc[kBins] = {0};
+            for (int b = 0; b < kBins; b++) bb[b].reset();
+            const float k = float(kBins) / ext;
+            for (int i = start; i < start + count; i++) {
+                const int t = idx[i];
+                int b = int((cen[3 * t + a] - cb.lo[a]) * k);
+                b = std::min(std::max(b, 0), kBins - 1);
+                bb[b].grow(tb[t]);
+                bc[b]++;
+            }
+            double ra[kBins];
+            int rc[kBins];
+            AABB acc; acc.reset();
+            int c = 0;
+            for (int b = kBins - 1; b > 0; b--) {
+                acc.grow(bb[b]); c += bc[b];
+                ra[b] = acc.area(); rc[b] = c;
+            }
+            acc.reset(); c = 0;
+            for (int b = 0; b < kBins - 1; b++) {
+                acc.grow(bb[b]); c += bc[b];
+                if (c == 0 || rc[b + 1] == 0) continue;
+                const double cost = acc.area() * c + ra[b + 1] * rc[b + 1];
+                if (cost < best_cost) { best_cost = cost; best_axis = a; best_split = b; }
+            }
+        }
+        const double split_cost = parea > 0 ? 1.0 + best_cost / parea : std::numeric_limits<double>::infinity();
+        if (count <= kMaxLeaf && (best_axis < 0 || double(count) <= split_cost)) return;  // leaf
+
+        int mid = -1;
+        if (best_axis >= 0 && depth < kMedianDepth) {
+            const float ext = cb.hi[best_axis] - cb.lo[best_axis];
+            const float k = float(kBins) / ext;
+            auto it = std::partition(idx.begin() + start, idx.begin() + start + count, [&](int32_t t) {
+                int b = int((cen[3 * t + best_axis] - cb.lo[best_axis]) * k);
+                b = std::min(std::max(b, 0), kBins - 1);
+                return b <= best_split;
+            });
+            mid = int(it - idx.begin());
+        }
+        if (mid <= start || mid >= start + count) {
+            int axis = 0;
+            for (int a = 1; a < 3; a++)
+                if (cb.hi[a] - cb.lo[a] > cb.hi[axis] - cb.lo[axis]) axis = a;
+            split_median(start, count, axis, mid);
+        }
+        const int32_t l = next.fetch_add(2);
+        node.left = l;
+        node.right = l + 1;
+        const int lc = mid - start, rcnt = start + count - mid;
+        if (count > kTaskGrain) {
+#pragma omp task default(shared) firstprivate(l, start, lc, depth)
+            build(l, start, lc, depth + 1);
+#pragma omp task default(shared) firstprivate(l, mid, rcnt, depth)
+            build(l + 1, mid, rcnt, depth + 1);
+        } else {
+            build(l, start, lc, depth + 1);
+            build(l + 1, mid, rcnt, depth + 1);
+        }
+    }
+
+    double sah(int32_t ni, double root_area) const {
+        const BinNode& b = nodes[ni];
+        const double rel = root_area > 0 ? b.box.area() / root_area : 0.0;
+        if (b.left < 0) return rel * b.count;
+        return rel + sah(b.left, root_area) + sah(b.right, root_area);
+    }
+};
+
+inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+inline float bitsf(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+
+// Quantizes child boxes into the node frame with outward rounding. Returns false if the chosen
+// exponents cannot cover the node (the caller then retries with larger exponents).
+bool quantize(const AABB& nb, const AABB* cbox, const bool* valid, int nslots, const int* eb_in, int* eb_out,
+              uint8_t qlo[3][8], uint8_t qhi[3][8]) {
+    for (int a = 0; a < 3; a++) {
+        const float px = nb.lo[a];
+        int eb = eb_in[a];
+        for (;;) {
+            const float scale = bitsf(uint32_t(eb) << 23);
+            if (std::fmaf(255.f, scale, px) >= nb.hi[a] || eb >= 254) break;
+            eb++;
+        }
+        eb_out[a] = eb;
+        const float scale = bitsf(uint32_t(eb) << 23);
+        for (int s = 0; s < nslots; s++) {
+            if (!valid[s]) { qlo[a][s] = 0; qhi[a][s] = 0; continue; }
+            double fl = std::floor((double(cbox[s].lo[a]) - px) / scale);
+            double fh = std::ceil((double(cbox[s].hi[a]) - px) / scale);
+            int ql = int(std::min(255.0, std::max(0.0, fl)));
+            int qh = int(std::min(255.0, std::max(0.0, fh)));
+            while (ql > 0 && std::fmaf(float(ql), scale, px) > cbox[s].lo[a]) ql--;
+            while (qh < 255 && std::fmaf(float(qh), scale, px) < cbox[s].hi[a]) qh++;
+            if (std::fmaf(float(ql), scale, px) > cbox[s].lo[a]) return false;
+            if (std::fmaf(float(qh), scale, px) < cbox[s].hi[a]) return false;
+            qlo[a][s] = uint8_t(ql);
+            qhi[a][s] = uint8_t(qh);
+        }
+    }
+    return true;
+}
+
+int initial_exponent(float extent) {
+    if (!(extent > 0.f)) return 1;
+    int e2;
+    std::frexp(double(extent) / 255.0, &e2);  // extent/255 = m * 2^e2, m in [0.5, 1)
+    int eb = e2 + 127;
+    return std::min(254, std::max(1, eb));
+}
+
+}  // namespace
+
+bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) {
+    out = Bvh8Host();
+    if (n <= 0) {
+        if (err) *err = "accel build: no triangles";
+        return false;
+    }
+    if (n > (int64_t(1) << 31) - 1) {
+        if (err) *err = "accel build: more than 2^31-1 triangles";
+        return false;
+    }
+    Builder B;
+    B.P = tri_p;
+    B.n = n;
+    B.tb.resize(n);
+    B.cen.resize(3 * n);
+    B.idx.resize(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; i++) {
+        AABB b; b.reset();
+        for (int k = 0; k < 3; k++) b.grow(tri_p + 9 * i + 3 * k);
+        for (int a = 0; a < 3; a++) {
+            if (!std::isfinite(b.lo[a]) || !std::isfinite(b.hi[a])) { b.lo[a] = 0; b.hi[a] = 0; }
+            B.cen[3 * i + a] = 0.5f * (b.lo[a] + b.hi[a]);
+        }
+        B.tb[i] = b;
+        B.idx[i] = int32_t(i);
+    }
+    for (int64_t i = 0; i < n; i++)
+        for (int k = 0; k < 9; k++)
+            if (!std::isfinite(tri_p[9 * i + k])) {
+                if (err) *err = "accel build: non-finite vertex coordinate";
+                return false;
+            }
+    B.nodes.resize(size_t(2) * n);
+#pragma omp parallel
+#pragma omp single
+    B.build(0, 0, int(n), 0);
+    const int32_t nb = B.next.load();
+    B.nodes.resize(nb);
+    out.sah_cost = B.sah(0, B.nodes[0].box.area());
+
+    // ---- collapse to 8-wide nodes, breadth first ------------------------------------------------
+    struct Pending { int32_t bin; int32_t wide; int32_t depth; };
+    std::vector<Pending> queue;
+    queue.push_back({0, 0, 1});
+    out.nodes.assign(20, 0);
+    out.tris.reserve(size_t(12) * n);
+    size_t qi = 0;
+    int32_t max_depth = 1;
+    while (qi < queue.size()) {
+        const Pending pd = queue[qi++];
+        max_depth = std::max(max_depth, pd.depth);
+        // children of this wide node, as binary node indices
+        int32_t ch[8];
+        int nch = 0;
+        const BinNode& root = B.nodes[pd.bin];
+        if (root.count <= kMaxLeaf || root.left < 0) {
+            ch[nch++] = pd.bin;
+        } else {
+            ch[nch++] = root.left;
+            ch[nch++] = root.right;
+            while (nch < 8) {
+                int pick = -1;
+                double pa = -1;
+                for (int i = 0; i < nch; i++) {
+                    const BinNode& c = B.nodes[ch[i]];
+                    if (c.left < 0 || c.count <= kMaxLeaf) continue;
+                    const double a = c.box.area();
+                    if (a > pa) { pa = a; pick = i; }
+                }
+                if (pick < 0) break;
+                const BinNode& c = B.nodes[ch[pick]];
+                ch[pick] = c.left;
+                ch[nch++] = c.right;
+            }
+        }
+        // octant-ordered slot assignment (greedy on dot(centroid - center, octant direction))
+        AABB nbox; nbox.reset();
+        for (int i = 0; i < nch; i++) nbox.grow(B.nodes[ch[i]].box);
+        float ctr[3];
+        for (int a = 0; a < 3; a++) ctr[a] = 0.5f * (nbox.lo[a] + nbox.hi[a]);
+        double cost[8][8];
+        for (int i = 0; i < nch; i++) {
+            const AABB& b = B.nodes[ch[i]].box;
+            for (int s = 0; s < 8; s++) {
+                double c = 0;
+                for (int a = 0; a < 3; a++) {
+                    const double d = 0.5 * (double(b.lo[a]) + b.hi[a]) - ctr[a];
+                    c += ((s >> a) & 1) ? -d : d;
+                }
+                cost[i][s] = c;
+            }
+        }
+        int slot_of[8];
+        int child_in[8];
+        for (int s = 0; s < 8; s++) child_in[s] = -1;
+        bool used[8] = {false};
+        for (int k = 0; k < nch; k++) {
+            int bi = -1, bs = -1;
+            double bc = std::numeric_limits<double>::infinity();
+            for (int i = 0; i < nch; i++) {
+                if (used[i]) continue;
+                for (int s = 0; s < 8; s++) {
+                    if (child_in[s] >= 0) continue;
+                    if (cost[i][s] < bc) { bc = cost[i][s]; bi = i; bs = s; }
+                }
+            }
+            used[bi] = true;
+            child_in[bs] = bi;
+            slot_of[bi] = bs;
+        }
+        (void)slot_of;
+        // allocate internal children (slot order) and leaf triangles (slot order)
+        uint8_t imask = 0, meta[8] = {0};
+        AABB cbox[8];
+        bool valid[8] = {false};
+        const uint32_t child_base = uint32_t(out.nodes.size() / 20);
+        const uint32_t tri_base = uint32_t(out.tris.size() / 12);
+        for (int s = 0; s < 8; s++) {
+            const int i = child_in[s];
+            if (i < 0) continue;
+            const BinNode& c = B.nodes[ch[i]];
+            valid[s] = true;
+            cbox[s] = c.box;
+            if (c.left >= 0 && c.count > kMaxLeaf) {
+                imask |= uint8_t(1u << s);
+                meta[s] = 0x80;  // any nonzero value marks the slot as used
+                const int32_t wi = int32_t(out.nodes.size() / 20);
+                out.nodes.resize(out.nodes.size() + 20, 0);
+                queue.push_back({ch[i], wi, pd.depth + 1});
+            }
+        }
+        for (int s = 0; s < 8; s++) {
+            const int i = child_in[s];
+            if (i < 0 || (imask >> s) & 1) continue;
+            const BinNode& c = B.nodes[ch[i]];
+            const uint32_t off = uint32_t(out.tris.size() / 12) - tri_base;
+            if (c.count < 1 || c.count > kMaxLeaf || off > 31) {
+                if (err) *err = "accel build: internal error (leaf layout)";
+                return false;
+            }
+            meta[s] = uint8_t((c.count << 5) | off);
+            for (int k = c.start; k < c.start + c.count; k++) {
+                const int32_t t = B.idx[k];
+                const float* p = tri_p + 9 * int64_t(t);
+                const float p1[3] = {p[0], p[1], p[2]};
+                const float e1[3] = {p[3] - p[0], p[4] - p[1], p[5] - p[2]};
+                const float e2[3] = {p[6] - p[0], p[7] - p[1], p[8] - p[2]};
+                const float rec[12] = {p1[0], p1[1], p1[2], e1[0], e1[1], e1[2], e2[0], e2[1], e2[2], bitsf(uint32_t(t)), 0.f, 0.f};
+                out.tris.insert(out.tris.end(), rec, rec + 12);
+            }
+        }
+        // quantize
+        int eb0[3], eb[3];
+        for (int a = 0; a < 3; a++) eb0[a] = initial_exponent(nbox.hi[a] - nbox.lo[a]);
+        uint8_t qlo[3][8], qhi[3][8];
+        bool ok = false;
+        for (int attempt = 0; attempt < 8 && !ok; attempt++) {
+            ok = quantize(nbox, cbox, valid, 8, eb0, eb, qlo, qhi);
+            if (!ok) for (int a = 0; a < 3; a++) eb0[a] = std::min(254, eb[a] + 1);
+        }
+        if (!ok) {
+            if (err) *err = "accel build: box quantization failed";
+            return false;
+        }
+        uint32_t* w = &out.nodes[size_t(pd.wide) * 20];
+        w[0] = fbits(nbox.lo[0]); w[1] = fbits(nbox.lo[1]); w[2] = fbits(nbox.lo[2]);
+        w[3] = uint32_t(eb[0]) | (uint32_t(eb[1]) << 8) | (uint32_t(eb[2]) << 16) | (uint32_t(imask) << 24);
+        w[4] = child_base;
+        w[5] = tri_base;
+        auto pack4 = [](const uint8_t* b) {
+            return uint32_t(b[0]) | (uint32_t(b[1]) << 8) | (uint32_t(b[2]) << 16) | (uint32_t(b[3]) << 24);
+        };
+        w[6] = pack4(meta); w[7] = pack4(meta + 4);
+        w[8] = pack4(qlo[0]); w[9] = pack4(qlo[0] + 4); w[10] = pack4(qlo[1]); w[11] = pack4(qlo[1] + 4);
+        w[12] = pack4(qlo[2]); w[13] = pack4(qlo[2] + 4); w[14] = pack4(qhi[0]); w[15] = pack4(qhi[0] + 4);
+        w[16] = pack4(qhi[1]); w[17] = pack4(qhi[1] + 4); w[18] = pack4(qhi[2]); w[19] = pack4(qhi[2] + 4);
+    }
+    out.max_depth = max_depth;
+    if (int64_t(out.tris.size() / 12) != n) {
+        if (err) *err = "accel build: internal error (triangle count)";
+        return false;
+    }
+    return true;
+}
+
+Bvh8NodeView decode_node(const uint32_t* w) {
+    Bvh8NodeView v;
+    for (int a = 0; a < 3; a++) {
+        v.origin[a] = bitsf(w[a]);
+        v.scale[a] = bitsf(((w[3] >> (8 * a)) & 0xffu) << 23);
+    }
+    v.imask = uint8_t(w[3] >> 24);
+    v.child_base = w[4];
+    v.tri_base = w[5];
+    for (int s = 0; s < 8; s++) {
+        v.meta[s] = uint8_t(w[6 + s / 4] >> (8 * (s % 4)));
+        for (int a = 0; a < 3; a++) {
+            v.qlo[a][s] = uint8_t(w[8 + 2 * a + s / 4] >> (8 * (s % 4)));
+            v.qhi[a][s] = uint8_t(w[14 + 2 * a + s / 4] >> (8 * (s % 4)));
+        }
+    }
+    return v;
+}
+
+}  // namespace lmgpu

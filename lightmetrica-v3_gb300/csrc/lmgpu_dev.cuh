@@ -1,0 +1,216 @@
+// Device building blocks shared by the trace and render kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lmgpu {
+
+constexpr float kInf = 1e10f;  // include/lm/math.h:54
+constexpr float kEps = 1e-3f;  // include/lm/math.h:55
+constexpr float kPi = 3.14159265358979323846f;
+
+// ---------------------------------------------------------------------------------------------
+// fp32 vector math. The `ieee` namespace spells out every multiply and add with the _rn
+// intrinsics, which the compiler never contracts into FMA, in glm's operation order; it is used
+// wherever results must match the host restatement bit for bit (ray generation, triangle test).
+struct f3 { float x, y, z; };
+__host__ __device__ inline f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ inline f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ inline f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ inline f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ inline f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ inline f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ inline f3 operator*(float s, f3 a) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ inline f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ inline f3 cross(f3 a, f3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+__device__ inline f3 normalize(f3 v) { return v * (1.0f / sqrtf(dot(v, v))); }
+__device__ inline float length(f3 v) { return sqrtf(dot(v, v)); }
+__device__ inline float cmax(f3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }
+__device__ inline bool is_zero(f3 v) { return v.x == 0.f && v.y == 0.f && v.z == 0.f; }
+
+namespace ieee {
+__device__ inline float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ inline float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ inline float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ inline float div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ inline f3 sub3(f3 a, f3 b) { return {sub(a.x, b.x), sub(a.y, b.y), sub(a.z, b.z)}; }
+__device__ inline f3 add3(f3 a, f3 b) { return {add(a.x, b.x), add(a.y, b.y), add(a.z, b.z)}; }
+__device__ inline f3 scale3(f3 a, float s) { return {mul(a.x, s), mul(a.y, s), mul(a.z, s)}; }
+// glm compute_dot: (x*x' + y*y') + z*z'
+__device__ inline float dot3(f3 a, f3 b) { return add(add(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z)); }
+// glm cross: (x.y*y.z - y.y*x.z, x.z*y.x - y.z*x.x, x.x*y.y - y.x*x.y)
+__device__ inline f3 cross3(f3 x, f3 y) {
+    return {sub(mul(x.y, y.z), mul(y.y, x.z)), sub(mul(x.z, y.x), mul(y.z, x.x)), sub(mul(x.x, y.y), mul(y.x, x.y))};
+}
+// glm normalize: v * inversesqrt(dot(v, v)), inversesqrt(x) = 1 / sqrt(x)
+__device__ inline f3 normalize3(f3 v) { return scale3(v, div(1.0f, __fsqrt_rn(dot3(v, v)))); }
+}  // namespace ieee
+
+// ---------------------------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC 2011), keyed per path:
+//   key = (seed, 0x6c6d6770), counter = (4*vertex + slot/4, path_lo, path_hi, 0)
+// Slots of one vertex: 0-7 light sample, 8-11 direction, 12 Russian roulette, 13-14 component.
+struct U4 { float v[4]; };
+__device__ inline U4 philox_block(uint32_t seed, uint64_t path, uint32_t block) {
+    uint32_t c0 = block, c1 = uint32_t(path), c2 = uint32_t(path >> 32), c3 = 0u;
+    uint32_t k0 = seed, k1 = 0x6c6d6770u;
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    const float s = 1.0f / 16777216.0f;
+    return U4{{float(c0 >> 8) * s, float(c1 >> 8) * s, float(c2 >> 8) * s, float(c3 >> 8) * s}};
+}
+
+// ---------------------------------------------------------------------------------------------
+// 8-wide BVH (layout in bvh_build.h).
+struct Bvh8 {
+    const uint4* nodes;   // 5 words per node
+    const float4* tris;   // 3 words per triangle
+    int32_t depth;        // levels; bounds the traversal stack
+    uint32_t num_nodes;   // a ray visits each node at most once; more visits flag corruption
+};
+
+struct TraceHit {
+    float t, u, v;
+    int32_t id;
+};
+
+// Moller-Trumbore exactly as accel_sahbvh.cpp:58-75 in fp32 (IEEE ops, no FMA). Returns true and
+// fills t/u/v if accepted in [tl, th].
+__device__ inline bool tri_test(f3 o, f3 d, f3 p1, f3 e1, f3 e2, float tl, float th, float& t, float& u, float& v) {
+    using ieee::add; using ieee::mul; using ieee::div;
+    const f3 p = ieee::cross3(d, e2);
+    const f3 tv = ieee::sub3(o, p1);
+    const f3 q = ieee::cross3(tv, e1);
+    const float det = ieee::dot3(e1, p);
+    const float ad = fabsf(det);
+    const float s = copysignf(1.0f, det);
+    const float uu = mul(ieee::dot3(tv, p), s);
+    const float vv = mul(ieee::dot3(d, q), s);
+    if (ad < 1e-8f || uu < 0.0f || vv < 0.0f || add(uu, vv) > ad) return false;
+    const float tt = div(ieee::dot3(e2, q), det);
+    if (tt < tl || th < tt) return false;
+    t = tt;
+    u = div(uu, ad);
+    v = div(vv, ad);
+    return true;
+}
+
+__device__ inline uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
+
+// Permutes the 8 slot bits of `m` so that bit (s ^ oct) holds slot s.
+__device__ inline uint32_t oct_permute(uint32_t m, uint32_t oct) {
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    return m;
+}
+
+// Ray traversal of the 8-wide BVH. Closest hit: the smallest t over every triangle whose test
+// accepts the ray in [tmin, tmax], ties broken toward the smaller flattened index. Any hit
+// (`any_hit`): returns at the first accepted triangle. The per-thread stack of sibling groups
+// lives in shared memory: stk[i * stride] for i < bvh.depth. Child boxes are tested with the
+// plane positions the builder verified to enclose the exact boxes, and the far distance is
+// widened by (1 + 2^-21) (Ize 2013), so no triangle the exact test would accept is culled.
+// Returns the number of visited nodes in *nodes_visited when non-null (instrumented builds).
+template <bool kAnyHit, bool kCount>
+__device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, float tmax, uint32_t* stk_base,
+                                      uint32_t* stk_bits, int stride, uint32_t* nodes_visited, uint32_t* tris_tested,
+                                      int* err) {
+    TraceHit best{tmax, 0.f, 0.f, -1};
+    const f3 inv = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    const uint32_t oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
+    int sp = 0;
+    uint32_t node = 0;
+    uint32_t nvis = 0, ntri = 0;
+    while (true) {
+        // ---- visit `node` ---------------------------------------------------------------------
+        if (node >= bvh.num_nodes || nvis >= bvh.num_nodes) { *err = 2; break; }
+        const uint4* np = bvh.nodes + size_t(node) * 5;
+        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+        nvis++;
+        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+        const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+        const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+        const uint32_t imask = w0.w >> 24;
+        // near/far plane bytes per axis, chosen by the ray's octant
+        const uint32_t lx0 = w2.x, lx1 = w2.y, ly0 = w2.z, ly1 = w2.w, lz0 = w3.x, lz1 = w3.y;
+        const uint32_t hx0 = w3.z, hx1 = w3.w, hy0 = w4.x, hy1 = w4.y, hz0 = w4.z, hz1 = w4.w;
+        const uint32_t nx0 = (oct & 1u) ? hx0 : lx0, nx1 = (oct & 1u) ? hx1 : lx1;
+        const uint32_t fx0 = (oct & 1u) ? lx0 : hx0, fx1 = (oct & 1u) ? lx1 : hx1;
+        const uint32_t ny0 = (oct & 2u) ? hy0 : ly0, ny1 = (oct & 2u) ? hy1 : ly1;
+        const uint32_t fy0 = (oct & 2u) ? ly0 : hy0, fy1 = (oct & 2u) ? ly1 : hy1;
+        const uint32_t nz0 = (oct & 4u) ? hz0 : lz0, nz1 = (oct & 4u) ? hz1 : lz1;
+        const uint32_t fz0 = (oct & 4u) ? lz0 : hz0, fz1 = (oct & 4u) ? lz1 : hz1;
+        uint32_t hitmask = 0;
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int k = s & 3;
+            const uint32_t mw = s < 4 ? w1.z : w1.w;
+            if (byte_of(mw, k) == 0u) continue;  // empty slot
+            const float qnx = float(byte_of(s < 4 ? nx0 : nx1, k)), qfx = float(byte_of(s < 4 ? fx0 : fx1, k));
+            const float qny = float(byte_of(s < 4 ? ny0 : ny1, k)), qfy = float(byte_of(s < 4 ? fy0 : fy1, k));
+            const float qnz = float(byte_of(s < 4 ? nz0 : nz1, k)), qfz = float(byte_of(s < 4 ? fz0 : fz1, k));
+            const float tnx = (fmaf(qnx, sx, px) - o.x) * inv.x, tfx = (fmaf(qfx, sx, px) - o.x) * inv.x;
+            const float tny = (fmaf(qny, sy, py) - o.y) * inv.y, tfy = (fmaf(qfy, sy, py) - o.y) * inv.y;
+            const float tnz = (fmaf(qnz, sz, pz) - o.z) * inv.z, tfz = (fmaf(qfz, sz, pz) - o.z) * inv.z;
+            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best.t)) * 1.00000048f;
+            if (tn <= tf) hitmask |= 1u << s;
+        }
+        // ---- leaf children: test their triangles now -------------------------------------------
+        uint32_t leaves = hitmask & ~imask;
+        while (leaves) {
+            const int s = __ffs(leaves) - 1;
+            leaves &= leaves - 1;
+            const uint32_t meta = byte_of(s < 4 ? w1.z : w1.w, s & 3);
+            const uint32_t cnt = meta >> 5, off = meta & 31u;
+            for (uint32_t j = 0; j < cnt; j++) {
+                const float4* tp = bvh.tris + size_t(w1.y + off + j) * 3;
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                if (kCount) ntri++;
+                float t, u, v;
+                if (tri_test(o, d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), tmin, best.t, t, u, v)) {
+                    const int32_t id = int32_t(__float_as_uint(c.y));
+                    if (kAnyHit) {
+                        if (kCount) { *nodes_visited += nvis; *tris_tested += ntri; }
+                        return TraceHit{t, u, v, id};
+                    }
+                    if (t < best.t || best.id < 0 || id < best.id) best = TraceHit{t, u, v, id};
+                }
+            }
+        }
+        // ---- next node: nearest-first by octant order ------------------------------------------
+        uint32_t inner = oct_permute(hitmask & imask, oct);
+        uint32_t g_base = w1.x, g_imask = imask;
+        if (inner == 0u) {
+            if (sp == 0) break;
+            sp--;
+            g_base = stk_base[sp * stride];
+            const uint32_t bits = stk_bits[sp * stride];
+            g_imask = bits >> 8;
+            inner = bits & 0xffu;
+        }
+        const int k = __ffs(inner) - 1;
+        inner &= inner - 1;
+        const uint32_t slot = uint32_t(k) ^ oct;
+        node = g_base + __popc(g_imask & ((1u << slot) - 1u));
+        if (inner != 0u) {
+            if (sp >= bvh.depth) { *err = 1; break; }
+            stk_base[sp * stride] = g_base;
+            stk_bits[sp * stride] = (g_imask << 8) | inner;
+            sp++;
+        }
+    }
+    if (kCount) { *nodes_visited += nvis; *tris_tested += ntri; }
+    return best;
+}
+
+}  // namespace lmgpu

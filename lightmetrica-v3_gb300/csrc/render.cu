@@ -1,0 +1,1160 @@
+// Scene, film and renderer C-ABI (include/lmgpu.h): renderer::raycast as one kernel, renderer::pt
+// as a wavefront of generate -> [extend -> shade -> shadow] x (max_verts - 1) kernels over
+// structure-of-arrays queues whose lengths stay on the device.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "lmgpu_dev.cuh"
+#include "runtime.h"
+
+namespace cg = cooperative_groups;
+
+namespace lmgpu {
+
+Bvh8 device_view(const lmgpu_accel* a);
+size_t trace_smem(const lmgpu_accel* a);
+
+// ---------------------------------------------------------------------------------------------
+// Device scene
+struct DevMaterial {
+    int32_t type;
+    float c[3];
+    float ax, ay, ni;
+    int32_t pad;
+};
+struct DevLight {
+    int32_t type;
+    float ke[3];
+    int32_t tri_off, tri_cnt, cdf_off;
+    float invA_J;  // (1 / mesh-local area) / |det M|, light_area.cpp:41-46
+    int32_t env_w, env_h, tex_off, marg_off, cond_off;
+    float rot, scale;
+};
+struct DevScene {
+    Bvh8 bvh;
+    const float4* shade;   // 6 words per triangle: p1 p2 p3 n1 n2 n3 gn prim
+    const int2* prim_ml;   // (material, light) per primitive
+    const DevMaterial* mats;
+    const DevLight* lights;
+    int32_t num_lights;
+    int32_t env_light;     // index into lights or -1
+    const float4* ltri;    // 3 words per light triangle: (a, b.x) (b.yz, c.xy) (c.z, gn)
+    const float* cdf;      // area-light CDFs (tri_cnt + 1 entries each)
+    const float* env;      // env texels, marginal and conditional CDFs
+    f3 cam_p, cam_u, cam_v, cam_w;
+    float tf, aspect;
+    int32_t has_camera;
+};
+
+}  // namespace lmgpu
+
+struct lmgpu_scene {
+    lmgpu_accel* accel = nullptr;
+    lmgpu::DevScene dev{};
+    lmgpu::DevBuf shade, prim_ml, mats, lights, ltri, cdf, env;
+    // wavefront queues, grown on demand
+    lmgpu::DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
+    int64_t q_cap = 0;
+};
+
+struct lmgpu_film {
+    int32_t w = 0, h = 0;
+    lmgpu::DevBuf sum, out;
+    double scale = 1.0;
+    int64_t accumulated_spp = 0;
+};
+
+namespace lmgpu {
+
+// ---------------------------------------------------------------------------------------------
+// Geometry (include/lm/surface.h)
+struct Geom {
+    f3 p, n, gn, wo;
+    f3 u, v;
+    bool degenerated, infinite;
+};
+
+// math::orthonormal_basis (Duff et al. 2017), include/lm/math.h:540-547
+__device__ inline void onb(f3 n, f3& u, f3& v) {
+    const float s = copysignf(1.f, n.z);
+    const float a = -1.f / (s + n.z);
+    const float b = n.x * n.y * a;
+    u = mk(1.f + s * n.x * n.x * a, s * b, -s * n.x);
+    v = mk(b, s + n.y * n.y * a, -n.y);
+}
+__device__ inline Geom on_surface(f3 p, f3 n, f3 gn) {
+    Geom g;
+    g.p = p; g.n = n; g.gn = gn; g.wo = mk(0, 0, 0);
+    g.degenerated = false; g.infinite = false;
+    onb(n, g.u, g.v);
+    return g;
+}
+__device__ inline Geom infinite_point(f3 wo) {
+    Geom g;
+    g.p = mk(0, 0, 0); g.n = mk(0, 0, 0); g.gn = g.n; g.u = g.n; g.v = g.n;
+    g.wo = wo; g.degenerated = false; g.infinite = true;
+    return g;
+}
+__device__ inline bool opposite(const Geom& g, f3 a, f3 b) { return dot(a, g.n) * dot(b, g.n) <= 0.f; }
+
+// surface.h:329-348 for a finite or degenerate s1 and any s2
+__device__ inline float geometry_term(const Geom& s1, const Geom& s2) {
+    f3 d;
+    float L2;
+    if (s2.infinite) {
+        d = -s2.wo;
+        L2 = 1.f;
+    } else {
+        d = s2.p - s1.p;
+        L2 = dot(d, d);
+        d = d / sqrtf(L2);
+    }
+    const float c1 = s1.degenerated ? 1.f : fabsf(dot(s1.n, d));
+    const float c2 = (s2.degenerated || s2.infinite) ? 1.f : fabsf(dot(s2.n, -d));
+    return c1 * c2 / L2;
+}
+// surface.h:377-390
+__device__ inline float pdf_sa_to_projsa(float pdf, const Geom& g, f3 d) {
+    if (g.degenerated) return pdf;
+    const float J = fabsf(dot(g.n, d));
+    return J == 0.f ? 0.f : pdf / J;
+}
+// surface.h:424-438, transport direction EL
+__device__ inline float sn_correction(const Geom& g, f3 wi, f3 wo) {
+    const float wi_ng = dot(wi, g.gn), wo_ng = dot(wo, g.gn);
+    const float wi_ns = dot(wi, g.n), wo_ns = dot(wo, g.n);
+    return (wi_ng * wi_ns <= 0.f || wo_ng * wo_ns <= 0.f) ? 0.f : 1.f;
+}
+
+__device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float v, int32_t& prim) {
+    const float4* sp = S.shade + size_t(id) * 6;
+    const float4 s0 = __ldg(sp), s1 = __ldg(sp + 1), s2 = __ldg(sp + 2), s3 = __ldg(sp + 3), s4 = __ldg(sp + 4),
+                 s5 = __ldg(sp + 5);
+    const f3 p1 = mk(s0.x, s0.y, s0.z), p2 = mk(s0.w, s1.x, s1.y), p3 = mk(s1.z, s1.w, s2.x);
+    const f3 n1 = mk(s2.y, s2.z, s2.w), n2 = mk(s3.x, s3.y, s3.z), n3 = mk(s3.w, s4.x, s4.y);
+    const f3 gn = mk(s4.z, s4.w, s5.x);
+    prim = int32_t(__float_as_uint(s5.y));
+    const float b0 = 1.f - u - v;  // mix_barycentric, math.h:572-575
+    const f3 p = p1 * b0 + p2 * u + p3 * v;
+    const f3 n = normalize(n1 * b0 + n2 * u + n3 * v);
+    return on_surface(p, n, gn);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Camera (camera_pinhole.cpp)
+__device__ inline f3 primary_dir(const DevScene& S, float rx, float ry) {
+    using ieee::mul; using ieee::sub;
+    const float x = sub(mul(2.f, rx), 1.f), y = sub(mul(2.f, ry), 1.f);
+    const f3 d = ieee::normalize3(mk(mul(mul(S.aspect, S.tf), x), mul(S.tf, y), -1.f));
+    return ieee::add3(ieee::add3(ieee::scale3(S.cam_u, d.x), ieee::scale3(S.cam_v, d.y)), ieee::scale3(S.cam_w, d.z));
+}
+__device__ inline bool raster_pos(const DevScene& S, f3 wo, float& rx, float& ry) {
+    const float ex = dot(S.cam_u, wo), ey = dot(S.cam_v, wo), ez = dot(S.cam_w, wo);
+    if (ez >= 0.f) return false;
+    rx = (-ex / ez / S.tf / S.aspect) * .5f + .5f;
+    ry = (-ey / ez / S.tf) * .5f + .5f;
+    return !(rx < 0.f || rx > 1.f || ry < 0.f || ry > 1.f);
+}
+__device__ inline float cam_J(const DevScene& S, f3 wo) {
+    const float c = -dot(S.cam_w, wo);
+    const float ic = 1.f / c;
+    return ic * ic * ic / (S.tf * S.tf * S.aspect * 4.f);
+}
+__device__ inline float cam_pdf(const DevScene& S, f3 wo) {
+    float rx, ry;
+    return raster_pos(S, wo, rx, ry) ? cam_J(S, wo) : 0.f;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Materials (material_{diffuse,glossy,glass,mirror}.cpp)
+__device__ inline void basis2(const Geom& g, f3 wi, f3& n, f3& u, f3& v) {
+    const bool i = dot(wi, g.n) > 0.f;
+    n = i ? g.n : -g.n;
+    u = g.u;
+    v = i ? g.v : -g.v;
+}
+__device__ inline float ggx_d(const DevMaterial& m, f3 wh, f3 u, f3 v, f3 n) {
+    const float a = dot(wh, u) / m.ax, b = dot(wh, v) / m.ay, c = dot(wh, n);
+    const float s = a * a + b * b + c * c;
+    return 1.f / (kPi * m.ax * m.ay * s * s);
+}
+__device__ inline float ggx_g1(const DevMaterial& m, f3 w, f3 u, f3 v, f3 n) {
+    const float c = dot(w, n);
+    const float s = fmaxf(kEps, sqrtf(fmaxf(0.f, 1.f - c * c)));
+    const float cp = dot(w, u) / s, cs = dot(w, v) / s;
+    const float a2 = (cp * m.ax) * (cp * m.ax) + (cs * m.ay) * (cs * m.ay);
+    const float sc = s / c;
+    return c == 0.f ? 0.f : 2.f / (1.f + sqrtf(fmaxf(0.f, 1.f + a2 * sc * sc)));
+}
+__device__ inline void glass_fresnel(const DevMaterial& m, const Geom& g, f3 wi, f3& wt, bool& total, float& eta, float& Fr) {
+    const bool in = dot(wi, g.n) > 0.f;
+    const f3 n = in ? g.n : -g.n;
+    eta = in ? 1.f / m.ni : m.ni;
+    const float t = dot(wi, n);
+    const float t2 = 1.f - eta * eta * (1.f - t * t);
+    total = t2 <= 0.f;
+    if (total) {
+        wt = mk(0, 0, 0);
+        Fr = 1.f;
+        return;
+    }
+    wt = eta * (n * t - wi) - n * sqrtf(fmaxf(0.f, t2));
+    const float cs = in ? dot(wi, g.n) : dot(wt, g.n);
+    const float r = (1.f - m.ni) / (1.f + m.ni);
+    const float r2 = r * r;
+    Fr = r2 + (1.f - r2) * powf(1.f - cs, 5.f);
+}
+__device__ inline bool mat_specular(const DevMaterial& m) { return m.type == LMGPU_MAT_GLASS || m.type == LMGPU_MAT_MIRROR; }
+
+__device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, int comp, bool eval_delta) {
+    switch (m.type) {
+    case LMGPU_MAT_DIFFUSE:
+        if (opposite(g, wi, wo)) return mk(0, 0, 0);
+        return mk(m.c[0], m.c[1], m.c[2]) / kPi;
+    case LMGPU_MAT_GLOSSY: {
+        if (opposite(g, wi, wo)) return mk(0, 0, 0);
+        const f3 wh = normalize(wi + wo);
+        f3 n, u, v;
+        basis2(g, wi, n, u, v);
+        const f3 ks = mk(m.c[0], m.c[1], m.c[2]);
+        const float f5 = powf(1.f - dot(wo, wh), 5.f);
+        const f3 Fr = ks + (mk(1, 1, 1) - ks) * f5;
+        const float k = ggx_d(m, wh, u, v, n) * (ggx_g1(m, wi, u, v, n) * ggx_g1(m, wo, u, v, n)) / (4.f * dot(wi, n) * dot(wo, n));
+        return ks * Fr * k;
+    }
+    case LMGPU_MAT_GLASS: {
+        if (eval_delta) return mk(0, 0, 0);
+        f3 wt; bool total; float eta, Fr;
+        glass_fresnel(m, g, wi, wt, total, eta, Fr);
+        if (comp == 0) return mk(Fr, Fr, Fr);
+        const float r = (1.f - Fr) * eta * eta;
+        return mk(r, r, r);
+    }
+    default:
+        return eval_delta ? mk(0, 0, 0) : mk(1, 1, 1);
+    }
+}
+__device__ inline float mat_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, bool eval_delta) {
+    switch (m.type) {
+    case LMGPU_MAT_DIFFUSE:
+        return opposite(g, wi, wo) ? 0.f : 1.f / kPi;
+    case LMGPU_MAT_GLOSSY: {
+        if (opposite(g, wi, wo)) return 0.f;
+        const f3 wh = normalize(wi + wo);
+        f3 n, u, v;
+        basis2(g, wi, n, u, v);
+        return ggx_d(m, wh, u, v, n) * dot(wh, n) / (4.f * dot(wo, wh) * dot(wo, n));
+    }
+    default:
+        return eval_delta ? 0.f : 1.f;
+    }
+}
+// Returns false when no direction is produced (glossy below the surface).
+__device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, int comp, float u0, float u1, f3& wo, f3& w) {
+    switch (m.type) {
+    case LMGPU_MAT_DIFFUSE: {
+        f3 n, u, v;
+        basis2(g, wi, n, u, v);
+        const float r = sqrtf(fmaxf(0.f, u0)), t = 2.f * kPi * u1;
+        float st, ct;
+        sincosf(t, &st, &ct);
+        const float x = r * ct, y = r * st;
+        const float z = sqrtf(fmaxf(0.f, 1.f - x * x - y * y));
+        wo = u * x + v * y + n * z;
+        w = mk(m.c[0], m.c[1], m.c[2]);
+        return true;
+    }
+    case LMGPU_MAT_GLOSSY: {
+        f3 n, u, v;
+        basis2(g, wi, n, u, v);
+        const float a1 = u0 * 2.f * kPi;
+        float s1, c1;
+        sincosf(a1, &s1, &c1);
+        const f3 wh = normalize(sqrtf(fmaxf(0.f, u1 / (1.f - u1))) * (m.ax * c1 * u + m.ay * s1 * v) + n);
+        wo = 2.f * dot(wi, wh) * wh - wi;
+        if (opposite(g, wi, wo)) return false;
+        const f3 f = mat_eval(m, g, wi, wo, 0, false);
+        const float p = mat_pdf(m, g, wi, wo, false);
+        w = f / p;
+        return true;
+    }
+    case LMGPU_MAT_GLASS: {
+        if (comp == 0) {
+            wo = 2.f * dot(wi, g.n) * g.n - wi;
+        } else {
+            f3 wt; bool total; float eta, Fr;
+            glass_fresnel(m, g, wi, wt, total, eta, Fr);
+            wo = wt;
+        }
+        w = mat_eval(m, g, wi, wo, comp, false);  // pdf of a component direction is 1
+        return true;
+    }
+    default:
+        wo = 2.f * dot(wi, g.n) * g.n - wi;
+        w = mk(1, 1, 1);
+        return true;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Lights (light_area.cpp, light_envconst.cpp, light_env.cpp)
+__device__ inline int cdf_sample(const float* c, int n, float u) {
+    // upper_bound over c[0..n], then clamp(index - 1, 0, n - 1)  (math.h:367-370)
+    int lo = 0, hi = n + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (u < __ldg(c + mid)) hi = mid; else lo = mid + 1;
+    }
+    return min(max(lo - 1, 0), n - 1);
+}
+__device__ inline float cdf_pmf(const float* c, int n, int i) {
+    return (i < 0 || i + 1 >= n + 1) ? 0.f : __ldg(c + i + 1) - __ldg(c + i);
+}
+__device__ inline void env_uv(const DevLight& L, f3 d, float& u, float& v) {
+    float at = atan2f(d.x, d.z);
+    at = at < 0.f ? at + 2.f * kPi : at;
+    const float t = (at - L.rot) * .5f / kPi;
+    u = t - floorf(t);
+    v = acosf(fminf(1.f, fmaxf(-1.f, d.y))) / kPi;
+}
+__device__ inline f3 env_eval(const DevScene& S, const DevLight& L, f3 gwo) {
+    if (L.type == LMGPU_LIGHT_ENVCONST) return mk(L.ke[0], L.ke[1], L.ke[2]);
+    const f3 d = -gwo;
+    float u, v;
+    env_uv(L, d, u, v);
+    const int x = min(max(int(u * L.env_w), 0), L.env_w - 1);
+    const int y = min(max(int(v * L.env_h), 0), L.env_h - 1);
+    const float* t = S.env + L.tex_off + 3 * (size_t(y) * L.env_w + x);
+    return mk(__ldg(t), __ldg(t + 1), __ldg(t + 2)) * L.scale;
+}
+// pdf_direct of an infinite light endpoint with direction gwo, seen from g (projected solid angle)
+__device__ inline float env_pdf_direct(const DevScene& S, const DevLight& L, const Geom& g, f3 gwo) {
+    const f3 d = -gwo;
+    if (L.type == LMGPU_LIGHT_ENVCONST) return pdf_sa_to_projsa(1.f / (4.f * kPi), g, d);
+    float u, v;
+    env_uv(L, d, u, v);
+    const float st = sqrtf(fmaxf(0.f, 1.f - d.y * d.y));
+    if (st == 0.f) return 0.f;
+    const float* marg = S.env + L.marg_off;
+    const int y = min(int(v * L.env_h), L.env_h - 1);
+    const float pdf2 = cdf_pmf(marg, L.env_h, y) * cdf_pmf(S.env + L.cond_off + size_t(y) * (L.env_w + 1), L.env_w, int(u * L.env_w)) *
+                       float(L.env_w) * float(L.env_h);
+    return pdf_sa_to_projsa(pdf2 / (2.f * kPi * kPi * st), g, d);
+}
+__device__ inline float area_pdf_direct(const DevLight& L, const Geom& g, const Geom& gL, f3 wo) {
+    if (dot(wo, gL.n) <= 0.f) return 0.f;
+    const float G = geometry_term(g, gL);
+    return G == 0.f ? 0.f : L.invA_J / G;
+}
+
+struct LightSample {
+    Geom gL;
+    f3 wo;      // direction from the light toward the shading point
+    f3 weight;  // Le / (p_sel * pdf)
+    int light;
+};
+
+// path::sample_direct(LE), path.h:493-530, with u = {up(0,1), upc(2,3), ud(4,5), udc(6,7)}
+__device__ inline bool sample_direct(const DevScene& S, const Geom& g, const float* u, LightSample& out) {
+    const int n = S.num_lights;
+    const int li = min(max(int(u[2] * float(n)), 0), n - 1);
+    const float p_sel = 1.f / float(n);
+    const DevLight L = S.lights[li];
+    out.light = li;
+    if (L.type == LMGPU_LIGHT_AREA) {
+        const int ti = cdf_sample(S.cdf + L.cdf_off, L.tri_cnt, u[3]);
+        const float4* tp = S.ltri + size_t(L.tri_off + ti) * 3;
+        const float4 a4 = __ldg(tp), b4 = __ldg(tp + 1), c4 = __ldg(tp + 2);
+        const f3 a = mk(a4.x, a4.y, a4.z), b = mk(a4.w, b4.x, b4.y), c = mk(b4.z, b4.w, c4.x), gn = mk(c4.y, c4.z, c4.w);
+        const float s = sqrtf(fmaxf(0.f, u[0]));
+        const float bu = 1.f - s, bv = u[1] * s;
+        const f3 p = a * (1.f - bu - bv) + b * bu + c * bv;
+        out.gL = on_surface(p, gn, gn);
+        out.wo = normalize(g.p - p);
+        const float pL = area_pdf_direct(L, g, out.gL, out.wo);
+        if (pL == 0.f) return false;
+        const f3 Le = dot(out.wo, out.gL.n) <= 0.f ? mk(0, 0, 0) : mk(L.ke[0], L.ke[1], L.ke[2]);
+        out.weight = Le / pL / p_sel;
+        return true;
+    }
+    f3 wo;
+    if (L.type == LMGPU_LIGHT_ENVCONST) {
+        const float z = 1.f - 2.f * u[4];
+        const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float st, ct;
+        sincosf(2.f * kPi * u[5], &st, &ct);
+        wo = mk(r * ct, r * st, z);
+    } else {
+        const float* marg = S.env + L.marg_off;
+        const int y = cdf_sample(marg, L.env_h, u[4]);
+        const int x = cdf_sample(S.env + L.cond_off + size_t(y) * (L.env_w + 1), L.env_w, u[5]);
+        const float su = (float(x) + u[0]) / float(L.env_w), sv = (float(y) + u[1]) / float(L.env_h);
+        const float t = kPi * sv;
+        const float st = sinf(t);
+        const float ph = 2.f * kPi * su + L.rot;
+        wo = -mk(st * sinf(ph), cosf(t), st * cosf(ph));
+    }
+    out.gL = infinite_point(wo);
+    out.wo = wo;
+    const float pL = env_pdf_direct(S, L, g, wo);
+    if (pL == 0.f) return false;
+    out.weight = env_eval(S, L, wo) / pL / p_sel;
+    return true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Film splats: lanes that hit the same pixel are summed first, one atomic per pixel and channel.
+__device__ inline void splat(float* film, uint32_t pixel, f3 c) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    cg::coalesced_group peers = cg::labeled_partition(g, pixel);
+    const float r = cg::reduce(peers, c.x, cg::plus<float>());
+    const float gg = cg::reduce(peers, c.y, cg::plus<float>());
+    const float b = cg::reduce(peers, c.z, cg::plus<float>());
+    if (peers.thread_rank() == 0) {
+        atomicAdd(film + 3 * size_t(pixel), r);
+        atomicAdd(film + 3 * size_t(pixel) + 1, gg);
+        atomicAdd(film + 3 * size_t(pixel) + 2, b);
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Wavefront state
+struct ExtQ {
+    float4* o;     // origin (w unused)
+    float4* d;     // direction (w unused)
+    float4* thr;   // throughput, pdf of the sampled direction (projected solid angle)
+    float4* nrm;   // shading normal of the origin vertex, flags (bit 0 NEE-samplable, bit 1 camera, bits 8-15 vertex)
+    uint2* ids;    // path index, pixel
+};
+struct ShadowQ {
+    float4* o;     // origin, tmax
+    float4* d;
+    float4* c;     // contribution, pixel
+};
+struct PtConst {
+    uint32_t seed;
+    int32_t max_verts;
+    int64_t spp;
+    int32_t mode;      // LMGPU_SAMPLING_*
+    int32_t image;     // 1: image primary-ray mode
+    int32_t w, h;
+};
+
+constexpr int kBlock = 256;
+
+__device__ inline void rng_slots(uint32_t seed, uint64_t path, uint32_t vertex, int first_block, int nblocks, float* u) {
+    for (int b = 0; b < nblocks; b++) {
+        const U4 r = philox_block(seed, path, vertex * 4u + uint32_t(first_block + b));
+        u[4 * b] = r.v[0]; u[4 * b + 1] = r.v[1]; u[4 * b + 2] = r.v[2]; u[4 * b + 3] = r.v[3];
+    }
+}
+
+__device__ inline void push_shadow(const ShadowQ& sq, int* count, f3 o, f3 d, float tmax, f3 c, uint32_t pixel) {
+    const int k = atomicAdd(count, 1);
+    sq.o[k] = make_float4(o.x, o.y, o.z, tmax);
+    sq.d[k] = make_float4(d.x, d.y, d.z, 0.f);
+    sq.c[k] = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
+}
+
+__device__ inline uint32_t pixel_of(const PtConst& P, float rx, float ry) {
+    const int x = min(max(int(rx * float(P.w)), 0), P.w - 1);
+    const int y = min(max(int(ry * float(P.h)), 0), P.h - 1);
+    return uint32_t(y) * uint32_t(P.w) + uint32_t(x);
+}
+
+// NEE connection from vertex g (material m, or the camera if m == nullptr); pushes a shadow ray
+// with the contribution it carries when the connection is nonzero (renderer_pt.cpp:142-192).
+__device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, const DevMaterial* m, f3 wi, int comp, f3 thr,
+                           const float* u8, uint32_t pixel, const ShadowQ& sq, int* scount) {
+    LightSample sL;
+    if (!sample_direct(S, g, u8, sL)) return;
+    const f3 wo = -sL.wo;
+    uint32_t px = pixel;
+    f3 fs;
+    if (m == nullptr) {
+        float rx, ry;
+        if (!raster_pos(S, wo, rx, ry)) return;
+        px = pixel_of(P, rx, ry);
+        fs = mk(cam_J(S, wo), cam_J(S, wo), cam_J(S, wo));
+    } else {
+        fs = mat_eval(*m, g, wi, wo, comp, true) * sn_correction(g, wi, wo);
+    }
+    if (is_zero(fs)) return;
+    float mis = 1.f;
+    if (P.mode == LMGPU_SAMPLING_MIS) {
+        const DevLight L = S.lights[sL.light];
+        const float pl = (1.f / float(S.num_lights)) *
+                         (L.type == LMGPU_LIGHT_AREA ? area_pdf_direct(L, g, sL.gL, sL.wo) : env_pdf_direct(S, L, g, sL.gL.wo));
+        const float pb = m == nullptr ? cam_pdf(S, wo) : mat_pdf(*m, g, wi, wo, true);
+        mis = (pl == 0.f && pb == 0.f) ? 0.f : pl / (pl + pb);
+    }
+    const f3 C = thr * fs * sL.weight * mis;
+    if (is_zero(C)) return;
+    f3 dir;
+    float tmax;
+    if (sL.gL.infinite) {
+        dir = -sL.gL.wo;
+        tmax = kInf - 1.f;
+    } else {
+        dir = normalize(sL.gL.p - g.p);
+        tmax = length(sL.gL.p - g.p) * (1.f - kEps);
+    }
+    push_shadow(sq, scount, g.p, dir, tmax, C, px);
+}
+
+__device__ inline void push_ext(const ExtQ& q, int* count, f3 o, f3 d, f3 thr, float pdf, f3 n, uint32_t flags, uint32_t path,
+                                uint32_t pixel) {
+    const int k = atomicAdd(count, 1);
+    q.o[k] = make_float4(o.x, o.y, o.z, 0.f);
+    q.d[k] = make_float4(d.x, d.y, d.z, 0.f);
+    q.thr[k] = make_float4(thr.x, thr.y, thr.z, pdf);
+    q.nrm[k] = make_float4(n.x, n.y, n.z, __uint_as_float(flags));
+    q.ids[k] = make_uint2(path, pixel);
+}
+
+// Camera vertex: renderer_pt.cpp:95-116 and the first pass of the loop (NEE in image mode, the
+// jittered primary direction, raster position caching).
+__global__ void __launch_bounds__(kBlock) k_pt_generate(DevScene S, PtConst P, int64_t start, int64_t count, ExtQ q,
+                                                        int* qcount, ShadowQ sq, int* scount) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        const uint64_t path = uint64_t(start + i);
+        const int64_t pix = int64_t(path / uint64_t(P.spp));
+        float wx = 0.f, wy = 0.f, ww = 1.f, wh = 1.f;
+        if (!P.image) {
+            const int x = int(pix % P.w), y = int(pix / P.w);
+            ww = 1.f / float(P.w);
+            wh = 1.f / float(P.h);
+            wx = ww * float(x);
+            wy = wh * float(y);
+        }
+        Geom g;
+        g.p = S.cam_p; g.n = mk(0, 0, 0); g.gn = g.n; g.u = g.n; g.v = g.n; g.wo = g.n;
+        g.degenerated = true; g.infinite = false;
+        const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && P.image;
+        float u[16];
+        rng_slots(P.seed, path, 1u, 0, 4, u);
+        if (nee_ok) nee(S, P, g, nullptr, mk(0, 0, 0), 0, mk(1, 1, 1), u, 0u, sq, scount);
+        const f3 d = primary_dir(S, wx + ww * u[8], wy + wh * u[9]);
+        float rx = 0.f, ry = 0.f;
+        raster_pos(S, d, rx, ry);
+        const uint32_t pixel = pixel_of(P, rx, ry);
+        const float pdf = nee_ok ? cam_pdf(S, d) : 0.f;
+        push_ext(q, qcount, S.cam_p, d, mk(1, 1, 1), pdf, mk(0, 0, 0), (nee_ok ? 1u : 0u) | 2u | (1u << 8), uint32_t(path), pixel);
+    }
+}
+
+// Extension rays: closest hit over [Eps, Inf].
+__global__ void __launch_bounds__(kBlock) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
+                                                      const int* __restrict__ qcount, float4* __restrict__ hits,
+                                                      unsigned long long* rays, int* err) {
+    extern __shared__ uint32_t smem[];
+    const int n = *qcount;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
+    uint32_t* sb = smem + threadIdx.x;
+    uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
+    int lerr = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float4 o = qo[k], d = qd[k];
+        const TraceHit h = trace_bvh8<false, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits,
+                                                    blockDim.x, nullptr, nullptr, &lerr);
+        hits[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.id));
+    }
+    if (lerr) atomicOr(err, lerr);
+}
+
+// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film.
+__global__ void __launch_bounds__(kBlock) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
+                                                      unsigned long long* rays, int* err) {
+    extern __shared__ uint32_t smem[];
+    const int n = *scount;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
+    uint32_t* sb = smem + threadIdx.x;
+    uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
+    int lerr = 0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float4 o = sq.o[k], d = sq.d[k];
+        const TraceHit h = trace_bvh8<true, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits,
+                                                   blockDim.x, nullptr, nullptr, &lerr);
+        if (h.id < 0) {
+            const float4 c = sq.c[k];
+            splat(film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+        }
+    }
+    if (lerr) atomicOr(err, lerr);
+}
+
+// One pass of the loop body after the intersection (renderer_pt.cpp:221-300) for the hits of the
+// rays that vertex `it` emitted, then NEE and direction sampling at the new vertex it+1.
+__global__ void __launch_bounds__(kBlock) k_pt_shade(DevScene S, PtConst P, int it, ExtQ qi, const float4* __restrict__ hits,
+                                                     const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
+                                                     int* scount, float* film) {
+    const int n = *qicount;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float4 o4 = qi.o[k], d4 = qi.d[k], t4 = qi.thr[k], n4 = qi.nrm[k], h4 = hits[k];
+        const uint2 ids = qi.ids[k];
+        const uint32_t flags = __float_as_uint(n4.w);
+        const bool prev_nee = flags & 1u;
+        const f3 d = mk(d4.x, d4.y, d4.z);
+        f3 thr = mk(t4.x, t4.y, t4.z);
+        const float prev_pdf = t4.w;
+        Geom gp;  // the vertex the ray left from
+        gp.p = mk(o4.x, o4.y, o4.z);
+        gp.n = mk(n4.x, n4.y, n4.z);
+        gp.degenerated = (flags & 2u) != 0;
+        gp.infinite = false;
+        const bool direct_ok = P.mode == LMGPU_SAMPLING_NEE ? !prev_nee : true;
+        const bool use_mis = P.mode != LMGPU_SAMPLING_NAIVE && prev_nee;
+        const int32_t id = __float_as_int(h4.w);
+        if (id < 0) {
+            // miss: the environment light endpoint (scene.cpp:321-331), then the env-hit break
+            if (S.env_light >= 0 && direct_ok) {
+                const DevLight L = S.lights[S.env_light];
+                const f3 gwo = -d;
+                float mis = 1.f;
+                if (use_mis) {
+                    const float pl = (1.f / float(S.num_lights)) * env_pdf_direct(S, L, gp, gwo);
+                    mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
+                }
+                const f3 C = thr * env_eval(S, L, gwo) * mis;
+                if (!is_zero(C)) splat(film, ids.y, C);
+            }
+            continue;
+        }
+        int32_t prim;
+        const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+        const int2 ml = __ldg(S.prim_ml + prim);
+        const f3 wi = -d;
+        if (ml.y >= 0 && direct_ok) {
+            const DevLight L = S.lights[ml.y];
+            const f3 woL = wi;
+            if (dot(woL, g.n) > 0.f) {
+                float mis = 1.f;
+                if (use_mis) {
+                    const float pl = (1.f / float(S.num_lights)) * area_pdf_direct(L, gp, g, woL);
+                    mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
+                }
+                const f3 C = thr * mk(L.ke[0], L.ke[1], L.ke[2]) * mis;
+                if (!is_zero(C)) splat(film, ids.y, C);
+            }
+        }
+        float u[16];
+        rng_slots(P.seed, ids.x, uint32_t(it), 3, 1, u + 12);
+        if (it > 5) {
+            const float qrr = fmaxf(.2f, 1.f - cmax(thr));
+            if (u[12] < qrr) continue;
+            thr = thr / (1.f - qrr);
+        }
+        const DevMaterial m = S.mats[ml.x];
+        int comp = 0;
+        if (m.type == LMGPU_MAT_GLASS) {
+            f3 wt; bool total; float eta, Fr;
+            glass_fresnel(m, g, wi, wt, total, eta, Fr);
+            comp = u[13] < Fr ? 0 : 1;
+            thr = thr * (1.f / (comp == 0 ? Fr : 1.f - Fr));
+        }
+        const int nv = it + 1;
+        if (nv >= P.max_verts) continue;
+        const bool spec = mat_specular(m);
+        const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && !spec;
+        rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
+        if (nee_ok) nee(S, P, g, &m, wi, comp, thr, u, ids.y, sq, scount);
+        f3 wo, w;
+        if (!mat_sample(m, g, wi, comp, u[8], u[9], wo, w)) continue;
+        w = w * sn_correction(g, wi, wo);
+        const float pdf = (P.mode == LMGPU_SAMPLING_MIS && nee_ok) ? mat_pdf(m, g, wi, wo, true) : 0.f;
+        thr = thr * w;
+        push_ext(qo, qocount, g.p, wo, thr, pdf, g.n, (nee_ok ? 1u : 0u) | (uint32_t(nv) << 8), ids.x, ids.y);
+    }
+}
+
+__global__ void k_scale(const float* __restrict__ in, float* __restrict__ out, int64_t n, float s) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = in[i] * s;
+}
+
+// renderer::raycast, one thread per pixel (renderer_raycast.cpp:70-98)
+__global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lmgpu_raycast_params prm, float* film, int* err) {
+    extern __shared__ uint32_t smem[];
+    uint32_t* sb = smem + threadIdx.x;
+    uint32_t* sbits = smem + blockDim.x * S.bvh.depth + threadIdx.x;
+    int lerr = 0;
+    const int64_t n = int64_t(w) * h;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int x = int(i % w), y = int(i / w);
+        const float rx = ieee::div(ieee::add(float(x), .5f), float(w)), ry = ieee::div(ieee::add(float(y), .5f), float(h));
+        const f3 d = primary_dir(S, rx, ry);
+        const TraceHit hit = trace_bvh8<false, false>(S.bvh, S.cam_p, d, kEps, kInf, sb, sbits, blockDim.x, nullptr, nullptr, &lerr);
+        f3 c;
+        if (hit.id < 0) {
+            if (S.env_light >= 0) {
+                const DevLight L = S.lights[S.env_light];
+                c = prm.visualize_normal ? mk(0, 0, 0) : env_eval(S, L, -d);
+            } else {
+                c = mk(prm.bg_color[0], prm.bg_color[1], prm.bg_color[2]);
+            }
+        } else {
+            int32_t prim;
+            const Geom g = surface_at(S, hit.id, hit.u, hit.v, prim);
+            if (prm.visualize_normal) {
+                c = mk(fabsf(g.n.x), fabsf(g.n.y), fabsf(g.n.z));
+            } else {
+                f3 R;
+                if (prm.has_color) {
+                    R = mk(prm.color[0], prm.color[1], prm.color[2]);
+                } else {
+                    const DevMaterial m = S.mats[__ldg(S.prim_ml + prim).x];
+                    R = (m.type == LMGPU_MAT_DIFFUSE || m.type == LMGPU_MAT_GLOSSY) ? mk(m.c[0], m.c[1], m.c[2]) : mk(0, 0, 0);
+                }
+                c = prm.use_constant_color ? R : R * (.2f + .8f * fabsf(dot(g.n, -d)));
+            }
+        }
+        film[3 * i] = c.x;
+        film[3 * i + 1] = c.y;
+        film[3 * i + 2] = c.z;
+    }
+    if (lerr) atomicOr(err, lerr);
+}
+
+template <typename K>
+int grid_for(K kernel, int block, size_t smem) {
+    int per_sm = 0;
+    LMGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem));
+    return std::max(1, per_sm) * current_device().num_sms;
+}
+
+void ensure_queues(lmgpu_scene* s, int64_t cap) {
+    if (s->q_cap >= cap) return;
+    for (int b = 0; b < 2; b++) {
+        s->q_o[b].alloc(size_t(cap) * 16);
+        s->q_d[b].alloc(size_t(cap) * 16);
+        s->q_thr[b].alloc(size_t(cap) * 16);
+        s->q_nrm[b].alloc(size_t(cap) * 16);
+        s->q_ids[b].alloc(size_t(cap) * 8);
+    }
+    s->hits.alloc(size_t(cap) * 16);
+    s->s_o.alloc(size_t(cap) * 16);
+    s->s_d.alloc(size_t(cap) * 16);
+    s->s_c.alloc(size_t(cap) * 16);
+    s->q_cap = cap;
+}
+
+}  // namespace lmgpu
+
+using namespace lmgpu;
+
+
+// ---------------------------------------------------------------------------------------------
+// Scene upload (Scene_::build, src/scene.cpp:274-317, for the GPU renderers)
+
+namespace {
+
+// camera_pinhole.cpp:86-96 in fp32 with glm's operation order (the same arithmetic as the
+// restatement's fp32 mode, so primary rays agree bit for bit).
+struct HostCam {
+    float p[3], u[3], v[3], w[3], tf, aspect;
+};
+inline float hdot(const float* a, const float* b) {
+    const float x = a[0] * b[0], y = a[1] * b[1], z = a[2] * b[2];
+    return (x + y) + z;
+}
+inline void hcross(const float* x, const float* y, float* o) {
+    o[0] = x[1] * y[2] - y[1] * x[2];
+    o[1] = x[2] * y[0] - y[2] * x[0];
+    o[2] = x[0] * y[1] - y[0] * x[1];
+}
+inline void hnormalize(float* v) {
+    const float inv = 1.0f / std::sqrt(hdot(v, v));
+    v[0] *= inv; v[1] *= inv; v[2] *= inv;
+}
+HostCam make_camera(const lmgpu_camera& c) {
+    HostCam h;
+    for (int i = 0; i < 3; i++) { h.p[i] = c.position[i]; h.w[i] = c.position[i] - c.center[i]; }
+    hnormalize(h.w);
+    hcross(c.up, h.w, h.u);
+    hnormalize(h.u);
+    hcross(h.w, h.u, h.v);
+    const float pi = 3.14159265358979323846f;
+    h.tf = std::tan(c.vfov * pi / 180.0f * 0.5f);
+    h.aspect = c.aspect;
+    return h;
+}
+
+void ensure_film(lmgpu_film* f) {
+    if (f->sum.p) return;
+    const size_t n = size_t(f->w) * f->h * 3;
+    f->sum.alloc(n * 4);
+    f->out.alloc(n * 4);
+    LMGPU_CUDA(cudaMemset(f->sum.p, 0, n * 4));
+    LMGPU_CUDA(cudaMemset(f->out.p, 0, n * 4));
+}
+
+}  // namespace
+
+extern "C" {
+
+int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_desc* D) {
+    return guarded([&] {
+        if (!out || !accel || !D) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (accel->num_nodes == 0) throw Error(LMGPU_ERR_UNINITIALIZED, "accel is not built");
+        if (D->num_tris != accel->num_tris)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "scene triangle count differs from the accel's");
+        if (D->num_tris > 0 && (!D->positions || !D->normals || !D->geo_normals || !D->tri_prim))
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "missing per-triangle arrays");
+        if (D->num_prims < 0 || D->num_materials < 0 || D->num_lights < 0 || D->num_light_tris < 0)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "negative table size");
+        if ((D->num_prims > 0 && (!D->prim_material || !D->prim_light)) || (D->num_materials > 0 && !D->materials) ||
+            (D->num_lights > 0 && !D->lights))
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "missing table");
+        auto s = std::make_unique<lmgpu_scene>();
+        s->accel = accel;
+        const int64_t nt = D->num_tris;
+
+        // per-triangle shading records: p1 p2 p3 n1 n2 n3 gn prim (24 floats)
+        std::vector<float> shade(size_t(nt) * 24, 0.f);
+        for (int64_t t = 0; t < nt; t++) {
+            float* r = &shade[size_t(t) * 24];
+            std::memcpy(r, D->positions + 9 * t, 9 * 4);
+            std::memcpy(r + 9, D->normals + 9 * t, 9 * 4);
+            std::memcpy(r + 18, D->geo_normals + 3 * t, 3 * 4);
+            const int32_t p = D->tri_prim[t];
+            if (p < 0 || p >= D->num_prims) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "tri_prim out of range");
+            std::memcpy(r + 21, &p, 4);
+        }
+        s->shade.upload(shade.data(), shade.size());
+
+        std::vector<int32_t> pml(size_t(D->num_prims) * 2);
+        for (int32_t p = 0; p < D->num_prims; p++) {
+            const int32_t m = D->prim_material[p], l = D->prim_light[p];
+            if (m < 0 || m >= D->num_materials) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "prim_material out of range");
+            if (l < -1 || l >= D->num_lights) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "prim_light out of range");
+            pml[2 * p] = m;
+            pml[2 * p + 1] = l;
+        }
+        s->prim_ml.upload(pml.data(), pml.size());
+
+        std::vector<DevMaterial> mats(D->num_materials);
+        for (int32_t i = 0; i < D->num_materials; i++) {
+            const lmgpu_material& m = D->materials[i];
+            if (m.type < LMGPU_MAT_DIFFUSE || m.type > LMGPU_MAT_MIRROR) throw Error(LMGPU_ERR_UNSUPPORTED, "unknown material type");
+            if (m.type == LMGPU_MAT_GLOSSY && !(m.ax > 0.f && m.ay > 0.f)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "glossy roughness must be > 0");
+            mats[i] = DevMaterial{m.type, {m.color[0], m.color[1], m.color[2]}, m.ax, m.ay, m.ni, 0};
+        }
+        s->mats.upload(mats.data(), mats.size());
+
+        // lights: area CDFs and env tables are built here in double precision, then stored fp32
+        std::vector<DevLight> lights(D->num_lights);
+        std::vector<float> cdf, ltri, env;
+        int32_t env_light = -1;
+        for (int32_t i = 0; i < D->num_lights; i++) {
+            const lmgpu_light& L = D->lights[i];
+            DevLight& dl = lights[i];
+            std::memset(&dl, 0, sizeof(dl));
+            dl.type = L.type;
+            dl.ke[0] = L.ke[0]; dl.ke[1] = L.ke[1]; dl.ke[2] = L.ke[2];
+            if (L.type == LMGPU_LIGHT_AREA) {
+                if (L.tri_count <= 0 || L.tri_offset < 0 || L.tri_offset + L.tri_count > D->num_light_tris)
+                    throw Error(LMGPU_ERR_INVALID_ARGUMENT, "area light triangle range out of bounds");
+                dl.tri_off = int32_t(ltri.size() / 12);
+                dl.tri_cnt = int32_t(L.tri_count);
+                dl.cdf_off = int32_t(cdf.size());
+                double sum = 0;
+                std::vector<double> c(size_t(L.tri_count) + 1, 0.0);
+                for (int64_t k = 0; k < L.tri_count; k++) {
+                    sum += double(D->light_tri_area[L.tri_offset + k]);
+                    c[k + 1] = sum;
+                }
+                if (!(sum > 0)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "area light has zero area");
+                for (double v : c) cdf.push_back(float(v / sum));
+                dl.invA_J = float((1.0 / sum) / double(L.transform_j));
+                for (int64_t k = 0; k < L.tri_count; k++) {
+                    const float* p = D->light_tri_p + 9 * (L.tri_offset + k);
+                    const float* g = D->light_tri_gn + 3 * (L.tri_offset + k);
+                    const float rec[12] = {p[0], p[1], p[2], p[3], p[4], p[5], p[6], p[7], p[8], g[0], g[1], g[2]};
+                    ltri.insert(ltri.end(), rec, rec + 12);
+                }
+            } else if (L.type == LMGPU_LIGHT_ENVCONST || L.type == LMGPU_LIGHT_ENV) {
+                if (env_light >= 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "only one environment light is allowed");
+                env_light = i;
+                if (L.type == LMGPU_LIGHT_ENV) {
+                    const int w = L.env_w, h = L.env_h;
+                    if (w <= 0 || h <= 0 || !D->env_texels || L.env_offset < 0 || L.env_offset + int64_t(w) * h * 3 > D->num_env_texels)
+                        throw Error(LMGPU_ERR_INVALID_ARGUMENT, "env texture out of bounds");
+                    const float* tex = D->env_texels + L.env_offset;
+                    dl.env_w = w; dl.env_h = h;
+                    dl.rot = L.rot_deg * 3.14159265358979323846f / 180.0f;
+                    dl.scale = L.scale;
+                    dl.tex_off = int32_t(env.size());
+                    env.insert(env.end(), tex, tex + size_t(w) * h * 3);
+                    // light_env.cpp:65-71 then Dist2::init (math.h:396-409)
+                    std::vector<double> rows(h + 1, 0.0);
+                    std::vector<double> cond(size_t(h) * (w + 1), 0.0);
+                    double msum = 0;
+                    for (int y = 0; y < h; y++) {
+                        double rs = 0;
+                        for (int x = 0; x < w; x++) {
+                            const int i2 = y * w + x;
+                            const float* t = tex + 3 * size_t(i2);
+                            const double m = std::max(std::max(double(t[0]) * L.scale, double(t[1]) * L.scale), double(t[2]) * L.scale);
+                            rs += m * std::sin(3.14159265358979323846 * (double(i2) / w + .5) / h);
+                            cond[size_t(y) * (w + 1) + x + 1] = rs;
+                        }
+                        for (int x = 0; x <= w; x++) cond[size_t(y) * (w + 1) + x] = rs > 0 ? cond[size_t(y) * (w + 1) + x] / rs : 0.0;
+                        msum += rs;
+                        rows[y + 1] = msum;
+                    }
+                    if (!(msum > 0)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "env map is black");
+                    dl.marg_off = int32_t(env.size());
+                    for (int y = 0; y <= h; y++) env.push_back(float(rows[y] / msum));
+                    dl.cond_off = int32_t(env.size());
+                    for (double v : cond) env.push_back(float(v));
+                }
+            } else {
+                throw Error(LMGPU_ERR_UNSUPPORTED, "unknown light type");
+            }
+        }
+        s->lights.upload(lights.data(), lights.size());
+        s->ltri.upload(ltri.data(), ltri.size());
+        s->cdf.upload(cdf.data(), cdf.size());
+        s->env.upload(env.data(), env.size());
+
+        DevScene& ds = s->dev;
+        ds.bvh = device_view(accel);
+        ds.shade = s->shade.as<const float4>();
+        ds.prim_ml = s->prim_ml.as<const int2>();
+        ds.mats = s->mats.as<const DevMaterial>();
+        ds.lights = s->lights.as<const DevLight>();
+        ds.num_lights = D->num_lights;
+        ds.env_light = env_light;
+        ds.ltri = s->ltri.as<const float4>();
+        ds.cdf = s->cdf.as<const float>();
+        ds.env = s->env.as<const float>();
+        ds.has_camera = D->has_camera;
+        if (D->has_camera) {
+            const HostCam c = make_camera(D->camera);
+            ds.cam_p = mk(c.p[0], c.p[1], c.p[2]);
+            ds.cam_u = mk(c.u[0], c.u[1], c.u[2]);
+            ds.cam_v = mk(c.v[0], c.v[1], c.v[2]);
+            ds.cam_w = mk(c.w[0], c.w[1], c.w[2]);
+            ds.tf = c.tf;
+            ds.aspect = c.aspect;
+        }
+        s->counters.alloc(64);
+        LMGPU_CUDA(cudaMemset(s->counters.p, 0, 64));
+        *out = s.release();
+    });
+}
+
+int lmgpu_scene_destroy(lmgpu_scene* scene) {
+    return guarded([&] { delete scene; });
+}
+
+int lmgpu_scene_device_bytes(const lmgpu_scene* s, int64_t* out) {
+    return guarded([&] {
+        if (!s || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        size_t b = s->shade.bytes + s->prim_ml.bytes + s->mats.bytes + s->lights.bytes + s->ltri.bytes + s->cdf.bytes + s->env.bytes;
+        for (int i = 0; i < 2; i++) b += s->q_o[i].bytes + s->q_d[i].bytes + s->q_thr[i].bytes + s->q_nrm[i].bytes + s->q_ids[i].bytes;
+        b += s->hits.bytes + s->s_o.bytes + s->s_d.bytes + s->s_c.bytes + s->counters.bytes;
+        *out = int64_t(b);
+    });
+}
+
+// ---------------------------------------------------------------------------------------------
+// Film
+
+int lmgpu_film_create(lmgpu_film** out, int32_t w, int32_t h) {
+    return guarded([&] {
+        if (!out || w <= 0 || h <= 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid film size");
+        auto f = std::make_unique<lmgpu_film>();
+        f->w = w;
+        f->h = h;
+        *out = f.release();  // device memory is allocated on first use
+    });
+}
+
+int lmgpu_film_destroy(lmgpu_film* film) {
+    return guarded([&] { delete film; });
+}
+
+int lmgpu_film_clear(lmgpu_film* f) {
+    return guarded([&] {
+        if (!f) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "film is null");
+        ensure_film(f);
+        const size_t n = size_t(f->w) * f->h * 3;
+        LMGPU_CUDA(cudaMemset(f->sum.p, 0, n * 4));
+        LMGPU_CUDA(cudaMemset(f->out.p, 0, n * 4));
+        f->accumulated_spp = 0;
+        f->scale = 1.0;
+    });
+}
+
+int lmgpu_film_read(lmgpu_film* f, float* out_rgb) {
+    return guarded([&] {
+        if (!f || !out_rgb) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        ensure_film(f);
+        LMGPU_CUDA(cudaMemcpy(out_rgb, f->out.p, size_t(f->w) * f->h * 3 * 4, cudaMemcpyDeviceToHost));
+    });
+}
+
+int lmgpu_film_device_ptr(lmgpu_film* f, void** out) {
+    return guarded([&] {
+        if (!f || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        ensure_film(f);
+        *out = f->out.p;
+    });
+}
+
+// ---------------------------------------------------------------------------------------------
+// Renderers
+
+int lmgpu_render_raycast(lmgpu_scene* s, lmgpu_film* f, const lmgpu_raycast_params* prm, void* stream) {
+    return guarded([&] {
+        if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        ensure_film(f);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const size_t smem = trace_smem(s->accel) * kBlock / 128;
+        int* err = s->counters.as<int>() + 3;
+        LMGPU_CUDA(cudaMemsetAsync(err, 0, 4, st));
+        const int64_t n = int64_t(f->w) * f->h;
+        int g = grid_for(k_raycast, kBlock, smem);
+        g = int(std::min<int64_t>(g, (n + kBlock - 1) / kBlock));
+        k_raycast<<<g, kBlock, smem, st>>>(s->dev, f->w, f->h, *prm, f->sum.as<float>(), err);
+        LMGPU_CUDA(cudaGetLastError());
+        k_scale<<<256, 256, 0, st>>>(f->sum.as<float>(), f->out.as<float>(), n * 3, 1.0f);
+        int herr = 0;
+        LMGPU_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
+        f->scale = 1.0;
+        f->accumulated_spp = 1;
+    });
+}
+
+int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, void* stream, lmgpu_render_stats* stats) {
+    return guarded([&] {
+        if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
+        if (prm->spp <= 0 || prm->max_verts < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "spp must be > 0 and max_verts >= 1");
+        if (prm->max_verts > 255) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 255");
+        if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
+        ensure_film(f);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int64_t npix = int64_t(f->w) * f->h;
+        const int64_t total = npix * prm->spp;
+        if (total > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "more than 2^32 paths in one render");
+        int64_t wave = prm->wave_paths > 0 ? prm->wave_paths : (int64_t(1) << 22);
+        wave = std::min(wave, total);
+        ensure_queues(s, wave);
+
+        PtConst P;
+        P.seed = prm->seed;
+        P.max_verts = prm->max_verts;
+        P.spp = prm->spp;
+        P.mode = prm->sampling_mode;
+        P.image = prm->primary_mode == LMGPU_PRIMARY_IMAGE;
+        P.w = f->w;
+        P.h = f->h;
+
+        ExtQ q[2];
+        for (int b = 0; b < 2; b++)
+            q[b] = ExtQ{s->q_o[b].as<float4>(), s->q_d[b].as<float4>(), s->q_thr[b].as<float4>(), s->q_nrm[b].as<float4>(),
+                        s->q_ids[b].as<uint2>()};
+        ShadowQ sq{s->s_o.as<float4>(), s->s_d.as<float4>(), s->s_c.as<float4>()};
+        int* cnt = s->counters.as<int>();  // [0],[1] extension queues, [2] shadow queue, [3] error
+        unsigned long long* rays = reinterpret_cast<unsigned long long*>(s->counters.as<char>() + 32);
+        float* film = f->sum.as<float>();
+        const Bvh8 bvh = s->dev.bvh;
+        const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
+
+        const int g_gen = grid_for(k_pt_generate, kBlock, 0);
+        const int g_ext = grid_for(k_pt_extend, kBlock, tsmem);
+        const int g_sh = grid_for(k_pt_shadow, kBlock, tsmem);
+        const int g_shade = grid_for(k_pt_shade, kBlock, 0);
+
+        cudaEvent_t e0, e1;
+        LMGPU_CUDA(cudaEventCreate(&e0));
+        LMGPU_CUDA(cudaEventCreate(&e1));
+        std::vector<cudaEvent_t> tev;
+        const bool time_trace = stats != nullptr;
+        auto tmark = [&]() {
+            if (!time_trace) return;
+            cudaEvent_t e;
+            LMGPU_CUDA(cudaEventCreate(&e));
+            LMGPU_CUDA(cudaEventRecord(e, st));
+            tev.push_back(e);
+        };
+
+        LMGPU_CUDA(cudaEventRecord(e0, st));
+        if (!prm->accumulate) {
+            LMGPU_CUDA(cudaMemsetAsync(film, 0, size_t(npix) * 3 * 4, st));
+            f->accumulated_spp = 0;
+        }
+        LMGPU_CUDA(cudaMemsetAsync(s->counters.p, 0, 64, st));
+        for (int64_t start = 0; start < total; start += wave) {
+            const int64_t n = std::min(wave, total - start);
+            int cur = 0;
+            LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
+            k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0], cnt + 0, sq, cnt + 2);
+            LMGPU_CUDA(cudaGetLastError());
+            if (P.image) {
+                tmark();
+                k_pt_shadow<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3);
+                tmark();
+                LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+            }
+            for (int it = 1; it < P.max_verts; it++) {
+                tmark();
+                k_pt_extend<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3);
+                tmark();
+                LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
+                LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, it, q[cur], s->hits.as<float4>(), cnt + cur, q[1 - cur],
+                                                      cnt + (1 - cur), sq, cnt + 2, film);
+                tmark();
+                k_pt_shadow<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3);
+                tmark();
+                LMGPU_CUDA(cudaGetLastError());
+                cur = 1 - cur;
+            }
+        }
+        f->accumulated_spp += prm->spp;
+        const double scale = P.image ? double(npix) / double(f->accumulated_spp) : 1.0 / double(f->accumulated_spp);
+        f->scale = scale;
+        k_scale<<<1024, 256, 0, st>>>(film, f->out.as<float>(), npix * 3, float(scale));
+        LMGPU_CUDA(cudaEventRecord(e1, st));
+        unsigned long long hr[2];
+        int herr = 0;
+        LMGPU_CUDA(cudaMemcpyAsync(hr, rays, sizeof(hr), cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, 4, cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        LMGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        double tms = 0;
+        for (size_t i = 0; i + 1 < tev.size(); i += 2) {
+            float m = 0.f;
+            LMGPU_CUDA(cudaEventElapsedTime(&m, tev[i], tev[i + 1]));
+            tms += m;
+        }
+        for (auto e : tev) cudaEventDestroy(e);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
+        if (stats) {
+            stats->paths = total;
+            stats->extension_rays = int64_t(hr[0]);
+            stats->shadow_rays = int64_t(hr[1]);
+            stats->rays = int64_t(hr[0] + hr[1]);
+            stats->elapsed_ms = ms;
+            stats->trace_ms = tms;
+        }
+    });
+}
+
+}  // extern "C"

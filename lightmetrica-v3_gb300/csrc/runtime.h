@@ -1,0 +1,96 @@
+// Host-side runtime shared by the C-ABI translation units: status codes, error text, device
+// buffers and the opaque handle types declared in include/lmgpu.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/lmgpu.h"
+#include "bvh_build.h"
+
+namespace lmgpu {
+
+// An error carrying an LMGPU_ERR_* code; C entry points catch it and return the code.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_last_error(const std::string& msg);
+
+#define LMGPU_CUDA(call)                                                                         \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            throw ::lmgpu::Error(e_ == cudaErrorMemoryAllocation ? LMGPU_ERR_OUT_OF_MEMORY : LMGPU_ERR_CUDA, \
+                                 std::string(#call) + ": " + cudaGetErrorString(e_));           \
+    } while (0)
+
+// Runs `fn` and converts any failure into a status code plus lmgpu_last_error() text.
+template <typename Fn>
+int guarded(Fn&& fn) {
+    try {
+        fn();
+        return LMGPU_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return LMGPU_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return LMGPU_ERR_INTERNAL;
+    }
+}
+
+// Owning device allocation.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void alloc(size_t n) {
+        if (n <= bytes && p) return;
+        release();
+        if (n == 0) return;
+        LMGPU_CUDA(cudaMalloc(&p, n));
+        bytes = n;
+    }
+    template <typename T>
+    void upload(const T* src, size_t count) {
+        alloc(count * sizeof(T));
+        if (count) LMGPU_CUDA(cudaMemcpy(p, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+struct DeviceInfo {
+    int device = 0;
+    int num_sms = 0;
+};
+DeviceInfo& current_device();
+
+}  // namespace lmgpu
+
+struct lmgpu_accel {
+    int device = 0;
+    int64_t num_tris = 0;
+    int64_t num_nodes = 0;
+    int32_t depth = 0;
+    double build_seconds = 0;
+    double sah_cost = 0;
+    lmgpu::DevBuf nodes, tris;
+    lmgpu::DevBuf scratch_rays, scratch_hits, err;
+};

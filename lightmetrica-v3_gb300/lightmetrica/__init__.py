@@ -1,0 +1,972 @@
+"""Drop-in `lightmetrica` module for the GPU rendering hot path.
+
+Mirrors the part of the reference's Python API (src/pylm.cpp, lightmetrica/__init__.py) that the
+functests use to build scenes and render them:
+
+    import lightmetrica as lm
+    lm.init()
+    film = lm.load_film('film', 'bitmap', w=1920, h=1080)
+    camera = lm.load_camera('camera', 'pinhole', position=[..], center=[..], up=[0,1,0], vfov=30, aspect=16/9)
+    mesh = lm.load_mesh('mesh', 'raw', ps=[..], ns=[..], ts=[..], fs={'p': [..], 't': [..], 'n': [..]})
+    material = lm.load_material('mat', 'diffuse', Kd=[.75, .75, .75])
+    accel = lm.load_accel('accel', 'sahbvh')
+    scene = lm.load_scene('scene', 'default', accel=accel)
+    scene.add_primitive(camera=camera)
+    scene.add_primitive(mesh=mesh, material=material)
+    scene.build()
+    renderer = lm.load_renderer('renderer', 'pt', scene=scene, output=film, max_verts=9, scheduler='sample', spp=16)
+    renderer.render()
+    img = film.buffer()
+
+Every accel key the reference registers (accel::sahbvh, accel::nanort, accel::embree,
+accel::embreeinstanced) and accel::gpu resolve to the GB300 8-wide BVH; renderer::pt and
+renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a missing
+liblmgpu.so raises at the first render or build.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+from typing import Any
+
+import numpy as np
+
+from . import _native as N
+from ._native import LmGpuError
+
+Release = True
+Inf = 1e10
+Eps = 1e-3
+
+# ---------------------------------------------------------------------------------------------
+# Component registry (include/lm/component.h: keys "interface::impl", locators "$.assets.<name>")
+
+_assets: dict[str, "Component"] = {}
+_registry: dict[str, type] = {}
+
+
+def _reg(key: str, *aliases: str):
+    def deco(cls):
+        _registry[key] = cls
+        for a in aliases:
+            _registry[a] = cls
+        cls.key_name = key
+        return cls
+    return deco
+
+
+class Component:
+    key_name = ""
+
+    def __init__(self, name: str, prop: dict):
+        self._name = name
+        self._prop = dict(prop)
+        self.construct(self._prop)
+
+    def construct(self, prop: dict) -> None:
+        pass
+
+    def key(self) -> str:
+        return self.key_name
+
+    def loc(self) -> str:
+        return "$.assets." + self._name
+
+    def name(self) -> str:
+        return self._name
+
+    @property
+    def prop(self) -> dict:
+        return self._prop
+
+    def __repr__(self) -> str:
+        return f"<{self.key_name} {self.loc()}>"
+
+
+def _resolve(v: Any) -> Any:
+    """A Component argument or its locator string resolves to the component (json.h:225-247)."""
+    if isinstance(v, Component) or v is None:
+        return v
+    if isinstance(v, str):
+        if v.startswith("$.assets."):
+            name = v[len("$.assets."):]
+        else:
+            name = v
+        if name in _assets:
+            return _assets[name]
+    raise LmGpuError(1, f"Invalid component reference: {v!r}")
+
+
+def _req(prop: dict, key: str) -> Any:
+    if key not in prop:
+        raise LmGpuError(1, f"Missing property [name='{key}']")
+    return prop[key]
+
+
+def _vec3(v) -> np.ndarray:
+    a = np.asarray(v, dtype=np.float64).reshape(-1)
+    if a.size == 1:
+        a = np.repeat(a, 3)
+    if a.size != 3:
+        raise LmGpuError(1, f"Expected a 3-vector, got {v!r}")
+    return a
+
+
+# ---------------------------------------------------------------------------------------------
+# Library lifecycle (src/user.cpp:54-112)
+
+def init(prop: dict | None = None, **kwargs) -> None:
+    """lm.init: loads liblmgpu.so (raises if it is not built) and clears the asset tree."""
+    N.lib()
+    reset()
+
+
+def shutdown() -> None:
+    reset()
+
+
+def reset() -> None:
+    for a in list(_assets.values()):
+        if hasattr(a, "_release"):
+            a._release()
+    _assets.clear()
+
+
+def info() -> None:
+    print("lightmetrica (GB300 hot path): liblmgpu", N.lib().lmgpu_version())
+
+
+def get(loc: str) -> Component:
+    return _resolve(loc)
+
+
+def _load(iface: str, name: str, impl: str, prop: dict | None, kwargs: dict) -> Component:
+    p = dict(prop or {})
+    p.update(kwargs)
+    key = impl if "::" in impl else f"{iface}::{impl}"
+    cls = _registry.get(key)
+    if cls is None:
+        raise LmGpuError(1, f"Missing component [key='{key}']")
+    if name in _assets and hasattr(_assets[name], "_release"):
+        _assets[name]._release()
+    comp = cls(name, p)
+    _assets[name] = comp
+    return comp
+
+
+def load_film(name, impl, prop=None, **kw): return _load("film", name, impl, prop, kw)
+def load_camera(name, impl, prop=None, **kw): return _load("camera", name, impl, prop, kw)
+def load_mesh(name, impl, prop=None, **kw): return _load("mesh", name, impl, prop, kw)
+def load_material(name, impl, prop=None, **kw): return _load("material", name, impl, prop, kw)
+def load_light(name, impl, prop=None, **kw): return _load("light", name, impl, prop, kw)
+def load_texture(name, impl, prop=None, **kw): return _load("texture", name, impl, prop, kw)
+def load_accel(name, impl, prop=None, **kw): return _load("accel", name, impl, prop, kw)
+def load_scene(name, impl, prop=None, **kw): return _load("scene", name, impl, prop, kw)
+def load_renderer(name, impl, prop=None, **kw): return _load("renderer", name, impl, prop, kw)
+
+
+def load(name: str, impl_key: str, prop: dict | None = None, **kw) -> Component:
+    iface = impl_key.split("::")[0]
+    return _load(iface, name, impl_key, prop, kw)
+
+
+class _Namespace:
+    pass
+
+
+comp = _Namespace()
+comp.get = get
+comp.load_plugin = lambda path: None          # accel/renderer plugins are built in
+comp.load_plugin_directory = lambda path: None
+comp.unload_plugin = lambda path: None
+comp.unload_all_plugins = lambda: None
+comp.foreach_registered = lambda f: [f(k) for k in sorted(_registry)]
+
+# Subsystems of the reference that have no work to do on the GPU path.
+log = _Namespace()
+log.init = lambda *a, **k: None
+log.shutdown = lambda: None
+progress = _Namespace()
+progress.init = lambda *a, **k: None
+progress.shutdown = lambda: None
+parallel = _Namespace()
+parallel.init = lambda *a, **k: None
+parallel.shutdown = lambda: None
+debug = _Namespace()
+debug.attach_to_debugger = lambda: None
+debug.print_asset_tree = lambda *a, **k: None
+
+
+def registered_components() -> list[str]:
+    return sorted(_registry)
+
+
+def pylm_component(name: str):
+    def deco(cls):
+        _registry[name] = cls
+        return cls
+    return deco
+
+
+def array(*args, **kwargs):
+    kwargs.setdefault("dtype", np.float32)
+    return np.array(*args, **kwargs)
+
+
+# ---------------------------------------------------------------------------------------------
+# Transforms (src/pylm.cpp:88-99): 4x4 numpy matrices acting on column vectors.
+
+def identity() -> np.ndarray:
+    return np.eye(4)
+
+
+def translate(v) -> np.ndarray:
+    m = np.eye(4)
+    m[:3, 3] = _vec3(v)
+    return m
+
+
+def scale(v) -> np.ndarray:
+    m = np.eye(4)
+    m[0, 0], m[1, 1], m[2, 2] = _vec3(v)
+    return m
+
+
+def rotate(angle: float, axis) -> np.ndarray:
+    a = _vec3(axis)
+    a = a / np.linalg.norm(a)
+    c, s = math.cos(angle), math.sin(angle)
+    x, y, z = a
+    r = np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                  [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
+                  [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]])
+    m = np.eye(4)
+    m[:3, :3] = r
+    return m
+
+
+def rad(deg: float) -> float:
+    return deg * math.pi / 180.0
+
+
+def v3(a, b, c) -> np.ndarray:
+    return np.array([a, b, c], dtype=np.float64)
+
+
+# ---------------------------------------------------------------------------------------------
+# Assets
+
+@_reg("film::bitmap")
+class FilmBitmap(Component):
+    """film::bitmap (src/film/film_bitmap.cpp) backed by a device fp32 accumulator."""
+
+    def construct(self, prop):
+        self.w = int(_req(prop, "w"))
+        self.h = int(_req(prop, "h"))
+        h = C.c_void_p()
+        N.check(N.lib().lmgpu_film_create(C.byref(h), self.w, self.h))
+        self._h = h
+
+    def _release(self):
+        if getattr(self, "_h", None):
+            N.lib().lmgpu_film_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._release()
+        except Exception:
+            pass
+
+    def size(self):
+        return (self.w, self.h)
+
+    def num_pixels(self) -> int:
+        return self.w * self.h
+
+    def aspect(self) -> float:
+        return self.w / self.h
+
+    def clear(self):
+        N.check(N.lib().lmgpu_film_clear(self._h))
+
+    def buffer_f32(self) -> np.ndarray:
+        out = np.empty((self.h, self.w, 3), dtype=np.float32)
+        N.check(N.lib().lmgpu_film_read(self._h, N.fptr(out)))
+        return out
+
+    def buffer(self) -> np.ndarray:
+        """Film::buffer: (h, w, 3) pixels, row 0 at the bottom (film.h:166-171)."""
+        return self.buffer_f32().astype(np.float64)
+
+    def save(self, path: str) -> bool:
+        """Writes .pfm (film_bitmap.cpp:197-201, rows unflipped) or .npy."""
+        img = self.buffer_f32()
+        if path.endswith(".pfm"):
+            with open(path, "wb") as f:
+                f.write(f"PF\n{self.w} {self.h}\n-1\n".encode())
+                f.write(np.ascontiguousarray(img, dtype="<f4").tobytes())
+            return True
+        if path.endswith(".npy"):
+            np.save(path, img)
+            return True
+        raise LmGpuError(2, f"Invalid extension [path='{path}']")
+
+
+@_reg("camera::pinhole")
+class CameraPinhole(Component):
+    def construct(self, prop):
+        if "matrix" in prop:
+            raise LmGpuError(2, "camera::pinhole 'matrix' prop is not supported on the GPU path")
+        self.position = _vec3(_req(prop, "position"))
+        self.center = _vec3(_req(prop, "center"))
+        self.up = _vec3(_req(prop, "up"))
+        self.vfov = float(_req(prop, "vfov"))
+        self.aspect = float(_req(prop, "aspect"))
+
+    def set_aspect_ratio(self, aspect: float) -> None:
+        self.aspect = float(aspect)
+
+
+@_reg("mesh::raw")
+class MeshRaw(Component):
+    """mesh::raw (src/mesh/mesh_raw.cpp:50-68). ps/ns/ts flat lists or arrays; fs {'p','t','n'}."""
+
+    def construct(self, prop):
+        self.ps = np.asarray(_req(prop, "ps"), dtype=np.float32).reshape(-1, 3)
+        self.ns = np.asarray(prop.get("ns", []), dtype=np.float32).reshape(-1, 3)
+        self.ts = np.asarray(prop.get("ts", []), dtype=np.float32).reshape(-1, 2)
+        fs = _req(prop, "fs")
+        self.fp = np.asarray(fs["p"], dtype=np.int32).reshape(-1)
+        self.fn = np.asarray(fs.get("n", fs["p"]), dtype=np.int32).reshape(-1)
+        self.ft = np.asarray(fs.get("t", fs["p"]), dtype=np.int32).reshape(-1)
+        if self.fp.size % 3 != 0:
+            raise LmGpuError(1, "mesh::raw: face index count is not a multiple of 3")
+        if self.fp.size and (self.fp.min() < 0 or self.fp.max() >= len(self.ps)):
+            raise LmGpuError(1, "mesh::raw: position index out of range")
+        if self.ns.size == 0:
+            raise LmGpuError(1, "mesh::raw: normals are required")
+        if self.fn.size and (self.fn.min() < 0 or self.fn.max() >= len(self.ns)):
+            raise LmGpuError(1, "mesh::raw: normal index out of range")
+
+    def num_triangles(self) -> int:
+        return self.fp.size // 3
+
+    def tri_positions(self) -> np.ndarray:
+        return self.ps[self.fp].reshape(-1, 3, 3)
+
+    def tri_normals(self) -> np.ndarray:
+        return self.ns[self.fn].reshape(-1, 3, 3)
+
+
+_MAT_TYPES = {"material::diffuse": 0, "material::glossy": 1, "material::glass": 2, "material::mirror": 3}
+
+
+class _Material(Component):
+    def native(self) -> N.Material:
+        m = N.Material()
+        m.type = _MAT_TYPES[self.key_name]
+        return m
+
+
+@_reg("material::diffuse")
+class MaterialDiffuse(_Material):
+    def construct(self, prop):
+        if "mapKd" in prop:
+            raise LmGpuError(2, "material::diffuse mapKd textures are not supported on the GPU path")
+        self.Kd = _vec3(prop.get("Kd", [1, 1, 1]))
+
+    def native(self):
+        m = super().native()
+        m.color[:] = [float(x) for x in self.Kd]
+        return m
+
+
+@_reg("material::glossy")
+class MaterialGlossy(_Material):
+    def construct(self, prop):
+        self.Ks = _vec3(_req(prop, "Ks"))
+        self.ax = float(_req(prop, "ax"))
+        self.ay = float(_req(prop, "ay"))
+
+    def native(self):
+        m = super().native()
+        m.color[:] = [float(x) for x in self.Ks]
+        m.ax, m.ay = self.ax, self.ay
+        return m
+
+
+@_reg("material::glass")
+class MaterialGlass(_Material):
+    def construct(self, prop):
+        self.Ni = float(_req(prop, "Ni"))
+
+    def native(self):
+        m = super().native()
+        m.ni = self.Ni
+        return m
+
+
+@_reg("material::mirror")
+class MaterialMirror(_Material):
+    pass
+
+
+@_reg("texture::bitmap")
+class TextureBitmap(Component):
+    """texture::bitmap with an in-memory array ('data': h x w x 3) or a .pfm/.npy 'path'."""
+
+    def construct(self, prop):
+        if "data" in prop:
+            self.data = np.ascontiguousarray(np.asarray(prop["data"], dtype=np.float32)[..., :3])
+        else:
+            path = _req(prop, "path")
+            self.data = _read_image(path)
+        self.h, self.w = self.data.shape[:2]
+
+
+def _read_image(path: str) -> np.ndarray:
+    if path.endswith(".npy"):
+        return np.ascontiguousarray(np.load(path).astype(np.float32)[..., :3])
+    if path.endswith(".pfm"):
+        with open(path, "rb") as f:
+            kind = f.readline().strip()
+            w, h = map(int, f.readline().split())
+            s = float(f.readline())
+            ch = 3 if kind == b"PF" else 1
+            data = np.frombuffer(f.read(), dtype="<f4" if s < 0 else ">f4").reshape(h, w, ch).astype(np.float32)
+            if ch == 1:
+                data = np.repeat(data, 3, axis=2)
+            return np.ascontiguousarray(data)
+    raise LmGpuError(2, f"Unsupported image format [path='{path}'] (use .pfm or .npy)")
+
+
+class _Light(Component):
+    pass
+
+
+@_reg("light::area")
+class LightArea(_Light):
+    def construct(self, prop):
+        self.Ke = _vec3(_req(prop, "Ke"))
+        self.mesh = _resolve(_req(prop, "mesh"))
+
+
+@_reg("light::envconst")
+class LightEnvConst(_Light):
+    def construct(self, prop):
+        self.Le = _vec3(_req(prop, "Le"))
+
+
+@_reg("light::env")
+class LightEnv(_Light):
+    """light::env. The reference loads envmap_path through texture::bitmap; here 'envmap_path'
+    may be a .pfm/.npy file, or 'envmap' an in-memory (h, w, 3) array or texture component."""
+
+    def construct(self, prop):
+        if "envmap" in prop:
+            e = prop["envmap"]
+            self.data = _resolve(e).data if isinstance(e, (str, Component)) else np.ascontiguousarray(np.asarray(e, np.float32)[..., :3])
+        else:
+            self.data = _read_image(_req(prop, "envmap_path"))
+        self.rot = float(prop.get("rot", 0.0))
+        self.scale = float(prop.get("scale", 1.0))
+
+
+@_reg("accel::gpu", "accel::sahbvh", "accel::nanort", "accel::embree", "accel::embreeinstanced")
+class AccelGpu(Component):
+    """The accel slot (include/lm/accel.h): an 8-wide quantized BVH built on the host and traced on
+    the GPU. Registered under every key the reference's accels use."""
+
+    def construct(self, prop):
+        h = C.c_void_p()
+        N.check(N.lib().lmgpu_accel_create(C.byref(h)))
+        self._h = h
+        self.num_tris = 0
+
+    def _release(self):
+        if getattr(self, "_h", None):
+            N.lib().lmgpu_accel_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._release()
+        except Exception:
+            pass
+
+    def build_triangles(self, tri_p: np.ndarray) -> None:
+        tri_p = np.ascontiguousarray(tri_p, dtype=np.float32).reshape(-1, 9)
+        N.check(N.lib().lmgpu_accel_build(self._h, N.fptr(tri_p), tri_p.shape[0]))
+        self.num_tris = tri_p.shape[0]
+
+    def build(self, scene: "SceneDefault") -> None:
+        """Accel::build(const Scene&): flattens the scene and builds over its triangles."""
+        flat = scene._flatten()
+        self.build_triangles(flat["positions"])
+
+    def stats(self) -> dict:
+        s = N.AccelStats()
+        N.check(N.lib().lmgpu_accel_get_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in N.AccelStats._fields_ if k != "reserved"}
+
+    def intersect_batch(self, rays: np.ndarray) -> np.ndarray:
+        """Batched Accel::intersect. rays: (n, 8) float32 (o, tmin, d, tmax). Returns a structured
+        array with fields t, u, v, prim (flattened triangle index, -1 = miss)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        out = np.zeros(rays.shape[0], dtype=[("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<i4")])
+        N.check(N.lib().lmgpu_accel_intersect(self._h, N.fptr(rays), rays.shape[0],
+                                              out.ctypes.data_as(C.POINTER(N.Hit))))
+        return out
+
+    def intersect(self, ray_o, ray_d, tmin: float = Eps, tmax: float = Inf):
+        """Single-ray Accel::intersect; returns (t, (u, v), flattened triangle index) or None."""
+        r = np.array([[*_vec3(ray_o), tmin, *_vec3(ray_d), tmax]], dtype=np.float32)
+        h = self.intersect_batch(r)[0]
+        if h["prim"] < 0:
+            return None
+        return float(h["t"]), (float(h["u"]), float(h["v"])), int(h["prim"])
+
+
+# ---------------------------------------------------------------------------------------------
+# Scene (src/scene.cpp, include/lm/scene.h)
+
+def _f32_matmul(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """4x4 product in fp32 with glm's order: column i = ((A0*B0i + A1*B1i) + A2*B2i) + A3*B3i."""
+    a = a.astype(np.float32)
+    b = b.astype(np.float32)
+    out = np.empty((4, 4), dtype=np.float32)
+    for i in range(4):
+        for k in range(4):
+            out[k, i] = ((a[k, 0] * b[0, i] + a[k, 1] * b[1, i]) + a[k, 2] * b[2, i]) + a[k, 3] * b[3, i]
+    return out
+
+
+def _f32_xform(m: np.ndarray, p: np.ndarray) -> np.ndarray:
+    """M * vec4(p, 1) in fp32 with glm's pairing: (m0*x + m1*y) + (m2*z + m3*1)."""
+    m = m.astype(np.float32)
+    x, y, z = p[..., 0], p[..., 1], p[..., 2]
+    one = np.float32(1)
+    out = np.empty(p.shape, dtype=np.float32)
+    for i in range(3):
+        out[..., i] = (m[i, 0] * x + m[i, 1] * y) + (m[i, 2] * z + m[i, 3] * one)
+    return out
+
+
+def _is_identity(m: np.ndarray) -> bool:
+    return bool(np.array_equal(m, np.eye(4, dtype=m.dtype)))
+
+
+@_reg("scene::default")
+class SceneDefault(Component):
+    def construct(self, prop):
+        self._accel = _resolve(prop["accel"]) if prop.get("accel") is not None else None
+        self._h = None
+        self._flat = None
+        self.reset()
+
+    def _release(self):
+        if getattr(self, "_h", None):
+            N.lib().lmgpu_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self._release()
+        except Exception:
+            pass
+
+    # -- graph (scene.cpp:54-230) --------------------------------------------------------------
+    def reset(self) -> None:
+        self._release()
+        self._flat = None
+        self.nodes: list[dict] = [{"type": "group", "children": [], "transform": None, "instanced": False}]
+        self._camera: int | None = None
+        self._env: int | None = None
+
+    def root_node(self) -> int:
+        return 0
+
+    def num_nodes(self) -> int:
+        return len(self.nodes)
+
+    def create_primitive_node(self, prop: dict | None = None, **kw) -> int:
+        p = dict(prop or {})
+        p.update(kw)
+        mesh = _resolve(p.get("mesh"))
+        material = _resolve(p.get("material"))
+        light = _resolve(p.get("light"))
+        camera = _resolve(p.get("camera"))
+        if "medium" in p:
+            raise LmGpuError(2, "media are not supported on the GPU path")
+        if not any([mesh, material, light, camera]):
+            raise LmGpuError(1, "Invalid primitive node. Given assets are invalid.")
+        if camera is not None and light is not None:
+            raise LmGpuError(1, "Primitive cannot be both camera and light.")
+        if (mesh is None) != (material is None):
+            raise LmGpuError(1, "You must specify both mesh and material.")
+        idx = len(self.nodes)
+        if camera is not None:
+            self._camera = idx
+        if light is not None and isinstance(light, (LightEnvConst, LightEnv)):
+            if self._env is not None:
+                raise LmGpuError(1, "Environment light is already registered. You can register only one environment light in the scene.")
+            self._env = idx
+        self.nodes.append({"type": "primitive", "mesh": mesh, "material": material, "light": light, "camera": camera})
+        return idx
+
+    def create_group_node(self, transform) -> int:
+        self.nodes.append({"type": "group", "children": [], "transform": np.asarray(transform, dtype=np.float64),
+                           "instanced": False})
+        return len(self.nodes) - 1
+
+    def create_instance_group_node(self) -> int:
+        self.nodes.append({"type": "group", "children": [], "transform": None, "instanced": True})
+        return len(self.nodes) - 1
+
+    def add_child(self, parent: int, child: int) -> None:
+        if parent < 0 or parent >= len(self.nodes) or self.nodes[parent]["type"] != "group":
+            return
+        self.nodes[parent]["children"].append(child)
+
+    def add_primitive(self, prop: dict | None = None, **kw) -> None:
+        self.add_transformed_primitive(np.eye(4), prop, **kw)
+
+    def add_transformed_primitive(self, transform, prop: dict | None = None, **kw) -> None:
+        p = dict(prop or {})
+        p.update(kw)
+        if "model" in p:
+            raise LmGpuError(2, "model assets are not supported on the GPU path")
+        t = self.create_group_node(transform)
+        self.add_child(t, self.create_primitive_node(p))
+        self.add_child(0, t)
+
+    def traverse_primitive_nodes(self, fn) -> None:
+        """Depth-first traversal with fp32 global transforms (scene.cpp:216-230)."""
+        def visit(i: int, m: np.ndarray):
+            n = self.nodes[i]
+            fn(i, n, m)
+            if n["type"] == "group":
+                mm = _f32_matmul(m, n["transform"]) if n["transform"] is not None else m
+                for c in n["children"]:
+                    visit(c, mm)
+        visit(0, np.eye(4, dtype=np.float32))
+
+    def camera_node(self) -> int:
+        return -1 if self._camera is None else self._camera
+
+    def env_light_node(self) -> int:
+        return -1 if self._env is None else self._env
+
+    def num_lights(self) -> int:
+        return sum(1 for n in self.nodes if n["type"] == "primitive" and n["light"] is not None)
+
+    def accel(self):
+        return self._accel
+
+    def set_accel(self, loc) -> None:
+        self._accel = _resolve(loc)
+
+    # -- flatten + build (scene.cpp:274-317, accel_sahbvh.cpp:132-151) ------------------------
+    def _flatten(self) -> dict:
+        pos, nrm, gns, tri_prim = [], [], [], []
+        prim_mat, prim_light, prim_node = [], [], []
+        mats: list[_Material] = []
+        lights: list[tuple] = []        # (light component, global transform, node index)
+        light_index_of_node: dict[int, int] = {}
+
+        def collect_lights(i, n, m):
+            if n["type"] == "primitive" and n["light"] is not None:
+                light_index_of_node[i] = len(lights)
+                lights.append((n["light"], m, i))
+        self.traverse_primitive_nodes(collect_lights)
+
+        def collect_geometry(i, n, m):
+            if n["type"] != "primitive" or n["mesh"] is None:
+                return
+            mesh = n["mesh"]
+            tp = mesh.tri_positions()
+            tn = mesh.tri_normals()
+            ident = _is_identity(m)
+            if ident:
+                wp = tp.astype(np.float32)
+                wn = tn.astype(np.float32)
+                nm = np.eye(3, dtype=np.float32)
+            else:
+                wp = _f32_xform(m, tp)
+                nm = np.linalg.inv(m.astype(np.float64)).T[:3, :3].astype(np.float32)
+                wn = (tn @ nm.T).astype(np.float32)
+            lp = tp.astype(np.float32)
+            g = np.cross(lp[:, 1] - lp[:, 0], lp[:, 2] - lp[:, 0]).astype(np.float32)
+            g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
+            if not ident:
+                g = (g @ nm.T).astype(np.float32)
+                g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
+            mat = n["material"]
+            if mat not in mats:
+                mats.append(mat)
+            pi = len(prim_mat)
+            prim_mat.append(mats.index(mat))
+            prim_light.append(light_index_of_node.get(i, -1))
+            prim_node.append(i)
+            pos.append(wp.reshape(-1, 9))
+            nrm.append(wn.reshape(-1, 9))
+            gns.append(g.reshape(-1, 3))
+            tri_prim.append(np.full(tp.shape[0], pi, dtype=np.int32))
+        self.traverse_primitive_nodes(collect_geometry)
+
+        if pos:
+            positions = np.ascontiguousarray(np.concatenate(pos), dtype=np.float32)
+            normals = np.ascontiguousarray(np.concatenate(nrm), dtype=np.float32)
+            geo = np.ascontiguousarray(np.concatenate(gns), dtype=np.float32)
+            tprim = np.ascontiguousarray(np.concatenate(tri_prim), dtype=np.int32)
+        else:
+            positions = np.zeros((0, 9), np.float32)
+            normals = np.zeros((0, 9), np.float32)
+            geo = np.zeros((0, 3), np.float32)
+            tprim = np.zeros(0, np.int32)
+
+        # lights (light_area.cpp:68-80; light_env.cpp:55-72)
+        nl = []
+        ltp, ltg, lta = [], [], []
+        env_tex = []
+        env_off = 0
+        ltri_off = 0
+        for comp_, m, node in lights:
+            L = N.Light()
+            if isinstance(comp_, LightArea):
+                L.type = 0
+                L.ke[:] = [float(x) for x in comp_.Ke]
+                lm_ = comp_.mesh
+                lp = lm_.tri_positions().astype(np.float32)
+                cr = np.cross((lp[:, 1] - lp[:, 0]).astype(np.float64), (lp[:, 2] - lp[:, 0]).astype(np.float64))
+                area = 0.5 * np.sqrt(np.sum(cr * cr, axis=1))
+                gl = cr / np.linalg.norm(cr, axis=1, keepdims=True)
+                if _is_identity(m):
+                    wp = lp
+                    gw = gl
+                    J = 1.0
+                else:
+                    wp = _f32_xform(m, lp)
+                    nm = np.linalg.inv(m.astype(np.float64)).T[:3, :3]
+                    gw = gl @ nm.T
+                    gw = gw / np.linalg.norm(gw, axis=1, keepdims=True)
+                    J = abs(float(np.linalg.det(m.astype(np.float64)[:3, :3])))
+                L.tri_offset = ltri_off
+                L.tri_count = lp.shape[0]
+                L.transform_j = J
+                ltri_off += lp.shape[0]
+                ltp.append(np.asarray(wp, np.float32).reshape(-1, 9))
+                ltg.append(np.asarray(gw, np.float32).reshape(-1, 3))
+                lta.append(np.asarray(area, np.float32))
+            elif isinstance(comp_, LightEnvConst):
+                L.type = 1
+                L.ke[:] = [float(x) for x in comp_.Le]
+            elif isinstance(comp_, LightEnv):
+                L.type = 2
+                L.env_w, L.env_h = comp_.data.shape[1], comp_.data.shape[0]
+                L.env_offset = env_off
+                L.rot_deg = comp_.rot
+                L.scale = comp_.scale
+                env_tex.append(comp_.data.reshape(-1).astype(np.float32))
+                env_off += comp_.data.size
+            else:
+                raise LmGpuError(2, f"Unsupported light {comp_!r}")
+            nl.append(L)
+        return {
+            "positions": positions, "normals": normals, "geo_normals": geo, "tri_prim": tprim,
+            "prim_material": np.asarray(prim_mat, np.int32), "prim_light": np.asarray(prim_light, np.int32),
+            "prim_node": np.asarray(prim_node, np.int32), "materials": mats, "lights": nl,
+            "light_tri_p": np.concatenate(ltp) if ltp else np.zeros((0, 9), np.float32),
+            "light_tri_gn": np.concatenate(ltg) if ltg else np.zeros((0, 3), np.float32),
+            "light_tri_area": np.concatenate(lta) if lta else np.zeros(0, np.float32),
+            "env_texels": np.concatenate(env_tex) if env_tex else np.zeros(0, np.float32),
+        }
+
+    def build(self) -> None:
+        """Scene::build: flattens the graph, builds the accel and uploads shading data."""
+        if self._accel is None:
+            raise LmGpuError(2, "Missing acceleration structure.")
+        self._release()
+        flat = self._flatten()
+        if flat["positions"].shape[0] == 0:
+            raise LmGpuError(2, "Missing primitives. Use lm::primitive() function to add primitives.")
+        self._accel.build_triangles(flat["positions"])
+        d = N.SceneDesc()
+        keep = []
+
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a
+        d.num_tris = flat["positions"].shape[0]
+        d.positions = N.fptr(arr(flat["positions"], np.float32))
+        d.normals = N.fptr(arr(flat["normals"], np.float32))
+        d.geo_normals = N.fptr(arr(flat["geo_normals"], np.float32))
+        d.tri_prim = N.iptr(arr(flat["tri_prim"], np.int32))
+        d.num_prims = len(flat["prim_material"])
+        d.prim_material = N.iptr(arr(flat["prim_material"], np.int32))
+        d.prim_light = N.iptr(arr(flat["prim_light"], np.int32))
+        mats = (N.Material * max(1, len(flat["materials"])))(*[m.native() for m in flat["materials"]])
+        d.num_materials = len(flat["materials"])
+        d.materials = C.cast(mats, C.POINTER(N.Material))
+        lights = (N.Light * max(1, len(flat["lights"])))(*flat["lights"])
+        d.num_lights = len(flat["lights"])
+        d.lights = C.cast(lights, C.POINTER(N.Light))
+        d.num_light_tris = flat["light_tri_p"].shape[0]
+        d.light_tri_p = N.fptr(arr(flat["light_tri_p"], np.float32))
+        d.light_tri_gn = N.fptr(arr(flat["light_tri_gn"], np.float32))
+        d.light_tri_area = N.fptr(arr(flat["light_tri_area"], np.float32))
+        d.num_env_texels = flat["env_texels"].size
+        d.env_texels = N.fptr(arr(flat["env_texels"], np.float32))
+        if self._camera is not None:
+            cam = self.nodes[self._camera]["camera"]
+            d.has_camera = 1
+            d.camera.position[:] = [float(x) for x in cam.position]
+            d.camera.center[:] = [float(x) for x in cam.center]
+            d.camera.up[:] = [float(x) for x in cam.up]
+            d.camera.vfov = cam.vfov
+            d.camera.aspect = cam.aspect
+        h = C.c_void_p()
+        N.check(N.lib().lmgpu_scene_create(C.byref(h), self._accel._h, C.byref(d)))
+        self._h = h
+        self._flat = flat
+
+    def flattened(self) -> dict:
+        if self._flat is None:
+            raise LmGpuError(3, "scene is not built")
+        return self._flat
+
+    # -- requirements (scene.h:247-300) -----------------------------------------------------------
+    def require_primitive(self):
+        if len(self.nodes) <= 1:
+            raise LmGpuError(2, "Missing primitives. Use lm::primitive() function to add primitives.")
+
+    def require_camera(self):
+        if self._camera is None:
+            raise LmGpuError(2, "Missing camera primitive. Use lm::primitive() function to add camera primitive.")
+
+    def require_light(self):
+        if self.num_lights() == 0:
+            raise LmGpuError(2, "No light in the scene. Add at least one light sources to the scene.")
+
+    def require_accel(self):
+        if self._accel is None:
+            raise LmGpuError(2, "Missing acceleration structure. Use lm::build() function before rendering.")
+
+    def require_renderable(self):
+        self.require_primitive()
+        self.require_camera()
+        self.require_light()
+        self.require_accel()
+
+    def _require_built(self):
+        if self._h is None:
+            raise LmGpuError(3, "Scene is not built. Call scene.build() before rendering.")
+
+
+# ---------------------------------------------------------------------------------------------
+# Renderers
+
+_SAMPLING = {"naive": 0, "nee": 1, "mis": 2}
+_PRIMARY = {"pixel": 0, "image": 1}
+
+
+@_reg("renderer::raycast", "renderer::raycast_gpu")
+class RendererRaycast(Component):
+    """renderer::raycast (src/renderer/renderer_raycast.cpp:48-101)."""
+
+    def construct(self, prop):
+        self.scene = _resolve(_req(prop, "scene"))
+        self.film = _resolve(_req(prop, "output"))
+        self.params = N.RaycastParams()
+        self.params.bg_color[:] = [float(x) for x in _vec3(prop.get("bg_color", [0, 0, 0]))]
+        self.params.use_constant_color = int(bool(prop.get("use_constant_color", False)))
+        self.params.visualize_normal = int(bool(prop.get("visualize_normal", False)))
+        if prop.get("color") is not None:
+            self.params.has_color = 1
+            self.params.color[:] = [float(x) for x in _vec3(prop["color"])]
+
+    def render(self) -> dict:
+        self.scene.require_primitive()
+        self.scene.require_accel()
+        self.scene.require_camera()
+        self.scene._require_built()
+        t0 = time.perf_counter()
+        N.check(N.lib().lmgpu_render_raycast(self.scene._h, self.film._h, C.byref(self.params), None))
+        return {"elapsed": time.perf_counter() - t0}
+
+
+@_reg("renderer::pt", "renderer::pt_gpu")
+class RendererPT(Component):
+    """renderer::pt (src/renderer/renderer_pt.cpp:51-315) as a wavefront on the GPU.
+
+    Props as the reference: scene, output, max_verts, seed, sampling_mode (naive|nee|mis),
+    primary_ray_sampling_mode (pixel|image), scheduler ('sample' with spp; 'time' with
+    render_time renders progressively in rounds of `spp_per_round` until the time is spent).
+    GPU extras: wave_paths (paths in flight per wave)."""
+
+    def construct(self, prop):
+        self.scene = _resolve(_req(prop, "scene"))
+        self.film = _resolve(_req(prop, "output"))
+        self.max_verts = int(_req(prop, "max_verts"))
+        seed = prop.get("seed")
+        self.seed = int(seed) if seed is not None else int(time.time_ns() & 0xFFFFFFFF)
+        sm = prop.get("sampling_mode", "mis")
+        if sm not in _SAMPLING:
+            raise LmGpuError(1, f"Invalid sampling_mode '{sm}'")
+        self.sampling_mode = _SAMPLING[sm]
+        pm = prop.get("primary_ray_sampling_mode", "pixel")
+        if pm not in _PRIMARY:
+            raise LmGpuError(1, f"Invalid primary_ray_sampling_mode '{pm}'")
+        self.primary_mode = _PRIMARY[pm]
+        self.scheduler = _req(prop, "scheduler")
+        if self.scheduler == "sample":
+            self.spp = int(_req(prop, "spp"))
+        elif self.scheduler == "time":
+            self.render_time = float(_req(prop, "render_time"))
+            self.spp_per_round = int(prop.get("spp_per_round", 1))
+        else:
+            raise LmGpuError(1, f"Invalid scheduler '{self.scheduler}'")
+        self.wave_paths = int(prop.get("wave_paths", 0))
+        self.last_stats: dict = {}
+
+    def _params(self, spp: int, accumulate: bool, seed: int) -> N.PTParams:
+        p = N.PTParams()
+        p.spp = spp
+        p.max_verts = self.max_verts
+        p.seed = seed & 0xFFFFFFFF
+        p.sampling_mode = self.sampling_mode
+        p.primary_mode = self.primary_mode
+        p.wave_paths = self.wave_paths
+        p.accumulate = int(accumulate)
+        return p
+
+    def render(self) -> dict:
+        self.scene.require_renderable()
+        self.scene._require_built()
+        t0 = time.perf_counter()
+        st = N.RenderStats()
+        if self.scheduler == "sample":
+            N.check(N.lib().lmgpu_render_pt(self.scene._h, self.film._h, C.byref(self._params(self.spp, False, self.seed)),
+                                            None, C.byref(st)))
+            processed = self.spp
+            rays, dev_ms = st.rays, st.elapsed_ms
+        else:
+            processed, rays, dev_ms, k = 0, 0, 0.0, 0
+            while True:
+                N.check(N.lib().lmgpu_render_pt(self.scene._h, self.film._h,
+                                                C.byref(self._params(self.spp_per_round, k > 0, self.seed + 7919 * k)),
+                                                None, C.byref(st)))
+                processed += self.spp_per_round
+                rays += st.rays
+                dev_ms += st.elapsed_ms
+                k += 1
+                if time.perf_counter() - t0 >= self.render_time:
+                    break
+        elapsed = time.perf_counter() - t0
+        self.last_stats = {"rays": rays, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
+                           "device_ms": dev_ms, "trace_ms": st.trace_ms}
+        return {"processed": processed, "elapsed": elapsed, "rays": rays,
+                "Mrays_per_s": rays / max(dev_ms, 1e-9) / 1e3}

@@ -1,0 +1,1056 @@
+// Oracle (test infrastructure only): CPU restatement of Lightmetrica v3's rendering hot path.
+//
+// Used by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker for
+// the CUDA path; never shipped, never measured as the product. Parity is not pinned to golden
+// vectors from the reference: the reference holds none for this path and cannot be built here
+// (glm, nlohmann_json, cereal, stb are absent). It is pinned instead by analytic known-answer
+// cases (tests/test_oracle_kat.py) and by following these files line by line:
+//   src/accel/accel_sahbvh.cpp            -> Accel (build, intersect)
+//   src/scene.cpp, include/lm/scene.h     -> Scene (graph, lights, intersect, visible)
+//   include/lm/surface.h, include/lm/path.h -> PointGeometry, path:: functions
+//   src/mesh/mesh_raw.cpp                 -> Mesh
+//   src/camera/camera_pinhole.cpp         -> Camera
+//   src/material/material_{diffuse,glossy,glass,mirror}.cpp -> Material
+//   src/light/light_{area,envconst,env}.cpp, src/texture/texture_bitmap.cpp -> Light
+//   src/renderer/renderer_{raycast,pt}.cpp, src/scheduler.cpp, src/parallel/parallel_openmp.cpp
+//   src/film/film_bitmap.cpp, include/lm/film.h -> Film
+// Templated on Float: double is the faithful mode (the reference's Float), float is the fp32
+// parity mode that the GPU is compared with bit-exactly.
+#pragma once
+#include "lmo_math.hpp"
+#include "lmo_philox.hpp"
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
+#include <numeric>
+#include <optional>
+#include <queue>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <omp.h>
+
+namespace lmo {
+
+// ------------------------------------------------------------------------------------------------
+// include/lm/surface.h:52-196 (PointGeometry)
+template <typename F> struct PointGeometry {
+    bool degenerated = false;
+    bool infinite = false;
+    V3<F> p, n, gn, wo;
+    V2<F> t;
+    V3<F> u, v;
+    M3<F> to_world, to_local;
+
+    static PointGeometry make_degenerated(V3<F> p) {
+        PointGeometry g; g.degenerated = true; g.infinite = false; g.p = p; return g;
+    }
+    static PointGeometry make_infinite(V3<F> wo) {
+        PointGeometry g; g.degenerated = false; g.infinite = true; g.wo = wo; return g;
+    }
+    static PointGeometry make_on_surface(V3<F> p, V3<F> n, V3<F> gn, V2<F> t) {
+        PointGeometry g;
+        g.degenerated = false; g.infinite = false;
+        g.p = p; g.n = n; g.gn = gn; g.t = t;
+        orthonormal_basis(n, g.u, g.v);
+        g.to_world = M3<F>(g.u, g.v, g.n);
+        g.to_local = transpose(g.to_world);
+        return g;
+    }
+    static PointGeometry make_on_surface(V3<F> p, V3<F> gn) { return make_on_surface(p, gn, gn, {}); }
+    bool opposite(V3<F> w1, V3<F> w2) const { return dot(w1, n) * dot(w2, n) <= F(0); }
+    void basis_twosided(V3<F> wi, V3<F>& on, V3<F>& ou, V3<F>& ov) const {
+        const bool i = dot(wi, n) > F(0);
+        on = i ? n : -n; ou = u; ov = i ? v : -v;
+    }
+};
+
+// include/lm/surface.h:211-297
+enum SIType { SI_None = 0, SI_Camera = 1, SI_Light = 2, SI_Surface = 4 };
+template <typename F> struct SceneInteraction {
+    int type = SI_None;
+    int primitive = -1;
+    PointGeometry<F> geom;
+    bool is_type(int f) const { return (type & f) > 0; }
+    SceneInteraction as_type(int t) const { auto s = *this; s.type = t; return s; }
+};
+
+enum class TransDir { LE, EL };
+
+// include/lm/surface.h:329-363
+template <typename F> F geometry_term(const PointGeometry<F>& s1, const PointGeometry<F>& s2) {
+    if (s1.infinite && s2.infinite) return F(0);
+    V3<F> d; F L2;
+    if (s1.infinite || s2.infinite) {
+        d = s1.infinite ? s1.wo : -s2.wo;
+        L2 = F(1);
+    } else {
+        d = s2.p - s1.p;
+        L2 = dot(d, d);
+        d = d / std::sqrt(L2);
+    }
+    const auto cos1 = s1.degenerated || s1.infinite ? F(1) : std::abs(dot(s1.n, d));
+    const auto cos2 = s2.degenerated || s2.infinite ? F(1) : std::abs(dot(s2.n, -d));
+    return cos1 * cos2 / L2;
+}
+// include/lm/surface.h:377-390
+template <typename F> F convert_pdf_SA_to_projSA(F pdf_SA, const PointGeometry<F>& g, V3<F> d) {
+    if (g.degenerated) return pdf_SA;
+    const auto J = std::abs(dot(g.n, d));
+    if (J == F(0)) return F(0);
+    return pdf_SA / J;
+}
+// include/lm/surface.h:424-438
+template <typename F> F shading_normal_correction(const PointGeometry<F>& g, V3<F> wi, V3<F> wo, TransDir td) {
+    const auto local_wi = g.to_local * wi;
+    const auto local_wo = g.to_local * wo;
+    const auto wi_dot_ng = dot(wi, g.gn);
+    const auto wo_dot_ng = dot(wo, g.gn);
+    const auto wi_dot_ns = local_wi.z;
+    const auto wo_dot_ns = local_wo.z;
+    if (wi_dot_ng * wi_dot_ns <= F(0) || wo_dot_ng * wo_dot_ns <= F(0)) return F(0);
+    if (td == TransDir::LE) return wi_dot_ns * wo_dot_ng / (wo_dot_ns * wi_dot_ng);
+    return F(1);
+}
+
+// ------------------------------------------------------------------------------------------------
+// src/mesh/mesh_raw.cpp:37-104
+template <typename F> struct Mesh {
+    struct FI { int p, t, n; };
+    std::vector<V3<F>> ps, ns;
+    std::vector<V2<F>> ts;
+    std::vector<FI> fs;
+    struct Point { V3<F> p, n; V2<F> t; };
+    struct Tri { Point p1, p2, p3; };
+    struct InterpolatedPoint { V3<F> p, n, gn; V2<F> t; };
+    int num_triangles() const { return int(fs.size()) / 3; }
+    Tri triangle_at(int face) const {
+        const auto f1 = fs[3 * face], f2 = fs[3 * face + 1], f3 = fs[3 * face + 2];
+        return {{ps[f1.p], ns[f1.n], ts[f1.t]}, {ps[f2.p], ns[f2.n], ts[f2.t]}, {ps[f3.p], ns[f3.n], ts[f3.t]}};
+    }
+    InterpolatedPoint surface_point(int face, V2<F> uv) const {
+        const auto i1 = fs[3 * face], i2 = fs[3 * face + 1], i3 = fs[3 * face + 2];
+        return {mix_barycentric(ps[i1.p], ps[i2.p], ps[i3.p], uv),
+                normalize(mix_barycentric(ns[i1.n], ns[i2.n], ns[i3.n], uv)),
+                geometry_normal(ps[i1.p], ps[i2.p], ps[i3.p]),
+                V2<F>()};
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// src/camera/camera_pinhole.cpp:48-238
+template <typename F> struct Camera {
+    V3<F> position, center, up, u, v, w;
+    F vfov = 0, tf = 0, aspect = 1;
+    void construct(V3<F> pos, V3<F> ctr, V3<F> up_, F vfov_, F aspect_) {
+        position = pos; center = ctr; up = up_;
+        w = normalize(position - center);
+        u = normalize(cross(up, w));
+        v = cross(w, u);
+        vfov = vfov_;
+        tf = std::tan(vfov * C<F>::Pi / F(180) * F(.5));
+        aspect = aspect_;
+    }
+    F J(V3<F> wo) const {
+        const auto V = transpose(M3<F>(u, v, w));
+        const auto wo_eye = V * wo;
+        const F cos_theta = -wo_eye.z;
+        const F inv_cos_theta = F(1) / cos_theta;
+        const F A = tf * tf * aspect * F(4);
+        return inv_cos_theta * inv_cos_theta * inv_cos_theta / A;
+    }
+    Ray<F> primary_ray(V2<F> rp) const {
+        rp = V2<F>(F(2) * rp.x - F(1), F(2) * rp.y - F(1));
+        const auto d = normalize(V3<F>(aspect * tf * rp.x, tf * rp.y, F(-1)));
+        return {position, u * d.x + v * d.y + w * d.z};
+    }
+    std::optional<V2<F>> raster_position(V3<F> wo) const {
+        const auto to_eye = transpose(M3<F>(u, v, w));
+        const auto wo_eye = to_eye * wo;
+        if (wo_eye.z >= 0) return {};
+        const auto rp = V2<F>(-wo_eye.x / wo_eye.z / tf / aspect, -wo_eye.y / wo_eye.z / tf) * F(.5);
+        const auto rq = V2<F>(rp.x + F(.5), rp.y + F(.5));
+        if (rq.x < F(0) || rq.x > F(1) || rq.y < F(0) || rq.y > F(1)) return {};
+        return rq;
+    }
+    F pdf_direction(V3<F> wo) const {
+        if (!raster_position(wo)) return F(0);
+        return J(wo);
+    }
+    V3<F> eval(V3<F> wo) const {
+        if (!raster_position(wo)) return V3<F>(F(0));
+        return V3<F>(J(wo));
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// Materials: src/material/material_{diffuse,glossy,glass,mirror}.cpp
+enum MatType { MAT_DIFFUSE = 0, MAT_GLOSSY = 1, MAT_GLASS = 2, MAT_MIRROR = 3 };
+
+template <typename F> struct DirectionSample { V3<F> wo; V3<F> weight; };
+template <typename F> struct ComponentSample { int comp; F weight; };
+
+template <typename F> struct Material {
+    int type = MAT_DIFFUSE;
+    V3<F> Kd = V3<F>(F(1)), Ks;
+    F ax = 0, ay = 0, Ni = 1;
+
+    // material_glossy.cpp:43-59
+    F normal_dist(V3<F> wh, V3<F> u, V3<F> v, V3<F> n) const {
+        return F(1) / (C<F>::Pi * ax * ay * sq(sq(dot(wh, u) / ax) + sq(dot(wh, v) / ay) + sq(dot(wh, n))));
+    }
+    F shadowG(V3<F> wi, V3<F> wo, V3<F> u, V3<F> v, V3<F> n) const {
+        auto G1 = [&](V3<F> w) {
+            const auto c = dot(w, n);
+            const auto s = std::max(C<F>::Eps, safe_sqrt(F(1) - c * c));
+            const auto cp = dot(w, u) / s;
+            const auto cs = dot(w, v) / s;
+            const auto a2 = sq(cp * ax) + sq(cs * ay);
+            return c == F(0) ? F(0) : F(2) / (F(1) + safe_sqrt(F(1) + a2 * sq(s / c)));
+        };
+        return G1(wi) * G1(wo);
+    }
+    // material_glass.cpp:84-98
+    F fresnel(V3<F> wi, V3<F> wt, const PointGeometry<F>& g) const {
+        const bool in = dot(wi, g.n) > F(0);
+        const auto cos = in ? dot(wi, g.n) : dot(wt, g.n);
+        const auto r = (F(1) - Ni) / (F(1) + Ni);
+        const auto r2 = r * r;
+        return r2 + (F(1) - r2) * std::pow(F(1) - cos, F(5));
+    }
+    void glass_refr(const PointGeometry<F>& g, V3<F> wi, V3<F>& wt, bool& total, F& eta, F& Fr) const {
+        const bool in = dot(wi, g.n) > F(0);
+        const auto n = in ? g.n : -g.n;
+        eta = in ? F(1) / Ni : Ni;
+        const auto rr = refraction(wi, n, eta);
+        wt = rr.wt; total = rr.total;
+        Fr = total ? F(1) : fresnel(wi, wt, g);
+    }
+
+    bool is_specular_component(int) const { return type == MAT_GLASS || type == MAT_MIRROR; }
+
+    ComponentSample<F> sample_component(V2<F> uc, const PointGeometry<F>& g, V3<F> wi) const {
+        if (type == MAT_GLASS) {  // material_glass.cpp:123-143 (component sampling on)
+            V3<F> wt; bool total; F eta, Fr;
+            glass_refr(g, wi, wt, total, eta, Fr);
+            const int comp = uc.x < Fr ? 0 : 1;
+            const auto pdf = comp == 0 ? Fr : F(1) - Fr;
+            return {comp, F(1) / pdf};
+        }
+        return {0, F(1)};
+    }
+
+    std::optional<DirectionSample<F>> sample_direction(V2<F> ud, V2<F> /*udc*/, const PointGeometry<F>& g, V3<F> wi, int comp, TransDir td) const {
+        switch (type) {
+        case MAT_DIFFUSE: {  // material_diffuse.cpp:63-71
+            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+            const auto d = sample_cosine_weighted(ud);
+            return DirectionSample<F>{u * d.x + v * d.y + n * d.z, Kd};
+        }
+        case MAT_GLOSSY: {  // material_glossy.cpp:70-86
+            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+            const auto u1 = ud.x * F(2) * C<F>::Pi;
+            const auto u2 = ud.y;
+            const auto wh = normalize(safe_sqrt(u2 / (F(1) - u2)) * (ax * std::cos(u1) * u + ay * std::sin(u1) * v) + n);
+            const auto wo = reflection(wi, wh);
+            if (g.opposite(wi, wo)) return {};
+            const auto f = eval(g, wi, wo, 0, td, false);
+            const auto p = pdf_direction(g, wi, wo, 0, false);
+            return DirectionSample<F>{wo, f / p};
+        }
+        case MAT_GLASS: {  // material_glass.cpp:163-188
+            if (comp == 0) {
+                const auto wo = reflection(wi, g.n);
+                const auto f = eval(g, wi, wo, comp, td, false);
+                const auto p = pdf_direction(g, wi, wo, comp, false);
+                return DirectionSample<F>{wo, f / p};
+            } else {
+                V3<F> wt; bool total; F eta, Fr;
+                glass_refr(g, wi, wt, total, eta, Fr);
+                const auto wo = wt;
+                const auto f = eval(g, wi, wo, comp, td, false);
+                const auto p = pdf_direction(g, wi, wo, comp, false);
+                return DirectionSample<F>{wo, f / p};
+            }
+        }
+        case MAT_MIRROR:  // material_mirror.cpp:40-45
+            return DirectionSample<F>{reflection(wi, g.n), V3<F>(F(1))};
+        }
+        return {};
+    }
+
+    F pdf_direction(const PointGeometry<F>& g, V3<F> wi, V3<F> wo, int, bool eval_delta) const {
+        switch (type) {
+        case MAT_DIFFUSE: return g.opposite(wi, wo) ? F(0) : F(1) / C<F>::Pi;
+        case MAT_GLOSSY: {
+            if (g.opposite(wi, wo)) return F(0);
+            const auto wh = normalize(wi + wo);
+            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+            return normal_dist(wh, u, v, n) * dot(wh, n) / (F(4) * dot(wo, wh) * dot(wo, n));
+        }
+        case MAT_GLASS: return eval_delta ? F(0) : F(1);
+        case MAT_MIRROR: return eval_delta ? F(0) : F(1);
+        }
+        return F(0);
+    }
+
+    V3<F> eval(const PointGeometry<F>& g, V3<F> wi, V3<F> wo, int comp, TransDir td, bool eval_delta) const {
+        switch (type) {
+        case MAT_DIFFUSE:
+            if (g.opposite(wi, wo)) return V3<F>();
+            return Kd / C<F>::Pi;
+        case MAT_GLOSSY: {
+            if (g.opposite(wi, wo)) return V3<F>();
+            const auto wh = normalize(wi + wo);
+            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+            const auto one_m = V3<F>(F(1)) - Ks;
+            const auto Fr = Ks + one_m * std::pow(F(1) - dot(wo, wh), F(5));
+            return Ks * Fr * (normal_dist(wh, u, v, n) * shadowG(wi, wo, u, v, n) / (F(4) * dot(wi, n) * dot(wo, n)));
+        }
+        case MAT_GLASS: {
+            if (eval_delta) return V3<F>(F(0));
+            V3<F> wt; bool total; F eta, Fr;
+            glass_refr(g, wi, wt, total, eta, Fr);
+            if (comp == 0) return V3<F>(Fr);
+            const auto refr_corr = td == TransDir::EL ? eta * eta : F(1);
+            return V3<F>((F(1) - Fr) * refr_corr);
+        }
+        case MAT_MIRROR:
+            return eval_delta ? V3<F>(F(0)) : V3<F>(F(1));
+        }
+        return V3<F>();
+    }
+
+    std::optional<V3<F>> reflectance() const {
+        switch (type) {
+        case MAT_DIFFUSE: return Kd;
+        case MAT_GLOSSY: return Ks;
+        default: return V3<F>(F(0));
+        }
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// Lights: src/light/light_area.cpp, light_envconst.cpp, light_env.cpp
+enum LightType { LIGHT_AREA = 0, LIGHT_ENVCONST = 1, LIGHT_ENV = 2 };
+
+template <typename F> struct LightSample { PointGeometry<F> geom; V3<F> wo; V3<F> weight; };
+
+template <typename F> struct Light {
+    int type = LIGHT_AREA;
+    V3<F> Ke;            // area: Ke; envconst: Le
+    int mesh = -1;       // area
+    Dist<F> dist;        // area: triangle-area CDF
+    F invA = 0;          // area
+    // env
+    int tw = 0, th = 0, tc = 3;
+    std::vector<float> texels;
+    F rot = 0, scale = 1;
+    Dist2<F> dist2;
+
+    bool is_env() const { return type != LIGHT_AREA; }
+    bool is_infinite() const { return type != LIGHT_AREA; }
+
+    // texture_bitmap.cpp:68-75
+    V3<F> tex_eval(V2<F> t) const {
+        const auto u = t.x - std::floor(t.x);
+        const auto v = t.y - std::floor(t.y);
+        const int x = std::clamp(int(u * tw), 0, tw - 1);
+        const int y = std::clamp(int(v * th), 0, th - 1);
+        const int i = tw * y + x;
+        return V3<F>(F(texels[tc * i]), F(texels[tc * i + 1]), F(texels[tc * i + 2]));
+    }
+    // light_env.cpp:55-72
+    void init_env() {
+        std::vector<F> ls(size_t(tw) * th);
+        for (int i = 0; i < tw * th; i++) {
+            const int x = i % tw, y = i / tw;
+            const int k = tw * y + x;
+            const auto v = V3<F>(F(texels[tc * k]), F(texels[tc * k + 1]), F(texels[tc * k + 2])) * scale;
+            ls[i] = comp_max(v) * std::sin(C<F>::Pi * (F(i) / tw + F(.5)) / th);
+        }
+        dist2.init(ls, tw, th);
+    }
+
+    V3<F> eval(const PointGeometry<F>& g, V3<F> wo) const {
+        switch (type) {
+        case LIGHT_AREA: return dot(wo, g.n) <= F(0) ? V3<F>(F(0)) : Ke;
+        case LIGHT_ENVCONST: return Ke;
+        case LIGHT_ENV: {
+            const auto d = -g.wo;
+            auto at = std::atan2(d.x, d.z);
+            at = at < F(0) ? at + F(2) * C<F>::Pi : at;
+            const auto t = (at - rot) * F(.5) / C<F>::Pi;
+            return tex_eval(V2<F>(t - std::floor(t), std::acos(d.y) / C<F>::Pi)) * scale;
+        }
+        }
+        return V3<F>();
+    }
+
+    F pdf_direct(const PointGeometry<F>& g, const PointGeometry<F>& gL, const Transform<F>& tr, V3<F> wo) const {
+        switch (type) {
+        case LIGHT_AREA: {  // light_area.cpp:163-169
+            if (dot(wo, gL.n) <= F(0)) return F(0);
+            const auto G = geometry_term(g, gL);
+            return G == F(0) ? F(0) : (invA / tr.J) / G;
+        }
+        case LIGHT_ENVCONST: {  // light_envconst.cpp:109-112
+            const auto d = -gL.wo;
+            return convert_pdf_SA_to_projSA(pdf_uniform_sphere<F>(), g, d);
+        }
+        case LIGHT_ENV: {  // light_env.cpp:165-181
+            const auto d = -gL.wo;
+            auto at = std::atan2(d.x, d.z);
+            at = at < F(0) ? at + F(2) * C<F>::Pi : at;
+            const auto t = (at - rot) * F(.5) / C<F>::Pi;
+            const auto u = t - std::floor(t);
+            const auto v = std::acos(d.y) / C<F>::Pi;
+            const auto st = safe_sqrt(F(1) - d.y * d.y);
+            if (st == F(0)) return F(0);
+            const auto pdfSA = dist2.pdf(u, v) / (F(2) * C<F>::Pi * C<F>::Pi * st);
+            return convert_pdf_SA_to_projSA(pdfSA, g, d);
+        }
+        }
+        return F(0);
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// include/lm/scenenode.h
+template <typename F> struct SceneNode {
+    bool is_primitive = false;
+    int index = 0;
+    int mesh = -1, material = -1, light = -1, camera = -1;
+    std::vector<int> children;
+    bool instanced = false;
+    std::optional<M4<F>> local;
+};
+
+template <typename F> struct Hit {
+    F t; V2<F> uv; int flattened_node; int primitive; int face; int global_tri;
+};
+
+// ------------------------------------------------------------------------------------------------
+// src/accel/accel_sahbvh.cpp:26-300
+template <typename F> struct Tri {
+    V3<F> p1, e1, e2;
+    Bound<F> b;
+    V3<F> c;
+    int flattened_node = 0, face = 0;
+    Tri() {}
+    Tri(V3<F> p1_, V3<F> p2, V3<F> p3, int fn, int f) : p1(p1_), flattened_node(fn), face(f) {
+        e1 = p2 - p1; e2 = p3 - p1;
+        b = merge(b, p1); b = merge(b, p2); b = merge(b, p3);
+        c = b.center();
+    }
+    struct TriHit { F t, u, v; };
+    // Moller & Trumbore 1997, as accel_sahbvh.cpp:58-75
+    std::optional<TriHit> intersect(const Ray<F>& r, F tl, F th) const {
+        const auto p = cross(r.d, e2);
+        const auto tv = r.o - p1;
+        const auto q = cross(tv, e1);
+        const auto d = dot(e1, p);
+        const auto ad = std::abs(d);
+        const auto s = std::copysign(F(1), d);
+        const auto u = dot(tv, p) * s;
+        const auto v = dot(r.d, q) * s;
+        if (ad < F(1e-8) || u < F(0) || v < F(0) || u + v > ad) return {};
+        const auto t = dot(e2, q) / d;
+        if (t < tl || th < t) return {};
+        return TriHit{t, u / ad, v / ad};
+    }
+};
+
+template <typename F> struct Accel {
+    struct Node { Bound<F> b; bool leaf = false; int s = 0, e = 0, c1 = 0, c2 = 0; };
+    struct Flat { Transform<F> tr; int primitive; };
+    std::vector<Node> nodes;
+    std::vector<Tri<F>> trs;
+    std::vector<int> indices;
+    std::vector<Flat> flat;
+    bool robust = false;  // fp32 parity mode only (see Bound::isect)
+
+    template <typename TraverseFn>
+    void build(TraverseFn traverse_tris, int nthreads) {
+        trs.clear(); flat.clear();
+        traverse_tris(trs, flat);
+        const int nt = int(trs.size());
+        if (nt == 0) { nodes.clear(); indices.clear(); return; }
+        struct Entry { int index, start, end; };
+        std::queue<Entry> q;
+        q.push({0, 0, nt});
+        nodes.assign(size_t(2) * nt - 1, {});
+        indices.assign(nt, 0);
+        std::iota(indices.begin(), indices.end(), 0);
+        std::mutex mu;
+        std::condition_variable cv;
+        std::atomic<int> pr{0};
+        std::atomic<int> nn{1};
+        bool done = false;
+        auto process = [&]() {
+            std::vector<F> l(nt + 1), r(nt + 1);
+            while (true) {
+                Entry en;
+                {
+                    std::unique_lock<std::mutex> lk(mu);
+                    cv.wait(lk, [&]() { return done || !q.empty(); });
+                    if (done) break;
+                    en = q.front(); q.pop();
+                }
+                const int ni = en.index, s = en.start, e = en.end;
+                Node& n = nodes[ni];
+                for (int i = s; i < e; i++) n.b = merge(n.b, trs[indices[i]].b);
+                auto st = [&](int ax) {
+                    std::sort(&indices[s], &indices[e - 1] + 1, [&](int i1, int i2) { return trs[i1].c[ax] < trs[i2].c[ax]; });
+                };
+                auto make_leaf = [&]() {
+                    n.leaf = true; n.s = s; n.e = e;
+                    pr += e - s;
+                    if (pr == nt) {
+                        std::unique_lock<std::mutex> lk(mu);
+                        done = true;
+                        cv.notify_all();
+                    }
+                };
+                if (e - s < 2) { make_leaf(); continue; }
+                F b = C<F>::Inf;
+                int bi = -1, ba = -1;
+                for (int a = 0; a < 3; a++) {
+                    st(a);
+                    Bound<F> bl, br;
+                    for (int i = 0; i <= e - s; i++) {
+                        const int j = e - s - i;
+                        l[i] = bl.surface_area() * F(i);
+                        r[j] = br.surface_area() * F(i);
+                        bl = i < e - s ? merge(bl, trs[indices[s + i]].b) : bl;
+                        br = j > 0 ? merge(br, trs[indices[s + j - 1]].b) : br;
+                    }
+                    for (int i = 1; i < e - s; i++) {
+                        const auto c = F(1) + (l[i] + r[i]) / n.b.surface_area();
+                        if (c < b) { b = c; bi = i; ba = a; }
+                    }
+                }
+                if (b > F(e - s)) { make_leaf(); continue; }
+                st(ba);
+                const int m = s + bi;
+                std::unique_lock<std::mutex> lk(mu);
+                q.push({n.c1 = nn++, s, m});
+                q.push({n.c2 = nn++, m, e});
+                cv.notify_one();
+            }
+        };
+        std::vector<std::thread> ths(std::max(1, nthreads));
+        for (auto& th : ths) th = std::thread(process);
+        for (auto& th : ths) th.join();
+    }
+
+    std::optional<Hit<F>> intersect(const Ray<F>& ray, F tmin, F tmax) const {
+        if (nodes.empty()) return {};
+        std::optional<typename Tri<F>::TriHit> mh, h;
+        int mi = -1;
+        int s[99]{};
+        int si = 0;
+        while (si >= 0) {
+            const auto& n = nodes.at(s[si--]);
+            if (!n.b.isect(ray, tmin, tmax, robust)) continue;
+            if (!n.leaf) {
+                s[++si] = n.c1;
+                s[++si] = n.c2;
+                continue;
+            }
+            for (int i = n.s; i < n.e; i++) {
+                if ((h = trs[indices[i]].intersect(ray, tmin, tmax))) {
+                    mh = h; tmax = h->t; mi = i;
+                }
+            }
+        }
+        if (!mh) return {};
+        const int gi = indices.at(mi);
+        const auto& tr = trs.at(gi);
+        const auto& fn = flat.at(tr.flattened_node);
+        return Hit<F>{tmax, V2<F>(mh->u, mh->v), tr.flattened_node, fn.primitive, tr.face, gi};
+    }
+
+    // Exhaustive closest hit (tests only): the smallest t over every triangle the Moller-Trumbore
+    // test accepts in [tmin, tmax], ties to the smallest flattened triangle index.
+    std::optional<Hit<F>> intersect_brute(const Ray<F>& ray, F tmin, F tmax) const {
+        int best = -1; typename Tri<F>::TriHit bh{};
+        for (int i = 0; i < int(trs.size()); i++) {
+            const auto h = trs[i].intersect(ray, tmin, tmax);
+            if (h && (best < 0 || h->t < bh.t)) { best = i; bh = *h; }
+        }
+        if (best < 0) return {};
+        const auto& tr = trs[best];
+        return Hit<F>{bh.t, V2<F>(bh.u, bh.v), tr.flattened_node, flat[tr.flattened_node].primitive, tr.face, best};
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// src/scene.cpp:20-400 + include/lm/scene.h:343-364
+template <typename F> struct Scene {
+    using Float = F;
+    std::vector<SceneNode<F>> nodes;
+    std::vector<Mesh<F>> meshes;
+    std::vector<Material<F>> materials;
+    std::vector<Light<F>> lights_assets;
+    std::vector<Camera<F>> cameras;
+    std::optional<int> camera_;
+    struct LightPrimitiveIndex { Transform<F> tr; int index; };
+    std::vector<LightPrimitiveIndex> lights_;
+    std::unordered_map<int, int> light_indices_map_;
+    std::optional<int> env_light_;
+    Accel<F> accel;
+    bool built = false;
+
+    Scene() { reset(); }
+    void reset() {
+        nodes.clear(); camera_ = {}; lights_.clear(); light_indices_map_.clear(); env_light_ = {};
+        SceneNode<F> root; root.index = 0; nodes.push_back(root);
+        built = false;
+    }
+    int create_primitive_node(int mesh, int material, int light, int camera) {
+        if (mesh < 0 && material < 0 && light < 0 && camera < 0) throw std::invalid_argument("Invalid primitive node. Given assets are invalid.");
+        if (camera >= 0 && light >= 0) throw std::invalid_argument("Primitive cannot be both camera and light.");
+        if ((mesh < 0 && material >= 0) || (mesh >= 0 && material < 0)) throw std::invalid_argument("You must specify both mesh and material.");
+        const int index = int(nodes.size());
+        if (camera >= 0) camera_ = index;
+        if (light >= 0 && lights_assets.at(light).is_env()) {
+            if (env_light_) throw std::invalid_argument("Environment light is already registered.");
+            env_light_ = index;
+        }
+        SceneNode<F> n; n.is_primitive = true; n.index = index;
+        n.mesh = mesh; n.material = material; n.light = light; n.camera = camera;
+        nodes.push_back(n);
+        return index;
+    }
+    int create_group_node(const M4<F>& m) {
+        SceneNode<F> n; n.index = int(nodes.size()); n.local = m; nodes.push_back(n); return n.index;
+    }
+    int create_instance_group_node() {
+        SceneNode<F> n; n.index = int(nodes.size()); n.instanced = true; nodes.push_back(n); return n.index;
+    }
+    void add_child(int parent, int child) {
+        if (parent < 0 || parent >= int(nodes.size())) return;
+        auto& node = nodes.at(parent);
+        if (node.is_primitive) return;
+        node.children.push_back(child);
+    }
+    void traverse_primitive_nodes(const std::function<void(const SceneNode<F>&, const M4<F>&)>& fn) const {
+        std::function<void(int, M4<F>)> visit = [&](int index, M4<F> gm) {
+            const auto& node = nodes.at(index);
+            fn(node, gm);
+            if (!node.is_primitive) {
+                const auto M = node.local ? gm * *node.local : gm;
+                for (int c : node.children) visit(c, M);
+            }
+        };
+        visit(0, M4<F>());
+    }
+    static V3<F> xform_point(const M4<F>& m, V3<F> p) {
+        const auto r = m * V4<F>(p, F(1));
+        return {r.x, r.y, r.z};
+    }
+
+    void build(int nthreads, bool robust) {
+        light_indices_map_.clear();
+        lights_.clear();
+        traverse_primitive_nodes([&](const SceneNode<F>& node, const M4<F>& gm) {
+            if (node.is_primitive && node.light >= 0) {
+                light_indices_map_[node.index] = int(lights_.size());
+                lights_.push_back({Transform<F>(gm), node.index});
+            }
+        });
+        accel.robust = robust;
+        accel.build([&](std::vector<Tri<F>>& trs, std::vector<typename Accel<F>::Flat>& flat) {
+            traverse_primitive_nodes([&](const SceneNode<F>& node, const M4<F>& gm) {
+                if (!node.is_primitive || node.mesh < 0) return;
+                const int fi = int(flat.size());
+                flat.push_back({Transform<F>(gm), node.index});
+                const auto& mesh = meshes.at(node.mesh);
+                for (int f = 0; f < mesh.num_triangles(); f++) {
+                    const auto tri = mesh.triangle_at(f);
+                    trs.emplace_back(xform_point(gm, tri.p1.p), xform_point(gm, tri.p2.p), xform_point(gm, tri.p3.p), fi, f);
+                }
+            });
+        }, nthreads);
+        built = true;
+    }
+
+    SceneInteraction<F> surface_from_hit(const Hit<F>& h) const {
+        const auto& prim = nodes.at(h.primitive);
+        const auto p = meshes.at(prim.mesh).surface_point(h.face, h.uv);
+        const auto& tr = accel.flat.at(h.flattened_node).tr;
+        SceneInteraction<F> si;
+        si.type = SI_Surface;
+        si.primitive = h.primitive;
+        si.geom = PointGeometry<F>::make_on_surface(xform_point(tr.M, p.p), normalize(tr.normal_M * p.n), normalize(tr.normal_M * p.gn), p.t);
+        return si;
+    }
+
+    std::optional<SceneInteraction<F>> intersect(const Ray<F>& ray, F tmin = C<F>::Eps, F tmax = C<F>::Inf) const {
+        const auto hit = accel.intersect(ray, tmin, tmax);
+        if (!hit) {
+            if (tmax < C<F>::Inf) return {};
+            if (!env_light_) return {};
+            SceneInteraction<F> si;
+            si.type = SI_Light; si.primitive = *env_light_;
+            si.geom = PointGeometry<F>::make_infinite(-ray.d);
+            return si;
+        }
+        return surface_from_hit(*hit);
+    }
+    bool visible(const SceneInteraction<F>& a, const SceneInteraction<F>& b) const {
+        auto vis = [&](const SceneInteraction<F>& s1, const SceneInteraction<F>& s2) {
+            const auto wo = s2.geom.infinite ? -s2.geom.wo : normalize(s2.geom.p - s1.geom.p);
+            const auto tmax = s2.geom.infinite ? C<F>::Inf - F(1) : distance(s1.geom.p, s2.geom.p) * (F(1) - C<F>::Eps);
+            return !intersect(Ray<F>{s1.geom.p, wo}, C<F>::Eps, tmax);
+        };
+        return a.geom.infinite ? vis(b, a) : vis(a, b);
+    }
+    bool is_light(const SceneInteraction<F>& sp) const { return nodes.at(sp.primitive).light >= 0; }
+    int num_lights() const { return int(lights_.size()); }
+    std::pair<int, F> sample_light_selection(F u) const {
+        const int n = int(lights_.size());
+        const int i = std::clamp(int(u * n), 0, n - 1);
+        return {i, F(1) / n};
+    }
+    F pdf_light_selection() const { return F(1) / int(lights_.size()); }
+    const Camera<F>& camera() const { return cameras.at(nodes.at(*camera_).camera); }
+    const Light<F>& light_of(int node) const { return lights_assets.at(nodes.at(node).light); }
+    const Material<F>& material_of(int node) const { return materials.at(nodes.at(node).material); }
+
+    // light_area.cpp:48-60 (position sampling on the light's mesh, transformed)
+    PointGeometry<F> sample_position_on_triangle_mesh(const Light<F>& L, V2<F> up, F upc, const Transform<F>& tr) const {
+        const int i = L.dist.sample(upc);
+        const auto s = safe_sqrt(up.x);
+        const auto tri = meshes.at(L.mesh).triangle_at(i);
+        const auto a = tri.p1.p, b = tri.p2.p, c = tri.p3.p;
+        const auto p = mix_barycentric(a, b, c, V2<F>(F(1) - s, up.y * s));
+        const auto gn = geometry_normal(a, b, c);
+        const auto p_trans = xform_point(tr.M, p);
+        const auto gn_trans = normalize(tr.normal_M * gn);
+        return PointGeometry<F>::make_on_surface(p_trans, gn_trans);
+    }
+
+    // path.h:493-530 sample_direct(LE) with RaySampleU u = {up, upc, ud, udc}
+    std::optional<LightSample<F>> sample_direct_light(const double* u8, const SceneInteraction<F>& sp, int& light_node) const {
+        const V2<F> up{F(u8[0]), F(u8[1])}, upc{F(u8[2]), F(u8[3])}, ud{F(u8[4]), F(u8[5])};
+        const auto [li, p_sel] = sample_light_selection(upc.x);
+        const auto& lpi = lights_.at(li);
+        light_node = lpi.index;
+        const auto& L = light_of(lpi.index);
+        const auto& g = sp.geom;
+        std::optional<LightSample<F>> s;
+        switch (L.type) {
+        case LIGHT_AREA: {  // light_area.cpp:148-161
+            const auto gL = sample_position_on_triangle_mesh(L, up, upc.y, lpi.tr);
+            const auto wo = normalize(g.p - gL.p);
+            const auto pL = L.pdf_direct(g, gL, lpi.tr, wo);
+            if (pL == F(0)) return {};
+            const auto Le = L.eval(gL, wo);
+            s = LightSample<F>{gL, wo, Le / pL};
+            break;
+        }
+        case LIGHT_ENVCONST: {  // light_envconst.cpp:94-107
+            const auto wo = sample_uniform_sphere(ud);
+            const auto gL = PointGeometry<F>::make_infinite(wo);
+            const auto Le = L.eval(gL, wo);
+            const auto pL = L.pdf_direct(g, gL, lpi.tr, wo);
+            if (pL == F(0)) return {};
+            s = LightSample<F>{gL, wo, Le / pL};
+            break;
+        }
+        case LIGHT_ENV: {  // light_env.cpp:146-163
+            const auto uu = L.dist2.sample(ud.x, ud.y, up.x, up.y);
+            const auto t = C<F>::Pi * uu.y;
+            const auto st = std::sin(t);
+            const auto p = F(2) * C<F>::Pi * uu.x + L.rot;
+            const auto wo = -V3<F>(st * std::sin(p), std::cos(t), st * std::cos(p));
+            const auto gL = PointGeometry<F>::make_infinite(wo);
+            const auto pL = L.pdf_direct(g, gL, lpi.tr, wo);
+            if (pL == F(0)) return {};
+            const auto Le = L.eval(gL, wo);
+            s = LightSample<F>{gL, wo, Le / pL};
+            break;
+        }
+        }
+        if (s) s->weight = s->weight / p_sel;
+        return s;
+    }
+    // path.h:563-583 pdf_direct for a light endpoint
+    F pdf_direct_light(const SceneInteraction<F>& sp, const SceneInteraction<F>& spL, V3<F> wo) const {
+        const int li = light_indices_map_.at(spL.primitive);
+        const auto& lpi = lights_.at(li);
+        return pdf_light_selection() * light_of(spL.primitive).pdf_direct(sp.geom, spL.geom, lpi.tr, wo);
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// Random numbers. RngMT restates include/lm/math.h:204-271 (std::mt19937 with
+// uniform_real_distribution<double>; the float variant rounds the double toward -inf).
+// RngPhilox is the counter-based stream the GPU uses: path-keyed, fixed slots per vertex, so a
+// GPU path and an oracle path consume identical numbers.
+struct RngMT {
+    std::mt19937 eng;
+    std::uniform_real_distribution<double> dist;
+    bool as_float = false;
+    explicit RngMT(unsigned int seed, bool f) : as_float(f) { eng.seed(seed); }
+    double u() {
+        const double rd = dist(eng);
+        if (!as_float) return rd;
+        float rf = float(rd);
+        if (double(rf) > rd) rf = std::nextafter(rf, -std::numeric_limits<float>::infinity());
+        return double(rf);
+    }
+};
+
+struct PathRng {
+    // mode 0: sequential mt19937 (the reference's consumption order); mode 1: philox slots
+    int mode = 0;
+    RngMT* mt = nullptr;
+    uint32_t seed = 0;
+    uint64_t path = 0;
+    double seq() { return mt->u(); }
+    // slot in [0,16) of vertex nv
+    double slot(int nv, int s) { return double(philox_uniform(seed, path, uint32_t(nv), uint32_t(s))); }
+};
+
+// ------------------------------------------------------------------------------------------------
+// src/film/film_bitmap.cpp (splat via CAS, rescale) with double accumulators.
+struct Film {
+    int w = 0, h = 0;
+    struct Px { double r, g, b; };
+    std::vector<std::atomic<Px>> data;
+    std::vector<std::atomic<Px>> m2;
+    bool with_m2 = false;
+    Film(int w_, int h_, bool m2_) : w(w_), h(h_), data(size_t(w_) * h_), m2(m2_ ? size_t(w_) * h_ : 0), with_m2(m2_) {
+        for (auto& v : data) v.store(Px{0, 0, 0});
+        for (auto& v : m2) v.store(Px{0, 0, 0});
+    }
+    static void add(std::atomic<Px>& a, Px v) {
+        Px e = a.load();
+        while (!a.compare_exchange_weak(e, Px{e.r + v.r, e.g + v.g, e.b + v.b})) {}
+    }
+    template <typename F> void raster_to_pixel(V2<F> rp, int& x, int& y) const {
+        x = std::clamp(int(rp.x * F(w)), 0, w - 1);
+        y = std::clamp(int(rp.y * F(h)), 0, h - 1);
+    }
+    template <typename F> void splat(V2<F> rp, V3<F> c) {
+        int x, y; raster_to_pixel(rp, x, y);
+        add(data[size_t(y) * w + x], Px{double(c.x), double(c.y), double(c.z)});
+    }
+    template <typename F> void splat_path(V2<F> rp, V3<F> c) {
+        int x, y; raster_to_pixel(rp, x, y);
+        const size_t i = size_t(y) * w + x;
+        add(data[i], Px{double(c.x), double(c.y), double(c.z)});
+        if (with_m2) add(m2[i], Px{double(c.x) * double(c.x), double(c.y) * double(c.y), double(c.z) * double(c.z)});
+    }
+};
+
+// ------------------------------------------------------------------------------------------------
+// src/renderer/renderer_raycast.cpp:62-101
+template <typename F>
+void render_raycast(const Scene<F>& scene, int w, int h, V3<F> bg, bool use_constant_color, bool visualize_normal,
+                    const V3<F>* color, double* out, int nthreads) {
+    const auto& cam = scene.camera();
+    const long long n = (long long)w * h;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (long long index = 0; index < n; index++) {
+        const int x = int(index % w), y = int(index / w);
+        const auto ray = cam.primary_ray(V2<F>((F(x) + F(.5)) / F(w), (F(y) + F(.5)) / F(h)));
+        const auto sp = scene.intersect(ray);
+        V3<F> c;
+        if (!sp) c = bg;
+        else if (visualize_normal) c = vabs(sp->geom.n);
+        else if (sp->geom.infinite) c = scene.light_of(sp->primitive).eval(sp->geom, sp->geom.wo);
+        else {
+            const auto R = color ? std::optional<V3<F>>(*color) : scene.material_of(sp->primitive).reflectance();
+            c = R ? *R : V3<F>();
+            if (!use_constant_color) c *= F(.2) + F(.8) * std::abs(dot(sp->geom.n, -ray.d));
+        }
+        out[3 * index] = double(c.x); out[3 * index + 1] = double(c.y); out[3 * index + 2] = double(c.z);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// src/renderer/renderer_pt.cpp:80-315
+struct PTParams {
+    int w, h;
+    long long spp;
+    int max_verts;
+    unsigned int seed;
+    int sampling_mode;    // 0 naive, 1 nee, 2 mis
+    int primary_mode;     // 0 pixel, 1 image
+    int rng_mode;         // 0 mt19937 per thread (reference), 1 philox per path
+    int with_m2;
+};
+
+template <typename F>
+void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* out_m2, long long* rays_out, int nthreads) {
+    using V3F = V3<F>;
+    if (scene.nodes.size() <= 1) throw std::runtime_error("Missing primitives.");
+    if (!scene.camera_) throw std::runtime_error("Missing camera primitive.");
+    if (scene.num_lights() == 0) throw std::runtime_error("No light in the scene.");
+    Film film(P.w, P.h, P.with_m2 && P.primary_mode == 0);
+    const auto& cam = scene.camera();
+    const bool pixel_mode = P.primary_mode == 0;
+    const long long num_pixels = (long long)P.w * P.h;
+    const long long total = num_pixels * P.spp;
+    const int nth = std::max(1, nthreads);
+    std::vector<RngMT*> rngs(nth, nullptr);
+    for (int i = 0; i < nth; i++) rngs[i] = new RngMT(P.seed + i, std::is_same<F, float>::value);
+    std::vector<long long> rays(nth, 0);
+
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+    for (long long index = 0; index < total; index++) {
+        const int tid = omp_get_thread_num();
+        const long long pixel_index = index / P.spp;
+        PathRng rng; rng.mode = P.rng_mode; rng.mt = rngs[tid]; rng.seed = P.seed; rng.path = (uint64_t)index;
+        auto U = [&](int nv, int s) -> double { return rng.mode == 0 ? rng.seq() : rng.slot(nv, s); };
+        long long& nrays = rays[tid];
+
+        F wx, wy, ww, wh;
+        if (pixel_mode) {
+            const int x = int(pixel_index % P.w), y = int(pixel_index / P.w);
+            const F dx = F(1) / F(P.w), dy = F(1) / F(P.h);
+            wx = dx * F(x); wy = dy * F(y); ww = dx; wh = dy;
+        } else { wx = 0; wy = 0; ww = 1; wh = 1; }
+
+        // sample_position(EL) + sample_component(camera): PositionSampleU (4) + ComponentSampleU (2)
+        if (rng.mode == 0) { for (int k = 0; k < 6; k++) rng.seq(); }
+        SceneInteraction<F> sp;
+        sp.type = SI_Camera; sp.primitive = *scene.camera_;
+        sp.geom = PointGeometry<F>::make_degenerated(cam.position);
+        int comp = 0;
+        V3F throughput(F(1));
+        V3F wi{};
+        V2<F> raster_pos{};
+        V3F L(F(0));  // path contribution (pixel mode: every splat of a path lands on raster_pos)
+        bool have_rp = false;
+
+        for (int nv = 1; nv < P.max_verts; nv++) {
+            const bool is_specular = sp.type == SI_Surface && scene.material_of(sp.primitive).is_specular_component(comp);
+            const bool samplable_by_nee = P.sampling_mode != 0 && (pixel_mode ? (nv > 1 && !is_specular) : !is_specular);
+
+            if (samplable_by_nee) [&] {
+                double u8[8];
+                for (int k = 0; k < 8; k++) u8[k] = U(nv, k);
+                int light_node = -1;
+                const auto sL = scene.sample_direct_light(u8, sp, light_node);
+                if (!sL) return;
+                SceneInteraction<F> spL; spL.type = SI_Light; spL.primitive = light_node; spL.geom = sL->geom;
+                nrays++;
+                if (!scene.visible(sp, spL)) return;
+                V2<F> rp = raster_pos;
+                if (nv == 1) {
+                    const auto rp_ = cam.raster_position(-sL->wo);
+                    if (!rp_) return;
+                    rp = *rp_;
+                }
+                const auto wo = -sL->wo;
+                V3F fs;
+                if (sp.type == SI_Camera) fs = cam.eval(wo);
+                else fs = scene.material_of(sp.primitive).eval(sp.geom, wi, wo, comp, TransDir::EL, true) *
+                          shading_normal_correction(sp.geom, wi, wo, TransDir::EL);
+                if (is_zero(fs)) return;
+                F mis_w = F(1);
+                if (P.sampling_mode == 2) {
+                    const F p_light = scene.pdf_direct_light(sp, spL, sL->wo);
+                    const F p_bsdf = sp.type == SI_Camera ? cam.pdf_direction(wo)
+                                                          : scene.material_of(sp.primitive).pdf_direction(sp.geom, wi, wo, comp, true);
+                    mis_w = balance_heuristic(p_light, p_bsdf);
+                }
+                const auto Cc = throughput * fs * sL->weight * mis_w;
+                if (pixel_mode) L += Cc; else film.splat(rp, Cc);
+            }();
+
+            // Direction sampling
+            std::optional<DirectionSample<F>> s;
+            if (nv == 1) {
+                // camera_pinhole.cpp:143-148 with the pixel-window jitter of renderer_pt.cpp:199-201
+                const double j0 = U(nv, 8);
+                const double j1 = U(nv, 9);
+                const V2<F> ud(wx + ww * F(j0), wy + wh * F(j1));
+                U(nv, 10); U(nv, 11);
+                s = DirectionSample<F>{cam.primary_ray(ud).d, V3F(F(1))};
+            } else {
+                const V2<F> ud(F(U(nv, 8)), F(U(nv, 9)));
+                const V2<F> udc(F(U(nv, 10)), F(U(nv, 11)));
+                const auto& mat = scene.material_of(sp.primitive);
+                const auto ms = mat.sample_direction(ud, udc, sp.geom, wi, comp, TransDir::EL);
+                if (ms) s = DirectionSample<F>{ms->wo, ms->weight * shading_normal_correction(sp.geom, wi, ms->wo, TransDir::EL)};
+            }
+            if (!s) break;
+
+            if (nv == 1) {
+                const auto rp = cam.raster_position(s->wo);
+                raster_pos = rp ? *rp : V2<F>();
+                have_rp = true;
+            }
+
+            nrays++;
+            const auto hit = scene.intersect(Ray<F>{sp.geom.p, s->wo});
+            if (!hit) break;
+
+            throughput *= s->weight;
+
+            const bool samplable_by_direct_hit = P.sampling_mode == 1 ? !samplable_by_nee : true;
+            if (samplable_by_direct_hit && scene.is_light(*hit)) [&] {
+                const auto spL = hit->as_type(SI_Light);
+                const auto woL = -s->wo;
+                const auto fs = scene.light_of(spL.primitive).eval(spL.geom, woL);
+                F mis_w = F(1);
+                if (P.sampling_mode != 0 && samplable_by_nee) {
+                    const F pdf_bsdf = sp.type == SI_Camera ? cam.pdf_direction(s->wo)
+                                                            : scene.material_of(sp.primitive).pdf_direction(sp.geom, wi, s->wo, comp, true);
+                    const F pdf_light = scene.pdf_direct_light(sp, spL, woL);
+                    mis_w = balance_heuristic(pdf_bsdf, pdf_light);
+                }
+                const auto Cc = throughput * fs * mis_w;
+                if (pixel_mode) L += Cc; else film.splat(raster_pos, Cc);
+            }();
+
+            if (hit->geom.infinite) break;
+
+            if (nv > 5) {
+                const F q = std::max(F(.2), F(1) - comp_max(throughput));
+                if (F(U(nv, 12)) < q) break;
+                throughput /= F(1) - q;
+            }
+
+            ComponentSample<F> sc{0, F(1)};
+            {
+                const V2<F> uc(F(U(nv, 13)), F(U(nv, 14)));
+                if (hit->type == SI_Surface) sc = scene.material_of(hit->primitive).sample_component(uc, hit->geom, -s->wo);
+            }
+            throughput *= sc.weight;
+
+            wi = -s->wo;
+            sp = *hit;
+            comp = sc.comp;
+        }
+        if (pixel_mode && have_rp) film.splat_path(raster_pos, L);
+    }
+
+    for (auto* r : rngs) delete r;
+    // renderer_pt.cpp:307-312 (rescale)
+    const double scale = pixel_mode ? 1.0 / double(P.spp) : double(num_pixels) / double(P.spp);
+    for (long long i = 0; i < num_pixels; i++) {
+        const auto v = film.data[i].load();
+        out[3 * i] = v.r * scale; out[3 * i + 1] = v.g * scale; out[3 * i + 2] = v.b * scale;
+        if (out_m2 && film.with_m2) {
+            const auto m = film.m2[i].load();
+            out_m2[3 * i] = m.r; out_m2[3 * i + 1] = m.g; out_m2[3 * i + 2] = m.b;
+        }
+    }
+    if (rays_out) {
+        long long t = 0;
+        for (auto r : rays) t += r;
+        *rays_out = t;
+    }
+}
+
+}  // namespace lmo

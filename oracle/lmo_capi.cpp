@@ -1,0 +1,269 @@
+// Oracle (test infrastructure only): C entry points over the CPU restatement in lmo.hpp, loaded
+// with ctypes by tests/ and by bench.py's CPU-baseline leg. One handle holds a scene in either
+// precision (double = the reference's Float, float = the fp32 parity mode).
+#include "lmo.hpp"
+#include <chrono>
+#include <cstring>
+#include <memory>
+
+using namespace lmo;
+
+namespace {
+
+thread_local std::string g_err;
+
+struct Handle {
+    bool dbl;
+    std::unique_ptr<Scene<double>> sd;
+    std::unique_ptr<Scene<float>> sf;
+};
+
+template <typename Fn>
+int dispatch(Handle* h, Fn&& fn) {
+    try {
+        return h->dbl ? fn(*h->sd) : fn(*h->sf);
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -1;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lmo_last_error() { return g_err.c_str(); }
+
+void* lmo_create(int use_double) {
+    auto* h = new Handle();
+    h->dbl = use_double != 0;
+    if (h->dbl) h->sd.reset(new Scene<double>());
+    else h->sf.reset(new Scene<float>());
+    return h;
+}
+
+void lmo_destroy(void* p) { delete static_cast<Handle*>(p); }
+
+// mesh::raw (src/mesh/mesh_raw.cpp:50-68): ps/ns flat xyz, ts flat uv, per-corner indices.
+int lmo_add_mesh(void* p, const float* ps, int nps, const float* ns, int nns, const float* ts, int nts,
+                 const int* fp, const int* ft, const int* fn, int ncorners) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Mesh<F> m;
+        for (int i = 0; i < nps; i++) m.ps.push_back(V3<F>(F(ps[3 * i]), F(ps[3 * i + 1]), F(ps[3 * i + 2])));
+        for (int i = 0; i < nns; i++) m.ns.push_back(V3<F>(F(ns[3 * i]), F(ns[3 * i + 1]), F(ns[3 * i + 2])));
+        for (int i = 0; i < nts; i++) m.ts.push_back(V2<F>(F(ts[2 * i]), F(ts[2 * i + 1])));
+        if (m.ts.empty()) m.ts.push_back(V2<F>());
+        for (int i = 0; i < ncorners; i++) m.fs.push_back({fp[i], ft ? ft[i] : 0, fn[i]});
+        S.meshes.push_back(std::move(m));
+        return int(S.meshes.size()) - 1;
+    });
+}
+
+// type: 0 diffuse (Kd), 1 glossy (Ks, ax, ay), 2 glass (Ni), 3 mirror. params: 5 doubles.
+int lmo_add_material(void* p, int type, const double* prm) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Material<F> m;
+        m.type = type;
+        if (type == MAT_DIFFUSE) m.Kd = V3<F>(F(prm[0]), F(prm[1]), F(prm[2]));
+        if (type == MAT_GLOSSY) { m.Ks = V3<F>(F(prm[0]), F(prm[1]), F(prm[2])); m.ax = F(prm[3]); m.ay = F(prm[4]); }
+        if (type == MAT_GLASS) m.Ni = F(prm[0]);
+        S.materials.push_back(m);
+        return int(S.materials.size()) - 1;
+    });
+}
+
+// light::area (src/light/light_area.cpp:68-80): the triangle-area CDF is built on the untransformed mesh.
+int lmo_add_light_area(void* p, const double* Ke, int mesh) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Light<F> L;
+        L.type = LIGHT_AREA;
+        L.Ke = V3<F>(F(Ke[0]), F(Ke[1]), F(Ke[2]));
+        L.mesh = mesh;
+        const auto& m = S.meshes.at(mesh);
+        for (int f = 0; f < m.num_triangles(); f++) {
+            const auto tri = m.triangle_at(f);
+            const auto cr = cross(tri.p2.p - tri.p1.p, tri.p3.p - tri.p1.p);
+            L.dist.add(safe_sqrt(dot(cr, cr)) * F(.5));
+        }
+        L.invA = F(1) / L.dist.c.back();
+        L.dist.norm();
+        S.lights_assets.push_back(std::move(L));
+        return int(S.lights_assets.size()) - 1;
+    });
+}
+
+int lmo_add_light_envconst(void* p, const double* Le) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Light<F> L;
+        L.type = LIGHT_ENVCONST;
+        L.Ke = V3<F>(F(Le[0]), F(Le[1]), F(Le[2]));
+        S.lights_assets.push_back(std::move(L));
+        return int(S.lights_assets.size()) - 1;
+    });
+}
+
+// light::env with an in-memory texture (row 0 = first row of `texels`, c channels, fp32).
+int lmo_add_light_env(void* p, const float* texels, int w, int hgt, int c, double rot_deg, double scale) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Light<F> L;
+        L.type = LIGHT_ENV;
+        L.tw = w; L.th = hgt; L.tc = c;
+        L.texels.assign(texels, texels + size_t(w) * hgt * c);
+        L.rot = F(rot_deg) * C<F>::Pi / F(180);
+        L.scale = F(scale);
+        L.init_env();
+        S.lights_assets.push_back(std::move(L));
+        return int(S.lights_assets.size()) - 1;
+    });
+}
+
+int lmo_add_camera(void* p, const double* pos, const double* center, const double* up, double vfov, double aspect) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Camera<F> c;
+        c.construct(V3<F>(F(pos[0]), F(pos[1]), F(pos[2])), V3<F>(F(center[0]), F(center[1]), F(center[2])),
+                    V3<F>(F(up[0]), F(up[1]), F(up[2])), F(vfov), F(aspect));
+        S.cameras.push_back(c);
+        return int(S.cameras.size()) - 1;
+    });
+}
+
+int lmo_create_primitive_node(void* p, int mesh, int material, int light, int camera) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float; return S.create_primitive_node(mesh, material, light, camera); });
+}
+
+int lmo_create_group_node(void* p, const double* m16) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float; return S.create_group_node(M4<F>::from_colmajor(m16)); });
+}
+
+int lmo_create_instance_group_node(void* p) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float; return S.create_instance_group_node(); });
+}
+
+int lmo_add_child(void* p, int parent, int child) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float; S.add_child(parent, child); return 0; });
+}
+
+int lmo_root_node(void*) { return 0; }
+
+// Scene::build (src/scene.cpp:274-317) with the accel::sahbvh build; returns seconds via *secs.
+int lmo_build(void* p, int nthreads, int robust, double* secs) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        const auto t0 = std::chrono::steady_clock::now();
+        S.build(nthreads > 0 ? nthreads : int(std::thread::hardware_concurrency()), robust != 0);
+        if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return 0;
+    });
+}
+
+int lmo_num_triangles(void* p) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float; return int(S.accel.trs.size()); });
+}
+
+// Flattened triangles as the accel stores them (accel_sahbvh.cpp:41-49): p1, e1 = p2 - p1,
+// e2 = p3 - p1, each rounded in the scene's precision.
+int lmo_get_triangles(void* p, float* out9) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        for (size_t i = 0; i < S.accel.trs.size(); i++) {
+            const auto& t = S.accel.trs[i];
+            const F v[9] = {t.p1.x, t.p1.y, t.p1.z, t.e1.x, t.e1.y, t.e1.z, t.e2.x, t.e2.y, t.e2.z};
+            for (int k = 0; k < 9; k++) out9[9 * i + k] = float(v[k]);
+        }
+        return 0;
+    });
+}
+
+// Accel::intersect over a batch of rays. rays: n x 8 floats (ox,oy,oz,tmin,dx,dy,dz,tmax).
+// Outputs: t (float64), u, v (float64), global triangle index (-1 = miss). brute != 0 uses the
+// exhaustive test instead of the BVH. Returns the elapsed seconds in *secs.
+int lmo_intersect(void* p, const float* rays, long long n, double* t_out, double* uv_out, int* tri_out,
+                  int nthreads, int brute, double* secs) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        const auto t0 = std::chrono::steady_clock::now();
+        const int nth = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nth)
+        for (long long i = 0; i < n; i++) {
+            const float* r = rays + 8 * i;
+            Ray<F> ray{V3<F>(F(r[0]), F(r[1]), F(r[2])), V3<F>(F(r[4]), F(r[5]), F(r[6]))};
+            const auto hit = brute ? S.accel.intersect_brute(ray, F(r[3]), F(r[7])) : S.accel.intersect(ray, F(r[3]), F(r[7]));
+            if (hit) {
+                t_out[i] = double(hit->t); uv_out[2 * i] = double(hit->uv.x); uv_out[2 * i + 1] = double(hit->uv.y);
+                tri_out[i] = hit->global_tri;
+            } else {
+                t_out[i] = 0; uv_out[2 * i] = 0; uv_out[2 * i + 1] = 0; tri_out[i] = -1;
+            }
+        }
+        if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return 0;
+    });
+}
+
+int lmo_render_raycast(void* p, int w, int hgt, const double* bg, int use_constant_color, int visualize_normal,
+                       const double* color, double* out, int nthreads, double* secs) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        const auto t0 = std::chrono::steady_clock::now();
+        V3<F> bgc{F(bg[0]), F(bg[1]), F(bg[2])};
+        V3<F> col;
+        if (color) col = V3<F>(F(color[0]), F(color[1]), F(color[2]));
+        render_raycast<F>(S, w, hgt, bgc, use_constant_color != 0, visualize_normal != 0, color ? &col : nullptr, out,
+                          nthreads > 0 ? nthreads : omp_get_max_threads());
+        if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return 0;
+    });
+}
+
+int lmo_render_pt(void* p, int w, int hgt, long long spp, int max_verts, unsigned int seed, int sampling_mode,
+                  int primary_mode, int rng_mode, double* out, double* out_m2, long long* rays, int nthreads, double* secs) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        const auto t0 = std::chrono::steady_clock::now();
+        PTParams P{w, hgt, spp, max_verts, seed, sampling_mode, primary_mode, rng_mode, out_m2 != nullptr};
+        render_pt<F>(S, P, out, out_m2, rays, nthreads > 0 ? nthreads : omp_get_max_threads());
+        if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return 0;
+    });
+}
+
+float lmo_philox_uniform(unsigned int seed, unsigned long long path, unsigned int vertex, unsigned int slot) {
+    return philox_uniform(seed, path, vertex, slot);
+}
+
+int lmo_max_threads() { return omp_get_max_threads(); }
+
+}  // extern "C"
+
+extern "C" void lmo_philox4x32(unsigned int c0, unsigned int c1, unsigned int c2, unsigned int c3, unsigned int k0,
+                               unsigned int k1, unsigned int* out4) {
+    const Philox4 r = philox4x32_10(c0, c1, c2, c3, k0, k1);
+    for (int i = 0; i < 4; i++) out4[i] = r.v[i];
+}

@@ -1,0 +1,58 @@
+"""The C-ABI library loads and exports every entry point include/lmgpu.h declares; error codes and
+messages come back without a GPU (no compute call is made here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "lmgpu.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\**(lmgpu_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_header_parses():
+    names = declared_functions()
+    assert "lmgpu_accel_intersect" in names and "lmgpu_render_pt" in names
+    assert len(names) >= 20
+
+
+def test_every_declared_symbol_is_exported(native_lib):
+    missing = [n for n in declared_functions() if not hasattr(native_lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header(native_lib):
+    from lightmetrica import _native as N
+    bound = {name for name, _, _ in N.SIGNATURES}
+    assert set(declared_functions()) <= bound
+
+
+def test_errors_without_device(native_lib):
+    from lightmetrica import _native as N
+    L = native_lib
+    f = C.c_void_p()
+    assert L.lmgpu_film_create(C.byref(f), 0, 4) == 1  # LMGPU_ERR_INVALID_ARGUMENT
+    assert b"film size" in L.lmgpu_last_error()
+    a = C.c_void_p()
+    assert L.lmgpu_accel_create(C.byref(a)) == 0
+    hits = (N.Hit * 1)()
+    rays = (C.c_float * 8)()
+    assert L.lmgpu_accel_intersect(a, rays, 1, hits) == 3  # LMGPU_ERR_UNINITIALIZED
+    assert b"not built" in L.lmgpu_last_error()
+    assert L.lmgpu_accel_destroy(a) == 0
+    st = N.AccelStats()
+    assert L.lmgpu_accel_get_stats(None, C.byref(st)) == 1
+    assert L.lmgpu_scene_create(None, None, None) == 1
+
+
+def test_version(native_lib):
+    assert native_lib.lmgpu_version() >= 1
+
+
+def test_oracle_library_loads(oracle_mod):
+    assert oracle_mod.max_threads() >= 1

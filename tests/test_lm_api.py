@@ -1,0 +1,126 @@
+"""The drop-in `lightmetrica` API (host side, no GPU): component keys, scene-graph rules
+(src/scene.cpp:72-156), and flattening that agrees bit for bit with the oracle's fp32 mode."""
+import numpy as np
+import pytest
+
+
+def test_registered_keys(lm):
+    keys = lm.registered_components()
+    for k in ["accel::sahbvh", "accel::nanort", "accel::embree", "accel::embreeinstanced", "accel::gpu",
+              "renderer::pt", "renderer::raycast", "film::bitmap", "camera::pinhole", "mesh::raw",
+              "material::diffuse", "material::glossy", "material::glass", "material::mirror",
+              "light::area", "light::envconst", "light::env", "scene::default"]:
+        assert k in keys
+
+
+def test_locators_and_missing_keys(lm):
+    m = lm.load_material("mat", "diffuse", Kd=[0.5, 0.5, 0.5])
+    assert m.loc() == "$.assets.mat"
+    assert lm.get("$.assets.mat") is m
+    with pytest.raises(lm.LmGpuError):
+        lm.load_material("x", "nonexistent")
+    with pytest.raises(lm.LmGpuError):
+        lm.load_material("g", "glossy", Ks=[1, 1, 1])  # missing ax/ay
+
+
+def _tri_mesh(lm, name="tri"):
+    return lm.load_mesh(name, "raw", ps=[0, 0, 0, 1, 0, 0, 0, 1, 0], ns=[0, 0, 1], ts=[0, 0],
+                        fs={"p": [0, 1, 2], "n": [0, 0, 0], "t": [0, 0, 0]})
+
+
+def test_scene_graph_rules(lm):
+    scene = lm.load_scene("scene", "default", accel=lm.load_accel("accel", "sahbvh"))
+    mesh = _tri_mesh(lm)
+    mat = lm.load_material("mat", "diffuse")
+    cam = lm.load_camera("cam", "pinhole", position=[0, 0, 5], center=[0, 0, 0], up=[0, 1, 0], vfov=30, aspect=1)
+    light = lm.load_light("l", "area", Ke=[1, 1, 1], mesh=mesh)
+    with pytest.raises(lm.LmGpuError):
+        scene.create_primitive_node()                                # no assets
+    with pytest.raises(lm.LmGpuError):
+        scene.create_primitive_node(mesh=mesh)                       # mesh without material
+    with pytest.raises(lm.LmGpuError):
+        scene.create_primitive_node(camera=cam, light=light)         # camera and light
+    scene.add_primitive(light=lm.load_light("e1", "envconst", Le=[1, 1, 1]))
+    with pytest.raises(lm.LmGpuError):
+        scene.add_primitive(light=lm.load_light("e2", "envconst", Le=[1, 1, 1]))  # second env light
+    scene.add_primitive(camera=cam)
+    scene.add_primitive(mesh=mesh, material=mat, light=light)
+    assert scene.camera_node() >= 0 and scene.env_light_node() >= 0
+    assert scene.num_lights() == 2
+    flat = scene._flatten()
+    # lights in traversal order (scene.cpp:279-286): env first here, then the area light
+    assert [L.type for L in flat["lights"]] == [1, 0]
+    assert flat["prim_light"].tolist() == [1]
+
+
+def _instanced_scene(lm):
+    """Nested groups with rotation, translation and scale, plus an instance group."""
+    scene = lm.load_scene("scene", "default", accel=lm.load_accel("accel", "embree"))
+    rng = np.random.default_rng(3)
+    ps = rng.random((30, 3)).astype(np.float32)
+    mesh = lm.load_mesh("m", "raw", ps=ps, ns=[0, 0, 1], ts=[0, 0],
+                        fs={"p": np.arange(30), "n": np.zeros(30, int), "t": np.zeros(30, int)})
+    mat = lm.load_material("mat", "diffuse")
+    scene.add_transformed_primitive(lm.rotate(0.3, [1, 2, 3]) @ lm.scale([1.5, 0.5, 2.0]), mesh=mesh, material=mat)
+    g = scene.create_instance_group_node()
+    scene.add_child(g, scene.create_primitive_node(mesh=mesh, material=mat))
+    for k in range(3):
+        t = scene.create_group_node(lm.translate([k * 1.5, 0.25, -k]) @ lm.rotate(0.7 * k, [0, 1, 0]))
+        scene.add_child(t, g)
+        scene.add_child(scene.root_node(), t)
+    return scene
+
+
+def test_flatten_bitexact_with_oracle_fp32(lm, oracle_mod):
+    """World-space triangles (the accel input) equal the oracle's fp32 flattening bit for bit,
+    including nested group transforms and instance groups (accel_sahbvh.cpp:132-151)."""
+    scene = _instanced_scene(lm)
+    pos = scene._flatten()["positions"]
+    S = oracle_mod.from_lm_scene(scene, double=False)
+    S.build()
+    assert S.num_tris == pos.shape[0] == 40
+    p = pos.reshape(-1, 3, 3)
+    mine = np.concatenate([p[:, 0], p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]], 1)  # fp32 subtraction
+    assert np.array_equal(S.triangles(), mine)
+
+
+def test_flatten_close_to_oracle_fp64(lm, oracle_mod):
+    scene = _instanced_scene(lm)
+    pos = scene._flatten()["positions"]
+    S = oracle_mod.from_lm_scene(scene, double=True)
+    S.build()
+    p = pos.reshape(-1, 3, 3).astype(np.float64)
+    mine = np.concatenate([p[:, 0], p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]], 1)
+    assert np.allclose(S.triangles(), mine, atol=1e-5)
+
+
+def test_synthetic_box_geometry(lm):
+    """The benchmark box: 10 wall quads (20 triangles), two 12-triangle boxes, a 2-triangle light;
+    every triangle's winding agrees with its shading normal (a mismatch would zero its shading)."""
+    from lightmetrica import synthetic as syn
+    scene, film = syn.box_scene()
+    flat = scene._flatten()
+    assert flat["positions"].shape[0] == 20 + 24 + 2
+    p = flat["positions"].reshape(-1, 3, 3)
+    gn = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    sn = flat["normals"].reshape(-1, 3, 3).sum(1)
+    assert np.all(np.sum(gn * sn, axis=1) > 0)
+
+
+def test_synthetic_spheres_counts(lm):
+    from lightmetrica import synthetic as syn
+    scene, film, info = syn.spheres_scene(n_spheres=3, subdiv=2, ground_quads=8, w=32, h=18)
+    flat = scene._flatten()
+    assert flat["positions"].shape[0] == info["triangles"] == 3 * 320 + 2 * 64 + 12
+    kinds = sorted({m.key_name for m in flat["materials"]})
+    assert "material::diffuse" in kinds
+    # icosphere subdivision counts: 20 * 4^s faces
+    v, f = syn.icosphere(6)
+    assert f.shape[0] == 81920 and v.shape[0] == 40962
+
+
+def test_sphere_rays_unit_directions():
+    from lightmetrica import synthetic as syn
+    r = syn.sphere_rays(1000, [0, 1, 0])
+    assert r.shape == (1000, 8) and r.dtype == np.float32
+    assert np.allclose(np.linalg.norm(r[:, 4:7], axis=1), 1, atol=1e-6)
