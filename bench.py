@@ -1,0 +1,343 @@
+#!/usr/bin/env python
+"""Benchmark: renderer::pt on the plain drop-in workload, on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl lmgpu|reference]
+
+Workload (one step = one full render): the displaced-sphere scene of lightmetrica.synthetic
+(40 icospheres at subdivision 6 on a 512 x 512-quad ground: 3,801,100 triangles; 50 % diffuse,
+30 % GGX glossy, 20 % dielectric; 6 area lights + constant environment), 1920 x 1080, 64 spp,
+max path length 10 (max_verts = 11), MIS, pixel sampling, fp32. Synthetic seeded data stands in
+for the reference's external scenes.
+
+Metric: Mrays/s = every traced segment (extension + shadow rays) / device time of the render,
+timed with CUDA events on the launching stream. `e2e` is the same metric through the public
+`lightmetrica` API (renderer.render() + film.buffer(): host parameters in, the film copied back to
+host memory every step). The scene (BVH, triangles, shading data: well above the 129 MB L2)
+stays resident; L2 is also flushed between timed steps with a 256 MB write.
+
+--impl reference times the CPU restatement of the reference's path (fp64 accel::sahbvh +
+renderer::pt with std::mt19937 per thread under OpenMP, all host cores) on a bounded sample of
+the same workload: one full-frame render at 1 spp per step. The reference itself cannot be built
+here (glm, nlohmann_json, cereal, stb are absent), so the restatement stands in for it.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "lightmetrica-v3_gb300"))
+
+METRIC = "Mrays/s (renderer::pt, all traced segments)"
+W_PX, H_PX, SPP, MAX_VERTS = 1920, 1080, 64, 11
+SEED_SCENE, SEED_RENDER = 7, 12345
+NODE_BYTES, TRI_BYTES = 80, 48
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap")
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def build_scene():
+    import lightmetrica as lm
+    from lightmetrica import synthetic as syn
+    lm.init()
+    scene, film, info = syn.spheres_scene(seed=SEED_SCENE, w=W_PX, h=H_PX)
+    return lm, scene, film, info
+
+
+def cpu_port(scene, spp: int, threads: int = 0):
+    """Times the CPU restatement (fp64, reference RNG stream) on one render of `spp`."""
+    from oracle import oracle as O
+    S = O.from_lm_scene(scene, double=True)
+    S.build(nthreads=threads)
+    return S
+
+
+def run_reference(args) -> None:
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    lm, scene, film, info = build_scene()
+    S = cpu_port(scene, 1)
+    cores = O.max_threads()
+    for _ in range(args.warmup):
+        S.render_pt(W_PX, H_PX, 1, MAX_VERTS, seed=SEED_RENDER, rng="mt19937")
+    rays = 0
+    secs = 0.0
+    for k in range(args.steps):
+        _, _, r, s = S.render_pt(W_PX, H_PX, 1, MAX_VERTS, seed=SEED_RENDER + k, rng="mt19937")
+        rays += r
+        secs += s
+    v = rays / secs / 1e6
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"displaced spheres {info['triangles']} tris, {W_PX}x{H_PX}, path length {MAX_VERTS - 1}, "
+                                  f"MIS; sample: 1 spp per step", "triangles": info["triangles"]},
+           "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port",
+                            "sample": f"{W_PX}x{H_PX} at 1 spp per step ({W_PX * H_PX} paths), {args.steps} steps"},
+           "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "build_seconds": S.build_seconds}
+    print(json.dumps(out))
+
+
+def run_gpu(args) -> None:
+    import ctypes as C
+
+    ws, rank, local = _dist()
+    import lightmetrica as lm_mod
+    from lightmetrica import _native as N
+    N.check(N.lib().lmgpu_set_device(local))
+    dist = None
+    if ws > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+        dist = td
+    lm, scene, film, info = build_scene()
+    t0 = time.perf_counter()
+    scene.build()
+    build_s = time.perf_counter() - t0
+    acc = scene.accel().stats()
+    L = N.lib()
+
+    def params(spp, seed, instrument=0):
+        p = N.PTParams()
+        p.spp = spp
+        p.max_verts = MAX_VERTS
+        p.seed = seed
+        p.sampling_mode = 2
+        p.primary_mode = 0
+        p.instrument = instrument
+        return p
+
+    # instrumented (untimed) pass: node / triangle visits per ray for the roofline's byte count
+    st = N.RenderStats()
+    N.check(L.lmgpu_render_pt(scene._h, film._h, C.byref(params(4, 1, 1)), None, C.byref(st)))
+    counts = {"ext_nodes": st.ext_nodes, "ext_tris": st.ext_tris, "shadow_nodes": st.shadow_nodes,
+              "shadow_tris": st.shadow_tris}
+
+    # L2 flush buffer (256 MB)
+    flush = C.c_void_p()
+    cudart = _cudart()
+    assert cudart.cudaMalloc(C.byref(flush), 256 << 20) == 0
+
+    def flush_l2():
+        cudart.cudaMemset(flush, 0, 256 << 20)
+
+    for k in range(args.warmup):
+        N.check(L.lmgpu_render_pt(scene._h, film._h, C.byref(params(SPP, SEED_RENDER + 1000 + k)), None, None))
+    cudart.cudaDeviceSynchronize()
+
+    tot = {"rays": 0, "ext": 0, "sh": 0, "ms": 0.0, "ext_ms": 0.0, "shade_ms": 0.0, "shadow_ms": 0.0, "gen_ms": 0.0,
+           "ext_launches": 0, "sh_launches": 0}
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        for k in range(args.steps):
+            flush_l2()
+            cudart.cudaDeviceSynchronize()
+            s = N.RenderStats()
+            N.check(L.lmgpu_render_pt(scene._h, film._h, C.byref(params(SPP, SEED_RENDER + k)), None, C.byref(s)))
+            tot["rays"] += s.rays
+            tot["ext"] += s.extension_rays
+            tot["sh"] += s.shadow_rays
+            tot["ms"] += s.elapsed_ms
+            tot["ext_ms"] += s.extend_ms
+            tot["shade_ms"] += s.shade_ms
+            tot["shadow_ms"] += s.shadow_ms
+            tot["gen_ms"] += s.generate_ms
+            tot["ext_launches"] += s.extend_launches
+            tot["sh_launches"] += s.shadow_launches
+        cudart.cudaDeviceSynchronize()
+        if dist:
+            dist.barrier()
+    clocks = clk.summary()
+
+    # e2e through the public API: renderer.render() + film.buffer() per step
+    r = lm.load_renderer("renderer", "pt", scene=scene, output=film, max_verts=MAX_VERTS, seed=SEED_RENDER,
+                         sampling_mode="mis", scheduler="sample", spp=SPP)
+    r.render()
+    film.buffer()
+    e2e_rays, e2e_s = 0, 0.0
+    for k in range(max(1, args.steps)):
+        t = time.perf_counter()
+        out = r.render()
+        img = film.buffer_f32()
+        e2e_s += time.perf_counter() - t
+        e2e_rays += out["rays"]
+    d2h = img.nbytes
+    h2d = C.sizeof(N.PTParams)
+
+    sec = tot["ms"] / 1e3
+    if dist:
+        import torch
+        t = torch.tensor([sec], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec = float(t.item())
+    value = tot["rays"] * ws / sec / 1e6
+
+    # roofline of the dominant kernel
+    peaks = _peaks()
+    kern = {"extend": tot["ext_ms"], "shade": tot["shade_ms"], "shadow": tot["shadow_ms"], "generate": tot["gen_ms"]}
+    dom = max(kern, key=kern.get)
+    b_ext = 32 + 16 + NODE_BYTES * counts["ext_nodes"] + TRI_BYTES * counts["ext_tris"]
+    b_sh = 48 + NODE_BYTES * counts["shadow_nodes"] + TRI_BYTES * counts["shadow_tris"]
+    if dom == "extend":
+        bytes_total, launches = tot["ext"] * b_ext, tot["ext_launches"]
+    elif dom == "shadow":
+        bytes_total, launches = tot["sh"] * b_sh, tot["sh_launches"]
+    else:
+        # per extension-ray hit: ray+state read 88 B, next ray+state written 88 B, shading record 96 B,
+        # shadow ray written 48 B
+        bytes_total, launches = tot["ext"] * (88 + 88 + 96 + 48), tot["ext_launches"]
+    achieved = bytes_total / (kern[dom] / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+    if os.path.exists(tf):
+        traffic = json.load(open(tf)).get(dom)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        S = cpu_port(scene, 1)
+        _, _, crays, csec = S.render_pt(W_PX, H_PX, 1, MAX_VERTS, seed=SEED_RENDER, rng="mt19937")
+        cpu = {"value": crays / csec / 1e6, "unit": "Mrays/s", "cores": O.max_threads(), "kind": "port",
+               "sample": f"{W_PX}x{H_PX} at 1 spp ({W_PX * H_PX} paths, {crays} rays, {csec:.1f} s)",
+               "build_seconds": S.build_seconds}
+
+    waves = -(-(W_PX * H_PX * SPP) // (1 << 22))
+    launches_per_step = waves * (1 + 3 * (MAX_VERTS - 1)) + 1
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot["ms"] / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"renderer::pt, displaced spheres ({info['triangles']} tris), {W_PX}x{H_PX}, "
+                                   f"{SPP} spp, max path length {MAX_VERTS - 1}, MIS",
+                       "triangles": info["triangles"], "spp": SPP, "max_verts": MAX_VERTS,
+                       "l2": "inputs larger than L2 (scene resident) and a 256 MB L2 flush between steps",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "rays_per_step": tot["rays"] / max(1, args.steps),
+            "kernel_ms_per_step": {k: v / max(1, args.steps) for k, v in kern.items()},
+            "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                         "traffic": traffic, "bytes_per_ray": {"extend": b_ext, "shadow": b_sh},
+                         "launches": launches, **counts},
+            "cpu_baseline": cpu,
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks,
+            "accel": {"nodes": acc["num_nodes"], "depth": acc["max_depth"], "build_seconds": acc["build_seconds"],
+                      "scene_build_seconds": build_s, "sah_cost": acc["sah_cost"]},
+        }
+        print(json.dumps(out))
+    cudart.cudaFree(flush)
+    if dist:
+        dist.destroy_process_group()
+
+
+def _cudart():
+    import ctypes as C
+    import glob
+    cands = ["libcudart.so", "libcudart.so.13"] + sorted(glob.glob("/usr/local/cuda*/lib64/libcudart.so*"))
+    for c in cands:
+        try:
+            lib = C.CDLL(c)
+            lib.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+            lib.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
+            lib.cudaFree.argtypes = [C.c_void_p]
+            return lib
+        except OSError:
+            continue
+    raise RuntimeError("libcudart not found")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -222,8 +222,8 @@ typedef struct lmgpu_pt_params {
     int32_t sampling_mode;      /* LMGPU_SAMPLING_* ("mis" is the reference default) */
     int32_t primary_mode;       /* LMGPU_PRIMARY_* ("pixel" is the reference default) */
     int64_t wave_paths;         /* paths in flight per wave; 0 = library default */
-    int32_t accumulate;         /* 1: add to the film without clearing or rescaling */
-    int32_t reserved;
+    int32_t accumulate;         /* 1: add to the film; the film's scale becomes 1 / (total spp) */
+    int32_t instrument;         /* 1: count node visits / triangle tests on every 64th traced ray */
 } lmgpu_pt_params;
 
 typedef struct lmgpu_render_stats {
@@ -233,6 +233,10 @@ typedef struct lmgpu_render_stats {
     int64_t shadow_rays;
     double elapsed_ms;          /* device time of the render (CUDA events) */
     double trace_ms;            /* device time inside the extension + shadow trace kernels */
+    double extend_ms, shade_ms, shadow_ms, generate_ms;  /* device time per kernel kind */
+    int64_t extend_launches, shadow_launches;
+    /* with params->instrument: mean 8-wide nodes visited / triangles tested per traced ray */
+    double ext_nodes, ext_tris, shadow_nodes, shadow_tris;
 } lmgpu_render_stats;
 
 /* Renders into `film` (cleared first unless params->accumulate) on `stream` and waits for it.

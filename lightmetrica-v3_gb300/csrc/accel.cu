@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_count(Bvh8 bvh, const flo
 
 template <typename K>
 int trace_grid(K kernel, size_t smem, int64_t n) {
+    if (smem > 48 * 1024) LMGPU_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
     LMGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceBlock, smem));
     per_sm = per_sm < 1 ? 1 : per_sm;

@@ -548,42 +548,72 @@ __global__ void __launch_bounds__(kBlock) k_pt_generate(DevScene S, PtConst P, i
     }
 }
 
-// Extension rays: closest hit over [Eps, Inf].
+// Extension rays: closest hit over [Eps, Inf]. kCount: every 64th ray also counts node visits and
+// triangle tests into sums[0..2] (instrumented runs only).
+template <bool kCount>
 __global__ void __launch_bounds__(kBlock) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       const int* __restrict__ qcount, float4* __restrict__ hits,
-                                                      unsigned long long* rays, int* err) {
+                                                      unsigned long long* rays, int* err, unsigned long long* sums) {
     extern __shared__ uint32_t smem[];
     const int n = *qcount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
     int lerr = 0;
+    uint32_t cn = 0, ct = 0, cc = 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const float4 o = qo[k], d = qd[k];
-        const TraceHit h = trace_bvh8<false, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits,
-                                                    blockDim.x, nullptr, nullptr, &lerr);
+        TraceHit h;
+        if (kCount && (k & 63) == 0) {
+            h = trace_bvh8<false, true>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
+                                        &ct, &lerr);
+            cc++;
+        } else {
+            h = trace_bvh8<false, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
+                                         nullptr, nullptr, &lerr);
+        }
         hits[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.id));
+    }
+    if (kCount && cc) {
+        atomicAdd(sums + 0, (unsigned long long)cn);
+        atomicAdd(sums + 1, (unsigned long long)ct);
+        atomicAdd(sums + 2, (unsigned long long)cc);
     }
     if (lerr) atomicOr(err, lerr);
 }
 
-// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film.
+// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount as in
+// k_pt_extend, into sums[3..5].
+template <bool kCount>
 __global__ void __launch_bounds__(kBlock) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
-                                                      unsigned long long* rays, int* err) {
+                                                      unsigned long long* rays, int* err, unsigned long long* sums) {
     extern __shared__ uint32_t smem[];
     const int n = *scount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
     int lerr = 0;
+    uint32_t cn = 0, ct = 0, cc = 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const float4 o = sq.o[k], d = sq.d[k];
-        const TraceHit h = trace_bvh8<true, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits,
-                                                   blockDim.x, nullptr, nullptr, &lerr);
+        TraceHit h;
+        if (kCount && (k & 63) == 0) {
+            h = trace_bvh8<true, true>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
+                                       &ct, &lerr);
+            cc++;
+        } else {
+            h = trace_bvh8<true, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
+                                        nullptr, nullptr, &lerr);
+        }
         if (h.id < 0) {
             const float4 c = sq.c[k];
             splat(film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
         }
+    }
+    if (kCount && cc) {
+        atomicAdd(sums + 3, (unsigned long long)cn);
+        atomicAdd(sums + 4, (unsigned long long)ct);
+        atomicAdd(sums + 5, (unsigned long long)cc);
     }
     if (lerr) atomicOr(err, lerr);
 }
@@ -722,6 +752,7 @@ __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lm
 
 template <typename K>
 int grid_for(K kernel, int block, size_t smem) {
+    if (smem > 48 * 1024) LMGPU_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int per_sm = 0;
     LMGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem));
     return std::max(1, per_sm) * current_device().num_sms;
@@ -943,8 +974,8 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
             ds.tf = c.tf;
             ds.aspect = c.aspect;
         }
-        s->counters.alloc(64);
-        LMGPU_CUDA(cudaMemset(s->counters.p, 0, 64));
+        s->counters.alloc(128);
+        LMGPU_CUDA(cudaMemset(s->counters.p, 0, 128));
         *out = s.release();
     });
 }
@@ -1073,53 +1104,68 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         const Bvh8 bvh = s->dev.bvh;
         const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
 
+        const bool inst = prm->instrument != 0;
+        auto ext_k = inst ? k_pt_extend<true> : k_pt_extend<false>;
+        auto sh_k = inst ? k_pt_shadow<true> : k_pt_shadow<false>;
         const int g_gen = grid_for(k_pt_generate, kBlock, 0);
-        const int g_ext = grid_for(k_pt_extend, kBlock, tsmem);
-        const int g_sh = grid_for(k_pt_shadow, kBlock, tsmem);
+        const int g_ext = grid_for(ext_k, kBlock, tsmem);
+        const int g_sh = grid_for(sh_k, kBlock, tsmem);
         const int g_shade = grid_for(k_pt_shade, kBlock, 0);
+        unsigned long long* sums = reinterpret_cast<unsigned long long*>(s->counters.as<char>() + 64);
 
-        cudaEvent_t e0, e1;
-        LMGPU_CUDA(cudaEventCreate(&e0));
-        LMGPU_CUDA(cudaEventCreate(&e1));
-        std::vector<cudaEvent_t> tev;
-        const bool time_trace = stats != nullptr;
-        auto tmark = [&]() {
-            if (!time_trace) return;
+        // per-kernel device time: events bracket every launch when stats are requested
+        enum { K_GEN = 0, K_EXT = 1, K_SHADE = 2, K_SHADOW = 3 };
+        std::vector<std::pair<int, cudaEvent_t>> marks;
+        const bool timed = stats != nullptr;
+        auto mark = [&](int kind) {
+            if (!timed) return;
             cudaEvent_t e;
             LMGPU_CUDA(cudaEventCreate(&e));
             LMGPU_CUDA(cudaEventRecord(e, st));
-            tev.push_back(e);
+            marks.emplace_back(kind, e);
         };
+        cudaEvent_t e0, e1;
+        LMGPU_CUDA(cudaEventCreate(&e0));
+        LMGPU_CUDA(cudaEventCreate(&e1));
+        int64_t n_ext = 0, n_sh = 0;
 
         LMGPU_CUDA(cudaEventRecord(e0, st));
         if (!prm->accumulate) {
             LMGPU_CUDA(cudaMemsetAsync(film, 0, size_t(npix) * 3 * 4, st));
             f->accumulated_spp = 0;
         }
-        LMGPU_CUDA(cudaMemsetAsync(s->counters.p, 0, 64, st));
+        LMGPU_CUDA(cudaMemsetAsync(s->counters.p, 0, 128, st));
         for (int64_t start = 0; start < total; start += wave) {
             const int64_t n = std::min(wave, total - start);
             int cur = 0;
             LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
-            k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0], cnt + 0, sq, cnt + 2);
+            mark(K_GEN);
+            k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0],
+                                                                                               cnt + 0, sq, cnt + 2);
+            mark(-1);
             LMGPU_CUDA(cudaGetLastError());
             if (P.image) {
-                tmark();
-                k_pt_shadow<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3);
-                tmark();
+                mark(K_SHADOW);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums);
+                mark(-1);
+                n_sh++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
             }
             for (int it = 1; it < P.max_verts; it++) {
-                tmark();
-                k_pt_extend<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3);
-                tmark();
+                mark(K_EXT);
+                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3, sums);
+                mark(-1);
+                n_ext++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+                mark(K_SHADE);
                 k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, it, q[cur], s->hits.as<float4>(), cnt + cur, q[1 - cur],
                                                       cnt + (1 - cur), sq, cnt + 2, film);
-                tmark();
-                k_pt_shadow<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3);
-                tmark();
+                mark(-1);
+                mark(K_SHADOW);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums);
+                mark(-1);
+                n_sh++;
                 LMGPU_CUDA(cudaGetLastError());
                 cur = 1 - cur;
             }
@@ -1129,20 +1175,22 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         f->scale = scale;
         k_scale<<<1024, 256, 0, st>>>(film, f->out.as<float>(), npix * 3, float(scale));
         LMGPU_CUDA(cudaEventRecord(e1, st));
-        unsigned long long hr[2];
+        unsigned long long hr[2], hs[6];
         int herr = 0;
         LMGPU_CUDA(cudaMemcpyAsync(hr, rays, sizeof(hr), cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaMemcpyAsync(hs, sums, sizeof(hs), cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, 4, cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaStreamSynchronize(st));
         float ms = 0.f;
         LMGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        double tms = 0;
-        for (size_t i = 0; i + 1 < tev.size(); i += 2) {
+        double kms[4] = {0, 0, 0, 0};
+        for (size_t i = 0; i + 1 < marks.size(); i++) {
+            if (marks[i].first < 0) continue;
             float m = 0.f;
-            LMGPU_CUDA(cudaEventElapsedTime(&m, tev[i], tev[i + 1]));
-            tms += m;
+            LMGPU_CUDA(cudaEventElapsedTime(&m, marks[i].second, marks[i + 1].second));
+            kms[marks[i].first] += m;
         }
-        for (auto e : tev) cudaEventDestroy(e);
+        for (auto& e : marks) cudaEventDestroy(e.second);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
@@ -1152,7 +1200,17 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             stats->shadow_rays = int64_t(hr[1]);
             stats->rays = int64_t(hr[0] + hr[1]);
             stats->elapsed_ms = ms;
-            stats->trace_ms = tms;
+            stats->generate_ms = kms[K_GEN];
+            stats->extend_ms = kms[K_EXT];
+            stats->shade_ms = kms[K_SHADE];
+            stats->shadow_ms = kms[K_SHADOW];
+            stats->trace_ms = kms[K_EXT] + kms[K_SHADOW];
+            stats->extend_launches = n_ext;
+            stats->shadow_launches = n_sh;
+            stats->ext_nodes = hs[2] ? double(hs[0]) / double(hs[2]) : 0.0;
+            stats->ext_tris = hs[2] ? double(hs[1]) / double(hs[2]) : 0.0;
+            stats->shadow_nodes = hs[5] ? double(hs[3]) / double(hs[5]) : 0.0;
+            stats->shadow_tris = hs[5] ? double(hs[4]) / double(hs[5]) : 0.0;
         }
     });
 }

@@ -57,12 +57,15 @@ class RaycastParams(C.Structure):
 class PTParams(C.Structure):
     _fields_ = [("spp", C.c_int64), ("max_verts", C.c_int32), ("seed", C.c_uint32), ("sampling_mode", C.c_int32),
                 ("primary_mode", C.c_int32), ("wave_paths", C.c_int64), ("accumulate", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("instrument", C.c_int32)]
 
 
 class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("rays", C.c_int64), ("extension_rays", C.c_int64), ("shadow_rays", C.c_int64),
-                ("elapsed_ms", C.c_double), ("trace_ms", C.c_double)]
+                ("elapsed_ms", C.c_double), ("trace_ms", C.c_double), ("extend_ms", C.c_double),
+                ("shade_ms", C.c_double), ("shadow_ms", C.c_double), ("generate_ms", C.c_double),
+                ("extend_launches", C.c_int64), ("shadow_launches", C.c_int64), ("ext_nodes", C.c_double),
+                ("ext_tris", C.c_double), ("shadow_nodes", C.c_double), ("shadow_tris", C.c_double)]
 
 
 # (name, restype, argtypes) of every entry point include/lmgpu.h declares
