@@ -114,6 +114,14 @@ def build_scene():
     return lm, scene, film, info
 
 
+def _apply_overrides(args) -> None:
+    """--width/--height/--spp shrink the frame for profiling captures (same scene)."""
+    global W_PX, H_PX, SPP
+    W_PX = args.width or W_PX
+    H_PX = args.height or H_PX
+    SPP = args.spp or SPP
+
+
 def cpu_port(scene, spp: int, threads: int = 0):
     """Times the CPU restatement (fp64, reference RNG stream) on one render of `spp`."""
     from oracle import oracle as O
@@ -180,6 +188,7 @@ def run_gpu(args) -> None:
         p.sampling_mode = 2
         p.primary_mode = 0
         p.instrument = instrument
+        p.wave_paths = args.wave
         return p
 
     # instrumented (untimed) pass: node / triangle visits per ray for the roofline's byte count
@@ -227,16 +236,18 @@ def run_gpu(args) -> None:
 
     # e2e through the public API: renderer.render() + film.buffer() per step
     r = lm.load_renderer("renderer", "pt", scene=scene, output=film, max_verts=MAX_VERTS, seed=SEED_RENDER,
-                         sampling_mode="mis", scheduler="sample", spp=SPP)
-    r.render()
-    film.buffer()
+                         sampling_mode="mis", scheduler="sample", spp=SPP, wave_paths=args.wave)
     e2e_rays, e2e_s = 0, 0.0
-    for k in range(max(1, args.steps)):
-        t = time.perf_counter()
-        out = r.render()
-        img = film.buffer_f32()
-        e2e_s += time.perf_counter() - t
-        e2e_rays += out["rays"]
+    img = film.buffer_f32()
+    if not args.skip_e2e:
+        r.render()
+        film.buffer()
+        for k in range(max(1, args.steps)):
+            t = time.perf_counter()
+            out = r.render()
+            img = film.buffer_f32()
+            e2e_s += time.perf_counter() - t
+            e2e_rays += out["rays"]
     d2h = img.nbytes
     h2d = C.sizeof(N.PTParams)
 
@@ -277,7 +288,7 @@ def run_gpu(args) -> None:
                "sample": f"{W_PX}x{H_PX} at 1 spp ({W_PX * H_PX} paths, {crays} rays, {csec:.1f} s)",
                "build_seconds": S.build_seconds}
 
-    waves = -(-(W_PX * H_PX * SPP) // (1 << 22))
+    waves = -(-(W_PX * H_PX * SPP) // (args.wave or (1 << 22)))
     launches_per_step = waves * (1 + 3 * (MAX_VERTS - 1)) + 1
     if rank == 0:
         out = {
@@ -291,8 +302,8 @@ def run_gpu(args) -> None:
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "rays_per_step": tot["rays"] / max(1, args.steps),
             "kernel_ms_per_step": {k: v / max(1, args.steps) for k, v in kern.items()},
-            "e2e": {"value": e2e_rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+            "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else None, "unit": "Mrays/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
                          "traffic": traffic, "bytes_per_ray": {"extend": b_ext, "shadow": b_sh},
@@ -332,7 +343,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="lmgpu", choices=["lmgpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--skip-e2e", action="store_true", help="skip the end-to-end API pass (profiling runs)")
+    ap.add_argument("--width", type=int, default=0)
+    ap.add_argument("--height", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0)
+    ap.add_argument("--wave", type=int, default=0, help="paths in flight per wave (0 = library default)")
     args = ap.parse_args()
+    _apply_overrides(args)
     if args.impl == "reference":
         run_reference(args)
     else:
