@@ -245,6 +245,26 @@ typedef struct lmgpu_render_stats {
 int lmgpu_render_pt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params, void* stream,
                     lmgpu_render_stats* stats);
 
+/* No counterpart in the reference. renderer::pt for callers that must not allocate device memory:
+ * code that renders while a CUDA graph is being captured (cudaMalloc is not a capturable call),
+ * hosts that hand every byte of HBM to their own pool allocator and forbid libraries from calling
+ * cudaMalloc/cudaFree behind their back, and latency-bound loops that cannot afford the allocator's
+ * implicit synchronization. It renders exactly like lmgpu_render_pt, but its wavefront queues live
+ * in one file-scope device array of fixed size (about 6.5 MiB, held by every GPU that loads the
+ * library until the process exits) instead of buffers the library allocates, so at most
+ * LMGPU_NOALLOC_MAX_WAVE paths are in flight per wave (params->wave_paths = 0 picks that size;
+ * larger values are rejected with LMGPU_ERR_INVALID_ARGUMENT). The scene must already be created.
+ * The caller passes the output: d_film, a device buffer of h x w x 3 floats, which receives the
+ * estimate scaled by 1/spp (pixel mode) or w*h/spp (image mode); params->accumulate must be 0.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress) and
+ * caches it; make that first call before any stream capture begins. Every call shares the one
+ * array and clears what must start at zero, so calls whose work overlaps on the GPU (different
+ * streams, or concurrent host threads) race: serialize them. The call enqueues on `stream` and
+ * waits for it, and calls no cudaMalloc, cudaFree or other allocating routine. */
+#define LMGPU_NOALLOC_MAX_WAVE 32768
+int lmgpu_render_pt_noalloc(lmgpu_scene* scene, float* d_film, int32_t w, int32_t h, const lmgpu_pt_params* params,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

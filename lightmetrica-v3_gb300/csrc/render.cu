@@ -8,6 +8,8 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
+#include <string>
 
 #include "lmgpu_dev.cuh"
 #include "runtime.h"
@@ -1212,6 +1214,143 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             stats->shadow_nodes = hs[5] ? double(hs[3]) / double(hs[5]) : 0.0;
             stats->shadow_tris = hs[5] ? double(hs[4]) / double(hs[5]) : 0.0;
         }
+    });
+}
+
+// ---------------------------------------------------------------------------------------------
+// renderer::pt without device allocation (lmgpu_render_pt_noalloc): the wavefront queues live in
+// one fixed file-scope device array instead of library-allocated buffers.
+
+}  // extern "C"
+
+namespace lmgpu {
+namespace {
+
+// Bytes per in-flight path: two extension queues (origin, direction, throughput, normal: 4 x 16 B,
+// ids 8 B), hits 16 B, shadow queue 3 x 16 B.
+constexpr size_t kNoallocPerPath = 2 * (4 * 16 + 8) + 16 + 3 * 16;
+constexpr size_t kNoallocCounters = 256;
+constexpr size_t kNoallocBytes = kNoallocCounters + size_t(LMGPU_NOALLOC_MAX_WAVE) * kNoallocPerPath;
+
+// In host code this name is only a stand-in for the symbol; the device address comes from
+// cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64] = {nullptr};
+
+void* noalloc_scratch(int device) {
+    if (device < 0 || device >= 64) throw Error(LMGPU_ERR_UNSUPPORTED, "device ordinal above 63");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        LMGPU_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        if (!p) throw Error(LMGPU_ERR_CUDA, "cudaGetSymbolAddress returned a null scratch address");
+        g_noalloc_ptr[device] = p;
+    }
+    return g_noalloc_ptr[device];
+}
+
+}  // namespace
+}  // namespace lmgpu
+
+extern "C" {
+
+int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h, const lmgpu_pt_params* prm, void* stream) {
+    return guarded([&] {
+        if (!s || !d_film || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (w <= 0 || h <= 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid film size");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
+        if (prm->spp <= 0 || prm->max_verts < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "spp must be > 0 and max_verts >= 1");
+        if (prm->max_verts > 255) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 255");
+        if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
+        if (prm->accumulate) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "lmgpu_render_pt_noalloc does not accumulate (accumulate must be 0)");
+        if (prm->wave_paths < 0 || prm->wave_paths > LMGPU_NOALLOC_MAX_WAVE)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "wave_paths " + std::to_string(prm->wave_paths) +
+                                                        " exceeds LMGPU_NOALLOC_MAX_WAVE (" +
+                                                        std::to_string(LMGPU_NOALLOC_MAX_WAVE) + ")");
+        int device = 0;
+        LMGPU_CUDA(cudaGetDevice(&device));
+        char* base = static_cast<char*>(noalloc_scratch(device));
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int64_t npix = int64_t(w) * h;
+        const int64_t total = npix * prm->spp;
+        if (total > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "more than 2^32 paths in one render");
+        const int64_t cap = LMGPU_NOALLOC_MAX_WAVE;
+        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : cap, total);
+
+        // carve the fixed array: counters, then the per-path queues
+        int* cnt = reinterpret_cast<int*>(base);  // [0],[1] extension queues, [2] shadow queue, [3] error
+        unsigned long long* rays = reinterpret_cast<unsigned long long*>(base + 32);
+        unsigned long long* sums = reinterpret_cast<unsigned long long*>(base + 64);
+        char* p = base + kNoallocCounters;
+        auto take = [&](size_t per_path) {
+            char* r = p;
+            p += per_path * size_t(cap);
+            return r;
+        };
+        ExtQ q[2];
+        for (int b = 0; b < 2; b++) {
+            q[b].o = reinterpret_cast<float4*>(take(16));
+            q[b].d = reinterpret_cast<float4*>(take(16));
+            q[b].thr = reinterpret_cast<float4*>(take(16));
+            q[b].nrm = reinterpret_cast<float4*>(take(16));
+            q[b].ids = reinterpret_cast<uint2*>(take(8));
+        }
+        float4* hits = reinterpret_cast<float4*>(take(16));
+        ShadowQ sq;
+        sq.o = reinterpret_cast<float4*>(take(16));
+        sq.d = reinterpret_cast<float4*>(take(16));
+        sq.c = reinterpret_cast<float4*>(take(16));
+        if (size_t(p - base) > kNoallocBytes) throw Error(LMGPU_ERR_INTERNAL, "scratch layout exceeds the static array");
+
+        PtConst P;
+        P.seed = prm->seed;
+        P.max_verts = prm->max_verts;
+        P.spp = prm->spp;
+        P.mode = prm->sampling_mode;
+        P.image = prm->primary_mode == LMGPU_PRIMARY_IMAGE;
+        P.w = w;
+        P.h = h;
+        const Bvh8 bvh = s->dev.bvh;
+        const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
+        const int g_gen = grid_for(k_pt_generate, kBlock, 0);
+        const int g_ext = grid_for(k_pt_extend<false>, kBlock, tsmem);
+        const int g_sh = grid_for(k_pt_shadow<false>, kBlock, tsmem);
+        const int g_shade = grid_for(k_pt_shade, kBlock, 0);
+
+        LMGPU_CUDA(cudaMemsetAsync(d_film, 0, size_t(npix) * 3 * sizeof(float), st));
+        LMGPU_CUDA(cudaMemsetAsync(base, 0, kNoallocCounters, st));
+        for (int64_t start = 0; start < total; start += wave) {
+            const int64_t n = std::min(wave, total - start);
+            int cur = 0;
+            LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
+            k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0],
+                                                                                               cnt + 0, sq, cnt + 2);
+            if (P.image) {
+                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums);
+                LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+            }
+            for (int it = 1; it < P.max_verts; it++) {
+                k_pt_extend<false><<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, hits, rays, cnt + 3, sums);
+                LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
+                LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, it, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
+                                                      cnt + 2, d_film);
+                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums);
+                LMGPU_CUDA(cudaGetLastError());
+                cur = 1 - cur;
+            }
+        }
+        const double scale = P.image ? double(npix) / double(prm->spp) : 1.0 / double(prm->spp);
+        k_scale<<<1024, 256, 0, st>>>(d_film, d_film, npix * 3, float(scale));
+        LMGPU_CUDA(cudaGetLastError());
+        int herr = 0;
+        LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
     });
 }
 

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("lmgpu_film_device_ptr", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("lmgpu_render_raycast", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RaycastParams), C.c_void_p]),
     ("lmgpu_render_pt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.c_void_p, C.POINTER(RenderStats)]),
+    ("lmgpu_render_pt_noalloc", C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32, C.POINTER(PTParams), C.c_void_p]),
 ]
 
 ERROR_NAMES = {1: "InvalidArgument", 2: "Unsupported", 3: "Uninitialized", 4: "CUDA", 5: "OutOfMemory",
