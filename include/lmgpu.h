@@ -223,7 +223,8 @@ typedef struct lmgpu_pt_params {
     int32_t primary_mode;       /* LMGPU_PRIMARY_* ("pixel" is the reference default) */
     int64_t wave_paths;         /* paths in flight per wave; 0 = library default */
     int32_t accumulate;         /* 1: add to the film; the film's scale becomes 1 / (total spp) */
-    int32_t instrument;         /* 1: count node visits / triangle tests on every 64th traced ray */
+    int32_t instrument;         /* 1: count node visits / triangle tests on every 64th traced ray;
+                                   2: on every traced ray, and record the ray with the most visits */
 } lmgpu_pt_params;
 
 typedef struct lmgpu_render_stats {
@@ -237,6 +238,9 @@ typedef struct lmgpu_render_stats {
     int64_t extend_launches, shadow_launches;
     /* with params->instrument: mean 8-wide nodes visited / triangles tested per traced ray */
     double ext_nodes, ext_tris, shadow_nodes, shadow_tris;
+    /* with params->instrument == 2: the most nodes one ray visited, and that ray (o, tmin, d, tmax) */
+    int64_t ext_max_nodes, shadow_max_nodes;
+    float ext_worst_ray[8], shadow_worst_ray[8];
 } lmgpu_render_stats;
 
 /* Renders into `film` (cleared first unless params->accumulate) on `stream` and waits for it.

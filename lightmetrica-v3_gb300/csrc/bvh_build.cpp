@@ -150,43 +150,56 @@ struct Builder {
 inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
 inline float bitsf(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
 
-// Quantizes child boxes into the node frame with outward rounding. Returns false if the chosen
-// exponents cannot cover the node (the caller then retries with larger exponents).
-bool quantize(const AABB& nb, const AABB* cbox, const bool* valid, int nslots, const int* eb_in, int* eb_out,
-              uint8_t qlo[3][8], uint8_t qhi[3][8]) {
-    for (int a = 0; a < 3; a++) {
-        const float px = nb.lo[a];
-        int eb = eb_in[a];
-        for (;;) {
-            const float scale = bitsf(uint32_t(eb) << 23);
-            if (std::fmaf(255.f, scale, px) >= nb.hi[a] || eb >= 254) break;
-            eb++;
-        }
-        eb_out[a] = eb;
-        const float scale = bitsf(uint32_t(eb) << 23);
-        for (int s = 0; s < nslots; s++) {
-            if (!valid[s]) { qlo[a][s] = 0; qhi[a][s] = 0; continue; }
-            double fl = std::floor((double(cbox[s].lo[a]) - px) / scale);
-            double fh = std::ceil((double(cbox[s].hi[a]) - px) / scale);
-            int ql = int(std::min(255.0, std::max(0.0, fl)));
-            int qh = int(std::min(255.0, std::max(0.0, fh)));
-            while (ql > 0 && std::fmaf(float(ql), scale, px) > cbox[s].lo[a]) ql--;
-            while (qh < 255 && std::fmaf(float(qh), scale, px) < cbox[s].hi[a]) qh++;
-            if (std::fmaf(float(ql), scale, px) > cbox[s].lo[a]) return false;
-            if (std::fmaf(float(qh), scale, px) < cbox[s].hi[a]) return false;
-            qlo[a][s] = uint8_t(ql);
-            qhi[a][s] = uint8_t(qh);
-        }
+// Quantizes child boxes into the node frame. Per axis the frame is origin p and quantum
+// s = 2^(eb-127); plane q lies at the exact real value p + q*s. Every child gets a margin of at
+// least one quantum outside its exact box on both sides (qlo <= (lo - p)/s - 1, qhi >= (hi - p)/s
+// + 1), which the traversal's one-FMA slab test needs to stay conservative. The origin sits two
+// quanta below the node box so that the margins always fit in [0, 255].
+int exponent_for(double v) {  // smallest biased exponent eb with 2^(eb-127) >= v
+    if (!(v > 0)) return 1;
+    int e2;
+    const double m = std::frexp(v, &e2);  // v = m * 2^e2, m in [0.5, 1)
+    int eb = (m == 0.5 ? e2 - 1 : e2) + 127;
+    return std::min(254, std::max(1, eb));
+}
+
+bool quantize_axis(float lo, float hi, const AABB* cbox, const bool* valid, int a, int eb, float& origin,
+                   uint8_t* qlo, uint8_t* qhi) {
+    const double s = std::ldexp(1.0, eb - 127);
+    double pd = double(lo) - 2.0 * s;
+    float p = float(pd);
+    if (double(p) > pd) p = std::nextafter(p, -std::numeric_limits<float>::infinity());
+    if (!(double(p) < double(lo) - s)) return false;  // quantum below float resolution at lo
+    for (int k = 0; k < 8; k++) {
+        if (!valid[k]) { qlo[k] = 0; qhi[k] = 0; continue; }
+        const double l = (double(cbox[k].lo[a]) - double(p)) / s;
+        const double h = (double(cbox[k].hi[a]) - double(p)) / s;
+        const double ql = std::floor(l) - 1.0, qh = std::ceil(h) + 1.0;
+        if (ql < 0.0 || qh > 255.0) return false;
+        // margins re-checked in long double: plane + s stays at or below lo, plane - s at or above hi
+        const long double pl = (long double)p + (long double)ql * s, ph = (long double)p + (long double)qh * s;
+        if (pl + s > (long double)cbox[k].lo[a] || ph - s < (long double)cbox[k].hi[a]) return false;
+        qlo[k] = uint8_t(ql);
+        qhi[k] = uint8_t(qh);
     }
+    origin = p;
     return true;
 }
 
-int initial_exponent(float extent) {
-    if (!(extent > 0.f)) return 1;
-    int e2;
-    std::frexp(double(extent) / 255.0, &e2);  // extent/255 = m * 2^e2, m in [0.5, 1)
-    int eb = e2 + 127;
-    return std::min(254, std::max(1, eb));
+bool quantize(const AABB& nb, const AABB* cbox, const bool* valid, int eb_out[3], float origin[3], uint8_t qlo[3][8],
+              uint8_t qhi[3][8]) {
+    for (int a = 0; a < 3; a++) {
+        const double ext = double(nb.hi[a]) - double(nb.lo[a]);
+        const double mag = std::max(std::fabs(double(nb.lo[a])), std::fabs(double(nb.hi[a])));
+        int eb = std::max(exponent_for(ext / 251.0), exponent_for(mag * 1.2e-7));
+        bool ok = false;
+        for (; eb <= 254 && !ok; eb++) {
+            ok = quantize_axis(nb.lo[a], nb.hi[a], cbox, valid, a, eb, origin[a], qlo[a], qhi[a]);
+            if (ok) eb_out[a] = eb;
+        }
+        if (!ok) return false;
+    }
+    return true;
 }
 
 }  // namespace
@@ -344,20 +357,15 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
             }
         }
         // quantize
-        int eb0[3], eb[3];
-        for (int a = 0; a < 3; a++) eb0[a] = initial_exponent(nbox.hi[a] - nbox.lo[a]);
+        int eb[3];
+        float origin[3];
         uint8_t qlo[3][8], qhi[3][8];
-        bool ok = false;
-        for (int attempt = 0; attempt < 8 && !ok; attempt++) {
-            ok = quantize(nbox, cbox, valid, 8, eb0, eb, qlo, qhi);
-            if (!ok) for (int a = 0; a < 3; a++) eb0[a] = std::min(254, eb[a] + 1);
-        }
-        if (!ok) {
+        if (!quantize(nbox, cbox, valid, eb, origin, qlo, qhi)) {
             if (err) *err = "accel build: box quantization failed";
             return false;
         }
         uint32_t* w = &out.nodes[size_t(pd.wide) * 20];
-        w[0] = fbits(nbox.lo[0]); w[1] = fbits(nbox.lo[1]); w[2] = fbits(nbox.lo[2]);
+        w[0] = fbits(origin[0]); w[1] = fbits(origin[1]); w[2] = fbits(origin[2]);
         w[3] = uint32_t(eb[0]) | (uint32_t(eb[1]) << 8) | (uint32_t(eb[2]) << 16) | (uint32_t(imask) << 24);
         w[4] = child_base;
         w[5] = tri_base;

@@ -3,7 +3,8 @@
 // The reference builds a binary SAH BVH with a full sort per node (accel_sahbvh.cpp:127-267) and
 // walks it with a depth-first stack. Here a binned SAH binary tree is built on the host threads,
 // then collapsed into 8-wide nodes whose child boxes are quantized to 8 bits per plane relative to
-// the node frame and rounded outward, so a dequantized box always contains the exact child box.
+// the node frame and rounded outward with a margin of at least one quantum on every side, so each
+// dequantized box strictly contains the exact child box (the slab test relies on the margin).
 //
 // Node layout (80 bytes, five 16-byte words, read with vectorized loads):
 //   w0: px, py, pz (float bits)      | ex | ey<<8 | ez<<16 | imask<<24

@@ -115,16 +115,24 @@ __device__ inline uint32_t oct_permute(uint32_t m, uint32_t oct) {
 // Ray traversal of the 8-wide BVH. Closest hit: the smallest t over every triangle whose test
 // accepts the ray in [tmin, tmax], ties broken toward the smaller flattened index. Any hit
 // (`any_hit`): returns at the first accepted triangle. The per-thread stack of sibling groups
-// lives in shared memory: stk[i * stride] for i < bvh.depth. Child boxes are tested with the
-// plane positions the builder verified to enclose the exact boxes, and the far distance is
-// widened by (1 + 2^-21) (Ize 2013), so no triangle the exact test would accept is culled.
+// lives in shared memory: stk[i * stride] for i < bvh.depth. Child boxes carry a margin of one
+// quantum and the slab comparison widens by 2^-19 relative, which bounds the rounding of the
+// one-FMA slab distances (see the node visit below), so no triangle the exact test would accept
+// is culled.
 // Returns the number of visited nodes in *nodes_visited when non-null (instrumented builds).
 template <bool kAnyHit, bool kCount>
 __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, float tmax, uint32_t* stk_base,
                                       uint32_t* stk_bits, int stride, uint32_t* nodes_visited, uint32_t* tris_tested,
                                       int* err) {
     TraceHit best{tmax, 0.f, 0.f, -1};
-    const f3 inv = {1.0f / d.x, 1.0f / d.y, 1.0f / d.z};
+    // Slab reciprocals from a direction whose zero (or tiny) components are replaced by +-1e-20,
+    // keeping the sign: every slab distance stays finite (an exact zero would give infinities and
+    // then NaN in the one-FMA form, which would disable culling on that axis). The triangle test
+    // still uses the true direction.
+    const float dxs = fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x);
+    const float dys = fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y);
+    const float dzs = fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z);
+    const f3 inv = {1.0f / dxs, 1.0f / dys, 1.0f / dzs};
     const uint32_t oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
     int sp = 0;
     uint32_t node = 0;
@@ -135,11 +143,22 @@ __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, f
         const uint4* np = bvh.nodes + size_t(node) * 5;
         const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
         nvis++;
-        const float px = __uint_as_float(w0.x), py = __uint_as_float(w0.y), pz = __uint_as_float(w0.z);
+        // Slab distances with one FMA per plane. Plane q of an axis lies at p + q*s; with
+        // a = s*inv and b = (p - o)*inv, t = q*a + b. The byte is unpacked straight into the float
+        // X = 2^23 + 256*q (one byte permute), so t = fma(X, a/256, b - 2^15*a): the large offset
+        // cancels exactly inside the FMA. Error: about 5 ulp relative plus 0.003 quanta absolute;
+        // the builder leaves one quantum of margin around every child box and the comparison
+        // widens by 2^-19 relative, so the test never culls a box the exact ray enters.
         const float sx = __uint_as_float((w0.w & 0xffu) << 23);
         const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
         const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
         const uint32_t imask = w0.w >> 24;
+        const float ax = sx * inv.x, ay = sy * inv.y, az = sz * inv.z;
+        const float bx = (__uint_as_float(w0.x) - o.x) * inv.x;
+        const float by = (__uint_as_float(w0.y) - o.y) * inv.y;
+        const float bz = (__uint_as_float(w0.z) - o.z) * inv.z;
+        const float ax8 = ax * 0.00390625f, ay8 = ay * 0.00390625f, az8 = az * 0.00390625f;
+        const float bx8 = fmaf(-32768.0f, ax, bx), by8 = fmaf(-32768.0f, ay, by), bz8 = fmaf(-32768.0f, az, bz);
         // near/far plane bytes per axis, chosen by the ray's octant
         const uint32_t lx0 = w2.x, lx1 = w2.y, ly0 = w2.z, ly1 = w2.w, lz0 = w3.x, lz1 = w3.y;
         const uint32_t hx0 = w3.z, hx1 = w3.w, hy0 = w4.x, hy1 = w4.y, hz0 = w4.z, hz1 = w4.w;
@@ -152,18 +171,20 @@ __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, f
         uint32_t hitmask = 0;
 #pragma unroll
         for (int s = 0; s < 8; s++) {
-            const int k = s & 3;
-            const uint32_t mw = s < 4 ? w1.z : w1.w;
-            if (byte_of(mw, k) == 0u) continue;  // empty slot
-            const float qnx = float(byte_of(s < 4 ? nx0 : nx1, k)), qfx = float(byte_of(s < 4 ? fx0 : fx1, k));
-            const float qny = float(byte_of(s < 4 ? ny0 : ny1, k)), qfy = float(byte_of(s < 4 ? fy0 : fy1, k));
-            const float qnz = float(byte_of(s < 4 ? nz0 : nz1, k)), qfz = float(byte_of(s < 4 ? fz0 : fz1, k));
-            const float tnx = (fmaf(qnx, sx, px) - o.x) * inv.x, tfx = (fmaf(qfx, sx, px) - o.x) * inv.x;
-            const float tny = (fmaf(qny, sy, py) - o.y) * inv.y, tfy = (fmaf(qfy, sy, py) - o.y) * inv.y;
-            const float tnz = (fmaf(qnz, sz, pz) - o.z) * inv.z, tfz = (fmaf(qfz, sz, pz) - o.z) * inv.z;
-            const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
-            const float tf = fminf(fminf(tfx, tfy), fminf(tfz, best.t)) * 1.00000048f;
-            if (tn <= tf) hitmask |= 1u << s;
+            const uint32_t sel = 0x5404u | (uint32_t(s & 3) << 4);  // bytes: 00, q, 00, 4B
+            const float qnx = __uint_as_float(__byte_perm(s < 4 ? nx0 : nx1, 0x4B00u, sel));
+            const float qfx = __uint_as_float(__byte_perm(s < 4 ? fx0 : fx1, 0x4B00u, sel));
+            const float qny = __uint_as_float(__byte_perm(s < 4 ? ny0 : ny1, 0x4B00u, sel));
+            const float qfy = __uint_as_float(__byte_perm(s < 4 ? fy0 : fy1, 0x4B00u, sel));
+            const float qnz = __uint_as_float(__byte_perm(s < 4 ? nz0 : nz1, 0x4B00u, sel));
+            const float qfz = __uint_as_float(__byte_perm(s < 4 ? fz0 : fz1, 0x4B00u, sel));
+            const float tn0 = fmaxf(fmaxf(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8)), fmaf(qnz, az8, bz8));
+            const float tf0 = fminf(fminf(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8)), fminf(fmaf(qfz, az8, bz8), best.t));
+            // widen by 2^-19 relative: tn toward -inf, tf (positive when it matters) upward
+            const float tn = fmaxf(fmaf(-fabsf(tn0), 1.9073486e-6f, tn0), tmin);
+            const float tf = tf0 * 1.0000019f;
+            const bool used = byte_of(s < 4 ? w1.z : w1.w, s & 3) != 0u;
+            if (used && tn <= tf) hitmask |= 1u << s;
         }
         // ---- leaf children: test their triangles now -------------------------------------------
         uint32_t leaves = hitmask & ~imask;

@@ -448,6 +448,9 @@ struct PtConst {
 };
 
 constexpr int kBlock = 256;
+#ifndef LMGPU_TRACE_MINBLOCKS
+#define LMGPU_TRACE_MINBLOCKS 4  // resident 256-thread blocks per SM (5 and 6 spill and measured slower)
+#endif
 
 __device__ inline void rng_slots(uint32_t seed, uint64_t path, uint32_t vertex, int first_block, int nblocks, float* u) {
     for (int b = 0; b < nblocks; b++) {
@@ -550,12 +553,26 @@ __global__ void __launch_bounds__(kBlock) k_pt_generate(DevScene S, PtConst P, i
     }
 }
 
+// Instrumented runs: keeps the largest per-ray node count in *maxv and (racily, for diagnosis)
+// the ray that produced it in worst[0..7].
+__device__ inline void record_worst(unsigned long long* maxv, float* worst, uint32_t visits, float4 o, float4 d,
+                                    float tmin, float tmax) {
+    if (visits > *reinterpret_cast<volatile unsigned long long*>(maxv)) {
+        const unsigned long long prev = atomicMax(maxv, (unsigned long long)visits);
+        if (prev < visits) {
+            worst[0] = o.x; worst[1] = o.y; worst[2] = o.z; worst[3] = tmin;
+            worst[4] = d.x; worst[5] = d.y; worst[6] = d.z; worst[7] = tmax;
+        }
+    }
+}
+
 // Extension rays: closest hit over [Eps, Inf]. kCount: every 64th ray also counts node visits and
 // triangle tests into sums[0..2] (instrumented runs only).
 template <bool kCount>
-__global__ void __launch_bounds__(kBlock) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
+__global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       const int* __restrict__ qcount, float4* __restrict__ hits,
-                                                      unsigned long long* rays, int* err, unsigned long long* sums) {
+                                                      unsigned long long* rays, int* err, unsigned long long* sums,
+                                                      int count_mask, float* worst) {
     extern __shared__ uint32_t smem[];
     const int n = *qcount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
@@ -566,10 +583,12 @@ __global__ void __launch_bounds__(kBlock) k_pt_extend(Bvh8 bvh, const float4* __
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const float4 o = qo[k], d = qd[k];
         TraceHit h;
-        if (kCount && (k & 63) == 0) {
+        if (kCount && (k & count_mask) == 0) {
+            const uint32_t before = cn;
             h = trace_bvh8<false, true>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
                                         &ct, &lerr);
             cc++;
+            record_worst(sums + 6, worst, cn - before, o, d, kEps, kInf);
         } else {
             h = trace_bvh8<false, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
                                          nullptr, nullptr, &lerr);
@@ -587,8 +606,9 @@ __global__ void __launch_bounds__(kBlock) k_pt_extend(Bvh8 bvh, const float4* __
 // Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount as in
 // k_pt_extend, into sums[3..5].
 template <bool kCount>
-__global__ void __launch_bounds__(kBlock) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
-                                                      unsigned long long* rays, int* err, unsigned long long* sums) {
+__global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
+                                                      unsigned long long* rays, int* err, unsigned long long* sums,
+                                                      int count_mask, float* worst) {
     extern __shared__ uint32_t smem[];
     const int n = *scount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
@@ -599,10 +619,12 @@ __global__ void __launch_bounds__(kBlock) k_pt_shadow(Bvh8 bvh, ShadowQ sq, cons
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const float4 o = sq.o[k], d = sq.d[k];
         TraceHit h;
-        if (kCount && (k & 63) == 0) {
+        if (kCount && (k & count_mask) == 0) {
+            const uint32_t before = cn;
             h = trace_bvh8<true, true>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
                                        &ct, &lerr);
             cc++;
+            record_worst(sums + 7, worst + 8, cn - before, o, d, kEps, o.w);
         } else {
             h = trace_bvh8<true, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
                                         nullptr, nullptr, &lerr);
@@ -976,8 +998,8 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
             ds.tf = c.tf;
             ds.aspect = c.aspect;
         }
-        s->counters.alloc(128);
-        LMGPU_CUDA(cudaMemset(s->counters.p, 0, 128));
+        s->counters.alloc(192);
+        LMGPU_CUDA(cudaMemset(s->counters.p, 0, 192));
         *out = s.release();
     });
 }
@@ -1113,7 +1135,9 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
         const int g_shade = grid_for(k_pt_shade, kBlock, 0);
-        unsigned long long* sums = reinterpret_cast<unsigned long long*>(s->counters.as<char>() + 64);
+        unsigned long long* sums = reinterpret_cast<unsigned long long*>(s->counters.as<char>() + 64);  // 8 counters
+        float* worst = reinterpret_cast<float*>(s->counters.as<char>() + 128);                           // 2 rays
+        const int cmask = prm->instrument == 2 ? 0 : 63;
 
         // per-kernel device time: events bracket every launch when stats are requested
         enum { K_GEN = 0, K_EXT = 1, K_SHADE = 2, K_SHADOW = 3 };
@@ -1136,7 +1160,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             LMGPU_CUDA(cudaMemsetAsync(film, 0, size_t(npix) * 3 * 4, st));
             f->accumulated_spp = 0;
         }
-        LMGPU_CUDA(cudaMemsetAsync(s->counters.p, 0, 128, st));
+        LMGPU_CUDA(cudaMemsetAsync(s->counters.p, 0, 192, st));
         for (int64_t start = 0; start < total; start += wave) {
             const int64_t n = std::min(wave, total - start);
             int cur = 0;
@@ -1148,14 +1172,15 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             LMGPU_CUDA(cudaGetLastError());
             if (P.image) {
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
             }
             for (int it = 1; it < P.max_verts; it++) {
                 mark(K_EXT);
-                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3, sums);
+                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3, sums,
+                                                    cmask, worst);
                 mark(-1);
                 n_ext++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
@@ -1165,7 +1190,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
                                                       cnt + (1 - cur), sq, cnt + 2, film);
                 mark(-1);
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaGetLastError());
@@ -1177,10 +1202,12 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         f->scale = scale;
         k_scale<<<1024, 256, 0, st>>>(film, f->out.as<float>(), npix * 3, float(scale));
         LMGPU_CUDA(cudaEventRecord(e1, st));
-        unsigned long long hr[2], hs[6];
+        unsigned long long hr[2], hs[8];
+        float hw[16];
         int herr = 0;
         LMGPU_CUDA(cudaMemcpyAsync(hr, rays, sizeof(hr), cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaMemcpyAsync(hs, sums, sizeof(hs), cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaMemcpyAsync(hw, worst, sizeof(hw), cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, 4, cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaStreamSynchronize(st));
         float ms = 0.f;
@@ -1213,6 +1240,12 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             stats->ext_tris = hs[2] ? double(hs[1]) / double(hs[2]) : 0.0;
             stats->shadow_nodes = hs[5] ? double(hs[3]) / double(hs[5]) : 0.0;
             stats->shadow_tris = hs[5] ? double(hs[4]) / double(hs[5]) : 0.0;
+            stats->ext_max_nodes = int64_t(hs[6]);
+            stats->shadow_max_nodes = int64_t(hs[7]);
+            for (int i = 0; i < 8; i++) {
+                stats->ext_worst_ray[i] = hw[i];
+                stats->shadow_worst_ray[i] = hw[8 + i];
+            }
         }
     });
 }
@@ -1330,16 +1363,18 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
             k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0],
                                                                                                cnt + 0, sq, cnt + 2);
             if (P.image) {
-                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums);
+                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
             }
             for (int it = 1; it < P.max_verts; it++) {
-                k_pt_extend<false><<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, hits, rays, cnt + 3, sums);
+                k_pt_extend<false><<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, hits, rays, cnt + 3, sums,
+                                                                 63, nullptr);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, it, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
                                                       cnt + 2, d_film);
-                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums);
+                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63,
+                                                                nullptr);
                 LMGPU_CUDA(cudaGetLastError());
                 cur = 1 - cur;
             }

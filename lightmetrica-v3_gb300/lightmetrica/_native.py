@@ -65,7 +65,9 @@ class RenderStats(C.Structure):
                 ("elapsed_ms", C.c_double), ("trace_ms", C.c_double), ("extend_ms", C.c_double),
                 ("shade_ms", C.c_double), ("shadow_ms", C.c_double), ("generate_ms", C.c_double),
                 ("extend_launches", C.c_int64), ("shadow_launches", C.c_int64), ("ext_nodes", C.c_double),
-                ("ext_tris", C.c_double), ("shadow_nodes", C.c_double), ("shadow_tris", C.c_double)]
+                ("ext_tris", C.c_double), ("shadow_nodes", C.c_double), ("shadow_tris", C.c_double),
+                ("ext_max_nodes", C.c_int64), ("shadow_max_nodes", C.c_int64), ("ext_worst_ray", C.c_float * 8),
+                ("shadow_worst_ray", C.c_float * 8)]
 
 
 # (name, restype, argtypes) of every entry point include/lmgpu.h declares

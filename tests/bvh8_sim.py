@@ -44,8 +44,8 @@ def decode(w: np.ndarray) -> dict:
 
 
 def child_box(nd: dict, s: int):
-    """Dequantized planes: fmaf(q, scale, origin). q * scale is exact in fp32 (q < 256, scale a
-    power of two), so one fp32 addition gives the fused result."""
+    """Dequantized planes rounded to fp32: fmaf(q, scale, origin). q * scale is exact in fp32
+    (q < 256, scale a power of two), so one fp32 addition gives the fused result."""
     lo = [f32(nd["origin"][a] + f32(f32(nd["qlo"][a][s]) * nd["scale"][a])) for a in range(3)]
     hi = [f32(nd["origin"][a] + f32(f32(nd["qhi"][a][s]) * nd["scale"][a])) for a in range(3)]
     return lo, hi
@@ -92,8 +92,8 @@ def trace(nodes: np.ndarray, tris: np.ndarray, depth: int, ray: np.ndarray, any_
     o = tuple(f32(x) for x in ray[0:3])
     tmin = f32(ray[3])
     d = tuple(f32(x) for x in ray[4:7])
-    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
-        inv = tuple(f32(1.0) / x if x != 0 else f32(math.copysign(math.inf, x)) for x in d)
+    # the kernel's slab reciprocals: zero or tiny components become +-1e-20 (sign kept)
+    ds = tuple(x if abs(x) > 1e-20 else math.copysign(1e-20, x) for x in d)
     oct_ = sum((1 << a) for a in range(3) if math.copysign(1.0, d[a]) < 0)
     best_t, best_u, best_v, best_id = f32(ray[7]), f32(0), f32(0), -1
     stack = []
@@ -110,15 +110,17 @@ def trace(nodes: np.ndarray, tris: np.ndarray, depth: int, ray: np.ndarray, any_
         for s in range(8):
             if nd["meta"][s] == 0:
                 continue
-            lo, hi = child_box(nd, s)
+            # exact plane positions p + q*s (in double) with the kernel's 2^-19 widening
             tn, tf = [], []
             for a in range(3):
-                near, far = (hi[a], lo[a]) if (oct_ >> a) & 1 else (lo[a], hi[a])
-                with np.errstate(invalid="ignore", over="ignore"):
-                    tn.append(f32(f32(near - o[a]) * inv[a]))
-                    tf.append(f32(f32(far - o[a]) * inv[a]))
-            tnv = np.nanmax([*tn, tmin])
-            tfv = f32(np.nanmin([*tf, best_t]) * f32(1.00000048))
+                lo = float(nd["origin"][a]) + nd["qlo"][a][s] * float(nd["scale"][a])
+                hi = float(nd["origin"][a]) + nd["qhi"][a][s] * float(nd["scale"][a])
+                near, far = (hi, lo) if (oct_ >> a) & 1 else (lo, hi)
+                tn.append((near - float(o[a])) / float(ds[a]))
+                tf.append((far - float(o[a])) / float(ds[a]))
+            tn0 = max(tn) if tn else -math.inf
+            tnv = max(tn0 - abs(tn0) * 2.0 ** -19 if math.isfinite(tn0) else tn0, float(tmin))
+            tfv = min(tf + [float(best_t)]) * (1 + 2.0 ** -19)
             if tnv <= tfv:
                 hitmask |= 1 << s
         leaves = hitmask & ~nd["imask"]

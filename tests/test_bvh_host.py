@@ -55,6 +55,12 @@ def _check_structure(nodes, tris, tri_p):
             lo, hi = sim.child_box(nd, s)
             v = tri_p[tids].reshape(-1, 3)
             assert np.all(v.min(0) >= np.array(lo, np.float32)) and np.all(v.max(0) <= np.array(hi, np.float32))
+            # the exact planes p + q*s sit at least one quantum outside the exact bounds
+            for a in range(3):
+                sc = float(nd["scale"][a])
+                plo = float(nd["origin"][a]) + nd["qlo"][a][s] * sc
+                phi = float(nd["origin"][a]) + nd["qhi"][a][s] * sc
+                assert plo + sc <= float(v[:, a].min()) and phi - sc >= float(v[:, a].max())
         for s in range(8):
             if nd["meta"][s] == 0:
                 assert not (nd["imask"] >> s) & 1
@@ -122,3 +128,21 @@ def test_traversal_replica_matches_exhaustive(native_lib, oracle_mod):
         # any-hit agrees on occlusion
         occ = sim.trace(nodes, tris, depth, r, any_hit=True)[3] >= 0
         assert occ == (id_ref[i] >= 0)
+
+
+def test_axis_aligned_rays_stay_cheap(native_lib):
+    """Rays with exactly-zero direction components must be culled like any other ray: a straight-
+    down ray over a ground grid visits a handful of nodes, not the whole tree."""
+    from lightmetrica import synthetic as syn
+    ps, ns, f = syn.ground_grid(64, 1.0)
+    tri_p = ps[f].reshape(-1, 9).astype(np.float32)
+    nodes, tris, depth = sim.build_host(native_lib, tri_p)
+    rng = np.random.default_rng(0)
+    for d in ([0, -1, 0], [1, 0, 0], [0, 0, -1], [0.6, 0, 0.8]):
+        for _ in range(5):
+            o = [rng.uniform(-0.9, 0.9), 0.5 if d[1] else 0.0, rng.uniform(-0.9, 0.9)]
+            if d[1] == 0:
+                o[1] = 0.25  # above the grid, parallel to it: must not touch every node
+            ray = np.array([*o, 1e-3, *d, 1e10], np.float32)
+            t, u, v, tid, visited = sim.trace(nodes, tris, depth, ray)
+            assert visited <= 4 * depth + 16, (d, visited, len(nodes))

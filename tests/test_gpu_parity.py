@@ -389,3 +389,35 @@ def test_render_errors(lm):
     r = lm.load_renderer("pt", "pt", scene=scene, output=film, max_verts=5, scheduler="sample", spp=1)
     with pytest.raises(lm.LmGpuError):
         r.render()  # scene not built
+
+
+def test_axis_aligned_rays_visit_few_nodes(lm):
+    """Rays with exactly-zero direction components (straight down from a light, along a wall) are
+    culled like any other ray: counted on the GPU, they visit a handful of nodes, not the tree."""
+    from lightmetrica import _native as N
+    from lightmetrica import synthetic as syn
+    scene, film, info = syn.spheres_scene(n_spheres=6, subdiv=4, ground_quads=64, w=32, h=18)
+    scene._accel.build(scene)
+    rng = np.random.default_rng(9)
+    n = 4096
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0] = rng.uniform(-10, 10, n)
+    rays[:, 1] = 7.0
+    rays[:, 2] = rng.uniform(-10, 10, n)
+    rays[:, 3] = 1e-3
+    rays[:, 5] = -1.0            # d = (0, -1, 0) exactly
+    rays[:, 7] = 1e10
+    rays[n // 2:, 1] = 0.5       # second half: horizontal rays d = (1, 0, 0) exactly
+    rays[n // 2:, 4:7] = [1.0, 0.0, 0.0]
+    rt = _cudart()
+    d_rays = _dev_alloc(rt, rays.nbytes)
+    try:
+        _h2d(rt, d_rays, rays)
+        mn, mt = C.c_double(), C.c_double()
+        N.check(N.lib().lmgpu_accel_trace_counts(scene._accel._h, d_rays, n, 0, 1, C.byref(mn), C.byref(mt)))
+    finally:
+        rt.cudaFree(d_rays)
+    st = scene._accel.stats()
+    assert mn.value < 40, (mn.value, st["num_nodes"])
+    hits = scene._accel.intersect_batch(rays)
+    assert (hits["prim"][: n // 2] >= 0).all()  # every downward ray hits the ground
