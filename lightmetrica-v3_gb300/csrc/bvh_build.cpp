@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <limits>
 #include <omp.h>
 
@@ -105,7 +106,7 @@ struct Builder {
             }
         }
         const double split_cost = parea > 0 ? 1.0 + best_cost / parea : std::numeric_limits<double>::infinity();
-        if (count <= kMaxLeaf && (best_axis < 0 || double(count) <= split_cost)) return;  // leaf
+        (void)split_cost;  // the binary tree splits down to single triangles; the collapse picks leaves
 
         int mid = -1;
         if (best_axis >= 0 && depth < kMedianDepth) {
@@ -138,13 +139,6 @@ struct Builder {
             build(l + 1, mid, rcnt, depth + 1);
         }
     }
-
-    double sah(int32_t ni, double root_area) const {
-        const BinNode& b = nodes[ni];
-        const double rel = root_area > 0 ? b.box.area() / root_area : 0.0;
-        if (b.left < 0) return rel * b.count;
-        return rel + sah(b.left, root_area) + sah(b.right, root_area);
-    }
 };
 
 inline uint32_t fbits(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
@@ -171,7 +165,7 @@ bool quantize_axis(float lo, float hi, const AABB* cbox, const bool* valid, int 
     if (double(p) > pd) p = std::nextafter(p, -std::numeric_limits<float>::infinity());
     if (!(double(p) < double(lo) - s)) return false;  // quantum below float resolution at lo
     for (int k = 0; k < 8; k++) {
-        if (!valid[k]) { qlo[k] = 0; qhi[k] = 0; continue; }
+        if (!valid[k]) { qlo[k] = 255; qhi[k] = 0; continue; }  // inverted: no ray enters
         const double l = (double(cbox[k].lo[a]) - double(p)) / s;
         const double h = (double(cbox[k].hi[a]) - double(p)) / s;
         const double ql = std::floor(l) - 1.0, qh = std::ceil(h) + 1.0;
@@ -243,9 +237,65 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
     B.build(0, 0, int(n), 0);
     const int32_t nb = B.next.load();
     B.nodes.resize(nb);
-    out.sah_cost = B.sah(0, B.nodes[0].box.area());
 
-    // ---- collapse to 8-wide nodes, breadth first ------------------------------------------------
+    // ---- SAH-optimal collapse to 8-wide nodes (Ylitie, Karras & Laine, HPG 2017) ----------------
+    // cost[n][i-1]: cheapest way to represent binary subtree n with at most i slots of its parent:
+    //   i = 1: a leaf (at most kMaxLeaf triangles, cost A * c_prim * count) or a wide node
+    //          (A * c_node + the best split of its two children over 8 slots);
+    //   i > 1: the i-1 option, or the subtree's two children placed directly with k and i-k slots.
+    constexpr float kCNode = 1.0f, kCPrim = 0.3f;
+    const float inf = std::numeric_limits<float>::infinity();
+    std::vector<float> cost(size_t(nb) * 8);
+    std::vector<int8_t> dec(size_t(nb) * 8);  // i=1: 0 leaf / 1 node; i>1: 0 = as i-1, k = split
+    std::vector<int8_t> dnode(size_t(nb), 0);  // k of the node's own 8-slot split
+    for (int32_t ni = nb - 1; ni >= 0; ni--) {
+        const BinNode& b = B.nodes[ni];
+        const float A = float(b.box.area());
+        float* c = &cost[size_t(ni) * 8];
+        int8_t* d = &dec[size_t(ni) * 8];
+        const float cleaf = b.count <= kMaxLeaf ? A * kCPrim * float(b.count) : inf;
+        if (b.left < 0) {
+            for (int i = 0; i < 8; i++) { c[i] = cleaf; d[i] = 0; }
+            continue;
+        }
+        const float* cl = &cost[size_t(b.left) * 8];
+        const float* cr = &cost[size_t(b.right) * 8];
+        float dist[9];
+        int8_t dk[9];
+        for (int j = 2; j <= 8; j++) {
+            dist[j] = inf;
+            dk[j] = 1;
+            for (int k = 1; k < j; k++) {
+                const float v = cl[k - 1] + cr[j - k - 1];
+                if (v < dist[j]) { dist[j] = v; dk[j] = int8_t(k); }
+            }
+        }
+        const float cnode = A * kCNode + dist[8];
+        c[0] = std::min(cleaf, cnode);
+        d[0] = cleaf <= cnode ? 0 : 1;
+        dnode[ni] = dk[8];
+        for (int i = 2; i <= 8; i++) {
+            if (c[i - 2] <= dist[i]) { c[i - 1] = c[i - 2]; d[i - 1] = 0; }
+            else { c[i - 1] = dist[i]; d[i - 1] = dk[i]; }
+        }
+    }
+    {
+        const float ra = float(B.nodes[0].box.area());
+        out.sah_cost = ra > 0 ? double(cost[0]) / ra : 0.0;
+    }
+    struct Child { int32_t bin; bool leaf; };
+    // children of binary subtree m given i slots, appended to `out`
+    std::function<void(int32_t, int, std::vector<Child>&)> emit = [&](int32_t m, int i, std::vector<Child>& v) {
+        while (i > 1 && dec[size_t(m) * 8 + i - 1] == 0) i--;
+        if (i == 1) {
+            v.push_back({m, B.nodes[m].left < 0 || dec[size_t(m) * 8] == 0});
+            return;
+        }
+        const int k = dec[size_t(m) * 8 + i - 1];
+        emit(B.nodes[m].left, k, v);
+        emit(B.nodes[m].right, i - k, v);
+    };
+
     struct Pending { int32_t bin; int32_t wide; int32_t depth; };
     std::vector<Pending> queue;
     queue.push_back({0, 0, 1});
@@ -253,33 +303,28 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
     out.tris.reserve(size_t(12) * n);
     size_t qi = 0;
     int32_t max_depth = 1;
+    std::vector<Child> kids;
+    kids.reserve(8);
     while (qi < queue.size()) {
         const Pending pd = queue[qi++];
         max_depth = std::max(max_depth, pd.depth);
         // children of this wide node, as binary node indices
-        int32_t ch[8];
-        int nch = 0;
+        kids.clear();
         const BinNode& root = B.nodes[pd.bin];
-        if (root.count <= kMaxLeaf || root.left < 0) {
-            ch[nch++] = pd.bin;
+        if (root.left < 0 || (pd.bin == 0 && dec[0] == 0)) {
+            kids.push_back({pd.bin, true});  // the whole tree is one leaf
         } else {
-            ch[nch++] = root.left;
-            ch[nch++] = root.right;
-            while (nch < 8) {
-                int pick = -1;
-                double pa = -1;
-                for (int i = 0; i < nch; i++) {
-                    const BinNode& c = B.nodes[ch[i]];
-                    if (c.left < 0 || c.count <= kMaxLeaf) continue;
-                    const double a = c.box.area();
-                    if (a > pa) { pa = a; pick = i; }
-                }
-                if (pick < 0) break;
-                const BinNode& c = B.nodes[ch[pick]];
-                ch[pick] = c.left;
-                ch[nch++] = c.right;
-            }
+            emit(root.left, dnode[pd.bin], kids);
+            emit(root.right, 8 - dnode[pd.bin], kids);
         }
+        const int nch = int(kids.size());
+        if (nch < 1 || nch > 8) {
+            if (err) *err = "accel build: internal error (child count)";
+            return false;
+        }
+        int32_t ch[8];
+        bool is_leaf[8];
+        for (int i = 0; i < nch; i++) { ch[i] = kids[i].bin; is_leaf[i] = kids[i].leaf; }
         // octant-ordered slot assignment (greedy on dot(centroid - center, octant direction))
         AABB nbox; nbox.reset();
         for (int i = 0; i < nch; i++) nbox.grow(B.nodes[ch[i]].box);
@@ -328,7 +373,7 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
             const BinNode& c = B.nodes[ch[i]];
             valid[s] = true;
             cbox[s] = c.box;
-            if (c.left >= 0 && c.count > kMaxLeaf) {
+            if (!is_leaf[i]) {
                 imask |= uint8_t(1u << s);
                 meta[s] = 0x80;  // any nonzero value marks the slot as used
                 const int32_t wi = int32_t(out.nodes.size() / 20);
@@ -338,7 +383,7 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
         }
         for (int s = 0; s < 8; s++) {
             const int i = child_in[s];
-            if (i < 0 || (imask >> s) & 1) continue;
+            if (i < 0 || (imask >> s) & 1) continue;  // empty or internal
             const BinNode& c = B.nodes[ch[i]];
             const uint32_t off = uint32_t(out.tris.size() / 12) - tri_base;
             if (c.count < 1 || c.count > kMaxLeaf || off > 31) {

@@ -116,7 +116,7 @@ __device__ inline uint32_t oct_permute(uint32_t m, uint32_t oct) {
 // accepts the ray in [tmin, tmax], ties broken toward the smaller flattened index. Any hit
 // (`any_hit`): returns at the first accepted triangle. The per-thread stack of sibling groups
 // lives in shared memory: stk[i * stride] for i < bvh.depth. Child boxes carry a margin of one
-// quantum and the slab comparison widens by 2^-19 relative, which bounds the rounding of the
+// quantum and the slab comparison widens by 2^-18 relative, which bounds the rounding of the
 // one-FMA slab distances (see the node visit below), so no triangle the exact test would accept
 // is culled.
 // Returns the number of visited nodes in *nodes_visited when non-null (instrumented builds).
@@ -148,7 +148,7 @@ __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, f
         // X = 2^23 + 256*q (one byte permute), so t = fma(X, a/256, b - 2^15*a): the large offset
         // cancels exactly inside the FMA. Error: about 5 ulp relative plus 0.003 quanta absolute;
         // the builder leaves one quantum of margin around every child box and the comparison
-        // widens by 2^-19 relative, so the test never culls a box the exact ray enters.
+        // widens by 2^-18 relative, so the test never culls a box the exact ray enters.
         const float sx = __uint_as_float((w0.w & 0xffu) << 23);
         const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
         const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
@@ -178,13 +178,12 @@ __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, f
             const float qfy = __uint_as_float(__byte_perm(s < 4 ? fy0 : fy1, 0x4B00u, sel));
             const float qnz = __uint_as_float(__byte_perm(s < 4 ? nz0 : nz1, 0x4B00u, sel));
             const float qfz = __uint_as_float(__byte_perm(s < 4 ? fz0 : fz1, 0x4B00u, sel));
-            const float tn0 = fmaxf(fmaxf(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8)), fmaf(qnz, az8, bz8));
+            const float tn = fmaxf(fmaxf(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8)), fmaxf(fmaf(qnz, az8, bz8), tmin));
             const float tf0 = fminf(fminf(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8)), fminf(fmaf(qfz, az8, bz8), best.t));
-            // widen by 2^-19 relative: tn toward -inf, tf (positive when it matters) upward
-            const float tn = fmaxf(fmaf(-fabsf(tn0), 1.9073486e-6f, tn0), tmin);
-            const float tf = tf0 * 1.0000019f;
-            const bool used = byte_of(s < 4 ? w1.z : w1.w, s & 3) != 0u;
-            if (used && tn <= tf) hitmask |= 1u << s;
+            // Widening the far side by 2^-18 covers the relative error of both sides. Empty slots
+            // hold inverted boxes (qlo = 255, qhi = 0) that no ray enters; one accepted through
+            // rounding is a leaf of zero triangles.
+            if (tn <= tf0 * 1.0000038f) hitmask |= 1u << s;
         }
         // ---- leaf children: test their triangles now -------------------------------------------
         uint32_t leaves = hitmask & ~imask;

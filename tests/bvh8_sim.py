@@ -110,7 +110,7 @@ def trace(nodes: np.ndarray, tris: np.ndarray, depth: int, ray: np.ndarray, any_
         for s in range(8):
             if nd["meta"][s] == 0:
                 continue
-            # exact plane positions p + q*s (in double) with the kernel's 2^-19 widening
+            # exact plane positions p + q*s (in double) with the kernel's 2^-18 far-side widening
             tn, tf = [], []
             for a in range(3):
                 lo = float(nd["origin"][a]) + nd["qlo"][a][s] * float(nd["scale"][a])
@@ -118,9 +118,8 @@ def trace(nodes: np.ndarray, tris: np.ndarray, depth: int, ray: np.ndarray, any_
                 near, far = (hi, lo) if (oct_ >> a) & 1 else (lo, hi)
                 tn.append((near - float(o[a])) / float(ds[a]))
                 tf.append((far - float(o[a])) / float(ds[a]))
-            tn0 = max(tn) if tn else -math.inf
-            tnv = max(tn0 - abs(tn0) * 2.0 ** -19 if math.isfinite(tn0) else tn0, float(tmin))
-            tfv = min(tf + [float(best_t)]) * (1 + 2.0 ** -19)
+            tnv = max(max(tn), float(tmin))
+            tfv = min(tf + [float(best_t)]) * (1 + 2.0 ** -18)
             if tnv <= tfv:
                 hitmask |= 1 << s
         leaves = hitmask & ~nd["imask"]
