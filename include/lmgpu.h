@@ -249,6 +249,38 @@ typedef struct lmgpu_render_stats {
 int lmgpu_render_pt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params, void* stream,
                     lmgpu_render_stats* stats);
 
+/* ---------------------------------------------------------------------------------------------
+ * Shared wavefront for many jobs (no reference counterpart: the reference renders one job at a
+ * time). Each job is a built scene, a film and renderer::pt parameters; the paths of every job go
+ * through the same generate / extend / shade / shadow kernels, each carrying its job id, and
+ * paths that finish are replaced by new ones (from the same or the next job) until the queue is
+ * drained. A job's film receives exactly what lmgpu_render_pt gives for it alone (same Philox
+ * keys), up to the order of fp32 additions. Jobs may be submitted while earlier ones are still
+ * in flight (continuous batching).
+ */
+typedef struct lmgpu_batch lmgpu_batch;
+
+/* queue_paths: paths in flight (0 = 2^22). */
+int lmgpu_batch_create(lmgpu_batch** out, int64_t queue_paths);
+int lmgpu_batch_destroy(lmgpu_batch* batch);
+/* Appends a job; its paths follow those of earlier jobs. Without params->accumulate the film is
+ * cleared first. The scene and film must outlive the job. */
+int lmgpu_batch_submit(lmgpu_batch* batch, lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params,
+                       int32_t* job_id);
+/* Runs the wavefront for at most max_chunks chunks of 8 bounce iterations (max_chunks <= 0: until
+ * every submitted path is done) on `stream`, then refreshes the job progress the status call
+ * reports. *paths_left receives the paths still in flight or not yet started. */
+int lmgpu_batch_run(lmgpu_batch* batch, int32_t max_chunks, void* stream, int64_t* paths_left);
+/* Progress of a job as of the last lmgpu_batch_run: leading samples-per-pixel passes whose every
+ * pixel has finished, and whether the whole job is done. */
+int lmgpu_batch_job_status(const lmgpu_batch* batch, int32_t job, int32_t* passes_complete, int32_t* done);
+/* Rescales a finished job's film (as lmgpu_render_pt does at the end of a render). */
+int lmgpu_batch_resolve(lmgpu_batch* batch, int32_t job, void* stream);
+/* Cumulative rays traced and device time since creation or the last reset. */
+int lmgpu_batch_get_stats(const lmgpu_batch* batch, lmgpu_render_stats* out);
+/* Forgets every job (buffers stay allocated). */
+int lmgpu_batch_reset(lmgpu_batch* batch);
+
 /* No counterpart in the reference. renderer::pt for callers that must not allocate device memory:
  * code that renders while a CUDA graph is being captured (cudaMalloc is not a capturable call),
  * hosts that hand every byte of HBM to their own pool allocator and forbid libraries from calling

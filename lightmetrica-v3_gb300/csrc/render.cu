@@ -410,17 +410,20 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
 }
 
 // ---------------------------------------------------------------------------------------------
-// Film splats: lanes that hit the same pixel are summed first, one atomic per pixel and channel.
+// Film splats: lanes that hit the same pixel of the same film are summed first, one atomic per
+// pixel and channel. The lanes are grouped by the pixel's address, not its index: in a shared
+// wavefront the lanes of one warp can write different jobs' films.
 __device__ inline void splat(float* film, uint32_t pixel, f3 c) {
+    float* px = film + 3 * size_t(pixel);
     cg::coalesced_group g = cg::coalesced_threads();
-    cg::coalesced_group peers = cg::labeled_partition(g, pixel);
+    cg::coalesced_group peers = cg::labeled_partition(g, px);
     const float r = cg::reduce(peers, c.x, cg::plus<float>());
     const float gg = cg::reduce(peers, c.y, cg::plus<float>());
     const float b = cg::reduce(peers, c.z, cg::plus<float>());
     if (peers.thread_rank() == 0) {
-        atomicAdd(film + 3 * size_t(pixel), r);
-        atomicAdd(film + 3 * size_t(pixel) + 1, gg);
-        atomicAdd(film + 3 * size_t(pixel) + 2, b);
+        atomicAdd(px, r);
+        atomicAdd(px + 1, gg);
+        atomicAdd(px + 2, b);
     }
 }
 
@@ -431,12 +434,14 @@ struct ExtQ {
     float4* d;     // direction (w unused)
     float4* thr;   // throughput, pdf of the sampled direction (projected solid angle)
     float4* nrm;   // shading normal of the origin vertex, flags (bit 0 NEE-samplable, bit 1 camera, bits 8-15 vertex)
-    uint2* ids;    // path index, pixel
+    uint2* ids;    // path index (RNG key pixel * spp + sample), film pixel
+    uint32_t* job; // job of each entry (job-table mode only)
 };
 struct ShadowQ {
     float4* o;     // origin, tmax
     float4* d;
     float4* c;     // contribution, pixel
+    uint32_t* job; // job of each entry (job-table mode only)
 };
 struct PtConst {
     uint32_t seed;
@@ -445,6 +450,19 @@ struct PtConst {
     int32_t mode;      // LMGPU_SAMPLING_*
     int32_t image;     // 1: image primary-ray mode
     int32_t w, h;
+};
+// One job of a shared wavefront: its scene, renderer parameters and film. Its paths occupy
+// [path_begin, path_begin + npix * spp) of the wavefront's path space, enumerated sample-major
+// (all pixels of sample 0 first), so pass s of the job is complete when pass_done[pass_off + s]
+// reaches npix.
+struct JobDev {
+    DevScene S;
+    PtConst P;
+    float* film;
+    int64_t path_begin;
+    int64_t npix;
+    uint32_t pass_off;
+    uint32_t pad;
 };
 
 constexpr int kBlock = 256;
@@ -459,11 +477,13 @@ __device__ inline void rng_slots(uint32_t seed, uint64_t path, uint32_t vertex, 
     }
 }
 
-__device__ inline void push_shadow(const ShadowQ& sq, int* count, f3 o, f3 d, float tmax, f3 c, uint32_t pixel) {
+template <bool kBatched>
+__device__ inline void push_shadow(const ShadowQ& sq, int* count, f3 o, f3 d, float tmax, f3 c, uint32_t pixel, uint32_t job) {
     const int k = atomicAdd(count, 1);
     sq.o[k] = make_float4(o.x, o.y, o.z, tmax);
     sq.d[k] = make_float4(d.x, d.y, d.z, 0.f);
     sq.c[k] = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
+    if (kBatched) sq.job[k] = job;
 }
 
 __device__ inline uint32_t pixel_of(const PtConst& P, float rx, float ry) {
@@ -474,8 +494,9 @@ __device__ inline uint32_t pixel_of(const PtConst& P, float rx, float ry) {
 
 // NEE connection from vertex g (material m, or the camera if m == nullptr); pushes a shadow ray
 // with the contribution it carries when the connection is nonzero (renderer_pt.cpp:142-192).
+template <bool kBatched>
 __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, const DevMaterial* m, f3 wi, int comp, f3 thr,
-                           const float* u8, uint32_t pixel, const ShadowQ& sq, int* scount) {
+                           const float* u8, uint32_t pixel, const ShadowQ& sq, int* scount, uint32_t job) {
     LightSample sL;
     if (!sample_direct(S, g, u8, sL)) return;
     const f3 wo = -sL.wo;
@@ -509,47 +530,81 @@ __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, c
         dir = normalize(sL.gL.p - g.p);
         tmax = length(sL.gL.p - g.p) * (1.f - kEps);
     }
-    push_shadow(sq, scount, g.p, dir, tmax, C, px);
+    push_shadow<kBatched>(sq, scount, g.p, dir, tmax, C, px, job);
 }
 
+template <bool kBatched>
 __device__ inline void push_ext(const ExtQ& q, int* count, f3 o, f3 d, f3 thr, float pdf, f3 n, uint32_t flags, uint32_t path,
-                                uint32_t pixel) {
+                                uint32_t pixel, uint32_t job) {
     const int k = atomicAdd(count, 1);
     q.o[k] = make_float4(o.x, o.y, o.z, 0.f);
     q.d[k] = make_float4(d.x, d.y, d.z, 0.f);
     q.thr[k] = make_float4(thr.x, thr.y, thr.z, pdf);
     q.nrm[k] = make_float4(n.x, n.y, n.z, __uint_as_float(flags));
     q.ids[k] = make_uint2(path, pixel);
+    if (kBatched) q.job[k] = job;
 }
 
-// Camera vertex: renderer_pt.cpp:95-116 and the first pass of the loop (NEE in image mode, the
-// jittered primary direction, raster position caching).
-__global__ void __launch_bounds__(kBlock) k_pt_generate(DevScene S, PtConst P, int64_t start, int64_t count, ExtQ q,
-                                                        int* qcount, ShadowQ sq, int* scount) {
+// Camera vertex of one path: renderer_pt.cpp:95-116 and the first pass of the loop (NEE in image
+// mode, the jittered primary direction, raster position caching). `path` is the RNG key
+// pixel * spp + sample; `pix` the pixel whose window is sampled.
+template <bool kBatched>
+__device__ __forceinline__ void generate_path(const DevScene& S, const PtConst& P, uint64_t path, int64_t pix, const ExtQ& q,
+                                              int* qcount, const ShadowQ& sq, int* scount, uint32_t job) {
+    float wx = 0.f, wy = 0.f, ww = 1.f, wh = 1.f;
+    if (!P.image) {
+        const int x = int(pix % P.w), y = int(pix / P.w);
+        ww = 1.f / float(P.w);
+        wh = 1.f / float(P.h);
+        wx = ww * float(x);
+        wy = wh * float(y);
+    }
+    Geom g;
+    g.p = S.cam_p; g.n = mk(0, 0, 0); g.gn = g.n; g.u = g.n; g.v = g.n; g.wo = g.n;
+    g.degenerated = true; g.infinite = false;
+    const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && P.image;
+    float u[16];
+    rng_slots(P.seed, path, 1u, 0, 4, u);
+    if (nee_ok) nee<kBatched>(S, P, g, nullptr, mk(0, 0, 0), 0, mk(1, 1, 1), u, 0u, sq, scount, job);
+    const f3 d = primary_dir(S, wx + ww * u[8], wy + wh * u[9]);
+    float rx = 0.f, ry = 0.f;
+    raster_pos(S, d, rx, ry);
+    const uint32_t pixel = pixel_of(P, rx, ry);
+    const float pdf = nee_ok ? cam_pdf(S, d) : 0.f;
+    push_ext<kBatched>(q, qcount, S.cam_p, d, mk(1, 1, 1), pdf, mk(0, 0, 0), (nee_ok ? 1u : 0u) | 2u | (1u << 8),
+                       uint32_t(path), pixel, job);
+}
+
+// Single scene: paths [start, start + count) enumerated pixel-major (path = pixel * spp + sample).
+__global__ void __launch_bounds__(kBlock) k_pt_generate(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                        int64_t start, int64_t count, ExtQ q, int* qcount, ShadowQ sq,
+                                                        int* scount) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
         const uint64_t path = uint64_t(start + i);
-        const int64_t pix = int64_t(path / uint64_t(P.spp));
-        float wx = 0.f, wy = 0.f, ww = 1.f, wh = 1.f;
-        if (!P.image) {
-            const int x = int(pix % P.w), y = int(pix / P.w);
-            ww = 1.f / float(P.w);
-            wh = 1.f / float(P.h);
-            wx = ww * float(x);
-            wy = wh * float(y);
+        generate_path<false>(S, P, path, int64_t(path / uint64_t(P.spp)), q, qcount, sq, scount, 0u);
+    }
+}
+
+// Job table: a range of the shared path space, as chosen by k_wf_plan; each index maps to
+// (job, sample, pixel) with the job's sample-major enumeration.
+__global__ void __launch_bounds__(kBlock) k_wf_generate(const JobDev* __restrict__ jobs, const int64_t* __restrict__ job_begin,
+                                                        const int64_t* __restrict__ ctl, ExtQ q, int* qcount, ShadowQ sq,
+                                                        int* scount) {
+    // ctl[2], ctl[3]: the range chosen by k_wf_plan; ctl[5]: number of jobs (read here, not baked
+    // into a captured launch, so jobs submitted later are found)
+    const int64_t start = ctl[2], count = ctl[3];
+    const int njobs = int(ctl[5]);
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t gidx = start + i;
+        int lo = 0, hi = njobs;  // last job with job_begin <= gidx
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (job_begin[mid] <= gidx) lo = mid; else hi = mid;
         }
-        Geom g;
-        g.p = S.cam_p; g.n = mk(0, 0, 0); g.gn = g.n; g.u = g.n; g.v = g.n; g.wo = g.n;
-        g.degenerated = true; g.infinite = false;
-        const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && P.image;
-        float u[16];
-        rng_slots(P.seed, path, 1u, 0, 4, u);
-        if (nee_ok) nee(S, P, g, nullptr, mk(0, 0, 0), 0, mk(1, 1, 1), u, 0u, sq, scount);
-        const f3 d = primary_dir(S, wx + ww * u[8], wy + wh * u[9]);
-        float rx = 0.f, ry = 0.f;
-        raster_pos(S, d, rx, ry);
-        const uint32_t pixel = pixel_of(P, rx, ry);
-        const float pdf = nee_ok ? cam_pdf(S, d) : 0.f;
-        push_ext(q, qcount, S.cam_p, d, mk(1, 1, 1), pdf, mk(0, 0, 0), (nee_ok ? 1u : 0u) | 2u | (1u << 8), uint32_t(path), pixel);
+        const JobDev& J = jobs[lo];
+        const int64_t local = gidx - J.path_begin;
+        const int64_t sample = local / J.npix, pix = local - sample * J.npix;
+        generate_path<true>(J.S, J.P, uint64_t(pix * J.P.spp + sample), pix, q, qcount, sq, scount, uint32_t(lo));
     }
 }
 
@@ -566,13 +621,15 @@ __device__ inline void record_worst(unsigned long long* maxv, float* worst, uint
     }
 }
 
-// Extension rays: closest hit over [Eps, Inf]. kCount: every 64th ray also counts node visits and
-// triangle tests into sums[0..2] (instrumented runs only).
-template <bool kCount>
+// Extension rays: closest hit over [Eps, Inf]. kCount: rays with (k & count_mask) == 0 also count
+// node visits and triangle tests into sums[0..2] (instrumented runs only). kBatched: each entry
+// traverses its own job's BVH; bvh.depth is then the largest depth of the table (stack size).
+template <bool kCount, bool kBatched = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       const int* __restrict__ qcount, float4* __restrict__ hits,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
-                                                      int count_mask, float* worst) {
+                                                      int count_mask, float* worst, const JobDev* __restrict__ jobs = nullptr,
+                                                      const uint32_t* __restrict__ qjob = nullptr) {
     extern __shared__ uint32_t smem[];
     const int n = *qcount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
@@ -582,15 +639,16 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
     uint32_t cn = 0, ct = 0, cc = 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const float4 o = qo[k], d = qd[k];
+        const Bvh8& B = kBatched ? jobs[qjob[k]].S.bvh : bvh;
         TraceHit h;
         if (kCount && (k & count_mask) == 0) {
             const uint32_t before = cn;
-            h = trace_bvh8<false, true>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
+            h = trace_bvh8<false, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
                                         &ct, &lerr);
             cc++;
             record_worst(sums + 6, worst, cn - before, o, d, kEps, kInf);
         } else {
-            h = trace_bvh8<false, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
+            h = trace_bvh8<false, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
                                          nullptr, nullptr, &lerr);
         }
         hits[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.id));
@@ -603,12 +661,12 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
     if (lerr) atomicOr(err, lerr);
 }
 
-// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount as in
-// k_pt_extend, into sums[3..5].
-template <bool kCount>
+// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount and
+// kBatched as in k_pt_extend, counts into sums[3..5].
+template <bool kCount, bool kBatched = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
-                                                      int count_mask, float* worst) {
+                                                      int count_mask, float* worst, const JobDev* __restrict__ jobs = nullptr) {
     extern __shared__ uint32_t smem[];
     const int n = *scount;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
@@ -618,20 +676,22 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
     uint32_t cn = 0, ct = 0, cc = 0;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const float4 o = sq.o[k], d = sq.d[k];
+        const uint32_t job = kBatched ? sq.job[k] : 0u;
+        const Bvh8& B = kBatched ? jobs[job].S.bvh : bvh;
         TraceHit h;
         if (kCount && (k & count_mask) == 0) {
             const uint32_t before = cn;
-            h = trace_bvh8<true, true>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
+            h = trace_bvh8<true, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
                                        &ct, &lerr);
             cc++;
             record_worst(sums + 7, worst + 8, cn - before, o, d, kEps, o.w);
         } else {
-            h = trace_bvh8<true, false>(bvh, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
+            h = trace_bvh8<true, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
                                         nullptr, nullptr, &lerr);
         }
         if (h.id < 0) {
             const float4 c = sq.c[k];
-            splat(film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+            splat(kBatched ? jobs[job].film : film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
         }
     }
     if (kCount && cc) {
@@ -642,88 +702,129 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
     if (lerr) atomicOr(err, lerr);
 }
 
-// One pass of the loop body after the intersection (renderer_pt.cpp:221-300) for the hits of the
-// rays that vertex `it` emitted, then NEE and direction sampling at the new vertex it+1.
-__global__ void __launch_bounds__(kBlock) k_pt_shade(DevScene S, PtConst P, int it, ExtQ qi, const float4* __restrict__ hits,
+// One pass of the loop body after the intersection (renderer_pt.cpp:221-300) for one path whose
+// ray left vertex nv (flags bits 8-15), then NEE and direction sampling at the new vertex nv+1.
+// Returns false when the path ends here.
+template <bool kBatched>
+__device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, float* film, uint32_t job, float4 o4, float4 d4,
+                                           float4 t4, float4 n4, float4 h4, uint2 ids, const ExtQ& qo, int* qocount,
+                                           const ShadowQ& sq, int* scount) {
+    const uint32_t flags = __float_as_uint(n4.w);
+    const int it = int((flags >> 8) & 0xffu);
+    const bool prev_nee = flags & 1u;
+    const f3 d = mk(d4.x, d4.y, d4.z);
+    f3 thr = mk(t4.x, t4.y, t4.z);
+    const float prev_pdf = t4.w;
+    Geom gp;  // the vertex the ray left from
+    gp.p = mk(o4.x, o4.y, o4.z);
+    gp.n = mk(n4.x, n4.y, n4.z);
+    gp.degenerated = (flags & 2u) != 0;
+    gp.infinite = false;
+    const bool direct_ok = P.mode == LMGPU_SAMPLING_NEE ? !prev_nee : true;
+    const bool use_mis = P.mode != LMGPU_SAMPLING_NAIVE && prev_nee;
+    const int32_t id = __float_as_int(h4.w);
+    if (id < 0) {
+        // miss: the environment light endpoint (scene.cpp:321-331), then the env-hit break
+        if (S.env_light >= 0 && direct_ok) {
+            const DevLight L = S.lights[S.env_light];
+            const f3 gwo = -d;
+            float mis = 1.f;
+            if (use_mis) {
+                const float pl = (1.f / float(S.num_lights)) * env_pdf_direct(S, L, gp, gwo);
+                mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
+            }
+            const f3 C = thr * env_eval(S, L, gwo) * mis;
+            if (!is_zero(C)) splat(film, ids.y, C);
+        }
+        return false;
+    }
+    int32_t prim;
+    const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+    const int2 ml = __ldg(S.prim_ml + prim);
+    const f3 wi = -d;
+    if (ml.y >= 0 && direct_ok) {
+        const DevLight L = S.lights[ml.y];
+        const f3 woL = wi;
+        if (dot(woL, g.n) > 0.f) {
+            float mis = 1.f;
+            if (use_mis) {
+                const float pl = (1.f / float(S.num_lights)) * area_pdf_direct(L, gp, g, woL);
+                mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
+            }
+            const f3 C = thr * mk(L.ke[0], L.ke[1], L.ke[2]) * mis;
+            if (!is_zero(C)) splat(film, ids.y, C);
+        }
+    }
+    float u[16];
+    rng_slots(P.seed, ids.x, uint32_t(it), 3, 1, u + 12);
+    if (it > 5) {
+        const float qrr = fmaxf(.2f, 1.f - cmax(thr));
+        if (u[12] < qrr) return false;
+        thr = thr / (1.f - qrr);
+    }
+    const DevMaterial m = S.mats[ml.x];
+    int comp = 0;
+    if (m.type == LMGPU_MAT_GLASS) {
+        f3 wt; bool total; float eta, Fr;
+        glass_fresnel(m, g, wi, wt, total, eta, Fr);
+        comp = u[13] < Fr ? 0 : 1;
+        thr = thr * (1.f / (comp == 0 ? Fr : 1.f - Fr));
+    }
+    const int nv = it + 1;
+    if (nv >= P.max_verts) return false;
+    const bool spec = mat_specular(m);
+    const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && !spec;
+    rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
+    if (nee_ok) nee<kBatched>(S, P, g, &m, wi, comp, thr, u, ids.y, sq, scount, job);
+    f3 wo, w;
+    if (!mat_sample(m, g, wi, comp, u[8], u[9], wo, w)) return false;
+    w = w * sn_correction(g, wi, wo);
+    const float pdf = (P.mode == LMGPU_SAMPLING_MIS && nee_ok) ? mat_pdf(m, g, wi, wo, true) : 0.f;
+    thr = thr * w;
+    push_ext<kBatched>(qo, qocount, g.p, wo, thr, pdf, g.n, (nee_ok ? 1u : 0u) | (uint32_t(nv) << 8), ids.x, ids.y, job);
+    return true;
+}
+
+__global__ void __launch_bounds__(kBlock) k_pt_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                     ExtQ qi, const float4* __restrict__ hits, const int* __restrict__ qicount,
+                                                     ExtQ qo, int* qocount, ShadowQ sq, int* scount, float* film) {
+    const int n = *qicount;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        shade_path<false>(S, P, film, 0u, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], qi.ids[k], qo, qocount, sq, scount);
+}
+
+// Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
+// counter (warp-aggregated per pass).
+__global__ void __launch_bounds__(kBlock) k_wf_shade(const JobDev* __restrict__ jobs, ExtQ qi, const float4* __restrict__ hits,
                                                      const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
-                                                     int* scount, float* film) {
+                                                     int* scount, unsigned int* pass_done) {
     const int n = *qicount;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const float4 o4 = qi.o[k], d4 = qi.d[k], t4 = qi.thr[k], n4 = qi.nrm[k], h4 = hits[k];
+        const uint32_t job = qi.job[k];
+        const JobDev& J = jobs[job];
         const uint2 ids = qi.ids[k];
-        const uint32_t flags = __float_as_uint(n4.w);
-        const bool prev_nee = flags & 1u;
-        const f3 d = mk(d4.x, d4.y, d4.z);
-        f3 thr = mk(t4.x, t4.y, t4.z);
-        const float prev_pdf = t4.w;
-        Geom gp;  // the vertex the ray left from
-        gp.p = mk(o4.x, o4.y, o4.z);
-        gp.n = mk(n4.x, n4.y, n4.z);
-        gp.degenerated = (flags & 2u) != 0;
-        gp.infinite = false;
-        const bool direct_ok = P.mode == LMGPU_SAMPLING_NEE ? !prev_nee : true;
-        const bool use_mis = P.mode != LMGPU_SAMPLING_NAIVE && prev_nee;
-        const int32_t id = __float_as_int(h4.w);
-        if (id < 0) {
-            // miss: the environment light endpoint (scene.cpp:321-331), then the env-hit break
-            if (S.env_light >= 0 && direct_ok) {
-                const DevLight L = S.lights[S.env_light];
-                const f3 gwo = -d;
-                float mis = 1.f;
-                if (use_mis) {
-                    const float pl = (1.f / float(S.num_lights)) * env_pdf_direct(S, L, gp, gwo);
-                    mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
-                }
-                const f3 C = thr * env_eval(S, L, gwo) * mis;
-                if (!is_zero(C)) splat(film, ids.y, C);
-            }
-            continue;
+        const bool alive = shade_path<true>(J.S, J.P, J.film, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
+                                            qocount, sq, scount);
+        if (!alive) {
+            const uint32_t key = J.pass_off + uint32_t(uint64_t(ids.x) % uint64_t(J.P.spp));
+            cg::coalesced_group g = cg::coalesced_threads();
+            cg::coalesced_group peers = cg::labeled_partition(g, key);
+            if (peers.thread_rank() == 0) atomicAdd(pass_done + key, peers.size());
         }
-        int32_t prim;
-        const Geom g = surface_at(S, id, h4.y, h4.z, prim);
-        const int2 ml = __ldg(S.prim_ml + prim);
-        const f3 wi = -d;
-        if (ml.y >= 0 && direct_ok) {
-            const DevLight L = S.lights[ml.y];
-            const f3 woL = wi;
-            if (dot(woL, g.n) > 0.f) {
-                float mis = 1.f;
-                if (use_mis) {
-                    const float pl = (1.f / float(S.num_lights)) * area_pdf_direct(L, gp, g, woL);
-                    mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
-                }
-                const f3 C = thr * mk(L.ke[0], L.ke[1], L.ke[2]) * mis;
-                if (!is_zero(C)) splat(film, ids.y, C);
-            }
-        }
-        float u[16];
-        rng_slots(P.seed, ids.x, uint32_t(it), 3, 1, u + 12);
-        if (it > 5) {
-            const float qrr = fmaxf(.2f, 1.f - cmax(thr));
-            if (u[12] < qrr) continue;
-            thr = thr / (1.f - qrr);
-        }
-        const DevMaterial m = S.mats[ml.x];
-        int comp = 0;
-        if (m.type == LMGPU_MAT_GLASS) {
-            f3 wt; bool total; float eta, Fr;
-            glass_fresnel(m, g, wi, wt, total, eta, Fr);
-            comp = u[13] < Fr ? 0 : 1;
-            thr = thr * (1.f / (comp == 0 ? Fr : 1.f - Fr));
-        }
-        const int nv = it + 1;
-        if (nv >= P.max_verts) continue;
-        const bool spec = mat_specular(m);
-        const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && !spec;
-        rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
-        if (nee_ok) nee(S, P, g, &m, wi, comp, thr, u, ids.y, sq, scount);
-        f3 wo, w;
-        if (!mat_sample(m, g, wi, comp, u[8], u[9], wo, w)) continue;
-        w = w * sn_correction(g, wi, wo);
-        const float pdf = (P.mode == LMGPU_SAMPLING_MIS && nee_ok) ? mat_pdf(m, g, wi, wo, true) : 0.f;
-        thr = thr * w;
-        push_ext(qo, qocount, g.p, wo, thr, pdf, g.n, (nee_ok ? 1u : 0u) | (uint32_t(nv) << 8), ids.x, ids.y);
     }
+}
+
+// Device-side planner (one thread): how many new paths fit into the next queue, taken from the
+// path space in order. ctl: [0] next path, [1] total paths, [2..3] chosen range, [4] paths still
+// in flight or waiting (0 = done).
+__global__ void k_wf_plan(int64_t* ctl, const int* qcount, int64_t cap) {
+    const int64_t next = ctl[0], total = ctl[1];
+    const int64_t inq = *qcount;
+    const int64_t take = min(cap - inq, total - next);
+    ctl[2] = next;
+    ctl[3] = take > 0 ? take : 0;
+    ctl[0] = next + ctl[3];
+    ctl[4] = inq + (total - next);
 }
 
 __global__ void k_scale(const float* __restrict__ in, float* __restrict__ out, int64_t n, float s) {
@@ -1172,7 +1273,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             LMGPU_CUDA(cudaGetLastError());
             if (P.image) {
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, nullptr);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
@@ -1180,17 +1281,17 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             for (int it = 1; it < P.max_verts; it++) {
                 mark(K_EXT);
                 ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3, sums,
-                                                    cmask, worst);
+                                                    cmask, worst, nullptr, nullptr);
                 mark(-1);
                 n_ext++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 mark(K_SHADE);
-                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, it, q[cur], s->hits.as<float4>(), cnt + cur, q[1 - cur],
+                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], s->hits.as<float4>(), cnt + cur, q[1 - cur],
                                                       cnt + (1 - cur), sq, cnt + 2, film);
                 mark(-1);
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, nullptr);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaGetLastError());
@@ -1331,12 +1432,14 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
             q[b].thr = reinterpret_cast<float4*>(take(16));
             q[b].nrm = reinterpret_cast<float4*>(take(16));
             q[b].ids = reinterpret_cast<uint2*>(take(8));
+            q[b].job = nullptr;
         }
         float4* hits = reinterpret_cast<float4*>(take(16));
         ShadowQ sq;
         sq.o = reinterpret_cast<float4*>(take(16));
         sq.d = reinterpret_cast<float4*>(take(16));
         sq.c = reinterpret_cast<float4*>(take(16));
+        sq.job = nullptr;
         if (size_t(p - base) > kNoallocBytes) throw Error(LMGPU_ERR_INTERNAL, "scratch layout exceeds the static array");
 
         PtConst P;
@@ -1371,7 +1474,7 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
                                                                  63, nullptr);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
-                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, it, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
+                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
                                                       cnt + 2, d_film);
                 k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63,
                                                                 nullptr);
@@ -1386,6 +1489,325 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
         LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaStreamSynchronize(st));
         if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Shared wavefront over many jobs (lmgpu_batch_*)
+
+struct lmgpu_batch {
+    int64_t cap = 0;
+    lmgpu::DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], q_job[2], hits, s_o, s_d, s_c, s_job;
+    lmgpu::DevBuf ctl;        // int64: next, total, range[2], remaining, njobs; then int counters, then u64 rays
+    lmgpu::DevBuf jobs, job_begin, pass_done;
+    size_t jobs_cap = 0, begin_cap = 0, pass_cap = 0;
+    std::vector<lmgpu::JobDev> host_jobs;
+    std::vector<int64_t> host_begin{0};
+    std::vector<lmgpu_film*> films;
+    std::vector<uint32_t> host_pass;      // mirror of pass_done after the last run
+    int64_t total = 0;
+    uint32_t passes = 0;
+    bool table_dirty = false;
+    int32_t max_depth = 1;
+    // captured chunk of iterations
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int32_t graph_depth = 0;
+    int cur = 0;
+    double elapsed_ms = 0;
+    ~lmgpu_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+namespace lmgpu {
+namespace {
+
+constexpr int kChunkIters = 8;  // even: the queue parity is the same at every chunk boundary
+
+// ctl layout (bytes): 0 next, 8 total, 16 range start, 24 range count, 32 remaining, 40 njobs,
+// 48 int counters [0],[1] extension queues, [2] shadow queue, [3] error; 64 u64 rays [2];
+// 80 u64 sums [8]
+int64_t* ctl64(lmgpu_batch* b) { return b->ctl.as<int64_t>(); }
+int* ctl_cnt(lmgpu_batch* b) { return reinterpret_cast<int*>(b->ctl.as<char>() + 48); }
+unsigned long long* ctl_rays(lmgpu_batch* b) { return reinterpret_cast<unsigned long long*>(b->ctl.as<char>() + 64); }
+unsigned long long* ctl_sums(lmgpu_batch* b) { return reinterpret_cast<unsigned long long*>(b->ctl.as<char>() + 80); }
+
+template <typename T>
+void grow_upload(DevBuf& buf, size_t& cap, const std::vector<T>& v, cudaStream_t st, bool& realloc) {
+    if (v.size() > cap) {
+        size_t c = std::max<size_t>(v.size(), 2 * cap);
+        if (c < 64) c = 64;
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        DevBuf nb;
+        nb.alloc(c * sizeof(T));
+        std::swap(buf.p, nb.p);
+        std::swap(buf.bytes, nb.bytes);
+        cap = c;
+        realloc = true;
+    }
+    if (!v.empty()) LMGPU_CUDA(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+}
+
+__global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
+    ctl[1] = total;
+    ctl[5] = njobs;
+}
+
+// Stream-ordered view of one chunk of iterations; captured into a graph.
+void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
+    const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
+    Bvh8 bmax{};
+    bmax.depth = b->max_depth;
+    const int g_ext = grid_for(k_pt_extend<false, true>, kBlock, tsmem);
+    const int g_sh = grid_for(k_pt_shadow<false, true>, kBlock, tsmem);
+    const int g_shade = grid_for(k_wf_shade, kBlock, 0);
+    const int g_gen = grid_for(k_wf_generate, kBlock, 0);
+    int* cnt = ctl_cnt(b);
+    const JobDev* jobs = b->jobs.as<JobDev>();
+    ExtQ q[2];
+    for (int i = 0; i < 2; i++)
+        q[i] = ExtQ{b->q_o[i].as<float4>(), b->q_d[i].as<float4>(), b->q_thr[i].as<float4>(), b->q_nrm[i].as<float4>(),
+                    b->q_ids[i].as<uint2>(), b->q_job[i].as<uint32_t>()};
+    ShadowQ sq{b->s_o.as<float4>(), b->s_d.as<float4>(), b->s_c.as<float4>(), b->s_job.as<uint32_t>()};
+    float4* hits = b->hits.as<float4>();
+    int cur = 0;
+    for (int it = 0; it < kChunkIters; it++) {
+        k_pt_extend<false, true><<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
+                                                               ctl_sums(b), 63, nullptr, jobs, q[cur].job);
+        LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
+        k_wf_shade<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
+                                               b->pass_done.as<unsigned int>());
+        k_pt_shadow<false, true><<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
+                                                              ctl_sums(b), 63, nullptr, jobs);
+        LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
+        k_wf_plan<<<1, 1, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap);
+        k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->job_begin.as<int64_t>(), ctl64(b), q[1 - cur], cnt + (1 - cur), sq,
+                                                cnt + 2);
+        cur = 1 - cur;
+    }
+}
+
+void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
+    if (b->exec && !realloc && b->graph_depth == b->max_depth) return;
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    cudaStream_t cs;
+    LMGPU_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    // warm-up query of grid sizes outside the capture (occupancy calls are not capturable work)
+    const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
+    (void)grid_for(k_pt_extend<false, true>, kBlock, tsmem);
+    (void)grid_for(k_pt_shadow<false, true>, kBlock, tsmem);
+    (void)grid_for(k_wf_shade, kBlock, 0);
+    (void)grid_for(k_wf_generate, kBlock, 0);
+    LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    try {
+        enqueue_chunk(b, cs);
+    } catch (...) {
+        cudaGraph_t g;
+        cudaStreamEndCapture(cs, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(cs);
+        throw;
+    }
+    LMGPU_CUDA(cudaStreamEndCapture(cs, &b->graph));
+    LMGPU_CUDA(cudaStreamDestroy(cs));
+    LMGPU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    b->graph_depth = b->max_depth;
+    (void)st;
+}
+
+}  // namespace
+}  // namespace lmgpu
+
+extern "C" {
+
+int lmgpu_batch_create(lmgpu_batch** out, int64_t queue_paths) {
+    return guarded([&] {
+        if (!out || queue_paths < 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid argument");
+        auto b = std::make_unique<lmgpu_batch>();
+        b->cap = queue_paths > 0 ? queue_paths : (int64_t(1) << 22);
+        if (b->cap > (int64_t(1) << 30)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "queue_paths above 2^30");
+        const size_t c = size_t(b->cap);
+        for (int i = 0; i < 2; i++) {
+            b->q_o[i].alloc(c * 16); b->q_d[i].alloc(c * 16); b->q_thr[i].alloc(c * 16); b->q_nrm[i].alloc(c * 16);
+            b->q_ids[i].alloc(c * 8); b->q_job[i].alloc(c * 4);
+        }
+        b->hits.alloc(c * 16);
+        b->s_o.alloc(2 * c * 16); b->s_d.alloc(2 * c * 16); b->s_c.alloc(2 * c * 16); b->s_job.alloc(2 * c * 4);
+        b->ctl.alloc(256);
+        LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
+        *out = b.release();
+    });
+}
+
+int lmgpu_batch_destroy(lmgpu_batch* b) {
+    return guarded([&] { delete b; });
+}
+
+int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, int32_t* job_id) {
+    return guarded([&] {
+        if (!b || !s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
+        if (prm->spp <= 0 || prm->max_verts < 1 || prm->max_verts > 255) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid spp or max_verts");
+        if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
+        const int64_t npix = int64_t(f->w) * f->h;
+        if (npix * prm->spp > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "more than 2^32 paths in one job");
+        if (b->host_jobs.size() >= size_t(1) << 30) throw Error(LMGPU_ERR_UNSUPPORTED, "too many jobs");
+        ensure_film(f);
+        if (!prm->accumulate) {
+            LMGPU_CUDA(cudaMemset(f->sum.p, 0, size_t(npix) * 3 * 4));
+            f->accumulated_spp = 0;
+        }
+        JobDev J{};
+        J.S = s->dev;
+        J.P.seed = prm->seed;
+        J.P.max_verts = prm->max_verts;
+        J.P.spp = prm->spp;
+        J.P.mode = prm->sampling_mode;
+        J.P.image = prm->primary_mode == LMGPU_PRIMARY_IMAGE;
+        J.P.w = f->w;
+        J.P.h = f->h;
+        J.film = f->sum.as<float>();
+        J.path_begin = b->total;
+        J.npix = npix;
+        J.pass_off = b->passes;
+        b->host_jobs.push_back(J);
+        b->films.push_back(f);
+        b->total += npix * prm->spp;
+        b->host_begin.back() = J.path_begin;
+        b->host_begin.push_back(b->total);
+        b->passes += uint32_t(prm->spp);
+        b->host_pass.resize(b->passes, 0);
+        b->max_depth = std::max(b->max_depth, s->dev.bvh.depth);
+        b->table_dirty = true;
+        if (job_id) *job_id = int32_t(b->host_jobs.size() - 1);
+    });
+}
+
+int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* paths_left) {
+    return guarded([&] {
+        if (!b) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "batch is null");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        bool realloc = false;
+        if (b->table_dirty) {
+            grow_upload(b->jobs, b->jobs_cap, b->host_jobs, st, realloc);
+            grow_upload(b->job_begin, b->begin_cap, b->host_begin, st, realloc);
+            // new pass counters start at zero; existing ones keep their device values
+            if (b->passes > b->pass_cap) {
+                LMGPU_CUDA(cudaStreamSynchronize(st));
+                size_t c = std::max<size_t>(size_t(b->passes), 2 * b->pass_cap);
+                DevBuf nb;
+                nb.alloc(c * 4);
+                LMGPU_CUDA(cudaMemset(nb.p, 0, c * 4));
+                if (b->pass_cap) LMGPU_CUDA(cudaMemcpy(nb.p, b->pass_done.p, b->pass_cap * 4, cudaMemcpyDeviceToDevice));
+                std::swap(b->pass_done.p, nb.p);
+                std::swap(b->pass_done.bytes, nb.bytes);
+                b->pass_cap = c;
+                realloc = true;
+            }
+            k_wf_set_total<<<1, 1, 0, st>>>(ctl64(b), b->total, int64_t(b->host_jobs.size()));
+            LMGPU_CUDA(cudaGetLastError());
+            b->table_dirty = false;
+        }
+        if (b->host_jobs.empty()) {
+            if (paths_left) *paths_left = 0;
+            return;
+        }
+        ensure_graph(b, st, realloc);
+        cudaEvent_t e0, e1;
+        LMGPU_CUDA(cudaEventCreate(&e0));
+        LMGPU_CUDA(cudaEventCreate(&e1));
+        LMGPU_CUDA(cudaEventRecord(e0, st));
+        int64_t left = 0;
+        int chunks = 0;
+        int herr = 0;
+        for (;;) {
+            LMGPU_CUDA(cudaGraphLaunch(b->exec, st));
+            chunks++;
+            LMGPU_CUDA(cudaMemcpyAsync(&left, ctl64(b) + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+            LMGPU_CUDA(cudaMemcpyAsync(&herr, ctl_cnt(b) + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
+            LMGPU_CUDA(cudaStreamSynchronize(st));
+            if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
+            if (left == 0 || (max_chunks > 0 && chunks >= max_chunks)) break;
+        }
+        LMGPU_CUDA(cudaEventRecord(e1, st));
+        LMGPU_CUDA(cudaMemcpyAsync(b->host_pass.data(), b->pass_done.p, size_t(b->passes) * 4, cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        LMGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        b->elapsed_ms += ms;
+        if (paths_left) *paths_left = left;
+    });
+}
+
+int lmgpu_batch_job_status(const lmgpu_batch* b, int32_t job, int32_t* passes_complete, int32_t* done) {
+    return guarded([&] {
+        if (!b || job < 0 || size_t(job) >= b->host_jobs.size()) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown job");
+        const JobDev& J = b->host_jobs[job];
+        int32_t k = 0;
+        while (k < J.P.spp && int64_t(b->host_pass[J.pass_off + k]) >= J.npix) k++;
+        if (passes_complete) *passes_complete = k;
+        if (done) {
+            int32_t all = 1;
+            for (int64_t s = 0; s < J.P.spp; s++)
+                if (int64_t(b->host_pass[J.pass_off + s]) < J.npix) { all = 0; break; }
+            *done = all;
+        }
+    });
+}
+
+int lmgpu_batch_resolve(lmgpu_batch* b, int32_t job, void* stream) {
+    return guarded([&] {
+        if (!b || job < 0 || size_t(job) >= b->host_jobs.size()) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown job");
+        const JobDev& J = b->host_jobs[job];
+        lmgpu_film* f = b->films[job];
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        f->accumulated_spp += J.P.spp;
+        const double scale = J.P.image ? double(J.npix) / double(f->accumulated_spp) : 1.0 / double(f->accumulated_spp);
+        f->scale = scale;
+        k_scale<<<256, 256, 0, st>>>(f->sum.as<float>(), f->out.as<float>(), J.npix * 3, float(scale));
+        LMGPU_CUDA(cudaGetLastError());
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int lmgpu_batch_get_stats(const lmgpu_batch* b, lmgpu_render_stats* out) {
+    return guarded([&] {
+        if (!b || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        std::memset(out, 0, sizeof(*out));
+        unsigned long long r[2];
+        LMGPU_CUDA(cudaMemcpy(r, reinterpret_cast<const char*>(b->ctl.p) + 64, sizeof(r), cudaMemcpyDeviceToHost));
+        out->paths = b->total;
+        out->extension_rays = int64_t(r[0]);
+        out->shadow_rays = int64_t(r[1]);
+        out->rays = int64_t(r[0] + r[1]);
+        out->elapsed_ms = b->elapsed_ms;
+    });
+}
+
+int lmgpu_batch_reset(lmgpu_batch* b) {
+    return guarded([&] {
+        if (!b) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "batch is null");
+        LMGPU_CUDA(cudaDeviceSynchronize());
+        b->host_jobs.clear();
+        b->films.clear();
+        b->host_begin.assign(1, 0);
+        b->host_pass.clear();
+        b->total = 0;
+        b->passes = 0;
+        b->max_depth = 1;
+        b->elapsed_ms = 0;
+        b->table_dirty = false;
+        LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
+        if (b->pass_cap) LMGPU_CUDA(cudaMemset(b->pass_done.p, 0, b->pass_cap * 4));
     });
 }
 

@@ -96,6 +96,14 @@ SIGNATURES = [
     ("lmgpu_film_device_ptr", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     ("lmgpu_render_raycast", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RaycastParams), C.c_void_p]),
     ("lmgpu_render_pt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.c_void_p, C.POINTER(RenderStats)]),
+    ("lmgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int64]),
+    ("lmgpu_batch_destroy", C.c_int, [C.c_void_p]),
+    ("lmgpu_batch_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.POINTER(C.c_int32)]),
+    ("lmgpu_batch_run", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)]),
+    ("lmgpu_batch_job_status", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("lmgpu_batch_resolve", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    ("lmgpu_batch_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
+    ("lmgpu_batch_reset", C.c_int, [C.c_void_p]),
     ("lmgpu_render_pt_noalloc", C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32, C.POINTER(PTParams), C.c_void_p]),
 ]
 

@@ -79,16 +79,17 @@ def cuboid(center, size, angle):
 # ---------------------------------------------------------------------------------------------
 # Box scene
 
-def box_scene(seed: int = 1234, w: int = 256, h: int = 256, accel: str = "sahbvh"):
-    """Closed Cornell-style box. Returns (scene, film)."""
+def box_scene(seed: int = 1234, w: int = 256, h: int = 256, accel: str = "sahbvh", prefix: str = ""):
+    """Closed Cornell-style box. Returns (scene, film). Asset names start with `prefix`, so several
+    scenes can be resident at once (loading an existing name replaces that asset)."""
     rng = np.random.default_rng(seed)
-    film = lm.load_film("film", "bitmap", w=w, h=h)
-    camera = lm.load_camera("camera", "pinhole", position=[0.5, 0.5, 0.99], center=[0.5, 0.5, 0.0], up=[0, 1, 0],
+    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
+    camera = lm.load_camera(prefix + "camera", "pinhole", position=[0.5, 0.5, 0.99], center=[0.5, 0.5, 0.0], up=[0, 1, 0],
                             vfov=30, aspect=w / h)
-    grey = lm.load_material("grey", "diffuse", Kd=[0.75, 0.75, 0.75])
-    red = lm.load_material("red", "diffuse", Kd=[0.75, 0.25, 0.25])
-    green = lm.load_material("green", "diffuse", Kd=[0.25, 0.75, 0.25])
-    black = lm.load_material("black", "diffuse", Kd=[0.0, 0.0, 0.0])
+    grey = lm.load_material(prefix + "grey", "diffuse", Kd=[0.75, 0.75, 0.75])
+    red = lm.load_material(prefix + "red", "diffuse", Kd=[0.75, 0.25, 0.25])
+    green = lm.load_material(prefix + "green", "diffuse", Kd=[0.25, 0.75, 0.25])
+    black = lm.load_material(prefix + "black", "diffuse", Kd=[0.0, 0.0, 0.0])
     up, down = (0, 1, 0), (0, -1, 0)
     a, b = 0.375, 0.625
     grey_quads = [
@@ -101,22 +102,22 @@ def box_scene(seed: int = 1234, w: int = 256, h: int = 256, accel: str = "sahbvh
         quad((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1)),       # back wall
         quad((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1), (0, 0, -1)),      # front wall
     ]
-    scene_accel = lm.load_accel("accel", accel)
-    scene = lm.load_scene("scene", "default", accel=scene_accel)
+    scene_accel = lm.load_accel(prefix + "accel", accel)
+    scene = lm.load_scene(prefix + "scene", "default", accel=scene_accel)
     scene.add_primitive(camera=camera)
-    m = load_mesh("walls", *merge(grey_quads))
+    m = load_mesh(prefix + "walls", *merge(grey_quads))
     scene.add_primitive(mesh=m, material=grey)
-    scene.add_primitive(mesh=load_mesh("left", *quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (1, 0, 0))), material=red)
-    scene.add_primitive(mesh=load_mesh("right", *quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0), (-1, 0, 0))), material=green)
+    scene.add_primitive(mesh=load_mesh(prefix + "left", *quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (1, 0, 0))), material=red)
+    scene.add_primitive(mesh=load_mesh(prefix + "right", *quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0), (-1, 0, 0))), material=green)
     # two inner boxes, placed and rotated from the seed
     tall = cuboid((0.33 + rng.uniform(-0.05, 0.05), 0.3, 0.33 + rng.uniform(-0.05, 0.05)), (0.28, 0.6, 0.28), rng.uniform(0.2, 0.5))
     short = cuboid((0.68 + rng.uniform(-0.05, 0.05), 0.15, 0.62 + rng.uniform(-0.05, 0.05)), (0.28, 0.3, 0.28), -rng.uniform(0.2, 0.5))
-    scene.add_primitive(mesh=load_mesh("tall", *tall), material=grey)
-    scene.add_primitive(mesh=load_mesh("short", *short), material=grey)
+    scene.add_primitive(mesh=load_mesh(prefix + "tall", *tall), material=grey)
+    scene.add_primitive(mesh=load_mesh(prefix + "short", *short), material=grey)
     # ceiling light, slightly below the ceiling plane, facing down
     ly = 1.0 - 1e-4
-    lmesh = load_mesh("light_mesh", *quad((a, ly, a), (b, ly, a), (b, ly, b), (a, ly, b), down))
-    light = lm.load_light("light", "area", Ke=[17, 17, 17], mesh=lmesh)
+    lmesh = load_mesh(prefix + "light_mesh", *quad((a, ly, a), (b, ly, a), (b, ly, b), (a, ly, b), down))
+    light = lm.load_light(prefix + "light", "area", Ke=[17, 17, 17], mesh=lmesh)
     scene.add_primitive(mesh=lmesh, material=black, light=light)
     return scene, film
 
@@ -208,17 +209,18 @@ SPHERES_CAMERA = dict(position=[0.0, 4.0, 15.0], center=[0.0, 0.6, 0.0], up=[0, 
 
 
 def spheres_scene(seed: int = 7, n_spheres: int = 40, subdiv: int = 6, ground_quads: int = 512, w: int = 1920,
-                  h: int = 1080, accel: str = "sahbvh", env_le: float = 0.3, half: float = 12.0):
-    """Displaced icospheres on a ground plane. Returns (scene, film, info dict)."""
+                  h: int = 1080, accel: str = "sahbvh", env_le: float = 0.3, half: float = 12.0, prefix: str = ""):
+    """Displaced icospheres on a ground plane. Returns (scene, film, info dict). Asset names start
+    with `prefix`."""
     rng = np.random.default_rng(seed)
-    film = lm.load_film("film", "bitmap", w=w, h=h)
-    camera = lm.load_camera("camera", "pinhole", aspect=w / h, **SPHERES_CAMERA)
-    scene = lm.load_scene("scene", "default", accel=lm.load_accel("accel", accel))
+    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
+    camera = lm.load_camera(prefix + "camera", "pinhole", aspect=w / h, **SPHERES_CAMERA)
+    scene = lm.load_scene(prefix + "scene", "default", accel=lm.load_accel(prefix + "accel", accel))
     scene.add_primitive(camera=camera)
     gp, gn, gf = ground_grid(ground_quads, half)
-    ground = lm.load_mesh("ground", "raw", ps=gp, ns=gn, ts=np.zeros((1, 2), np.float32),
+    ground = lm.load_mesh(prefix + "ground", "raw", ps=gp, ns=gn, ts=np.zeros((1, 2), np.float32),
                           fs={"p": gf.reshape(-1), "n": np.zeros(gf.size, np.int32), "t": np.zeros(gf.size, np.int32)})
-    scene.add_primitive(mesh=ground, material=lm.load_material("ground_mat", "diffuse", Kd=[0.6, 0.6, 0.6]))
+    scene.add_primitive(mesh=ground, material=lm.load_material(prefix + "ground_mat", "diffuse", Kd=[0.6, 0.6, 0.6]))
     kinds = np.array(["diffuse"] * int(round(0.5 * n_spheres)) + ["glossy"] * int(round(0.3 * n_spheres)))
     kinds = np.concatenate([kinds, np.array(["glass"] * (n_spheres - len(kinds)))])
     rng.shuffle(kinds)
@@ -232,28 +234,28 @@ def spheres_scene(seed: int = 7, n_spheres: int = 40, subdiv: int = 6, ground_qu
                 break
         centers.append((c, r))
         p, n, f = displaced_sphere(subdiv, c, r, 0.05, seed * 1000 + i)
-        mesh = lm.load_mesh(f"sphere{i}", "raw", ps=p, ns=n, ts=np.zeros((1, 2), np.float32),
+        mesh = lm.load_mesh(prefix + f"sphere{i}", "raw", ps=p, ns=n, ts=np.zeros((1, 2), np.float32),
                             fs={"p": f.reshape(-1), "n": f.reshape(-1), "t": np.zeros(f.size, np.int32)})
         if kinds[i] == "diffuse":
-            mat = lm.load_material(f"mat{i}", "diffuse", Kd=rng.uniform(0.2, 0.9, 3))
+            mat = lm.load_material(prefix + f"mat{i}", "diffuse", Kd=rng.uniform(0.2, 0.9, 3))
         elif kinds[i] == "glossy":
             rough = rng.uniform(0.05, 0.5)
-            mat = lm.load_material(f"mat{i}", "glossy", Ks=rng.uniform(0.5, 0.95, 3), ax=rough, ay=rough)
+            mat = lm.load_material(prefix + f"mat{i}", "glossy", Ks=rng.uniform(0.5, 0.95, 3), ax=rough, ay=rough)
         else:
-            mat = lm.load_material(f"mat{i}", "glass", Ni=1.5)
+            mat = lm.load_material(prefix + f"mat{i}", "glass", Ni=1.5)
         scene.add_primitive(mesh=mesh, material=mat)
         tris += f.shape[0]
-    black = lm.load_material("light_mat", "diffuse", Kd=[0, 0, 0])
+    black = lm.load_material(prefix + "light_mat", "diffuse", Kd=[0, 0, 0])
     for k in range(6):
         ang = 2 * math.pi * k / 6 + rng.uniform(-0.2, 0.2)
         cx, cz, y, s = 6.0 * math.cos(ang), 6.0 * math.sin(ang), rng.uniform(6.0, 8.0), 0.75
-        lmesh = load_mesh(f"light_mesh{k}", *quad((cx - s, y, cz - s), (cx + s, y, cz - s), (cx + s, y, cz + s),
+        lmesh = load_mesh(prefix + f"light_mesh{k}", *quad((cx - s, y, cz - s), (cx + s, y, cz - s), (cx + s, y, cz + s),
                                                   (cx - s, y, cz + s), (0, -1, 0)))
-        light = lm.load_light(f"light{k}", "area", Ke=list(rng.uniform(8.0, 16.0, 3)), mesh=lmesh)
+        light = lm.load_light(prefix + f"light{k}", "area", Ke=list(rng.uniform(8.0, 16.0, 3)), mesh=lmesh)
         scene.add_primitive(mesh=lmesh, material=black, light=light)
         tris += 2
     if env_le > 0:
-        scene.add_primitive(light=lm.load_light("env", "envconst", Le=[env_le, env_le, env_le * 1.1]))
+        scene.add_primitive(light=lm.load_light(prefix + "env", "envconst", Le=[env_le, env_le, env_le * 1.1]))
     return scene, film, {"triangles": tris, "spheres": n_spheres, "subdiv": subdiv, "ground_quads": ground_quads}
 
 
@@ -274,22 +276,22 @@ def sphere_rays(n: int, origin, seed: int = 11, tmin: float = 1e-3, tmax: float 
     return out
 
 
-def furnace_scene(material: str = "diffuse", w: int = 32, h: int = 32, subdiv: int = 3):
+def furnace_scene(material: str = "diffuse", w: int = 32, h: int = 32, subdiv: int = 3, prefix: str = ""):
     """White furnace: a unit sphere of albedo 1 (or glass) inside a constant environment of
     radiance 1. Every pixel's expected value is 1 for a convex diffuse sphere."""
-    film = lm.load_film("film", "bitmap", w=w, h=h)
-    camera = lm.load_camera("camera", "pinhole", position=[0, 0, 4], center=[0, 0, 0], up=[0, 1, 0], vfov=40, aspect=w / h)
-    scene = lm.load_scene("scene", "default", accel=lm.load_accel("accel", "sahbvh"))
+    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
+    camera = lm.load_camera(prefix + "camera", "pinhole", position=[0, 0, 4], center=[0, 0, 0], up=[0, 1, 0], vfov=40, aspect=w / h)
+    scene = lm.load_scene(prefix + "scene", "default", accel=lm.load_accel(prefix + "accel", "sahbvh"))
     scene.add_primitive(camera=camera)
     v, f = icosphere(subdiv)
-    mesh = lm.load_mesh("sphere", "raw", ps=v.astype(np.float32), ns=v.astype(np.float32), ts=np.zeros((1, 2), np.float32),
+    mesh = lm.load_mesh(prefix + "sphere", "raw", ps=v.astype(np.float32), ns=v.astype(np.float32), ts=np.zeros((1, 2), np.float32),
                         fs={"p": f.reshape(-1), "n": f.reshape(-1), "t": np.zeros(f.size, np.int32)})
     if material == "diffuse":
-        mat = lm.load_material("mat", "diffuse", Kd=[1, 1, 1])
+        mat = lm.load_material(prefix + "mat", "diffuse", Kd=[1, 1, 1])
     else:
-        mat = lm.load_material("mat", "glass", Ni=1.5)
+        mat = lm.load_material(prefix + "mat", "glass", Ni=1.5)
     scene.add_primitive(mesh=mesh, material=mat)
-    scene.add_primitive(light=lm.load_light("env", "envconst", Le=[1, 1, 1]))
+    scene.add_primitive(light=lm.load_light(prefix + "env", "envconst", Le=[1, 1, 1]))
     return scene, film
 
 

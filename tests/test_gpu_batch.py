@@ -1,0 +1,135 @@
+"""The shared wavefront (lmgpu_batch_*): every job's image is the same alone and in the mix, jobs
+admitted while others are in flight, progressive refinement, and the served request loop."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = dict(rtol=1e-5, atol=1e-6)  # the order of fp32 film additions is all that differs
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device(native_lib):
+    from lightmetrica import _native as N
+    N.check(native_lib.lmgpu_set_device(0))
+
+
+def _alone(lm, scene, film, **kw):
+    r = lm.load_renderer(f"pt_{id(film)}", "pt", scene=scene, output=film, scheduler="sample", **kw)
+    r.render()
+    return film.buffer_f32().copy()
+
+
+def _scenes(lm):
+    """Three unlike jobs: the box, the spheres (glossy/glass/env) and the box in image mode."""
+    from lightmetrica import synthetic as syn
+    out = []
+    s1, f1 = syn.box_scene(w=24, h=20, prefix="mixbox_")
+    s1.build()
+    out.append((s1, f1, dict(max_verts=9, spp=8, seed=3)))
+    s2, lm_film2, _ = syn.spheres_scene(n_spheres=5, subdiv=3, ground_quads=16, w=32, h=18, prefix="mixsph_")
+    s2.build()
+    out.append((s2, lm_film2, dict(max_verts=11, spp=4, seed=7)))
+    lm_film3 = lm.load_film("film3", "bitmap", w=24, h=20)
+    out.append((s1, lm_film3, dict(max_verts=6, spp=5, seed=11, primary_ray_sampling_mode="image")))
+    return out
+
+
+def test_each_job_same_alone_and_in_mix(lm):
+    from lightmetrica.serving import BatchRenderer
+    jobs = _scenes(lm)
+    alone = [_alone(lm, s, f, **kw) for s, f, kw in jobs]
+    b = BatchRenderer(queue_paths=1000)  # a small queue: paths of several jobs share it
+    ids = b.render([dict(scene=s, film=f, **kw) for s, f, kw in jobs])
+    for (s, f, kw), a, j in zip(jobs, alone, ids):
+        np.testing.assert_allclose(f.buffer_f32(), a, **TOL)
+        assert b.status(j) == (kw["spp"], True)
+    st = b.stats()
+    assert st["rays"] > 0 and st["paths"] == sum(f.w * f.h * kw["spp"] for _, f, kw in jobs)
+    b.close()
+
+
+def test_continuous_batching_admits_while_in_flight(lm):
+    """A job submitted after the wavefront started runs alongside the first and still matches its
+    standalone render."""
+    from lightmetrica.serving import BatchRenderer
+    jobs = _scenes(lm)
+    alone = [_alone(lm, s, f, **kw) for s, f, kw in jobs[:2]]
+    b = BatchRenderer(queue_paths=512)
+    j0 = b.submit(jobs[0][0], jobs[0][1], **jobs[0][2])
+    left = b.run(max_chunks=1)
+    assert left > 0
+    j1 = b.submit(jobs[1][0], jobs[1][1], **jobs[1][2])
+    b.run(0)
+    for j, (s, f, kw), a in zip((j0, j1), jobs[:2], alone):
+        assert b.status(j)[1]
+        b.resolve(j)
+        np.testing.assert_allclose(f.buffer_f32(), a, **TOL)
+    b.close()
+
+
+def test_progressive_refinement_accumulates(lm):
+    """+spp on a resident film: two passes equal one render with both passes' samples averaged."""
+    from lightmetrica import synthetic as syn
+    from lightmetrica.serving import BatchRenderer
+    s, f = syn.box_scene(w=16, h=16, prefix="refine_")
+    s.build()
+    a = _alone(lm, s, f, max_verts=9, spp=8, seed=1)
+    g = lm.load_film("g", "bitmap", w=16, h=16)
+    c = _alone(lm, s, g, max_verts=9, spp=8, seed=2)
+    b = BatchRenderer(queue_paths=2048)
+    h = lm.load_film("h", "bitmap", w=16, h=16)
+    j0 = b.submit(s, h, max_verts=9, spp=8, seed=1)
+    b.run(0)
+    b.resolve(j0)
+    j1 = b.submit(s, h, max_verts=9, spp=8, seed=2, accumulate=True)
+    b.run(0)
+    b.resolve(j1)
+    np.testing.assert_allclose(h.buffer_f32(), 0.5 * (a + c), rtol=1e-5, atol=2e-6)
+    b.close()
+
+
+def test_render_server_admission_and_latency(lm):
+    """Requests arriving over time under a small HBM budget: every request completes, scenes are
+    evicted when the budget demands, and refinements reuse the resident film."""
+    from lightmetrica import synthetic as syn
+    from lightmetrica.serving import RenderServer, Request
+
+    def make_scene(key):
+        s, _ = syn.box_scene(seed=key, w=8, h=8, prefix=f"served{key}_")
+        s.build()
+        return s
+    from lightmetrica.serving import scene_footprint
+    fps = []
+    for key in range(4):
+        probe, _ = syn.box_scene(seed=key, w=8, h=8, prefix=f"probe{key}_")
+        probe.build()
+        fps.append(scene_footprint(probe))
+    film = 16 * 12 * 3 * 4 * 2
+    # room for every film (ten; the refinement reuses one) and two and a half scenes: the four
+    # scenes cannot all stay resident, so some idle scene is evicted
+    budget = 2 * max(fps) + 10 * film + min(fps) // 2
+    assert 4 * min(fps) + 10 * film > budget
+    srv = RenderServer(make_scene, hbm_budget=budget, queue_paths=4096)
+    t0 = srv.clock()
+    reqs = []
+    for i in range(10):
+        reqs.append(Request(rid=i, arrival=t0, scene_key=i % 4, w=16, h=12, spp=4, max_verts=7, seed=i))
+    reqs.append(Request(rid=10, arrival=t0, scene_key=0, w=16, h=12, spp=4, max_verts=7, seed=99, refine=0))
+    for r in reqs:
+        srv.submit(r)
+    for _ in range(2000):
+        srv.step()
+        if srv.idle():
+            break
+    assert srv.idle()
+    assert len(srv.finished) == 11
+    lat = srv.latencies()
+    assert lat["ttfi_p50"] <= lat["done_p50"] and lat["done_p99"] >= lat["done_p50"]
+    assert srv.evictions > 0
+    assert srv.resident_bytes <= srv.budget
+    assert reqs[10].film is reqs[0].film
+    # a released film leaves the budget
+    before = srv.resident_bytes
+    srv.release(1)
+    assert srv.resident_bytes == before - film and reqs[1].film is None
