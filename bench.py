@@ -15,6 +15,18 @@ timed with CUDA events on the launching stream. `e2e` is the same metric through
 host memory every step). The scene (BVH, triangles, shading data: well above the 129 MB L2)
 stays resident; L2 is also flushed between timed steps with a 256 MB write.
 
+Two more legs (rank 0) report the batched and served forms (keys "batched" and "served"):
+
+* batched -- 256 procedural jobs (lightmetrica.synthetic.batch_jobs: random-triangle scenes of
+  1k-200k triangles, 64^2-512^2, 4-64 spp, path length 6-12), rendered job by job with
+  renderer::pt and then all at once through the shared wavefront (queue size autotuned on a
+  32-job probe). jobs/s = jobs / wall-clock seconds (host overhead included); the images of the
+  two forms are compared (same random streams, so the same estimate up to fp32 summation order).
+* served -- a Poisson stream of requests over the same scenes (30 % are +16 spp refinements of
+  earlier requests) at 80 % of the batched capacity just measured, through RenderServer under a
+  150 GB HBM budget; reports p50/p99 time-to-first-image (first complete sample pass) and
+  time-to-done from arrival.
+
 --impl reference times the CPU restatement of the reference's path (fp64 accel::sahbvh +
 renderer::pt with std::mt19937 per thread under OpenMP, all host cores) on a bounded sample of
 the same workload: one full-frame render at 1 spp per step. The reference itself cannot be built
@@ -314,10 +326,113 @@ def run_gpu(args) -> None:
             "accel": {"nodes": acc["num_nodes"], "depth": acc["max_depth"], "build_seconds": acc["build_seconds"],
                       "scene_build_seconds": build_s, "sah_cost": acc["sah_cost"]},
         }
+        if not args.no_batched:
+            out["batched"], ctx = run_batched(lm, args)
+            if args.served_requests > 0:
+                out["served"] = run_served(lm, args, ctx)
         print(json.dumps(out))
     cudart.cudaFree(flush)
     if dist:
         dist.destroy_process_group()
+
+
+def _batched_scenes(lm, n_jobs: int):
+    from lightmetrica import synthetic as syn
+    jobs = syn.batch_jobs(n_jobs)
+    scenes = []
+    t = time.perf_counter()
+    for i, j in enumerate(jobs):
+        s, f = syn.triangles_scene(j["scene_seed"], j["tris"], j["res"], j["res"], prefix=f"batch{i}_")
+        s.build()
+        scenes.append((s, f))
+    return jobs, scenes, time.perf_counter() - t
+
+
+def run_batched(lm, args) -> tuple[dict, dict]:
+    """Plain job-by-job renderer::pt vs the shared wavefront on the batched workload."""
+    import numpy as np
+    from lightmetrica.autotune import tune_queue
+    from lightmetrica.serving import BatchRenderer
+    jobs, scenes, build_s = _batched_scenes(lm, args.batched_jobs)
+    paths = sum(j["res"] ** 2 * j["spp"] for j in jobs)
+    # warm-up of both forms
+    s0, f0 = scenes[0]
+    lm.load_renderer("batch_warm", "pt", scene=s0, output=f0, max_verts=7, seed=1, spp=2, scheduler="sample").render()
+    # plain: one renderer::pt per job, in order
+    t = time.perf_counter()
+    plain_rays = 0
+    for i, (j, (s, f)) in enumerate(zip(jobs, scenes)):
+        r = lm.load_renderer(f"batch_r{i}", "pt", scene=s, output=f, max_verts=j["max_verts"], seed=j["seed"],
+                             spp=j["spp"], scheduler="sample")
+        plain_rays += r.render()["rays"]
+    plain_s = time.perf_counter() - t
+    plain_imgs = [f.buffer_f32().copy() for _, f in scenes]
+    films = [lm.load_film(f"batch_out{i}", "bitmap", w=j["res"], h=j["res"]) for i, j in enumerate(jobs)]
+    spec = [dict(scene=s, film=f2, max_verts=j["max_verts"], spp=j["spp"], seed=j["seed"])
+            for j, (s, _), f2 in zip(jobs, scenes, films)]
+    queue, tune = tune_queue(spec[: min(32, len(spec))])
+    b = BatchRenderer(queue_paths=queue)
+    b.submit(s0, films[0], max_verts=7, spp=1, seed=0)
+    b.run(0)
+    b.reset()
+    t = time.perf_counter()
+    b.render(spec)
+    batch_s = time.perf_counter() - t
+    st = b.stats()
+    b.close()
+    diff = 0.0
+    for f2, a in zip(films, plain_imgs):
+        diff = max(diff, float(np.max(np.abs(f2.buffer_f32() - a))) / (float(np.max(np.abs(a))) + 1e-12))
+    out = {
+        "workload": f"{len(jobs)} random-triangle scenes ({sum(j['tris'] for j in jobs)} triangles in all, 1k-200k "
+                    f"log-uniform), 64^2-512^2, spp 4-64, path length 6-12, MIS; {paths} paths",
+        "jobs": len(jobs), "paths": paths,
+        "plain": {"jobs_per_s": len(jobs) / plain_s, "seconds": plain_s, "Mrays_per_s": plain_rays / plain_s / 1e6},
+        "batched": {"jobs_per_s": len(jobs) / batch_s, "seconds": batch_s, "Mrays_per_s": st["rays"] / batch_s / 1e6,
+                    "device_ms": st["device_ms"], "queue_paths": queue},
+        "speedup": plain_s / batch_s,
+        "autotune_seconds": {str(k): v for k, v in tune.items()},
+        "max_rel_image_diff": diff,
+        "timing": "wall clock around all jobs (host overhead included); scene builds excluded",
+        "scene_build_seconds": build_s,
+    }
+    return out, {"jobs": jobs, "scenes": scenes, "queue": queue, "capacity": len(jobs) / batch_s}
+
+
+def run_served(lm, args, ctx) -> dict:
+    """Poisson request stream through RenderServer at 80 % of the measured batched capacity."""
+    from lightmetrica import synthetic as syn
+    from lightmetrica.serving import RenderServer, Request
+    scenes = ctx["scenes"]
+    rate = 0.8 * ctx["capacity"]
+    reqs = syn.served_requests(args.served_requests, rate=rate, n_scenes=len(scenes))
+    srv = RenderServer(lambda k: scenes[k][0], hbm_budget=150 * 10**9, queue_paths=ctx["queue"], max_inflight=1024)
+    srv.owns_scenes = False
+    t0 = srv.clock()
+    i, n = 0, len(reqs)
+    while i < n or not srv.idle():
+        now = srv.clock() - t0
+        while i < n and reqs[i]["arrival"] <= now:
+            q = reqs[i]
+            srv.submit(Request(rid=q["rid"], arrival=t0 + q["arrival"], scene_key=q["scene"], w=q["res"], h=q["res"],
+                               spp=q["spp"], max_verts=q["max_verts"], seed=q["seed"], refine=q["refine"]))
+            i += 1
+        if srv.idle() and i < n:
+            time.sleep(max(0.0, reqs[i]["arrival"] - (srv.clock() - t0)))
+            continue
+        srv.step()
+    total = srv.clock() - t0
+    lat = srv.latencies()
+    st = srv.batch.stats()
+    srv.batch.close()
+    return {"workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the batched capacity), "
+                        f"{sum(1 for q in reqs if q['refine'] is not None)} refinements (+16 spp), scenes of the "
+                        f"batched workload, 150 GB HBM budget",
+            "requests": n, "rate_per_s": rate, "seconds": total, "jobs_per_s": n / total,
+            "Mrays_per_s": st["rays"] / total / 1e6,
+            "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"],
+            "done_p50_s": lat["done_p50"], "done_p99_s": lat["done_p99"], "evictions": lat["evictions"],
+            "peak_resident_bytes": srv.peak_resident_bytes}
 
 
 def _cudart():
@@ -348,6 +463,9 @@ def main():
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--wave", type=int, default=0, help="paths in flight per wave (0 = library default)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched and served legs")
+    ap.add_argument("--batched-jobs", type=int, default=256)
+    ap.add_argument("--served-requests", type=int, default=5000, help="0 skips the served leg")
     args = ap.parse_args()
     _apply_overrides(args)
     if args.impl == "reference":

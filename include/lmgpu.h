@@ -245,7 +245,9 @@ typedef struct lmgpu_render_stats {
 
 /* Renders into `film` (cleared first unless params->accumulate) on `stream` and waits for it.
  * stats may be NULL. The film holds the estimate scaled by 1/spp (pixel mode) or w*h/spp (image
- * mode), as renderer_pt.cpp:307-312 rescales it. */
+ * mode), as renderer_pt.cpp:307-312 rescales it. The wavefront queues (about 210 bytes per path
+ * in flight) belong to the device, not the scene: calls on one device from several host threads
+ * take turns. */
 int lmgpu_render_pt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params, void* stream,
                     lmgpu_render_stats* stats);
 

@@ -59,9 +59,7 @@ struct lmgpu_scene {
     lmgpu_accel* accel = nullptr;
     lmgpu::DevScene dev{};
     lmgpu::DevBuf shade, prim_ml, mats, lights, ltri, cdf, env;
-    // wavefront queues, grown on demand
-    lmgpu::DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
-    int64_t q_cap = 0;
+    lmgpu::DevBuf counters;  // raycast error flag
 };
 
 struct lmgpu_film {
@@ -883,20 +881,39 @@ int grid_for(K kernel, int block, size_t smem) {
     return std::max(1, per_sm) * current_device().num_sms;
 }
 
-void ensure_queues(lmgpu_scene* s, int64_t cap) {
-    if (s->q_cap >= cap) return;
+// Wavefront queues of lmgpu_render_pt: one set per device, shared by every scene and held for the
+// whole of a call (the call ends with its stream synchronized), so scenes cost only their own
+// tables. Grown on demand; kept for the life of the process.
+struct Workspace {
+    std::mutex m;
+    int64_t cap = 0;
+    DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
+};
+
+Workspace& workspace(int device) {
+    static std::mutex reg_m;
+    static Workspace* reg[64] = {};
+    if (device < 0 || device >= 64) throw Error(LMGPU_ERR_UNSUPPORTED, "device index above 63");
+    std::lock_guard<std::mutex> lk(reg_m);
+    if (!reg[device]) reg[device] = new Workspace();  // never freed: outlives the CUDA runtime's teardown order
+    return *reg[device];
+}
+
+void ensure_queues(Workspace& w, int64_t cap) {
+    if (!w.counters.p) w.counters.alloc(192);
+    if (w.cap >= cap) return;
     for (int b = 0; b < 2; b++) {
-        s->q_o[b].alloc(size_t(cap) * 16);
-        s->q_d[b].alloc(size_t(cap) * 16);
-        s->q_thr[b].alloc(size_t(cap) * 16);
-        s->q_nrm[b].alloc(size_t(cap) * 16);
-        s->q_ids[b].alloc(size_t(cap) * 8);
+        w.q_o[b].alloc(size_t(cap) * 16);
+        w.q_d[b].alloc(size_t(cap) * 16);
+        w.q_thr[b].alloc(size_t(cap) * 16);
+        w.q_nrm[b].alloc(size_t(cap) * 16);
+        w.q_ids[b].alloc(size_t(cap) * 8);
     }
-    s->hits.alloc(size_t(cap) * 16);
-    s->s_o.alloc(size_t(cap) * 16);
-    s->s_d.alloc(size_t(cap) * 16);
-    s->s_c.alloc(size_t(cap) * 16);
-    s->q_cap = cap;
+    w.hits.alloc(size_t(cap) * 16);
+    w.s_o.alloc(size_t(cap) * 16);
+    w.s_d.alloc(size_t(cap) * 16);
+    w.s_c.alloc(size_t(cap) * 16);
+    w.cap = cap;
 }
 
 }  // namespace lmgpu
@@ -1112,9 +1129,8 @@ int lmgpu_scene_destroy(lmgpu_scene* scene) {
 int lmgpu_scene_device_bytes(const lmgpu_scene* s, int64_t* out) {
     return guarded([&] {
         if (!s || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
-        size_t b = s->shade.bytes + s->prim_ml.bytes + s->mats.bytes + s->lights.bytes + s->ltri.bytes + s->cdf.bytes + s->env.bytes;
-        for (int i = 0; i < 2; i++) b += s->q_o[i].bytes + s->q_d[i].bytes + s->q_thr[i].bytes + s->q_nrm[i].bytes + s->q_ids[i].bytes;
-        b += s->hits.bytes + s->s_o.bytes + s->s_d.bytes + s->s_c.bytes + s->counters.bytes;
+        const size_t b = s->shade.bytes + s->prim_ml.bytes + s->mats.bytes + s->lights.bytes + s->ltri.bytes + s->cdf.bytes +
+                         s->env.bytes + s->counters.bytes;
         *out = int64_t(b);
     });
 }
@@ -1207,7 +1223,9 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         if (total > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "more than 2^32 paths in one render");
         int64_t wave = prm->wave_paths > 0 ? prm->wave_paths : (int64_t(1) << 22);
         wave = std::min(wave, total);
-        ensure_queues(s, wave);
+        Workspace& ws = workspace(current_device().device);
+        std::lock_guard<std::mutex> ws_lock(ws.m);
+        ensure_queues(ws, wave);
 
         PtConst P;
         P.seed = prm->seed;
@@ -1220,11 +1238,11 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
 
         ExtQ q[2];
         for (int b = 0; b < 2; b++)
-            q[b] = ExtQ{s->q_o[b].as<float4>(), s->q_d[b].as<float4>(), s->q_thr[b].as<float4>(), s->q_nrm[b].as<float4>(),
-                        s->q_ids[b].as<uint2>()};
-        ShadowQ sq{s->s_o.as<float4>(), s->s_d.as<float4>(), s->s_c.as<float4>()};
-        int* cnt = s->counters.as<int>();  // [0],[1] extension queues, [2] shadow queue, [3] error
-        unsigned long long* rays = reinterpret_cast<unsigned long long*>(s->counters.as<char>() + 32);
+            q[b] = ExtQ{ws.q_o[b].as<float4>(), ws.q_d[b].as<float4>(), ws.q_thr[b].as<float4>(), ws.q_nrm[b].as<float4>(),
+                        ws.q_ids[b].as<uint2>()};
+        ShadowQ sq{ws.s_o.as<float4>(), ws.s_d.as<float4>(), ws.s_c.as<float4>()};
+        int* cnt = ws.counters.as<int>();  // [0],[1] extension queues, [2] shadow queue, [3] error
+        unsigned long long* rays = reinterpret_cast<unsigned long long*>(ws.counters.as<char>() + 32);
         float* film = f->sum.as<float>();
         const Bvh8 bvh = s->dev.bvh;
         const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
@@ -1236,8 +1254,8 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
         const int g_shade = grid_for(k_pt_shade, kBlock, 0);
-        unsigned long long* sums = reinterpret_cast<unsigned long long*>(s->counters.as<char>() + 64);  // 8 counters
-        float* worst = reinterpret_cast<float*>(s->counters.as<char>() + 128);                           // 2 rays
+        unsigned long long* sums = reinterpret_cast<unsigned long long*>(ws.counters.as<char>() + 64);  // 8 counters
+        float* worst = reinterpret_cast<float*>(ws.counters.as<char>() + 128);                           // 2 rays
         const int cmask = prm->instrument == 2 ? 0 : 63;
 
         // per-kernel device time: events bracket every launch when stats are requested
@@ -1261,7 +1279,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             LMGPU_CUDA(cudaMemsetAsync(film, 0, size_t(npix) * 3 * 4, st));
             f->accumulated_spp = 0;
         }
-        LMGPU_CUDA(cudaMemsetAsync(s->counters.p, 0, 192, st));
+        LMGPU_CUDA(cudaMemsetAsync(ws.counters.p, 0, 192, st));
         for (int64_t start = 0; start < total; start += wave) {
             const int64_t n = std::min(wave, total - start);
             int cur = 0;
@@ -1280,14 +1298,14 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             }
             for (int it = 1; it < P.max_verts; it++) {
                 mark(K_EXT);
-                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, s->hits.as<float4>(), rays, cnt + 3, sums,
+                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, ws.hits.as<float4>(), rays, cnt + 3, sums,
                                                     cmask, worst, nullptr, nullptr);
                 mark(-1);
                 n_ext++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 mark(K_SHADE);
-                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], s->hits.as<float4>(), cnt + cur, q[1 - cur],
+                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], ws.hits.as<float4>(), cnt + cur, q[1 - cur],
                                                       cnt + (1 - cur), sq, cnt + 2, film);
                 mark(-1);
                 mark(K_SHADOW);
@@ -1503,6 +1521,7 @@ struct lmgpu_batch {
     lmgpu::DevBuf ctl;        // int64: next, total, range[2], remaining, njobs; then int counters, then u64 rays
     lmgpu::DevBuf jobs, job_begin, pass_done;
     size_t jobs_cap = 0, begin_cap = 0, pass_cap = 0;
+    size_t jobs_done = 0, begin_done = 0;  // entries already on the device
     std::vector<lmgpu::JobDev> host_jobs;
     std::vector<int64_t> host_begin{0};
     std::vector<lmgpu_film*> films;
@@ -1536,8 +1555,9 @@ int* ctl_cnt(lmgpu_batch* b) { return reinterpret_cast<int*>(b->ctl.as<char>() +
 unsigned long long* ctl_rays(lmgpu_batch* b) { return reinterpret_cast<unsigned long long*>(b->ctl.as<char>() + 64); }
 unsigned long long* ctl_sums(lmgpu_batch* b) { return reinterpret_cast<unsigned long long*>(b->ctl.as<char>() + 80); }
 
+// Appends v[done, size) to the device copy (all of v after a reallocation); `done` becomes size.
 template <typename T>
-void grow_upload(DevBuf& buf, size_t& cap, const std::vector<T>& v, cudaStream_t st, bool& realloc) {
+void grow_upload(DevBuf& buf, size_t& cap, size_t& done, const std::vector<T>& v, cudaStream_t st, bool& realloc) {
     if (v.size() > cap) {
         size_t c = std::max<size_t>(v.size(), 2 * cap);
         if (c < 64) c = 64;
@@ -1548,8 +1568,12 @@ void grow_upload(DevBuf& buf, size_t& cap, const std::vector<T>& v, cudaStream_t
         std::swap(buf.bytes, nb.bytes);
         cap = c;
         realloc = true;
+        done = 0;
     }
-    if (!v.empty()) LMGPU_CUDA(cudaMemcpyAsync(buf.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    if (v.size() > done)
+        LMGPU_CUDA(cudaMemcpyAsync(static_cast<T*>(buf.p) + done, v.data() + done, (v.size() - done) * sizeof(T),
+                                   cudaMemcpyHostToDevice, st));
+    done = v.size();
 }
 
 __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
@@ -1696,8 +1720,10 @@ int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* p
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         bool realloc = false;
         if (b->table_dirty) {
-            grow_upload(b->jobs, b->jobs_cap, b->host_jobs, st, realloc);
-            grow_upload(b->job_begin, b->begin_cap, b->host_begin, st, realloc);
+            grow_upload(b->jobs, b->jobs_cap, b->jobs_done, b->host_jobs, st, realloc);
+            // the last entry of job_begin changes with every submission (it ends the path space)
+            b->begin_done = std::min(b->begin_done, b->host_begin.size() >= 2 ? b->host_begin.size() - 2 : 0);
+            grow_upload(b->job_begin, b->begin_cap, b->begin_done, b->host_begin, st, realloc);
             // new pass counters start at zero; existing ones keep their device values
             if (b->passes > b->pass_cap) {
                 LMGPU_CUDA(cudaStreamSynchronize(st));
@@ -1801,6 +1827,7 @@ int lmgpu_batch_reset(lmgpu_batch* b) {
         b->films.clear();
         b->host_begin.assign(1, 0);
         b->host_pass.clear();
+        b->jobs_done = b->begin_done = 0;
         b->total = 0;
         b->passes = 0;
         b->max_depth = 1;

@@ -174,7 +174,9 @@ class RenderServer:
         self.finished: list[Request] = []
         self.by_id: dict[int, Request] = {}
         self.resident_bytes = 0
+        self.peak_resident_bytes = 0
         self.evictions = 0
+        self.owns_scenes = True  # False: make_scene hands out scenes the caller keeps; eviction only forgets them
         self._film_seq = 0
 
     # -- admission -------------------------------------------------------------------------------
@@ -191,7 +193,8 @@ class RenderServer:
             if self.resident_bytes + need <= self.budget:
                 break
             scene, nbytes = self.scenes.pop(k)
-            _release_scene(scene)
+            if self.owns_scenes:
+                _release_scene(scene)
             self.resident_bytes -= nbytes
             del self.scene_last_use[k]
             self.scene_users.pop(k, None)
@@ -212,7 +215,8 @@ class RenderServer:
             nbytes = scene_footprint(scene)
             self._evict_for(need + nbytes)
             if self.resident_bytes + need + nbytes > self.budget:
-                _release_scene(scene)
+                if self.owns_scenes:
+                    _release_scene(scene)
                 return False
             self.scenes[req.scene_key] = (scene, nbytes)
             self.resident_bytes += nbytes
@@ -230,6 +234,7 @@ class RenderServer:
             req.film = lm.load_film(f"__served_film_{self._film_seq}", "bitmap", w=req.w, h=req.h)
             accumulate = False
         self.resident_bytes += need
+        self.peak_resident_bytes = max(self.peak_resident_bytes, self.resident_bytes)
         req.job = self.batch.submit(scene, req.film, max_verts=req.max_verts, spp=req.spp, seed=req.seed,
                                     accumulate=accumulate)
         req.admitted = self.clock()

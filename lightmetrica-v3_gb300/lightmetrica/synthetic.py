@@ -301,3 +301,98 @@ def env_texture(w: int = 64, h: int = 32, seed: int = 5) -> np.ndarray:
     base = np.exp(rng.normal(-1.0, 0.7, (h, w, 1))).astype(np.float32) * np.array([0.9, 1.0, 1.1], np.float32)
     base[int(h * 0.75):int(h * 0.85), int(w * 0.2):int(w * 0.3)] *= 40.0
     return np.ascontiguousarray(base.astype(np.float32))
+
+
+# ---------------------------------------------------------------------------------------------
+# Many small independent jobs (the batched and served workloads)
+
+BATCH_RESOLUTIONS = (64, 128, 256, 512)
+
+
+def random_triangles(n: int, rng) -> tuple[np.ndarray, np.ndarray]:
+    """n independent triangles: centres U[0,1]^3, each corner at distance U(.001,.03) from the
+    centre in a uniform random direction. Returns (positions (3n,3), flat normals (n,3))."""
+    c = rng.random((n, 1, 3))
+    d = rng.normal(size=(n, 3, 3))
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    r = rng.uniform(0.001, 0.03, (n, 3, 1))
+    p = (c + d * r).astype(np.float32)
+    gn = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]).astype(np.float64)
+    ln = np.linalg.norm(gn, axis=1, keepdims=True)
+    gn = np.where(ln > 0, gn / np.where(ln > 0, ln, 1), np.array([0.0, 0.0, 1.0]))
+    return p.reshape(-1, 3), gn.astype(np.float32)
+
+
+def triangles_scene(seed: int, n_tris: int, w: int, h: int, accel: str = "sahbvh", prefix: str = ""):
+    """One batched-workload scene: `n_tris` random triangles in the unit cube split 50/30/20 %
+    over diffuse, GGX glossy and dielectric materials, a 0.5 x 0.5 area light above the cube, a
+    constant environment, and a pinhole camera looking at the cube. Returns (scene, film)."""
+    rng = np.random.default_rng(seed)
+    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
+    camera = lm.load_camera(prefix + "camera", "pinhole", position=[0.5, 0.6, 2.3], center=[0.5, 0.5, 0.5],
+                            up=[0, 1, 0], vfov=40, aspect=w / h)
+    scene = lm.load_scene(prefix + "scene", "default", accel=lm.load_accel(prefix + "accel", accel))
+    scene.add_primitive(camera=camera)
+    p, gn = random_triangles(n_tris, rng)
+    kinds = rng.choice(3, size=n_tris, p=[0.5, 0.3, 0.2])
+    rough = rng.uniform(0.05, 0.5)
+    mats = [lm.load_material(prefix + "diffuse", "diffuse", Kd=list(rng.uniform(0.2, 0.9, 3))),
+            lm.load_material(prefix + "glossy", "glossy", Ks=list(rng.uniform(0.5, 0.95, 3)), ax=rough, ay=rough),
+            lm.load_material(prefix + "glass", "glass", Ni=1.5)]
+    for k in range(3):
+        sel = np.nonzero(kinds == k)[0]
+        if len(sel) == 0:
+            continue
+        ps = p.reshape(-1, 3, 3)[sel].reshape(-1, 3)
+        fp = np.arange(3 * len(sel), dtype=np.int32)
+        fn = np.repeat(np.arange(len(sel), dtype=np.int32), 3)
+        mesh = lm.load_mesh(prefix + f"tris{k}", "raw", ps=ps, ns=gn[sel], ts=np.zeros((1, 2), np.float32),
+                            fs={"p": fp, "n": fn, "t": np.zeros_like(fp)})
+        scene.add_primitive(mesh=mesh, material=mats[k])
+    a, b, y = 0.25, 0.75, 1.3
+    lmesh = load_mesh(prefix + "light_mesh", *quad((a, y, a), (b, y, a), (b, y, b), (a, y, b), (0, -1, 0)))
+    light = lm.load_light(prefix + "light", "area", Ke=list(rng.uniform(6.0, 12.0, 3)), mesh=lmesh)
+    scene.add_primitive(mesh=lmesh, material=lm.load_material(prefix + "light_mat", "diffuse", Kd=[0, 0, 0]), light=light)
+    scene.add_primitive(light=lm.load_light(prefix + "env", "envconst", Le=[0.4, 0.45, 0.5]))
+    return scene, film
+
+
+def batch_jobs(n_jobs: int = 256, seed: int = 2024, min_tris: int = 1000, max_tris: int = 200000):
+    """Job specs of the batched workload: per job a scene seed, a triangle count log-uniform in
+    [min_tris, max_tris], a square resolution from BATCH_RESOLUTIONS, spp U{4..64} and a maximum
+    path length U{6..12} (max_verts = length + 1)."""
+    rng = np.random.default_rng(seed)
+    jobs = []
+    for i in range(n_jobs):
+        jobs.append({
+            "scene_seed": int(rng.integers(0, 2**31)),
+            "tris": int(np.exp(rng.uniform(math.log(min_tris), math.log(max_tris)))),
+            "res": int(rng.choice(BATCH_RESOLUTIONS)),
+            "spp": int(rng.integers(4, 65)),
+            "max_verts": int(rng.integers(6, 13)) + 1,
+            "seed": int(rng.integers(0, 2**31)),
+        })
+    return jobs
+
+
+def served_requests(n: int, rate: float, n_scenes: int, seed: int = 77, refine_frac: float = 0.3,
+                    refine_spp: int = 16):
+    """Poisson request stream: `n` requests at `rate` per second. A request renders one of
+    `n_scenes` batched-workload scenes (resolution, spp and length drawn as in batch_jobs), or
+    with probability `refine_frac` adds `refine_spp` samples to an earlier request's film.
+    Returns dicts with arrival (s from the start), scene, res, spp, max_verts, seed, refine."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        fresh = [r for r in out if r["refine"] is None]
+        if fresh and rng.random() < refine_frac:
+            base = fresh[int(rng.integers(0, len(fresh)))]
+            out.append({"rid": i, "arrival": t, "scene": base["scene"], "res": base["res"], "spp": refine_spp,
+                        "max_verts": base["max_verts"], "seed": int(rng.integers(0, 2**31)), "refine": base["rid"]})
+        else:
+            out.append({"rid": i, "arrival": t, "scene": int(rng.integers(0, n_scenes)),
+                        "res": int(rng.choice(BATCH_RESOLUTIONS)), "spp": int(rng.integers(4, 65)),
+                        "max_verts": int(rng.integers(6, 13)) + 1, "seed": int(rng.integers(0, 2**31)), "refine": None})
+    return out
