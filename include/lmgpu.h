@@ -57,6 +57,14 @@ typedef struct lmgpu_accel_stats {
  */
 const char* lmgpu_last_error(void);
 int lmgpu_version(void);
+/* Launch-shape tuning (no reference counterpart). Keys:
+ *   "trace_refill"  persistent trace kernels of the path tracers: a warp's idle lanes fetch new
+ *                   rays once fewer than this many lanes still trace (1..32; default 24); 0 runs
+ *                   one ray per thread without refills.
+ * Tuning changes speed only, never results. Process-wide; set it between renders. */
+int lmgpu_tune_set(const char* key, int64_t value);
+int lmgpu_tune_get(const char* key, int64_t* value);
+
 /* Selects the CUDA device used by every later call on this thread's handles (default 0). */
 int lmgpu_set_device(int device);
 

@@ -26,6 +26,11 @@ DeviceInfo& current_device() {
     return info;
 }
 
+Tuning& tuning() {
+    static Tuning t;
+    return t;
+}
+
 constexpr int kTraceBlock = 128;
 
 // One thread per ray, grid-stride. rays: 2 float4 per ray (o, tmin) (d, tmax).
@@ -135,6 +140,28 @@ extern "C" {
 const char* lmgpu_last_error(void) { return g_last_error.c_str(); }
 
 int lmgpu_version(void) { return 1; }
+
+int lmgpu_tune_set(const char* key, int64_t value) {
+    return guarded([&] {
+        if (!key) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "key is null");
+        const std::string k(key);
+        if (k == "trace_refill") {
+            if (value < 0 || value > 32) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "trace_refill must be in [0, 32]");
+            tuning().trace_refill = int(value);
+        } else {
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
+        }
+    });
+}
+
+int lmgpu_tune_get(const char* key, int64_t* value) {
+    return guarded([&] {
+        if (!key || !value) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        const std::string k(key);
+        if (k == "trace_refill") *value = tuning().trace_refill;
+        else throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
+    });
+}
 
 int lmgpu_set_device(int device) {
     return guarded([&] {

@@ -114,17 +114,30 @@ __device__ inline uint32_t oct_permute(uint32_t m, uint32_t oct) {
 
 // Ray traversal of the 8-wide BVH. Closest hit: the smallest t over every triangle whose test
 // accepts the ray in [tmin, tmax], ties broken toward the smaller flattened index. Any hit
-// (`any_hit`): returns at the first accepted triangle. The per-thread stack of sibling groups
+// (`any_hit`): ends at the first accepted triangle. The per-thread stack of sibling groups
 // lives in shared memory: stk[i * stride] for i < bvh.depth. Child boxes carry a margin of one
 // quantum and the slab comparison widens by 2^-18 relative, which bounds the rounding of the
 // one-FMA slab distances (see the node visit below), so no triangle the exact test would accept
 // is culled.
-// Returns the number of visited nodes in *nodes_visited when non-null (instrumented builds).
-template <bool kAnyHit, bool kCount>
-__device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, float tmax, uint32_t* stk_base,
-                                      uint32_t* stk_bits, int stride, uint32_t* nodes_visited, uint32_t* tris_tested,
-                                      int* err) {
-    TraceHit best{tmax, 0.f, 0.f, -1};
+//
+// The traversal is a resumable state (Trav) advanced one node visit at a time by trav_step, so
+// a persistent kernel can interleave rays on a lane (dynamic ray fetch); trace_bvh8 runs one ray
+// to the end. Either way a ray's visits, tests and result are the same.
+struct Trav {
+    f3 o, d, inv;
+    float tmin;
+    uint32_t oct;
+    int sp;
+    uint32_t node;
+    uint32_t nvis, ntri;
+    TraceHit best;
+};
+
+__device__ inline void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
+    s.o = o;
+    s.d = d;
+    s.tmin = tmin;
+    s.best = TraceHit{tmax, 0.f, 0.f, -1};
     // Slab reciprocals from a direction whose zero (or tiny) components are replaced by +-1e-20,
     // keeping the sign: every slab distance stays finite (an exact zero would give infinities and
     // then NaN in the one-FMA form, which would disable culling on that axis). The triangle test
@@ -132,105 +145,126 @@ __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, f
     const float dxs = fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x);
     const float dys = fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y);
     const float dzs = fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z);
-    const f3 inv = {1.0f / dxs, 1.0f / dys, 1.0f / dzs};
-    const uint32_t oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
-    int sp = 0;
-    uint32_t node = 0;
-    uint32_t nvis = 0, ntri = 0;
-    while (true) {
-        // ---- visit `node` ---------------------------------------------------------------------
-        if (node >= bvh.num_nodes || nvis >= bvh.num_nodes) { *err = 2; break; }
-        const uint4* np = bvh.nodes + size_t(node) * 5;
-        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
-        nvis++;
-        // Slab distances with one FMA per plane. Plane q of an axis lies at p + q*s; with
-        // a = s*inv and b = (p - o)*inv, t = q*a + b. The byte is unpacked straight into the float
-        // X = 2^23 + 256*q (one byte permute), so t = fma(X, a/256, b - 2^15*a): the large offset
-        // cancels exactly inside the FMA. Error: about 5 ulp relative plus 0.003 quanta absolute;
-        // the builder leaves one quantum of margin around every child box and the comparison
-        // widens by 2^-18 relative, so the test never culls a box the exact ray enters.
-        const float sx = __uint_as_float((w0.w & 0xffu) << 23);
-        const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
-        const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
-        const uint32_t imask = w0.w >> 24;
-        const float ax = sx * inv.x, ay = sy * inv.y, az = sz * inv.z;
-        const float bx = (__uint_as_float(w0.x) - o.x) * inv.x;
-        const float by = (__uint_as_float(w0.y) - o.y) * inv.y;
-        const float bz = (__uint_as_float(w0.z) - o.z) * inv.z;
-        const float ax8 = ax * 0.00390625f, ay8 = ay * 0.00390625f, az8 = az * 0.00390625f;
-        const float bx8 = fmaf(-32768.0f, ax, bx), by8 = fmaf(-32768.0f, ay, by), bz8 = fmaf(-32768.0f, az, bz);
-        // near/far plane bytes per axis, chosen by the ray's octant
-        const uint32_t lx0 = w2.x, lx1 = w2.y, ly0 = w2.z, ly1 = w2.w, lz0 = w3.x, lz1 = w3.y;
-        const uint32_t hx0 = w3.z, hx1 = w3.w, hy0 = w4.x, hy1 = w4.y, hz0 = w4.z, hz1 = w4.w;
-        const uint32_t nx0 = (oct & 1u) ? hx0 : lx0, nx1 = (oct & 1u) ? hx1 : lx1;
-        const uint32_t fx0 = (oct & 1u) ? lx0 : hx0, fx1 = (oct & 1u) ? lx1 : hx1;
-        const uint32_t ny0 = (oct & 2u) ? hy0 : ly0, ny1 = (oct & 2u) ? hy1 : ly1;
-        const uint32_t fy0 = (oct & 2u) ? ly0 : hy0, fy1 = (oct & 2u) ? ly1 : hy1;
-        const uint32_t nz0 = (oct & 4u) ? hz0 : lz0, nz1 = (oct & 4u) ? hz1 : lz1;
-        const uint32_t fz0 = (oct & 4u) ? lz0 : hz0, fz1 = (oct & 4u) ? lz1 : hz1;
-        uint32_t hitmask = 0;
+    s.inv = {1.0f / dxs, 1.0f / dys, 1.0f / dzs};
+    s.oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
+    s.sp = 0;
+    s.node = 0;
+    s.nvis = 0;
+    s.ntri = 0;
+}
+
+// Visits s.node (testing the triangles of every leaf child the ray enters) and moves to the next
+// node. Returns true when the traversal has ended; s.best is then the result. Sets *err (and
+// ends) on a stack overflow (1) or a visit count above the node count (2), which only a corrupt
+// BVH can cause.
+template <bool kAnyHit, bool kCount>
+__device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* stk_base, uint32_t* stk_bits, int stride,
+                                          int* err) {
+    if (s.node >= bvh.num_nodes || s.nvis >= bvh.num_nodes) { *err = 2; return true; }
+    const uint4* np = bvh.nodes + size_t(s.node) * 5;
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    s.nvis++;
+    const uint32_t oct = s.oct;
+    // Slab distances with one FMA per plane. Plane q of an axis lies at p + q*s; with
+    // a = s*inv and b = (p - o)*inv, t = q*a + b. The byte is unpacked straight into the float
+    // X = 2^23 + 256*q (one byte permute), so t = fma(X, a/256, b - 2^15*a): the large offset
+    // cancels exactly inside the FMA. Error: about 5 ulp relative plus 0.003 quanta absolute;
+    // the builder leaves one quantum of margin around every child box and the comparison
+    // widens by 2^-18 relative, so the test never culls a box the exact ray enters.
+    const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    const uint32_t imask = w0.w >> 24;
+    const float ax = sx * s.inv.x, ay = sy * s.inv.y, az = sz * s.inv.z;
+    const float bx = (__uint_as_float(w0.x) - s.o.x) * s.inv.x;
+    const float by = (__uint_as_float(w0.y) - s.o.y) * s.inv.y;
+    const float bz = (__uint_as_float(w0.z) - s.o.z) * s.inv.z;
+    const float ax8 = ax * 0.00390625f, ay8 = ay * 0.00390625f, az8 = az * 0.00390625f;
+    const float bx8 = fmaf(-32768.0f, ax, bx), by8 = fmaf(-32768.0f, ay, by), bz8 = fmaf(-32768.0f, az, bz);
+    // near/far plane bytes per axis, chosen by the ray's octant
+    const uint32_t lx0 = w2.x, lx1 = w2.y, ly0 = w2.z, ly1 = w2.w, lz0 = w3.x, lz1 = w3.y;
+    const uint32_t hx0 = w3.z, hx1 = w3.w, hy0 = w4.x, hy1 = w4.y, hz0 = w4.z, hz1 = w4.w;
+    const uint32_t nx0 = (oct & 1u) ? hx0 : lx0, nx1 = (oct & 1u) ? hx1 : lx1;
+    const uint32_t fx0 = (oct & 1u) ? lx0 : hx0, fx1 = (oct & 1u) ? lx1 : hx1;
+    const uint32_t ny0 = (oct & 2u) ? hy0 : ly0, ny1 = (oct & 2u) ? hy1 : ly1;
+    const uint32_t fy0 = (oct & 2u) ? ly0 : hy0, fy1 = (oct & 2u) ? ly1 : hy1;
+    const uint32_t nz0 = (oct & 4u) ? hz0 : lz0, nz1 = (oct & 4u) ? hz1 : lz1;
+    const uint32_t fz0 = (oct & 4u) ? lz0 : hz0, fz1 = (oct & 4u) ? lz1 : hz1;
+    uint32_t hitmask = 0;
 #pragma unroll
-        for (int s = 0; s < 8; s++) {
-            const uint32_t sel = 0x5404u | (uint32_t(s & 3) << 4);  // bytes: 00, q, 00, 4B
-            const float qnx = __uint_as_float(__byte_perm(s < 4 ? nx0 : nx1, 0x4B00u, sel));
-            const float qfx = __uint_as_float(__byte_perm(s < 4 ? fx0 : fx1, 0x4B00u, sel));
-            const float qny = __uint_as_float(__byte_perm(s < 4 ? ny0 : ny1, 0x4B00u, sel));
-            const float qfy = __uint_as_float(__byte_perm(s < 4 ? fy0 : fy1, 0x4B00u, sel));
-            const float qnz = __uint_as_float(__byte_perm(s < 4 ? nz0 : nz1, 0x4B00u, sel));
-            const float qfz = __uint_as_float(__byte_perm(s < 4 ? fz0 : fz1, 0x4B00u, sel));
-            const float tn = fmaxf(fmaxf(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8)), fmaxf(fmaf(qnz, az8, bz8), tmin));
-            const float tf0 = fminf(fminf(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8)), fminf(fmaf(qfz, az8, bz8), best.t));
-            // Widening the far side by 2^-18 covers the relative error of both sides. Empty slots
-            // hold inverted boxes (qlo = 255, qhi = 0) that no ray enters; one accepted through
-            // rounding is a leaf of zero triangles.
-            if (tn <= tf0 * 1.0000038f) hitmask |= 1u << s;
-        }
-        // ---- leaf children: test their triangles now -------------------------------------------
-        uint32_t leaves = hitmask & ~imask;
-        while (leaves) {
-            const int s = __ffs(leaves) - 1;
-            leaves &= leaves - 1;
-            const uint32_t meta = byte_of(s < 4 ? w1.z : w1.w, s & 3);
-            const uint32_t cnt = meta >> 5, off = meta & 31u;
-            for (uint32_t j = 0; j < cnt; j++) {
-                const float4* tp = bvh.tris + size_t(w1.y + off + j) * 3;
-                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                if (kCount) ntri++;
-                float t, u, v;
-                if (tri_test(o, d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), tmin, best.t, t, u, v)) {
-                    const int32_t id = int32_t(__float_as_uint(c.y));
-                    if (kAnyHit) {
-                        if (kCount) { *nodes_visited += nvis; *tris_tested += ntri; }
-                        return TraceHit{t, u, v, id};
-                    }
-                    if (t < best.t || best.id < 0 || id < best.id) best = TraceHit{t, u, v, id};
+    for (int k = 0; k < 8; k++) {
+        const uint32_t sel = 0x5404u | (uint32_t(k & 3) << 4);  // bytes: 00, q, 00, 4B
+        const float qnx = __uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x4B00u, sel));
+        const float qfx = __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x4B00u, sel));
+        const float qny = __uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x4B00u, sel));
+        const float qfy = __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x4B00u, sel));
+        const float qnz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x4B00u, sel));
+        const float qfz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B00u, sel));
+        const float tn = fmaxf(fmaxf(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8)), fmaxf(fmaf(qnz, az8, bz8), s.tmin));
+        const float tf0 = fminf(fminf(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8)), fminf(fmaf(qfz, az8, bz8), s.best.t));
+        // Widening the far side by 2^-18 covers the relative error of both sides. Empty slots
+        // hold inverted boxes (qlo = 255, qhi = 0) that no ray enters; one accepted through
+        // rounding is a leaf of zero triangles.
+        if (tn <= tf0 * 1.0000038f) hitmask |= 1u << k;
+    }
+    // ---- leaf children: test their triangles now -----------------------------------------------
+    uint32_t leaves = hitmask & ~imask;
+    while (leaves) {
+        const int k = __ffs(leaves) - 1;
+        leaves &= leaves - 1;
+        const uint32_t meta = byte_of(k < 4 ? w1.z : w1.w, k & 3);
+        const uint32_t cnt = meta >> 5, off = meta & 31u;
+        for (uint32_t j = 0; j < cnt; j++) {
+            const float4* tp = bvh.tris + size_t(w1.y + off + j) * 3;
+            const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+            if (kCount) s.ntri++;
+            float t, u, v;
+            if (tri_test(s.o, s.d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), s.tmin, s.best.t, t, u, v)) {
+                const int32_t id = int32_t(__float_as_uint(c.y));
+                if (kAnyHit) {
+                    s.best = TraceHit{t, u, v, id};
+                    return true;
                 }
+                if (t < s.best.t || s.best.id < 0 || id < s.best.id) s.best = TraceHit{t, u, v, id};
             }
         }
-        // ---- next node: nearest-first by octant order ------------------------------------------
-        uint32_t inner = oct_permute(hitmask & imask, oct);
-        uint32_t g_base = w1.x, g_imask = imask;
-        if (inner == 0u) {
-            if (sp == 0) break;
-            sp--;
-            g_base = stk_base[sp * stride];
-            const uint32_t bits = stk_bits[sp * stride];
-            g_imask = bits >> 8;
-            inner = bits & 0xffu;
-        }
-        const int k = __ffs(inner) - 1;
-        inner &= inner - 1;
-        const uint32_t slot = uint32_t(k) ^ oct;
-        node = g_base + __popc(g_imask & ((1u << slot) - 1u));
-        if (inner != 0u) {
-            if (sp >= bvh.depth) { *err = 1; break; }
-            stk_base[sp * stride] = g_base;
-            stk_bits[sp * stride] = (g_imask << 8) | inner;
-            sp++;
-        }
     }
-    if (kCount) { *nodes_visited += nvis; *tris_tested += ntri; }
-    return best;
+    // ---- next node: nearest-first by octant order ----------------------------------------------
+    uint32_t inner = oct_permute(hitmask & imask, oct);
+    uint32_t g_base = w1.x, g_imask = imask;
+    if (inner == 0u) {
+        if (s.sp == 0) return true;
+        s.sp--;
+        g_base = stk_base[s.sp * stride];
+        const uint32_t bits = stk_bits[s.sp * stride];
+        g_imask = bits >> 8;
+        inner = bits & 0xffu;
+    }
+    const int k = __ffs(inner) - 1;
+    inner &= inner - 1;
+    const uint32_t slot = uint32_t(k) ^ oct;
+    s.node = g_base + __popc(g_imask & ((1u << slot) - 1u));
+    if (inner != 0u) {
+        if (s.sp >= bvh.depth) { *err = 1; return true; }
+        stk_base[s.sp * stride] = g_base;
+        stk_bits[s.sp * stride] = (g_imask << 8) | inner;
+        s.sp++;
+    }
+    return false;
+}
+
+// One ray to the end. Adds the node visits and triangle tests to *nodes_visited / *tris_tested
+// when kCount.
+template <bool kAnyHit, bool kCount>
+__device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, float tmax, uint32_t* stk_base,
+                                      uint32_t* stk_bits, int stride, uint32_t* nodes_visited, uint32_t* tris_tested,
+                                      int* err) {
+    Trav s;
+    trav_init(s, o, d, tmin, tmax);
+    while (!trav_step<kAnyHit, kCount>(bvh, s, stk_base, stk_bits, stride, err)) {
+    }
+    if (kCount) { *nodes_visited += s.nvis; *tris_tested += s.ntri; }
+    return s.best;
 }
 
 }  // namespace lmgpu

@@ -619,37 +619,113 @@ __device__ inline void record_worst(unsigned long long* maxv, float* worst, uint
     }
 }
 
+// Dynamic ray fetch for the persistent trace kernels: `self` hands out queue entries, `other` is
+// the counter of the other trace kernel, which this launch resets for its next launch (the two
+// alternate on one stream, so neither is in use while the other runs). refill as in Tuning.
+struct Fetch {
+    int* self;
+    int* other;
+    int refill;
+};
+
+// Persistent traversal with dynamic ray fetch (Aila & Laine, HPG 2009): every lane of a warp
+// holds one ray in flight; once fewer than f.refill lanes still trace, the idle lanes take the
+// next entries of the queue (one atomic per warp), so a warp no longer waits for its slowest
+// ray. begin(k, s, B) loads entry k into the traversal state (and B, the BVH it traverses);
+// end(k, s) consumes the finished traversal. Called by every thread of full warps.
+template <bool kAnyHit, bool kCount, typename Begin, typename End>
+__device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bvh0, uint32_t* sb, uint32_t* sbits,
+                                           int stride, int* lerr, Begin begin, End end) {
+    const int lane = int(threadIdx.x & 31u);
+    const unsigned below = (1u << lane) - 1u;
+    Trav s;
+    Bvh8 B = bvh0;
+    int k = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        if (!exhausted) {
+            const unsigned idle = __ballot_sync(0xffffffffu, !active);
+            if (idle) {
+                const int leader = __ffs(idle) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(f.self, __popc(idle));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (base + __popc(idle) >= n) exhausted = true;  // warp-uniform
+                if (!active) {
+                    k = base + __popc(idle & below);
+                    if (k < n) {
+                        begin(k, s, B);
+                        active = true;
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) break;
+        const int keep = exhausted ? 1 : f.refill;
+        do {
+            if (active && trav_step<kAnyHit, kCount>(B, s, sb, sbits, stride, lerr)) {
+                end(k, s);
+                active = false;
+            }
+        } while (__popc(__ballot_sync(0xffffffffu, active)) >= keep);
+    }
+}
+
 // Extension rays: closest hit over [Eps, Inf]. kCount: rays with (k & count_mask) == 0 also count
 // node visits and triangle tests into sums[0..2] (instrumented runs only). kBatched: each entry
 // traverses its own job's BVH; bvh.depth is then the largest depth of the table (stack size).
+// f.refill > 0: persistent with dynamic fetch; 0: one ray per thread, grid-stride.
 template <bool kCount, bool kBatched = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       const int* __restrict__ qcount, float4* __restrict__ hits,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
-                                                      int count_mask, float* worst, const JobDev* __restrict__ jobs = nullptr,
+                                                      int count_mask, float* worst, Fetch f, const JobDev* __restrict__ jobs = nullptr,
                                                       const uint32_t* __restrict__ qjob = nullptr) {
     extern __shared__ uint32_t smem[];
     const int n = *qcount;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(rays, (unsigned long long)n);
+        *f.other = 0;
+    }
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
     int lerr = 0;
     uint32_t cn = 0, ct = 0, cc = 0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const float4 o = qo[k], d = qd[k];
-        const Bvh8& B = kBatched ? jobs[qjob[k]].S.bvh : bvh;
-        TraceHit h;
-        if (kCount && (k & count_mask) == 0) {
-            const uint32_t before = cn;
-            h = trace_bvh8<false, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
-                                        &ct, &lerr);
-            cc++;
-            record_worst(sums + 6, worst, cn - before, o, d, kEps, kInf);
-        } else {
-            h = trace_bvh8<false, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
-                                         nullptr, nullptr, &lerr);
+    if (f.refill > 0) {
+        fetch_loop<false, kCount>(
+            n, f, bvh, sb, sbits, int(blockDim.x), &lerr,
+            [&](int k, Trav& s, Bvh8& B) {
+                const float4 o = qo[k], d = qd[k];
+                if (kBatched) B = jobs[qjob[k]].S.bvh;
+                trav_init(s, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf);
+            },
+            [&](int k, const Trav& s) {
+                hits[k] = make_float4(s.best.t, s.best.u, s.best.v, __int_as_float(s.best.id));
+                if (kCount && (k & count_mask) == 0) {
+                    cn += s.nvis;
+                    ct += s.ntri;
+                    cc++;
+                    record_worst(sums + 6, worst, s.nvis, make_float4(s.o.x, s.o.y, s.o.z, 0.f),
+                                 make_float4(s.d.x, s.d.y, s.d.z, 0.f), kEps, kInf);
+                }
+            });
+    } else {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            const float4 o = qo[k], d = qd[k];
+            const Bvh8& B = kBatched ? jobs[qjob[k]].S.bvh : bvh;
+            TraceHit h;
+            if (kCount && (k & count_mask) == 0) {
+                const uint32_t before = cn;
+                h = trace_bvh8<false, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
+                                            &ct, &lerr);
+                cc++;
+                record_worst(sums + 6, worst, cn - before, o, d, kEps, kInf);
+            } else {
+                h = trace_bvh8<false, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
+                                             nullptr, nullptr, &lerr);
+            }
+            hits[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.id));
         }
-        hits[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.id));
     }
     if (kCount && cc) {
         atomicAdd(sums + 0, (unsigned long long)cn);
@@ -659,37 +735,63 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
     if (lerr) atomicOr(err, lerr);
 }
 
-// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount and
-// kBatched as in k_pt_extend, counts into sums[3..5].
+// Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount,
+// kBatched and f as in k_pt_extend; counts into sums[3..5].
 template <bool kCount, bool kBatched = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
-                                                      int count_mask, float* worst, const JobDev* __restrict__ jobs = nullptr) {
+                                                      int count_mask, float* worst, Fetch f, const JobDev* __restrict__ jobs = nullptr) {
     extern __shared__ uint32_t smem[];
     const int n = *scount;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(rays, (unsigned long long)n);
+        *f.other = 0;
+    }
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
     int lerr = 0;
     uint32_t cn = 0, ct = 0, cc = 0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const float4 o = sq.o[k], d = sq.d[k];
-        const uint32_t job = kBatched ? sq.job[k] : 0u;
-        const Bvh8& B = kBatched ? jobs[job].S.bvh : bvh;
-        TraceHit h;
-        if (kCount && (k & count_mask) == 0) {
-            const uint32_t before = cn;
-            h = trace_bvh8<true, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
-                                       &ct, &lerr);
-            cc++;
-            record_worst(sums + 7, worst + 8, cn - before, o, d, kEps, o.w);
-        } else {
-            h = trace_bvh8<true, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
-                                        nullptr, nullptr, &lerr);
-        }
-        if (h.id < 0) {
-            const float4 c = sq.c[k];
-            splat(kBatched ? jobs[job].film : film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+    if (f.refill > 0) {
+        fetch_loop<true, kCount>(
+            n, f, bvh, sb, sbits, int(blockDim.x), &lerr,
+            [&](int k, Trav& s, Bvh8& B) {
+                const float4 o = sq.o[k], d = sq.d[k];
+                if (kBatched) B = jobs[sq.job[k]].S.bvh;
+                trav_init(s, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w);
+            },
+            [&](int k, const Trav& s) {
+                if (s.best.id < 0) {
+                    const float4 c = sq.c[k];
+                    splat(kBatched ? jobs[sq.job[k]].film : film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+                }
+                if (kCount && (k & count_mask) == 0) {
+                    cn += s.nvis;
+                    ct += s.ntri;
+                    cc++;
+                    record_worst(sums + 7, worst + 8, s.nvis, make_float4(s.o.x, s.o.y, s.o.z, 0.f),
+                                 make_float4(s.d.x, s.d.y, s.d.z, 0.f), kEps, s.best.t);
+                }
+            });
+    } else {
+        for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+            const float4 o = sq.o[k], d = sq.d[k];
+            const uint32_t job = kBatched ? sq.job[k] : 0u;
+            const Bvh8& B = kBatched ? jobs[job].S.bvh : bvh;
+            TraceHit h;
+            if (kCount && (k & count_mask) == 0) {
+                const uint32_t before = cn;
+                h = trace_bvh8<true, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
+                                           &ct, &lerr);
+                cc++;
+                record_worst(sums + 7, worst + 8, cn - before, o, d, kEps, o.w);
+            } else {
+                h = trace_bvh8<true, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
+                                            nullptr, nullptr, &lerr);
+            }
+            if (h.id < 0) {
+                const float4 c = sq.c[k];
+                splat(kBatched ? jobs[job].film : film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+            }
         }
     }
     if (kCount && cc) {
@@ -1241,7 +1343,10 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             q[b] = ExtQ{ws.q_o[b].as<float4>(), ws.q_d[b].as<float4>(), ws.q_thr[b].as<float4>(), ws.q_nrm[b].as<float4>(),
                         ws.q_ids[b].as<uint2>()};
         ShadowQ sq{ws.s_o.as<float4>(), ws.s_d.as<float4>(), ws.s_c.as<float4>()};
-        int* cnt = ws.counters.as<int>();  // [0],[1] extension queues, [2] shadow queue, [3] error
+        // [0],[1] extension queues, [2] shadow queue, [3] error, [4],[5] extension / shadow ray fetch
+        int* cnt = ws.counters.as<int>();
+        const int refill = tuning().trace_refill;
+        const Fetch f_ext{cnt + 4, cnt + 5, refill}, f_sh{cnt + 5, cnt + 4, refill};
         unsigned long long* rays = reinterpret_cast<unsigned long long*>(ws.counters.as<char>() + 32);
         float* film = f->sum.as<float>();
         const Bvh8 bvh = s->dev.bvh;
@@ -1284,6 +1389,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             const int64_t n = std::min(wave, total - start);
             int cur = 0;
             LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
+            LMGPU_CUDA(cudaMemsetAsync(cnt + 4, 0, 8, st));
             mark(K_GEN);
             k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0],
                                                                                                cnt + 0, sq, cnt + 2);
@@ -1291,7 +1397,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             LMGPU_CUDA(cudaGetLastError());
             if (P.image) {
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, nullptr);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, f_sh, nullptr);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
@@ -1299,7 +1405,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
             for (int it = 1; it < P.max_verts; it++) {
                 mark(K_EXT);
                 ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, ws.hits.as<float4>(), rays, cnt + 3, sums,
-                                                    cmask, worst, nullptr, nullptr);
+                                                    cmask, worst, f_ext, nullptr, nullptr);
                 mark(-1);
                 n_ext++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
@@ -1309,7 +1415,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
                                                       cnt + (1 - cur), sq, cnt + 2, film);
                 mark(-1);
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, nullptr);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, f_sh, nullptr);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaGetLastError());
@@ -1434,7 +1540,10 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
         const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : cap, total);
 
         // carve the fixed array: counters, then the per-path queues
-        int* cnt = reinterpret_cast<int*>(base);  // [0],[1] extension queues, [2] shadow queue, [3] error
+        // [0],[1] extension queues, [2] shadow queue, [3] error, [4],[5] extension / shadow ray fetch
+        int* cnt = reinterpret_cast<int*>(base);
+        const int refill = tuning().trace_refill;
+        const Fetch f_ext{cnt + 4, cnt + 5, refill}, f_sh{cnt + 5, cnt + 4, refill};
         unsigned long long* rays = reinterpret_cast<unsigned long long*>(base + 32);
         unsigned long long* sums = reinterpret_cast<unsigned long long*>(base + 64);
         char* p = base + kNoallocCounters;
@@ -1481,21 +1590,23 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
             const int64_t n = std::min(wave, total - start);
             int cur = 0;
             LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
+            LMGPU_CUDA(cudaMemsetAsync(cnt + 4, 0, 8, st));
             k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0],
                                                                                                cnt + 0, sq, cnt + 2);
             if (P.image) {
-                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr);
+                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr,
+                                                                f_sh);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
             }
             for (int it = 1; it < P.max_verts; it++) {
                 k_pt_extend<false><<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, hits, rays, cnt + 3, sums,
-                                                                 63, nullptr);
+                                                                 63, nullptr, f_ext);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
                                                       cnt + 2, d_film);
                 k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63,
-                                                                nullptr);
+                                                                nullptr, f_sh);
                 LMGPU_CUDA(cudaGetLastError());
                 cur = 1 - cur;
             }
@@ -1534,6 +1645,8 @@ struct lmgpu_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int32_t graph_depth = 0;
+    int graph_refill = -1;  // trace_refill the graph was captured with
+    int refill = 0;
     int cur = 0;
     double elapsed_ms = 0;
     ~lmgpu_batch() {
@@ -1549,11 +1662,12 @@ constexpr int kChunkIters = 8;  // even: the queue parity is the same at every c
 
 // ctl layout (bytes): 0 next, 8 total, 16 range start, 24 range count, 32 remaining, 40 njobs,
 // 48 int counters [0],[1] extension queues, [2] shadow queue, [3] error; 64 u64 rays [2];
-// 80 u64 sums [8]
+// 80 u64 sums [8]; 144 int extension / shadow ray fetch
 int64_t* ctl64(lmgpu_batch* b) { return b->ctl.as<int64_t>(); }
 int* ctl_cnt(lmgpu_batch* b) { return reinterpret_cast<int*>(b->ctl.as<char>() + 48); }
 unsigned long long* ctl_rays(lmgpu_batch* b) { return reinterpret_cast<unsigned long long*>(b->ctl.as<char>() + 64); }
 unsigned long long* ctl_sums(lmgpu_batch* b) { return reinterpret_cast<unsigned long long*>(b->ctl.as<char>() + 80); }
+int* ctl_fetch(lmgpu_batch* b) { return reinterpret_cast<int*>(b->ctl.as<char>() + 144); }
 
 // Appends v[done, size) to the device copy (all of v after a reallocation); `done` becomes size.
 template <typename T>
@@ -1598,15 +1712,17 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
                     b->q_ids[i].as<uint2>(), b->q_job[i].as<uint32_t>()};
     ShadowQ sq{b->s_o.as<float4>(), b->s_d.as<float4>(), b->s_c.as<float4>(), b->s_job.as<uint32_t>()};
     float4* hits = b->hits.as<float4>();
+    int* fetch = ctl_fetch(b);
+    const Fetch f_ext{fetch, fetch + 1, b->refill}, f_sh{fetch + 1, fetch, b->refill};
     int cur = 0;
     for (int it = 0; it < kChunkIters; it++) {
         k_pt_extend<false, true><<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
-                                                               ctl_sums(b), 63, nullptr, jobs, q[cur].job);
+                                                               ctl_sums(b), 63, nullptr, f_ext, jobs, q[cur].job);
         LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
         k_wf_shade<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
                                                b->pass_done.as<unsigned int>());
         k_pt_shadow<false, true><<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
-                                                              ctl_sums(b), 63, nullptr, jobs);
+                                                              ctl_sums(b), 63, nullptr, f_sh, jobs);
         LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
         k_wf_plan<<<1, 1, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap);
         k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->job_begin.as<int64_t>(), ctl64(b), q[1 - cur], cnt + (1 - cur), sq,
@@ -1616,7 +1732,8 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
 }
 
 void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
-    if (b->exec && !realloc && b->graph_depth == b->max_depth) return;
+    b->refill = tuning().trace_refill;
+    if (b->exec && !realloc && b->graph_depth == b->max_depth && b->graph_refill == b->refill) return;
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
     cudaStream_t cs;
@@ -1641,6 +1758,7 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     LMGPU_CUDA(cudaStreamDestroy(cs));
     LMGPU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     b->graph_depth = b->max_depth;
+    b->graph_refill = b->refill;
     (void)st;
 }
 

@@ -82,6 +82,14 @@ struct DeviceInfo {
 };
 DeviceInfo& current_device();
 
+// Launch-shape parameters that change speed but never results (set through lmgpu_tune_set).
+struct Tuning {
+    // Persistent trace kernels: idle lanes of a warp fetch new rays once fewer than this many
+    // lanes still trace (1..32); 0 runs one ray per thread, grid-stride, without refills.
+    int trace_refill = 24;
+};
+Tuning& tuning();
+
 }  // namespace lmgpu
 
 struct lmgpu_accel {

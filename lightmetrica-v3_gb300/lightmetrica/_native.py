@@ -74,6 +74,8 @@ class RenderStats(C.Structure):
 SIGNATURES = [
     ("lmgpu_last_error", C.c_char_p, []),
     ("lmgpu_version", C.c_int, []),
+    ("lmgpu_tune_set", C.c_int, [C.c_char_p, C.c_int64]),
+    ("lmgpu_tune_get", C.c_int, [C.c_char_p, C.POINTER(C.c_int64)]),
     ("lmgpu_set_device", C.c_int, [C.c_int]),
     ("lmgpu_accel_create", C.c_int, [C.POINTER(C.c_void_p)]),
     ("lmgpu_accel_destroy", C.c_int, [C.c_void_p]),
