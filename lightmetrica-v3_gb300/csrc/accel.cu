@@ -33,20 +33,21 @@ Tuning& tuning() {
 
 constexpr int kTraceBlock = 128;
 
-// One thread per ray, grid-stride. rays: 2 float4 per ray (o, tmin) (d, tmax).
+// rays: 2 float4 per ray (o, tmin) (d, tmax). refill > 0: each block takes one contiguous chunk
+// of the rays and its warps fetch from it dynamically through a shared-memory counter (no state
+// outside the launch, so calls on several streams may overlap); 0: one ray per thread,
+// grid-stride.
 template <bool kAnyHit>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const float4* __restrict__ rays, int64_t n,
                                                             lmgpu_hit* __restrict__ hits, uint8_t* __restrict__ occluded,
-                                                            int* __restrict__ err) {
+                                                            int* __restrict__ err, int refill) {
     extern __shared__ uint32_t smem[];
+    __shared__ int s_fetch;
     const int stride = blockDim.x;
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + stride * bvh.depth + threadIdx.x;
     int lerr = 0;
-    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-        const float4 a = rays[2 * i], b = rays[2 * i + 1];
-        const TraceHit h = trace_bvh8<kAnyHit, false>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits,
-                                                      stride, nullptr, nullptr, &lerr);
+    auto store = [&](int64_t i, const TraceHit& h) {
         if (kAnyHit) {
             occluded[i] = h.id >= 0 ? 1 : 0;
         } else {
@@ -56,6 +57,25 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const flo
             r.v = h.v;
             r.prim = h.id;
             hits[i] = r;
+        }
+    };
+    if (refill > 0) {
+        const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+        const int64_t b0 = min(n, per * int64_t(blockIdx.x)), b1 = min(n, b0 + per);
+        if (threadIdx.x == 0) s_fetch = 0;
+        __syncthreads();
+        fetch_loop<kAnyHit, false>(
+            int(b1 - b0), Fetch{&s_fetch, nullptr, refill}, bvh, sb, sbits, stride, &lerr,
+            [&](int k, Trav& s, Bvh8&) {
+                const float4 a = rays[2 * (b0 + k)], b = rays[2 * (b0 + k) + 1];
+                trav_init(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
+            },
+            [&](int k, const Trav& s) { store(b0 + k, s.best); });
+    } else {
+        for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+            const float4 a = rays[2 * i], b = rays[2 * i + 1];
+            store(i, trace_bvh8<kAnyHit, false>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits, stride,
+                                                nullptr, nullptr, &lerr));
         }
     }
     if (lerr) atomicOr(err, lerr);
@@ -122,11 +142,13 @@ void launch_trace(const lmgpu_accel* a, const void* d_rays, int64_t n, void* d_h
     const size_t smem = trace_smem(a);
     if (d_occ) {
         const int g = trace_grid(k_trace_batch<true>, smem, n);
-        k_trace_batch<true><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n, nullptr, d_occ, d_err);
+        k_trace_batch<true><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n, nullptr, d_occ, d_err,
+                                                          tuning().trace_refill);
     } else {
         const int g = trace_grid(k_trace_batch<false>, smem, n);
         k_trace_batch<false><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n,
-                                                           static_cast<lmgpu_hit*>(d_hits), nullptr, d_err);
+                                                           static_cast<lmgpu_hit*>(d_hits), nullptr, d_err,
+                                                           tuning().trace_refill);
     }
     LMGPU_CUDA(cudaGetLastError());
 }

@@ -267,4 +267,57 @@ __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, f
     return s.best;
 }
 
+// Dynamic ray fetch for the persistent trace kernels: `self` hands out queue entries (zero at
+// launch); `other`, when set, is the counter of another trace kernel that this launch resets for
+// that kernel's next launch (the path tracers' extension and shadow kernels alternate on one
+// stream, so neither counter is in use while the other kernel runs). refill: see Tuning.
+struct Fetch {
+    int* self;
+    int* other;
+    int refill;
+};
+
+// Persistent traversal with dynamic ray fetch (Aila & Laine, HPG 2009): every lane of a warp
+// holds one ray in flight; once fewer than f.refill lanes still trace, the idle lanes take the
+// next entries of the queue (one atomic per warp), so a warp no longer waits for its slowest
+// ray. begin(k, s, B) loads entry k into the traversal state (and B, the BVH it traverses);
+// end(k, s) consumes the finished traversal. Called by every thread of full warps.
+template <bool kAnyHit, bool kCount, typename Begin, typename End>
+__device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bvh0, uint32_t* sb, uint32_t* sbits,
+                                           int stride, int* lerr, Begin begin, End end) {
+    const int lane = int(threadIdx.x & 31u);
+    const unsigned below = (1u << lane) - 1u;
+    Trav s;
+    Bvh8 B = bvh0;
+    int k = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        if (!exhausted) {
+            const unsigned idle = __ballot_sync(0xffffffffu, !active);
+            if (idle) {
+                const int leader = __ffs(idle) - 1;
+                int base = 0;
+                if (lane == leader) base = atomicAdd(f.self, __popc(idle));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (base + __popc(idle) >= n) exhausted = true;  // warp-uniform
+                if (!active) {
+                    k = base + __popc(idle & below);
+                    if (k < n) {
+                        begin(k, s, B);
+                        active = true;
+                    }
+                }
+            }
+        }
+        if (__ballot_sync(0xffffffffu, active) == 0u) break;
+        const int keep = exhausted ? 1 : f.refill;
+        do {
+            if (active && trav_step<kAnyHit, kCount>(B, s, sb, sbits, stride, lerr)) {
+                end(k, s);
+                active = false;
+            }
+        } while (__popc(__ballot_sync(0xffffffffu, active)) >= keep);
+    }
+}
+
 }  // namespace lmgpu

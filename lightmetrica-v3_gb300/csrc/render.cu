@@ -475,9 +475,18 @@ __device__ inline void rng_slots(uint32_t seed, uint64_t path, uint32_t vertex, 
     }
 }
 
+// Queue slot for the calling lane: one atomic per warp (the lanes that push together take
+// consecutive slots, so their stores coalesce).
+__device__ inline int queue_slot(int* count) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, int(g.size()));
+    return g.shfl(base, 0) + int(g.thread_rank());
+}
+
 template <bool kBatched>
 __device__ inline void push_shadow(const ShadowQ& sq, int* count, f3 o, f3 d, float tmax, f3 c, uint32_t pixel, uint32_t job) {
-    const int k = atomicAdd(count, 1);
+    const int k = queue_slot(count);
     sq.o[k] = make_float4(o.x, o.y, o.z, tmax);
     sq.d[k] = make_float4(d.x, d.y, d.z, 0.f);
     sq.c[k] = make_float4(c.x, c.y, c.z, __uint_as_float(pixel));
@@ -534,7 +543,7 @@ __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, c
 template <bool kBatched>
 __device__ inline void push_ext(const ExtQ& q, int* count, f3 o, f3 d, f3 thr, float pdf, f3 n, uint32_t flags, uint32_t path,
                                 uint32_t pixel, uint32_t job) {
-    const int k = atomicAdd(count, 1);
+    const int k = queue_slot(count);
     q.o[k] = make_float4(o.x, o.y, o.z, 0.f);
     q.d[k] = make_float4(d.x, d.y, d.z, 0.f);
     q.thr[k] = make_float4(thr.x, thr.y, thr.z, pdf);
@@ -619,58 +628,6 @@ __device__ inline void record_worst(unsigned long long* maxv, float* worst, uint
     }
 }
 
-// Dynamic ray fetch for the persistent trace kernels: `self` hands out queue entries, `other` is
-// the counter of the other trace kernel, which this launch resets for its next launch (the two
-// alternate on one stream, so neither is in use while the other runs). refill as in Tuning.
-struct Fetch {
-    int* self;
-    int* other;
-    int refill;
-};
-
-// Persistent traversal with dynamic ray fetch (Aila & Laine, HPG 2009): every lane of a warp
-// holds one ray in flight; once fewer than f.refill lanes still trace, the idle lanes take the
-// next entries of the queue (one atomic per warp), so a warp no longer waits for its slowest
-// ray. begin(k, s, B) loads entry k into the traversal state (and B, the BVH it traverses);
-// end(k, s) consumes the finished traversal. Called by every thread of full warps.
-template <bool kAnyHit, bool kCount, typename Begin, typename End>
-__device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bvh0, uint32_t* sb, uint32_t* sbits,
-                                           int stride, int* lerr, Begin begin, End end) {
-    const int lane = int(threadIdx.x & 31u);
-    const unsigned below = (1u << lane) - 1u;
-    Trav s;
-    Bvh8 B = bvh0;
-    int k = 0;
-    bool active = false, exhausted = false;
-    while (true) {
-        if (!exhausted) {
-            const unsigned idle = __ballot_sync(0xffffffffu, !active);
-            if (idle) {
-                const int leader = __ffs(idle) - 1;
-                int base = 0;
-                if (lane == leader) base = atomicAdd(f.self, __popc(idle));
-                base = __shfl_sync(0xffffffffu, base, leader);
-                if (base + __popc(idle) >= n) exhausted = true;  // warp-uniform
-                if (!active) {
-                    k = base + __popc(idle & below);
-                    if (k < n) {
-                        begin(k, s, B);
-                        active = true;
-                    }
-                }
-            }
-        }
-        if (__ballot_sync(0xffffffffu, active) == 0u) break;
-        const int keep = exhausted ? 1 : f.refill;
-        do {
-            if (active && trav_step<kAnyHit, kCount>(B, s, sb, sbits, stride, lerr)) {
-                end(k, s);
-                active = false;
-            }
-        } while (__popc(__ballot_sync(0xffffffffu, active)) >= keep);
-    }
-}
-
 // Extension rays: closest hit over [Eps, Inf]. kCount: rays with (k & count_mask) == 0 also count
 // node visits and triangle tests into sums[0..2] (instrumented runs only). kBatched: each entry
 // traverses its own job's BVH; bvh.depth is then the largest depth of the table (stack size).
@@ -685,7 +642,7 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
     const int n = *qcount;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(rays, (unsigned long long)n);
-        *f.other = 0;
+        if (f.other) *f.other = 0;
     }
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;
@@ -745,7 +702,7 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
     const int n = *scount;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(rays, (unsigned long long)n);
-        *f.other = 0;
+        if (f.other) *f.other = 0;
     }
     uint32_t* sb = smem + threadIdx.x;
     uint32_t* sbits = smem + blockDim.x * bvh.depth + threadIdx.x;

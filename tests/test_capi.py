@@ -56,3 +56,23 @@ def test_version(native_lib):
 
 def test_oracle_library_loads(oracle_mod):
     assert oracle_mod.max_threads() >= 1
+
+
+def test_tuning_keys(native_lib):
+    """lmgpu_tune_set/get: known keys round-trip, bad keys and out-of-range values are refused."""
+    L = native_lib
+    v = C.c_int64()
+    assert L.lmgpu_tune_get(b"trace_refill", C.byref(v)) == 0
+    old = v.value
+    assert 0 <= old <= 32
+    try:
+        assert L.lmgpu_tune_set(b"trace_refill", 7) == 0
+        assert L.lmgpu_tune_get(b"trace_refill", C.byref(v)) == 0 and v.value == 7
+        assert L.lmgpu_tune_set(b"trace_refill", 33) == 1
+        assert b"trace_refill" in L.lmgpu_last_error()
+        assert L.lmgpu_tune_set(b"no_such_key", 1) == 1
+        assert b"unknown tuning key" in L.lmgpu_last_error()
+        assert L.lmgpu_tune_get(b"no_such_key", C.byref(v)) == 1
+        assert L.lmgpu_tune_set(None, 1) == 1
+    finally:
+        assert L.lmgpu_tune_set(b"trace_refill", old) == 0
