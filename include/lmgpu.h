@@ -61,6 +61,8 @@ int lmgpu_version(void);
  *   "trace_refill"  persistent trace kernels of the path tracers: a warp's idle lanes fetch new
  *                   rays once fewer than this many lanes still trace (1..32; default 24); 0 runs
  *                   one ray per thread without refills.
+ *   "shade_minblocks" shade kernels: 256-thread blocks per SM their register budget must allow
+ *                   (2: up to 128 registers; 3: up to 80; 4: up to 64, the default).
  * Tuning changes speed only, never results. Process-wide; set it between renders. */
 int lmgpu_tune_set(const char* key, int64_t value);
 int lmgpu_tune_get(const char* key, int64_t* value);

@@ -170,6 +170,9 @@ int lmgpu_tune_set(const char* key, int64_t value) {
         if (k == "trace_refill") {
             if (value < 0 || value > 32) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "trace_refill must be in [0, 32]");
             tuning().trace_refill = int(value);
+        } else if (k == "shade_minblocks") {
+            if (value < 2 || value > 4) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "shade_minblocks must be 2, 3 or 4");
+            tuning().shade_minblocks = int(value);
         } else {
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
         }
@@ -181,6 +184,7 @@ int lmgpu_tune_get(const char* key, int64_t* value) {
         if (!key || !value) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         const std::string k(key);
         if (k == "trace_refill") *value = tuning().trace_refill;
+        else if (k == "shade_minblocks") *value = tuning().shade_minblocks;
         else throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
     });
 }

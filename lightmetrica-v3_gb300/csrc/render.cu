@@ -842,7 +842,10 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
     return true;
 }
 
-__global__ void __launch_bounds__(kBlock) k_pt_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+// kMinBlocks: resident 256-thread blocks per SM the register allocation must allow (2: up to 128
+// registers; 3: 80; 4: 64), selected at run time by the "shade_minblocks" tuning key.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_pt_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
                                                      ExtQ qi, const float4* __restrict__ hits, const int* __restrict__ qicount,
                                                      ExtQ qo, int* qocount, ShadowQ sq, int* scount, float* film) {
     const int n = *qicount;
@@ -852,7 +855,8 @@ __global__ void __launch_bounds__(kBlock) k_pt_shade(const __grid_constant__ Dev
 
 // Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
 // counter (warp-aggregated per pass).
-__global__ void __launch_bounds__(kBlock) k_wf_shade(const JobDev* __restrict__ jobs, ExtQ qi, const float4* __restrict__ hits,
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* __restrict__ jobs, ExtQ qi, const float4* __restrict__ hits,
                                                      const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
                                                      int* scount, unsigned int* pass_done) {
     const int n = *qicount;
@@ -930,6 +934,11 @@ __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lm
         film[3 * i + 2] = c.z;
     }
     if (lerr) atomicOr(err, lerr);
+}
+
+template <typename K>
+K pick_shade(K two, K three, K four, int minblocks) {
+    return minblocks <= 2 ? two : (minblocks == 3 ? three : four);
 }
 
 template <typename K>
@@ -1315,7 +1324,8 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         const int g_gen = grid_for(k_pt_generate, kBlock, 0);
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
-        const int g_shade = grid_for(k_pt_shade, kBlock, 0);
+        auto shade_k = pick_shade(k_pt_shade<2>, k_pt_shade<3>, k_pt_shade<4>, tuning().shade_minblocks);
+        const int g_shade = grid_for(shade_k, kBlock, 0);
         unsigned long long* sums = reinterpret_cast<unsigned long long*>(ws.counters.as<char>() + 64);  // 8 counters
         float* worst = reinterpret_cast<float*>(ws.counters.as<char>() + 128);                           // 2 rays
         const int cmask = prm->instrument == 2 ? 0 : 63;
@@ -1368,7 +1378,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 mark(K_SHADE);
-                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], ws.hits.as<float4>(), cnt + cur, q[1 - cur],
+                shade_k<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], ws.hits.as<float4>(), cnt + cur, q[1 - cur],
                                                       cnt + (1 - cur), sq, cnt + 2, film);
                 mark(-1);
                 mark(K_SHADOW);
@@ -1539,7 +1549,8 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
         const int g_gen = grid_for(k_pt_generate, kBlock, 0);
         const int g_ext = grid_for(k_pt_extend<false>, kBlock, tsmem);
         const int g_sh = grid_for(k_pt_shadow<false>, kBlock, tsmem);
-        const int g_shade = grid_for(k_pt_shade, kBlock, 0);
+        auto shade_k = pick_shade(k_pt_shade<2>, k_pt_shade<3>, k_pt_shade<4>, tuning().shade_minblocks);
+        const int g_shade = grid_for(shade_k, kBlock, 0);
 
         LMGPU_CUDA(cudaMemsetAsync(d_film, 0, size_t(npix) * 3 * sizeof(float), st));
         LMGPU_CUDA(cudaMemsetAsync(base, 0, kNoallocCounters, st));
@@ -1560,7 +1571,7 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
                                                                  63, nullptr, f_ext);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
-                k_pt_shade<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
+                shade_k<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
                                                       cnt + 2, d_film);
                 k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63,
                                                                 nullptr, f_sh);
@@ -1602,8 +1613,8 @@ struct lmgpu_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int32_t graph_depth = 0;
-    int graph_refill = -1;  // trace_refill the graph was captured with
-    int refill = 0;
+    int graph_refill = -1, graph_shade = -1;  // tuning the graph was captured with
+    int refill = 0, shade_minblocks = 3;
     int cur = 0;
     double elapsed_ms = 0;
     ~lmgpu_batch() {
@@ -1659,7 +1670,8 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
     bmax.depth = b->max_depth;
     const int g_ext = grid_for(k_pt_extend<false, true>, kBlock, tsmem);
     const int g_sh = grid_for(k_pt_shadow<false, true>, kBlock, tsmem);
-    const int g_shade = grid_for(k_wf_shade, kBlock, 0);
+    auto shade_k = pick_shade(k_wf_shade<2>, k_wf_shade<3>, k_wf_shade<4>, b->shade_minblocks);
+    const int g_shade = grid_for(shade_k, kBlock, 0);
     const int g_gen = grid_for(k_wf_generate, kBlock, 0);
     int* cnt = ctl_cnt(b);
     const JobDev* jobs = b->jobs.as<JobDev>();
@@ -1676,7 +1688,7 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
         k_pt_extend<false, true><<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
                                                                ctl_sums(b), 63, nullptr, f_ext, jobs, q[cur].job);
         LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
-        k_wf_shade<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
+        shade_k<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
                                                b->pass_done.as<unsigned int>());
         k_pt_shadow<false, true><<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
                                                               ctl_sums(b), 63, nullptr, f_sh, jobs);
@@ -1690,7 +1702,10 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
 
 void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     b->refill = tuning().trace_refill;
-    if (b->exec && !realloc && b->graph_depth == b->max_depth && b->graph_refill == b->refill) return;
+    b->shade_minblocks = tuning().shade_minblocks;
+    if (b->exec && !realloc && b->graph_depth == b->max_depth && b->graph_refill == b->refill &&
+        b->graph_shade == b->shade_minblocks)
+        return;
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
     cudaStream_t cs;
@@ -1699,7 +1714,7 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
     (void)grid_for(k_pt_extend<false, true>, kBlock, tsmem);
     (void)grid_for(k_pt_shadow<false, true>, kBlock, tsmem);
-    (void)grid_for(k_wf_shade, kBlock, 0);
+    (void)grid_for(pick_shade(k_wf_shade<2>, k_wf_shade<3>, k_wf_shade<4>, b->shade_minblocks), kBlock, 0);
     (void)grid_for(k_wf_generate, kBlock, 0);
     LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
@@ -1716,6 +1731,7 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     LMGPU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     b->graph_depth = b->max_depth;
     b->graph_refill = b->refill;
+    b->graph_shade = b->shade_minblocks;
     (void)st;
 }
 

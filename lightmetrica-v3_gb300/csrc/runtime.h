@@ -87,6 +87,8 @@ struct Tuning {
     // Persistent trace kernels: idle lanes of a warp fetch new rays once fewer than this many
     // lanes still trace (1..32); 0 runs one ray per thread, grid-stride, without refills.
     int trace_refill = 24;
+    // Shade kernels: resident blocks per SM their register budget allows (2, 3 or 4).
+    int shade_minblocks = 4;
 };
 Tuning& tuning();
 
