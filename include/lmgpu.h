@@ -45,8 +45,8 @@ typedef struct lmgpu_hit {
 typedef struct lmgpu_accel_stats {
     int64_t num_tris;
     int64_t num_nodes;       /* 8-wide nodes, 80 bytes each */
-    int32_t max_depth;       /* 8-wide levels, root = 1 */
-    int32_t reserved;
+    int32_t max_depth;       /* 8-wide levels, root = 1 (two-level: top + deepest BLAS) */
+    int32_t num_instances;   /* 0 for a single-level build */
     double build_seconds;    /* host SAH build + collapse + upload */
     double sah_cost;         /* SAH cost of the binary tree before collapsing */
     int64_t device_bytes;    /* nodes + triangles resident on the device */
@@ -83,6 +83,27 @@ int lmgpu_accel_destroy(lmgpu_accel* accel);
  * graph first). The caller passes the flattened triangles: tri_p holds num_tris x 9 floats, the
  * world-space p1, p2, p3 of each triangle in flattening order. The data is copied. */
 int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris);
+
+/* One instance of a bottom-level triangle set: `transform` is its world-from-local matrix, the top
+ * three rows of the 4x4 (row-major; the last row is 0 0 0 1). */
+typedef struct lmgpu_instance {
+    int32_t blas;
+    int32_t reserved;
+    float transform[12];
+} lmgpu_instance;
+
+/* Two-level build, the accel::embreeinstanced form of Accel::build (accel_embree_instanced.cpp:
+ * 84-230: one level of instancing; an instance group's subtree is flattened once in its own frame
+ * and shared by all its instances). tri_p holds the triangles of every bottom-level set (BLAS)
+ * back to back, each set in its own frame; BLAS b owns triangles [blas_offsets[b],
+ * blas_offsets[b + 1]). The top level is an 8-wide tree over the instances' world boxes. Hit
+ * indices count the instances' triangles in instance order: instance i's local triangle j is
+ * index id_base(i) + j with id_base(i) the sum of the earlier instances' BLAS sizes, the order in
+ * which a flattening of the same scene graph would list them. Triangle tests run in the
+ * instance's frame (ray moved by the fp32 inverse transform), so t, u, v agree with a flattened
+ * build up to that rounding. The data is copied. */
+int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const int64_t* blas_offsets, int32_t num_blas,
+                                const lmgpu_instance* instances, int32_t num_instances);
 
 /* Accel::intersect(Ray, tmin, tmax) (include/lm/accel.h:70; accel_sahbvh.cpp:269-299) over a
  * batch. Host buffers: rays is n x 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax); hits receives n

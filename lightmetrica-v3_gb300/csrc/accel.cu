@@ -1,5 +1,8 @@
 // Accel C-ABI (include/lmgpu.h): build the 8-wide BVH on the host, keep it resident on the
 // device, and trace batches of rays with one thread per ray.
+#include <algorithm>
+#include <array>
+#include <cmath>
 #include <chrono>
 #include <cstring>
 #include <mutex>
@@ -37,7 +40,7 @@ constexpr int kTraceBlock = 128;
 // of the rays and its warps fetch from it dynamically through a shared-memory counter (no state
 // outside the launch, so calls on several streams may overlap); 0: one ray per thread,
 // grid-stride.
-template <bool kAnyHit>
+template <bool kAnyHit, bool kTwoLevel>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const float4* __restrict__ rays, int64_t n,
                                                             lmgpu_hit* __restrict__ hits, uint8_t* __restrict__ occluded,
                                                             int* __restrict__ err, int refill) {
@@ -64,7 +67,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const flo
         const int64_t b0 = min(n, per * int64_t(blockIdx.x)), b1 = min(n, b0 + per);
         if (threadIdx.x == 0) s_fetch = 0;
         __syncthreads();
-        fetch_loop<kAnyHit, false>(
+        fetch_loop<kAnyHit, false, kTwoLevel>(
             int(b1 - b0), Fetch{&s_fetch, nullptr, refill}, bvh, sb, sbits, stride, &lerr,
             [&](int k, Trav& s, Bvh8&) {
                 const float4 a = rays[2 * (b0 + k)], b = rays[2 * (b0 + k) + 1];
@@ -74,7 +77,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const flo
     } else {
         for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
             const float4 a = rays[2 * i], b = rays[2 * i + 1];
-            store(i, trace_bvh8<kAnyHit, false>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits, stride,
+            store(i, trace_bvh8<kAnyHit, false, kTwoLevel>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits, stride,
                                                 nullptr, nullptr, &lerr));
         }
     }
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const flo
 }
 
 // Instrumented pass: node visits and triangle tests summed over every `sample`-th ray.
-template <bool kAnyHit>
+template <bool kAnyHit, bool kTwoLevel>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_count(Bvh8 bvh, const float4* __restrict__ rays, int64_t n,
                                                             int sample, unsigned long long* sums, int* err) {
     extern __shared__ uint32_t smem[];
@@ -94,7 +97,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_count(Bvh8 bvh, const flo
     for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j * sample < n; j += int64_t(gridDim.x) * blockDim.x) {
         const int64_t i = j * sample;
         const float4 a = rays[2 * i], b = rays[2 * i + 1];
-        trace_bvh8<kAnyHit, true>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits, stride, &nodes, &tris,
+        trace_bvh8<kAnyHit, true, kTwoLevel>(bvh, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w, sb, sbits, stride, &nodes, &tris,
                                   &lerr);
         cnt++;
     }
@@ -122,6 +125,8 @@ Bvh8 device_view(const lmgpu_accel* a) {
     b.tris = a->tris.as<const float4>();
     b.depth = a->depth;
     b.num_nodes = uint32_t(a->num_nodes);
+    b.inst = a->num_instances > 0 ? a->inst.as<const float4>() : nullptr;
+    b.max_visits = a->max_visits ? a->max_visits : uint32_t(a->num_nodes);
     return b;
 }
 
@@ -140,16 +145,14 @@ void launch_trace(const lmgpu_accel* a, const void* d_rays, int64_t n, void* d_h
         throw Error(LMGPU_ERR_INVALID_ARGUMENT, "ray buffer must be 16-byte aligned");
     const Bvh8 b = device_view(a);
     const size_t smem = trace_smem(a);
-    if (d_occ) {
-        const int g = trace_grid(k_trace_batch<true>, smem, n);
-        k_trace_batch<true><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n, nullptr, d_occ, d_err,
-                                                          tuning().trace_refill);
-    } else {
-        const int g = trace_grid(k_trace_batch<false>, smem, n);
-        k_trace_batch<false><<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n,
-                                                           static_cast<lmgpu_hit*>(d_hits), nullptr, d_err,
-                                                           tuning().trace_refill);
-    }
+    auto run = [&](auto kernel) {
+        const int g = trace_grid(kernel, smem, n);
+        kernel<<<g, kTraceBlock, smem, st>>>(b, static_cast<const float4*>(d_rays), n, static_cast<lmgpu_hit*>(d_hits), d_occ,
+                                             d_err, tuning().trace_refill);
+    };
+    const bool two = a->num_instances > 0;
+    if (d_occ) two ? run(k_trace_batch<true, true>) : run(k_trace_batch<true, false>);
+    else two ? run(k_trace_batch<false, true>) : run(k_trace_batch<false, false>);
     LMGPU_CUDA(cudaGetLastError());
 }
 
@@ -224,6 +227,142 @@ int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris) 
         accel->num_nodes = int64_t(h.nodes.size() / 20);
         accel->depth = h.max_depth;
         accel->sah_cost = h.sah_cost;
+        accel->inst.release();
+        accel->num_instances = 0;
+        accel->max_visits = 0;
+        accel->inst_blas.clear();
+        accel->inst_xform.clear();
+        accel->inst_id_base.clear();
+        accel->blas_offsets.clear();
+        LMGPU_CUDA(cudaDeviceSynchronize());
+        accel->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    });
+}
+
+int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const int64_t* blas_offsets, int32_t num_blas,
+                                const lmgpu_instance* instances, int32_t num_instances) {
+    return guarded([&] {
+        if (!accel || !tri_p || !blas_offsets || !instances) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (num_blas < 1 || num_instances < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "need at least one BLAS and one instance");
+        if (blas_offsets[0] != 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "blas_offsets[0] must be 0");
+        for (int32_t b = 0; b < num_blas; b++)
+            if (blas_offsets[b + 1] <= blas_offsets[b]) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "every BLAS needs a triangle");
+        const auto t0 = std::chrono::steady_clock::now();
+        // bottom level: one 8-wide tree per triangle set, hit indices local to the set
+        std::vector<Bvh8Host> bl(static_cast<size_t>(num_blas));
+        std::vector<std::array<double, 6>> lbox(static_cast<size_t>(num_blas));
+        for (int32_t b = 0; b < num_blas; b++) {
+            const int64_t off = blas_offsets[b], cnt = blas_offsets[b + 1] - off;
+            std::string err;
+            if (!build_bvh8(tri_p + 9 * off, cnt, bl[b], &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+            std::array<double, 6> bx{1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+            for (int64_t i = 9 * off; i < 9 * (off + cnt); i += 3)
+                for (int a = 0; a < 3; a++) {
+                    bx[a] = std::min(bx[a], double(tri_p[i + a]));
+                    bx[3 + a] = std::max(bx[3 + a], double(tri_p[i + a]));
+                }
+            lbox[b] = bx;
+        }
+        // instances: inverse transforms, world boxes (the 8 transformed corners of the BLAS box,
+        // rounded outward to fp32), first hit indices
+        std::vector<float> tl(size_t(9) * num_instances);
+        std::vector<float4> rec(size_t(4) * num_instances);
+        std::vector<int64_t> id_base(static_cast<size_t>(num_instances));
+        std::vector<double> xf(size_t(12) * num_instances);
+        int64_t total = 0;
+        for (int32_t i = 0; i < num_instances; i++) {
+            const lmgpu_instance& in = instances[i];
+            if (in.blas < 0 || in.blas >= num_blas) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "instance refers to a missing BLAS");
+            double M[12];
+            for (int k = 0; k < 12; k++) {
+                M[k] = double(in.transform[k]);
+                if (!std::isfinite(M[k])) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "non-finite instance transform");
+                xf[size_t(12) * i + k] = M[k];
+            }
+            const double a00 = M[0], a01 = M[1], a02 = M[2], a10 = M[4], a11 = M[5], a12 = M[6], a20 = M[8], a21 = M[9], a22 = M[10];
+            const double det = a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
+            if (!(std::fabs(det) > 1e-30)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "singular instance transform");
+            const double inv[9] = {(a11 * a22 - a12 * a21) / det, (a02 * a21 - a01 * a22) / det, (a01 * a12 - a02 * a11) / det,
+                                   (a12 * a20 - a10 * a22) / det, (a00 * a22 - a02 * a20) / det, (a02 * a10 - a00 * a12) / det,
+                                   (a10 * a21 - a11 * a20) / det, (a01 * a20 - a00 * a21) / det, (a00 * a11 - a01 * a10) / det};
+            const double t[3] = {M[3], M[7], M[11]};
+            for (int r = 0; r < 3; r++) {
+                const double tr = -(inv[3 * r] * t[0] + inv[3 * r + 1] * t[1] + inv[3 * r + 2] * t[2]);
+                rec[4 * size_t(i) + r] = make_float4(float(inv[3 * r]), float(inv[3 * r + 1]), float(inv[3 * r + 2]), float(tr));
+            }
+            const auto& bx = lbox[in.blas];
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            for (int c = 0; c < 8; c++) {
+                const double p[3] = {bx[(c & 1) ? 3 : 0], bx[(c & 2) ? 4 : 1], bx[(c & 4) ? 5 : 2]};
+                for (int r = 0; r < 3; r++) {
+                    const double w = M[4 * r] * p[0] + M[4 * r + 1] * p[1] + M[4 * r + 2] * p[2] + M[4 * r + 3];
+                    lo[r] = std::min(lo[r], w);
+                    hi[r] = std::max(hi[r], w);
+                }
+            }
+            for (int r = 0; r < 3; r++) {
+                // pad by a relative 2^-20 for the fp32 rounding of the ray transform, then round outward
+                const double pad = 1e-6 * std::max({std::fabs(lo[r]), std::fabs(hi[r]), hi[r] - lo[r], 1e-30});
+                float l = float(lo[r] - pad), h = float(hi[r] + pad);
+                if (double(l) > lo[r] - pad) l = std::nextafter(l, -INFINITY);
+                if (double(h) < hi[r] + pad) h = std::nextafter(h, INFINITY);
+                tl[9 * size_t(i) + r] = l;
+                tl[9 * size_t(i) + 3 + r] = h;
+                tl[9 * size_t(i) + 6 + r] = l;
+            }
+            id_base[i] = total;
+            total += blas_offsets[in.blas + 1] - blas_offsets[in.blas];
+        }
+        if (total > (int64_t(1) << 31) - 1) throw Error(LMGPU_ERR_UNSUPPORTED, "more than 2^31-1 instanced triangles");
+        // top level over the instance boxes; its leaves are instance pseudo-nodes
+        Bvh8Host top;
+        std::string err;
+        BuildOptions opt;
+        opt.leaf_nodes = true;
+        if (!build_bvh8(tl.data(), num_instances, top, &err, opt)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+        // one node array: top level first, then every BLAS with its child and triangle bases moved
+        std::vector<uint32_t> nodes = top.nodes;
+        std::vector<float> tris;
+        std::vector<uint32_t> root(static_cast<size_t>(num_blas));
+        std::vector<uint64_t> bnodes(static_cast<size_t>(num_blas));
+        int32_t bdepth = 0;
+        for (int32_t b = 0; b < num_blas; b++) {
+            const uint32_t noff = uint32_t(nodes.size() / 20), toff = uint32_t(tris.size() / 12);
+            root[b] = noff;
+            bnodes[b] = bl[b].nodes.size() / 20;
+            for (size_t k = 0; k < bl[b].nodes.size(); k += 20) {
+                uint32_t w[20];
+                std::memcpy(w, &bl[b].nodes[k], sizeof(w));
+                w[4] += noff;
+                w[5] += toff;
+                nodes.insert(nodes.end(), w, w + 20);
+            }
+            tris.insert(tris.end(), bl[b].tris.begin(), bl[b].tris.end());
+            bdepth = std::max(bdepth, bl[b].max_depth);
+        }
+        if (nodes.size() / 20 > size_t(UINT32_MAX)) throw Error(LMGPU_ERR_UNSUPPORTED, "too many BVH nodes");
+        uint64_t visits = top.nodes.size() / 20;
+        for (int32_t i = 0; i < num_instances; i++) {
+            visits += bnodes[instances[i].blas];
+            const uint32_t rb[4] = {root[instances[i].blas], uint32_t(id_base[i]), 0u, 0u};
+            std::memcpy(&rec[4 * size_t(i) + 3], rb, sizeof(rb));
+        }
+        accel->nodes.upload(nodes.data(), nodes.size());
+        accel->tris.upload(tris.data(), tris.size());
+        accel->inst.upload(rec.data(), rec.size());
+        accel->err.alloc(sizeof(int));
+        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
+        accel->num_tris = total;
+        accel->num_nodes = int64_t(nodes.size() / 20);
+        accel->depth = top.max_depth + bdepth;
+        accel->sah_cost = top.sah_cost;
+        accel->num_instances = num_instances;
+        accel->max_visits = uint32_t(std::min<uint64_t>(visits, UINT32_MAX));
+        accel->inst_blas.resize(size_t(num_instances));
+        for (int32_t i = 0; i < num_instances; i++) accel->inst_blas[i] = instances[i].blas;
+        accel->inst_xform = xf;
+        accel->inst_id_base = id_base;
+        accel->blas_offsets.assign(blas_offsets, blas_offsets + num_blas + 1);
         LMGPU_CUDA(cudaDeviceSynchronize());
         accel->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     });
@@ -271,7 +410,8 @@ int lmgpu_accel_get_stats(const lmgpu_accel* accel, lmgpu_accel_stats* out) {
         out->max_depth = accel->depth;
         out->build_seconds = accel->build_seconds;
         out->sah_cost = accel->sah_cost;
-        out->device_bytes = int64_t(accel->nodes.bytes + accel->tris.bytes);
+        out->device_bytes = int64_t(accel->nodes.bytes + accel->tris.bytes + accel->inst.bytes);
+        out->num_instances = accel->num_instances;
     });
 }
 
@@ -304,15 +444,14 @@ int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, 
         const Bvh8 b = device_view(accel);
         const size_t smem = trace_smem(accel);
         const int64_t m = (n + sample - 1) / sample;
-        if (any_hit) {
-            const int g = trace_grid(k_trace_count<true>, smem, m);
-            k_trace_count<true><<<g, kTraceBlock, smem>>>(b, static_cast<const float4*>(d_rays), n, sample,
-                                                          sums.as<unsigned long long>(), accel->err.as<int>());
-        } else {
-            const int g = trace_grid(k_trace_count<false>, smem, m);
-            k_trace_count<false><<<g, kTraceBlock, smem>>>(b, static_cast<const float4*>(d_rays), n, sample,
-                                                           sums.as<unsigned long long>(), accel->err.as<int>());
-        }
+        auto run = [&](auto kernel) {
+            const int g = trace_grid(kernel, smem, m);
+            kernel<<<g, kTraceBlock, smem>>>(b, static_cast<const float4*>(d_rays), n, sample, sums.as<unsigned long long>(),
+                                             accel->err.as<int>());
+        };
+        const bool two = accel->num_instances > 0;
+        if (any_hit) two ? run(k_trace_count<true, true>) : run(k_trace_count<true, false>);
+        else two ? run(k_trace_count<false, true>) : run(k_trace_count<false, false>);
         LMGPU_CUDA(cudaGetLastError());
         unsigned long long h[3];
         LMGPU_CUDA(cudaMemcpy(h, sums.p, sizeof(h), cudaMemcpyDeviceToHost));

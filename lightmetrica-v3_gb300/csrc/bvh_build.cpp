@@ -198,7 +198,7 @@ bool quantize(const AABB& nb, const AABB* cbox, const bool* valid, int eb_out[3]
 
 }  // namespace
 
-bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) {
+bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err, const BuildOptions& opt) {
     out = Bvh8Host();
     if (n <= 0) {
         if (err) *err = "accel build: no triangles";
@@ -253,7 +253,8 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
         const float A = float(b.box.area());
         float* c = &cost[size_t(ni) * 8];
         int8_t* d = &dec[size_t(ni) * 8];
-        const float cleaf = b.count <= kMaxLeaf ? A * kCPrim * float(b.count) : inf;
+        const int max_leaf = opt.leaf_nodes ? 1 : kMaxLeaf;
+        const float cleaf = b.count <= max_leaf ? A * kCPrim * float(b.count) : inf;
         if (b.left < 0) {
             for (int i = 0; i < 8; i++) { c[i] = cleaf; d[i] = 0; }
             continue;
@@ -300,7 +301,7 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
     std::vector<Pending> queue;
     queue.push_back({0, 0, 1});
     out.nodes.assign(20, 0);
-    out.tris.reserve(size_t(12) * n);
+    if (!opt.leaf_nodes) out.tris.reserve(size_t(12) * n);
     size_t qi = 0;
     int32_t max_depth = 1;
     std::vector<Child> kids;
@@ -379,11 +380,22 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
                 const int32_t wi = int32_t(out.nodes.size() / 20);
                 out.nodes.resize(out.nodes.size() + 20, 0);
                 queue.push_back({ch[i], wi, pd.depth + 1});
+            } else if (opt.leaf_nodes) {
+                if (c.count != 1) {
+                    if (err) *err = "accel build: internal error (top-level leaf size)";
+                    return false;
+                }
+                imask |= uint8_t(1u << s);
+                meta[s] = 0x80;
+                const size_t wi = out.nodes.size();
+                out.nodes.resize(out.nodes.size() + 20, 0);
+                out.nodes[wi + 3] = kInstanceMarker;
+                out.nodes[wi + 4] = uint32_t(B.idx[c.start]);
             }
         }
         for (int s = 0; s < 8; s++) {
             const int i = child_in[s];
-            if (i < 0 || (imask >> s) & 1) continue;  // empty or internal
+            if (i < 0 || (imask >> s) & 1) continue;  // empty, internal or an instance pseudo-node
             const BinNode& c = B.nodes[ch[i]];
             const uint32_t off = uint32_t(out.tris.size() / 12) - tri_base;
             if (c.count < 1 || c.count > kMaxLeaf || off > 31) {
@@ -423,7 +435,7 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err) 
         w[16] = pack4(qhi[1]); w[17] = pack4(qhi[1] + 4); w[18] = pack4(qhi[2]); w[19] = pack4(qhi[2] + 4);
     }
     out.max_depth = max_depth;
-    if (int64_t(out.tris.size() / 12) != n) {
+    if (!opt.leaf_nodes && int64_t(out.tris.size() / 12) != n) {
         if (err) *err = "accel build: internal error (triangle count)";
         return false;
     }

@@ -36,8 +36,19 @@ struct Bvh8Host {
     double sah_cost = 0;
 };
 
-// tri_p: n x 9 floats (p1, p2, p3). Returns false with `err` set on invalid input.
-bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err);
+// Top-level (instance) trees: every leaf holds exactly one primitive and is written as a child
+// pseudo-node instead of triangle records, marked by an exponent byte ex = 0xFF (no real node
+// uses it) and carrying the primitive index in child_base (w1.x). The traversal enters the
+// instance there.
+constexpr uint32_t kInstanceMarker = 0xFFu;
+
+struct BuildOptions {
+    bool leaf_nodes = false;  // top-level mode (see above); tris stays empty
+};
+
+// tri_p: n x 9 floats (p1, p2, p3); in top-level mode each "triangle" is (lo, hi, lo) of one
+// instance's world box. Returns false with `err` set on invalid input.
+bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err, const BuildOptions& opt = {});
 
 // Decoded view of one node, for tests and debugging.
 struct Bvh8NodeView {

@@ -73,7 +73,11 @@ struct Bvh8 {
     const uint4* nodes;   // 5 words per node
     const float4* tris;   // 3 words per triangle
     int32_t depth;        // levels; bounds the traversal stack
-    uint32_t num_nodes;   // a ray visits each node at most once; more visits flag corruption
+    uint32_t num_nodes;   // node index bound
+    // Two-level trees (instancing): per instance 4 float4, the rows of its local-from-world
+    // transform and {root node, first hit index, 0, 0} as bits; null for single-level trees.
+    const float4* inst;
+    uint32_t max_visits;  // node visits one ray can make; more flag corruption
 };
 
 struct TraceHit {
@@ -123,6 +127,14 @@ __device__ inline uint32_t oct_permute(uint32_t m, uint32_t oct) {
 // The traversal is a resumable state (Trav) advanced one node visit at a time by trav_step, so
 // a persistent kernel can interleave rays on a lane (dynamic ray fetch); trace_bvh8 runs one ray
 // to the end. Either way a ray's visits, tests and result are the same.
+//
+// Two-level trees (kTwoLevel): a top-level child whose node carries the instance marker
+// (exponent byte 0xFF) stands for one instance. Visiting it saves the world ray, moves the ray
+// into the instance's local frame (o' = M^-1 o, d' = M^-1 d, not renormalized, so t keeps its
+// meaning and best.t stays valid), records the stack level and continues at the instance's BLAS
+// root; hit indices get the instance's first hit index added. When the traversal pops back to
+// the recorded level the world ray is restored and the top level resumes. One instancing level,
+// as accel::embreeinstanced builds (accel_embree_instanced.cpp:84-230).
 struct Trav {
     f3 o, d, inv;
     float tmin;
@@ -131,13 +143,15 @@ struct Trav {
     uint32_t node;
     uint32_t nvis, ntri;
     TraceHit best;
+    // two-level only (never read, so never allocated, in single-level code)
+    f3 wo, wd;
+    int inst_sp;
+    int32_t id_base;
 };
 
-__device__ inline void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
+__device__ inline void trav_set_ray(Trav& s, f3 o, f3 d) {
     s.o = o;
     s.d = d;
-    s.tmin = tmin;
-    s.best = TraceHit{tmax, 0.f, 0.f, -1};
     // Slab reciprocals from a direction whose zero (or tiny) components are replaced by +-1e-20,
     // keeping the sign: every slab distance stays finite (an exact zero would give infinities and
     // then NaN in the one-FMA form, which would disable culling on that axis). The triangle test
@@ -147,23 +161,49 @@ __device__ inline void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
     const float dzs = fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z);
     s.inv = {1.0f / dxs, 1.0f / dys, 1.0f / dzs};
     s.oct = (signbit(d.x) ? 1u : 0u) | (signbit(d.y) ? 2u : 0u) | (signbit(d.z) ? 4u : 0u);
+}
+
+__device__ inline void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
+    trav_set_ray(s, o, d);
+    s.tmin = tmin;
+    s.best = TraceHit{tmax, 0.f, 0.f, -1};
     s.sp = 0;
     s.node = 0;
     s.nvis = 0;
     s.ntri = 0;
+    s.inst_sp = -1;
+    s.id_base = 0;
 }
 
 // Visits s.node (testing the triangles of every leaf child the ray enters) and moves to the next
 // node. Returns true when the traversal has ended; s.best is then the result. Sets *err (and
 // ends) on a stack overflow (1) or a visit count above the node count (2), which only a corrupt
 // BVH can cause.
-template <bool kAnyHit, bool kCount>
+template <bool kAnyHit, bool kCount, bool kTwoLevel = false>
 __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* stk_base, uint32_t* stk_bits, int stride,
                                           int* err) {
-    if (s.node >= bvh.num_nodes || s.nvis >= bvh.num_nodes) { *err = 2; return true; }
+    if (s.node >= bvh.num_nodes || s.nvis >= bvh.max_visits) { *err = 2; return true; }
     const uint4* np = bvh.nodes + size_t(s.node) * 5;
-    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1);
     s.nvis++;
+    if (kTwoLevel && (w0.w & 0xffu) == 0xffu) {
+        // instance pseudo-node: continue in the instance's frame at its BLAS root
+        const float4* ip = bvh.inst + size_t(w1.x) * 4;
+        const float4 r0 = __ldg(ip), r1 = __ldg(ip + 1), r2 = __ldg(ip + 2);
+        const uint4 m = __ldg(reinterpret_cast<const uint4*>(ip + 3));
+        s.wo = s.o;
+        s.wd = s.d;
+        const f3 lo = {r0.x * s.o.x + r0.y * s.o.y + r0.z * s.o.z + r0.w, r1.x * s.o.x + r1.y * s.o.y + r1.z * s.o.z + r1.w,
+                       r2.x * s.o.x + r2.y * s.o.y + r2.z * s.o.z + r2.w};
+        const f3 ld = {r0.x * s.d.x + r0.y * s.d.y + r0.z * s.d.z, r1.x * s.d.x + r1.y * s.d.y + r1.z * s.d.z,
+                       r2.x * s.d.x + r2.y * s.d.y + r2.z * s.d.z};
+        trav_set_ray(s, lo, ld);
+        s.inst_sp = s.sp;
+        s.id_base = int32_t(m.y);
+        s.node = m.x;
+        return false;
+    }
+    const uint4 w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
     const uint32_t oct = s.oct;
     // Slab distances with one FMA per plane. Plane q of an axis lies at p + q*s; with
     // a = s*inv and b = (p - o)*inv, t = q*a + b. The byte is unpacked straight into the float
@@ -220,7 +260,7 @@ __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* st
             if (kCount) s.ntri++;
             float t, u, v;
             if (tri_test(s.o, s.d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), s.tmin, s.best.t, t, u, v)) {
-                const int32_t id = int32_t(__float_as_uint(c.y));
+                const int32_t id = (kTwoLevel ? s.id_base : 0) + int32_t(__float_as_uint(c.y));
                 if (kAnyHit) {
                     s.best = TraceHit{t, u, v, id};
                     return true;
@@ -233,6 +273,11 @@ __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* st
     uint32_t inner = oct_permute(hitmask & imask, oct);
     uint32_t g_base = w1.x, g_imask = imask;
     if (inner == 0u) {
+        if (kTwoLevel && s.sp == s.inst_sp) {  // the instance is done: back to the world ray
+            trav_set_ray(s, s.wo, s.wd);
+            s.inst_sp = -1;
+            s.id_base = 0;
+        }
         if (s.sp == 0) return true;
         s.sp--;
         g_base = stk_base[s.sp * stride];
@@ -242,7 +287,7 @@ __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* st
     }
     const int k = __ffs(inner) - 1;
     inner &= inner - 1;
-    const uint32_t slot = uint32_t(k) ^ oct;
+    const uint32_t slot = uint32_t(k) ^ s.oct;
     s.node = g_base + __popc(g_imask & ((1u << slot) - 1u));
     if (inner != 0u) {
         if (s.sp >= bvh.depth) { *err = 1; return true; }
@@ -255,13 +300,13 @@ __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* st
 
 // One ray to the end. Adds the node visits and triangle tests to *nodes_visited / *tris_tested
 // when kCount.
-template <bool kAnyHit, bool kCount>
+template <bool kAnyHit, bool kCount, bool kTwoLevel = false>
 __device__ inline TraceHit trace_bvh8(const Bvh8& bvh, f3 o, f3 d, float tmin, float tmax, uint32_t* stk_base,
                                       uint32_t* stk_bits, int stride, uint32_t* nodes_visited, uint32_t* tris_tested,
                                       int* err) {
     Trav s;
     trav_init(s, o, d, tmin, tmax);
-    while (!trav_step<kAnyHit, kCount>(bvh, s, stk_base, stk_bits, stride, err)) {
+    while (!trav_step<kAnyHit, kCount, kTwoLevel>(bvh, s, stk_base, stk_bits, stride, err)) {
     }
     if (kCount) { *nodes_visited += s.nvis; *tris_tested += s.ntri; }
     return s.best;
@@ -282,7 +327,7 @@ struct Fetch {
 // next entries of the queue (one atomic per warp), so a warp no longer waits for its slowest
 // ray. begin(k, s, B) loads entry k into the traversal state (and B, the BVH it traverses);
 // end(k, s) consumes the finished traversal. Called by every thread of full warps.
-template <bool kAnyHit, bool kCount, typename Begin, typename End>
+template <bool kAnyHit, bool kCount, bool kTwoLevel, typename Begin, typename End>
 __device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bvh0, uint32_t* sb, uint32_t* sbits,
                                            int stride, int* lerr, Begin begin, End end) {
     const int lane = int(threadIdx.x & 31u);
@@ -312,7 +357,7 @@ __device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bv
         if (__ballot_sync(0xffffffffu, active) == 0u) break;
         const int keep = exhausted ? 1 : f.refill;
         do {
-            if (active && trav_step<kAnyHit, kCount>(B, s, sb, sbits, stride, lerr)) {
+            if (active && trav_step<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr)) {
                 end(k, s);
                 active = false;
             }

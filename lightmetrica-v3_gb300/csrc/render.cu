@@ -51,6 +51,10 @@ struct DevScene {
     f3 cam_p, cam_u, cam_v, cam_w;
     float tf, aspect;
     int32_t has_camera;
+    // Two-level scenes: shading records are per BLAS in the BLAS's frame; per instance 7 float4:
+    // world-from-local rows (3), normal-matrix rows (3), {first hit index, first shading record}.
+    const float4* inst;
+    int32_t num_inst;      // 0: records are in world space, indexed by hit index
 };
 
 }  // namespace lmgpu
@@ -59,6 +63,7 @@ struct lmgpu_scene {
     lmgpu_accel* accel = nullptr;
     lmgpu::DevScene dev{};
     lmgpu::DevBuf shade, prim_ml, mats, lights, ltri, cdf, env;
+    lmgpu::DevBuf inst;      // two-level scenes: per-instance shading transforms
     lmgpu::DevBuf counters;  // raycast error flag
 };
 
@@ -132,6 +137,34 @@ __device__ inline float sn_correction(const Geom& g, f3 wi, f3 wo) {
 }
 
 __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float v, int32_t& prim) {
+    if (S.num_inst > 0) {
+        // instance holding hit index id (the last whose first hit index is <= id), then the local
+        // surface point moved to world space as scene.cpp:335-343 does with the hit's transform
+        int lo = 0, hi = S.num_inst;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (int32_t(__float_as_uint(__ldg(S.inst + 7 * size_t(mid) + 6).x)) <= id) lo = mid; else hi = mid;
+        }
+        const float4* ip = S.inst + 7 * size_t(lo);
+        const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
+        const float4 q0 = __ldg(ip + 3), q1 = __ldg(ip + 4), q2 = __ldg(ip + 5), mt = __ldg(ip + 6);
+        const int64_t rec = int64_t(__float_as_uint(mt.y)) + (id - int32_t(__float_as_uint(mt.x)));
+        const float4* sp = S.shade + size_t(rec) * 6;
+        const float4 s0 = __ldg(sp), s1 = __ldg(sp + 1), s2 = __ldg(sp + 2), s3 = __ldg(sp + 3), s4 = __ldg(sp + 4),
+                     s5 = __ldg(sp + 5);
+        const f3 p1 = mk(s0.x, s0.y, s0.z), p2 = mk(s0.w, s1.x, s1.y), p3 = mk(s1.z, s1.w, s2.x);
+        const f3 n1 = mk(s2.y, s2.z, s2.w), n2 = mk(s3.x, s3.y, s3.z), n3 = mk(s3.w, s4.x, s4.y);
+        const f3 gl = mk(s4.z, s4.w, s5.x);
+        prim = int32_t(__float_as_uint(s5.y));
+        const float b0 = 1.f - u - v;
+        const f3 pl = p1 * b0 + p2 * u + p3 * v;
+        const f3 nl = normalize(n1 * b0 + n2 * u + n3 * v);
+        const f3 p = mk(m0.x * pl.x + m0.y * pl.y + m0.z * pl.z + m0.w, m1.x * pl.x + m1.y * pl.y + m1.z * pl.z + m1.w,
+                        m2.x * pl.x + m2.y * pl.y + m2.z * pl.z + m2.w);
+        const f3 n = normalize(mk(dot(mk(q0.x, q0.y, q0.z), nl), dot(mk(q1.x, q1.y, q1.z), nl), dot(mk(q2.x, q2.y, q2.z), nl)));
+        const f3 gn = normalize(mk(dot(mk(q0.x, q0.y, q0.z), gl), dot(mk(q1.x, q1.y, q1.z), gl), dot(mk(q2.x, q2.y, q2.z), gl)));
+        return on_surface(p, n, gn);
+    }
     const float4* sp = S.shade + size_t(id) * 6;
     const float4 s0 = __ldg(sp), s1 = __ldg(sp + 1), s2 = __ldg(sp + 2), s3 = __ldg(sp + 3), s4 = __ldg(sp + 4),
                  s5 = __ldg(sp + 5);
@@ -632,7 +665,7 @@ __device__ inline void record_worst(unsigned long long* maxv, float* worst, uint
 // node visits and triangle tests into sums[0..2] (instrumented runs only). kBatched: each entry
 // traverses its own job's BVH; bvh.depth is then the largest depth of the table (stack size).
 // f.refill > 0: persistent with dynamic fetch; 0: one ray per thread, grid-stride.
-template <bool kCount, bool kBatched = false>
+template <bool kCount, bool kBatched = false, bool kTwoLevel = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh8 bvh, const float4* __restrict__ qo, const float4* __restrict__ qd,
                                                       const int* __restrict__ qcount, float4* __restrict__ hits,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
@@ -649,7 +682,7 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
     int lerr = 0;
     uint32_t cn = 0, ct = 0, cc = 0;
     if (f.refill > 0) {
-        fetch_loop<false, kCount>(
+        fetch_loop<false, kCount, kTwoLevel>(
             n, f, bvh, sb, sbits, int(blockDim.x), &lerr,
             [&](int k, Trav& s, Bvh8& B) {
                 const float4 o = qo[k], d = qd[k];
@@ -673,12 +706,12 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
             TraceHit h;
             if (kCount && (k & count_mask) == 0) {
                 const uint32_t before = cn;
-                h = trace_bvh8<false, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
+                h = trace_bvh8<false, true, kTwoLevel>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x, &cn,
                                             &ct, &lerr);
                 cc++;
                 record_worst(sums + 6, worst, cn - before, o, d, kEps, kInf);
             } else {
-                h = trace_bvh8<false, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
+                h = trace_bvh8<false, false, kTwoLevel>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, kInf, sb, sbits, blockDim.x,
                                              nullptr, nullptr, &lerr);
             }
             hits[k] = make_float4(h.t, h.u, h.v, __int_as_float(h.id));
@@ -694,7 +727,7 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
 
 // Shadow rays: any hit over [Eps, tmax]; unoccluded contributions go to the film. kCount,
 // kBatched and f as in k_pt_extend; counts into sums[3..5].
-template <bool kCount, bool kBatched = false>
+template <bool kCount, bool kBatched = false, bool kTwoLevel = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
                                                       int count_mask, float* worst, Fetch f, const JobDev* __restrict__ jobs = nullptr) {
@@ -709,7 +742,7 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
     int lerr = 0;
     uint32_t cn = 0, ct = 0, cc = 0;
     if (f.refill > 0) {
-        fetch_loop<true, kCount>(
+        fetch_loop<true, kCount, kTwoLevel>(
             n, f, bvh, sb, sbits, int(blockDim.x), &lerr,
             [&](int k, Trav& s, Bvh8& B) {
                 const float4 o = sq.o[k], d = sq.d[k];
@@ -737,12 +770,12 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
             TraceHit h;
             if (kCount && (k & count_mask) == 0) {
                 const uint32_t before = cn;
-                h = trace_bvh8<true, true>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
+                h = trace_bvh8<true, true, kTwoLevel>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x, &cn,
                                            &ct, &lerr);
                 cc++;
                 record_worst(sums + 7, worst + 8, cn - before, o, d, kEps, o.w);
             } else {
-                h = trace_bvh8<true, false>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
+                h = trace_bvh8<true, false, kTwoLevel>(B, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), kEps, o.w, sb, sbits, blockDim.x,
                                             nullptr, nullptr, &lerr);
             }
             if (h.id < 0) {
@@ -894,6 +927,7 @@ __global__ void k_scale(const float* __restrict__ in, float* __restrict__ out, i
 }
 
 // renderer::raycast, one thread per pixel (renderer_raycast.cpp:70-98)
+template <bool kTwoLevel>
 __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lmgpu_raycast_params prm, float* film, int* err) {
     extern __shared__ uint32_t smem[];
     uint32_t* sb = smem + threadIdx.x;
@@ -904,7 +938,8 @@ __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lm
         const int x = int(i % w), y = int(i / w);
         const float rx = ieee::div(ieee::add(float(x), .5f), float(w)), ry = ieee::div(ieee::add(float(y), .5f), float(h));
         const f3 d = primary_dir(S, rx, ry);
-        const TraceHit hit = trace_bvh8<false, false>(S.bvh, S.cam_p, d, kEps, kInf, sb, sbits, blockDim.x, nullptr, nullptr, &lerr);
+        const TraceHit hit =
+            trace_bvh8<false, false, kTwoLevel>(S.bvh, S.cam_p, d, kEps, kInf, sb, sbits, blockDim.x, nullptr, nullptr, &lerr);
         f3 c;
         if (hit.id < 0) {
             if (S.env_light >= 0) {
@@ -1042,7 +1077,8 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
     return guarded([&] {
         if (!out || !accel || !D) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         if (accel->num_nodes == 0) throw Error(LMGPU_ERR_UNINITIALIZED, "accel is not built");
-        if (D->num_tris != accel->num_tris)
+        const bool two_level = accel->num_instances > 0;
+        if (D->num_tris != (two_level ? accel->blas_offsets.back() : accel->num_tris))
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "scene triangle count differs from the accel's");
         if (D->num_tris > 0 && (!D->positions || !D->normals || !D->geo_normals || !D->tri_prim))
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "missing per-triangle arrays");
@@ -1067,6 +1103,29 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
             std::memcpy(r + 21, &p, 4);
         }
         s->shade.upload(shade.data(), shade.size());
+        if (two_level) {
+            // per instance: world-from-local rows, normal-matrix rows (inverse transpose of the
+            // linear part, math.h:742-745), first hit index, first shading record of its BLAS
+            std::vector<float4> it(size_t(7) * accel->num_instances);
+            for (int32_t i = 0; i < accel->num_instances; i++) {
+                const double* M = &accel->inst_xform[size_t(12) * i];
+                const double a00 = M[0], a01 = M[1], a02 = M[2], a10 = M[4], a11 = M[5], a12 = M[6], a20 = M[8], a21 = M[9],
+                             a22 = M[10];
+                const double det = a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
+                // inverse transpose: (A^-1)^T = cofactor(A) / det
+                const double nm[9] = {(a11 * a22 - a12 * a21) / det, (a12 * a20 - a10 * a22) / det, (a10 * a21 - a11 * a20) / det,
+                                      (a02 * a21 - a01 * a22) / det, (a00 * a22 - a02 * a20) / det, (a01 * a20 - a00 * a21) / det,
+                                      (a01 * a12 - a02 * a11) / det, (a02 * a10 - a00 * a12) / det, (a00 * a11 - a01 * a10) / det};
+                float4* r = &it[size_t(7) * i];
+                for (int k = 0; k < 3; k++) {
+                    r[k] = make_float4(float(M[4 * k]), float(M[4 * k + 1]), float(M[4 * k + 2]), float(M[4 * k + 3]));
+                    r[3 + k] = make_float4(float(nm[3 * k]), float(nm[3 * k + 1]), float(nm[3 * k + 2]), 0.f);
+                }
+                const uint32_t meta[4] = {uint32_t(accel->inst_id_base[i]), uint32_t(accel->blas_offsets[accel->inst_blas[i]]), 0u, 0u};
+                std::memcpy(&r[6], meta, sizeof(meta));
+            }
+            s->inst.upload(it.data(), it.size());
+        }
 
         std::vector<int32_t> pml(size_t(D->num_prims) * 2);
         for (int32_t p = 0; p < D->num_prims; p++) {
@@ -1175,6 +1234,8 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         ds.cdf = s->cdf.as<const float>();
         ds.env = s->env.as<const float>();
         ds.has_camera = D->has_camera;
+        ds.inst = two_level ? s->inst.as<const float4>() : nullptr;
+        ds.num_inst = two_level ? accel->num_instances : 0;
         if (D->has_camera) {
             const HostCam c = make_camera(D->camera);
             ds.cam_p = mk(c.p[0], c.p[1], c.p[2]);
@@ -1198,7 +1259,7 @@ int lmgpu_scene_device_bytes(const lmgpu_scene* s, int64_t* out) {
     return guarded([&] {
         if (!s || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         const size_t b = s->shade.bytes + s->prim_ml.bytes + s->mats.bytes + s->lights.bytes + s->ltri.bytes + s->cdf.bytes +
-                         s->env.bytes + s->counters.bytes;
+                         s->env.bytes + s->inst.bytes + s->counters.bytes;
         *out = int64_t(b);
     });
 }
@@ -1261,9 +1322,10 @@ int lmgpu_render_raycast(lmgpu_scene* s, lmgpu_film* f, const lmgpu_raycast_para
         int* err = s->counters.as<int>() + 3;
         LMGPU_CUDA(cudaMemsetAsync(err, 0, 4, st));
         const int64_t n = int64_t(f->w) * f->h;
-        int g = grid_for(k_raycast, kBlock, smem);
+        auto rk = s->dev.num_inst > 0 ? k_raycast<true> : k_raycast<false>;
+        int g = grid_for(rk, kBlock, smem);
         g = int(std::min<int64_t>(g, (n + kBlock - 1) / kBlock));
-        k_raycast<<<g, kBlock, smem, st>>>(s->dev, f->w, f->h, *prm, f->sum.as<float>(), err);
+        rk<<<g, kBlock, smem, st>>>(s->dev, f->w, f->h, *prm, f->sum.as<float>(), err);
         LMGPU_CUDA(cudaGetLastError());
         k_scale<<<256, 256, 0, st>>>(f->sum.as<float>(), f->out.as<float>(), n * 3, 1.0f);
         int herr = 0;
@@ -1319,8 +1381,11 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
 
         const bool inst = prm->instrument != 0;
-        auto ext_k = inst ? k_pt_extend<true> : k_pt_extend<false>;
-        auto sh_k = inst ? k_pt_shadow<true> : k_pt_shadow<false>;
+        const bool two = s->dev.num_inst > 0;
+        auto ext_k = inst ? (two ? k_pt_extend<true, false, true> : k_pt_extend<true, false, false>)
+                          : (two ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>);
+        auto sh_k = inst ? (two ? k_pt_shadow<true, false, true> : k_pt_shadow<true, false, false>)
+                         : (two ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>);
         const int g_gen = grid_for(k_pt_generate, kBlock, 0);
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
@@ -1547,8 +1612,11 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
         const Bvh8 bvh = s->dev.bvh;
         const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
         const int g_gen = grid_for(k_pt_generate, kBlock, 0);
-        const int g_ext = grid_for(k_pt_extend<false>, kBlock, tsmem);
-        const int g_sh = grid_for(k_pt_shadow<false>, kBlock, tsmem);
+        const bool two = s->dev.num_inst > 0;
+        auto ext_k = two ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>;
+        auto sh_k = two ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>;
+        const int g_ext = grid_for(ext_k, kBlock, tsmem);
+        const int g_sh = grid_for(sh_k, kBlock, tsmem);
         auto shade_k = pick_shade(k_pt_shade<2>, k_pt_shade<3>, k_pt_shade<4>, tuning().shade_minblocks);
         const int g_shade = grid_for(shade_k, kBlock, 0);
 
@@ -1562,19 +1630,19 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
             k_pt_generate<<<std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock), kBlock, 0, st>>>(s->dev, P, start, n, q[0],
                                                                                                cnt + 0, sq, cnt + 2);
             if (P.image) {
-                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr,
-                                                                f_sh);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr, f_sh,
+                                                  nullptr);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
             }
             for (int it = 1; it < P.max_verts; it++) {
-                k_pt_extend<false><<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, hits, rays, cnt + 3, sums,
-                                                                 63, nullptr, f_ext);
+                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, hits, rays, cnt + 3, sums, 63,
+                                                    nullptr, f_ext, nullptr, nullptr);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
                 shade_k<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
                                                       cnt + 2, d_film);
-                k_pt_shadow<false><<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63,
-                                                                nullptr, f_sh);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr, f_sh,
+                                                  nullptr);
                 LMGPU_CUDA(cudaGetLastError());
                 cur = 1 - cur;
             }
@@ -1615,6 +1683,7 @@ struct lmgpu_batch {
     int32_t graph_depth = 0;
     int graph_refill = -1, graph_shade = -1;  // tuning the graph was captured with
     int refill = 0, shade_minblocks = 3;
+    bool two_level = false, graph_two_level = false;  // some job's scene is instanced
     int cur = 0;
     double elapsed_ms = 0;
     ~lmgpu_batch() {
@@ -1668,8 +1737,10 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
     Bvh8 bmax{};
     bmax.depth = b->max_depth;
-    const int g_ext = grid_for(k_pt_extend<false, true>, kBlock, tsmem);
-    const int g_sh = grid_for(k_pt_shadow<false, true>, kBlock, tsmem);
+    auto ext_k = b->two_level ? k_pt_extend<false, true, true> : k_pt_extend<false, true, false>;
+    auto sh_k = b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>;
+    const int g_ext = grid_for(ext_k, kBlock, tsmem);
+    const int g_sh = grid_for(sh_k, kBlock, tsmem);
     auto shade_k = pick_shade(k_wf_shade<2>, k_wf_shade<3>, k_wf_shade<4>, b->shade_minblocks);
     const int g_shade = grid_for(shade_k, kBlock, 0);
     const int g_gen = grid_for(k_wf_generate, kBlock, 0);
@@ -1685,12 +1756,12 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
     const Fetch f_ext{fetch, fetch + 1, b->refill}, f_sh{fetch + 1, fetch, b->refill};
     int cur = 0;
     for (int it = 0; it < kChunkIters; it++) {
-        k_pt_extend<false, true><<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
+        ext_k<<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
                                                                ctl_sums(b), 63, nullptr, f_ext, jobs, q[cur].job);
         LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
         shade_k<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
                                                b->pass_done.as<unsigned int>());
-        k_pt_shadow<false, true><<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
+        sh_k<<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
                                                               ctl_sums(b), 63, nullptr, f_sh, jobs);
         LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
         k_wf_plan<<<1, 1, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap);
@@ -1704,7 +1775,7 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     b->refill = tuning().trace_refill;
     b->shade_minblocks = tuning().shade_minblocks;
     if (b->exec && !realloc && b->graph_depth == b->max_depth && b->graph_refill == b->refill &&
-        b->graph_shade == b->shade_minblocks)
+        b->graph_shade == b->shade_minblocks && b->graph_two_level == b->two_level)
         return;
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
@@ -1712,8 +1783,8 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     LMGPU_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     // warm-up query of grid sizes outside the capture (occupancy calls are not capturable work)
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
-    (void)grid_for(k_pt_extend<false, true>, kBlock, tsmem);
-    (void)grid_for(k_pt_shadow<false, true>, kBlock, tsmem);
+    (void)grid_for(b->two_level ? k_pt_extend<false, true, true> : k_pt_extend<false, true, false>, kBlock, tsmem);
+    (void)grid_for(b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>, kBlock, tsmem);
     (void)grid_for(pick_shade(k_wf_shade<2>, k_wf_shade<3>, k_wf_shade<4>, b->shade_minblocks), kBlock, 0);
     (void)grid_for(k_wf_generate, kBlock, 0);
     LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
@@ -1731,6 +1802,7 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     LMGPU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
     b->graph_depth = b->max_depth;
     b->graph_refill = b->refill;
+    b->graph_two_level = b->two_level;
     b->graph_shade = b->shade_minblocks;
     (void)st;
 }
@@ -1800,6 +1872,7 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         b->passes += uint32_t(prm->spp);
         b->host_pass.resize(b->passes, 0);
         b->max_depth = std::max(b->max_depth, s->dev.bvh.depth);
+        b->two_level = b->two_level || s->dev.num_inst > 0;
         b->table_dirty = true;
         if (job_id) *job_id = int32_t(b->host_jobs.size() - 1);
     });
@@ -1922,6 +1995,7 @@ int lmgpu_batch_reset(lmgpu_batch* b) {
         b->total = 0;
         b->passes = 0;
         b->max_depth = 1;
+        b->two_level = false;
         b->elapsed_ms = 0;
         b->table_dirty = false;
         LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));

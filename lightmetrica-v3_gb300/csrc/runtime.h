@@ -96,11 +96,19 @@ Tuning& tuning();
 
 struct lmgpu_accel {
     int device = 0;
-    int64_t num_tris = 0;
-    int64_t num_nodes = 0;
-    int32_t depth = 0;
+    int64_t num_tris = 0;    // triangles a ray can hit (instanced: counted once per instance)
+    int64_t num_nodes = 0;   // node records (instanced: top-level + instance pseudo-nodes + every BLAS)
+    int32_t depth = 0;       // traversal stack bound (instanced: top-level depth + deepest BLAS)
     double build_seconds = 0;
     double sah_cost = 0;
     lmgpu::DevBuf nodes, tris;
     lmgpu::DevBuf scratch_rays, scratch_hits, err;
+    // two-level builds only
+    lmgpu::DevBuf inst;                      // per instance: inverse transform rows (3 float4), {root, id_base}
+    int32_t num_instances = 0;
+    uint32_t max_visits = 0;                 // node visits one ray can make (0: num_nodes)
+    std::vector<int32_t> inst_blas;          // per instance: its BLAS
+    std::vector<double> inst_xform;          // per instance: world-from-local, 12 doubles (row-major 3x4)
+    std::vector<int64_t> inst_id_base;       // per instance: first hit index
+    std::vector<int64_t> blas_offsets;       // BLAS b owns triangles [blas_offsets[b], blas_offsets[b+1])
 };

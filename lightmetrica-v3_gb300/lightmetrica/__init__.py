@@ -474,16 +474,21 @@ class LightEnv(_Light):
         self.scale = float(prop.get("scale", 1.0))
 
 
-@_reg("accel::gpu", "accel::sahbvh", "accel::nanort", "accel::embree", "accel::embreeinstanced")
+@_reg("accel::sahbvh", "accel::nanort", "accel::embree")
 class AccelGpu(Component):
     """The accel slot (include/lm/accel.h): an 8-wide quantized BVH built on the host and traced on
-    the GPU. Registered under every key the reference's accels use."""
+    the GPU. Registered under every key the reference's accels use. Like accel::sahbvh, nanort
+    and embree it flattens instance groups into one tree; prop `instancing=True` (the default of
+    accel::embreeinstanced and accel::gpu) builds the two-level form instead."""
+
+    default_instancing = False
 
     def construct(self, prop):
         h = C.c_void_p()
         N.check(N.lib().lmgpu_accel_create(C.byref(h)))
         self._h = h
         self.num_tris = 0
+        self.instancing = bool(prop.get("instancing", self.default_instancing))
 
     def _release(self):
         if getattr(self, "_h", None):
@@ -501,15 +506,33 @@ class AccelGpu(Component):
         N.check(N.lib().lmgpu_accel_build(self._h, N.fptr(tri_p), tri_p.shape[0]))
         self.num_tris = tri_p.shape[0]
 
+    def build_instanced(self, tri_p: np.ndarray, blas_offsets, instances) -> None:
+        """Two-level build: tri_p holds every BLAS's triangles back to back (each in its own frame),
+        blas_offsets the BLAS boundaries (len = number of BLAS + 1), instances a list of
+        (blas index, 4x4 world-from-local matrix)."""
+        tri_p = np.ascontiguousarray(tri_p, dtype=np.float32).reshape(-1, 9)
+        offs = np.ascontiguousarray(blas_offsets, dtype=np.int64)
+        arr = (N.Instance * len(instances))()
+        for k, (b, m) in enumerate(instances):
+            arr[k].blas = int(b)
+            arr[k].transform[:] = [float(x) for x in np.asarray(m, np.float64)[:3, :4].reshape(-1)]
+        N.check(N.lib().lmgpu_accel_build_instanced(self._h, N.fptr(tri_p), offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                     len(offs) - 1, arr, len(instances)))
+        self.num_tris = self.stats()["num_tris"]
+
     def build(self, scene: "SceneDefault") -> None:
-        """Accel::build(const Scene&): flattens the scene and builds over its triangles."""
-        flat = scene._flatten()
-        self.build_triangles(flat["positions"])
+        """Accel::build(const Scene&): flattens the scene (two-level when `instancing` and the
+        scene has instance groups) and builds over its triangles."""
+        if self.instancing and scene._has_instances():
+            g = scene._flatten_instanced()
+            self.build_instanced(g["positions"], g["blas_offsets"], g["instances"])
+        else:
+            self.build_triangles(scene._flatten()["positions"])
 
     def stats(self) -> dict:
         s = N.AccelStats()
         N.check(N.lib().lmgpu_accel_get_stats(self._h, C.byref(s)))
-        return {k: getattr(s, k) for k, _ in N.AccelStats._fields_ if k != "reserved"}
+        return {k: getattr(s, k) for k, _ in N.AccelStats._fields_}
 
     def intersect_batch(self, rays: np.ndarray) -> np.ndarray:
         """Batched Accel::intersect. rays: (n, 8) float32 (o, tmin, d, tmax). Returns a structured
@@ -527,6 +550,11 @@ class AccelGpu(Component):
         if h["prim"] < 0:
             return None
         return float(h["t"]), (float(h["u"]), float(h["v"])), int(h["prim"])
+
+
+@_reg("accel::embreeinstanced", "accel::gpu")
+class AccelGpuInstanced(AccelGpu):
+    default_instancing = True
 
 
 # ---------------------------------------------------------------------------------------------
@@ -669,6 +697,114 @@ class SceneDefault(Component):
         self._accel = _resolve(loc)
 
     # -- flatten + build (scene.cpp:274-317, accel_sahbvh.cpp:132-151) ------------------------
+    @staticmethod
+    def _prim_geometry(mesh, m: np.ndarray):
+        """One primitive's triangles under transform m (fp32, glm order): positions (k, 9),
+        shading normals (k, 9) and normalized geometric normals (k, 3)."""
+        tp = mesh.tri_positions()
+        tn = mesh.tri_normals()
+        ident = _is_identity(m)
+        if ident:
+            wp = tp.astype(np.float32)
+            wn = tn.astype(np.float32)
+            nm = np.eye(3, dtype=np.float32)
+        else:
+            wp = _f32_xform(m, tp)
+            nm = np.linalg.inv(m.astype(np.float64)).T[:3, :3].astype(np.float32)
+            wn = (tn @ nm.T).astype(np.float32)
+        lp = tp.astype(np.float32)
+        g = np.cross(lp[:, 1] - lp[:, 0], lp[:, 2] - lp[:, 0]).astype(np.float32)
+        g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
+        if not ident:
+            g = (g @ nm.T).astype(np.float32)
+            g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
+        return wp.reshape(-1, 9), wn.reshape(-1, 9), g.reshape(-1, 3)
+
+    def _has_instances(self) -> bool:
+        return any(n["type"] == "group" and n["instanced"] for n in self.nodes)
+
+    def _flatten_instanced(self) -> dict:
+        """Two-level flattening as accel::embreeinstanced does it (accel_embree_instanced.cpp:
+        84-181): primitives outside instance groups go, in world space, to BLAS 0 (an identity
+        instance); each instance group reached from the root is flattened once, in its own frame
+        and with nested instance groups treated as plain groups, into its own BLAS, and every
+        path to it adds an instance with the global transform at the group. Hit indices count the
+        instances' triangles in instance order."""
+        prim_mat, prim_light, prim_node = [], [], []
+        mats: list = []
+        light_index_of_node: dict[int, int] = {}
+        nl = [0]
+
+        def collect_lights(i, n, m):
+            if n["type"] == "primitive" and n["light"] is not None:
+                light_index_of_node[i] = nl[0]
+                nl[0] += 1
+        self.traverse_primitive_nodes(collect_lights)
+        blas: list[dict] = [{"pos": [], "nrm": [], "gn": [], "prim": []}]
+        blas_of_group: dict[int, int] = {}
+        instances: list = []
+
+        def add_prim(b, i, n, m):
+            wp, wn, g = self._prim_geometry(n["mesh"], m)
+            mat = n["material"]
+            if mat not in mats:
+                mats.append(mat)
+            pi = len(prim_mat)
+            prim_mat.append(mats.index(mat))
+            prim_light.append(light_index_of_node.get(i, -1))
+            prim_node.append(i)
+            blas[b]["pos"].append(wp)
+            blas[b]["nrm"].append(wn)
+            blas[b]["gn"].append(g)
+            blas[b]["prim"].append(np.full(wp.shape[0], pi, dtype=np.int32))
+
+        def visit_local(i, m, b):  # inside an instance group: plain flattening into BLAS b
+            n = self.nodes[i]
+            if n["type"] == "primitive":
+                if n["mesh"] is not None:
+                    add_prim(b, i, n, m)
+                return
+            mm = _f32_matmul(m, n["transform"]) if n["transform"] is not None else m
+            for c in n["children"]:
+                visit_local(c, mm, b)
+
+        def visit_root(i, m):
+            n = self.nodes[i]
+            if n["type"] == "primitive":
+                if n["mesh"] is not None:
+                    add_prim(0, i, n, m)
+                return
+            if n["instanced"]:
+                if i not in blas_of_group:
+                    blas_of_group[i] = len(blas)
+                    blas.append({"pos": [], "nrm": [], "gn": [], "prim": []})
+                    visit_local(i, np.eye(4, dtype=np.float32), blas_of_group[i])
+                instances.append((blas_of_group[i], m.astype(np.float64)))
+                return
+            mm = _f32_matmul(m, n["transform"]) if n["transform"] is not None else m
+            for c in n["children"]:
+                visit_root(c, mm)
+        visit_root(0, np.eye(4, dtype=np.float32))
+        if blas[0]["pos"]:
+            instances.insert(0, (0, np.eye(4)))
+        # drop empty BLAS (the root one without primitives, or groups without meshes)
+        keep = [b for b in range(len(blas)) if blas[b]["pos"]]
+        remap = {b: k for k, b in enumerate(keep)}
+        instances = [(remap[b], m) for b, m in instances if b in remap]
+        pos = [np.concatenate(blas[b]["pos"]) for b in keep]
+        offs = np.zeros(len(keep) + 1, np.int64)
+        for k, p_ in enumerate(pos):
+            offs[k + 1] = offs[k] + p_.shape[0]
+
+        def cat(key, width, dt):
+            parts = [np.concatenate(blas[b][key]) for b in keep]
+            return np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros((0, width), dt), dtype=dt)
+        return {"positions": cat("pos", 9, np.float32), "normals": cat("nrm", 9, np.float32),
+                "geo_normals": cat("gn", 3, np.float32), "tri_prim": cat("prim", 1, np.int32).reshape(-1),
+                "blas_offsets": offs, "instances": instances,
+                "prim_material": np.asarray(prim_mat, np.int32), "prim_light": np.asarray(prim_light, np.int32),
+                "prim_node": np.asarray(prim_node, np.int32), "materials": mats}
+
     def _flatten(self) -> dict:
         pos, nrm, gns, tri_prim = [], [], [], []
         prim_mat, prim_light, prim_node = [], [], []
@@ -685,24 +821,7 @@ class SceneDefault(Component):
         def collect_geometry(i, n, m):
             if n["type"] != "primitive" or n["mesh"] is None:
                 return
-            mesh = n["mesh"]
-            tp = mesh.tri_positions()
-            tn = mesh.tri_normals()
-            ident = _is_identity(m)
-            if ident:
-                wp = tp.astype(np.float32)
-                wn = tn.astype(np.float32)
-                nm = np.eye(3, dtype=np.float32)
-            else:
-                wp = _f32_xform(m, tp)
-                nm = np.linalg.inv(m.astype(np.float64)).T[:3, :3].astype(np.float32)
-                wn = (tn @ nm.T).astype(np.float32)
-            lp = tp.astype(np.float32)
-            g = np.cross(lp[:, 1] - lp[:, 0], lp[:, 2] - lp[:, 0]).astype(np.float32)
-            g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
-            if not ident:
-                g = (g @ nm.T).astype(np.float32)
-                g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
+            wp, wn, g = self._prim_geometry(n["mesh"], m)
             mat = n["material"]
             if mat not in mats:
                 mats.append(mat)
@@ -710,10 +829,10 @@ class SceneDefault(Component):
             prim_mat.append(mats.index(mat))
             prim_light.append(light_index_of_node.get(i, -1))
             prim_node.append(i)
-            pos.append(wp.reshape(-1, 9))
-            nrm.append(wn.reshape(-1, 9))
-            gns.append(g.reshape(-1, 3))
-            tri_prim.append(np.full(tp.shape[0], pi, dtype=np.int32))
+            pos.append(wp)
+            nrm.append(wn)
+            gns.append(g)
+            tri_prim.append(np.full(wp.shape[0], pi, dtype=np.int32))
         self.traverse_primitive_nodes(collect_geometry)
 
         if pos:
@@ -792,7 +911,16 @@ class SceneDefault(Component):
         flat = self._flatten()
         if flat["positions"].shape[0] == 0:
             raise LmGpuError(2, "Missing primitives. Use lm::primitive() function to add primitives.")
-        self._accel.build_triangles(flat["positions"])
+        if getattr(self._accel, "instancing", False) and self._has_instances():
+            # shading data per BLAS in its own frame; lights stay as flattened in world space
+            g = self._flatten_instanced()
+            self._accel.build_instanced(g["positions"], g["blas_offsets"], g["instances"])
+            flat = dict(flat)
+            for k in ("positions", "normals", "geo_normals", "tri_prim", "prim_material", "prim_light", "prim_node",
+                      "materials", "blas_offsets", "instances"):
+                flat[k] = g[k]
+        else:
+            self._accel.build_triangles(flat["positions"])
         d = N.SceneDesc()
         keep = []
 

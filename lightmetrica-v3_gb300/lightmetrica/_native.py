@@ -19,8 +19,12 @@ class Hit(C.Structure):
     _fields_ = [("t", C.c_float), ("u", C.c_float), ("v", C.c_float), ("prim", C.c_int32)]
 
 
+class Instance(C.Structure):
+    _fields_ = [("blas", C.c_int32), ("reserved", C.c_int32), ("transform", C.c_float * 12)]
+
+
 class AccelStats(C.Structure):
-    _fields_ = [("num_tris", C.c_int64), ("num_nodes", C.c_int64), ("max_depth", C.c_int32), ("reserved", C.c_int32),
+    _fields_ = [("num_tris", C.c_int64), ("num_nodes", C.c_int64), ("max_depth", C.c_int32), ("num_instances", C.c_int32),
                 ("build_seconds", C.c_double), ("sah_cost", C.c_double), ("device_bytes", C.c_int64)]
 
 
@@ -80,6 +84,8 @@ SIGNATURES = [
     ("lmgpu_accel_create", C.c_int, [C.POINTER(C.c_void_p)]),
     ("lmgpu_accel_destroy", C.c_int, [C.c_void_p]),
     ("lmgpu_accel_build", C.c_int, [C.c_void_p, c_float_p, C.c_int64]),
+    ("lmgpu_accel_build_instanced", C.c_int, [C.c_void_p, c_float_p, C.POINTER(C.c_int64), C.c_int32,
+                                              C.POINTER(Instance), C.c_int32]),
     ("lmgpu_accel_intersect", C.c_int, [C.c_void_p, c_float_p, C.c_int64, C.POINTER(Hit)]),
     ("lmgpu_accel_intersect_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("lmgpu_accel_occluded_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),

@@ -396,3 +396,100 @@ def served_requests(n: int, rate: float, n_scenes: int, seed: int = 77, refine_f
                         "res": int(rng.choice(BATCH_RESOLUTIONS)), "spp": int(rng.integers(4, 65)),
                         "max_verts": int(rng.integers(6, 13)) + 1, "seed": int(rng.integers(0, 2**31)), "refine": None})
     return out
+
+
+# ---------------------------------------------------------------------------------------------
+# Instancing (the instanced stress workload)
+
+def displaced_uv_sphere(n_lat: int, n_lon: int, amplitude: float = 0.05, seed: int = 3):
+    """Unit UV sphere of 2 * n_lon * (n_lat - 1) triangles displaced by 3-octave value noise.
+    Returns (positions (v, 3), vertex normals (v, 3), faces (f, 3))."""
+    th = np.linspace(0.0, math.pi, n_lat + 1)
+    ph = np.linspace(0.0, 2.0 * math.pi, n_lon, endpoint=False)
+    st, ct = np.sin(th), np.cos(th)
+    v = np.stack([np.outer(st, np.cos(ph)), np.repeat(ct[:, None], n_lon, 1), np.outer(st, np.sin(ph))], -1).reshape(-1, 3)
+    d = np.zeros(len(v))
+    for o in range(3):
+        d += (0.5 ** o) * value_noise(v * 3.0 * (2 ** o), seed + 17 * o)
+    p = v * (1.0 + d * amplitude / 1.75)[:, None]
+    faces = []
+    for i in range(n_lat):
+        a = i * n_lon + np.arange(n_lon)
+        b = i * n_lon + (np.arange(n_lon) + 1) % n_lon
+        c, e = a + n_lon, b + n_lon
+        if i > 0:
+            faces.append(np.stack([a, b, e], 1))
+        if i < n_lat - 1:
+            faces.append(np.stack([a, e, c], 1))
+    f = np.concatenate(faces).astype(np.int64)
+    fn = np.cross(p[f[:, 1]] - p[f[:, 0]], p[f[:, 2]] - p[f[:, 0]])
+    keep = np.linalg.norm(fn, axis=1) > 0  # the pole rows collapse to points
+    f, fn = f[keep], fn[keep]
+    vn = np.zeros_like(p)
+    for k in range(3):
+        np.add.at(vn, f[:, k], fn)
+    vn /= np.maximum(np.linalg.norm(vn, axis=1, keepdims=True), 1e-30)
+    return p.astype(np.float32), vn.astype(np.float32), f.astype(np.int32)
+
+
+def random_affine(rng, spread: float) -> np.ndarray:
+    """4x4 world-from-local: random rotation, anisotropic scale U(.4, 1.1), translation
+    U(-spread, spread) in x/z and U(.5, 2.5) in y."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    M = np.eye(4)
+    M[:3, :3] = R @ np.diag(rng.uniform(0.4, 1.1, 3))
+    M[:3, 3] = [rng.uniform(-spread, spread), rng.uniform(0.5, 2.5), rng.uniform(-spread, spread)]
+    return M
+
+
+def instanced_scene(n_instances: int = 64, n_lat: int = 500, n_lon: int = 500, n_lights: int = 16, w: int = 4096,
+                    h: int = 2160, env_w: int = 1024, env_h: int = 512, seed: int = 5, spread: float = 8.0,
+                    accel: str = "embreeinstanced", prefix: str = ""):
+    """`n_instances` instances of one displaced UV-sphere mesh (2 * n_lon * (n_lat - 1) triangles,
+    about 500k by default) under seed-drawn affine transforms, a ground plane, `n_lights` small
+    area lights and a procedural lat-long environment (log-normal radiance) of env_w x env_h texels.
+    Each instance is its own instance group (scene.create_instance_group_node); they all share
+    the mesh's group. Returns (scene, film, info)."""
+    rng = np.random.default_rng(seed)
+    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
+    camera = lm.load_camera(prefix + "camera", "pinhole", position=[0.0, 6.0, 22.0], center=[0.0, 1.0, 0.0],
+                            up=[0, 1, 0], vfov=40, aspect=w / h)
+    scene = lm.load_scene(prefix + "scene", "default", accel=lm.load_accel(prefix + "accel", accel))
+    scene.add_primitive(camera=camera)
+    gp, gn, gf = ground_grid(8, spread * 1.6)
+    ground = lm.load_mesh(prefix + "ground", "raw", ps=gp, ns=gn, ts=np.zeros((1, 2), np.float32),
+                          fs={"p": gf.reshape(-1), "n": np.zeros(gf.size, np.int32), "t": np.zeros(gf.size, np.int32)})
+    scene.add_primitive(mesh=ground, material=lm.load_material(prefix + "ground_mat", "diffuse", Kd=[0.55, 0.55, 0.5]))
+    p, vn, f = displaced_uv_sphere(n_lat, n_lon, seed=seed)
+    mesh = lm.load_mesh(prefix + "inst_mesh", "raw", ps=p, ns=vn, ts=np.zeros((1, 2), np.float32),
+                        fs={"p": f.reshape(-1), "n": f.reshape(-1), "t": np.zeros(f.size, np.int32)})
+    mats = [lm.load_material(prefix + "inst_diffuse", "diffuse", Kd=[0.7, 0.45, 0.3]),
+            lm.load_material(prefix + "inst_glossy", "glossy", Ks=[0.8, 0.8, 0.85], ax=0.15, ay=0.15),
+            lm.load_material(prefix + "inst_glass", "glass", Ni=1.5)]
+    # one shared group per material, instanced n_instances times in all
+    groups = []
+    for k, mat in enumerate(mats):
+        g = scene.create_instance_group_node()
+        scene.add_child(g, scene.create_primitive_node(mesh=mesh, material=mat))
+        groups.append(g)
+    for i in range(n_instances):
+        t = scene.create_group_node(random_affine(rng, spread))
+        scene.add_child(t, groups[int(rng.choice(3, p=[0.5, 0.3, 0.2]))])
+        scene.add_child(scene.root_node(), t)
+    black = lm.load_material(prefix + "light_mat", "diffuse", Kd=[0, 0, 0])
+    for k in range(n_lights):
+        cx, cz = rng.uniform(-spread, spread, 2)
+        y, s = rng.uniform(5.0, 8.0), 0.35
+        lmesh = load_mesh(prefix + f"light_mesh{k}", *quad((cx - s, y, cz - s), (cx + s, y, cz - s), (cx + s, y, cz + s),
+                                                          (cx - s, y, cz + s), (0, -1, 0)))
+        light = lm.load_light(prefix + f"light{k}", "area", Ke=list(rng.uniform(10.0, 30.0, 3)), mesh=lmesh)
+        scene.add_primitive(mesh=lmesh, material=black, light=light)
+    lm.load_texture(prefix + "env_tex", "bitmap", data=env_texture(env_w, env_h, seed=seed))
+    scene.add_primitive(light=lm.load_light(prefix + "env", "env", envmap="$.assets." + prefix + "env_tex", rot=30.0))
+    tris = n_instances * f.shape[0] + gf.shape[0] + 2 * n_lights
+    return scene, film, {"instances": n_instances, "mesh_triangles": int(f.shape[0]), "triangles": int(tris)}
