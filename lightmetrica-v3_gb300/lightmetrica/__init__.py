@@ -805,7 +805,9 @@ class SceneDefault(Component):
                 "prim_material": np.asarray(prim_mat, np.int32), "prim_light": np.asarray(prim_light, np.int32),
                 "prim_node": np.asarray(prim_node, np.int32), "materials": mats}
 
-    def _flatten(self) -> dict:
+    def _flatten(self, geometry: bool = True) -> dict:
+        """Flattened scene: world-space triangles with shading data (unless geometry=False, which
+        gives the light tables alone), primitive and material tables, lights in traversal order."""
         pos, nrm, gns, tri_prim = [], [], [], []
         prim_mat, prim_light, prim_node = [], [], []
         mats: list[_Material] = []
@@ -833,7 +835,8 @@ class SceneDefault(Component):
             nrm.append(wn)
             gns.append(g)
             tri_prim.append(np.full(wp.shape[0], pi, dtype=np.int32))
-        self.traverse_primitive_nodes(collect_geometry)
+        if geometry:
+            self.traverse_primitive_nodes(collect_geometry)
 
         if pos:
             positions = np.ascontiguousarray(np.concatenate(pos), dtype=np.float32)
@@ -908,17 +911,18 @@ class SceneDefault(Component):
         if self._accel is None:
             raise LmGpuError(2, "Missing acceleration structure.")
         self._release()
-        flat = self._flatten()
-        if flat["positions"].shape[0] == 0:
-            raise LmGpuError(2, "Missing primitives. Use lm::primitive() function to add primitives.")
-        if getattr(self._accel, "instancing", False) and self._has_instances():
+        instanced = getattr(self._accel, "instancing", False) and self._has_instances()
+        flat = self._flatten(geometry=not instanced)
+        if instanced:
             # shading data per BLAS in its own frame; lights stay as flattened in world space
             g = self._flatten_instanced()
-            self._accel.build_instanced(g["positions"], g["blas_offsets"], g["instances"])
-            flat = dict(flat)
             for k in ("positions", "normals", "geo_normals", "tri_prim", "prim_material", "prim_light", "prim_node",
                       "materials", "blas_offsets", "instances"):
                 flat[k] = g[k]
+        if flat["positions"].shape[0] == 0:
+            raise LmGpuError(2, "Missing primitives. Use lm::primitive() function to add primitives.")
+        if instanced:
+            self._accel.build_instanced(flat["positions"], flat["blas_offsets"], flat["instances"])
         else:
             self._accel.build_triangles(flat["positions"])
         d = N.SceneDesc()
