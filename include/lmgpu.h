@@ -63,6 +63,9 @@ int lmgpu_version(void);
  *                   one ray per thread without refills.
  *   "shade_minblocks" shade kernels: 256-thread blocks per SM their register budget must allow
  *                   (2: up to 128 registers; 3: up to 80; 4: up to 64, the default).
+ *   "batch_first_pass" shared wavefront: start the sample-0 paths of every job before any other
+ *                   path (1, the default: a newly admitted job's first image does not wait behind
+ *                   older jobs' later samples) or start paths in submission order (0).
  * Tuning changes speed only, never results. Process-wide; set it between renders. */
 int lmgpu_tune_set(const char* key, int64_t value);
 int lmgpu_tune_get(const char* key, int64_t* value);

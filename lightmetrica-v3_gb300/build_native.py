@@ -22,7 +22,9 @@ LIB = os.path.join(LIBDIR, "liblmgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
-    "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+    # --fmad=false: every product and sum rounds as written (explicit fmaf() stays fused), so the
+    # same device function gives the same bits in every kernel that inlines it
+    "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "--fmad=false",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fno-fast-math",
     "-I", INCLUDE,
 ]

@@ -173,6 +173,9 @@ int lmgpu_tune_set(const char* key, int64_t value) {
         if (k == "trace_refill") {
             if (value < 0 || value > 32) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "trace_refill must be in [0, 32]");
             tuning().trace_refill = int(value);
+        } else if (k == "batch_first_pass") {
+            if (value != 0 && value != 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "batch_first_pass must be 0 or 1");
+            tuning().batch_first_pass = int(value);
         } else if (k == "shade_minblocks") {
             if (value < 2 || value > 4) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "shade_minblocks must be 2, 3 or 4");
             tuning().shade_minblocks = int(value);
@@ -188,6 +191,7 @@ int lmgpu_tune_get(const char* key, int64_t* value) {
         const std::string k(key);
         if (k == "trace_refill") *value = tuning().trace_refill;
         else if (k == "shade_minblocks") *value = tuning().shade_minblocks;
+        else if (k == "batch_first_pass") *value = tuning().batch_first_pass;
         else throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
     });
 }

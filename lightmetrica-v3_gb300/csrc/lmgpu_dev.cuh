@@ -22,8 +22,16 @@ __device__ inline f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z *
 __device__ inline f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
 __device__ inline f3 operator*(float s, f3 a) { return {a.x * s, a.y * s, a.z * s}; }
 __device__ inline f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
-__device__ inline float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ inline f3 cross(f3 a, f3 b) { return {a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y}; }
+// Shading math fuses with explicit fmaf (the library is compiled with --fmad=false, so nothing is
+// fused implicitly and every kernel inlining these gets the same bits).
+__device__ inline float dot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+__device__ inline f3 cross(f3 a, f3 b) {
+    return {fmaf(a.y, b.z, -(b.y * a.z)), fmaf(a.z, b.x, -(b.z * a.x)), fmaf(a.x, b.y, -(b.x * a.y))};
+}
+// a*s + b*t + c*r per component (barycentric interpolation, basis expansion)
+__device__ inline f3 mix3(f3 a, float s, f3 b, float t, f3 c, float r) {
+    return {fmaf(c.x, r, fmaf(b.x, t, a.x * s)), fmaf(c.y, r, fmaf(b.y, t, a.y * s)), fmaf(c.z, r, fmaf(b.z, t, a.z * s))};
+}
 __device__ inline f3 normalize(f3 v) { return v * (1.0f / sqrtf(dot(v, v))); }
 __device__ inline float length(f3 v) { return sqrtf(dot(v, v)); }
 __device__ inline float cmax(f3 v) { return fmaxf(fmaxf(v.x, v.y), v.z); }

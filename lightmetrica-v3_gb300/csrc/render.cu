@@ -157,8 +157,8 @@ __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float 
         const f3 gl = mk(s4.z, s4.w, s5.x);
         prim = int32_t(__float_as_uint(s5.y));
         const float b0 = 1.f - u - v;
-        const f3 pl = p1 * b0 + p2 * u + p3 * v;
-        const f3 nl = normalize(n1 * b0 + n2 * u + n3 * v);
+        const f3 pl = mix3(p1, b0, p2, u, p3, v);
+        const f3 nl = normalize(mix3(n1, b0, n2, u, n3, v));
         const f3 p = mk(m0.x * pl.x + m0.y * pl.y + m0.z * pl.z + m0.w, m1.x * pl.x + m1.y * pl.y + m1.z * pl.z + m1.w,
                         m2.x * pl.x + m2.y * pl.y + m2.z * pl.z + m2.w);
         const f3 n = normalize(mk(dot(mk(q0.x, q0.y, q0.z), nl), dot(mk(q1.x, q1.y, q1.z), nl), dot(mk(q2.x, q2.y, q2.z), nl)));
@@ -173,8 +173,8 @@ __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float 
     const f3 gn = mk(s4.z, s4.w, s5.x);
     prim = int32_t(__float_as_uint(s5.y));
     const float b0 = 1.f - u - v;  // mix_barycentric, math.h:572-575
-    const f3 p = p1 * b0 + p2 * u + p3 * v;
-    const f3 n = normalize(n1 * b0 + n2 * u + n3 * v);
+    const f3 p = mix3(p1, b0, p2, u, p3, v);
+    const f3 n = normalize(mix3(n1, b0, n2, u, n3, v));
     return on_surface(p, n, gn);
 }
 
@@ -298,7 +298,7 @@ __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, in
         sincosf(t, &st, &ct);
         const float x = r * ct, y = r * st;
         const float z = sqrtf(fmaxf(0.f, 1.f - x * x - y * y));
-        wo = u * x + v * y + n * z;
+        wo = mix3(u, x, v, y, n, z);
         w = mk(m.c[0], m.c[1], m.c[2]);
         return true;
     }
@@ -482,10 +482,9 @@ struct PtConst {
     int32_t image;     // 1: image primary-ray mode
     int32_t w, h;
 };
-// One job of a shared wavefront: its scene, renderer parameters and film. Its paths occupy
-// [path_begin, path_begin + npix * spp) of the wavefront's path space, enumerated sample-major
-// (all pixels of sample 0 first), so pass s of the job is complete when pass_done[pass_off + s]
-// reaches npix.
+// One job of a shared wavefront: its scene, renderer parameters and film. Its npix * spp paths
+// are started in sample-major order (all pixels of sample 0 first), so pass s of the job is
+// complete when pass_done[pass_off + s] reaches npix. path_begin: paths submitted before it.
 struct JobDev {
     DevScene S;
     PtConst P;
@@ -625,26 +624,36 @@ __global__ void __launch_bounds__(kBlock) k_pt_generate(const __grid_constant__ 
     }
 }
 
-// Job table: a range of the shared path space, as chosen by k_wf_plan; each index maps to
-// (job, sample, pixel) with the job's sample-major enumeration.
-__global__ void __launch_bounds__(kBlock) k_wf_generate(const JobDev* __restrict__ jobs, const int64_t* __restrict__ job_begin,
+// Shared wavefront: the planner's allocation list. Entry e gives queue slots [slot_e, slot_{e+1})
+// to job `job`, starting at its path `local` (sample-major: local = sample * npix + pixel).
+struct AllocEntry {
+    int64_t local, slot;
+    int32_t job, pad;
+};
+// Planner's view of a job that still has paths to start.
+struct ActiveJob {
+    int64_t npix, total;
+    int32_t job, pad;
+};
+
+// New paths for the slots the planner handed out this iteration (ctl[3] of them, in ctl[22]
+// allocation entries; both read here, not baked into a captured launch).
+__global__ void __launch_bounds__(kBlock) k_wf_generate(const JobDev* __restrict__ jobs, const AllocEntry* __restrict__ alloc,
                                                         const int64_t* __restrict__ ctl, ExtQ q, int* qcount, ShadowQ sq,
                                                         int* scount) {
-    // ctl[2], ctl[3]: the range chosen by k_wf_plan; ctl[5]: number of jobs (read here, not baked
-    // into a captured launch, so jobs submitted later are found)
-    const int64_t start = ctl[2], count = ctl[3];
-    const int njobs = int(ctl[5]);
+    const int64_t count = ctl[3];
+    const int na = int(ctl[22]);
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
-        const int64_t gidx = start + i;
-        int lo = 0, hi = njobs;  // last job with job_begin <= gidx
+        int lo = 0, hi = na;  // last entry with slot <= i
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if (job_begin[mid] <= gidx) lo = mid; else hi = mid;
+            if (alloc[mid].slot <= i) lo = mid; else hi = mid;
         }
-        const JobDev& J = jobs[lo];
-        const int64_t local = gidx - J.path_begin;
+        const AllocEntry e = alloc[lo];
+        const JobDev& J = jobs[e.job];
+        const int64_t local = e.local + (i - e.slot);
         const int64_t sample = local / J.npix, pix = local - sample * J.npix;
-        generate_path<true>(J.S, J.P, uint64_t(pix * J.P.spp + sample), pix, q, qcount, sq, scount, uint32_t(lo));
+        generate_path<true>(J.S, J.P, uint64_t(pix * J.P.spp + sample), pix, q, qcount, sq, scount, uint32_t(e.job));
     }
 }
 
@@ -908,17 +917,85 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* _
     }
 }
 
-// Device-side planner (one thread): how many new paths fit into the next queue, taken from the
-// path space in order. ctl: [0] next path, [1] total paths, [2..3] chosen range, [4] paths still
-// in flight or waiting (0 = done).
-__global__ void k_wf_plan(int64_t* ctl, const int* qcount, int64_t cap) {
-    const int64_t next = ctl[0], total = ctl[1];
+// Device-side planner, one warp. Tops the next queue up to `cap` paths: with `first_pass`, first
+// the remaining sample-0 paths of every job that has not started them all (in submission order),
+// so a newly admitted job's first image does not wait behind older jobs' later samples; then
+// paths in submission order. Only the order in which paths start changes, never a path's random
+// stream. Keeps per job the next path to start (job_next) and the list of jobs with paths left
+// (active, compacted in place). ctl: [0] paths started, [1] paths submitted, [3] slots handed
+// out, [4] paths in flight or waiting (0 = done), [5] jobs submitted, [20] jobs seen, [21]
+// active jobs, [22] allocation entries.
+__global__ void __launch_bounds__(32) k_wf_plan(int64_t* ctl, const int* qcount, int64_t cap, const JobDev* __restrict__ jobs,
+                                                int64_t* job_next, ActiveJob* active, AllocEntry* alloc, int first_pass) {
+    const int lane = int(threadIdx.x);
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t njobs = ctl[5], seen = ctl[20];
+    int64_t nact = ctl[21];
+    for (int64_t j = seen + lane; j < njobs; j += 32) {
+        const JobDev& J = jobs[j];
+        active[nact + (j - seen)] = ActiveJob{J.npix, J.npix * J.P.spp, int32_t(j), 0};
+    }
+    nact += njobs > seen ? njobs - seen : 0;
+    __syncwarp();
     const int64_t inq = *qcount;
-    const int64_t take = min(cap - inq, total - next);
-    ctl[2] = next;
-    ctl[3] = take > 0 ? take : 0;
-    ctl[0] = next + ctl[3];
-    ctl[4] = inq + (total - next);
+    int64_t left = cap > inq ? cap - inq : 0;
+    int64_t slot = 0, na = 0;
+    for (int phase = first_pass ? 0 : 1; phase < 2 && left > 0; phase++) {
+        for (int64_t base = 0; base < nact && left > 0; base += 32) {
+            const int64_t a = base + lane;
+            int64_t want = 0, nx = 0;
+            int32_t j = 0;
+            if (a < nact) {
+                const ActiveJob A = active[a];
+                j = A.job;
+                nx = job_next[j];
+                const int64_t end = phase == 0 ? min(A.npix, A.total) : A.total;
+                want = end > nx ? end - nx : 0;
+            }
+            int64_t inc = want;  // inclusive scan of the wants across the warp
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            const int64_t before = inc - want;
+            const int64_t take = min(want, left > before ? left - before : 0);
+            const unsigned has = __ballot_sync(0xffffffffu, take > 0);
+            if (take > 0) {
+                alloc[na + __popc(has & below)] = AllocEntry{nx, slot + before, j, 0};
+                job_next[j] = nx + take;
+            }
+            const int64_t chunk = __shfl_sync(0xffffffffu, inc, 31);
+            const int64_t used = min(chunk, left);
+            slot += used;
+            left -= used;
+            na += __popc(has);
+            __syncwarp();
+        }
+    }
+    // keep the jobs with paths still to start; entries move down only, and a chunk is read
+    // completely before any of it is written
+    int64_t k = 0;
+    for (int64_t base = 0; base < nact; base += 32) {
+        const int64_t a = base + lane;
+        bool keep = false;
+        ActiveJob A{};
+        if (a < nact) {
+            A = active[a];
+            keep = job_next[A.job] < A.total;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) active[k + __popc(m & below)] = A;
+        k += __popc(m);
+        __syncwarp();
+    }
+    if (lane == 0) {
+        ctl[20] = njobs;
+        ctl[21] = k;
+        ctl[22] = na;
+        ctl[3] = slot;
+        ctl[0] += slot;
+        ctl[4] = inq + (ctl[1] - ctl[0]);
+    }
 }
 
 __global__ void k_scale(const float* __restrict__ in, float* __restrict__ out, int64_t n, float s) {
@@ -1666,11 +1743,11 @@ struct lmgpu_batch {
     int64_t cap = 0;
     lmgpu::DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], q_job[2], hits, s_o, s_d, s_c, s_job;
     lmgpu::DevBuf ctl;        // int64: next, total, range[2], remaining, njobs; then int counters, then u64 rays
-    lmgpu::DevBuf jobs, job_begin, pass_done;
-    size_t jobs_cap = 0, begin_cap = 0, pass_cap = 0;
-    size_t jobs_done = 0, begin_done = 0;  // entries already on the device
+    lmgpu::DevBuf jobs, pass_done;
+    lmgpu::DevBuf job_next, active, alloc;  // planner state: per job, per job, two per job
+    size_t jobs_cap = 0, pass_cap = 0, aux_cap = 0;
+    size_t jobs_done = 0;                   // job-table entries already on the device
     std::vector<lmgpu::JobDev> host_jobs;
-    std::vector<int64_t> host_begin{0};
     std::vector<lmgpu_film*> films;
     std::vector<uint32_t> host_pass;      // mirror of pass_done after the last run
     int64_t total = 0;
@@ -1682,7 +1759,7 @@ struct lmgpu_batch {
     cudaGraphExec_t exec = nullptr;
     int32_t graph_depth = 0;
     int graph_refill = -1, graph_shade = -1;  // tuning the graph was captured with
-    int refill = 0, shade_minblocks = 3;
+    int refill = 0, shade_minblocks = 3, first_pass = 1, graph_first_pass = -1;
     bool two_level = false, graph_two_level = false;  // some job's scene is instanced
     int cur = 0;
     double elapsed_ms = 0;
@@ -1764,8 +1841,9 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
         sh_k<<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
                                                               ctl_sums(b), 63, nullptr, f_sh, jobs);
         LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
-        k_wf_plan<<<1, 1, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap);
-        k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->job_begin.as<int64_t>(), ctl64(b), q[1 - cur], cnt + (1 - cur), sq,
+        k_wf_plan<<<1, 32, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap, jobs, b->job_next.as<int64_t>(), b->active.as<ActiveJob>(),
+                                    b->alloc.as<AllocEntry>(), b->first_pass);
+        k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->alloc.as<AllocEntry>(), ctl64(b), q[1 - cur], cnt + (1 - cur), sq,
                                                 cnt + 2);
         cur = 1 - cur;
     }
@@ -1774,8 +1852,9 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
 void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     b->refill = tuning().trace_refill;
     b->shade_minblocks = tuning().shade_minblocks;
+    b->first_pass = tuning().batch_first_pass;
     if (b->exec && !realloc && b->graph_depth == b->max_depth && b->graph_refill == b->refill &&
-        b->graph_shade == b->shade_minblocks && b->graph_two_level == b->two_level)
+        b->graph_shade == b->shade_minblocks && b->graph_two_level == b->two_level && b->graph_first_pass == b->first_pass)
         return;
     if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
     if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
@@ -1803,6 +1882,7 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     b->graph_depth = b->max_depth;
     b->graph_refill = b->refill;
     b->graph_two_level = b->two_level;
+    b->graph_first_pass = b->first_pass;
     b->graph_shade = b->shade_minblocks;
     (void)st;
 }
@@ -1867,8 +1947,6 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         b->host_jobs.push_back(J);
         b->films.push_back(f);
         b->total += npix * prm->spp;
-        b->host_begin.back() = J.path_begin;
-        b->host_begin.push_back(b->total);
         b->passes += uint32_t(prm->spp);
         b->host_pass.resize(b->passes, 0);
         b->max_depth = std::max(b->max_depth, s->dev.bvh.depth);
@@ -1885,9 +1963,26 @@ int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* p
         bool realloc = false;
         if (b->table_dirty) {
             grow_upload(b->jobs, b->jobs_cap, b->jobs_done, b->host_jobs, st, realloc);
-            // the last entry of job_begin changes with every submission (it ends the path space)
-            b->begin_done = std::min(b->begin_done, b->host_begin.size() >= 2 ? b->host_begin.size() - 2 : 0);
-            grow_upload(b->job_begin, b->begin_cap, b->begin_done, b->host_begin, st, realloc);
+            // planner state follows the job table's capacity; job_next and active keep their
+            // device values, new job_next entries start at zero
+            if (b->aux_cap < b->jobs_cap) {
+                LMGPU_CUDA(cudaStreamSynchronize(st));
+                const size_t c = b->jobs_cap;
+                DevBuf nn, na, nal;
+                nn.alloc(c * sizeof(int64_t));
+                na.alloc(c * sizeof(ActiveJob));
+                nal.alloc(2 * c * sizeof(AllocEntry));
+                LMGPU_CUDA(cudaMemset(nn.p, 0, c * sizeof(int64_t)));
+                if (b->aux_cap) {
+                    LMGPU_CUDA(cudaMemcpy(nn.p, b->job_next.p, b->aux_cap * sizeof(int64_t), cudaMemcpyDeviceToDevice));
+                    LMGPU_CUDA(cudaMemcpy(na.p, b->active.p, b->aux_cap * sizeof(ActiveJob), cudaMemcpyDeviceToDevice));
+                }
+                std::swap(b->job_next.p, nn.p); std::swap(b->job_next.bytes, nn.bytes);
+                std::swap(b->active.p, na.p); std::swap(b->active.bytes, na.bytes);
+                std::swap(b->alloc.p, nal.p); std::swap(b->alloc.bytes, nal.bytes);
+                b->aux_cap = c;
+                realloc = true;
+            }
             // new pass counters start at zero; existing ones keep their device values
             if (b->passes > b->pass_cap) {
                 LMGPU_CUDA(cudaStreamSynchronize(st));
@@ -1989,9 +2084,8 @@ int lmgpu_batch_reset(lmgpu_batch* b) {
         LMGPU_CUDA(cudaDeviceSynchronize());
         b->host_jobs.clear();
         b->films.clear();
-        b->host_begin.assign(1, 0);
         b->host_pass.clear();
-        b->jobs_done = b->begin_done = 0;
+        b->jobs_done = 0;
         b->total = 0;
         b->passes = 0;
         b->max_depth = 1;
@@ -2000,6 +2094,7 @@ int lmgpu_batch_reset(lmgpu_batch* b) {
         b->table_dirty = false;
         LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
         if (b->pass_cap) LMGPU_CUDA(cudaMemset(b->pass_done.p, 0, b->pass_cap * 4));
+        if (b->aux_cap) LMGPU_CUDA(cudaMemset(b->job_next.p, 0, b->aux_cap * sizeof(int64_t)));
     });
 }
 

@@ -89,6 +89,9 @@ struct Tuning {
     int trace_refill = 24;
     // Shade kernels: resident blocks per SM their register budget allows (2, 3 or 4).
     int shade_minblocks = 4;
+    // Shared wavefront: start every job's sample-0 paths before other paths (1) or start paths
+    // strictly in submission order (0).
+    int batch_first_pass = 1;
 };
 Tuning& tuning();
 

@@ -187,8 +187,9 @@ class RenderServer:
     def _film_bytes(self, req: Request) -> int:
         return 0 if req.refine is not None else req.w * req.h * 3 * 4 * 2
 
-    def _evict_for(self, need: int) -> None:
-        idle = sorted((t, k) for k, t in self.scene_last_use.items() if self.scene_users.get(k, 0) == 0)
+    def _evict_for(self, need: int, keep=None) -> None:
+        """Evicts idle scenes (least recently used first, never `keep`) until `need` more bytes fit."""
+        idle = sorted((t, k) for k, t in self.scene_last_use.items() if self.scene_users.get(k, 0) == 0 and k != keep)
         for _, k in idle:
             if self.resident_bytes + need <= self.budget:
                 break
@@ -221,7 +222,7 @@ class RenderServer:
             self.scenes[req.scene_key] = (scene, nbytes)
             self.resident_bytes += nbytes
         else:
-            self._evict_for(need)
+            self._evict_for(need, keep=req.scene_key)
             if self.resident_bytes + need > self.budget:
                 return False
         scene, _ = self.scenes[req.scene_key]

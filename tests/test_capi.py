@@ -74,5 +74,8 @@ def test_tuning_keys(native_lib):
         assert b"unknown tuning key" in L.lmgpu_last_error()
         assert L.lmgpu_tune_get(b"no_such_key", C.byref(v)) == 1
         assert L.lmgpu_tune_set(None, 1) == 1
+        assert L.lmgpu_tune_get(b"batch_first_pass", C.byref(v)) == 0 and v.value in (0, 1)
+        assert L.lmgpu_tune_set(b"batch_first_pass", 2) == 1
+        assert L.lmgpu_tune_set(b"shade_minblocks", 5) == 1
     finally:
         assert L.lmgpu_tune_set(b"trace_refill", old) == 0

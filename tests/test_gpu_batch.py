@@ -133,3 +133,33 @@ def test_render_server_admission_and_latency(lm):
     before = srv.resident_bytes
     srv.release(1)
     assert srv.resident_bytes == before - film and reqs[1].film is None
+
+
+def test_first_pass_priority(lm, native_lib):
+    """With batch_first_pass on (the default), a small job submitted while a large one is in
+    flight shows its first complete sample pass before the large job finishes; every image is
+    still the standalone one."""
+    from lightmetrica import synthetic as syn
+    from lightmetrica.serving import BatchRenderer
+    big_s, big_f = syn.box_scene(w=64, h=64, prefix="fpbig_")
+    big_s.build()
+    small_s, small_f = syn.box_scene(seed=9, w=8, h=8, prefix="fpsmall_")
+    small_s.build()
+    a_big = _alone(lm, big_s, big_f, max_verts=8, spp=48, seed=4)
+    a_small = _alone(lm, small_s, small_f, max_verts=8, spp=4, seed=6)
+    b = BatchRenderer(queue_paths=4096)
+    jb = b.submit(big_s, big_f, max_verts=8, spp=48, seed=4)
+    b.run(max_chunks=1)
+    js = b.submit(small_s, small_f, max_verts=8, spp=4, seed=6)
+    chunks_to_first, chunks = None, 0
+    while b.run(max_chunks=1) > 0:
+        chunks += 1
+        if chunks_to_first is None and b.status(js)[0] >= 1:
+            chunks_to_first = chunks
+            assert not b.status(jb)[1]
+    assert chunks_to_first is not None and chunks_to_first <= 2
+    for j in (jb, js):
+        b.resolve(j)
+    np.testing.assert_allclose(big_f.buffer_f32(), a_big, **TOL)
+    np.testing.assert_allclose(small_f.buffer_f32(), a_small, **TOL)
+    b.close()

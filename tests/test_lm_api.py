@@ -124,3 +124,32 @@ def test_sphere_rays_unit_directions():
     r = syn.sphere_rays(1000, [0, 1, 0])
     assert r.shape == (1000, 8) and r.dtype == np.float32
     assert np.allclose(np.linalg.norm(r[:, 4:7], axis=1), 1, atol=1e-6)
+
+
+def test_render_server_never_evicts_the_scene_it_admits(monkeypatch):
+    """Admitting a request on a resident but idle scene may evict other idle scenes, never that one
+    (host logic only: the batch and footprint calls are stubbed)."""
+    from lightmetrica import serving
+
+    class FakeBatch:
+        def __init__(self, *a, **k):
+            self.n = 0
+
+        def submit(self, *a, **k):
+            self.n += 1
+            return self.n - 1
+
+    monkeypatch.setattr(serving, "BatchRenderer", FakeBatch)
+    monkeypatch.setattr(serving, "scene_footprint", lambda s: 100)
+    monkeypatch.setattr(serving, "_release_scene", lambda s: None)
+    import lightmetrica as lm
+    monkeypatch.setattr(lm, "load_film", lambda *a, **k: object())
+    srv = serving.RenderServer(lambda k: f"scene{k}", hbm_budget=2 * 100 + 2 * 96)  # two scenes + two 2x2 films
+    for rid, key in ((0, "a"), (1, "b")):
+        srv.submit(serving.Request(rid=rid, arrival=0.0, scene_key=key, w=2, h=2, spp=1, max_verts=2, seed=0))
+        assert srv._try_admit(srv.pending.pop())
+        srv.scene_users[key] = 0          # finished: both scenes idle, budget full
+    srv.scene_last_use = {"a": 1.0, "b": 0.5}
+    req = serving.Request(rid=2, arrival=0.0, scene_key="b", w=2, h=2, spp=1, max_verts=2, seed=0)
+    assert srv._try_admit(req)            # evicts "a" (older use time does not matter: "b" is needed)
+    assert "b" in srv.scenes and "a" not in srv.scenes and srv.evictions == 1
