@@ -289,11 +289,16 @@ def run_gpu(args) -> None:
         # shadow ray written 48 B
         bytes_total, launches = tot["ext"] * (88 + 88 + 96 + 48), tot["ext_launches"]
     achieved = bytes_total / (kern[dom] / 1e3) / 1e9
+    # DRAM traffic per launch of the dominant kernel: bytes per traced ray from an ncu capture of
+    # every launch of that kernel in one step (profiles/traffic_per_ray.json) times the rays one
+    # launch of this run traces on average
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
-    if os.path.exists(tf):
-        traffic = json.load(open(tf)).get(dom)
-
+    tf = os.path.join(ROOT, "profiles", "traffic_per_ray.json")
+    if os.path.exists(tf) and dom in ("extend", "shadow"):
+        per_ray = json.load(open(tf)).get(dom)
+        if per_ray:
+            n_rays, n_launch = (tot["ext"], tot["ext_launches"]) if dom == "extend" else (tot["sh"], tot["sh_launches"])
+            traffic = per_ray * n_rays / max(1, n_launch)
     cpu = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
@@ -316,6 +321,8 @@ def run_gpu(args) -> None:
                        "l2": "inputs larger than L2 (scene resident) and a 256 MB L2 flush between steps",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "rays_per_step": tot["rays"] / max(1, args.steps),
+            "extension_rays_per_step": tot["ext"] / max(1, args.steps),
+            "shadow_rays_per_step": tot["sh"] / max(1, args.steps),
             "kernel_ms_per_step": {k: v / max(1, args.steps) for k, v in kern.items()},
             "e2e": {"value": e2e_rays / e2e_s / 1e6 if e2e_s > 0 else None, "unit": "Mrays/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
