@@ -25,6 +25,10 @@ Two more legs (rank 0) report the batched and served forms (keys "batched" and "
 * instanced -- renderer::pt through the two-level accel on lightmetrica.synthetic.instanced_scene:
   64 instances of a 499k-triangle displaced mesh (32M triangles effective, 1.5M stored), a
   1024x512 procedural HDR environment and 16 area lights, 4096x2160, path length 16.
+* served_stress -- the heavy-tailed mix of the instanced configuration: 1 request in 10 renders
+  the instanced scene at 4096x2160 (1-4 spp), the rest batched-workload scenes, through a
+  RenderServer that builds scenes on admission under a 1.5 GB HBM budget, so memory admission,
+  eviction and rebuilds are exercised (bounded to 300 requests).
 * served -- a Poisson stream of requests over the same scenes (30 % are +16 spp refinements of
   earlier requests) at 80 % of the batched capacity just measured, through RenderServer under a
   150 GB HBM budget; reports p50/p99 time-to-first-image (first complete sample pass) and
@@ -340,6 +344,8 @@ def run_gpu(args) -> None:
             out["batched"], ctx = run_batched(lm, args)
             if args.served_requests > 0:
                 out["served"] = run_served(lm, args, ctx)
+            if args.stress_requests > 0:
+                out["served_stress"] = run_served_stress(lm, args, ctx)
         if args.instanced_spp > 0:
             out["instanced"] = run_instanced(lm, args)
         print(json.dumps(out))
@@ -408,7 +414,8 @@ def run_batched(lm, args) -> tuple[dict, dict]:
         "timing": "wall clock around all jobs (host overhead included); scene builds excluded",
         "scene_build_seconds": build_s,
     }
-    return out, {"jobs": jobs, "scenes": scenes, "queue": queue, "capacity": len(jobs) / batch_s}
+    return out, {"jobs": jobs, "scenes": scenes, "queue": queue, "capacity": len(jobs) / batch_s,
+                 "paths_per_s": paths / batch_s}
 
 
 def run_served(lm, args, ctx) -> dict:
@@ -445,6 +452,78 @@ def run_served(lm, args, ctx) -> dict:
             "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"],
             "done_p50_s": lat["done_p50"], "done_p99_s": lat["done_p99"], "evictions": lat["evictions"],
             "peak_resident_bytes": srv.peak_resident_bytes}
+
+
+def run_served_stress(lm, args, ctx) -> dict:
+    """Heavy-tailed served mix: 1 request in 10 renders the instanced scene at 4096x2160 (path
+    length 16, 1-4 spp), the rest batched-workload scenes (the first 32 of the mix), under a small
+    HBM budget, so admission waits for memory and idle scenes are evicted and rebuilt. Scenes are
+    built on admission and released on eviction by the server; films are released when done."""
+    import numpy as np
+    from lightmetrica import synthetic as syn
+    from lightmetrica.serving import RenderServer, Request
+    jobs = ctx["jobs"]
+    rng = np.random.default_rng(99)
+    reqs = []
+    for i in range(args.stress_requests):
+        if rng.random() < 0.1:
+            reqs.append({"key": "inst", "w": 4096, "h": 2160, "spp": int(rng.integers(1, 5)), "max_verts": 17})
+        else:
+            r = int(rng.choice(syn.BATCH_RESOLUTIONS))
+            reqs.append({"key": int(rng.integers(0, 32)), "w": r, "h": r, "spp": int(rng.integers(4, 65)),
+                         "max_verts": int(rng.integers(6, 13)) + 1})
+        reqs[-1]["seed"] = int(rng.integers(0, 2**31))
+    mean_paths = float(np.mean([q["w"] * q["h"] * q["spp"] for q in reqs]))
+    rate = 0.8 * ctx["paths_per_s"] / mean_paths
+    t = 0.0
+    for q in reqs:
+        t += rng.exponential(1.0 / rate)
+        q["arrival"] = t
+
+    def make_scene(key):
+        if key == "inst":
+            s, _, _ = syn.instanced_scene(prefix="stress_inst_")
+        else:
+            j = jobs[key]
+            s, _ = syn.triangles_scene(j["scene_seed"], j["tris"], 64, 64, prefix=f"stress{key}_")
+        s.build()
+        return s
+    budget = args.stress_budget_mb << 20
+    srv = RenderServer(make_scene, hbm_budget=budget, queue_paths=ctx["queue"], max_inflight=256)
+    t0 = srv.clock()
+    i, n, released = 0, len(reqs), 0
+    while i < n or not srv.idle():
+        now = srv.clock() - t0
+        while i < n and reqs[i]["arrival"] <= now:
+            q = reqs[i]
+            srv.submit(Request(rid=i, arrival=t0 + q["arrival"], scene_key=q["key"], w=q["w"], h=q["h"], spp=q["spp"],
+                               max_verts=q["max_verts"], seed=q["seed"]))
+            i += 1
+        if srv.idle() and i < n:
+            time.sleep(max(0.0, reqs[i]["arrival"] - (srv.clock() - t0)))
+            continue
+        srv.step()
+        for r in srv.finished[released:]:
+            srv.release(r.rid)
+        released = len(srv.finished)
+    total = srv.clock() - t0
+    lat = srv.latencies()
+    inst = [r for r in srv.finished if r.scene_key == "inst"]
+    small = [r for r in srv.finished if r.scene_key != "inst"]
+    pct = lambda xs, p: float(np.percentile(xs, p)) if xs else None  # noqa: E731
+    st = srv.batch.stats()
+    srv.batch.close()
+    return {"workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the measured path throughput for this mix), "
+                        f"{len(inst)} instanced 4096x2160 jobs (1-4 spp, length 16) among batched-workload jobs on 32 "
+                        f"scenes; {args.stress_budget_mb} MB HBM budget; scenes built on admission",
+            "requests": n, "seconds": total, "jobs_per_s": n / total, "Mrays_per_s": st["rays"] / total / 1e6,
+            "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"], "done_p50_s": lat["done_p50"],
+            "done_p99_s": lat["done_p99"],
+            "instanced_done_p50_s": pct([r.done - r.arrival for r in inst], 50),
+            "small_done_p99_s": pct([r.done - r.arrival for r in small], 99),
+            "evictions": srv.evictions, "scene_builds": srv.scene_builds,
+            "scene_build_seconds": srv.scene_build_seconds, "peak_resident_bytes": srv.peak_resident_bytes,
+            "budget_bytes": budget}
 
 
 def run_instanced(lm, args) -> dict:
@@ -518,6 +597,8 @@ def main():
     ap.add_argument("--batched-jobs", type=int, default=256)
     ap.add_argument("--served-requests", type=int, default=5000, help="0 skips the served leg")
     ap.add_argument("--instanced-spp", type=int, default=4, help="spp of the instanced leg (0 skips it)")
+    ap.add_argument("--stress-requests", type=int, default=300, help="requests of the served stress leg (0 skips it)")
+    ap.add_argument("--stress-budget-mb", type=int, default=1536)
     args = ap.parse_args()
     _apply_overrides(args)
     if args.impl == "reference":

@@ -177,6 +177,9 @@ class RenderServer:
         self.peak_resident_bytes = 0
         self.evictions = 0
         self.owns_scenes = True  # False: make_scene hands out scenes the caller keeps; eviction only forgets them
+        self.scene_builds = 0
+        self.scene_build_seconds = 0.0
+        self.footprints: dict[Any, int] = {}  # measured device bytes per scene key
         self._film_seq = 0
 
     # -- admission -------------------------------------------------------------------------------
@@ -187,9 +190,18 @@ class RenderServer:
     def _film_bytes(self, req: Request) -> int:
         return 0 if req.refine is not None else req.w * req.h * 3 * 4 * 2
 
-    def _evict_for(self, need: int, keep=None) -> None:
-        """Evicts idle scenes (least recently used first, never `keep`) until `need` more bytes fit."""
-        idle = sorted((t, k) for k, t in self.scene_last_use.items() if self.scene_users.get(k, 0) == 0 and k != keep)
+    def _evictable(self, keep=None) -> int:
+        return sum(nb for k, (_, nb) in self.scenes.items() if self.scene_users.get(k, 0) == 0 and k != keep)
+
+    def _evict_for(self, need: int, keep=None) -> bool:
+        """Makes `need` more bytes fit by evicting idle scenes (least recently used first, never
+        `keep`). Evicts nothing and returns False when even evicting every idle scene would not do."""
+        if self.resident_bytes + need <= self.budget:
+            return True
+        if self.resident_bytes - self._evictable(keep) + need > self.budget:
+            return False
+        idle = sorted(((t, k) for k, t in self.scene_last_use.items() if self.scene_users.get(k, 0) == 0 and k != keep),
+                      key=lambda e: e[0])
         for _, k in idle:
             if self.resident_bytes + need <= self.budget:
                 break
@@ -200,6 +212,7 @@ class RenderServer:
             del self.scene_last_use[k]
             self.scene_users.pop(k, None)
             self.evictions += 1
+        return self.resident_bytes + need <= self.budget
 
     def _try_admit(self, req: Request) -> bool:
         if len(self.inflight) >= self.max_inflight:
@@ -212,18 +225,24 @@ class RenderServer:
                 raise ValueError(f"request {req.rid} refines request {req.refine}, whose film was released")
         need = self._film_bytes(req)
         if req.scene_key not in self.scenes:
+            # a scene measured before is not rebuilt until its footprint fits
+            known = self.footprints.get(req.scene_key)
+            if known is not None and not self._evict_for(need + known):
+                return False
+            t0 = self.clock()
             scene = self.make_scene(req.scene_key)
+            self.scene_builds += 1
+            self.scene_build_seconds += self.clock() - t0
             nbytes = scene_footprint(scene)
-            self._evict_for(need + nbytes)
-            if self.resident_bytes + need + nbytes > self.budget:
+            self.footprints[req.scene_key] = nbytes
+            if not self._evict_for(need + nbytes):
                 if self.owns_scenes:
                     _release_scene(scene)
                 return False
             self.scenes[req.scene_key] = (scene, nbytes)
             self.resident_bytes += nbytes
         else:
-            self._evict_for(need, keep=req.scene_key)
-            if self.resident_bytes + need > self.budget:
+            if not self._evict_for(need, keep=req.scene_key):
                 return False
         scene, _ = self.scenes[req.scene_key]
         import lightmetrica as lm

@@ -153,3 +153,36 @@ def test_render_server_never_evicts_the_scene_it_admits(monkeypatch):
     req = serving.Request(rid=2, arrival=0.0, scene_key="b", w=2, h=2, spp=1, max_verts=2, seed=0)
     assert srv._try_admit(req)            # evicts "a" (older use time does not matter: "b" is needed)
     assert "b" in srv.scenes and "a" not in srv.scenes and srv.evictions == 1
+
+
+def test_render_server_does_not_rebuild_a_scene_that_cannot_fit(monkeypatch):
+    """A scene whose measured footprint does not fit is built once and then waits; nothing is
+    evicted for a request that eviction cannot make room for (host logic; device calls stubbed)."""
+    from lightmetrica import serving
+
+    class FakeBatch:
+        def __init__(self, *a, **k):
+            self.n = 0
+
+        def submit(self, *a, **k):
+            self.n += 1
+            return self.n - 1
+
+    builds = []
+    monkeypatch.setattr(serving, "BatchRenderer", FakeBatch)
+    monkeypatch.setattr(serving, "scene_footprint", lambda s: 1000 if s == "big" else 100)
+    monkeypatch.setattr(serving, "_release_scene", lambda s: None)
+    import lightmetrica as lm
+    monkeypatch.setattr(lm, "load_film", lambda *a, **k: object())
+
+    def make(k):
+        builds.append(k)
+        return k
+    srv = serving.RenderServer(make, hbm_budget=500)
+    small = serving.Request(rid=0, arrival=0.0, scene_key="small", w=2, h=2, spp=1, max_verts=2, seed=0)
+    assert srv._try_admit(small)
+    srv.scene_users["small"] = 0
+    big = serving.Request(rid=1, arrival=0.0, scene_key="big", w=2, h=2, spp=1, max_verts=2, seed=0)
+    for _ in range(5):
+        assert not srv._try_admit(big)
+    assert builds.count("big") == 1 and "small" in srv.scenes and srv.evictions == 0
