@@ -443,7 +443,7 @@ def run_served(lm, args, ctx) -> dict:
     total = srv.clock() - t0
     lat = srv.latencies()
     st = srv.batch.stats()
-    srv.batch.close()
+    srv.close()
     return {"workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the batched capacity), "
                         f"{sum(1 for q in reqs if q['refine'] is not None)} refinements (+16 spp), scenes of the "
                         f"batched workload, 150 GB HBM budget",
@@ -512,7 +512,7 @@ def run_served_stress(lm, args, ctx) -> dict:
     small = [r for r in srv.finished if r.scene_key != "inst"]
     pct = lambda xs, p: float(np.percentile(xs, p)) if xs else None  # noqa: E731
     st = srv.batch.stats()
-    srv.batch.close()
+    srv.close()
     return {"workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the measured path throughput for this mix), "
                         f"{len(inst)} instanced 4096x2160 jobs (1-4 spp, length 16) among batched-workload jobs on 32 "
                         f"scenes; {args.stress_budget_mb} MB HBM budget; scenes built on admission",

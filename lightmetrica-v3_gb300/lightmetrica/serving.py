@@ -18,9 +18,9 @@ the estimator or the intersection arithmetic:
 from __future__ import annotations
 
 import ctypes as C
-import heapq
 import time
-from dataclasses import dataclass, field
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass
 from typing import Any
 
 import numpy as np
@@ -152,14 +152,16 @@ class RenderServer:
     """Resident request loop with continuous batching and HBM-budget admission.
 
     make_scene(scene_key) -> a built `lightmetrica` scene whose asset names are unique to the key
-    (loading an existing asset name replaces that asset). Scenes are cached by key; their
+    (loading an existing asset name replaces that asset). With build_threads > 0 it runs on worker
+    threads, so the wavefront keeps serving admitted requests while a scene builds (the native
+    build releases the GIL). Scenes are cached by key; their
     measured device footprint plus the films of admitted requests count against hbm_budget.
     A request waits when admitting it would exceed the budget or the in-flight request limit; idle
     scenes (no admitted request uses them) are evicted least-recently-used to make room.
     """
 
     def __init__(self, make_scene, hbm_budget: int, queue_paths: int = 0, max_inflight: int = 256,
-                 chunks_per_step: int = 1, clock=time.perf_counter):
+                 chunks_per_step: int = 1, clock=time.perf_counter, build_threads: int = 1):
         self.make_scene = make_scene
         self.budget = int(hbm_budget)
         self.max_inflight = max_inflight
@@ -180,6 +182,8 @@ class RenderServer:
         self.scene_builds = 0
         self.scene_build_seconds = 0.0
         self.footprints: dict[Any, int] = {}  # measured device bytes per scene key
+        self._pool = ThreadPoolExecutor(build_threads) if build_threads > 0 else None
+        self._building: dict[Any, Any] = {}  # scene key -> future of (scene, build seconds)
         self._film_seq = 0
 
     # -- admission -------------------------------------------------------------------------------
@@ -227,12 +231,14 @@ class RenderServer:
         if req.scene_key not in self.scenes:
             # a scene measured before is not rebuilt until its footprint fits
             known = self.footprints.get(req.scene_key)
-            if known is not None and not self._evict_for(need + known):
+            if known is not None and req.scene_key not in self._building and not self._evict_for(need + known):
                 return False
-            t0 = self.clock()
-            scene = self.make_scene(req.scene_key)
+            built = self._scene_ready(req.scene_key)
+            if built is None:
+                return False
+            scene, secs = built
             self.scene_builds += 1
-            self.scene_build_seconds += self.clock() - t0
+            self.scene_build_seconds += secs
             nbytes = scene_footprint(scene)
             self.footprints[req.scene_key] = nbytes
             if not self._evict_for(need + nbytes):
@@ -263,6 +269,31 @@ class RenderServer:
         self.inflight.append(req)
         return True
 
+    def _build(self, key):
+        t0 = time.perf_counter()
+        scene = self.make_scene(key)
+        return scene, time.perf_counter() - t0
+
+    def _scene_ready(self, key):
+        """(scene, build seconds) once the scene for `key` is built, else None (a build is started
+        on the worker threads, or runs here when there are none)."""
+        if self._pool is None:
+            return self._build(key)
+        fut = self._building.get(key)
+        if fut is None:
+            self._building[key] = self._pool.submit(self._build, key)
+            return None
+        if not fut.done():
+            return None
+        del self._building[key]
+        return fut.result()
+
+    def close(self) -> None:
+        if self._pool is not None:
+            self._pool.shutdown(wait=True)
+            self._pool = None
+        self.batch.close()
+
     # -- loop ------------------------------------------------------------------------------------
     def step(self) -> None:
         """Admits what fits, advances the wavefront one step, and records progress."""
@@ -272,6 +303,8 @@ class RenderServer:
                 still.append(req)
         self.pending = still
         if not self.inflight:
+            if self._building:
+                time.sleep(2e-4)  # waiting for a scene build only: let the worker run
             return
         self.batch.run(self.chunks)
         now = self.clock()

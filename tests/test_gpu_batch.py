@@ -118,10 +118,10 @@ def test_render_server_admission_and_latency(lm):
     reqs.append(Request(rid=10, arrival=t0, scene_key=0, w=16, h=12, spp=4, max_verts=7, seed=99, refine=0))
     for r in reqs:
         srv.submit(r)
-    for _ in range(2000):
+    import time
+    t_end = time.time() + 120
+    while not srv.idle() and time.time() < t_end:
         srv.step()
-        if srv.idle():
-            break
     assert srv.idle()
     assert len(srv.finished) == 11
     lat = srv.latencies()
@@ -133,6 +133,7 @@ def test_render_server_admission_and_latency(lm):
     before = srv.resident_bytes
     srv.release(1)
     assert srv.resident_bytes == before - film and reqs[1].film is None
+    srv.close()
 
 
 def test_first_pass_priority(lm, native_lib):

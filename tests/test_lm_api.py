@@ -144,7 +144,7 @@ def test_render_server_never_evicts_the_scene_it_admits(monkeypatch):
     monkeypatch.setattr(serving, "_release_scene", lambda s: None)
     import lightmetrica as lm
     monkeypatch.setattr(lm, "load_film", lambda *a, **k: object())
-    srv = serving.RenderServer(lambda k: f"scene{k}", hbm_budget=2 * 100 + 2 * 96)  # two scenes + two 2x2 films
+    srv = serving.RenderServer(lambda k: f"scene{k}", hbm_budget=2 * 100 + 2 * 96, build_threads=0)  # two scenes + two films
     for rid, key in ((0, "a"), (1, "b")):
         srv.submit(serving.Request(rid=rid, arrival=0.0, scene_key=key, w=2, h=2, spp=1, max_verts=2, seed=0))
         assert srv._try_admit(srv.pending.pop())
@@ -178,7 +178,7 @@ def test_render_server_does_not_rebuild_a_scene_that_cannot_fit(monkeypatch):
     def make(k):
         builds.append(k)
         return k
-    srv = serving.RenderServer(make, hbm_budget=500)
+    srv = serving.RenderServer(make, hbm_budget=500, build_threads=0)
     small = serving.Request(rid=0, arrival=0.0, scene_key="small", w=2, h=2, spp=1, max_verts=2, seed=0)
     assert srv._try_admit(small)
     srv.scene_users["small"] = 0
@@ -186,3 +186,43 @@ def test_render_server_does_not_rebuild_a_scene_that_cannot_fit(monkeypatch):
     for _ in range(5):
         assert not srv._try_admit(big)
     assert builds.count("big") == 1 and "small" in srv.scenes and srv.evictions == 0
+
+
+def test_render_server_builds_scenes_on_a_worker(monkeypatch):
+    """With build threads, admission starts the build and returns; the request is admitted once
+    the scene is ready, and the scene is built once."""
+    import threading
+    import time
+    from lightmetrica import serving
+
+    class FakeBatch:
+        def __init__(self, *a, **k):
+            pass
+
+        def submit(self, *a, **k):
+            return 0
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(serving, "BatchRenderer", FakeBatch)
+    monkeypatch.setattr(serving, "scene_footprint", lambda s: 100)
+    import lightmetrica as lm
+    monkeypatch.setattr(lm, "load_film", lambda *a, **k: object())
+    gate = threading.Event()
+    builds = []
+
+    def make(k):
+        gate.wait(5)
+        builds.append(k)
+        return k
+    srv = serving.RenderServer(make, hbm_budget=10**6, build_threads=1)
+    req = serving.Request(rid=0, arrival=0.0, scene_key="s", w=2, h=2, spp=1, max_verts=2, seed=0)
+    assert not srv._try_admit(req) and not srv._try_admit(req)   # building
+    gate.set()
+    for _ in range(500):
+        if srv._try_admit(req):
+            break
+        time.sleep(0.01)
+    assert req.job is not None and builds == ["s"] and srv.scene_builds == 1
+    srv.close()
