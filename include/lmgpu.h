@@ -147,12 +147,14 @@ int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, 
 #define LMGPU_MAT_GLOSSY 1
 #define LMGPU_MAT_GLASS 2
 #define LMGPU_MAT_MIRROR 3
+#define LMGPU_MAT_MIXTURE 4  /* material::mixture_wavefrontobj without alpha mask: diffuse + glossy */
 
 typedef struct lmgpu_material {
     int32_t type;       /* LMGPU_MAT_* */
-    float color[3];     /* diffuse: Kd; glossy: Ks; otherwise unused */
-    float ax, ay;       /* glossy GGX roughness */
+    float color[3];     /* diffuse and mixture: Kd; glossy: Ks; otherwise unused */
+    float ax, ay;       /* glossy and mixture: GGX roughness */
     float ni;           /* glass index of refraction */
+    float ks[3];        /* mixture: Ks of its glossy lobe */
 } lmgpu_material;
 
 #define LMGPU_LIGHT_AREA 0

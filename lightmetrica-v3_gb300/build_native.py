@@ -54,7 +54,9 @@ def _stale(out: str, deps: list[str]) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None, force: bool = False) -> str:
+    """Compiles the stale sources (all of them with force=True, e.g. when extra_nvcc changes)
+    and links lightmetrica/_lib/liblmgpu.so."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     nvcc = _nvcc()
@@ -67,7 +69,7 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
-        if _stale(o, [s] + headers):
+        if force or _stale(o, [s] + headers):
             jobs.append([nvcc] + NVCC_FLAGS + (extra_nvcc or []) + ["-c", s, "-o", o])
     for src in CPP_SOURCES:
         s = os.path.join(CSRC, src)

@@ -116,6 +116,24 @@ __device__ inline bool tri_test(f3 o, f3 d, f3 p1, f3 e1, f3 e2, float tl, float
 
 __device__ inline uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
+// Three-input min / max (one instruction each on sm_100 and later; exact, like the two-input
+// forms, so the slab test's result does not change).
+#ifndef LMGPU_NO_MINMAX3
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+#else
+__device__ __forceinline__ float fmax3(float a, float b, float c) { return fmaxf(fmaxf(a, b), c); }
+__device__ __forceinline__ float fmin3(float a, float b, float c) { return fminf(fminf(a, b), c); }
+#endif
+
 // Permutes the 8 slot bits of `m` so that bit (s ^ oct) holds slot s.
 __device__ inline uint32_t oct_permute(uint32_t m, uint32_t oct) {
     if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
@@ -248,8 +266,8 @@ __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* st
         const float qfy = __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x4B00u, sel));
         const float qnz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x4B00u, sel));
         const float qfz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B00u, sel));
-        const float tn = fmaxf(fmaxf(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8)), fmaxf(fmaf(qnz, az8, bz8), s.tmin));
-        const float tf0 = fminf(fminf(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8)), fminf(fmaf(qfz, az8, bz8), s.best.t));
+        const float tn = fmax3(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8), fmaxf(fmaf(qnz, az8, bz8), s.tmin));
+        const float tf0 = fmin3(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8), fminf(fmaf(qfz, az8, bz8), s.best.t));
         // Widening the far side by 2^-18 covers the relative error of both sides. Empty slots
         // hold inverted boxes (qlo = 255, qhi = 0) that no ray enters; one accepted through
         // rounding is a leaf of zero triangles.

@@ -27,7 +27,7 @@ struct DevMaterial {
     int32_t type;
     float c[3];
     float ax, ay, ni;
-    int32_t pad;
+    float ks[3];  // mixture: the glossy lobe's Ks
 };
 struct DevLight {
     int32_t type;
@@ -244,21 +244,62 @@ __device__ inline void glass_fresnel(const DevMaterial& m, const Geom& g, f3 wi,
 }
 __device__ inline bool mat_specular(const DevMaterial& m) { return m.type == LMGPU_MAT_GLASS || m.type == LMGPU_MAT_MIRROR; }
 
+// Lobes shared by the glossy and mixture materials (material_glossy.cpp:35-113) and the diffuse
+// and mixture materials (material_diffuse.cpp:55-95).
+__device__ inline f3 glossy_eval(const DevMaterial& m, f3 ks, const Geom& g, f3 wi, f3 wo) {
+    if (opposite(g, wi, wo)) return mk(0, 0, 0);
+    const f3 wh = normalize(wi + wo);
+    f3 n, u, v;
+    basis2(g, wi, n, u, v);
+    const float f5 = powf(1.f - dot(wo, wh), 5.f);
+    const f3 Fr = ks + (mk(1, 1, 1) - ks) * f5;
+    const float k = ggx_d(m, wh, u, v, n) * (ggx_g1(m, wi, u, v, n) * ggx_g1(m, wo, u, v, n)) / (4.f * dot(wi, n) * dot(wo, n));
+    return ks * Fr * k;
+}
+__device__ inline float glossy_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 wo) {
+    if (opposite(g, wi, wo)) return 0.f;
+    const f3 wh = normalize(wi + wo);
+    f3 n, u, v;
+    basis2(g, wi, n, u, v);
+    return ggx_d(m, wh, u, v, n) * dot(wh, n) / (4.f * dot(wo, wh) * dot(wo, n));
+}
+__device__ inline bool glossy_dir(const DevMaterial& m, const Geom& g, f3 wi, float u0, float u1, f3& wo) {
+    f3 n, u, v;
+    basis2(g, wi, n, u, v);
+    const float a1 = u0 * 2.f * kPi;
+    float s1, c1;
+    sincosf(a1, &s1, &c1);
+    const f3 wh = normalize(sqrtf(fmaxf(0.f, u1 / (1.f - u1))) * (m.ax * c1 * u + m.ay * s1 * v) + n);
+    wo = 2.f * dot(wi, wh) * wh - wi;
+    return !opposite(g, wi, wo);
+}
+__device__ inline f3 diffuse_dir(const Geom& g, f3 wi, float u0, float u1) {
+    f3 n, u, v;
+    basis2(g, wi, n, u, v);
+    const float r = sqrtf(fmaxf(0.f, u0)), t = 2.f * kPi * u1;
+    float st, ct;
+    sincosf(t, &st, &ct);
+    const float x = r * ct, y = r * st;
+    const float z = sqrtf(fmaxf(0.f, 1.f - x * x - y * y));
+    return mix3(u, x, v, y, n, z);
+}
+// material::mixture_wavefrontobj: probability of the diffuse lobe, max(Kd) / (max(Kd) + max(Ks))
+// (model_wavefrontobj.cpp:427-435)
+__device__ inline float mixture_w(const DevMaterial& m) {
+    const float wd = fmaxf(fmaxf(m.c[0], m.c[1]), m.c[2]), wg = fmaxf(fmaxf(m.ks[0], m.ks[1]), m.ks[2]);
+    return (wd == 0.f && wg == 0.f) ? 1.f : wd / (wd + wg);
+}
+
 __device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, int comp, bool eval_delta) {
     switch (m.type) {
     case LMGPU_MAT_DIFFUSE:
         if (opposite(g, wi, wo)) return mk(0, 0, 0);
         return mk(m.c[0], m.c[1], m.c[2]) / kPi;
-    case LMGPU_MAT_GLOSSY: {
-        if (opposite(g, wi, wo)) return mk(0, 0, 0);
-        const f3 wh = normalize(wi + wo);
-        f3 n, u, v;
-        basis2(g, wi, n, u, v);
-        const f3 ks = mk(m.c[0], m.c[1], m.c[2]);
-        const float f5 = powf(1.f - dot(wo, wh), 5.f);
-        const f3 Fr = ks + (mk(1, 1, 1) - ks) * f5;
-        const float k = ggx_d(m, wh, u, v, n) * (ggx_g1(m, wi, u, v, n) * ggx_g1(m, wo, u, v, n)) / (4.f * dot(wi, n) * dot(wo, n));
-        return ks * Fr * k;
+    case LMGPU_MAT_GLOSSY:
+        return glossy_eval(m, mk(m.c[0], m.c[1], m.c[2]), g, wi, wo);
+    case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507 with alpha 1: the two lobes summed
+        const f3 fd = opposite(g, wi, wo) ? mk(0, 0, 0) : mk(m.c[0], m.c[1], m.c[2]) / kPi;
+        return fd + glossy_eval(m, mk(m.ks[0], m.ks[1], m.ks[2]), g, wi, wo);
     }
     case LMGPU_MAT_GLASS: {
         if (eval_delta) return mk(0, 0, 0);
@@ -276,41 +317,36 @@ __device__ inline float mat_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 w
     switch (m.type) {
     case LMGPU_MAT_DIFFUSE:
         return opposite(g, wi, wo) ? 0.f : 1.f / kPi;
-    case LMGPU_MAT_GLOSSY: {
-        if (opposite(g, wi, wo)) return 0.f;
-        const f3 wh = normalize(wi + wo);
-        f3 n, u, v;
-        basis2(g, wi, n, u, v);
-        return ggx_d(m, wh, u, v, n) * dot(wh, n) / (4.f * dot(wo, wh) * dot(wo, n));
+    case LMGPU_MAT_GLOSSY:
+        return glossy_pdf(m, g, wi, wo);
+    case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:484-494: the lobes' pdfs by selection probability
+        const float w = mixture_w(m);
+        const float pd = opposite(g, wi, wo) ? 0.f : 1.f / kPi;
+        return w * pd + (1.f - w) * glossy_pdf(m, g, wi, wo);
     }
     default:
         return eval_delta ? 0.f : 1.f;
     }
 }
-// Returns false when no direction is produced (glossy below the surface).
-__device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, int comp, float u0, float u1, f3& wo, f3& w) {
+// Returns false when no direction is produced (glossy below the surface). uc: the component
+// random number of the direction sample (DirectionSampleU::udc.x), used by the mixture.
+__device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, int comp, float u0, float u1, float uc, f3& wo,
+                                  f3& w) {
     switch (m.type) {
-    case LMGPU_MAT_DIFFUSE: {
-        f3 n, u, v;
-        basis2(g, wi, n, u, v);
-        const float r = sqrtf(fmaxf(0.f, u0)), t = 2.f * kPi * u1;
-        float st, ct;
-        sincosf(t, &st, &ct);
-        const float x = r * ct, y = r * st;
-        const float z = sqrtf(fmaxf(0.f, 1.f - x * x - y * y));
-        wo = mix3(u, x, v, y, n, z);
+    case LMGPU_MAT_DIFFUSE:
+        wo = diffuse_dir(g, wi, u0, u1);
         w = mk(m.c[0], m.c[1], m.c[2]);
         return true;
-    }
     case LMGPU_MAT_GLOSSY: {
-        f3 n, u, v;
-        basis2(g, wi, n, u, v);
-        const float a1 = u0 * 2.f * kPi;
-        float s1, c1;
-        sincosf(a1, &s1, &c1);
-        const f3 wh = normalize(sqrtf(fmaxf(0.f, u1 / (1.f - u1))) * (m.ax * c1 * u + m.ay * s1 * v) + n);
-        wo = 2.f * dot(wi, wh) * wh - wi;
-        if (opposite(g, wi, wo)) return false;
+        if (!glossy_dir(m, g, wi, u0, u1, wo)) return false;
+        const f3 f = mat_eval(m, g, wi, wo, 0, false);
+        const float p = mat_pdf(m, g, wi, wo, false);
+        w = f / p;
+        return true;
+    }
+    case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:437-461: one lobe sampled, weight f / p of the sum
+        if (uc < mixture_w(m)) wo = diffuse_dir(g, wi, u0, u1);
+        else if (!glossy_dir(m, g, wi, u0, u1, wo)) return false;
         const f3 f = mat_eval(m, g, wi, wo, 0, false);
         const float p = mat_pdf(m, g, wi, wo, false);
         w = f / p;
@@ -876,7 +912,7 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
     rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
     if (nee_ok) nee<kBatched>(S, P, g, &m, wi, comp, thr, u, ids.y, sq, scount, job);
     f3 wo, w;
-    if (!mat_sample(m, g, wi, comp, u[8], u[9], wo, w)) return false;
+    if (!mat_sample(m, g, wi, comp, u[8], u[9], u[10], wo, w)) return false;
     w = w * sn_correction(g, wi, wo);
     const float pdf = (P.mode == LMGPU_SAMPLING_MIS && nee_ok) ? mat_pdf(m, g, wi, wo, true) : 0.f;
     thr = thr * w;
@@ -1036,7 +1072,10 @@ __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lm
                     R = mk(prm.color[0], prm.color[1], prm.color[2]);
                 } else {
                     const DevMaterial m = S.mats[__ldg(S.prim_ml + prim).x];
-                    R = (m.type == LMGPU_MAT_DIFFUSE || m.type == LMGPU_MAT_GLOSSY) ? mk(m.c[0], m.c[1], m.c[2]) : mk(0, 0, 0);
+                    // Material::reflectance: Kd (diffuse, mixture), Ks (glossy), none for the specular ones
+                    R = (m.type == LMGPU_MAT_DIFFUSE || m.type == LMGPU_MAT_GLOSSY || m.type == LMGPU_MAT_MIXTURE)
+                            ? mk(m.c[0], m.c[1], m.c[2])
+                            : mk(0, 0, 0);
                 }
                 c = prm.use_constant_color ? R : R * (.2f + .8f * fabsf(dot(g.n, -d)));
             }
@@ -1217,9 +1256,11 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         std::vector<DevMaterial> mats(D->num_materials);
         for (int32_t i = 0; i < D->num_materials; i++) {
             const lmgpu_material& m = D->materials[i];
-            if (m.type < LMGPU_MAT_DIFFUSE || m.type > LMGPU_MAT_MIRROR) throw Error(LMGPU_ERR_UNSUPPORTED, "unknown material type");
+            if (m.type < LMGPU_MAT_DIFFUSE || m.type > LMGPU_MAT_MIXTURE) throw Error(LMGPU_ERR_UNSUPPORTED, "unknown material type");
+            if (m.type == LMGPU_MAT_MIXTURE && !(m.ax > 0.f && m.ay > 0.f))
+                throw Error(LMGPU_ERR_INVALID_ARGUMENT, "mixture roughness must be > 0");
             if (m.type == LMGPU_MAT_GLOSSY && !(m.ax > 0.f && m.ay > 0.f)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "glossy roughness must be > 0");
-            mats[i] = DevMaterial{m.type, {m.color[0], m.color[1], m.color[2]}, m.ax, m.ay, m.ni, 0};
+            mats[i] = DevMaterial{m.type, {m.color[0], m.color[1], m.color[2]}, m.ax, m.ay, m.ni, {m.ks[0], m.ks[1], m.ks[2]}};
         }
         s->mats.upload(mats.data(), mats.size());
 

@@ -95,6 +95,9 @@ def _resolve(v: Any) -> Any:
             name = v
         if name in _assets:
             return _assets[name]
+        head, _, rest = name.partition(".")
+        if rest and head in _assets and hasattr(_assets[head], "underlying"):
+            return _assets[head].underlying(rest)   # an asset a model owns: $.assets.model.mesh_0
     raise LmGpuError(1, f"Invalid component reference: {v!r}")
 
 
@@ -161,6 +164,7 @@ def load_mesh(name, impl, prop=None, **kw): return _load("mesh", name, impl, pro
 def load_material(name, impl, prop=None, **kw): return _load("material", name, impl, prop, kw)
 def load_light(name, impl, prop=None, **kw): return _load("light", name, impl, prop, kw)
 def load_texture(name, impl, prop=None, **kw): return _load("texture", name, impl, prop, kw)
+def load_model(name, impl, prop=None, **kw): return _load("model", name, impl, prop, kw)
 def load_accel(name, impl, prop=None, **kw): return _load("accel", name, impl, prop, kw)
 def load_scene(name, impl, prop=None, **kw): return _load("scene", name, impl, prop, kw)
 def load_renderer(name, impl, prop=None, **kw): return _load("renderer", name, impl, prop, kw)
@@ -360,7 +364,8 @@ class MeshRaw(Component):
         return self.ns[self.fn].reshape(-1, 3, 3)
 
 
-_MAT_TYPES = {"material::diffuse": 0, "material::glossy": 1, "material::glass": 2, "material::mirror": 3}
+_MAT_TYPES = {"material::diffuse": 0, "material::glossy": 1, "material::glass": 2, "material::mirror": 3,
+              "material::mixture_wavefrontobj": 4}
 
 
 class _Material(Component):
@@ -411,6 +416,124 @@ class MaterialGlass(_Material):
 @_reg("material::mirror")
 class MaterialMirror(_Material):
     pass
+
+
+@_reg("material::mixture_wavefrontobj")
+class MaterialMixtureWavefrontObj(_Material):
+    """material::mixture_wavefrontobj (src/model/model_wavefrontobj.cpp:361-517): the sum of a
+    diffuse (Kd) and a GGX glossy (Ks, ax, ay) lobe, one lobe sampled with probability
+    max(Kd) / (max(Kd) + max(Ks)). Textures (mapKd, and the alpha mask taken from them) are not
+    on the GPU path."""
+
+    def construct(self, prop):
+        if prop.get("mapKd"):
+            raise LmGpuError(2, "material::mixture_wavefrontobj mapKd textures are not supported on the GPU path")
+        self.Kd = _vec3(_req(prop, "Kd"))
+        self.Ks = _vec3(_req(prop, "Ks"))
+        self.ax = float(_req(prop, "ax"))
+        self.ay = float(_req(prop, "ay"))
+
+    def native(self):
+        m = super().native()
+        m.color[:] = [float(x) for x in self.Kd]
+        m.ks[:] = [float(x) for x in self.Ks]
+        m.ax, m.ay = self.ax, self.ay
+        return m
+
+
+@_reg("model::wavefrontobj")
+class ModelWavefrontObj(Component):
+    """model::wavefrontobj (src/model/model_wavefrontobj.cpp:73-235). Props: path; light (the
+    light key for materials with Ke > 0, default light::area); skip_specular_mat; base_material
+    (a material used for every group instead of the MTL ones).
+
+    Materials: illum 5 -> material::mirror, illum 7 -> material::glass (Ni), otherwise
+    material::mixture_wavefrontobj with r = 2 / (2 + Ns), a = sqrt(1 - 0.9 aniso), ax =
+    max(1e-3, r / a), ay = max(1e-3, r * a). One mesh per OBJ primitive, named mesh_<k> with k the
+    number of assets created before it; a material with Ke > 0 adds an area light mesh_<k>_light
+    on that mesh. Faces without normals use the geometric normal."""
+
+    def construct(self, prop):
+        from . import objloader
+        path = _req(prop, "path")
+        try:
+            obj = objloader.load_obj(path)
+        except OSError as e:
+            raise LmGpuError(4, f"Missing OBJ or MTL file: {e}") from None
+        except ValueError as e:
+            raise LmGpuError(4, str(e)) from None
+        self.assets: dict[str, Component] = {}
+        self.groups: list[tuple] = []
+        light_key = prop.get("light", "light::area")
+        skip_spec = bool(prop.get("skip_specular_mat", False))
+        base = _resolve(prop["base_material"]) if prop.get("base_material") is not None else None
+        mat_of: list[Component] = []
+        for m in obj.materials:
+            if base is not None:
+                mat = base
+            elif m.illum in (5, 7):
+                if skip_spec:
+                    mat = MaterialDiffuse(m.name, {"Kd": [0, 0, 0]})
+                elif m.illum == 7:
+                    mat = MaterialGlass(m.name, {"Ni": m.Ni})
+                else:
+                    mat = MaterialMirror(m.name, {})
+            else:
+                if m.map_Kd:
+                    raise LmGpuError(2, f"map_Kd textures are not supported on the GPU path [material='{m.name}']")
+                r = 2.0 / (2.0 + m.Ns)
+                a = math.sqrt(max(0.0, 1.0 - m.an * 0.9))
+                if a == 0.0:
+                    raise LmGpuError(1, f"aniso >= 1/0.9 gives an infinite roughness [material='{m.name}']")
+                mat = MaterialMixtureWavefrontObj(m.name, {"Kd": list(m.Kd), "Ks": list(m.Ks), "ax": max(1e-3, r / a),
+                                                          "ay": max(1e-3, r * a)})
+            self.assets[m.name] = mat
+            mat_of.append(mat)
+        n_ps, n_ns = len(obj.ps), len(obj.ns)
+        for prim in obj.primitives:
+            name = f"mesh_{len(self.assets)}"
+            faces = np.asarray(prim.faces, dtype=np.int64).reshape(-1, 3) if prim.faces else np.zeros((0, 3), np.int64)
+            fp = faces[:, 0]
+            if fp.size and (fp.min() < 0 or fp.max() >= n_ps):
+                raise LmGpuError(1, f"OBJ face refers to a missing position [{name}]")
+            tri = fp.reshape(-1, 3)
+            # the first corner's normal index decides per face (model_wavefrontobj.cpp:299-305)
+            has_n = faces[0::3, 2] >= 0 if faces.size else np.zeros(0, bool)
+            fn = faces[:, 2].copy()
+            if has_n.size and np.any(faces[:, 2].reshape(-1, 3)[has_n] >= n_ns):
+                raise LmGpuError(1, f"OBJ face refers to a missing normal [{name}]")
+            extra = []
+            if (~has_n).any():
+                p = obj.ps[tri[~has_n]]
+                g = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+                g /= np.maximum(np.linalg.norm(g, axis=1, keepdims=True), 1e-300)
+                extra = g
+                idx = n_ns + np.arange(len(g))
+                fn.reshape(-1, 3)[~has_n] = idx[:, None]
+            ns = np.concatenate([obj.ns, extra]) if len(extra) else obj.ns
+            mesh = MeshRaw(name, {"ps": obj.ps.astype(np.float32), "ns": (ns if len(ns) else np.zeros((1, 3))).astype(np.float32),
+                                  "ts": np.zeros((1, 2), np.float32),
+                                  "fs": {"p": fp.astype(np.int32), "n": fn.astype(np.int32), "t": np.zeros(fp.size, np.int32)}})
+            self.assets[name] = mesh
+            mtl = obj.materials[prim.material]
+            light = None
+            if max(mtl.Ke) > 0:
+                cls = _registry.get(light_key if "::" in light_key else f"light::{light_key}")
+                if cls is None:
+                    raise LmGpuError(1, f"Missing component [key='{light_key}']")
+                light = cls(name + "_light", {"Ke": list(mtl.Ke), "mesh": mesh})
+                self.assets[name + "_light"] = light
+            self.groups.append((mesh, mat_of[prim.material], light))
+
+    def underlying(self, name: str) -> Component:
+        if name not in self.assets:
+            raise LmGpuError(1, f"Invalid component reference: {name!r}")
+        return self.assets[name]
+
+    def create_primitives(self, fn) -> None:
+        """Model::create_primitives: fn(mesh, material, light) per group, in file order."""
+        for mesh, mat, light in self.groups:
+            fn(mesh, mat, light)
 
 
 @_reg("texture::bitmap")
@@ -664,11 +787,20 @@ class SceneDefault(Component):
     def add_transformed_primitive(self, transform, prop: dict | None = None, **kw) -> None:
         p = dict(prop or {})
         p.update(kw)
-        if "model" in p:
-            raise LmGpuError(2, "model assets are not supported on the GPU path")
         t = self.create_group_node(transform)
-        self.add_child(t, self.create_primitive_node(p))
+        if "model" in p:
+            self.add_child_from_model(t, p["model"])   # scene.h:141-152
+        else:
+            self.add_child(t, self.create_primitive_node(p))
         self.add_child(0, t)
+
+    def add_child_from_model(self, parent: int, model) -> None:
+        """scene.cpp:158-180: one primitive node per (mesh, material, light) of the model."""
+        m = _resolve(model)
+        if not hasattr(m, "create_primitives"):
+            raise LmGpuError(1, f"Invalid model [loc={model!r}]")
+        m.create_primitives(lambda mesh, mat, light: self.add_child(
+            parent, self.create_primitive_node(mesh=mesh, material=mat, light=light)))
 
     def traverse_primitive_nodes(self, fn) -> None:
         """Depth-first traversal with fp32 global transforms (scene.cpp:216-230)."""

@@ -29,7 +29,8 @@ class AccelStats(C.Structure):
 
 
 class Material(C.Structure):
-    _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("ax", C.c_float), ("ay", C.c_float), ("ni", C.c_float)]
+    _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("ax", C.c_float), ("ay", C.c_float), ("ni", C.c_float),
+                ("ks", C.c_float * 3)]
 
 
 class Light(C.Structure):

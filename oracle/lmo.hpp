@@ -187,8 +187,10 @@ template <typename F> struct Camera {
 };
 
 // ------------------------------------------------------------------------------------------------
-// Materials: src/material/material_{diffuse,glossy,glass,mirror}.cpp
-enum MatType { MAT_DIFFUSE = 0, MAT_GLOSSY = 1, MAT_GLASS = 2, MAT_MIRROR = 3 };
+// Materials: src/material/material_{diffuse,glossy,glass,mirror}.cpp, and
+// material::mixture_wavefrontobj (src/model/model_wavefrontobj.cpp:361-517) without a texture
+// alpha mask: diffuse (Kd) + GGX glossy (Ks, ax, ay) summed, one lobe sampled
+enum MatType { MAT_DIFFUSE = 0, MAT_GLOSSY = 1, MAT_GLASS = 2, MAT_MIRROR = 3, MAT_MIXTURE = 4 };
 
 template <typename F> struct DirectionSample { V3<F> wo; V3<F> weight; };
 template <typename F> struct ComponentSample { int comp; F weight; };
@@ -243,22 +245,64 @@ template <typename F> struct Material {
         return {0, F(1)};
     }
 
-    std::optional<DirectionSample<F>> sample_direction(V2<F> ud, V2<F> /*udc*/, const PointGeometry<F>& g, V3<F> wi, int comp, TransDir td) const {
+    // model_wavefrontobj.cpp:427-435: probability of sampling the diffuse lobe
+    F diffuse_selection_prob() const {
+        const F wd = std::max(Kd.x, std::max(Kd.y, Kd.z)), wg = std::max(Ks.x, std::max(Ks.y, Ks.z));
+        if (wd == F(0) && wg == F(0)) return F(1);
+        return wd / (wd + wg);
+    }
+    // material_diffuse.cpp:63-71 / material_glossy.cpp:70-86, direction only
+    V3<F> diffuse_dir(V2<F> ud, const PointGeometry<F>& g, V3<F> wi) const {
+        V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+        const auto d = sample_cosine_weighted(ud);
+        return u * d.x + v * d.y + n * d.z;
+    }
+    std::optional<V3<F>> glossy_dir(V2<F> ud, const PointGeometry<F>& g, V3<F> wi) const {
+        V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+        const auto u1 = ud.x * F(2) * C<F>::Pi;
+        const auto u2 = ud.y;
+        const auto wh = normalize(safe_sqrt(u2 / (F(1) - u2)) * (ax * std::cos(u1) * u + ay * std::sin(u1) * v) + n);
+        const auto wo = reflection(wi, wh);
+        if (g.opposite(wi, wo)) return {};
+        return wo;
+    }
+    V3<F> glossy_eval(const PointGeometry<F>& g, V3<F> wi, V3<F> wo) const {
+        if (g.opposite(wi, wo)) return V3<F>();
+        const auto wh = normalize(wi + wo);
+        V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+        const auto one_m = V3<F>(F(1)) - Ks;
+        const auto Fr = Ks + one_m * std::pow(F(1) - dot(wo, wh), F(5));
+        return Ks * Fr * (normal_dist(wh, u, v, n) * shadowG(wi, wo, u, v, n) / (F(4) * dot(wi, n) * dot(wo, n)));
+    }
+    F glossy_pdf(const PointGeometry<F>& g, V3<F> wi, V3<F> wo) const {
+        if (g.opposite(wi, wo)) return F(0);
+        const auto wh = normalize(wi + wo);
+        V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
+        return normal_dist(wh, u, v, n) * dot(wh, n) / (F(4) * dot(wo, wh) * dot(wo, n));
+    }
+
+    std::optional<DirectionSample<F>> sample_direction(V2<F> ud, V2<F> udc, const PointGeometry<F>& g, V3<F> wi, int comp, TransDir td) const {
         switch (type) {
-        case MAT_DIFFUSE: {  // material_diffuse.cpp:63-71
-            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
-            const auto d = sample_cosine_weighted(ud);
-            return DirectionSample<F>{u * d.x + v * d.y + n * d.z, Kd};
-        }
+        case MAT_DIFFUSE:  // material_diffuse.cpp:63-71
+            return DirectionSample<F>{diffuse_dir(ud, g, wi), Kd};
         case MAT_GLOSSY: {  // material_glossy.cpp:70-86
-            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
-            const auto u1 = ud.x * F(2) * C<F>::Pi;
-            const auto u2 = ud.y;
-            const auto wh = normalize(safe_sqrt(u2 / (F(1) - u2)) * (ax * std::cos(u1) * u + ay * std::sin(u1) * v) + n);
-            const auto wo = reflection(wi, wh);
-            if (g.opposite(wi, wo)) return {};
-            const auto f = eval(g, wi, wo, 0, td, false);
-            const auto p = pdf_direction(g, wi, wo, 0, false);
+            const auto wo = glossy_dir(ud, g, wi);
+            if (!wo) return {};
+            const auto f = eval(g, wi, *wo, 0, td, false);
+            const auto p = pdf_direction(g, wi, *wo, 0, false);
+            return DirectionSample<F>{*wo, f / p};
+        }
+        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:437-461, component 0 (no alpha mask)
+            V3<F> wo;
+            if (udc.x < diffuse_selection_prob()) {
+                wo = diffuse_dir(ud, g, wi);
+            } else {
+                const auto w = glossy_dir(ud, g, wi);
+                if (!w) return {};
+                wo = *w;
+            }
+            const auto f = eval(g, wi, wo, comp, td, false);
+            const auto p = pdf_direction(g, wi, wo, comp, false);
             return DirectionSample<F>{wo, f / p};
         }
         case MAT_GLASS: {  // material_glass.cpp:163-188
@@ -285,11 +329,11 @@ template <typename F> struct Material {
     F pdf_direction(const PointGeometry<F>& g, V3<F> wi, V3<F> wo, int, bool eval_delta) const {
         switch (type) {
         case MAT_DIFFUSE: return g.opposite(wi, wo) ? F(0) : F(1) / C<F>::Pi;
-        case MAT_GLOSSY: {
-            if (g.opposite(wi, wo)) return F(0);
-            const auto wh = normalize(wi + wo);
-            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
-            return normal_dist(wh, u, v, n) * dot(wh, n) / (F(4) * dot(wo, wh) * dot(wo, n));
+        case MAT_GLOSSY: return glossy_pdf(g, wi, wo);
+        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:484-494
+            const F w = diffuse_selection_prob();
+            const F pd = g.opposite(wi, wo) ? F(0) : F(1) / C<F>::Pi;
+            return w * pd + (F(1) - w) * glossy_pdf(g, wi, wo);
         }
         case MAT_GLASS: return eval_delta ? F(0) : F(1);
         case MAT_MIRROR: return eval_delta ? F(0) : F(1);
@@ -302,13 +346,10 @@ template <typename F> struct Material {
         case MAT_DIFFUSE:
             if (g.opposite(wi, wo)) return V3<F>();
             return Kd / C<F>::Pi;
-        case MAT_GLOSSY: {
-            if (g.opposite(wi, wo)) return V3<F>();
-            const auto wh = normalize(wi + wo);
-            V3<F> n, u, v; g.basis_twosided(wi, n, u, v);
-            const auto one_m = V3<F>(F(1)) - Ks;
-            const auto Fr = Ks + one_m * std::pow(F(1) - dot(wo, wh), F(5));
-            return Ks * Fr * (normal_dist(wh, u, v, n) * shadowG(wi, wo, u, v, n) / (F(4) * dot(wi, n) * dot(wo, n)));
+        case MAT_GLOSSY: return glossy_eval(g, wi, wo);
+        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507, alpha = 1
+            const V3<F> fd = g.opposite(wi, wo) ? V3<F>() : Kd / C<F>::Pi;
+            return fd + glossy_eval(g, wi, wo);
         }
         case MAT_GLASS: {
             if (eval_delta) return V3<F>(F(0));
@@ -328,6 +369,7 @@ template <typename F> struct Material {
         switch (type) {
         case MAT_DIFFUSE: return Kd;
         case MAT_GLOSSY: return Ks;
+        case MAT_MIXTURE: return Kd;
         default: return V3<F>(F(0));
         }
     }

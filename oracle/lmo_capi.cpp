@@ -71,6 +71,12 @@ int lmo_add_material(void* p, int type, const double* prm) {
         if (type == MAT_DIFFUSE) m.Kd = V3<F>(F(prm[0]), F(prm[1]), F(prm[2]));
         if (type == MAT_GLOSSY) { m.Ks = V3<F>(F(prm[0]), F(prm[1]), F(prm[2])); m.ax = F(prm[3]); m.ay = F(prm[4]); }
         if (type == MAT_GLASS) m.Ni = F(prm[0]);
+        if (type == MAT_MIXTURE) {
+            m.Kd = V3<F>(F(prm[0]), F(prm[1]), F(prm[2]));
+            m.Ks = V3<F>(F(prm[3]), F(prm[4]), F(prm[5]));
+            m.ax = F(prm[6]);
+            m.ay = F(prm[7]);
+        }
         S.materials.push_back(m);
         return int(S.materials.size()) - 1;
     });

@@ -71,7 +71,8 @@ def _chk(rc: int) -> int:
     return rc
 
 
-MAT = {"material::diffuse": 0, "material::glossy": 1, "material::glass": 2, "material::mirror": 3}
+MAT = {"material::diffuse": 0, "material::glossy": 1, "material::glass": 2, "material::mirror": 3,
+       "material::mixture_wavefrontobj": 4}
 
 
 class OracleScene:
@@ -106,7 +107,7 @@ class OracleScene:
                                        ft_.ctypes.data_as(I), fn.ctypes.data_as(I), fp.size))
 
     def add_material(self, kind: int, params) -> int:
-        p = np.zeros(5)
+        p = np.zeros(8)
         p[:len(params)] = params
         return _chk(lib().lmo_add_material(self.h, kind, _dp(p)))
 
@@ -223,7 +224,8 @@ def from_lm_scene(scene, double: bool = True) -> OracleScene:
             m = n["material"]
             if id(m) not in mat_id:
                 k = MAT[m.key_name]
-                params = {0: lambda: list(m.Kd), 1: lambda: list(m.Ks) + [m.ax, m.ay], 2: lambda: [m.Ni], 3: lambda: []}[k]()
+                params = {0: lambda: list(m.Kd), 1: lambda: list(m.Ks) + [m.ax, m.ay], 2: lambda: [m.Ni], 3: lambda: [],
+                          4: lambda: list(m.Kd) + list(m.Ks) + [m.ax, m.ay]}[k]()
                 mat_id[id(m)] = O.add_material(k, params)
             ma = mat_id[id(m)]
         li = -1
