@@ -305,17 +305,22 @@ class FilmBitmap(Component):
         return self.buffer_f32().astype(np.float64)
 
     def save(self, path: str) -> bool:
-        """Writes .pfm (film_bitmap.cpp:197-201, rows unflipped) or .npy."""
+        """Film::save (film_bitmap.cpp:156-210): .png (flipped, gamma 1/2.2, 8 bits), .hdr
+        (flipped, RGBE), .pfm (unflipped) or .npy; missing parent directories are created."""
+        from . import imageio
         img = self.buffer_f32()
         if path.endswith(".pfm"):
-            with open(path, "wb") as f:
-                f.write(f"PF\n{self.w} {self.h}\n-1\n".encode())
-                f.write(np.ascontiguousarray(img, dtype="<f4").tobytes())
-            return True
-        if path.endswith(".npy"):
+            imageio.write_pfm(path, img)
+        elif path.endswith(".hdr"):
+            imageio.write_hdr(path, img)
+        elif path.endswith(".png"):
+            imageio.write_png(path, img)
+        elif path.endswith(".npy"):
+            imageio._parent(path)
             np.save(path, img)
-            return True
-        raise LmGpuError(2, f"Invalid extension [path='{path}']")
+        else:
+            raise LmGpuError(2, f"Invalid extension [path='{path}']")
+        return True
 
 
 @_reg("camera::pinhole")
@@ -545,24 +550,24 @@ class TextureBitmap(Component):
             self.data = np.ascontiguousarray(np.asarray(prop["data"], dtype=np.float32)[..., :3])
         else:
             path = _req(prop, "path")
-            self.data = _read_image(path)
+            self.data = _read_image(path, flip=bool(prop.get("flip", True)))
         self.h, self.w = self.data.shape[:2]
 
 
-def _read_image(path: str) -> np.ndarray:
-    if path.endswith(".npy"):
-        return np.ascontiguousarray(np.load(path).astype(np.float32)[..., :3])
-    if path.endswith(".pfm"):
-        with open(path, "rb") as f:
-            kind = f.readline().strip()
-            w, h = map(int, f.readline().split())
-            s = float(f.readline())
-            ch = 3 if kind == b"PF" else 1
-            data = np.frombuffer(f.read(), dtype="<f4" if s < 0 else ">f4").reshape(h, w, ch).astype(np.float32)
-            if ch == 1:
-                data = np.repeat(data, 3, axis=2)
-            return np.ascontiguousarray(data)
-    raise LmGpuError(2, f"Unsupported image format [path='{path}'] (use .pfm or .npy)")
+def _read_image(path: str, flip: bool = True) -> np.ndarray:
+    """texture::bitmap's image (texture_bitmap.cpp:49-66), row 0 at the bottom: .hdr (flipped on
+    load unless flip=False), .pfm (stored bottom row first), .npy (as stored)."""
+    from . import imageio
+    try:
+        if path.endswith(".npy"):
+            return np.ascontiguousarray(np.load(path).astype(np.float32)[..., :3])
+        if path.endswith(".pfm"):
+            return imageio.read_pfm(path)
+        if path.endswith(".hdr"):
+            return imageio.read_hdr(path, flip=flip)
+    except (OSError, ValueError) as e:
+        raise LmGpuError(4, f"Failed to load image [path='{path}']: {e}") from None
+    raise LmGpuError(2, f"Unsupported image format [path='{path}'] (use .hdr, .pfm or .npy)")
 
 
 class _Light(Component):
