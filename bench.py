@@ -312,8 +312,9 @@ def run_gpu(args) -> None:
                "sample": f"{W_PX}x{H_PX} at 1 spp ({W_PX * H_PX} paths, {crays} rays, {csec:.1f} s)",
                "build_seconds": S.build_seconds}
 
-    waves = -(-(W_PX * H_PX * SPP) // (args.wave or (1 << 22)))
-    launches_per_step = waves * (1 + 3 * (MAX_VERTS - 1)) + 1
+    # kernels per step: every chunk of the shared wavefront launches extend, shade, shadow, plan and
+    # generate once per bounce iteration; one film resolve per render
+    launches_per_step = 5 * tot["ext_launches"] / max(1, args.steps) + 1
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -335,7 +336,7 @@ def run_gpu(args) -> None:
                          "traffic": traffic, "bytes_per_ray": {"extend": b_ext, "shadow": b_sh},
                          "launches": launches, **counts},
             "cpu_baseline": cpu,
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clocks,
             "accel": {"nodes": acc["num_nodes"], "depth": acc["max_depth"], "build_seconds": acc["build_seconds"],
                       "scene_build_seconds": build_s, "sah_cost": acc["sah_cost"]},

@@ -281,9 +281,12 @@ typedef struct lmgpu_render_stats {
 
 /* Renders into `film` (cleared first unless params->accumulate) on `stream` and waits for it.
  * stats may be NULL. The film holds the estimate scaled by 1/spp (pixel mode) or w*h/spp (image
- * mode), as renderer_pt.cpp:307-312 rescales it. The wavefront queues (about 210 bytes per path
- * in flight) belong to the device, not the scene: calls on one device from several host threads
- * take turns. */
+ * mode), as renderer_pt.cpp:307-312 rescales it. The render runs as one job of the device's
+ * shared wavefront (see lmgpu_batch_* below): params->wave_paths paths in flight (0: 2^23, about
+ * 270 bytes each, held by the device after the first call), finished paths replaced by new ones
+ * until the job drains. Instrumented renders (params->instrument) run in fixed waves instead,
+ * one launch per bounce. Either way the image is the same up to the order of fp32 additions.
+ * Calls on one device from several host threads take turns. */
 int lmgpu_render_pt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params, void* stream,
                     lmgpu_render_stats* stats);
 
@@ -318,6 +321,9 @@ int lmgpu_batch_resolve(lmgpu_batch* batch, int32_t job, void* stream);
 int lmgpu_batch_get_stats(const lmgpu_batch* batch, lmgpu_render_stats* out);
 /* Forgets every job (buffers stay allocated). */
 int lmgpu_batch_reset(lmgpu_batch* batch);
+/* on != 0: runs also time every kernel (event nodes in the captured chunk); lmgpu_batch_get_stats
+ * then reports extend_ms, shade_ms, shadow_ms and generate_ms (planner + camera vertices). */
+int lmgpu_batch_set_timing(lmgpu_batch* batch, int32_t on);
 
 /* No counterpart in the reference. renderer::pt for callers that must not allocate device memory:
  * code that renders while a CUDA graph is being captured (cudaMalloc is not a capturable call),

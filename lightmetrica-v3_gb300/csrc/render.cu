@@ -532,6 +532,7 @@ struct JobDev {
 };
 
 constexpr int kBlock = 256;
+constexpr int64_t kRenderQueue = int64_t(1) << 23;  // paths in flight of lmgpu_render_pt by default
 #ifndef LMGPU_TRACE_MINBLOCKS
 #define LMGPU_TRACE_MINBLOCKS 4  // resident 256-thread blocks per SM (5 and 6 spill and measured slower)
 #endif
@@ -1100,13 +1101,16 @@ int grid_for(K kernel, int block, size_t smem) {
     return std::max(1, per_sm) * current_device().num_sms;
 }
 
-// Wavefront queues of lmgpu_render_pt: one set per device, shared by every scene and held for the
-// whole of a call (the call ends with its stream synchronized), so scenes cost only their own
-// tables. Grown on demand; kept for the life of the process.
+// Per-device state of lmgpu_render_pt, shared by every scene and held for the whole of a call (the
+// call ends with its stream synchronized), so scenes cost only their own tables: the shared
+// wavefront a render runs its job on, and the fixed-wave queues of instrumented renders. Grown on
+// demand; kept for the life of the process.
 struct Workspace {
     std::mutex m;
     int64_t cap = 0;
     DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
+    lmgpu_batch* batch = nullptr;  // the regenerating wavefront lmgpu_render_pt runs its job on
+    int64_t batch_cap = 0;
 };
 
 Workspace& workspace(int device) {
@@ -1455,15 +1459,16 @@ int lmgpu_render_raycast(lmgpu_scene* s, lmgpu_film* f, const lmgpu_raycast_para
     });
 }
 
-int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, void* stream, lmgpu_render_stats* stats) {
-    return guarded([&] {
-        if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
-        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
-        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
-        if (prm->spp <= 0 || prm->max_verts < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "spp must be > 0 and max_verts >= 1");
-        if (prm->max_verts > 255) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 255");
-        if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
-            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
+namespace {
+
+void must(int rc) {
+    if (rc != LMGPU_OK) throw Error(rc, lmgpu_last_error());
+}
+
+// Fixed waves of at most wave_paths paths, each run for max_verts - 1 bounces with one launch per
+// kernel per bounce. Used for instrumented renders (node / triangle counts).
+void render_pt_waves(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, void* stream, lmgpu_render_stats* stats) {
+    {
         ensure_film(f);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         const int64_t npix = int64_t(f->w) * f->h;
@@ -1622,6 +1627,44 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
                 stats->shadow_worst_ray[i] = hw[8 + i];
             }
         }
+    }
+}
+
+}  // namespace
+
+int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, void* stream, lmgpu_render_stats* stats) {
+    return guarded([&] {
+        if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
+        if (prm->spp <= 0 || prm->max_verts < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "spp must be > 0 and max_verts >= 1");
+        if (prm->max_verts > 255) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 255");
+        if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
+        if (prm->instrument) {
+            render_pt_waves(s, f, prm, stream, stats);
+            return;
+        }
+        // One job on the device's shared wavefront: finished paths are replaced by new ones of
+        // the same job, so every bounce launch sees a full queue (a fixed wave thins out).
+        Workspace& ws = workspace(current_device().device);
+        std::lock_guard<std::mutex> ws_lock(ws.m);
+        const int64_t cap = prm->wave_paths > 0 ? prm->wave_paths : kRenderQueue;
+        if (!ws.batch || ws.batch_cap != cap) {
+            if (ws.batch) must(lmgpu_batch_destroy(ws.batch));
+            ws.batch = nullptr;
+            must(lmgpu_batch_create(&ws.batch, cap));
+            ws.batch_cap = cap;
+        }
+        lmgpu_batch* b = ws.batch;
+        must(lmgpu_batch_reset(b));
+        must(lmgpu_batch_set_timing(b, stats != nullptr));
+        int32_t job = 0;
+        must(lmgpu_batch_submit(b, s, f, prm, &job));
+        int64_t left = 0;
+        must(lmgpu_batch_run(b, 0, stream, &left));
+        must(lmgpu_batch_resolve(b, job, stream));
+        if (stats) must(lmgpu_batch_get_stats(b, stats));
     });
 }
 
@@ -1795,18 +1838,32 @@ struct lmgpu_batch {
     uint32_t passes = 0;
     bool table_dirty = false;
     int32_t max_depth = 1;
-    // captured chunk of iterations
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    int32_t graph_depth = 0;
-    int graph_refill = -1, graph_shade = -1;  // tuning the graph was captured with
-    int refill = 0, shade_minblocks = 3, first_pass = 1, graph_first_pass = -1;
-    bool two_level = false, graph_two_level = false;  // some job's scene is instanced
-    int cur = 0;
+    // captured chunk of iterations: [0] plain, [1] with event nodes between the kernels
+    struct GraphSlot {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int32_t depth = 0;
+        int refill = -1, shade = -1, first_pass = -1;
+        bool two_level = false;
+        void clear() {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+            exec = nullptr;
+            graph = nullptr;
+        }
+    } slot[2];
+    int refill = 0, shade_minblocks = 3, first_pass = 1;
+    bool two_level = false;  // some job's scene is instanced
+    bool timed = false;      // per-kernel device time (lmgpu_batch_set_timing)
+    cudaEvent_t ev[6 * 8] = {};
+    double kms[4] = {0, 0, 0, 0};  // extend, shade, shadow, plan + generate
+    int64_t chunks_run = 0;
     double elapsed_ms = 0;
     ~lmgpu_batch() {
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
+        slot[0].clear();
+        slot[1].clear();
+        for (auto& e : ev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
@@ -1851,7 +1908,7 @@ __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
 }
 
 // Stream-ordered view of one chunk of iterations; captured into a graph.
-void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
+void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
     Bvh8 bmax{};
     bmax.depth = b->max_depth;
@@ -1872,33 +1929,52 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st) {
     float4* hits = b->hits.as<float4>();
     int* fetch = ctl_fetch(b);
     const Fetch f_ext{fetch, fetch + 1, b->refill}, f_sh{fetch + 1, fetch, b->refill};
+    // timed: event record nodes around the kernels, read after each chunk (ev[6*it + k])
+    auto mark = [&](int it, int k) {
+        if (timed) LMGPU_CUDA(cudaEventRecordWithFlags(b->ev[6 * it + k], st, cudaEventRecordExternal));
+    };
     int cur = 0;
     for (int it = 0; it < kChunkIters; it++) {
+        mark(it, 0);
         ext_k<<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
                                                                ctl_sums(b), 63, nullptr, f_ext, jobs, q[cur].job);
+        mark(it, 1);
         LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
         shade_k<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
                                                b->pass_done.as<unsigned int>());
+        mark(it, 2);
         sh_k<<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
                                                               ctl_sums(b), 63, nullptr, f_sh, jobs);
+        mark(it, 3);
         LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
         k_wf_plan<<<1, 32, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap, jobs, b->job_next.as<int64_t>(), b->active.as<ActiveJob>(),
                                     b->alloc.as<AllocEntry>(), b->first_pass);
+        mark(it, 4);
         k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->alloc.as<AllocEntry>(), ctl64(b), q[1 - cur], cnt + (1 - cur), sq,
                                                 cnt + 2);
+        mark(it, 5);
         cur = 1 - cur;
     }
 }
 
-void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
+// The executable graph for the current tuning, depth and timing; recaptured only when one of
+// them changed or a device table moved (realloc).
+cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     b->refill = tuning().trace_refill;
     b->shade_minblocks = tuning().shade_minblocks;
     b->first_pass = tuning().batch_first_pass;
-    if (b->exec && !realloc && b->graph_depth == b->max_depth && b->graph_refill == b->refill &&
-        b->graph_shade == b->shade_minblocks && b->graph_two_level == b->two_level && b->graph_first_pass == b->first_pass)
-        return;
-    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
-    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    if (realloc) {
+        b->slot[0].clear();
+        b->slot[1].clear();
+    }
+    auto& g = b->slot[b->timed ? 1 : 0];
+    if (g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
+        g.two_level == b->two_level && g.first_pass == b->first_pass)
+        return g.exec;
+    g.clear();
+    if (b->timed)
+        for (auto& e : b->ev)
+            if (!e) LMGPU_CUDA(cudaEventCreate(&e));
     cudaStream_t cs;
     LMGPU_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
     // warm-up query of grid sizes outside the capture (occupancy calls are not capturable work)
@@ -1909,23 +1985,35 @@ void ensure_graph(lmgpu_batch* b, cudaStream_t st, bool realloc) {
     (void)grid_for(k_wf_generate, kBlock, 0);
     LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
-        enqueue_chunk(b, cs);
+        enqueue_chunk(b, cs, b->timed);
     } catch (...) {
-        cudaGraph_t g;
-        cudaStreamEndCapture(cs, &g);
-        if (g) cudaGraphDestroy(g);
+        cudaGraph_t gr;
+        cudaStreamEndCapture(cs, &gr);
+        if (gr) cudaGraphDestroy(gr);
         cudaStreamDestroy(cs);
         throw;
     }
-    LMGPU_CUDA(cudaStreamEndCapture(cs, &b->graph));
+    LMGPU_CUDA(cudaStreamEndCapture(cs, &g.graph));
     LMGPU_CUDA(cudaStreamDestroy(cs));
-    LMGPU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
-    b->graph_depth = b->max_depth;
-    b->graph_refill = b->refill;
-    b->graph_two_level = b->two_level;
-    b->graph_first_pass = b->first_pass;
-    b->graph_shade = b->shade_minblocks;
-    (void)st;
+    LMGPU_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    g.depth = b->max_depth;
+    g.refill = b->refill;
+    g.two_level = b->two_level;
+    g.first_pass = b->first_pass;
+    g.shade = b->shade_minblocks;
+    return g.exec;
+}
+
+// Adds one timed chunk's kernel times (events of its last launch) to b->kms.
+void read_chunk_times(lmgpu_batch* b) {
+    for (int it = 0; it < kChunkIters; it++) {
+        float m[5];
+        for (int k = 0; k < 5; k++) LMGPU_CUDA(cudaEventElapsedTime(&m[k], b->ev[6 * it + k], b->ev[6 * it + k + 1]));
+        b->kms[0] += m[0];
+        b->kms[1] += m[1];
+        b->kms[2] += m[2];
+        b->kms[3] += m[3] + m[4];
+    }
 }
 
 }  // namespace
@@ -1949,6 +2037,13 @@ int lmgpu_batch_create(lmgpu_batch** out, int64_t queue_paths) {
         b->ctl.alloc(256);
         LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
         *out = b.release();
+    });
+}
+
+int lmgpu_batch_set_timing(lmgpu_batch* b, int32_t on) {
+    return guarded([&] {
+        if (!b) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "batch is null");
+        b->timed = on != 0;
     });
 }
 
@@ -2045,7 +2140,7 @@ int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* p
             if (paths_left) *paths_left = 0;
             return;
         }
-        ensure_graph(b, st, realloc);
+        cudaGraphExec_t exec = ensure_graph(b, realloc);
         cudaEvent_t e0, e1;
         LMGPU_CUDA(cudaEventCreate(&e0));
         LMGPU_CUDA(cudaEventCreate(&e1));
@@ -2054,14 +2149,16 @@ int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* p
         int chunks = 0;
         int herr = 0;
         for (;;) {
-            LMGPU_CUDA(cudaGraphLaunch(b->exec, st));
+            LMGPU_CUDA(cudaGraphLaunch(exec, st));
             chunks++;
             LMGPU_CUDA(cudaMemcpyAsync(&left, ctl64(b) + 4, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
             LMGPU_CUDA(cudaMemcpyAsync(&herr, ctl_cnt(b) + 3, sizeof(int), cudaMemcpyDeviceToHost, st));
             LMGPU_CUDA(cudaStreamSynchronize(st));
+            if (b->timed) read_chunk_times(b);
             if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
             if (left == 0 || (max_chunks > 0 && chunks >= max_chunks)) break;
         }
+        b->chunks_run += chunks;
         LMGPU_CUDA(cudaEventRecord(e1, st));
         LMGPU_CUDA(cudaMemcpyAsync(b->host_pass.data(), b->pass_done.p, size_t(b->passes) * 4, cudaMemcpyDeviceToHost, st));
         LMGPU_CUDA(cudaStreamSynchronize(st));
@@ -2116,6 +2213,13 @@ int lmgpu_batch_get_stats(const lmgpu_batch* b, lmgpu_render_stats* out) {
         out->shadow_rays = int64_t(r[1]);
         out->rays = int64_t(r[0] + r[1]);
         out->elapsed_ms = b->elapsed_ms;
+        out->extend_ms = b->kms[0];
+        out->shade_ms = b->kms[1];
+        out->shadow_ms = b->kms[2];
+        out->generate_ms = b->kms[3];
+        out->trace_ms = b->kms[0] + b->kms[2];
+        out->extend_launches = b->chunks_run * kChunkIters;
+        out->shadow_launches = b->chunks_run * kChunkIters;
     });
 }
 
@@ -2129,9 +2233,11 @@ int lmgpu_batch_reset(lmgpu_batch* b) {
         b->jobs_done = 0;
         b->total = 0;
         b->passes = 0;
-        b->max_depth = 1;
-        b->two_level = false;
+        // the captured graphs stay valid: their stack depth and two-level traversal cover any
+        // shallower or single-level scene, so max_depth and two_level are kept
         b->elapsed_ms = 0;
+        b->chunks_run = 0;
+        for (double& k : b->kms) k = 0;
         b->table_dirty = false;
         LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
         if (b->pass_cap) LMGPU_CUDA(cudaMemset(b->pass_done.p, 0, b->pass_cap * 4));

@@ -113,6 +113,7 @@ SIGNATURES = [
     ("lmgpu_batch_resolve", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     ("lmgpu_batch_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
     ("lmgpu_batch_reset", C.c_int, [C.c_void_p]),
+    ("lmgpu_batch_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
     ("lmgpu_render_pt_noalloc", C.c_int, [C.c_void_p, c_float_p, C.c_int32, C.c_int32, C.POINTER(PTParams), C.c_void_p]),
 ]
 

@@ -383,6 +383,25 @@ def test_pt_wave_size_invariance(lm):
     assert np.allclose(outs[0], outs[1], rtol=1e-5, atol=1e-6)
 
 
+def test_pt_engines_agree(lm, native_lib):
+    """An instrumented render (fixed waves, one launch per bounce) and a plain one (the shared
+    wavefront regenerating paths) give the same image: the same paths, summed in another order."""
+    import ctypes as C
+    from lightmetrica import _native as N
+    from lightmetrica import synthetic as syn
+    scene, film, _ = syn.spheres_scene(n_spheres=4, subdiv=3, ground_quads=8, w=40, h=24, prefix="eng_")
+    scene.build()
+    imgs = []
+    for inst in (0, 1):
+        p = N.PTParams()
+        p.spp, p.max_verts, p.seed, p.sampling_mode, p.instrument = 12, 11, 21, 2, inst
+        st = N.RenderStats()
+        N.check(native_lib.lmgpu_render_pt(scene._h, film._h, C.byref(p), None, C.byref(st)))
+        assert st.rays > 0 and st.extend_ms > 0
+        imgs.append(film.buffer_f32().copy())
+    np.testing.assert_allclose(imgs[0], imgs[1], rtol=1e-5, atol=1e-6)
+
+
 def test_render_errors(lm):
     from lightmetrica import synthetic as syn
     scene, film = syn.box_scene(w=8, h=8)
