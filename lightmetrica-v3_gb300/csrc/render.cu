@@ -532,7 +532,7 @@ struct JobDev {
 };
 
 constexpr int kBlock = 256;
-constexpr int64_t kRenderQueue = int64_t(1) << 23;  // paths in flight of lmgpu_render_pt by default
+constexpr int64_t kRenderQueue = int64_t(1) << 24;  // paths in flight of lmgpu_render_pt by default
 #ifndef LMGPU_TRACE_MINBLOCKS
 #define LMGPU_TRACE_MINBLOCKS 4  // resident 256-thread blocks per SM (5 and 6 spill and measured slower)
 #endif
@@ -934,14 +934,16 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_pt_shade(const __grid_co
 
 // Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
 // counter (warp-aggregated per pass).
-template <int kMinBlocks>
+template <int kMinBlocks, bool kSingle>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* __restrict__ jobs, ExtQ qi, const float4* __restrict__ hits,
                                                      const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
-                                                     int* scount, unsigned int* pass_done) {
+                                                     int* scount, unsigned int* pass_done, const __grid_constant__ JobDev J0) {
     const int n = *qicount;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        const uint32_t job = qi.job[k];
-        const JobDev& J = jobs[job];
+        // kSingle: the batch holds one job, passed by value (its scene tables read through the
+        // parameter space instead of a per-path job-table lookup)
+        const uint32_t job = kSingle ? 0u : qi.job[k];
+        const JobDev& J = kSingle ? J0 : jobs[job];
         const uint2 ids = qi.ids[k];
         const bool alive = shade_path<true>(J.S, J.P, J.film, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
                                             qocount, sq, scount);
@@ -1845,6 +1847,8 @@ struct lmgpu_batch {
         int32_t depth = 0;
         int refill = -1, shade = -1, first_pass = -1;
         bool two_level = false;
+        bool single = false;      // captured for a one-job table, the job passed by value
+        lmgpu::JobDev job{};      // that job
         void clear() {
             if (exec) cudaGraphExecDestroy(exec);
             if (graph) cudaGraphDestroy(graph);
@@ -1902,6 +1906,9 @@ void grow_upload(DevBuf& buf, size_t& cap, size_t& done, const std::vector<T>& v
     done = v.size();
 }
 
+// paths in flight (the queue the next iteration starts from) plus paths not started yet
+__global__ void k_wf_left(int64_t* ctl, const int* qcount) { ctl[4] = int64_t(*qcount) + (ctl[1] - ctl[0]); }
+
 __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
     ctl[1] = total;
     ctl[5] = njobs;
@@ -1912,13 +1919,26 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
     Bvh8 bmax{};
     bmax.depth = b->max_depth;
-    auto ext_k = b->two_level ? k_pt_extend<false, true, true> : k_pt_extend<false, true, false>;
-    auto sh_k = b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>;
+    // one job: the plain trace kernels on its own tree and film, the job by value to shade
+    const bool single = b->host_jobs.size() == 1;
+    JobDev J0{};
+    if (single) J0 = b->host_jobs[0];
+    auto ext_k = single ? (b->two_level ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>)
+                        : (b->two_level ? k_pt_extend<false, true, true> : k_pt_extend<false, true, false>);
+    auto sh_k = single ? (b->two_level ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>)
+                       : (b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>);
     const int g_ext = grid_for(ext_k, kBlock, tsmem);
     const int g_sh = grid_for(sh_k, kBlock, tsmem);
-    auto shade_k = pick_shade(k_wf_shade<2>, k_wf_shade<3>, k_wf_shade<4>, b->shade_minblocks);
+    auto shade_k = single ? pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks)
+                          : pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks);
     const int g_shade = grid_for(shade_k, kBlock, 0);
     const int g_gen = grid_for(k_wf_generate, kBlock, 0);
+    Bvh8 tb = bmax;  // stack sized by the deepest tree seen; single job: its own tree
+    if (single) {
+        tb = J0.S.bvh;
+        tb.depth = b->max_depth;
+    }
+    float* sfilm = single ? J0.film : nullptr;
     int* cnt = ctl_cnt(b);
     const JobDev* jobs = b->jobs.as<JobDev>();
     ExtQ q[2];
@@ -1929,32 +1949,34 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
     float4* hits = b->hits.as<float4>();
     int* fetch = ctl_fetch(b);
     const Fetch f_ext{fetch, fetch + 1, b->refill}, f_sh{fetch + 1, fetch, b->refill};
-    // timed: event record nodes around the kernels, read after each chunk (ev[6*it + k])
+    // timed: event record nodes between the kernels, read after each chunk (ev[6*it + k])
     auto mark = [&](int it, int k) {
         if (timed) LMGPU_CUDA(cudaEventRecordWithFlags(b->ev[6 * it + k], st, cudaEventRecordExternal));
     };
+    // One bounce iteration: top the queue up with new paths (plan, generate), trace it (extend),
+    // shade the hits into the other queue and the shadow queue, trace the shadow rays.
     int cur = 0;
     for (int it = 0; it < kChunkIters; it++) {
         mark(it, 0);
-        ext_k<<<g_ext, kBlock, tsmem, st>>>(bmax, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3,
-                                                               ctl_sums(b), 63, nullptr, f_ext, jobs, q[cur].job);
+        k_wf_plan<<<1, 32, 0, st>>>(ctl64(b), cnt + cur, b->cap, jobs, b->job_next.as<int64_t>(), b->active.as<ActiveJob>(),
+                                    b->alloc.as<AllocEntry>(), b->first_pass);
+        k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->alloc.as<AllocEntry>(), ctl64(b), q[cur], cnt + cur, sq, cnt + 2);
         mark(it, 1);
+        ext_k<<<g_ext, kBlock, tsmem, st>>>(tb, q[cur].o, q[cur].d, cnt + cur, hits, ctl_rays(b), cnt + 3, ctl_sums(b), 63,
+                                            nullptr, f_ext, single ? nullptr : jobs, single ? nullptr : q[cur].job);
+        mark(it, 2);
         LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
         shade_k<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
-                                               b->pass_done.as<unsigned int>());
-        mark(it, 2);
-        sh_k<<<g_sh, kBlock, tsmem, st>>>(bmax, sq, cnt + 2, nullptr, ctl_rays(b) + 1, cnt + 3,
-                                                              ctl_sums(b), 63, nullptr, f_sh, jobs);
+                                            b->pass_done.as<unsigned int>(), J0);
         mark(it, 3);
-        LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
-        k_wf_plan<<<1, 32, 0, st>>>(ctl64(b), cnt + (1 - cur), b->cap, jobs, b->job_next.as<int64_t>(), b->active.as<ActiveJob>(),
-                                    b->alloc.as<AllocEntry>(), b->first_pass);
+        sh_k<<<g_sh, kBlock, tsmem, st>>>(tb, sq, cnt + 2, sfilm, ctl_rays(b) + 1, cnt + 3, ctl_sums(b), 63, nullptr, f_sh,
+                                          single ? nullptr : jobs);
         mark(it, 4);
-        k_wf_generate<<<g_gen, kBlock, 0, st>>>(jobs, b->alloc.as<AllocEntry>(), ctl64(b), q[1 - cur], cnt + (1 - cur), sq,
-                                                cnt + 2);
-        mark(it, 5);
+        LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
         cur = 1 - cur;
     }
+    // exact count of paths in flight or not started, for the host's end-of-chunk check
+    k_wf_left<<<1, 1, 0, st>>>(ctl64(b), cnt + cur);
 }
 
 // The executable graph for the current tuning, depth and timing; recaptured only when one of
@@ -1968,10 +1990,10 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
         b->slot[1].clear();
     }
     auto& g = b->slot[b->timed ? 1 : 0];
-    if (g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
-        g.two_level == b->two_level && g.first_pass == b->first_pass)
-        return g.exec;
-    g.clear();
+    const bool single = b->host_jobs.size() == 1;
+    const bool same_shape = g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
+                            g.two_level == b->two_level && g.first_pass == b->first_pass && g.single == single;
+    if (same_shape && (!single || std::memcmp(&g.job, &b->host_jobs[0], sizeof(JobDev)) == 0)) return g.exec;
     if (b->timed)
         for (auto& e : b->ev)
             if (!e) LMGPU_CUDA(cudaEventCreate(&e));
@@ -1981,8 +2003,12 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
     (void)grid_for(b->two_level ? k_pt_extend<false, true, true> : k_pt_extend<false, true, false>, kBlock, tsmem);
     (void)grid_for(b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>, kBlock, tsmem);
-    (void)grid_for(pick_shade(k_wf_shade<2>, k_wf_shade<3>, k_wf_shade<4>, b->shade_minblocks), kBlock, 0);
+    (void)grid_for(b->two_level ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>, kBlock, tsmem);
+    (void)grid_for(b->two_level ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>, kBlock, tsmem);
+    (void)grid_for(pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks), kBlock, 0);
+    (void)grid_for(pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks), kBlock, 0);
     (void)grid_for(k_wf_generate, kBlock, 0);
+    cudaGraph_t ng = nullptr;
     LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
     try {
         enqueue_chunk(b, cs, b->timed);
@@ -1993,26 +2019,43 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
         cudaStreamDestroy(cs);
         throw;
     }
-    LMGPU_CUDA(cudaStreamEndCapture(cs, &g.graph));
+    LMGPU_CUDA(cudaStreamEndCapture(cs, &ng));
     LMGPU_CUDA(cudaStreamDestroy(cs));
-    LMGPU_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    // only the job changed: the new graph has the same nodes, so update the executable in place
+    bool updated = false;
+    if (same_shape) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(g.exec, ng, &info) == cudaSuccess;
+        if (!updated) (void)cudaGetLastError();
+    }
+    if (updated) {
+        if (g.graph) cudaGraphDestroy(g.graph);
+        g.graph = ng;
+    } else {
+        g.clear();
+        g.graph = ng;
+        LMGPU_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+    }
     g.depth = b->max_depth;
     g.refill = b->refill;
     g.two_level = b->two_level;
     g.first_pass = b->first_pass;
     g.shade = b->shade_minblocks;
+    g.single = single;
+    if (single) g.job = b->host_jobs[0];
     return g.exec;
 }
 
-// Adds one timed chunk's kernel times (events of its last launch) to b->kms.
+// Adds one timed chunk's kernel times (events of its last launch) to b->kms: [0] extend,
+// [1] shade (with the queue-count reset before it), [2] shadow, [3] plan + generate.
 void read_chunk_times(lmgpu_batch* b) {
     for (int it = 0; it < kChunkIters; it++) {
-        float m[5];
-        for (int k = 0; k < 5; k++) LMGPU_CUDA(cudaEventElapsedTime(&m[k], b->ev[6 * it + k], b->ev[6 * it + k + 1]));
-        b->kms[0] += m[0];
-        b->kms[1] += m[1];
-        b->kms[2] += m[2];
-        b->kms[3] += m[3] + m[4];
+        float m[4];
+        for (int k = 0; k < 4; k++) LMGPU_CUDA(cudaEventElapsedTime(&m[k], b->ev[6 * it + k], b->ev[6 * it + k + 1]));
+        b->kms[3] += m[0];
+        b->kms[0] += m[1];
+        b->kms[1] += m[2];
+        b->kms[2] += m[3];
     }
 }
 
