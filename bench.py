@@ -32,7 +32,9 @@ Two more legs (rank 0) report the batched and served forms (keys "batched" and "
 * served -- a Poisson stream of requests over the same scenes (30 % are +16 spp refinements of
   earlier requests) at 80 % of the batched capacity just measured, through RenderServer under a
   150 GB HBM budget; reports p50/p99 time-to-first-image (first complete sample pass) and
-  time-to-done from arrival.
+  time-to-done from arrival, and from each finished image's relative-MSE estimate (even / odd
+  pass accumulators) the time to reach rel-MSE 1e-3 and 1e-2 over the requests whose sample
+  budget reached it, with the fraction that did.
 
 --impl reference times the CPU restatement of the reference's path (fp64 accel::sahbvh +
 renderer::pt with std::mt19937 per thread under OpenMP, all host cores) on a bounded sample of
@@ -452,7 +454,8 @@ def run_served(lm, args, ctx) -> dict:
             "Mrays_per_s": st["rays"] / total / 1e6,
             "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"],
             "done_p50_s": lat["done_p50"], "done_p99_s": lat["done_p99"], "evictions": lat["evictions"],
-            "peak_resident_bytes": srv.peak_resident_bytes}
+            "peak_resident_bytes": srv.peak_resident_bytes,
+            **{k: v for k, v in lat.items() if k.startswith(("rel_mse", "time_to_rel_mse", "reached_rel_mse"))}}
 
 
 def run_served_stress(lm, args, ctx) -> dict:
@@ -524,7 +527,8 @@ def run_served_stress(lm, args, ctx) -> dict:
             "small_done_p99_s": pct([r.done - r.arrival for r in small], 99),
             "evictions": srv.evictions, "scene_builds": srv.scene_builds,
             "scene_build_seconds": srv.scene_build_seconds, "peak_resident_bytes": srv.peak_resident_bytes,
-            "budget_bytes": budget}
+            "budget_bytes": budget,
+            **{k: v for k, v in lat.items() if k.startswith(("rel_mse", "time_to_rel_mse", "reached_rel_mse"))}}
 
 
 def run_instanced(lm, args) -> dict:

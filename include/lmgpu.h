@@ -225,6 +225,13 @@ int lmgpu_film_clear(lmgpu_film* film);
 int lmgpu_film_read(lmgpu_film* film, float* out_rgb);
 /* Device pointer to the h x w x 3 fp32 pixels (valid until the film is destroyed). */
 int lmgpu_film_device_ptr(lmgpu_film* film, void** out);
+/* No reference counterpart. Relative MSE of the film's estimate, from its even- and odd-pass
+ * accumulators (renders with split_passes): per pixel and channel the variance of the mean is
+ * (A - B)^2 * nA * nB / N^2 with A, B the even- and odd-pass means over nA, nB passes and N = nA +
+ * nB, divided by (I^2 + eps) with I the estimate; averaged over pixels and channels. The error of
+ * an N-pass estimate falls as 1/N, so N * rel_mse / target passes reach `target`. Needs at least
+ * one pass in each accumulator. */
+int lmgpu_film_rel_mse(lmgpu_film* film, double eps, double* rel_mse);
 
 /* ---------------------------------------------------------------------------------------------
  * Renderers.
@@ -261,6 +268,11 @@ typedef struct lmgpu_pt_params {
     int32_t accumulate;         /* 1: add to the film; the film's scale becomes 1 / (total spp) */
     int32_t instrument;         /* 1: count node visits / triangle tests on every 64th traced ray;
                                    2: on every traced ray, and record the ray with the most visits */
+    int32_t split_passes;       /* 1 (no reference counterpart): keep even and odd sample passes in two
+                                   accumulators of the film, for lmgpu_film_rel_mse. A film that holds
+                                   split passes keeps splitting the passes later jobs add to it.
+                                   Not with instrument. */
+    int32_t reserved;
 } lmgpu_pt_params;
 
 typedef struct lmgpu_render_stats {

@@ -60,10 +60,14 @@ __device__ inline f3 normalize3(f3 v) { return scale3(v, div(1.0f, __fsqrt_rn(do
 //   key = (seed, 0x6c6d6770), counter = (4*vertex + slot/4, path_lo, path_hi, 0)
 // Slots of one vertex: 0-7 light sample, 8-11 direction, 12 Russian roulette, 13-14 component.
 struct U4 { float v[4]; };
+#ifndef LMGPU_PHILOX_UNROLL
+#define LMGPU_PHILOX_UNROLL 10
+#endif
+constexpr int kPhiloxUnroll = LMGPU_PHILOX_UNROLL;  // rounds unrolled per loop trip (code size vs loop overhead)
 __device__ inline U4 philox_block(uint32_t seed, uint64_t path, uint32_t block) {
     uint32_t c0 = block, c1 = uint32_t(path), c2 = uint32_t(path >> 32), c3 = 0u;
     uint32_t k0 = seed, k1 = 0x6c6d6770u;
-#pragma unroll
+#pragma unroll kPhiloxUnroll
     for (int r = 0; r < 10; r++) {
         const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
         const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);

@@ -72,6 +72,11 @@ struct lmgpu_film {
     lmgpu::DevBuf sum, out;
     double scale = 1.0;
     int64_t accumulated_spp = 0;
+    // split passes (lmgpu_pt_params::split_passes): odd global passes accumulate in sum_odd
+    lmgpu::DevBuf sum_odd;
+    lmgpu::DevBuf mse_acc;  // lmgpu_film_rel_mse's accumulator, allocated once
+    bool split = false;
+    int64_t passes_even = 0, passes_odd = 0;
 };
 
 namespace lmgpu {
@@ -525,19 +530,27 @@ struct JobDev {
     DevScene S;
     PtConst P;
     float* film;
+    float* film_odd;   // split passes: odd global passes splat here (else null)
     int64_t path_begin;
     int64_t npix;
     uint32_t pass_off;
-    uint32_t pad;
+    uint32_t parity0;  // parity of the job's first pass among the film's passes
 };
 
 constexpr int kBlock = 256;
+// Shadow-queue pixel word: bit 31 marks an odd pass of a split-pass film (pixels stay below 2^31).
+constexpr uint32_t kOddPass = 0x80000000u;
 constexpr int64_t kRenderQueue = int64_t(1) << 24;  // paths in flight of lmgpu_render_pt by default
 #ifndef LMGPU_TRACE_MINBLOCKS
 #define LMGPU_TRACE_MINBLOCKS 4  // resident 256-thread blocks per SM (5 and 6 spill and measured slower)
 #endif
 
+#ifndef LMGPU_RNG_LOOP_UNROLL
+#define LMGPU_RNG_LOOP_UNROLL 4
+#endif
+constexpr int kRngLoopUnroll = LMGPU_RNG_LOOP_UNROLL;
 __device__ inline void rng_slots(uint32_t seed, uint64_t path, uint32_t vertex, int first_block, int nblocks, float* u) {
+#pragma unroll kRngLoopUnroll
     for (int b = 0; b < nblocks; b++) {
         const U4 r = philox_block(seed, path, vertex * 4u + uint32_t(first_block + b));
         u[4 * b] = r.v[0]; u[4 * b + 1] = r.v[1]; u[4 * b + 2] = r.v[2]; u[4 * b + 3] = r.v[3];
@@ -581,7 +594,7 @@ __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, c
     if (m == nullptr) {
         float rx, ry;
         if (!raster_pos(S, wo, rx, ry)) return;
-        px = pixel_of(P, rx, ry);
+        px = pixel_of(P, rx, ry) | (pixel & kOddPass);  // the camera vertex keeps the pass bit
         fs = mk(cam_J(S, wo), cam_J(S, wo), cam_J(S, wo));
     } else {
         fs = mat_eval(*m, g, wi, wo, comp, true) * sn_correction(g, wi, wo);
@@ -626,7 +639,7 @@ __device__ inline void push_ext(const ExtQ& q, int* count, f3 o, f3 d, f3 thr, f
 // pixel * spp + sample; `pix` the pixel whose window is sampled.
 template <bool kBatched>
 __device__ __forceinline__ void generate_path(const DevScene& S, const PtConst& P, uint64_t path, int64_t pix, const ExtQ& q,
-                                              int* qcount, const ShadowQ& sq, int* scount, uint32_t job) {
+                                              int* qcount, const ShadowQ& sq, int* scount, uint32_t job, uint32_t odd_bit) {
     float wx = 0.f, wy = 0.f, ww = 1.f, wh = 1.f;
     if (!P.image) {
         const int x = int(pix % P.w), y = int(pix / P.w);
@@ -641,7 +654,7 @@ __device__ __forceinline__ void generate_path(const DevScene& S, const PtConst& 
     const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && P.image;
     float u[16];
     rng_slots(P.seed, path, 1u, 0, 4, u);
-    if (nee_ok) nee<kBatched>(S, P, g, nullptr, mk(0, 0, 0), 0, mk(1, 1, 1), u, 0u, sq, scount, job);
+    if (nee_ok) nee<kBatched>(S, P, g, nullptr, mk(0, 0, 0), 0, mk(1, 1, 1), u, odd_bit, sq, scount, job);
     const f3 d = primary_dir(S, wx + ww * u[8], wy + wh * u[9]);
     float rx = 0.f, ry = 0.f;
     raster_pos(S, d, rx, ry);
@@ -657,7 +670,7 @@ __global__ void __launch_bounds__(kBlock) k_pt_generate(const __grid_constant__ 
                                                         int* scount) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
         const uint64_t path = uint64_t(start + i);
-        generate_path<false>(S, P, path, int64_t(path / uint64_t(P.spp)), q, qcount, sq, scount, 0u);
+        generate_path<false>(S, P, path, int64_t(path / uint64_t(P.spp)), q, qcount, sq, scount, 0u, 0u);
     }
 }
 
@@ -690,7 +703,8 @@ __global__ void __launch_bounds__(kBlock) k_wf_generate(const JobDev* __restrict
         const JobDev& J = jobs[e.job];
         const int64_t local = e.local + (i - e.slot);
         const int64_t sample = local / J.npix, pix = local - sample * J.npix;
-        generate_path<true>(J.S, J.P, uint64_t(pix * J.P.spp + sample), pix, q, qcount, sq, scount, uint32_t(e.job));
+        const uint32_t odd = (J.film_odd && ((uint32_t(sample) + J.parity0) & 1u)) ? kOddPass : 0u;
+        generate_path<true>(J.S, J.P, uint64_t(pix * J.P.spp + sample), pix, q, qcount, sq, scount, uint32_t(e.job), odd);
     }
 }
 
@@ -776,9 +790,15 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_extend(Bvh
 template <bool kCount, bool kBatched = false, bool kTwoLevel = false>
 __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh8 bvh, ShadowQ sq, const int* __restrict__ scount, float* film,
                                                       unsigned long long* rays, int* err, unsigned long long* sums,
-                                                      int count_mask, float* worst, Fetch f, const JobDev* __restrict__ jobs = nullptr) {
+                                                      int count_mask, float* worst, Fetch f, const JobDev* __restrict__ jobs = nullptr,
+                                                      float* film_odd = nullptr) {
     extern __shared__ uint32_t smem[];
     const int n = *scount;
+    // the accumulator of an unoccluded contribution: the pixel word's bit 31 marks an odd pass
+    auto target = [&](uint32_t job, uint32_t pw) -> float* {
+        if (pw & kOddPass) return kBatched ? jobs[job].film_odd : film_odd;
+        return kBatched ? jobs[job].film : film;
+    };
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(rays, (unsigned long long)n);
         if (f.other) *f.other = 0;
@@ -798,7 +818,8 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
             [&](int k, const Trav& s) {
                 if (s.best.id < 0) {
                     const float4 c = sq.c[k];
-                    splat(kBatched ? jobs[sq.job[k]].film : film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+                    const uint32_t pw = __float_as_uint(c.w);
+                    splat(target(kBatched ? sq.job[k] : 0u, pw), pw & ~kOddPass, mk(c.x, c.y, c.z));
                 }
                 if (kCount && (k & count_mask) == 0) {
                     cn += s.nvis;
@@ -826,7 +847,8 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
             }
             if (h.id < 0) {
                 const float4 c = sq.c[k];
-                splat(kBatched ? jobs[job].film : film, __float_as_uint(c.w), mk(c.x, c.y, c.z));
+                const uint32_t pw = __float_as_uint(c.w);
+                splat(target(job, pw), pw & ~kOddPass, mk(c.x, c.y, c.z));
             }
         }
     }
@@ -842,9 +864,16 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
 // ray left vertex nv (flags bits 8-15), then NEE and direction sampling at the new vertex nv+1.
 // Returns false when the path ends here.
 template <bool kBatched>
-__device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, float* film, uint32_t job, float4 o4, float4 d4,
-                                           float4 t4, float4 n4, float4 h4, uint2 ids, const ExtQ& qo, int* qocount,
-                                           const ShadowQ& sq, int* scount) {
+__device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, float* film, float* film_odd, uint32_t parity0,
+                                           uint32_t job, float4 o4, float4 d4, float4 t4, float4 n4, float4 h4, uint2 ids,
+                                           const ExtQ& qo, int* qocount, const ShadowQ& sq, int* scount) {
+    // split passes: the path's pass (sample index) picks the accumulator; NEE carries it in the
+    // shadow entry's pixel word
+    uint32_t odd_bit = 0u;
+    if (film_odd && ((uint32_t(uint64_t(ids.x) % uint64_t(P.spp)) + parity0) & 1u)) {
+        film = film_odd;
+        odd_bit = kOddPass;
+    }
     const uint32_t flags = __float_as_uint(n4.w);
     const int it = int((flags >> 8) & 0xffu);
     const bool prev_nee = flags & 1u;
@@ -911,7 +940,7 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
     const bool spec = mat_specular(m);
     const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && !spec;
     rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
-    if (nee_ok) nee<kBatched>(S, P, g, &m, wi, comp, thr, u, ids.y, sq, scount, job);
+    if (nee_ok) nee<kBatched>(S, P, g, &m, wi, comp, thr, u, ids.y | odd_bit, sq, scount, job);
     f3 wo, w;
     if (!mat_sample(m, g, wi, comp, u[8], u[9], u[10], wo, w)) return false;
     w = w * sn_correction(g, wi, wo);
@@ -929,7 +958,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_pt_shade(const __grid_co
                                                      ExtQ qo, int* qocount, ShadowQ sq, int* scount, float* film) {
     const int n = *qicount;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
-        shade_path<false>(S, P, film, 0u, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], qi.ids[k], qo, qocount, sq, scount);
+        shade_path<false>(S, P, film, nullptr, 0u, 0u, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], qi.ids[k], qo, qocount,
+                          sq, scount);
 }
 
 // Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
@@ -945,7 +975,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* _
         const uint32_t job = kSingle ? 0u : qi.job[k];
         const JobDev& J = kSingle ? J0 : jobs[job];
         const uint2 ids = qi.ids[k];
-        const bool alive = shade_path<true>(J.S, J.P, J.film, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
+        const bool alive = shade_path<true>(J.S, J.P, J.film, J.film_odd, J.parity0, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
                                             qocount, sq, scount);
         if (!alive) {
             const uint32_t key = J.pass_off + uint32_t(uint64_t(ids.x) % uint64_t(J.P.spp));
@@ -1035,6 +1065,26 @@ __global__ void __launch_bounds__(32) k_wf_plan(int64_t* ctl, const int* qcount,
         ctl[0] += slot;
         ctl[4] = inq + (ctl[1] - ctl[0]);
     }
+}
+
+__global__ void k_scale2(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out, int64_t n, float s) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = (a[i] + b[i]) * s;
+}
+
+// Sum over pixels and channels of Var(I) / (I^2 + eps) from the even / odd accumulators (see
+// lmgpu_film_rel_mse); u converts a per-pass sum into the estimate's units.
+__global__ void k_rel_mse(const float* __restrict__ a, const float* __restrict__ b, int64_t n, double na, double nb, double u,
+                          double eps, double* acc) {
+    double s = 0.0;
+    const double N = na + nb;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const double A = double(a[i]) * u / na, B = double(b[i]) * u / nb, I = (double(a[i]) + double(b[i])) * u / N;
+        const double var = (A - B) * (A - B) * na * nb / (N * N);
+        s += var / (I * I + eps);
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
 }
 
 __global__ void k_scale(const float* __restrict__ in, float* __restrict__ out, int64_t n, float s) {
@@ -1412,8 +1462,31 @@ int lmgpu_film_clear(lmgpu_film* f) {
         const size_t n = size_t(f->w) * f->h * 3;
         LMGPU_CUDA(cudaMemset(f->sum.p, 0, n * 4));
         LMGPU_CUDA(cudaMemset(f->out.p, 0, n * 4));
+        if (f->sum_odd.p) LMGPU_CUDA(cudaMemset(f->sum_odd.p, 0, n * 4));
         f->accumulated_spp = 0;
         f->scale = 1.0;
+        f->split = false;
+        f->passes_even = f->passes_odd = 0;
+    });
+}
+
+int lmgpu_film_rel_mse(lmgpu_film* f, double eps, double* rel_mse) {
+    return guarded([&] {
+        if (!f || !rel_mse || !(eps >= 0.0)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid argument");
+        if (!f->split || f->passes_even < 1 || f->passes_odd < 1)
+            throw Error(LMGPU_ERR_UNINITIALIZED, "film has no split passes (render with split_passes and spp >= 2)");
+        const int64_t n = int64_t(f->w) * f->h * 3;
+        const double N = double(f->passes_even + f->passes_odd);
+        DevBuf& acc = f->mse_acc;
+        acc.alloc(sizeof(double));
+        LMGPU_CUDA(cudaMemset(acc.p, 0, sizeof(double)));
+        // f->scale * N: 1 in pixel mode, the pixel count in image mode (renderer_pt.cpp:307-312)
+        k_rel_mse<<<256, 256>>>(f->sum.as<float>(), f->sum_odd.as<float>(), n, double(f->passes_even), double(f->passes_odd),
+                                f->scale * N, eps, acc.as<double>());
+        LMGPU_CUDA(cudaGetLastError());
+        double h = 0.0;
+        LMGPU_CUDA(cudaMemcpy(&h, acc.p, sizeof(double), cudaMemcpyDeviceToHost));
+        *rel_mse = h / double(n);
     });
 }
 
@@ -1554,7 +1627,8 @@ void render_pt_waves(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, 
             LMGPU_CUDA(cudaGetLastError());
             if (P.image) {
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, f_sh, nullptr);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, f_sh, nullptr,
+                                                  nullptr);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
@@ -1572,7 +1646,8 @@ void render_pt_waves(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, 
                                                       cnt + (1 - cur), sq, cnt + 2, film);
                 mark(-1);
                 mark(K_SHADOW);
-                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, f_sh, nullptr);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, sums, cmask, worst, f_sh, nullptr,
+                                                  nullptr);
                 mark(-1);
                 n_sh++;
                 LMGPU_CUDA(cudaGetLastError());
@@ -1644,6 +1719,7 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
         if (prm->instrument) {
+            if (prm->split_passes) throw Error(LMGPU_ERR_UNSUPPORTED, "split_passes with instrument");
             render_pt_waves(s, f, prm, stream, stats);
             return;
         }
@@ -1720,6 +1796,7 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
         if (prm->sampling_mode < 0 || prm->sampling_mode > 2 || prm->primary_mode < 0 || prm->primary_mode > 1)
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown sampling mode");
         if (prm->accumulate) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "lmgpu_render_pt_noalloc does not accumulate (accumulate must be 0)");
+        if (prm->split_passes) throw Error(LMGPU_ERR_UNSUPPORTED, "lmgpu_render_pt_noalloc does not split passes");
         if (prm->wave_paths < 0 || prm->wave_paths > LMGPU_NOALLOC_MAX_WAVE)
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "wave_paths " + std::to_string(prm->wave_paths) +
                                                         " exceeds LMGPU_NOALLOC_MAX_WAVE (" +
@@ -1794,7 +1871,7 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
                                                                                                cnt + 0, sq, cnt + 2);
             if (P.image) {
                 sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr, f_sh,
-                                                  nullptr);
+                                                  nullptr, nullptr);
                 LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
             }
             for (int it = 1; it < P.max_verts; it++) {
@@ -1805,7 +1882,7 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
                 shade_k<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq,
                                                       cnt + 2, d_film);
                 sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, d_film, rays + 1, cnt + 3, sums, 63, nullptr, f_sh,
-                                                  nullptr);
+                                                  nullptr, nullptr);
                 LMGPU_CUDA(cudaGetLastError());
                 cur = 1 - cur;
             }
@@ -1970,7 +2047,7 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
                                             b->pass_done.as<unsigned int>(), J0);
         mark(it, 3);
         sh_k<<<g_sh, kBlock, tsmem, st>>>(tb, sq, cnt + 2, sfilm, ctl_rays(b) + 1, cnt + 3, ctl_sums(b), 63, nullptr, f_sh,
-                                          single ? nullptr : jobs);
+                                          single ? nullptr : jobs, single ? J0.film_odd : nullptr);
         mark(it, 4);
         LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, sizeof(int), st));
         cur = 1 - cur;
@@ -2105,10 +2182,23 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         const int64_t npix = int64_t(f->w) * f->h;
         if (npix * prm->spp > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "more than 2^32 paths in one job");
         if (b->host_jobs.size() >= size_t(1) << 30) throw Error(LMGPU_ERR_UNSUPPORTED, "too many jobs");
+        if (prm->split_passes && prm->instrument) throw Error(LMGPU_ERR_UNSUPPORTED, "split_passes with instrument");
         ensure_film(f);
         if (!prm->accumulate) {
             LMGPU_CUDA(cudaMemset(f->sum.p, 0, size_t(npix) * 3 * 4));
             f->accumulated_spp = 0;
+            f->split = prm->split_passes != 0;
+            f->passes_even = f->passes_odd = 0;
+        } else if (prm->split_passes && !f->split && f->accumulated_spp > 0) {
+            throw Error(LMGPU_ERR_UNSUPPORTED, "split_passes on a film that already holds unsplit passes");
+        } else if (prm->split_passes) {
+            f->split = true;
+        }
+        if (f->split) {
+            if (!f->sum_odd.p || f->accumulated_spp == 0) {
+                f->sum_odd.alloc(size_t(npix) * 3 * 4);
+                LMGPU_CUDA(cudaMemset(f->sum_odd.p, 0, size_t(npix) * 3 * 4));
+            }
         }
         JobDev J{};
         J.S = s->dev;
@@ -2120,6 +2210,14 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         J.P.w = f->w;
         J.P.h = f->h;
         J.film = f->sum.as<float>();
+        J.film_odd = f->split ? f->sum_odd.as<float>() : nullptr;
+        if (f->split) {
+            // the film's global pass index decides the accumulator: even -> sum, odd -> sum_odd
+            const int64_t first = f->passes_even + f->passes_odd;
+            J.parity0 = uint32_t(first & 1);
+            f->passes_odd += (prm->spp + (first & 1)) / 2;
+            f->passes_even += prm->spp - (prm->spp + (first & 1)) / 2;
+        }
         J.path_begin = b->total;
         J.npix = npix;
         J.pass_off = b->passes;
@@ -2239,7 +2337,10 @@ int lmgpu_batch_resolve(lmgpu_batch* b, int32_t job, void* stream) {
         f->accumulated_spp += J.P.spp;
         const double scale = J.P.image ? double(J.npix) / double(f->accumulated_spp) : 1.0 / double(f->accumulated_spp);
         f->scale = scale;
-        k_scale<<<256, 256, 0, st>>>(f->sum.as<float>(), f->out.as<float>(), J.npix * 3, float(scale));
+        if (f->split)
+            k_scale2<<<256, 256, 0, st>>>(f->sum.as<float>(), f->sum_odd.as<float>(), f->out.as<float>(), J.npix * 3, float(scale));
+        else
+            k_scale<<<256, 256, 0, st>>>(f->sum.as<float>(), f->out.as<float>(), J.npix * 3, float(scale));
         LMGPU_CUDA(cudaGetLastError());
         LMGPU_CUDA(cudaStreamSynchronize(st));
     });

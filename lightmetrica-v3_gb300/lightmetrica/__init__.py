@@ -304,6 +304,14 @@ class FilmBitmap(Component):
         """Film::buffer: (h, w, 3) pixels, row 0 at the bottom (film.h:166-171)."""
         return self.buffer_f32().astype(np.float64)
 
+    def rel_mse(self, eps: float = 1e-2) -> float:
+        """Relative MSE of the film's estimate from its even- and odd-pass accumulators (renders
+        with split passes; no reference counterpart): mean over pixels and channels of
+        Var(I) / (I^2 + eps)."""
+        v = C.c_double()
+        N.check(N.lib().lmgpu_film_rel_mse(self._h, float(eps), C.byref(v)))
+        return v.value
+
     def save(self, path: str) -> bool:
         """Film::save (film_bitmap.cpp:156-210): .png (flipped, gamma 1/2.2, 8 bits), .hdr
         (flipped, RGBE), .pfm (unflipped) or .npy; missing parent directories are created."""

@@ -62,7 +62,7 @@ class RaycastParams(C.Structure):
 class PTParams(C.Structure):
     _fields_ = [("spp", C.c_int64), ("max_verts", C.c_int32), ("seed", C.c_uint32), ("sampling_mode", C.c_int32),
                 ("primary_mode", C.c_int32), ("wave_paths", C.c_int64), ("accumulate", C.c_int32),
-                ("instrument", C.c_int32)]
+                ("instrument", C.c_int32), ("split_passes", C.c_int32), ("reserved", C.c_int32)]
 
 
 class RenderStats(C.Structure):
@@ -103,6 +103,7 @@ SIGNATURES = [
     ("lmgpu_film_clear", C.c_int, [C.c_void_p]),
     ("lmgpu_film_read", C.c_int, [C.c_void_p, c_float_p]),
     ("lmgpu_film_device_ptr", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    ("lmgpu_film_rel_mse", C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double)]),
     ("lmgpu_render_raycast", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RaycastParams), C.c_void_p]),
     ("lmgpu_render_pt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.c_void_p, C.POINTER(RenderStats)]),
     ("lmgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int64]),

@@ -32,7 +32,7 @@ _PRIMARY = {"pixel": 0, "image": 1}
 
 
 def _params(spp: int, max_verts: int, seed: int, sampling_mode: str = "mis", primary: str = "pixel",
-            accumulate: bool = False) -> N.PTParams:
+            accumulate: bool = False, split: bool = False) -> N.PTParams:
     p = N.PTParams()
     p.spp = int(spp)
     p.max_verts = int(max_verts)
@@ -40,6 +40,7 @@ def _params(spp: int, max_verts: int, seed: int, sampling_mode: str = "mis", pri
     p.sampling_mode = _MODES[sampling_mode]
     p.primary_mode = _PRIMARY[primary]
     p.accumulate = int(bool(accumulate))
+    p.split_passes = int(bool(split))
     return p
 
 
@@ -64,11 +65,12 @@ class BatchRenderer:
             pass
 
     def submit(self, scene, film, *, max_verts: int, spp: int, seed: int = 0, sampling_mode: str = "mis",
-               primary_ray_sampling_mode: str = "pixel", accumulate: bool = False) -> int:
-        """Queues a renderer::pt job (`scene` built, `film` a film::bitmap); returns its job id."""
+               primary_ray_sampling_mode: str = "pixel", accumulate: bool = False, split: bool = False) -> int:
+        """Queues a renderer::pt job (`scene` built, `film` a film::bitmap); returns its job id.
+        split: even and odd sample passes accumulate apart, for film.rel_mse()."""
         scene._require_built()
         job = C.c_int32()
-        p = _params(spp, max_verts, seed, sampling_mode, primary_ray_sampling_mode, accumulate)
+        p = _params(spp, max_verts, seed, sampling_mode, primary_ray_sampling_mode, accumulate, split)
         N.check(N.lib().lmgpu_batch_submit(self._h, scene._h, film._h, C.byref(p), C.byref(job)))
         self._keep.append((scene, film))
         return job.value
@@ -146,6 +148,9 @@ class Request:
     done: float | None = None
     job: int | None = None
     film: Any = None
+    pass_times: list = None      # completion time of each of its sample passes
+    base_passes: int = 0         # passes the film held before this request (refinements)
+    rel_mse: float | None = None  # estimated relative MSE of the finished image
 
 
 class RenderServer:
@@ -182,6 +187,8 @@ class RenderServer:
         self.scene_builds = 0
         self.scene_build_seconds = 0.0
         self.footprints: dict[Any, int] = {}  # measured device bytes per scene key
+        self.track_error = True               # split passes: each finished image's rel-MSE estimate
+        self.rel_mse_eps = 1e-2
         self._pool = ThreadPoolExecutor(build_threads) if build_threads > 0 else None
         self._building: dict[Any, Any] = {}  # scene key -> future of (scene, build seconds)
         self._film_seq = 0
@@ -261,8 +268,12 @@ class RenderServer:
             accumulate = False
         self.resident_bytes += need
         self.peak_resident_bytes = max(self.peak_resident_bytes, self.resident_bytes)
+        if req.refine is not None:
+            base = self.by_id[req.refine]
+            req.base_passes = base.base_passes + base.spp
+        req.pass_times = []
         req.job = self.batch.submit(scene, req.film, max_verts=req.max_verts, spp=req.spp, seed=req.seed,
-                                    accumulate=accumulate)
+                                    accumulate=accumulate, split=self.track_error)
         req.admitted = self.clock()
         self.scene_users[req.scene_key] = self.scene_users.get(req.scene_key, 0) + 1
         self.scene_last_use[req.scene_key] = req.admitted
@@ -313,9 +324,13 @@ class RenderServer:
             passes, done = self.batch.status(req.job)
             if req.first_image is None and passes >= 1:
                 req.first_image = now
+            if passes > len(req.pass_times):
+                req.pass_times.extend([now] * (passes - len(req.pass_times)))
             if done:
                 self.batch.resolve(req.job)
                 req.done = now
+                if self.track_error and req.base_passes + req.spp >= 2:
+                    req.rel_mse = req.film.rel_mse(self.rel_mse_eps)
                 if req.first_image is None:
                     req.first_image = now
                 self.scene_users[req.scene_key] -= 1
@@ -340,12 +355,42 @@ class RenderServer:
     def idle(self) -> bool:
         return not self.pending and not self.inflight
 
-    def latencies(self) -> dict:
-        """p50/p99 of time-to-first-image and time-to-done, from arrival, in seconds."""
+    @staticmethod
+    def time_to_rel_mse(req: Request, target: float) -> float | None:
+        """Seconds from arrival until the request's image reached relative MSE `target`, or None if
+        its passes never did. The error of an N-pass estimate falls as 1/N, so with the finished
+        image's estimate e over N passes, pass k = ceil(N * e / target) of the film is the first
+        at or below target (0 for a refinement whose base image was already there)."""
+        if req.rel_mse is None or not req.pass_times:
+            return None
+        total = req.base_passes + req.spp
+        k = int(np.ceil(total * req.rel_mse / target - 1e-9))
+        if k > total:
+            return None
+        own = k - req.base_passes
+        if own <= 0:
+            return 0.0
+        return req.pass_times[own - 1] - req.arrival
+
+    def latencies(self, rel_mse_targets=(1e-3, 1e-2)) -> dict:
+        """p50/p99 of time-to-first-image and time-to-done (from arrival, seconds); with error
+        tracking also the finished images' relative MSE and, per target, the time to reach it over
+        the requests that did and the fraction that did."""
         tfi = np.array([r.first_image - r.arrival for r in self.finished])
         ttd = np.array([r.done - r.arrival for r in self.finished])
         if len(ttd) == 0:
             return {}
-        return {"requests": len(ttd), "ttfi_p50": float(np.percentile(tfi, 50)), "ttfi_p99": float(np.percentile(tfi, 99)),
-                "done_p50": float(np.percentile(ttd, 50)), "done_p99": float(np.percentile(ttd, 99)),
-                "evictions": self.evictions}
+        out = {"requests": len(ttd), "ttfi_p50": float(np.percentile(tfi, 50)), "ttfi_p99": float(np.percentile(tfi, 99)),
+               "done_p50": float(np.percentile(ttd, 50)), "done_p99": float(np.percentile(ttd, 99)),
+               "evictions": self.evictions}
+        errs = [r.rel_mse for r in self.finished if r.rel_mse is not None]
+        if errs:
+            out["rel_mse_p50"] = float(np.percentile(errs, 50))
+            out["rel_mse_p99"] = float(np.percentile(errs, 99))
+            for t in rel_mse_targets:
+                ts = [x for x in (self.time_to_rel_mse(r, t) for r in self.finished) if x is not None]
+                key = f"{t:g}"
+                out[f"time_to_rel_mse_{key}_p50"] = float(np.percentile(ts, 50)) if ts else None
+                out[f"time_to_rel_mse_{key}_p99"] = float(np.percentile(ts, 99)) if ts else None
+                out[f"reached_rel_mse_{key}"] = len(ts) / len(self.finished)
+        return out

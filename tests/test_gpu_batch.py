@@ -164,3 +164,37 @@ def test_first_pass_priority(lm, native_lib):
     np.testing.assert_allclose(big_f.buffer_f32(), a_big, **TOL)
     np.testing.assert_allclose(small_f.buffer_f32(), a_small, **TOL)
     b.close()
+
+
+def test_split_passes_estimate_relative_mse(lm):
+    """Even / odd pass accumulators: the image is unchanged, and the relative-MSE estimate agrees
+    with the error against the committed 16k-spp reference and falls as 1/spp."""
+    import json
+    import os
+    from lightmetrica import synthetic as syn
+    from lightmetrica.serving import BatchRenderer
+    gdir = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    ref = np.load(os.path.join(gdir, "box_ref_16k.npy")).astype(np.float64)
+    meta = json.load(open(os.path.join(gdir, "box_ref_16k.json")))
+    s, f = syn.box_scene(seed=1234, w=meta["w"], h=meta["h"], prefix="split_")
+    s.build()
+    plain = _alone(lm, s, f, max_verts=meta["max_verts"], spp=64, seed=5)
+    b = BatchRenderer(queue_paths=1 << 16)
+    est = {}
+    for spp in (16, 64):
+        j = b.submit(s, f, max_verts=meta["max_verts"], spp=spp, seed=5, split=True)
+        b.run(0)
+        b.resolve(j)
+        est[spp] = f.rel_mse(1e-2)
+        if spp == 64:
+            img = f.buffer_f32().astype(np.float64)
+            np.testing.assert_allclose(img, plain, **TOL)
+            true = float(np.mean((img - ref) ** 2 / (ref ** 2 + 1e-2)))
+            assert 0.7 < est[64] / true < 1.4, (est[64], true)
+    assert 2.8 < est[16] / est[64] < 5.7, est      # about 4: error falls as 1/spp
+    # refinement keeps splitting: 64 + 64 passes halve the estimate again
+    j = b.submit(s, f, max_verts=meta["max_verts"], spp=64, seed=6, accumulate=True)
+    b.run(0)
+    b.resolve(j)
+    assert 1.4 < est[64] / f.rel_mse(1e-2) < 2.9
+    b.close()
