@@ -967,13 +967,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_pt_shade(const __grid_co
 template <int kMinBlocks, bool kSingle>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* __restrict__ jobs, ExtQ qi, const float4* __restrict__ hits,
                                                      const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
-                                                     int* scount, unsigned int* pass_done, const __grid_constant__ JobDev J0) {
+                                                     int* scount, unsigned int* pass_done) {
     const int n = *qicount;
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-        // kSingle: the batch holds one job, passed by value (its scene tables read through the
-        // parameter space instead of a per-path job-table lookup)
+        // kSingle: the batch holds one job, so no per-path job id is read
         const uint32_t job = kSingle ? 0u : qi.job[k];
-        const JobDev& J = kSingle ? J0 : jobs[job];
+        const JobDev& J = jobs[job];
         const uint2 ids = qi.ids[k];
         const bool alive = shade_path<true>(J.S, J.P, J.film, J.film_odd, J.parity0, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
                                             qocount, sq, scount);
@@ -1924,8 +1923,10 @@ struct lmgpu_batch {
         int32_t depth = 0;
         int refill = -1, shade = -1, first_pass = -1;
         bool two_level = false;
-        bool single = false;      // captured for a one-job table, the job passed by value
-        lmgpu::JobDev job{};      // that job
+        bool single = false;      // captured for a one-job table
+        lmgpu::Bvh8 bvh{};        // that job's tree and films, passed by value to the trace kernels
+        float* film = nullptr;
+        float* film_odd = nullptr;
         void clear() {
             if (exec) cudaGraphExecDestroy(exec);
             if (graph) cudaGraphDestroy(graph);
@@ -1996,7 +1997,8 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
     Bvh8 bmax{};
     bmax.depth = b->max_depth;
-    // one job: the plain trace kernels on its own tree and film, the job by value to shade
+    // one job: the plain trace kernels on its own tree and film (by value: the captured graph is
+    // keyed on them), no per-path job ids
     const bool single = b->host_jobs.size() == 1;
     JobDev J0{};
     if (single) J0 = b->host_jobs[0];
@@ -2044,7 +2046,7 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
         mark(it, 2);
         LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, sizeof(int), st));
         shade_k<<<g_shade, kBlock, 0, st>>>(jobs, q[cur], hits, cnt + cur, q[1 - cur], cnt + (1 - cur), sq, cnt + 2,
-                                            b->pass_done.as<unsigned int>(), J0);
+                                            b->pass_done.as<unsigned int>());
         mark(it, 3);
         sh_k<<<g_sh, kBlock, tsmem, st>>>(tb, sq, cnt + 2, sfilm, ctl_rays(b) + 1, cnt + 3, ctl_sums(b), 63, nullptr, f_sh,
                                           single ? nullptr : jobs, single ? J0.film_odd : nullptr);
@@ -2070,7 +2072,11 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     const bool single = b->host_jobs.size() == 1;
     const bool same_shape = g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
                             g.two_level == b->two_level && g.first_pass == b->first_pass && g.single == single;
-    if (same_shape && (!single || std::memcmp(&g.job, &b->host_jobs[0], sizeof(JobDev)) == 0)) return g.exec;
+    auto same_job = [&] {
+        const JobDev& J = b->host_jobs[0];
+        return std::memcmp(&g.bvh, &J.S.bvh, sizeof(Bvh8)) == 0 && g.film == J.film && g.film_odd == J.film_odd;
+    };
+    if (same_shape && (!single || same_job())) return g.exec;
     if (b->timed)
         for (auto& e : b->ev)
             if (!e) LMGPU_CUDA(cudaEventCreate(&e));
@@ -2098,7 +2104,8 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     }
     LMGPU_CUDA(cudaStreamEndCapture(cs, &ng));
     LMGPU_CUDA(cudaStreamDestroy(cs));
-    // only the job changed: the new graph has the same nodes, so update the executable in place
+    // only the job's tree or film changed: the new graph has the same nodes, so update the
+    // executable in place
     bool updated = false;
     if (same_shape) {
         cudaGraphExecUpdateResultInfo info;
@@ -2119,7 +2126,11 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     g.first_pass = b->first_pass;
     g.shade = b->shade_minblocks;
     g.single = single;
-    if (single) g.job = b->host_jobs[0];
+    if (single) {
+        g.bvh = b->host_jobs[0].S.bvh;
+        g.film = b->host_jobs[0].film;
+        g.film_odd = b->host_jobs[0].film_odd;
+    }
     return g.exec;
 }
 
