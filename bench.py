@@ -428,7 +428,7 @@ def run_served(lm, args, ctx) -> dict:
     scenes = ctx["scenes"]
     rate = 0.8 * ctx["capacity"]
     reqs = syn.served_requests(args.served_requests, rate=rate, n_scenes=len(scenes))
-    srv = RenderServer(lambda k: scenes[k][0], hbm_budget=150 * 10**9, queue_paths=ctx["queue"], max_inflight=1024)
+    srv = RenderServer(lambda k: scenes[k][0], hbm_budget=150 * 10**9, queue_paths=args.served_queue, max_inflight=1024)
     srv.owns_scenes = False
     t0 = srv.clock()
     i, n = 0, len(reqs)
@@ -447,7 +447,8 @@ def run_served(lm, args, ctx) -> dict:
     lat = srv.latencies()
     st = srv.batch.stats()
     srv.close()
-    return {"workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the batched capacity), "
+    return {"queue_paths": args.served_queue,
+            "workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the batched capacity), "
                         f"{sum(1 for q in reqs if q['refine'] is not None)} refinements (+16 spp), scenes of the "
                         f"batched workload, 150 GB HBM budget",
             "requests": n, "rate_per_s": rate, "seconds": total, "jobs_per_s": n / total,
@@ -493,7 +494,7 @@ def run_served_stress(lm, args, ctx) -> dict:
         s.build()
         return s
     budget = args.stress_budget_mb << 20
-    srv = RenderServer(make_scene, hbm_budget=budget, queue_paths=ctx["queue"], max_inflight=256)
+    srv = RenderServer(make_scene, hbm_budget=budget, queue_paths=args.served_queue, max_inflight=256)
     t0 = srv.clock()
     i, n, released = 0, len(reqs), 0
     while i < n or not srv.idle():
@@ -517,7 +518,8 @@ def run_served_stress(lm, args, ctx) -> dict:
     pct = lambda xs, p: float(np.percentile(xs, p)) if xs else None  # noqa: E731
     st = srv.batch.stats()
     srv.close()
-    return {"workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the measured path throughput for this mix), "
+    return {"queue_paths": args.served_queue,
+            "workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the measured path throughput for this mix), "
                         f"{len(inst)} instanced 4096x2160 jobs (1-4 spp, length 16) among batched-workload jobs on 32 "
                         f"scenes; {args.stress_budget_mb} MB HBM budget; scenes built on admission",
             "requests": n, "seconds": total, "jobs_per_s": n / total, "Mrays_per_s": st["rays"] / total / 1e6,
@@ -603,6 +605,8 @@ def main():
     ap.add_argument("--served-requests", type=int, default=5000, help="0 skips the served leg")
     ap.add_argument("--instanced-spp", type=int, default=4, help="spp of the instanced leg (0 skips it)")
     ap.add_argument("--stress-requests", type=int, default=300, help="requests of the served stress leg (0 skips it)")
+    ap.add_argument("--served-queue", type=int, default=1 << 22,
+                    help="paths in flight of the served legs (smaller than the batched optimum: less queueing delay)")
     ap.add_argument("--stress-budget-mb", type=int, default=1536)
     args = ap.parse_args()
     _apply_overrides(args)

@@ -870,7 +870,7 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
     // split passes: the path's pass (sample index) picks the accumulator; NEE carries it in the
     // shadow entry's pixel word
     uint32_t odd_bit = 0u;
-    if (film_odd && ((uint32_t(uint64_t(ids.x) % uint64_t(P.spp)) + parity0) & 1u)) {
+    if (film_odd && ((ids.x % uint32_t(P.spp) + parity0) & 1u)) {
         film = film_odd;
         odd_bit = kOddPass;
     }
@@ -977,7 +977,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* _
         const bool alive = shade_path<true>(J.S, J.P, J.film, J.film_odd, J.parity0, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
                                             qocount, sq, scount);
         if (!alive) {
-            const uint32_t key = J.pass_off + uint32_t(uint64_t(ids.x) % uint64_t(J.P.spp));
+            const uint32_t key = J.pass_off + ids.x % uint32_t(J.P.spp);
             cg::coalesced_group g = cg::coalesced_threads();
             cg::coalesced_group peers = cg::labeled_partition(g, key);
             if (peers.thread_rank() == 0) atomicAdd(pass_done + key, peers.size());
