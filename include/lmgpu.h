@@ -302,6 +302,30 @@ typedef struct lmgpu_render_stats {
 int lmgpu_render_pt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_pt_params* params, void* stream,
                     lmgpu_render_stats* stats);
 
+/* renderer::lt (src/renderer/renderer_lt.cpp:50-160, light tracing with next-event connections
+ * to the camera) with scheduler::spi::sample (src/scheduler.cpp:114-138): num_samples light paths,
+ * each started from a light chosen uniformly (path::sample_primary_ray(LE), path.h:101-118; an
+ * environment light starts its rays on the disk of the scene's bounding sphere). Every surface
+ * vertex but specular ones connects to the pinhole camera; the film receives the sum over paths
+ * scaled by w*h / (light paths), renderer_lt.cpp:157. Light paths are numbered
+ * [first_path, first_path + num_samples); path p's random numbers are the Philox stream keyed by
+ * (seed, p, vertex), so a render split into calls with consecutive first_path and accumulate
+ * gives the single call's image (no reference counterpart: scheduler::spi::time's rounds). */
+typedef struct lmgpu_lt_params {
+    int64_t num_samples;
+    int64_t first_path;
+    int32_t max_verts;          /* path vertices including the light and the camera vertex */
+    uint32_t seed;
+    int64_t wave_paths;         /* light paths per wave; 0 = 2^22 */
+    int32_t accumulate;         /* 1: add to the film; the scale becomes w*h / (all light paths) */
+    int32_t reserved;
+} lmgpu_lt_params;
+
+/* Renders into `film` on `stream` and waits for it (the replacement of Renderer_LT_NEE::render).
+ * stats may be NULL; stats->paths counts light paths. */
+int lmgpu_render_lt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_lt_params* params, void* stream,
+                    lmgpu_render_stats* stats);
+
 /* ---------------------------------------------------------------------------------------------
  * Shared wavefront for many jobs (no reference counterpart: the reference renders one job at a
  * time). Each job is a built scene, a film and renderer::pt parameters; the paths of every job go

@@ -55,6 +55,10 @@ struct DevScene {
     // world-from-local rows (3), normal-matrix rows (3), {first hit index, first shading record}.
     const float4* inst;
     int32_t num_inst;      // 0: records are in world space, indexed by hit index
+    // bounding sphere of the scene's triangles (scene.cpp:288-311, light_envconst.cpp:38-43): where
+    // light tracing starts the rays of an environment light; radius 0 without triangles
+    f3 bound_c;
+    float bound_r;
 };
 
 }  // namespace lmgpu
@@ -139,6 +143,14 @@ __device__ inline float sn_correction(const Geom& g, f3 wi, f3 wo) {
     const float wi_ng = dot(wi, g.gn), wo_ng = dot(wo, g.gn);
     const float wi_ns = dot(wi, g.n), wo_ns = dot(wo, g.n);
     return (wi_ng * wi_ns <= 0.f || wo_ng * wo_ns <= 0.f) ? 0.f : 1.f;
+}
+
+// surface.h:424-438, transport direction LE: wi.ns wo.ng / (wo.ns wi.ng)
+__device__ inline float sn_correction_le(const Geom& g, f3 wi, f3 wo) {
+    const float wi_ng = dot(wi, g.gn), wo_ng = dot(wo, g.gn);
+    const float wi_ns = dot(wi, g.n), wo_ns = dot(wo, g.n);
+    if (wi_ng * wi_ns <= 0.f || wo_ng * wo_ns <= 0.f) return 0.f;
+    return wi_ns * wo_ng / (wo_ns * wi_ng);
 }
 
 __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float v, int32_t& prim) {
@@ -295,7 +307,8 @@ __device__ inline float mixture_w(const DevMaterial& m) {
     return (wd == 0.f && wg == 0.f) ? 1.f : wd / (wd + wg);
 }
 
-__device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, int comp, bool eval_delta) {
+// le: transport direction LE (light tracing): refraction carries no eta^2 (material_glass.cpp:85-87)
+__device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, int comp, bool eval_delta, bool le = false) {
     switch (m.type) {
     case LMGPU_MAT_DIFFUSE:
         if (opposite(g, wi, wo)) return mk(0, 0, 0);
@@ -311,7 +324,7 @@ __device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo,
         f3 wt; bool total; float eta, Fr;
         glass_fresnel(m, g, wi, wt, total, eta, Fr);
         if (comp == 0) return mk(Fr, Fr, Fr);
-        const float r = (1.f - Fr) * eta * eta;
+        const float r = le ? 1.f - Fr : (1.f - Fr) * eta * eta;
         return mk(r, r, r);
     }
     default:
@@ -336,7 +349,7 @@ __device__ inline float mat_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 w
 // Returns false when no direction is produced (glossy below the surface). uc: the component
 // random number of the direction sample (DirectionSampleU::udc.x), used by the mixture.
 __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, int comp, float u0, float u1, float uc, f3& wo,
-                                  f3& w) {
+                                  f3& w, bool le = false) {
     switch (m.type) {
     case LMGPU_MAT_DIFFUSE:
         wo = diffuse_dir(g, wi, u0, u1);
@@ -365,7 +378,7 @@ __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, in
             glass_fresnel(m, g, wi, wt, total, eta, Fr);
             wo = wt;
         }
-        w = mat_eval(m, g, wi, wo, comp, false);  // pdf of a component direction is 1
+        w = mat_eval(m, g, wi, wo, comp, false, le);  // pdf of a component direction is 1
         return true;
     }
     default:
@@ -478,6 +491,55 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
     const float pL = env_pdf_direct(S, L, g, wo);
     if (pL == 0.f) return false;
     out.weight = env_eval(S, L, wo) / pL / p_sel;
+    return true;
+}
+
+// path::sample_primary_ray(LE), path.h:101-118: a light by u[2], then its sample_ray with
+// u = {up(0,1), upc(2,3), ud(4,5), udc(6,7)}. Area lights (light_area.cpp:78-100): a point as in
+// sample_direct, a cosine-weighted direction about its normal, weight Le / (pA / pi). Environment
+// lights (light_envconst.cpp:47-68, light_env.cpp:86-107): a uniform direction d, a point on the
+// disk of the scene's bounding sphere facing d, weight Le(-d) / (1 / (4 pi) / (pi R^2)). Returns
+// false when nothing can be hit (an environment light in a scene without triangles).
+__device__ inline bool sample_light_ray(const DevScene& S, const float* u, f3& o, f3& d, f3& w) {
+    const int n = S.num_lights;
+    const int li = min(max(int(u[2] * float(n)), 0), n - 1);
+    const float p_sel = 1.f / float(n);
+    const DevLight L = S.lights[li];
+    if (L.type == LMGPU_LIGHT_AREA) {
+        const int ti = cdf_sample(S.cdf + L.cdf_off, L.tri_cnt, u[3]);
+        const float4* tp = S.ltri + size_t(L.tri_off + ti) * 3;
+        const float4 a4 = __ldg(tp), b4 = __ldg(tp + 1), c4 = __ldg(tp + 2);
+        const f3 a = mk(a4.x, a4.y, a4.z), b = mk(a4.w, b4.x, b4.y), c = mk(b4.z, b4.w, c4.x), gn = mk(c4.y, c4.z, c4.w);
+        const float s = sqrtf(fmaxf(0.f, u[0]));
+        const float bu = 1.f - s, bv = u[1] * s;
+        o = a * (1.f - bu - bv) + b * bu + c * bv;
+        f3 tu, tv;
+        onb(gn, tu, tv);
+        const float r = sqrtf(fmaxf(0.f, u[4]));
+        float st, ct;
+        sincosf(2.f * kPi * u[5], &st, &ct);
+        const float x = r * ct, y = r * st;
+        const float z = sqrtf(fmaxf(0.f, 1.f - x * x - y * y));
+        d = tu * x + tv * y + gn * z;
+        const f3 Le = dot(d, gn) <= 0.f ? mk(0, 0, 0) : mk(L.ke[0], L.ke[1], L.ke[2]);
+        w = Le / (L.invA_J * (1.f / kPi)) / p_sel;
+        return true;
+    }
+    if (!(S.bound_r > 0.f)) return false;
+    const float z = 1.f - 2.f * u[4];
+    const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+    float st, ct;
+    sincosf(2.f * kPi * u[5], &st, &ct);
+    d = mk(r * ct, r * st, z);
+    const float rd = sqrtf(fmaxf(0.f, u[0]));
+    float sd, cd;
+    sincosf(2.f * kPi * u[1], &sd, &cd);
+    const float px = rd * cd * S.bound_r, py = rd * sd * S.bound_r;
+    f3 tu, tv;
+    onb(d, tu, tv);
+    o = S.bound_c + (-d) * S.bound_r + (tu * px + tv * py);
+    const float pdf = (1.f / (4.f * kPi)) * (1.f / (kPi * S.bound_r * S.bound_r));
+    w = env_eval(S, L, d) / pdf / p_sel;
     return true;
 }
 
@@ -962,6 +1024,91 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_pt_shade(const __grid_co
                           sq, scount);
 }
 
+// ---------------------------------------------------------------------------------------------
+// renderer::lt (renderer_lt.cpp:50-160) on the same queues: light paths start at a light, every
+// surface vertex connects to the pinhole camera (a shadow ray whose unoccluded contribution
+// lands on the pixel the connection passes through), and the walk continues in transport
+// direction LE. Random numbers: philox keyed (seed, path); vertex 1 slots 0-7 the primary ray;
+// the ray that left vertex k takes its roulette (k > 5) from slot 12 and the hit's component from
+// slots 13-14 of vertex k; vertex k's direction from slots 8-11 (slots 0-7 would be the camera
+// sample, which the pinhole camera does not use).
+
+// Light paths [start, start + count): the primary ray from a sampled light (path = its index).
+__global__ void __launch_bounds__(kBlock) k_lt_generate(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                        int64_t start, int64_t count, ExtQ q, int* qcount) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        const uint64_t path = uint64_t(start + i);
+        float u[8];
+        rng_slots(P.seed, path, 1u, 0, 2, u);
+        f3 o, d, w;
+        if (!sample_light_ray(S, u, o, d, w)) continue;
+        if (is_zero(w)) continue;  // contributes nothing
+        push_ext<false>(q, qcount, o, d, w, 0.f, mk(0, 0, 0), 1u << 8, uint32_t(path), 0u, 0u);
+    }
+}
+
+// One light path after its extension ray: roulette and component at the hit (vertex k + 1), the
+// camera connection of that vertex (camera_pinhole.cpp:178-203: weight J(wo) G; the raster
+// position is tested before the shadow ray is queued), and the next direction.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                     ExtQ qi, const float4* __restrict__ hits, const int* __restrict__ qicount,
+                                                     ExtQ qo, int* qocount, ShadowQ sq, int* scount) {
+    const int n = *qicount;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float4 h4 = hits[k];
+        const int32_t id = __float_as_int(h4.w);
+        if (id < 0) continue;  // no surface (or the environment): the walk ends
+        const float4 d4 = qi.d[k], t4 = qi.thr[k], n4 = qi.nrm[k];
+        const uint2 ids = qi.ids[k];
+        const int it = int((__float_as_uint(n4.w) >> 8) & 0xffu);
+        f3 thr = mk(t4.x, t4.y, t4.z);
+        float u[16];
+        rng_slots(P.seed, ids.x, uint32_t(it), 3, 1, u + 12);
+        if (it > 5) {
+            const float qrr = fmaxf(.2f, 1.f - cmax(thr));
+            if (u[12] < qrr) continue;
+            thr = thr / (1.f - qrr);
+        }
+        int32_t prim;
+        const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+        const DevMaterial m = S.mats[__ldg(S.prim_ml + prim).x];
+        const f3 wi = -mk(d4.x, d4.y, d4.z);
+        int comp = 0;
+        if (m.type == LMGPU_MAT_GLASS) {
+            f3 wt; bool total; float eta, Fr;
+            glass_fresnel(m, g, wi, wt, total, eta, Fr);
+            comp = u[13] < Fr ? 0 : 1;
+            thr = thr * (1.f / (comp == 0 ? Fr : 1.f - Fr));
+        }
+        const int nv = it + 1;
+        if (nv >= P.max_verts) continue;
+        if (!mat_specular(m)) {  // a specular vertex's connection evaluates to 0
+            const f3 wE = normalize(g.p - S.cam_p);
+            float rx, ry;
+            if (raster_pos(S, wE, rx, ry)) {
+                const f3 dc = S.cam_p - g.p;
+                const float L2 = dot(dc, dc);
+                const float len = sqrtf(L2);
+                const float G = fabsf(dot(g.n, dc / len)) / L2;
+                if (G != 0.f) {
+                    const f3 wo = -wE;
+                    const f3 fs = mat_eval(m, g, wi, wo, comp, true, true) * sn_correction_le(g, wi, wo);
+                    const f3 C = thr * fs * (cam_J(S, wE) * G);
+                    if (!is_zero(C)) push_shadow<false>(sq, scount, g.p, normalize(dc), len * (1.f - kEps), C, pixel_of(P, rx, ry), 0u);
+                }
+            }
+        }
+        if (nv + 1 >= P.max_verts) continue;  // the next vertex would not connect
+        rng_slots(P.seed, ids.x, uint32_t(nv), 2, 1, u + 8);
+        f3 wo, w;
+        if (!mat_sample(m, g, wi, comp, u[8], u[9], u[10], wo, w, true)) continue;
+        thr = thr * (w * sn_correction_le(g, wi, wo));
+        if (is_zero(thr)) continue;
+        push_ext<false>(qo, qocount, g.p, wo, thr, 0.f, g.n, uint32_t(nv) << 8, ids.x, 0u, 0u);
+    }
+}
+
 // Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
 // counter (warp-aggregated per pass).
 template <int kMinBlocks, bool kSingle>
@@ -1395,8 +1542,39 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         s->cdf.upload(cdf.data(), cdf.size());
         s->env.upload(env.data(), env.size());
 
+        // scene.cpp:288-311 and light_envconst.cpp:38-43: the bound of every triangle in world space
+        // (two-level scenes: each instance's BLAS triangles moved by its transform), as a sphere
+        // of radius 1.01 |max - center|; only environment lights use it
+        double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+        auto grow = [&](double x, double y, double z) {
+            lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); lo[2] = std::min(lo[2], z);
+            hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y); hi[2] = std::max(hi[2], z);
+        };
+        if (env_light >= 0 && !two_level) {
+            for (int64_t k = 0; k < 3 * nt; k++) grow(D->positions[3 * k], D->positions[3 * k + 1], D->positions[3 * k + 2]);
+        } else if (env_light >= 0) {
+            for (int32_t i = 0; i < accel->num_instances; i++) {
+                const double* M = &accel->inst_xform[size_t(12) * i];
+                const int b = accel->inst_blas[i];
+                for (int64_t k = 3 * accel->blas_offsets[b]; k < 3 * accel->blas_offsets[b + 1]; k++) {
+                    const double x = D->positions[3 * k], y = D->positions[3 * k + 1], z = D->positions[3 * k + 2];
+                    grow(M[0] * x + M[1] * y + M[2] * z + M[3], M[4] * x + M[5] * y + M[6] * z + M[7], M[8] * x + M[9] * y + M[10] * z + M[11]);
+                }
+            }
+        }
+        f3 bound_c = mk(0, 0, 0);
+        float bound_r = 0.f;
+        if (lo[0] <= hi[0]) {
+            const double c[3] = {(hi[0] + lo[0]) * .5, (hi[1] + lo[1]) * .5, (hi[2] + lo[2]) * .5};
+            const double e[3] = {hi[0] - c[0], hi[1] - c[1], hi[2] - c[2]};
+            bound_c = mk(float(c[0]), float(c[1]), float(c[2]));
+            bound_r = float(std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * 1.01);
+        }
+
         DevScene& ds = s->dev;
         ds.bvh = device_view(accel);
+        ds.bound_c = bound_c;
+        ds.bound_r = bound_r;
         ds.shade = s->shade.as<const float4>();
         ds.prim_ml = s->prim_ml.as<const int2>();
         ds.mats = s->mats.as<const DevMaterial>();
@@ -1742,6 +1920,152 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
         must(lmgpu_batch_run(b, 0, stream, &left));
         must(lmgpu_batch_resolve(b, job, stream));
         if (stats) must(lmgpu_batch_get_stats(b, stats));
+    });
+}
+
+int lmgpu_render_lt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_lt_params* prm, void* stream, lmgpu_render_stats* stats) {
+    return guarded([&] {
+        if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
+        if (prm->num_samples <= 0 || prm->max_verts < 1 || prm->first_path < 0)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "num_samples must be > 0, first_path >= 0 and max_verts >= 1");
+        if (prm->max_verts > 255) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 255");
+        if (prm->first_path + prm->num_samples > (int64_t(1) << 32))
+            throw Error(LMGPU_ERR_UNSUPPORTED, "light path index above 2^32");
+        if (prm->accumulate && f->split) throw Error(LMGPU_ERR_UNSUPPORTED, "film holds split passes");
+        ensure_film(f);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int64_t npix = int64_t(f->w) * f->h;
+        const int64_t total = prm->num_samples;
+        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : (int64_t(1) << 22), total);
+        Workspace& ws = workspace(current_device().device);
+        std::lock_guard<std::mutex> ws_lock(ws.m);
+        ensure_queues(ws, wave);
+
+        PtConst P{};
+        P.seed = prm->seed;
+        P.max_verts = prm->max_verts;
+        P.spp = 1;
+        P.w = f->w;
+        P.h = f->h;
+        ExtQ q[2];
+        for (int b = 0; b < 2; b++)
+            q[b] = ExtQ{ws.q_o[b].as<float4>(), ws.q_d[b].as<float4>(), ws.q_thr[b].as<float4>(), ws.q_nrm[b].as<float4>(),
+                        ws.q_ids[b].as<uint2>()};
+        ShadowQ sq{ws.s_o.as<float4>(), ws.s_d.as<float4>(), ws.s_c.as<float4>()};
+        // [0],[1] extension queues, [2] shadow queue, [3] error, [4],[5] extension / shadow ray fetch
+        int* cnt = ws.counters.as<int>();
+        const int refill = tuning().trace_refill;
+        const Fetch f_ext{cnt + 4, cnt + 5, refill}, f_sh{cnt + 5, cnt + 4, refill};
+        unsigned long long* rays = reinterpret_cast<unsigned long long*>(ws.counters.as<char>() + 32);
+        float* film = f->sum.as<float>();
+        const Bvh8 bvh = s->dev.bvh;
+        const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
+        const bool two = s->dev.num_inst > 0;
+        auto ext_k = two ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>;
+        auto sh_k = two ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>;
+        auto shade_k = pick_shade(k_lt_shade<2>, k_lt_shade<3>, k_lt_shade<4>, tuning().shade_minblocks);
+        const int g_gen = grid_for(k_lt_generate, kBlock, 0);
+        const int g_ext = grid_for(ext_k, kBlock, tsmem);
+        const int g_sh = grid_for(sh_k, kBlock, tsmem);
+        const int g_shade = grid_for(shade_k, kBlock, 0);
+
+        enum { K_GEN = 0, K_EXT = 1, K_SHADE = 2, K_SHADOW = 3 };
+        std::vector<std::pair<int, cudaEvent_t>> marks;
+        const bool timed = stats != nullptr;
+        auto mark = [&](int kind) {
+            if (!timed) return;
+            cudaEvent_t e;
+            LMGPU_CUDA(cudaEventCreate(&e));
+            LMGPU_CUDA(cudaEventRecord(e, st));
+            marks.emplace_back(kind, e);
+        };
+        cudaEvent_t e0, e1;
+        LMGPU_CUDA(cudaEventCreate(&e0));
+        LMGPU_CUDA(cudaEventCreate(&e1));
+        int64_t n_ext = 0, n_sh = 0;
+
+        LMGPU_CUDA(cudaEventRecord(e0, st));
+        if (!prm->accumulate) {
+            LMGPU_CUDA(cudaMemsetAsync(film, 0, size_t(npix) * 3 * 4, st));
+            f->accumulated_spp = 0;
+            f->split = false;
+            f->passes_even = f->passes_odd = 0;
+        }
+        LMGPU_CUDA(cudaMemsetAsync(ws.counters.p, 0, 192, st));
+        // a path of max_verts <= 2 vertices cannot reach a camera connection (renderer_lt.cpp:89)
+        for (int64_t start = 0; prm->max_verts > 2 && start < total; start += wave) {
+            const int64_t n = std::min(wave, total - start);
+            int cur = 0;
+            LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
+            LMGPU_CUDA(cudaMemsetAsync(cnt + 4, 0, 8, st));
+            mark(K_GEN);
+            k_lt_generate<<<int(std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock)), kBlock, 0, st>>>(
+                s->dev, P, prm->first_path + start, n, q[0], cnt + 0);
+            mark(-1);
+            LMGPU_CUDA(cudaGetLastError());
+            // the ray that leaves vertex it; its hit connects when it + 1 < max_verts
+            for (int it = 1; it + 1 < P.max_verts; it++) {
+                mark(K_EXT);
+                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, ws.hits.as<float4>(), rays, cnt + 3, nullptr,
+                                                    0, nullptr, f_ext, nullptr, nullptr);
+                mark(-1);
+                n_ext++;
+                LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
+                LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+                mark(K_SHADE);
+                shade_k<<<g_shade, kBlock, 0, st>>>(s->dev, P, q[cur], ws.hits.as<float4>(), cnt + cur, q[1 - cur], cnt + (1 - cur),
+                                                      sq, cnt + 2);
+                mark(-1);
+                mark(K_SHADOW);
+                sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, nullptr, 0, nullptr, f_sh, nullptr,
+                                                  nullptr);
+                mark(-1);
+                n_sh++;
+                LMGPU_CUDA(cudaGetLastError());
+                cur = 1 - cur;
+            }
+        }
+        f->accumulated_spp += total;
+        const double scale = double(npix) / double(f->accumulated_spp);
+        f->scale = scale;
+        k_scale<<<1024, 256, 0, st>>>(film, f->out.as<float>(), npix * 3, float(scale));
+        LMGPU_CUDA(cudaGetLastError());
+        LMGPU_CUDA(cudaEventRecord(e1, st));
+        unsigned long long hr[2];
+        int herr = 0;
+        LMGPU_CUDA(cudaMemcpyAsync(hr, rays, sizeof(hr), cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, 4, cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        LMGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        double kms[4] = {0, 0, 0, 0};
+        for (size_t i = 0; i + 1 < marks.size(); i++) {
+            if (marks[i].first < 0) continue;
+            float m = 0.f;
+            LMGPU_CUDA(cudaEventElapsedTime(&m, marks[i].second, marks[i + 1].second));
+            kms[marks[i].first] += m;
+        }
+        for (auto& e : marks) cudaEventDestroy(e.second);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
+        if (stats) {
+            *stats = lmgpu_render_stats{};
+            stats->paths = total;
+            stats->extension_rays = int64_t(hr[0]);
+            stats->shadow_rays = int64_t(hr[1]);
+            stats->rays = int64_t(hr[0] + hr[1]);
+            stats->elapsed_ms = ms;
+            stats->generate_ms = kms[K_GEN];
+            stats->extend_ms = kms[K_EXT];
+            stats->shade_ms = kms[K_SHADE];
+            stats->shadow_ms = kms[K_SHADOW];
+            stats->trace_ms = kms[K_EXT] + kms[K_SHADOW];
+            stats->extend_launches = n_ext;
+            stats->shadow_launches = n_sh;
+        }
     });
 }
 

@@ -1247,3 +1247,70 @@ class RendererPT(Component):
                            "device_ms": dev_ms, "trace_ms": st.trace_ms}
         return {"processed": processed, "elapsed": elapsed, "rays": rays,
                 "Mrays_per_s": rays / max(dev_ms, 1e-9) / 1e3}
+
+
+@_reg("renderer::lt", "renderer::lt_gpu")
+class RendererLT(Component):
+    """renderer::lt (src/renderer/renderer_lt.cpp:18-160): light tracing with next-event
+    connections to the camera, on the GPU wavefront.
+
+    Props as the reference: scene, output, max_verts, seed, and the scheduler, which for this
+    renderer counts light paths (scheduler::spi::*, src/scheduler.cpp:113-183): 'sample' with
+    num_samples; 'time' with render_time and samples_per_iter (default 100000), rendering rounds
+    of samples_per_iter light paths until the time is spent. The film is rescaled by
+    w*h / (light paths processed). GPU extra: wave_paths (light paths per wave)."""
+
+    def construct(self, prop):
+        self.scene = _resolve(_req(prop, "scene"))
+        self.film = _resolve(_req(prop, "output"))
+        self.max_verts = int(_req(prop, "max_verts"))
+        seed = prop.get("seed")
+        self.seed = int(seed) if seed is not None else int(time.time_ns() & 0xFFFFFFFF)
+        self.scheduler = _req(prop, "scheduler")
+        if self.scheduler == "sample":
+            self.num_samples = int(_req(prop, "num_samples"))
+        elif self.scheduler == "time":
+            self.render_time = float(_req(prop, "render_time"))
+            self.samples_per_iter = int(prop.get("samples_per_iter", 100000))
+        else:
+            raise LmGpuError(1, f"Invalid scheduler '{self.scheduler}'")
+        self.wave_paths = int(prop.get("wave_paths", 0))
+        self.last_stats: dict = {}
+
+    def _params(self, n: int, first: int, accumulate: bool) -> N.LTParams:
+        p = N.LTParams()
+        p.num_samples = n
+        p.first_path = first
+        p.max_verts = self.max_verts
+        p.seed = self.seed & 0xFFFFFFFF
+        p.wave_paths = self.wave_paths
+        p.accumulate = int(accumulate)
+        return p
+
+    def render(self) -> dict:
+        self.scene.require_renderable()
+        self.scene._require_built()
+        t0 = time.perf_counter()
+        st = N.RenderStats()
+        lib = N.lib()
+        if self.scheduler == "sample":
+            N.check(lib.lmgpu_render_lt(self.scene._h, self.film._h, C.byref(self._params(self.num_samples, 0, False)), None,
+                                        C.byref(st)))
+            processed, rays, dev_ms = self.num_samples, st.rays, st.elapsed_ms
+        else:
+            # consecutive light paths per round, so the rounds together are one longer render
+            processed, rays, dev_ms = 0, 0, 0.0
+            while True:
+                N.check(lib.lmgpu_render_lt(self.scene._h, self.film._h,
+                                            C.byref(self._params(self.samples_per_iter, processed, processed > 0)), None,
+                                            C.byref(st)))
+                processed += self.samples_per_iter
+                rays += st.rays
+                dev_ms += st.elapsed_ms
+                if time.perf_counter() - t0 > self.render_time:
+                    break
+        elapsed = time.perf_counter() - t0
+        self.last_stats = {"rays": rays, "extension_rays": st.extension_rays, "shadow_rays": st.shadow_rays,
+                           "device_ms": dev_ms, "trace_ms": st.trace_ms}
+        return {"processed": processed, "elapsed": elapsed, "rays": rays,
+                "Mrays_per_s": rays / max(dev_ms, 1e-9) / 1e3}

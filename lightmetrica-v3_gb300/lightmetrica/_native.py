@@ -65,6 +65,11 @@ class PTParams(C.Structure):
                 ("instrument", C.c_int32), ("split_passes", C.c_int32), ("reserved", C.c_int32)]
 
 
+class LTParams(C.Structure):
+    _fields_ = [("num_samples", C.c_int64), ("first_path", C.c_int64), ("max_verts", C.c_int32), ("seed", C.c_uint32),
+                ("wave_paths", C.c_int64), ("accumulate", C.c_int32), ("reserved", C.c_int32)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("rays", C.c_int64), ("extension_rays", C.c_int64), ("shadow_rays", C.c_int64),
                 ("elapsed_ms", C.c_double), ("trace_ms", C.c_double), ("extend_ms", C.c_double),
@@ -106,6 +111,7 @@ SIGNATURES = [
     ("lmgpu_film_rel_mse", C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_double)]),
     ("lmgpu_render_raycast", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RaycastParams), C.c_void_p]),
     ("lmgpu_render_pt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.c_void_p, C.POINTER(RenderStats)]),
+    ("lmgpu_render_lt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(LTParams), C.c_void_p, C.POINTER(RenderStats)]),
     ("lmgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int64]),
     ("lmgpu_batch_destroy", C.c_int, [C.c_void_p]),
     ("lmgpu_batch_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.POINTER(C.c_int32)]),

@@ -646,6 +646,8 @@ template <typename F> struct Scene {
     std::optional<int> env_light_;
     Accel<F> accel;
     bool built = false;
+    V3<F> sphere_center;   // the lights' scene bound (SphereBound, math.h:184-195)
+    F sphere_radius = 0;
 
     Scene() { reset(); }
     void reset() {
@@ -705,6 +707,21 @@ template <typename F> struct Scene {
                 lights_.push_back({Transform<F>(gm), node.index});
             }
         });
+        // scene.cpp:288-311: the bound of every mesh primitive's transformed triangles, handed to
+        // the lights as a bounding sphere (light_envconst.cpp:38-43)
+        Bound<F> bound;
+        traverse_primitive_nodes([&](const SceneNode<F>& node, const M4<F>& gm) {
+            if (!node.is_primitive || node.mesh < 0) return;
+            const auto& mesh = meshes.at(node.mesh);
+            for (int f = 0; f < mesh.num_triangles(); f++) {
+                const auto tri = mesh.triangle_at(f);
+                bound = merge(bound, xform_point(gm, tri.p1.p));
+                bound = merge(bound, xform_point(gm, tri.p2.p));
+                bound = merge(bound, xform_point(gm, tri.p3.p));
+            }
+        });
+        sphere_center = (bound.max + bound.min) * F(.5);
+        sphere_radius = length(bound.max - sphere_center) * F(1.01);
         accel.robust = robust;
         accel.build([&](std::vector<Tri<F>>& trs, std::vector<typename Accel<F>::Flat>& flat) {
             traverse_primitive_nodes([&](const SceneNode<F>& node, const M4<F>& gm) {
@@ -820,6 +837,40 @@ template <typename F> struct Scene {
         }
         }
         if (s) s->weight = s->weight / p_sel;
+        return s;
+    }
+    // path.h:101-118 sample_primary_ray(LE) with u = {up, upc, ud, udc}: a light by upc.x, then its
+    // sample_ray (light_area.cpp:78-100, light_envconst.cpp:47-68, light_env.cpp:86-107); the
+    // weight is divided by the selection probability. LightSample::wo is the ray direction.
+    std::optional<LightSample<F>> sample_primary_ray_light(const double* u8) const {
+        const V2<F> up{F(u8[0]), F(u8[1])}, upc{F(u8[2]), F(u8[3])}, ud{F(u8[4]), F(u8[5])};
+        const auto [li, p_sel] = sample_light_selection(upc.x);
+        const auto& lpi = lights_.at(li);
+        const auto& L = light_of(lpi.index);
+        LightSample<F> s;
+        if (L.type == LIGHT_AREA) {
+            const auto gL = sample_position_on_triangle_mesh(L, up, upc.y, lpi.tr);
+            const auto pA = L.invA / lpi.tr.J;
+            const auto wl = sample_cosine_weighted(ud);
+            V3<F> u, v;
+            orthonormal_basis(gL.n, u, v);
+            const auto wo = u * wl.x + v * wl.y + gL.n * wl.z;
+            const auto Le = L.eval(gL, wo);
+            const auto p = pA * (F(1) / C<F>::Pi);
+            s = LightSample<F>{gL, wo, Le / p};
+        } else {
+            // a uniform direction, then a point on the disk of the scene's bounding sphere facing it
+            const auto d = sample_uniform_sphere(ud);
+            const auto pl = sample_uniform_disk(up) * sphere_radius;
+            V3<F> u, v;
+            orthonormal_basis(d, u, v);
+            auto gL = PointGeometry<F>::make_infinite(d);
+            gL.p = sphere_center + sphere_radius * (-d) + (u * pl.x + v * pl.y);
+            const auto Le = L.eval(gL, d);
+            const auto p = pdf_uniform_sphere<F>() * (F(1) / (C<F>::Pi * sphere_radius * sphere_radius));
+            s = LightSample<F>{gL, d, Le / p};
+        }
+        s.weight = s.weight / p_sel;
         return s;
     }
     // path.h:563-583 pdf_direct for a light endpoint
@@ -952,6 +1003,8 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
         const long long pixel_index = index / P.spp;
         PathRng rng; rng.mode = P.rng_mode; rng.mt = rngs[tid]; rng.seed = P.seed; rng.path = (uint64_t)index;
         auto U = [&](int nv, int s) -> double { return rng.mode == 0 ? rng.seq() : rng.slot(nv, s); };
+        // two numbers in stream order (the order of a constructor's arguments is unspecified)
+        auto U2 = [&](int nv, int s) { const double a = U(nv, s); const double b = U(nv, s + 1); return V2<F>(F(a), F(b)); };
         long long& nrays = rays[tid];
 
         F wx, wy, ww, wh;
@@ -1019,8 +1072,8 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
                 U(nv, 10); U(nv, 11);
                 s = DirectionSample<F>{cam.primary_ray(ud).d, V3F(F(1))};
             } else {
-                const V2<F> ud(F(U(nv, 8)), F(U(nv, 9)));
-                const V2<F> udc(F(U(nv, 10)), F(U(nv, 11)));
+                const V2<F> ud = U2(nv, 8);
+                const V2<F> udc = U2(nv, 10);
                 const auto& mat = scene.material_of(sp.primitive);
                 const auto ms = mat.sample_direction(ud, udc, sp.geom, wi, comp, TransDir::EL);
                 if (ms) s = DirectionSample<F>{ms->wo, ms->weight * shading_normal_correction(sp.geom, wi, ms->wo, TransDir::EL)};
@@ -1065,7 +1118,7 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
 
             ComponentSample<F> sc{0, F(1)};
             {
-                const V2<F> uc(F(U(nv, 13)), F(U(nv, 14)));
+                const V2<F> uc = U2(nv, 13);
                 if (hit->type == SI_Surface) sc = scene.material_of(hit->primitive).sample_component(uc, hit->geom, -s->wo);
             }
             throughput *= sc.weight;
@@ -1087,6 +1140,122 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
             const auto m = film.m2[i].load();
             out_m2[3 * i] = m.r; out_m2[3 * i + 1] = m.g; out_m2[3 * i + 2] = m.b;
         }
+    }
+    if (rays_out) {
+        long long t = 0;
+        for (auto r : rays) t += r;
+        *rays_out = t;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// src/renderer/renderer_lt.cpp:50-160 (light tracing with NEE to the camera), scheduled as
+// scheduler::spi::sample (src/scheduler.cpp:114-138): light paths [first_path, first_path +
+// num_samples). Philox slots: vertex 1 slots 0-7 the primary ray (up, upc, ud, udc), then as
+// render_pt: the ray that left vertex nv takes its roulette from slot 12 and the component of
+// the vertex it hits from slots 13-14 of vertex nv; vertex nv's camera connection slots 0-7
+// (unused by the pinhole camera) and its direction slots 8-11.
+struct LTParams {
+    int w, h;
+    long long num_samples;
+    long long first_path;
+    int max_verts;
+    unsigned int seed;
+    int rng_mode;
+};
+
+template <typename F>
+void render_lt(const Scene<F>& scene, const LTParams& P, double* out, long long* rays_out, int nthreads) {
+    using V3F = V3<F>;
+    if (scene.nodes.size() <= 1) throw std::runtime_error("Missing primitives.");
+    if (!scene.camera_) throw std::runtime_error("Missing camera primitive.");
+    if (scene.num_lights() == 0) throw std::runtime_error("No light in the scene.");
+    Film film(P.w, P.h, false);
+    const auto& cam = scene.camera();
+    const int nth = std::max(1, nthreads);
+    std::vector<RngMT*> rngs(nth, nullptr);
+    for (int i = 0; i < nth; i++) rngs[i] = new RngMT(P.seed + i, std::is_same<F, float>::value);
+    std::vector<long long> rays(nth, 0);
+
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nth)
+    for (long long index = 0; index < P.num_samples; index++) {
+        const int tid = omp_get_thread_num();
+        PathRng rng; rng.mode = P.rng_mode; rng.mt = rngs[tid]; rng.seed = P.seed; rng.path = (uint64_t)(P.first_path + index);
+        auto U = [&](int nv, int s) -> double { return rng.mode == 0 ? rng.seq() : rng.slot(nv, s); };
+        // two numbers in stream order (the order of a constructor's arguments is unspecified)
+        auto U2 = [&](int nv, int s) { const double a = U(nv, s); const double b = U(nv, s + 1); return V2<F>(F(a), F(b)); };
+        long long& nrays = rays[tid];
+
+        double u8[8];
+        for (int k = 0; k < 8; k++) u8[k] = U(1, k);
+        const auto s0 = scene.sample_primary_ray_light(u8);
+        if (!s0) continue;
+        nrays++;
+        const auto hit0 = scene.intersect(Ray<F>{s0->geom.p, s0->wo});
+        if (!hit0 || hit0->geom.infinite) continue;
+        V3F throughput = s0->weight;
+        auto sample_comp = [&](int nv, const SceneInteraction<F>& sp, V3<F> wi) {
+            const V2<F> uc = U2(nv, 13);
+            return sp.type == SI_Surface ? scene.material_of(sp.primitive).sample_component(uc, sp.geom, wi) : ComponentSample<F>{0, F(1)};
+        };
+        const auto sc0 = sample_comp(1, *hit0, -s0->wo);
+        throughput *= sc0.weight;
+        SceneInteraction<F> sp = *hit0;
+        V3F wi = -s0->wo;
+        int comp = sc0.comp;
+
+        for (int nv = 2; nv < P.max_verts; nv++) {
+            // camera_pinhole.cpp:178-203 sample_direct: the camera point, wo from it toward sp,
+            // weight J(wo) / (1 / G)
+            [&] {
+                for (int k = 0; k < 8; k++) U(nv, k);
+                const auto gE = PointGeometry<F>::make_degenerated(cam.position);
+                const auto wE = normalize(sp.geom.p - cam.position);
+                const F G = geometry_term(sp.geom, gE);
+                const F pE = G == F(0) ? F(0) : F(1) / G;
+                if (pE == F(0)) return;
+                const auto weightE = V3F(cam.J(wE)) / pE;
+                SceneInteraction<F> spE; spE.type = SI_Camera; spE.primitive = *scene.camera_; spE.geom = gE;
+                nrays++;
+                if (!scene.visible(sp, spE)) return;
+                const auto rp = cam.raster_position(wE);
+                if (!rp) return;
+                const auto wo = -wE;
+                const auto fs = scene.material_of(sp.primitive).eval(sp.geom, wi, wo, comp, TransDir::LE, true) *
+                                shading_normal_correction(sp.geom, wi, wo, TransDir::LE);
+                film.splat(*rp, throughput * fs * weightE);
+            }();
+
+            const V2<F> ud = U2(nv, 8);
+            const V2<F> udc = U2(nv, 10);
+            const auto ms = scene.material_of(sp.primitive).sample_direction(ud, udc, sp.geom, wi, comp, TransDir::LE);
+            if (!ms) break;
+            const auto w = ms->weight * shading_normal_correction(sp.geom, wi, ms->wo, TransDir::LE);
+            nrays++;
+            const auto hit = scene.intersect(Ray<F>{sp.geom.p, ms->wo});
+            if (!hit) break;
+            throughput *= w;
+            if (hit->geom.infinite) break;
+            if (nv > 5) {
+                const F q = std::max(F(.2), F(1) - comp_max(throughput));
+                if (F(U(nv, 12)) < q) break;
+                throughput /= F(1) - q;
+            }
+            const auto sc = sample_comp(nv, *hit, -ms->wo);
+            throughput *= sc.weight;
+            wi = -ms->wo;
+            sp = *hit;
+            comp = sc.comp;
+        }
+    }
+
+    for (auto* r : rngs) delete r;
+    // renderer_lt.cpp:157 (rescale by the pixel count over the light paths)
+    const long long num_pixels = (long long)P.w * P.h;
+    const double scale = double(num_pixels) / double(P.num_samples);
+    for (long long i = 0; i < num_pixels; i++) {
+        const auto v = film.data[i].load();
+        out[3 * i] = v.r * scale; out[3 * i + 1] = v.g * scale; out[3 * i + 2] = v.b * scale;
     }
     if (rays_out) {
         long long t = 0;

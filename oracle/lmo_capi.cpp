@@ -260,6 +260,19 @@ int lmo_render_pt(void* p, int w, int hgt, long long spp, int max_verts, unsigne
     });
 }
 
+int lmo_render_lt(void* p, int w, int hgt, long long num_samples, long long first_path, int max_verts, unsigned int seed,
+                  int rng_mode, double* out, long long* rays, int nthreads, double* secs) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        const auto t0 = std::chrono::steady_clock::now();
+        LTParams P{w, hgt, num_samples, first_path, max_verts, seed, rng_mode};
+        render_lt<F>(S, P, out, rays, nthreads > 0 ? nthreads : omp_get_max_threads());
+        if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return 0;
+    });
+}
+
 float lmo_philox_uniform(unsigned int seed, unsigned long long path, unsigned int vertex, unsigned int slot) {
     return philox_uniform(seed, path, vertex, slot);
 }

@@ -7,7 +7,8 @@ import pytest
 def test_registered_keys(lm):
     keys = lm.registered_components()
     for k in ["accel::sahbvh", "accel::nanort", "accel::embree", "accel::embreeinstanced", "accel::gpu",
-              "renderer::pt", "renderer::raycast", "film::bitmap", "camera::pinhole", "mesh::raw",
+              "renderer::pt", "renderer::lt", "renderer::raycast", "film::bitmap", "camera::pinhole", "mesh::raw",
+              "model::wavefrontobj", "material::mixture_wavefrontobj",
               "material::diffuse", "material::glossy", "material::glass", "material::mirror",
               "light::area", "light::envconst", "light::env", "scene::default"]:
         assert k in keys
