@@ -349,6 +349,8 @@ def run_gpu(args) -> None:
                 out["served"] = run_served(lm, args, ctx)
             if args.stress_requests > 0:
                 out["served_stress"] = run_served_stress(lm, args, ctx)
+        if args.lt_paths > 0:
+            out["lt"] = run_lt(lm, scene, film, args)
         if args.instanced_spp > 0:
             out["instanced"] = run_instanced(lm, args)
         print(json.dumps(out))
@@ -572,6 +574,55 @@ def run_instanced(lm, args) -> dict:
             "build_seconds": build_s}
 
 
+def run_lt(lm, scene, film, args) -> dict:
+    """renderer::lt on the headline scene (already built): args.lt_paths light paths per frame,
+    device-timed with CUDA events; end to end through RendererLT.render() + film.buffer(); and the
+    oracle's light tracer (fp64, the reference's std::mt19937 stream) on a bounded sample."""
+    import ctypes as C
+    from lightmetrica import _native as N
+    L = N.lib()
+
+    def frame(seed):
+        p = N.LTParams()
+        p.num_samples, p.first_path, p.max_verts, p.seed = args.lt_paths, 0, MAX_VERTS, seed
+        st = N.RenderStats()
+        N.check(L.lmgpu_render_lt(scene._h, film._h, C.byref(p), None, C.byref(st)))
+        return st
+    frame(1)
+    runs = [frame(200 + k) for k in range(3)]
+    ms = sorted(r.elapsed_ms for r in runs)
+    rays = sum(r.rays for r in runs)
+    value = rays / sum(r.elapsed_ms for r in runs) / 1e3
+    r = lm.load_renderer("lt_bench", "lt", scene=scene, output=film, max_verts=MAX_VERTS, seed=7, scheduler="sample",
+                         num_samples=args.lt_paths)
+    r.render()
+    e2e_rays, e2e_s = 0, 0.0
+    for _ in range(3):
+        t = time.perf_counter()
+        out = r.render()
+        film.buffer_f32()
+        e2e_s += time.perf_counter() - t
+        e2e_rays += out["rays"]
+    res = {"workload": f"renderer::lt on the headline scene ({W_PX}x{H_PX} film), {args.lt_paths} light paths per frame, "
+                       f"max path length {MAX_VERTS - 1}",
+           "Mrays_per_s": value, "ms_per_frame_median": ms[1], "rays_per_frame": rays / len(runs),
+           "extension_rays_per_frame": sum(r.extension_rays for r in runs) / len(runs),
+           "camera_connections_per_frame": sum(r.shadow_rays for r in runs) / len(runs),
+           "kernel_ms_per_frame": {"extend": sum(r.extend_ms for r in runs) / len(runs),
+                                   "shade": sum(r.shade_ms for r in runs) / len(runs),
+                                   "shadow": sum(r.shadow_ms for r in runs) / len(runs),
+                                   "generate": sum(r.generate_ms for r in runs) / len(runs)},
+           "e2e_Mrays_per_s": e2e_rays / e2e_s / 1e6}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        S = cpu_port(scene, 1)
+        n = 1 << 21
+        _, crays, csec = S.render_lt(W_PX, H_PX, n, MAX_VERTS, seed=7, rng="mt19937")
+        res["cpu_baseline"] = {"value": crays / csec / 1e6, "unit": "Mrays/s", "cores": O.max_threads(), "kind": "port",
+                               "sample": f"{n} light paths ({crays} rays, {csec:.1f} s)"}
+    return res
+
+
 def _cudart():
     import ctypes as C
     import glob
@@ -608,6 +659,7 @@ def main():
     ap.add_argument("--served-queue", type=int, default=1 << 22,
                     help="paths in flight of the served legs (smaller than the batched optimum: less queueing delay)")
     ap.add_argument("--stress-budget-mb", type=int, default=1536)
+    ap.add_argument("--lt-paths", type=int, default=1 << 24, help="light paths per frame of the renderer::lt leg (0 skips it)")
     args = ap.parse_args()
     _apply_overrides(args)
     if args.impl == "reference":

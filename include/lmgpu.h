@@ -316,7 +316,8 @@ typedef struct lmgpu_lt_params {
     int64_t first_path;
     int32_t max_verts;          /* path vertices including the light and the camera vertex */
     uint32_t seed;
-    int64_t wave_paths;         /* light paths per wave; 0 = 2^22 */
+    int64_t wave_paths;         /* light paths per wave; 0 = 2^24 (about 230 bytes each, held by the
+                                   device after the first call) */
     int32_t accumulate;         /* 1: add to the film; the scale becomes w*h / (all light paths) */
     int32_t reserved;
 } lmgpu_lt_params;

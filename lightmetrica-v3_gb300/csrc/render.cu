@@ -1938,7 +1938,7 @@ int lmgpu_render_lt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_lt_params* prm, v
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         const int64_t npix = int64_t(f->w) * f->h;
         const int64_t total = prm->num_samples;
-        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : (int64_t(1) << 22), total);
+        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : kRenderQueue, total);
         Workspace& ws = workspace(current_device().device);
         std::lock_guard<std::mutex> ws_lock(ws.m);
         ensure_queues(ws, wave);

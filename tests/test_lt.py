@@ -104,7 +104,7 @@ def test_lt_box_matches_oracle(lm, oracle_mod):
     S.build()
     ref, _, _ = S.render_lt(32, 32, 1 << 20, 8, seed=5)
     assert ref.sum() > 0
-    assert _rel_l1(gpu, ref) < 1e-2, _rel_l1(gpu, ref)
+    assert _rel_l1(gpu, ref) < 1e-3, _rel_l1(gpu, ref)
 
 
 @pytest.mark.gpu
@@ -119,7 +119,7 @@ def test_lt_spheres_env_glass_matches_oracle(lm, oracle_mod):
     S.build()
     ref, _, _ = S.render_lt(32, 24, 1 << 21, 8, seed=9)
     assert ref.sum() > 0
-    assert _rel_l1(gpu, ref) < 2e-2, _rel_l1(gpu, ref)
+    assert _rel_l1(gpu, ref) < 1e-3, _rel_l1(gpu, ref)
 
 
 @pytest.mark.gpu
