@@ -1657,7 +1657,7 @@ int lmgpu_film_rel_mse(lmgpu_film* f, double eps, double* rel_mse) {
         DevBuf& acc = f->mse_acc;
         acc.alloc(sizeof(double));
         LMGPU_CUDA(cudaMemset(acc.p, 0, sizeof(double)));
-        // f->scale * N: 1 in pixel mode, the pixel count in image mode (renderer_pt.cpp:307-312)
+        // f->scale * N = 1: the film is the sum over passes divided by the pass count
         k_rel_mse<<<256, 256>>>(f->sum.as<float>(), f->sum_odd.as<float>(), n, double(f->passes_even), double(f->passes_odd),
                                 f->scale * N, eps, acc.as<double>());
         LMGPU_CUDA(cudaGetLastError());
@@ -1832,7 +1832,8 @@ void render_pt_waves(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, 
             }
         }
         f->accumulated_spp += prm->spp;
-        const double scale = P.image ? double(npix) / double(f->accumulated_spp) : 1.0 / double(f->accumulated_spp);
+        // renderer_pt.cpp:307-312: 1 / spp in pixel mode; w*h / (paths) = 1 / spp in image mode
+        const double scale = 1.0 / double(f->accumulated_spp);
         f->scale = scale;
         k_scale<<<1024, 256, 0, st>>>(film, f->out.as<float>(), npix * 3, float(scale));
         LMGPU_CUDA(cudaEventRecord(e1, st));
@@ -2210,7 +2211,7 @@ int lmgpu_render_pt_noalloc(lmgpu_scene* s, float* d_film, int32_t w, int32_t h,
                 cur = 1 - cur;
             }
         }
-        const double scale = P.image ? double(npix) / double(prm->spp) : 1.0 / double(prm->spp);
+        const double scale = 1.0 / double(prm->spp);  // both primary modes (renderer_pt.cpp:307-312)
         k_scale<<<1024, 256, 0, st>>>(d_film, d_film, npix * 3, float(scale));
         LMGPU_CUDA(cudaGetLastError());
         int herr = 0;
@@ -2670,7 +2671,8 @@ int lmgpu_batch_resolve(lmgpu_batch* b, int32_t job, void* stream) {
         lmgpu_film* f = b->films[job];
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         f->accumulated_spp += J.P.spp;
-        const double scale = J.P.image ? double(J.npix) / double(f->accumulated_spp) : 1.0 / double(f->accumulated_spp);
+        // renderer_pt.cpp:307-312: 1 / spp in pixel mode; w*h / (w*h*spp paths) in image mode
+        const double scale = 1.0 / double(f->accumulated_spp);
         f->scale = scale;
         if (f->split)
             k_scale2<<<256, 256, 0, st>>>(f->sum.as<float>(), f->sum_odd.as<float>(), f->out.as<float>(), J.npix * 3, float(scale));

@@ -19,9 +19,9 @@ functests use to build scenes and render them:
     img = film.buffer()
 
 Every accel key the reference registers (accel::sahbvh, accel::nanort, accel::embree,
-accel::embreeinstanced) and accel::gpu resolve to the GB300 8-wide BVH; renderer::pt and
-renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a missing
-liblmgpu.so raises at the first render or build.
+accel::embreeinstanced) and accel::gpu resolve to the GB300 8-wide BVH; renderer::pt,
+renderer::lt and renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a
+missing liblmgpu.so raises at the first render or build.
 """
 from __future__ import annotations
 
@@ -1199,13 +1199,22 @@ class RendererPT(Component):
             raise LmGpuError(1, f"Invalid primary_ray_sampling_mode '{pm}'")
         self.primary_mode = _PRIMARY[pm]
         self.scheduler = _req(prop, "scheduler")
+        npix = self.film.w * self.film.h
         if self.scheduler == "sample":
-            self.spp = int(_req(prop, "spp"))
+            if self.primary_mode == _PRIMARY["image"] and "num_samples" in prop:
+                # scheduler::spi::sample counts paths (renderer_pt.cpp:71-75); the wavefront takes
+                # whole passes of w*h paths, so num_samples is rounded up to a multiple of w*h
+                self.spp = max(1, -(-int(prop["num_samples"]) // npix))
+            else:
+                self.spp = int(_req(prop, "spp"))
         elif self.scheduler == "time":
             self.render_time = float(_req(prop, "render_time"))
             self.spp_per_round = int(prop.get("spp_per_round", 1))
         else:
             raise LmGpuError(1, f"Invalid scheduler '{self.scheduler}'")
+        # processed samples as the reference's scheduler reports them: passes in pixel mode
+        # (scheduler::spp), paths in image mode (scheduler::spi)
+        self._per_pass = npix if self.primary_mode == _PRIMARY["image"] else 1
         self.wave_paths = int(prop.get("wave_paths", 0))
         self.last_stats: dict = {}
 
@@ -1228,7 +1237,7 @@ class RendererPT(Component):
         if self.scheduler == "sample":
             N.check(N.lib().lmgpu_render_pt(self.scene._h, self.film._h, C.byref(self._params(self.spp, False, self.seed)),
                                             None, C.byref(st)))
-            processed = self.spp
+            processed = self.spp * self._per_pass
             rays, dev_ms = st.rays, st.elapsed_ms
         else:
             processed, rays, dev_ms, k = 0, 0, 0.0, 0
@@ -1236,7 +1245,7 @@ class RendererPT(Component):
                 N.check(N.lib().lmgpu_render_pt(self.scene._h, self.film._h,
                                                 C.byref(self._params(self.spp_per_round, k > 0, self.seed + 7919 * k)),
                                                 None, C.byref(st)))
-                processed += self.spp_per_round
+                processed += self.spp_per_round * self._per_pass
                 rays += st.rays
                 dev_ms += st.elapsed_ms
                 k += 1

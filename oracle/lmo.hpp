@@ -234,6 +234,14 @@ template <typename F> struct Material {
 
     bool is_specular_component(int) const { return type == MAT_GLASS || type == MAT_MIRROR; }
 
+    // material_glass.cpp:143-158 (component sampling on); a single component elsewhere
+    F pdf_component(int comp, const PointGeometry<F>& g, V3<F> wi) const {
+        if (type != MAT_GLASS) return F(1);
+        V3<F> wt; bool total; F eta, Fr;
+        glass_refr(g, wi, wt, total, eta, Fr);
+        return comp == 0 ? Fr : F(1) - Fr;
+    }
+
     ComponentSample<F> sample_component(V2<F> uc, const PointGeometry<F>& g, V3<F> wi) const {
         if (type == MAT_GLASS) {  // material_glass.cpp:123-143 (component sampling on)
             V3<F> wt; bool total; F eta, Fr;
@@ -1132,7 +1140,9 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
 
     for (auto* r : rngs) delete r;
     // renderer_pt.cpp:307-312 (rescale)
-    const double scale = pixel_mode ? 1.0 / double(P.spp) : double(num_pixels) / double(P.spp);
+    // pixel mode: 1 / spp (scheduler::spp); image mode: w*h / (paths processed) with the
+    // w*h*spp paths this loop takes (scheduler::spi), also 1 / spp
+    const double scale = 1.0 / double(P.spp);
     for (long long i = 0; i < num_pixels; i++) {
         const auto v = film.data[i].load();
         out[3 * i] = v.r * scale; out[3 * i + 1] = v.g * scale; out[3 * i + 2] = v.b * scale;
@@ -1251,6 +1261,358 @@ void render_lt(const Scene<F>& scene, const LTParams& P, double* out, long long*
 
     for (auto* r : rngs) delete r;
     // renderer_lt.cpp:157 (rescale by the pixel count over the light paths)
+    const long long num_pixels = (long long)P.w * P.h;
+    const double scale = double(num_pixels) / double(P.num_samples);
+    for (long long i = 0; i < num_pixels; i++) {
+        const auto v = film.data[i].load();
+        out[3 * i] = v.r * scale; out[3 * i + 1] = v.g * scale; out[3 * i + 2] = v.b * scale;
+    }
+    if (rays_out) {
+        long long t = 0;
+        for (auto r : rays) t += r;
+        *rays_out = t;
+    }
+}
+
+// ------------------------------------------------------------------------------------------------
+// Bidirectional path tracing: src/renderer/renderer_bdpt.cpp:297-413 (renderer::bdpt) over the
+// path structure of include/lm/bidir.h. Every function below restates one of bidir.h's in the
+// same order of operations; the vertex and endpoint queries are path.h's dispatch by interaction
+// type. Philox slots: the eye subpath's vertex i draws from "vertex" kBdEye + i and the light
+// subpath's from kBdLight + i: slots 0-7 the primary ray (RaySampleU; the camera uses ud = slots
+// 4-5), slots 8-11 the direction sampled at vertex i, slots 13-14 the component of the vertex hit
+// by the ray that leaves vertex i.
+constexpr int kBdEye = 1;
+constexpr int kBdLight = 129;
+
+template <typename F> struct BdVert {
+    SceneInteraction<F> sp;
+    int comp = 0;
+};
+
+template <typename F> struct Bidir {
+    using V3F = V3<F>;
+    const Scene<F>& scene;
+    explicit Bidir(const Scene<F>& s) : scene(s) {}
+
+    const Camera<F>& cam() const { return scene.camera(); }
+    const Light<F>& light(const SceneInteraction<F>& sp) const { return scene.light_of(sp.primitive); }
+    const Transform<F>& light_tr(const SceneInteraction<F>& sp) const {
+        return scene.lights_.at(scene.light_indices_map_.at(sp.primitive)).tr;
+    }
+
+    // path.h:695-725
+    bool is_specular(const SceneInteraction<F>& sp, int comp) const {
+        if (sp.type == SI_Surface) return scene.material_of(sp.primitive).is_specular_component(comp);
+        return false;  // lights and the pinhole camera are not specular
+    }
+    bool is_connectable(const SceneInteraction<F>& sp) const {
+        if (sp.type == SI_Camera) return true;                   // camera_pinhole.cpp:228-230
+        return light(sp).type == LIGHT_AREA;                     // light_area.cpp:181 / light_env*.cpp
+    }
+    // path.h:761-775 (eval_contrb_direction)
+    V3F eval_dir(const SceneInteraction<F>& sp, V3F wi, V3F wo, int comp, TransDir td, bool eval_delta) const {
+        if (sp.type == SI_Camera) return cam().eval(wo);
+        if (sp.type == SI_Light) return light(sp).eval(sp.geom, wo);
+        return scene.material_of(sp.primitive).eval(sp.geom, wi, wo, comp, td, eval_delta) *
+               shading_normal_correction(sp.geom, wi, wo, td);
+    }
+    // path.h:457-470 (eval_delta false); light_area.cpp:124-129
+    F pdf_dir(const SceneInteraction<F>& sp, V3F wi, V3F wo, int comp) const {
+        if (sp.type == SI_Camera) return cam().pdf_direction(wo);
+        if (sp.type == SI_Light) {
+            if (light(sp).type != LIGHT_AREA) throw std::runtime_error("pdf_direction of an infinite light");
+            return dot(wo, sp.geom.n) <= F(0) ? F(0) : F(1) / C<F>::Pi;
+        }
+        return scene.material_of(sp.primitive).pdf_direction(sp.geom, wi, wo, comp, false);
+    }
+    // path.h:228-234
+    F pdf_comp(const SceneInteraction<F>& sp, V3F wi, int comp) const {
+        return sp.type == SI_Surface ? scene.material_of(sp.primitive).pdf_component(comp, sp.geom, wi) : F(1);
+    }
+    // path.h:327-344 with camera_pinhole.cpp:172 and light_area.cpp:142
+    F pdf_position(const SceneInteraction<F>& sp) const {
+        if (sp.type == SI_Camera) return F(1);
+        const auto& L = light(sp);
+        if (L.type != LIGHT_AREA) throw std::runtime_error("pdf_position of an infinite light");
+        return scene.pdf_light_selection() * (L.invA / light_tr(sp).J);
+    }
+    // path.h:149-162 with camera_pinhole.cpp:142-146, light_area.cpp:102-106,
+    // light_envconst.cpp:70-74 and light_env.cpp:109-113
+    F pdf_primary_ray(const SceneInteraction<F>& sp, V3F wo) const {
+        if (sp.type == SI_Camera) return cam().pdf_direction(wo) * F(1);
+        const auto& L = light(sp);
+        F p;
+        if (L.type == LIGHT_AREA) {
+            p = (L.invA / light_tr(sp).J) * (dot(wo, sp.geom.n) <= F(0) ? F(0) : F(1) / C<F>::Pi);
+        } else {
+            p = pdf_uniform_sphere<F>() * (F(1) / (C<F>::Pi * scene.sphere_radius * scene.sphere_radius));
+        }
+        return scene.pdf_light_selection() * p;
+    }
+
+    // bidir.h:140-155
+    static V3F direction(const BdVert<F>* a, const BdVert<F>* b) {
+        if (!a || !b) return V3F();
+        if (a->sp.geom.infinite) return a->sp.geom.wo;
+        if (b->sp.geom.infinite) return -b->sp.geom.wo;
+        return normalize(b->sp.geom.p - a->sp.geom.p);
+    }
+
+    // bidir.h:507-591 (sample_subpath_from_endpoint); U(vertex, slot) draws a number
+    template <typename Ufn>
+    std::vector<BdVert<F>> sample_subpath(Ufn&& U, int base, int max_verts, TransDir td, long long& nrays) const {
+        std::vector<BdVert<F>> vs;
+        auto U2 = [&](int nv, int k) { const double a = U(nv, k); const double b = U(nv, k + 1); return V2<F>(F(a), F(b)); };
+        if (max_verts == 0) return vs;
+        while (int(vs.size()) < max_verts) {
+            Ray<F> ray;
+            if (vs.empty()) {
+                double u8[8];
+                for (int k = 0; k < 8; k++) u8[k] = U(base, k);
+                SceneInteraction<F> sp;
+                V3F wo;
+                if (td == TransDir::EL) {
+                    sp.type = SI_Camera; sp.primitive = *scene.camera_;
+                    sp.geom = PointGeometry<F>::make_degenerated(cam().position);
+                    wo = cam().primary_ray(V2<F>(F(u8[4]), F(u8[5]))).d;
+                } else {
+                    const auto s = scene.sample_primary_ray_light(u8);
+                    if (!s) break;
+                    // the light chosen by u8[2] (path.h:102-104)
+                    const int li = scene.sample_light_selection(F(u8[2])).first;
+                    sp.type = SI_Light; sp.primitive = scene.lights_.at(li).index;
+                    sp.geom = s->geom;
+                    wo = s->wo;
+                }
+                vs.push_back({sp, 0});
+                ray = Ray<F>{sp.geom.p, wo};
+            } else {
+                const int i = int(vs.size()) - 1;
+                const auto& v = vs[i];
+                const auto wi = direction(&v, i > 0 ? &vs[i - 1] : nullptr);
+                const auto ud = U2(base + i, 8);
+                const auto udc = U2(base + i, 10);
+                const auto ms = scene.material_of(v.sp.primitive).sample_direction(ud, udc, v.sp.geom, wi, v.comp, td);
+                if (!ms) break;
+                ray = Ray<F>{v.sp.geom.p, ms->wo};
+            }
+            nrays++;
+            const auto hit = scene.intersect(ray);
+            if (!hit) break;
+            const auto uc = U2(base + int(vs.size()) - 1, 13);
+            const auto sc = hit->type == SI_Surface ? scene.material_of(hit->primitive).sample_component(uc, hit->geom, -ray.d)
+                                                    : ComponentSample<F>{0, F(1)};
+            vs.push_back({*hit, sc.comp});
+            if (hit->geom.infinite) break;
+        }
+        return vs;
+    }
+
+    // A full path x_0 (light endpoint) .. x_{n-1} (camera endpoint) with its accessors (bidir.h:79-111)
+    struct FullPath {
+        std::vector<BdVert<F>> vs;
+        int n() const { return int(vs.size()); }
+        const BdVert<F>* at(int i, TransDir td) const {
+            if (i < 0 || i >= n()) return nullptr;
+            return &vs[td == TransDir::LE ? i : n() - 1 - i];
+        }
+    };
+
+    // bidir.h:593-643 (connect_subpaths); `visible` counts the connection ray
+    std::optional<FullPath> connect(const std::vector<BdVert<F>>& L, const std::vector<BdVert<F>>& E, int s, int t,
+                                    long long& nrays) const {
+        FullPath P;
+        if (s == 0) {
+            if (E[t - 1].sp.geom.degenerated) return {};
+            for (int i = t - 1; i >= 0; i--) P.vs.push_back(E[i]);
+        } else if (t == 0) {
+            if (L[s - 1].sp.geom.degenerated) return {};
+            for (int i = 0; i < s; i++) P.vs.push_back(L[i]);
+        } else {
+            const auto& vL = L[s - 1];
+            const auto& vE = E[t - 1];
+            if (vL.sp.geom.infinite || vE.sp.geom.infinite) return {};
+            nrays++;
+            if (!scene.visible(vL.sp, vE.sp)) return {};
+            for (int i = 0; i < s; i++) P.vs.push_back(L[i]);
+            for (int i = t - 1; i >= 0; i--) P.vs.push_back(E[i]);
+        }
+        if (!scene.is_light(P.vs.front().sp)) return {};
+        if (P.vs.back().sp.type != SI_Camera) return {};
+        P.vs.front().sp = P.vs.front().sp.as_type(SI_Light);
+        return P;
+    }
+
+    // bidir.h:185-224
+    bool samplable(const FullPath& P, int s) const {
+        const int t = P.n() - s;
+        if (s == 0) {
+            const auto* v = P.at(0, TransDir::LE);
+            return !v->sp.geom.degenerated && !is_specular(v->sp, v->comp);
+        }
+        if (t == 0) {
+            const auto* v = P.at(0, TransDir::EL);
+            return !v->sp.geom.degenerated && !is_specular(v->sp, v->comp);
+        }
+        const auto* vL = P.at(s - 1, TransDir::LE);
+        const auto* vE = P.at(t - 1, TransDir::EL);
+        if (s == 1 && !is_connectable(vL->sp)) return false;
+        if (t == 1 && !is_connectable(vE->sp)) return false;
+        return !is_specular(vL->sp, vL->comp) && !is_specular(vE->sp, vE->comp);
+    }
+
+    // bidir.h:233-275 (eval_subpath_sampling_weight)
+    V3F alpha(const FullPath& P, int l, TransDir td) const {
+        if (l == 0) return V3F(F(1));
+        int i = 0;
+        V3F a(F(0));
+        const auto* v0 = P.at(0, td);
+        if (is_connectable(v0->sp)) {
+            a = V3F(F(1)) / (pdf_position(v0->sp) * pdf_comp(v0->sp, V3F(), v0->comp));
+        } else {
+            const auto* v1 = P.at(1, td);
+            const auto d01 = direction(v0, v1);
+            const auto f = eval_dir(v0->sp, V3F(), d01, v0->comp, td, false);
+            if (is_zero(f)) return V3F(F(0));
+            a = f / (pdf_primary_ray(v0->sp, d01) * pdf_comp(v0->sp, V3F(), v0->comp) * pdf_comp(v1->sp, -d01, v1->comp));
+            i++;
+        }
+        for (; i < l - 1; i++) {
+            const auto* v = P.at(i, td);
+            const auto* vn = P.at(i + 1, td);
+            const auto wi = direction(v, P.at(i - 1, td));
+            const auto wo = direction(v, vn);
+            const auto f = eval_dir(v->sp, wi, wo, v->comp, td, false);
+            if (is_zero(f)) return V3F(F(0));
+            a *= f / pdf_dir(v->sp, wi, wo, v->comp) / pdf_comp(vn->sp, -wo, vn->comp);
+        }
+        return a;
+    }
+
+    // bidir.h:288-313 (eval_connection_term)
+    V3F connection(const FullPath& P, int s) const {
+        const int t = P.n() - s;
+        if (s == 0 && t > 0) {
+            const auto* v = P.at(0, TransDir::LE);
+            return eval_dir(v->sp, V3F(), direction(v, P.at(1, TransDir::LE)), v->comp, TransDir::LE, true);
+        }
+        if (s > 0 && t == 0) {
+            const auto* v = P.at(0, TransDir::EL);
+            return eval_dir(v->sp, V3F(), direction(v, P.at(1, TransDir::EL)), v->comp, TransDir::EL, true);
+        }
+        const auto* vL = P.at(s - 1, TransDir::LE);
+        const auto* vE = P.at(t - 1, TransDir::EL);
+        const auto fL = eval_dir(vL->sp, direction(vL, P.at(s - 2, TransDir::LE)), direction(vL, vE), vL->comp, TransDir::LE, true);
+        const auto fE = eval_dir(vE->sp, direction(vE, P.at(t - 2, TransDir::EL)), direction(vE, vL), vE->comp, TransDir::EL, true);
+        return fL * geometry_term(vL->sp.geom, vE->sp.geom) * fE;
+    }
+
+    // bidir.h:325-343 (eval_sampling_weight_bidir)
+    V3F weight(const FullPath& P, int s) const {
+        const auto aL = alpha(P, s, TransDir::LE);
+        if (is_zero(aL)) return V3F(F(0));
+        const auto aE = alpha(P, P.n() - s, TransDir::EL);
+        if (is_zero(aE)) return V3F(F(0));
+        return aL * connection(P, s) * aE;
+    }
+
+    // bidir.h:397-449 (pdf_bidir)
+    F pdf(const FullPath& P, int s) const {
+        if (!samplable(P, s)) return F(0);
+        auto sub = [&](int l, TransDir td) -> F {
+            if (l == 0) return F(1);
+            int i = 0;
+            F p = F(0);
+            const auto* v0 = P.at(0, td);
+            if (is_connectable(v0->sp)) {
+                p = pdf_position(v0->sp) * pdf_comp(v0->sp, V3F(), v0->comp);
+            } else {
+                const auto* v1 = P.at(1, td);
+                const auto d01 = direction(v0, v1);
+                p = pdf_primary_ray(v0->sp, d01) * geometry_term(v0->sp.geom, v1->sp.geom) * pdf_comp(v0->sp, V3F(), v0->comp) *
+                    pdf_comp(v1->sp, -d01, v1->comp);
+                i++;
+            }
+            for (; i < l - 1; i++) {
+                const auto* v = P.at(i, td);
+                const auto* vn = P.at(i + 1, td);
+                const auto wi = direction(v, P.at(i - 1, td));
+                const auto wo = direction(v, vn);
+                p *= pdf_comp(vn->sp, -wo, vn->comp) * (pdf_dir(v->sp, wi, wo, v->comp) * geometry_term(v->sp.geom, vn->sp.geom));
+            }
+            return p;
+        };
+        return sub(s, TransDir::LE) * sub(P.n() - s, TransDir::EL);
+    }
+
+    // bidir.h:460-479 (power heuristic over every strategy of the path). The reference asserts a
+    // nonzero pdf of the strategy that sampled the path; a zero one contributes nothing here.
+    F mis(const FullPath& P, int s) const {
+        const F ps = pdf(P, s);
+        if (ps == F(0)) return F(0);
+        F inv = F(0);
+        for (int s2 = 0; s2 <= P.n(); s2++) {
+            const F pi = pdf(P, s2);
+            if (pi == F(0)) continue;
+            const F r = pi / ps;
+            inv += r * r;
+        }
+        return F(1) / inv;
+    }
+};
+
+struct BDPTParams {
+    int w, h;
+    long long num_samples;
+    long long first_path;
+    int min_verts, max_verts;
+    unsigned int seed;
+    int rng_mode;
+};
+
+template <typename F>
+void render_bdpt(const Scene<F>& scene, const BDPTParams& P, double* out, long long* rays_out, int nthreads) {
+    using V3F = V3<F>;
+    if (scene.nodes.size() <= 1) throw std::runtime_error("Missing primitives.");
+    if (!scene.camera_) throw std::runtime_error("Missing camera primitive.");
+    if (scene.num_lights() == 0) throw std::runtime_error("No light in the scene.");
+    Film film(P.w, P.h, false);
+    const Bidir<F> B(scene);
+    const int nth = std::max(1, nthreads);
+    std::vector<RngMT*> rngs(nth, nullptr);
+    for (int i = 0; i < nth; i++) rngs[i] = new RngMT(P.seed + i, std::is_same<F, float>::value);
+    std::vector<long long> rays(nth, 0);
+
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nth)
+    for (long long index = 0; index < P.num_samples; index++) {
+        const int tid = omp_get_thread_num();
+        PathRng rng; rng.mode = P.rng_mode; rng.mt = rngs[tid]; rng.seed = P.seed; rng.path = (uint64_t)(P.first_path + index);
+        auto U = [&](int nv, int s) -> double { return rng.mode == 0 ? rng.seq() : rng.slot(nv, s); };
+        long long& nrays = rays[tid];
+        const auto E = B.sample_subpath(U, kBdEye, P.max_verts, TransDir::EL, nrays);
+        const auto L = B.sample_subpath(U, kBdLight, P.max_verts, TransDir::LE, nrays);
+        const int nE = int(E.size()), nL = int(L.size());
+        for (int s = 0; s <= nL; s++) {
+            for (int t = 0; t <= nE; t++) {
+                const int k = s + t;
+                if (k < P.min_verts || P.max_verts < k) continue;
+                const auto path = B.connect(L, E, s, t, nrays);
+                if (!path) continue;
+                const auto Cu = B.weight(*path, s);
+                if (is_zero(Cu)) continue;
+                const F w = B.mis(*path, s);
+                // bidir.h:167-171: the raster position of the camera's first edge
+                const auto* vE = path->at(0, TransDir::EL);
+                const auto rp = scene.camera().raster_position(Bidir<F>::direction(vE, path->at(1, TransDir::EL)));
+                if (!rp) continue;  // the reference dereferences it unchecked; only rounding reaches here
+                film.splat(*rp, w * Cu);
+            }
+        }
+    }
+
+    for (auto* r : rngs) delete r;
+    // renderer_bdpt.cpp:397-399
     const long long num_pixels = (long long)P.w * P.h;
     const double scale = double(num_pixels) / double(P.num_samples);
     for (long long i = 0; i < num_pixels; i++) {

@@ -56,6 +56,8 @@ def lib() -> C.CDLL:
                                     dp, dp, C.POINTER(C.c_longlong), C.c_int, dp]
         L.lmo_render_lt.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int, C.c_uint, C.c_int, dp,
                                     C.POINTER(C.c_longlong), C.c_int, dp]
+        L.lmo_render_bdpt.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int, C.c_int, C.c_uint, C.c_int,
+                                      dp, C.POINTER(C.c_longlong), C.c_int, dp]
         L.lmo_philox_uniform.restype = C.c_float
         L.lmo_philox_uniform.argtypes = [C.c_uint, C.c_ulonglong, C.c_uint, C.c_uint]
         L.lmo_max_threads.restype = C.c_int
@@ -204,6 +206,18 @@ class OracleScene:
         rm = {"mt19937": 0, "philox": 1}[rng]
         _chk(lib().lmo_render_lt(self.h, w, h, num_samples, first_path, max_verts, seed & 0xFFFFFFFF, rm,
                                  out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(rays), nthreads, C.byref(s)))
+        return out, rays.value, s.value
+
+
+    def render_bdpt(self, w, h, num_samples, max_verts, seed=0, min_verts=2, first_path=0, rng="philox", nthreads: int = 0):
+        """renderer::bdpt: returns (image (h,w,3) scaled by w*h / num_samples, rays, seconds) for samples
+        [first_path, first_path + num_samples), each one eye and one light subpath."""
+        out = np.zeros((h, w, 3))
+        rays = C.c_longlong()
+        s = C.c_double()
+        rm = {"mt19937": 0, "philox": 1}[rng]
+        _chk(lib().lmo_render_bdpt(self.h, w, h, num_samples, first_path, min_verts, max_verts, seed & 0xFFFFFFFF, rm,
+                                   out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(rays), nthreads, C.byref(s)))
         return out, rays.value, s.value
 
 

@@ -160,3 +160,15 @@ def test_sampling_modes_agree_in_expectation(oracle_mod, lm):
         means[mode] = img.mean()
     assert abs(means["nee"] - means["mis"]) / means["mis"] < 0.03, means
     assert abs(means["naive"] - means["mis"]) / means["mis"] < 0.08, means
+
+
+def test_primary_modes_agree_in_expectation(oracle_mod, lm):
+    """Pixel and image primary-ray sampling estimate the same image: image mode's w*h*spp paths are
+    rescaled by w*h / (paths) (renderer_pt.cpp:307-312 with scheduler::spi), i.e. by 1 / spp."""
+    from lightmetrica import synthetic as syn
+    scene, film = syn.box_scene(w=8, h=8)
+    S = oracle_mod.from_lm_scene(scene, double=True)
+    S.build()
+    pix, _, _, _ = S.render_pt(8, 8, 512, 9, seed=11, rng="philox")
+    img, _, _, _ = S.render_pt(8, 8, 512, 9, seed=11, primary_mode="image", rng="philox")
+    assert abs(img.mean() / pix.mean() - 1) < 0.03, (img.mean(), pix.mean())
