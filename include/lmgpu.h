@@ -327,6 +327,29 @@ typedef struct lmgpu_lt_params {
 int lmgpu_render_lt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_lt_params* params, void* stream,
                     lmgpu_render_stats* stats);
 
+/* renderer::bdpt (src/renderer/renderer_bdpt.cpp:297-413 over include/lm/bidir.h) with
+ * scheduler::spi::sample: num_samples samples, each one eye subpath (a primary ray over the whole
+ * image) and one light subpath of up to max_verts vertices, combined by every strategy (s light
+ * vertices, t eye vertices, min_verts <= s + t <= max_verts) with the power-heuristic weight of
+ * bidir.h:460-479; the film is scaled by w*h / (samples), renderer_bdpt.cpp:397-399. Sample p's
+ * random numbers are the Philox stream keyed by (seed, p, subpath vertex), so consecutive calls
+ * with first_path and accumulate add up to one render. A strategy whose own pdf is 0 contributes
+ * nothing (the reference asserts it is not 0). */
+typedef struct lmgpu_bdpt_params {
+    int64_t num_samples;
+    int64_t first_path;
+    int32_t min_verts;          /* the reference's default is 2 */
+    int32_t max_verts;          /* 2..64 */
+    uint32_t seed;
+    int32_t accumulate;
+    int64_t wave_paths;         /* samples per wave; 0 = 2^20, or fewer so that the connection queue holds
+                                   at most 2^28 rays. Each sample of a wave takes 2 * max_verts * 64 bytes of
+                                   vertex records and max_verts * (max_verts - 1) / 2 * 48 bytes of queue. */
+} lmgpu_bdpt_params;
+
+int lmgpu_render_bdpt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_bdpt_params* params, void* stream,
+                      lmgpu_render_stats* stats);
+
 /* ---------------------------------------------------------------------------------------------
  * Shared wavefront for many jobs (no reference counterpart: the reference renders one job at a
  * time). Each job is a built scene, a film and renderer::pt parameters; the paths of every job go

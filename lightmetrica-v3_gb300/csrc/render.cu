@@ -499,12 +499,15 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
 // sample_direct, a cosine-weighted direction about its normal, weight Le / (pA / pi). Environment
 // lights (light_envconst.cpp:47-68, light_env.cpp:86-107): a uniform direction d, a point on the
 // disk of the scene's bounding sphere facing d, weight Le(-d) / (1 / (4 pi) / (pi R^2)). Returns
-// false when nothing can be hit (an environment light in a scene without triangles).
-__device__ inline bool sample_light_ray(const DevScene& S, const float* u, f3& o, f3& d, f3& w) {
+// false when nothing can be hit (an environment light in a scene without triangles). li_out: the
+// light chosen; n_out: an area light's normal at the sampled point.
+__device__ inline bool sample_light_ray(const DevScene& S, const float* u, f3& o, f3& d, f3& w, int* li_out = nullptr,
+                                        f3* n_out = nullptr) {
     const int n = S.num_lights;
     const int li = min(max(int(u[2] * float(n)), 0), n - 1);
     const float p_sel = 1.f / float(n);
     const DevLight L = S.lights[li];
+    if (li_out) *li_out = li;
     if (L.type == LMGPU_LIGHT_AREA) {
         const int ti = cdf_sample(S.cdf + L.cdf_off, L.tri_cnt, u[3]);
         const float4* tp = S.ltri + size_t(L.tri_off + ti) * 3;
@@ -521,6 +524,7 @@ __device__ inline bool sample_light_ray(const DevScene& S, const float* u, f3& o
         const float x = r * ct, y = r * st;
         const float z = sqrtf(fmaxf(0.f, 1.f - x * x - y * y));
         d = tu * x + tv * y + gn * z;
+        if (n_out) *n_out = gn;
         const f3 Le = dot(d, gn) <= 0.f ? mk(0, 0, 0) : mk(L.ke[0], L.ke[1], L.ke[2]);
         w = Le / (L.invA_J * (1.f / kPi)) / p_sel;
         return true;
@@ -1109,6 +1113,406 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_co
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// renderer::bdpt (renderer_bdpt.cpp:297-413 over include/lm/bidir.h): per sample one eye and one
+// light subpath, then every strategy (s light vertices, t eye vertices) with its power-heuristic
+// weight. Subpaths are traced on the shared extend kernel (eye and light rays in one queue) and
+// their vertices kept in records; k_bd_connect evaluates the strategies, queues one visibility
+// ray per connection (s, t >= 1) for k_pt_shadow and splats s = 0 directly.
+// The weight is the reference's (bidir.h:460-479: 1 / sum over strategies s' of (p_s' / p_s)^2
+// with pdf_bidir, bidir.h:397-449). p_s' is a product over the path's vertices of their local
+// pdfs, sampled from the light side (qL) for the first s' vertices and from the eye side (qE)
+// for the rest, so p_{s'+1} / p_s' = qL(s') / qE(s'). Each vertex keeps the local pdf of the
+// direction its subpath sampled it from (qf) and the factors of the opposite direction that its
+// subpath already fixes (pc_out, prev_rev, G); a strategy evaluates only the four local pdfs next
+// to its connection and sweeps the ratios: O(n) per strategy instead of O(n^2).
+// Philox: eye vertex i draws from "vertex" kBdEyeBase + i, light vertex i from kBdLightBase + i;
+// slots 0-7 the primary ray (the camera uses 4-5), 8-11 the direction sampled at the vertex,
+// 13-14 the component of the vertex the ray that leaves it hits.
+constexpr uint32_t kBdEyeBase = 1, kBdLightBase = 129;
+constexpr int kBdMaxVerts = 64;
+enum : uint32_t { kBdSurface = 0, kBdCamera = 1, kBdArea = 2, kBdInfinite = 3 };
+// ext-queue flags of the BDPT subpaths: bits 8-15 the vertex the ray leaves, then these
+constexpr uint32_t kBdLightSub = 1u << 16, kBdInfOrigin = 1u << 17, kBdDegOrigin = 1u << 18;
+
+// A subpath vertex. p: position (an infinite vertex: its direction wo, surface.h:90-110);
+// a: the subpath weight of the vertices before it (eval_subpath_sampling_weight, bidir.h:233-275)
+// without its own component pdf pc. qf: pc * pdf_direction(previous vertex) * G(previous, this),
+// the local pdf its subpath sampled it with (the endpoints: pdf_position, or 1). pc_out: the
+// component pdf toward the next vertex of the subpath; prev_rev: pdf_direction of this vertex
+// toward the previous one given the next one, times G(previous, this); G: that geometry term.
+struct BdVtx {
+    f3 p, n, gn, a;
+    uint32_t kind, comp;
+    int32_t light, mat;
+    float pc, qf, pc_out, prev_rev, G;
+    bool spec;
+};
+// Records: 5 float4 per vertex, [subpath][vertex][sample] so that consecutive samples read
+// consecutive records. r4 alone carries what the weight sweep reads (the sign of pc_out marks a
+// specular vertex). nv: vertices per subpath, [subpath][sample].
+struct BdRec {
+    float4* r;
+    int32_t* nv;
+    int64_t W;
+    int32_t mv;
+};
+constexpr int kBdRecWords = 5;
+__device__ inline size_t bd_at(const BdRec& R, int sub, int j, int64_t k) {
+    return ((size_t(sub) * R.mv + j) * size_t(R.W) + k) * kBdRecWords;
+}
+__device__ inline void bd_store(const BdRec& R, int sub, int j, int64_t k, const BdVtx& v) {
+    float4* q = R.r + bd_at(R, sub, j, k);
+    const uint32_t word = v.kind | (v.comp << 4) | (uint32_t(v.light + 1) << 8);
+    q[0] = make_float4(v.p.x, v.p.y, v.p.z, __uint_as_float(word));
+    q[1] = make_float4(v.n.x, v.n.y, v.n.z, __int_as_float(v.mat));
+    q[2] = make_float4(v.gn.x, v.gn.y, v.gn.z, v.pc);
+    q[3] = make_float4(v.a.x, v.a.y, v.a.z, 0.f);
+    q[4] = make_float4(v.qf, v.spec ? -v.pc_out : v.pc_out, v.prev_rev, v.G);
+}
+// the direction-sampling part of a vertex, written once its next direction is known
+__device__ inline void bd_store_out(const BdRec& R, int sub, int j, int64_t k, const BdVtx& v) {
+    R.r[bd_at(R, sub, j, k) + 4] = make_float4(v.qf, v.spec ? -v.pc_out : v.pc_out, v.prev_rev, v.G);
+}
+__device__ inline BdVtx bd_load(const BdRec& R, int sub, int j, int64_t k) {
+    const float4* q = R.r + bd_at(R, sub, j, k);
+    const float4 r0 = q[0], r1 = q[1], r2 = q[2], r3 = q[3], r4 = q[4];
+    BdVtx v;
+    const uint32_t word = __float_as_uint(r0.w);
+    v.p = mk(r0.x, r0.y, r0.z);
+    v.kind = word & 3u;
+    v.comp = (word >> 4) & 15u;
+    v.light = int32_t(word >> 8) - 1;
+    v.n = mk(r1.x, r1.y, r1.z);
+    v.mat = __float_as_int(r1.w);
+    v.gn = mk(r2.x, r2.y, r2.z);
+    v.pc = r2.w;
+    v.a = mk(r3.x, r3.y, r3.z);
+    v.qf = r4.x;
+    v.pc_out = fabsf(r4.y);
+    v.spec = signbit(r4.y);
+    v.prev_rev = r4.z;
+    v.G = r4.w;
+    return v;
+}
+__device__ inline float4 bd_pdfs(const BdRec& R, int sub, int j, int64_t k) { return R.r[bd_at(R, sub, j, k) + 4]; }
+// bidir.h:140-155: the direction from `from` toward record j (an infinite vertex: back along its wo)
+__device__ inline f3 bd_toward(const BdRec& R, int sub, int j, int64_t k, f3 from) {
+    const float4 r0 = R.r[bd_at(R, sub, j, k)];
+    if ((__float_as_uint(r0.w) & 3u) == kBdInfinite) return -mk(r0.x, r0.y, r0.z);
+    return normalize(mk(r0.x, r0.y, r0.z) - from);
+}
+__device__ inline Geom bd_geom(const BdVtx& v) { return on_surface(v.p, v.n, v.gn); }
+// path.h:228-234 with material_glass.cpp:143-158
+__device__ inline float bd_pcomp(const DevMaterial& m, const Geom& g, int comp, f3 wi) {
+    if (m.type != LMGPU_MAT_GLASS) return 1.f;
+    f3 wt; bool total; float eta, Fr;
+    glass_fresnel(m, g, wi, wt, total, eta, Fr);
+    return comp == 0 ? Fr : 1.f - Fr;
+}
+// pdf_primary_ray of an environment light (light_envconst.cpp:70-74), selection included
+__device__ inline float bd_env_pray(const DevScene& S) {
+    return (1.f / float(S.num_lights)) * (1.f / (4.f * kPi)) * (1.f / (kPi * S.bound_r * S.bound_r));
+}
+// pdf_position of an area light endpoint (light_area.cpp:142, selection included)
+__device__ inline float bd_area_pa(const DevScene& S, int light) { return (1.f / float(S.num_lights)) * S.lights[light].invA_J; }
+
+// Samples [start, start + count) of a wave (record slot = index in the wave): the camera endpoint
+// and its primary ray over the whole image (camera_pinhole.cpp:134-140), the light endpoint and
+// its ray (sample_light_ray). Both rays go to one queue; thr.w carries the pdf_direction of the
+// ray at its origin, nrm.xyz the origin's normal.
+__global__ void __launch_bounds__(kBlock) k_bd_generate(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                        BdRec R, int64_t start, int64_t count, ExtQ q, int* qcount) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += int64_t(gridDim.x) * blockDim.x) {
+        const uint64_t path = uint64_t(start + i);
+        float u[8];
+        rng_slots(P.seed, path, kBdEyeBase, 1, 1, u + 4);
+        BdVtx c;
+        c.p = S.cam_p; c.n = c.gn = mk(0, 0, 0); c.a = mk(1, 1, 1);
+        c.kind = kBdCamera; c.comp = 0; c.light = -1; c.mat = -1; c.pc = 1.f;
+        c.qf = 1.f; c.pc_out = 1.f; c.prev_rev = 0.f; c.G = 0.f; c.spec = false;
+        bd_store(R, 0, 0, i, c);
+        R.nv[i] = 1;
+        const f3 de = primary_dir(S, u[4], u[5]);
+        push_ext<false>(q, qcount, S.cam_p, de, mk(1, 1, 1), cam_pdf(S, de), mk(0, 0, 0), kBdDegOrigin, uint32_t(path), uint32_t(i), 0u);
+        rng_slots(P.seed, path, kBdLightBase, 0, 2, u);
+        f3 o, d, w, ln = mk(0, 0, 0);
+        int li = 0;
+        if (!sample_light_ray(S, u, o, d, w, &li, &ln)) {
+            R.nv[R.W + i] = 0;
+            continue;
+        }
+        BdVtx l;
+        l.comp = 0; l.light = li; l.mat = -1; l.pc = 1.f; l.pc_out = 1.f; l.prev_rev = 0.f; l.G = 0.f; l.spec = false;
+        float pdir;
+        if (S.lights[li].type == LMGPU_LIGHT_AREA) {
+            l.kind = kBdArea; l.p = o; l.n = l.gn = ln;
+            l.qf = bd_area_pa(S, li);
+            const float ia = 1.f / l.qf;
+            l.a = mk(ia, ia, ia);
+            pdir = dot(d, ln) <= 0.f ? 0.f : 1.f / kPi;
+        } else {
+            l.kind = kBdInfinite; l.p = d; l.n = l.gn = mk(0, 0, 0); l.a = mk(0, 0, 0);
+            l.qf = 1.f;
+            pdir = bd_env_pray(S);
+        }
+        bd_store(R, 1, 0, i, l);
+        R.nv[R.W + i] = 1;
+        if (is_zero(w)) continue;
+        push_ext<false>(q, qcount, o, d, w, pdir, l.n, kBdLightSub | (l.kind == kBdInfinite ? kBdInfOrigin : 0u), uint32_t(path),
+                        uint32_t(i), 0u);
+    }
+}
+
+// One subpath step (bidir.h:507-569): the hit becomes vertex j + 1 with the component sampled
+// there; then, while the subpath has fewer than max_verts vertices, the next direction in the
+// subpath's transport direction. The queue carries the subpath weight up to the hit.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                     BdRec R, ExtQ qi, const float4* __restrict__ hits, const int* __restrict__ qicount,
+                                                     ExtQ qo, int* qocount) {
+    const int n = *qicount;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const float4 h4 = hits[k], o4 = qi.o[k], d4 = qi.d[k], t4 = qi.thr[k], n4 = qi.nrm[k];
+        const uint2 ids = qi.ids[k];
+        const uint32_t flags = __float_as_uint(n4.w);
+        const int j = int((flags >> 8) & 0xffu);
+        const int sub = (flags & kBdLightSub) ? 1 : 0;
+        const uint32_t base = sub ? kBdLightBase : kBdEyeBase;
+        const int64_t slot = int64_t(ids.y);
+        const f3 o = mk(o4.x, o4.y, o4.z), d = mk(d4.x, d4.y, d4.z), thr = mk(t4.x, t4.y, t4.z), no = mk(n4.x, n4.y, n4.z);
+        const int32_t id = __float_as_int(h4.w);
+        BdVtx v;
+        v.a = thr; v.pc = 1.f; v.comp = 0; v.pc_out = 1.f; v.prev_rev = 0.f; v.spec = false;
+        if (id < 0) {
+            if (S.env_light < 0) continue;  // nothing hit: the subpath ends
+            // the environment as a vertex (scene.cpp:321-331); G with an infinite end: |n_o . d|
+            v.kind = kBdInfinite; v.p = -d; v.n = v.gn = mk(0, 0, 0); v.light = S.env_light; v.mat = -1;
+            v.G = (flags & (kBdDegOrigin | kBdInfOrigin)) ? 1.f : fabsf(dot(no, d));
+            v.qf = t4.w * v.G;
+            bd_store(R, sub, j + 1, slot, v);
+            R.nv[sub * R.W + slot] = j + 2;
+            continue;
+        }
+        int32_t prim;
+        const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+        const int2 ml = __ldg(S.prim_ml + prim);
+        const DevMaterial m = S.mats[ml.x];
+        float u[16];
+        rng_slots(P.seed, ids.x, base + uint32_t(j), 3, 1, u + 12);
+        if (m.type == LMGPU_MAT_GLASS) {
+            f3 wt; bool total; float eta, Fr;
+            glass_fresnel(m, g, -d, wt, total, eta, Fr);
+            v.comp = u[13] < Fr ? 0u : 1u;
+            v.pc = v.comp == 0 ? Fr : 1.f - Fr;
+        }
+        // geometry term of the edge just traced (surface.h:329-348), from the positions
+        {
+            f3 dd;
+            float L2, c1;
+            if (flags & kBdInfOrigin) {
+                dd = d; L2 = 1.f; c1 = 1.f;
+            } else {
+                dd = g.p - o; L2 = dot(dd, dd); dd = dd / sqrtf(L2);
+                c1 = (flags & kBdDegOrigin) ? 1.f : fabsf(dot(no, dd));
+            }
+            v.G = c1 * fabsf(dot(g.n, -dd)) / L2;
+        }
+        v.qf = v.pc * (t4.w * v.G);
+        v.kind = kBdSurface; v.p = g.p; v.n = g.n; v.gn = g.gn; v.light = ml.y; v.mat = ml.x;
+        v.spec = mat_specular(m);
+        bd_store(R, sub, j + 1, slot, v);
+        R.nv[sub * R.W + slot] = j + 2;
+        if (j + 2 >= P.max_verts) continue;
+        rng_slots(P.seed, ids.x, base + uint32_t(j + 1), 2, 1, u + 8);
+        // toward the previous vertex (bidir.h:530): from the positions, or back along an
+        // infinite origin's direction
+        const f3 wi = (flags & kBdInfOrigin) ? -d : normalize(o - g.p);
+        f3 wo, w;
+        if (!mat_sample(m, g, wi, int(v.comp), u[8], u[9], u[10], wo, w, sub == 1)) continue;
+        w = w * (sub ? sn_correction_le(g, wi, wo) : sn_correction(g, wi, wo));
+        const f3 next = (thr / v.pc) * w;
+        if (is_zero(next)) continue;  // every strategy through the next vertex weighs 0
+        v.pc_out = bd_pcomp(m, g, int(v.comp), wo);
+        v.prev_rev = mat_pdf(m, g, wo, wi, false) * v.G;
+        bd_store_out(R, sub, j + 1, slot, v);
+        push_ext<false>(qo, qocount, g.p, wo, next, mat_pdf(m, g, wi, wo, false), g.n, (uint32_t(j + 1) << 8) | (sub ? kBdLightSub : 0u),
+                        ids.x, ids.y, 0u);
+    }
+}
+
+// Every strategy of one sample (renderer_bdpt.cpp:343-390): the connection (bidir.h:593-643),
+// the unweighted contribution alpha_L * c_st * alpha_E (bidir.h:325-343) and the weight. s = 0
+// splats at the eye's raster position; s, t >= 1 queue a visibility ray from the light vertex
+// to the eye vertex. Strategies whose own pdf is 0 contribute nothing.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
+                                                       BdRec R, int64_t count, int32_t min_verts, ShadowQ sq, int* scount,
+                                                       int64_t scap, float* film, int* err) {
+    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < count; k += int64_t(gridDim.x) * blockDim.x) {
+        const int nE = R.nv[k], nL = R.nv[R.W + k];
+        uint32_t eye_px = 0;
+        if (nE >= 2) {  // bidir.h:167-171: the raster position of the camera's first edge
+            const float4 r0 = R.r[bd_at(R, 0, 1, k)];
+            const f3 e1 = mk(r0.x, r0.y, r0.z);
+            const f3 de = (__float_as_uint(r0.w) & 3u) == kBdInfinite ? -e1 : normalize(e1 - S.cam_p);
+            float rx = 0.f, ry = 0.f;
+            raster_pos(S, de, rx, ry);
+            eye_px = pixel_of(P, rx, ry);
+        }
+        const bool env_l0 = nL > 0 && (__float_as_uint(R.r[bd_at(R, 1, 0, k)].w) & 3u) == kBdInfinite;
+        for (int t = 1; t <= nE; t++) {
+            const BdVtx vE = bd_load(R, 0, t - 1, k);
+            for (int s = 0; s <= nL; s++) {
+                const int n = s + t;
+                if (n < min_verts || n > P.max_verts) continue;
+                f3 Cu;
+                uint32_t px = eye_px;
+                // fresh local pdfs next to the connection; x_i = L[i] for i < s, E[n-1-i] after
+                float qLs = 0.f, qLs1 = 0.f, qEs1 = 0.f, qEs2 = 0.f, qE0 = 0.f;
+                BdVtx vL;
+                if (s == 0) {
+                    // the eye subpath ends on a light, which becomes the light endpoint x_0
+                    if (t < 2 || vE.light < 0) continue;
+                    const DevLight L = S.lights[vE.light];
+                    const float4 e2 = bd_pdfs(R, 0, t - 2, k);
+                    f3 Le;
+                    float pdir;
+                    if (vE.kind == kBdInfinite) {
+                        Le = env_eval(S, L, vE.p);
+                        pdir = bd_env_pray(S);
+                        qLs = 1.f;
+                    } else {
+                        const f3 wo = bd_toward(R, 0, t - 2, k, vE.p);
+                        const bool front = dot(wo, vE.n) > 0.f;
+                        Le = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
+                        pdir = front ? 1.f / kPi : 0.f;
+                        qLs = bd_area_pa(S, vE.light);
+                    }
+                    Cu = Le * vE.a;  // alpha_L(0) = 1; alpha_E ends on the light endpoint (component pdf 1)
+                    qLs1 = fabsf(e2.y) * (pdir * vE.G);
+                    qE0 = vE.qf / vE.pc;
+                } else {
+                    vL = bd_load(R, 1, s - 1, k);
+                    if (vL.kind == kBdInfinite || vE.kind == kBdInfinite) continue;
+                    const f3 aL = vL.a / vL.pc, aE = vE.a / vE.pc;
+                    if (is_zero(aL) || is_zero(aE)) continue;
+                    const f3 dLE = normalize(vE.p - vL.p), dEL = -dLE;
+                    const float Gc = [&] {
+                        const f3 dv = vE.p - vL.p;
+                        const float L2 = dot(dv, dv);
+                        const f3 dn = dv / sqrtf(L2);
+                        const float c2 = vE.kind == kBdCamera ? 1.f : fabsf(dot(vE.n, -dn));
+                        return fabsf(dot(vL.n, dn)) * c2 / L2;
+                    }();
+                    f3 fL, fE;
+                    float pLf, pcL = 1.f;
+                    if (s == 1) {
+                        const DevLight L = S.lights[vL.light];
+                        const bool front = dot(dLE, vL.n) > 0.f;
+                        fL = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
+                        pLf = front ? 1.f / kPi : 0.f;
+                    } else {
+                        const DevMaterial m = S.mats[vL.mat];
+                        const Geom gL = bd_geom(vL);
+                        const f3 wi = bd_toward(R, 1, s - 2, k, vL.p);
+                        fL = mat_eval(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
+                        pLf = mat_pdf(m, gL, wi, dLE, false);
+                        pcL = bd_pcomp(m, gL, int(vL.comp), dLE);
+                        qEs2 = fabsf(bd_pdfs(R, 1, s - 2, k).y) * (mat_pdf(m, gL, dLE, wi, false) * vL.G);
+                    }
+                    if (is_zero(fL)) continue;
+                    float pEf, pcE = 1.f;
+                    if (t == 1) {
+                        float rx, ry;
+                        if (!raster_pos(S, dEL, rx, ry)) continue;
+                        const float J = cam_J(S, dEL);
+                        fE = mk(J, J, J);
+                        pEf = J;
+                        px = pixel_of(P, rx, ry);
+                    } else {
+                        const DevMaterial m = S.mats[vE.mat];
+                        const Geom gE = bd_geom(vE);
+                        const f3 wi = bd_toward(R, 0, t - 2, k, vE.p);
+                        fE = mat_eval(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
+                        pEf = mat_pdf(m, gE, wi, dEL, false);
+                        pcE = bd_pcomp(m, gE, int(vE.comp), dEL);
+                        qLs1 = fabsf(bd_pdfs(R, 0, t - 2, k).y) * (mat_pdf(m, gE, dEL, wi, false) * vE.G);
+                    }
+                    Cu = aL * (fL * Gc * fE) * aE;
+                    qLs = pcE * (pLf * Gc);
+                    qEs1 = pcL * (pEf * Gc);
+                }
+                if (is_zero(Cu)) continue;
+
+                // qL(i): i < s stored (L[i].qf); s, s+1 fresh; beyond from the eye subpath's
+                // reverse factors. qE(i): i >= s stored (E[n-1-i].qf; x_0 as endpoint: qE0);
+                // s-1, s-2 fresh; below from the light subpath's reverse factors.
+                auto qL = [&](int i) -> float {
+                    if (i < s) return bd_pdfs(R, 1, i, k).x;
+                    if (i == s) return qLs;
+                    if (i == s + 1) return qLs1;
+                    const int jj = n - 1 - i;  // eye vertex x_i; qL = pc_out(E[jj]) * prev_rev(E[jj + 1])
+                    return fabsf(bd_pdfs(R, 0, jj, k).y) * bd_pdfs(R, 0, jj + 1, k).z;
+                };
+                auto qE = [&](int i) -> float {
+                    if (i >= s) return (s == 0 && i == 0) ? qE0 : bd_pdfs(R, 0, n - 1 - i, k).x;
+                    if (i == s - 1) return qEs1;
+                    if (i == s - 2) return qEs2;
+                    return fabsf(bd_pdfs(R, 1, i, k).y) * bd_pdfs(R, 1, i + 1, k).z;
+                };
+                // bidir.h:185-224: x_{s2-1} and x_{s2} must not be specular; an infinite light
+                // endpoint is not connectable (s2 = 1); the camera endpoint is degenerate (s2 = n)
+                auto spec = [&](int i) -> bool {
+                    if (i == 0 || i == n - 1) return false;  // endpoints
+                    return signbit(i < s ? bd_pdfs(R, 1, i, k).y : bd_pdfs(R, 0, n - 1 - i, k).y);
+                };
+                const bool inf0 = s == 0 ? vE.kind == kBdInfinite : env_l0;
+                auto samplable = [&](int s2) -> bool {
+                    if (s2 == 0) return true;
+                    if (s2 >= n) return false;
+                    if (s2 == 1 && inf0) return false;
+                    return !spec(s2 - 1) && !spec(s2);
+                };
+                if (!samplable(s)) continue;
+                float inv = 1.f, r = 1.f;
+                bool ok = true;
+                for (int j = s; j <= n - 2; j++) {  // p_{j+1} / p_s
+                    const float den = qE(j);
+                    if (den == 0.f) { ok = false; break; }
+                    r *= qL(j) / den;
+                    if (r != 0.f && samplable(j + 1)) inv += r * r;
+                }
+                r = 1.f;
+                for (int j = s - 1; j >= 0 && ok; j--) {  // p_j / p_s
+                    const float den = qL(j);
+                    if (den == 0.f) { ok = false; break; }
+                    r *= qE(j) / den;
+                    if (r != 0.f && samplable(j)) inv += r * r;
+                }
+                if (!ok) continue;
+                const f3 C = Cu * (1.f / inv);
+                if (is_zero(C)) continue;
+                if (s == 0) {
+                    splat(film, px, C);
+                    continue;
+                }
+                const int slot = queue_slot(scount);
+                if (slot >= scap) {
+                    atomicOr(err, 2);
+                    continue;
+                }
+                // Scene::visible from the light vertex (include/lm/scene.h:343-364)
+                const f3 dv = vE.p - vL.p;
+                const f3 dn = normalize(dv);
+                sq.o[slot] = make_float4(vL.p.x, vL.p.y, vL.p.z, length(dv) * (1.f - kEps));
+                sq.d[slot] = make_float4(dn.x, dn.y, dn.z, 0.f);
+                sq.c[slot] = make_float4(C.x, C.y, C.z, __uint_as_float(px));
+            }
+        }
+    }
+}
+
 // Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
 // counter (warp-aggregated per pass).
 template <int kMinBlocks, bool kSingle>
@@ -1309,6 +1713,7 @@ struct Workspace {
     DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
     lmgpu_batch* batch = nullptr;  // the regenerating wavefront lmgpu_render_pt runs its job on
     int64_t batch_cap = 0;
+    DevBuf bd_rec, bd_nv, bd_s_o, bd_s_d, bd_s_c;  // lmgpu_render_bdpt: subpath records, connection rays
 };
 
 Workspace& workspace(int device) {
@@ -2051,6 +2456,170 @@ int lmgpu_render_lt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_lt_params* prm, v
         for (auto& e : marks) cudaEventDestroy(e.second);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
+        if (stats) {
+            *stats = lmgpu_render_stats{};
+            stats->paths = total;
+            stats->extension_rays = int64_t(hr[0]);
+            stats->shadow_rays = int64_t(hr[1]);
+            stats->rays = int64_t(hr[0] + hr[1]);
+            stats->elapsed_ms = ms;
+            stats->generate_ms = kms[K_GEN];
+            stats->extend_ms = kms[K_EXT];
+            stats->shade_ms = kms[K_SHADE];
+            stats->shadow_ms = kms[K_SHADOW];
+            stats->trace_ms = kms[K_EXT] + kms[K_SHADOW];
+            stats->extend_launches = n_ext;
+            stats->shadow_launches = n_sh;
+        }
+    });
+}
+
+int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* prm, void* stream, lmgpu_render_stats* stats) {
+    return guarded([&] {
+        if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
+        if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
+        if (prm->num_samples <= 0 || prm->first_path < 0 || prm->max_verts < 2 || prm->min_verts < 0)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "num_samples must be > 0, first_path >= 0, max_verts >= 2 and min_verts >= 0");
+        if (prm->max_verts > kBdMaxVerts) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 64");
+        if (prm->first_path + prm->num_samples > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "sample index above 2^32");
+        if (prm->accumulate && f->split) throw Error(LMGPU_ERR_UNSUPPORTED, "film holds split passes");
+        ensure_film(f);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int64_t npix = int64_t(f->w) * f->h;
+        const int64_t total = prm->num_samples;
+        const int mv = prm->max_verts;
+        const int64_t pairs = int64_t(mv) * (mv - 1) / 2;  // strategies with s, t >= 1 and s + t <= max_verts
+        // default: 2^20 samples, fewer for long paths so the connection queue stays within 2^28 rays
+        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : std::min<int64_t>(int64_t(1) << 20, (int64_t(1) << 28) / pairs),
+                                      total);
+        const int64_t scap = wave * pairs;
+        if (scap > (int64_t(1) << 31) - 1) throw Error(LMGPU_ERR_UNSUPPORTED, "wave_paths too large for max_verts");
+        Workspace& ws = workspace(current_device().device);
+        std::lock_guard<std::mutex> ws_lock(ws.m);
+        ensure_queues(ws, 2 * wave);
+        ws.bd_rec.alloc(size_t(2) * mv * size_t(wave) * kBdRecWords * 16);
+        ws.bd_nv.alloc(size_t(2) * size_t(wave) * 4);
+        ws.bd_s_o.alloc(size_t(scap) * 16);
+        ws.bd_s_d.alloc(size_t(scap) * 16);
+        ws.bd_s_c.alloc(size_t(scap) * 16);
+
+        PtConst P{};
+        P.seed = prm->seed;
+        P.max_verts = mv;
+        P.spp = 1;
+        P.w = f->w;
+        P.h = f->h;
+        const BdRec R{ws.bd_rec.as<float4>(), ws.bd_nv.as<int32_t>(), wave, mv};
+        ExtQ q[2];
+        for (int b = 0; b < 2; b++)
+            q[b] = ExtQ{ws.q_o[b].as<float4>(), ws.q_d[b].as<float4>(), ws.q_thr[b].as<float4>(), ws.q_nrm[b].as<float4>(),
+                        ws.q_ids[b].as<uint2>()};
+        ShadowQ sq{ws.bd_s_o.as<float4>(), ws.bd_s_d.as<float4>(), ws.bd_s_c.as<float4>()};
+        // [0],[1] extension queues, [2] connection rays, [3] error, [4],[5] ray fetch
+        int* cnt = ws.counters.as<int>();
+        const int refill = tuning().trace_refill;
+        const Fetch f_ext{cnt + 4, cnt + 5, refill}, f_sh{cnt + 5, cnt + 4, refill};
+        unsigned long long* rays = reinterpret_cast<unsigned long long*>(ws.counters.as<char>() + 32);
+        float* film = f->sum.as<float>();
+        const Bvh8 bvh = s->dev.bvh;
+        const size_t tsmem = size_t(2) * 4 * kBlock * size_t(bvh.depth);
+        const bool two = s->dev.num_inst > 0;
+        auto ext_k = two ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>;
+        auto sh_k = two ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>;
+        auto shade_k = pick_shade(k_bd_shade<2>, k_bd_shade<3>, k_bd_shade<4>, tuning().shade_minblocks);
+        const int g_gen = grid_for(k_bd_generate, kBlock, 0);
+        const int g_ext = grid_for(ext_k, kBlock, tsmem);
+        const int g_sh = grid_for(sh_k, kBlock, tsmem);
+        const int g_shade = grid_for(shade_k, kBlock, 0);
+        const int g_con = grid_for(k_bd_connect<2>, kBlock, 0);
+
+        enum { K_GEN = 0, K_EXT = 1, K_SHADE = 2, K_SHADOW = 3 };
+        std::vector<std::pair<int, cudaEvent_t>> marks;
+        const bool timed = stats != nullptr;
+        auto mark = [&](int kind) {
+            if (!timed) return;
+            cudaEvent_t e;
+            LMGPU_CUDA(cudaEventCreate(&e));
+            LMGPU_CUDA(cudaEventRecord(e, st));
+            marks.emplace_back(kind, e);
+        };
+        cudaEvent_t e0, e1;
+        LMGPU_CUDA(cudaEventCreate(&e0));
+        LMGPU_CUDA(cudaEventCreate(&e1));
+        int64_t n_ext = 0, n_sh = 0;
+
+        LMGPU_CUDA(cudaEventRecord(e0, st));
+        if (!prm->accumulate) {
+            LMGPU_CUDA(cudaMemsetAsync(film, 0, size_t(npix) * 3 * 4, st));
+            f->accumulated_spp = 0;
+            f->split = false;
+            f->passes_even = f->passes_odd = 0;
+        }
+        LMGPU_CUDA(cudaMemsetAsync(ws.counters.p, 0, 192, st));
+        for (int64_t start = 0; start < total; start += wave) {
+            const int64_t n = std::min(wave, total - start);
+            int cur = 0;
+            LMGPU_CUDA(cudaMemsetAsync(cnt, 0, 12, st));
+            LMGPU_CUDA(cudaMemsetAsync(cnt + 4, 0, 8, st));
+            mark(K_GEN);
+            k_bd_generate<<<int(std::min<int64_t>(g_gen, (n + kBlock - 1) / kBlock)), kBlock, 0, st>>>(
+                s->dev, P, R, prm->first_path + start, n, q[0], cnt + 0);
+            mark(-1);
+            LMGPU_CUDA(cudaGetLastError());
+            // the ray that leaves subpath vertex it creates vertex it + 1 (at most max_verts - 1)
+            for (int it = 0; it + 1 < mv; it++) {
+                // the extend kernel's fetch counter is otherwise reset by the shadow kernel, which
+                // runs once per wave here
+                LMGPU_CUDA(cudaMemsetAsync(cnt + 4, 0, 4, st));
+                mark(K_EXT);
+                ext_k<<<g_ext, kBlock, tsmem, st>>>(bvh, q[cur].o, q[cur].d, cnt + cur, ws.hits.as<float4>(), rays, cnt + 3, nullptr,
+                                                    0, nullptr, f_ext, nullptr, nullptr);
+                mark(-1);
+                n_ext++;
+                LMGPU_CUDA(cudaMemsetAsync(cnt + (1 - cur), 0, 4, st));
+                mark(K_SHADE);
+                shade_k<<<g_shade, kBlock, 0, st>>>(s->dev, P, R, q[cur], ws.hits.as<float4>(), cnt + cur, q[1 - cur], cnt + (1 - cur));
+                mark(-1);
+                LMGPU_CUDA(cudaGetLastError());
+                cur = 1 - cur;
+            }
+            mark(K_SHADE);
+            k_bd_connect<2><<<int(std::min<int64_t>(g_con, (n + kBlock - 1) / kBlock)), kBlock, 0, st>>>(
+                s->dev, P, R, n, prm->min_verts, sq, cnt + 2, scap, film, cnt + 3);
+            mark(-1);
+            mark(K_SHADOW);
+            sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, nullptr, 0, nullptr, f_sh, nullptr, nullptr);
+            mark(-1);
+            n_sh++;
+            LMGPU_CUDA(cudaGetLastError());
+            LMGPU_CUDA(cudaMemsetAsync(cnt + 2, 0, 4, st));
+        }
+        f->accumulated_spp += total;
+        const double scale = double(npix) / double(f->accumulated_spp);  // renderer_bdpt.cpp:397-399
+        f->scale = scale;
+        k_scale<<<1024, 256, 0, st>>>(film, f->out.as<float>(), npix * 3, float(scale));
+        LMGPU_CUDA(cudaGetLastError());
+        LMGPU_CUDA(cudaEventRecord(e1, st));
+        unsigned long long hr[2];
+        int herr = 0;
+        LMGPU_CUDA(cudaMemcpyAsync(hr, rays, sizeof(hr), cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaMemcpyAsync(&herr, cnt + 3, 4, cudaMemcpyDeviceToHost, st));
+        LMGPU_CUDA(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        LMGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        double kms[4] = {0, 0, 0, 0};
+        for (size_t i = 0; i + 1 < marks.size(); i++) {
+            if (marks[i].first < 0) continue;
+            float m = 0.f;
+            LMGPU_CUDA(cudaEventElapsedTime(&m, marks[i].second, marks[i + 1].second));
+            kms[marks[i].first] += m;
+        }
+        for (auto& e : marks) cudaEventDestroy(e.second);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (herr & 2) throw Error(LMGPU_ERR_INTERNAL, "connection queue overflow");
         if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
         if (stats) {
             *stats = lmgpu_render_stats{};

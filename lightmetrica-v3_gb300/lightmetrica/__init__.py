@@ -20,7 +20,7 @@ functests use to build scenes and render them:
 
 Every accel key the reference registers (accel::sahbvh, accel::nanort, accel::embree,
 accel::embreeinstanced) and accel::gpu resolve to the GB300 8-wide BVH; renderer::pt,
-renderer::lt and renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a
+renderer::lt, renderer::bdpt and renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a
 missing liblmgpu.so raises at the first render or build.
 """
 from __future__ import annotations
@@ -1258,18 +1258,14 @@ class RendererPT(Component):
                 "Mrays_per_s": rays / max(dev_ms, 1e-9) / 1e3}
 
 
-@_reg("renderer::lt", "renderer::lt_gpu")
-class RendererLT(Component):
-    """renderer::lt (src/renderer/renderer_lt.cpp:18-160): light tracing with next-event
-    connections to the camera, on the GPU wavefront.
+class _SpiRenderer(Component):
+    """Renderers scheduled per sample (scheduler::spi::*, src/scheduler.cpp:113-183): 'sample' with
+    num_samples; 'time' with render_time and samples_per_iter (default 100000), rounds of
+    samples_per_iter consecutive samples until the time is spent. The film is rescaled by
+    w*h / (samples processed). `_call(n, first, accumulate, stats)` renders samples
+    [first, first + n) on the GPU."""
 
-    Props as the reference: scene, output, max_verts, seed, and the scheduler, which for this
-    renderer counts light paths (scheduler::spi::*, src/scheduler.cpp:113-183): 'sample' with
-    num_samples; 'time' with render_time and samples_per_iter (default 100000), rendering rounds
-    of samples_per_iter light paths until the time is spent. The film is rescaled by
-    w*h / (light paths processed). GPU extra: wave_paths (light paths per wave)."""
-
-    def construct(self, prop):
+    def _spi_construct(self, prop):
         self.scene = _resolve(_req(prop, "scene"))
         self.film = _resolve(_req(prop, "output"))
         self.max_verts = int(_req(prop, "max_verts"))
@@ -1286,33 +1282,22 @@ class RendererLT(Component):
         self.wave_paths = int(prop.get("wave_paths", 0))
         self.last_stats: dict = {}
 
-    def _params(self, n: int, first: int, accumulate: bool) -> N.LTParams:
-        p = N.LTParams()
-        p.num_samples = n
-        p.first_path = first
-        p.max_verts = self.max_verts
-        p.seed = self.seed & 0xFFFFFFFF
-        p.wave_paths = self.wave_paths
-        p.accumulate = int(accumulate)
-        return p
+    def _call(self, n: int, first: int, accumulate: bool, st) -> None:
+        raise NotImplementedError
 
     def render(self) -> dict:
         self.scene.require_renderable()
         self.scene._require_built()
         t0 = time.perf_counter()
         st = N.RenderStats()
-        lib = N.lib()
         if self.scheduler == "sample":
-            N.check(lib.lmgpu_render_lt(self.scene._h, self.film._h, C.byref(self._params(self.num_samples, 0, False)), None,
-                                        C.byref(st)))
+            self._call(self.num_samples, 0, False, st)
             processed, rays, dev_ms = self.num_samples, st.rays, st.elapsed_ms
         else:
-            # consecutive light paths per round, so the rounds together are one longer render
+            # consecutive samples per round, so the rounds together are one longer render
             processed, rays, dev_ms = 0, 0, 0.0
             while True:
-                N.check(lib.lmgpu_render_lt(self.scene._h, self.film._h,
-                                            C.byref(self._params(self.samples_per_iter, processed, processed > 0)), None,
-                                            C.byref(st)))
+                self._call(self.samples_per_iter, processed, processed > 0, st)
                 processed += self.samples_per_iter
                 rays += st.rays
                 dev_ms += st.elapsed_ms
@@ -1323,3 +1308,38 @@ class RendererLT(Component):
                            "device_ms": dev_ms, "trace_ms": st.trace_ms}
         return {"processed": processed, "elapsed": elapsed, "rays": rays,
                 "Mrays_per_s": rays / max(dev_ms, 1e-9) / 1e3}
+
+
+@_reg("renderer::bdpt", "renderer::bdpt_gpu")
+class RendererBDPT(_SpiRenderer):
+    """renderer::bdpt (src/renderer/renderer_bdpt.cpp:20-62, 297-413): bidirectional path tracing
+    with every strategy weighted by the power heuristic (include/lm/bidir.h). Props as the
+    reference: scene, output, min_verts (default 2), max_verts, seed, scheduler ('sample' with
+    num_samples, or 'time'). GPU extra: wave_paths (samples per wave)."""
+
+    def construct(self, prop):
+        self._spi_construct(prop)
+        self.min_verts = int(prop.get("min_verts", 2))
+
+    def _call(self, n, first, accumulate, st):
+        p = N.BDPTParams()
+        p.num_samples, p.first_path, p.min_verts, p.max_verts = n, first, self.min_verts, self.max_verts
+        p.seed, p.accumulate, p.wave_paths = self.seed & 0xFFFFFFFF, int(accumulate), self.wave_paths
+        N.check(N.lib().lmgpu_render_bdpt(self.scene._h, self.film._h, C.byref(p), None, C.byref(st)))
+
+
+@_reg("renderer::lt", "renderer::lt_gpu")
+class RendererLT(_SpiRenderer):
+    """renderer::lt (src/renderer/renderer_lt.cpp:18-160): light tracing with next-event
+    connections to the camera, on the GPU wavefront. Props as the reference: scene, output,
+    max_verts, seed, and the scheduler, which counts light paths ('sample' with num_samples, or
+    'time'). GPU extra: wave_paths (light paths per wave)."""
+
+    def construct(self, prop):
+        self._spi_construct(prop)
+
+    def _call(self, n, first, accumulate, st):
+        p = N.LTParams()
+        p.num_samples, p.first_path, p.max_verts = n, first, self.max_verts
+        p.seed, p.wave_paths, p.accumulate = self.seed & 0xFFFFFFFF, self.wave_paths, int(accumulate)
+        N.check(N.lib().lmgpu_render_lt(self.scene._h, self.film._h, C.byref(p), None, C.byref(st)))

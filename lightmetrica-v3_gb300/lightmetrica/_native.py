@@ -70,6 +70,11 @@ class LTParams(C.Structure):
                 ("wave_paths", C.c_int64), ("accumulate", C.c_int32), ("reserved", C.c_int32)]
 
 
+class BDPTParams(C.Structure):
+    _fields_ = [("num_samples", C.c_int64), ("first_path", C.c_int64), ("min_verts", C.c_int32), ("max_verts", C.c_int32),
+                ("seed", C.c_uint32), ("accumulate", C.c_int32), ("wave_paths", C.c_int64)]
+
+
 class RenderStats(C.Structure):
     _fields_ = [("paths", C.c_int64), ("rays", C.c_int64), ("extension_rays", C.c_int64), ("shadow_rays", C.c_int64),
                 ("elapsed_ms", C.c_double), ("trace_ms", C.c_double), ("extend_ms", C.c_double),
@@ -112,6 +117,7 @@ SIGNATURES = [
     ("lmgpu_render_raycast", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RaycastParams), C.c_void_p]),
     ("lmgpu_render_pt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.c_void_p, C.POINTER(RenderStats)]),
     ("lmgpu_render_lt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(LTParams), C.c_void_p, C.POINTER(RenderStats)]),
+    ("lmgpu_render_bdpt", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(BDPTParams), C.c_void_p, C.POINTER(RenderStats)]),
     ("lmgpu_batch_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int64]),
     ("lmgpu_batch_destroy", C.c_int, [C.c_void_p]),
     ("lmgpu_batch_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.POINTER(C.c_int32)]),
