@@ -351,6 +351,8 @@ def run_gpu(args) -> None:
                 out["served_stress"] = run_served_stress(lm, args, ctx)
         if args.lt_paths > 0:
             out["lt"] = run_lt(lm, scene, film, args)
+        if args.bdpt_samples > 0:
+            out["bdpt"] = run_bdpt(lm, scene, film, args)
         if args.instanced_spp > 0:
             out["instanced"] = run_instanced(lm, args)
         print(json.dumps(out))
@@ -623,6 +625,57 @@ def run_lt(lm, scene, film, args) -> dict:
     return res
 
 
+def run_bdpt(lm, scene, film, args) -> dict:
+    """renderer::bdpt on the headline scene (already built): args.bdpt_samples samples per frame
+    (one eye and one light subpath each), device-timed with CUDA events; end to end through
+    RendererBDPT.render() + film.buffer(); and the oracle's BDPT (fp64, the reference's
+    std::mt19937 stream) on a bounded sample."""
+    import ctypes as C
+    from lightmetrica import _native as N
+    L = N.lib()
+
+    def frame(seed):
+        p = N.BDPTParams()
+        p.num_samples, p.first_path, p.min_verts, p.max_verts, p.seed = args.bdpt_samples, 0, 2, MAX_VERTS, seed
+        st = N.RenderStats()
+        N.check(L.lmgpu_render_bdpt(scene._h, film._h, C.byref(p), None, C.byref(st)))
+        return st
+    frame(1)
+    runs = [frame(300 + k) for k in range(3)]
+    ms = sorted(r.elapsed_ms for r in runs)
+    rays = sum(r.rays for r in runs)
+    r = lm.load_renderer("bdpt_bench", "bdpt", scene=scene, output=film, max_verts=MAX_VERTS, seed=7, scheduler="sample",
+                         num_samples=args.bdpt_samples)
+    r.render()
+    e2e_rays, e2e_s = 0, 0.0
+    for _ in range(3):
+        t = time.perf_counter()
+        out = r.render()
+        film.buffer_f32()
+        e2e_s += time.perf_counter() - t
+        e2e_rays += out["rays"]
+    res = {"workload": f"renderer::bdpt on the headline scene ({W_PX}x{H_PX} film), {args.bdpt_samples} samples per frame, "
+                       f"subpaths of up to {MAX_VERTS} vertices, every strategy with s + t <= {MAX_VERTS}",
+           "Mrays_per_s": rays / sum(r.elapsed_ms for r in runs) / 1e3, "ms_per_frame_median": ms[1],
+           "samples_per_s": args.bdpt_samples / (ms[1] / 1e3),
+           "rays_per_frame": rays / len(runs),
+           "subpath_rays_per_frame": sum(r.extension_rays for r in runs) / len(runs),
+           "connection_rays_per_frame": sum(r.shadow_rays for r in runs) / len(runs),
+           "kernel_ms_per_frame": {"extend": sum(r.extend_ms for r in runs) / len(runs),
+                                   "shade_and_connect": sum(r.shade_ms for r in runs) / len(runs),
+                                   "shadow": sum(r.shadow_ms for r in runs) / len(runs),
+                                   "generate": sum(r.generate_ms for r in runs) / len(runs)},
+           "e2e_Mrays_per_s": e2e_rays / e2e_s / 1e6}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        S = cpu_port(scene, 1)
+        n = 1 << 17
+        _, crays, csec = S.render_bdpt(W_PX, H_PX, n, MAX_VERTS, seed=7, rng="mt19937")
+        res["cpu_baseline"] = {"value": crays / csec / 1e6, "unit": "Mrays/s", "cores": O.max_threads(), "kind": "port",
+                               "samples_per_s": n / csec, "sample": f"{n} samples ({crays} rays, {csec:.1f} s)"}
+    return res
+
+
 def _cudart():
     import ctypes as C
     import glob
@@ -660,6 +713,7 @@ def main():
                     help="paths in flight of the served legs (smaller than the batched optimum: less queueing delay)")
     ap.add_argument("--stress-budget-mb", type=int, default=1536)
     ap.add_argument("--lt-paths", type=int, default=1 << 24, help="light paths per frame of the renderer::lt leg (0 skips it)")
+    ap.add_argument("--bdpt-samples", type=int, default=1 << 22, help="samples per frame of the renderer::bdpt leg (0 skips it)")
     args = ap.parse_args()
     _apply_overrides(args)
     if args.impl == "reference":

@@ -1341,18 +1341,63 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_co
     }
 }
 
-// Every strategy of one sample (renderer_bdpt.cpp:343-390): the connection (bidir.h:593-643),
-// the unweighted contribution alpha_L * c_st * alpha_E (bidir.h:325-343) and the weight. s = 0
-// splats at the eye's raster position; s, t >= 1 queue a visibility ray from the light vertex
-// to the eye vertex. Strategies whose own pdf is 0 contribute nothing.
+// The strategies of the wave's samples as a dense work list (renderer_bdpt.cpp:347-355): item
+// (sample, s | t << 8) for s <= n_L, 1 <= t <= n_E and min_verts <= s + t <= max_verts. One warp
+// takes 32 consecutive samples: their item count in closed form, one atomic for the warp's range,
+// then the items in (t, s) order across the lanes (ballot ranks), so neighbouring items share
+// their strategy and their samples' records.
+__global__ void __launch_bounds__(kBlock) k_bd_items(BdRec R, int64_t count, int32_t min_verts, int32_t max_verts, uint2* items,
+                                                     int* icount, int64_t icap, int* err) {
+    const unsigned full = 0xffffffffu;
+    const int lane = int(threadIdx.x & 31u);
+    const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w * 32 < count; w += nwarps) {
+        const int64_t k = w * 32 + lane;
+        const int nE = k < count ? R.nv[k] : 0, nL = k < count ? R.nv[R.W + k] : 0;
+        int mine = 0;
+        for (int t = 1; t <= nE; t++) mine += max(0, min(nL, max_verts - t) - max(0, min_verts - t) + 1);
+        int tot = mine, tmax = nE, smax = nL;
+        for (int o = 16; o > 0; o >>= 1) {
+            tot += __shfl_xor_sync(full, tot, o);
+            tmax = max(tmax, __shfl_xor_sync(full, tmax, o));
+            smax = max(smax, __shfl_xor_sync(full, smax, o));
+        }
+        int base = 0;
+        if (lane == 0 && tot > 0) base = atomicAdd(icount, tot);
+        base = __shfl_sync(full, base, 0);
+        if (int64_t(base) + tot > icap) {  // cannot happen with the capacity the host sizes
+            if (lane == 0) atomicOr(err, 4);
+            continue;
+        }
+        int off = 0;
+        for (int t = 1; t <= tmax; t++) {
+            for (int s = 0; s <= smax; s++) {
+                const bool have = t <= nE && s <= nL && s + t >= min_verts && s + t <= max_verts;
+                const unsigned b = __ballot_sync(full, have);
+                if (have) items[base + off + __popc(b & ((1u << lane) - 1u))] = make_uint2(uint32_t(k), uint32_t(s) | (uint32_t(t) << 8));
+                off += __popc(b);
+            }
+        }
+    }
+}
+
+// One strategy of one sample per item: the connection (bidir.h:593-643), the unweighted
+// contribution alpha_L * c_st * alpha_E (bidir.h:325-343) and the weight. s = 0 splats at the
+// eye's raster position; s, t >= 1 queue a visibility ray from the light vertex to the eye
+// vertex. Strategies whose own pdf is 0 contribute nothing.
 template <int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
-                                                       BdRec R, int64_t count, int32_t min_verts, ShadowQ sq, int* scount,
-                                                       int64_t scap, float* film, int* err) {
-    for (int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; k < count; k += int64_t(gridDim.x) * blockDim.x) {
-        const int nE = R.nv[k], nL = R.nv[R.W + k];
+                                                       BdRec R, const uint2* __restrict__ items, const int* __restrict__ icount,
+                                                       ShadowQ sq, int* scount, int64_t scap, float* film, int* err) {
+    const int nitems = *icount;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < nitems; it += gridDim.x * blockDim.x) {
+        const uint2 item = items[it];
+        const int64_t k = int64_t(item.x);
+        const int s = int(item.y & 0xffu), t = int(item.y >> 8);
+        const int n = s + t;
+        const int nL = R.nv[R.W + k];
         uint32_t eye_px = 0;
-        if (nE >= 2) {  // bidir.h:167-171: the raster position of the camera's first edge
+        if (t >= 2) {  // bidir.h:167-171: the raster position of the camera's first edge
             const float4 r0 = R.r[bd_at(R, 0, 1, k)];
             const f3 e1 = mk(r0.x, r0.y, r0.z);
             const f3 de = (__float_as_uint(r0.w) & 3u) == kBdInfinite ? -e1 : normalize(e1 - S.cam_p);
@@ -1361,155 +1406,150 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
             eye_px = pixel_of(P, rx, ry);
         }
         const bool env_l0 = nL > 0 && (__float_as_uint(R.r[bd_at(R, 1, 0, k)].w) & 3u) == kBdInfinite;
-        for (int t = 1; t <= nE; t++) {
-            const BdVtx vE = bd_load(R, 0, t - 1, k);
-            for (int s = 0; s <= nL; s++) {
-                const int n = s + t;
-                if (n < min_verts || n > P.max_verts) continue;
-                f3 Cu;
-                uint32_t px = eye_px;
-                // fresh local pdfs next to the connection; x_i = L[i] for i < s, E[n-1-i] after
-                float qLs = 0.f, qLs1 = 0.f, qEs1 = 0.f, qEs2 = 0.f, qE0 = 0.f;
-                BdVtx vL;
-                if (s == 0) {
-                    // the eye subpath ends on a light, which becomes the light endpoint x_0
-                    if (t < 2 || vE.light < 0) continue;
-                    const DevLight L = S.lights[vE.light];
-                    const float4 e2 = bd_pdfs(R, 0, t - 2, k);
-                    f3 Le;
-                    float pdir;
-                    if (vE.kind == kBdInfinite) {
-                        Le = env_eval(S, L, vE.p);
-                        pdir = bd_env_pray(S);
-                        qLs = 1.f;
-                    } else {
-                        const f3 wo = bd_toward(R, 0, t - 2, k, vE.p);
-                        const bool front = dot(wo, vE.n) > 0.f;
-                        Le = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
-                        pdir = front ? 1.f / kPi : 0.f;
-                        qLs = bd_area_pa(S, vE.light);
-                    }
-                    Cu = Le * vE.a;  // alpha_L(0) = 1; alpha_E ends on the light endpoint (component pdf 1)
-                    qLs1 = fabsf(e2.y) * (pdir * vE.G);
-                    qE0 = vE.qf / vE.pc;
-                } else {
-                    vL = bd_load(R, 1, s - 1, k);
-                    if (vL.kind == kBdInfinite || vE.kind == kBdInfinite) continue;
-                    const f3 aL = vL.a / vL.pc, aE = vE.a / vE.pc;
-                    if (is_zero(aL) || is_zero(aE)) continue;
-                    const f3 dLE = normalize(vE.p - vL.p), dEL = -dLE;
-                    const float Gc = [&] {
-                        const f3 dv = vE.p - vL.p;
-                        const float L2 = dot(dv, dv);
-                        const f3 dn = dv / sqrtf(L2);
-                        const float c2 = vE.kind == kBdCamera ? 1.f : fabsf(dot(vE.n, -dn));
-                        return fabsf(dot(vL.n, dn)) * c2 / L2;
-                    }();
-                    f3 fL, fE;
-                    float pLf, pcL = 1.f;
-                    if (s == 1) {
-                        const DevLight L = S.lights[vL.light];
-                        const bool front = dot(dLE, vL.n) > 0.f;
-                        fL = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
-                        pLf = front ? 1.f / kPi : 0.f;
-                    } else {
-                        const DevMaterial m = S.mats[vL.mat];
-                        const Geom gL = bd_geom(vL);
-                        const f3 wi = bd_toward(R, 1, s - 2, k, vL.p);
-                        fL = mat_eval(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
-                        pLf = mat_pdf(m, gL, wi, dLE, false);
-                        pcL = bd_pcomp(m, gL, int(vL.comp), dLE);
-                        qEs2 = fabsf(bd_pdfs(R, 1, s - 2, k).y) * (mat_pdf(m, gL, dLE, wi, false) * vL.G);
-                    }
-                    if (is_zero(fL)) continue;
-                    float pEf, pcE = 1.f;
-                    if (t == 1) {
-                        float rx, ry;
-                        if (!raster_pos(S, dEL, rx, ry)) continue;
-                        const float J = cam_J(S, dEL);
-                        fE = mk(J, J, J);
-                        pEf = J;
-                        px = pixel_of(P, rx, ry);
-                    } else {
-                        const DevMaterial m = S.mats[vE.mat];
-                        const Geom gE = bd_geom(vE);
-                        const f3 wi = bd_toward(R, 0, t - 2, k, vE.p);
-                        fE = mat_eval(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
-                        pEf = mat_pdf(m, gE, wi, dEL, false);
-                        pcE = bd_pcomp(m, gE, int(vE.comp), dEL);
-                        qLs1 = fabsf(bd_pdfs(R, 0, t - 2, k).y) * (mat_pdf(m, gE, dEL, wi, false) * vE.G);
-                    }
-                    Cu = aL * (fL * Gc * fE) * aE;
-                    qLs = pcE * (pLf * Gc);
-                    qEs1 = pcL * (pEf * Gc);
-                }
-                if (is_zero(Cu)) continue;
-
-                // qL(i): i < s stored (L[i].qf); s, s+1 fresh; beyond from the eye subpath's
-                // reverse factors. qE(i): i >= s stored (E[n-1-i].qf; x_0 as endpoint: qE0);
-                // s-1, s-2 fresh; below from the light subpath's reverse factors.
-                auto qL = [&](int i) -> float {
-                    if (i < s) return bd_pdfs(R, 1, i, k).x;
-                    if (i == s) return qLs;
-                    if (i == s + 1) return qLs1;
-                    const int jj = n - 1 - i;  // eye vertex x_i; qL = pc_out(E[jj]) * prev_rev(E[jj + 1])
-                    return fabsf(bd_pdfs(R, 0, jj, k).y) * bd_pdfs(R, 0, jj + 1, k).z;
-                };
-                auto qE = [&](int i) -> float {
-                    if (i >= s) return (s == 0 && i == 0) ? qE0 : bd_pdfs(R, 0, n - 1 - i, k).x;
-                    if (i == s - 1) return qEs1;
-                    if (i == s - 2) return qEs2;
-                    return fabsf(bd_pdfs(R, 1, i, k).y) * bd_pdfs(R, 1, i + 1, k).z;
-                };
-                // bidir.h:185-224: x_{s2-1} and x_{s2} must not be specular; an infinite light
-                // endpoint is not connectable (s2 = 1); the camera endpoint is degenerate (s2 = n)
-                auto spec = [&](int i) -> bool {
-                    if (i == 0 || i == n - 1) return false;  // endpoints
-                    return signbit(i < s ? bd_pdfs(R, 1, i, k).y : bd_pdfs(R, 0, n - 1 - i, k).y);
-                };
-                const bool inf0 = s == 0 ? vE.kind == kBdInfinite : env_l0;
-                auto samplable = [&](int s2) -> bool {
-                    if (s2 == 0) return true;
-                    if (s2 >= n) return false;
-                    if (s2 == 1 && inf0) return false;
-                    return !spec(s2 - 1) && !spec(s2);
-                };
-                if (!samplable(s)) continue;
-                float inv = 1.f, r = 1.f;
-                bool ok = true;
-                for (int j = s; j <= n - 2; j++) {  // p_{j+1} / p_s
-                    const float den = qE(j);
-                    if (den == 0.f) { ok = false; break; }
-                    r *= qL(j) / den;
-                    if (r != 0.f && samplable(j + 1)) inv += r * r;
-                }
-                r = 1.f;
-                for (int j = s - 1; j >= 0 && ok; j--) {  // p_j / p_s
-                    const float den = qL(j);
-                    if (den == 0.f) { ok = false; break; }
-                    r *= qE(j) / den;
-                    if (r != 0.f && samplable(j)) inv += r * r;
-                }
-                if (!ok) continue;
-                const f3 C = Cu * (1.f / inv);
-                if (is_zero(C)) continue;
-                if (s == 0) {
-                    splat(film, px, C);
-                    continue;
-                }
-                const int slot = queue_slot(scount);
-                if (slot >= scap) {
-                    atomicOr(err, 2);
-                    continue;
-                }
-                // Scene::visible from the light vertex (include/lm/scene.h:343-364)
+        const BdVtx vE = bd_load(R, 0, t - 1, k);
+        f3 Cu;
+        uint32_t px = eye_px;
+        // fresh local pdfs next to the connection; x_i = L[i] for i < s, E[n-1-i] after
+        float qLs = 0.f, qLs1 = 0.f, qEs1 = 0.f, qEs2 = 0.f, qE0 = 0.f;
+        BdVtx vL;
+        if (s == 0) {
+            // the eye subpath ends on a light, which becomes the light endpoint x_0
+            if (t < 2 || vE.light < 0) continue;
+            const DevLight L = S.lights[vE.light];
+            const float4 e2 = bd_pdfs(R, 0, t - 2, k);
+            f3 Le;
+            float pdir;
+            if (vE.kind == kBdInfinite) {
+                Le = env_eval(S, L, vE.p);
+                pdir = bd_env_pray(S);
+                qLs = 1.f;
+            } else {
+                const f3 wo = bd_toward(R, 0, t - 2, k, vE.p);
+                const bool front = dot(wo, vE.n) > 0.f;
+                Le = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
+                pdir = front ? 1.f / kPi : 0.f;
+                qLs = bd_area_pa(S, vE.light);
+            }
+            Cu = Le * vE.a;  // alpha_L(0) = 1; alpha_E ends on the light endpoint (component pdf 1)
+            qLs1 = fabsf(e2.y) * (pdir * vE.G);
+            qE0 = vE.qf / vE.pc;
+        } else {
+            vL = bd_load(R, 1, s - 1, k);
+            if (vL.kind == kBdInfinite || vE.kind == kBdInfinite) continue;
+            const f3 aL = vL.a / vL.pc, aE = vE.a / vE.pc;
+            if (is_zero(aL) || is_zero(aE)) continue;
+            const f3 dLE = normalize(vE.p - vL.p), dEL = -dLE;
+            const float Gc = [&] {
                 const f3 dv = vE.p - vL.p;
-                const f3 dn = normalize(dv);
-                sq.o[slot] = make_float4(vL.p.x, vL.p.y, vL.p.z, length(dv) * (1.f - kEps));
-                sq.d[slot] = make_float4(dn.x, dn.y, dn.z, 0.f);
-                sq.c[slot] = make_float4(C.x, C.y, C.z, __uint_as_float(px));
+                const float L2 = dot(dv, dv);
+                const f3 dn = dv / sqrtf(L2);
+                const float c2 = vE.kind == kBdCamera ? 1.f : fabsf(dot(vE.n, -dn));
+                return fabsf(dot(vL.n, dn)) * c2 / L2;
+            }();
+            f3 fL, fE;
+            float pLf, pcL = 1.f;
+            if (s == 1) {
+                const DevLight L = S.lights[vL.light];
+                const bool front = dot(dLE, vL.n) > 0.f;
+                fL = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
+                pLf = front ? 1.f / kPi : 0.f;
+            } else {
+                const DevMaterial m = S.mats[vL.mat];
+                const Geom gL = bd_geom(vL);
+                const f3 wi = bd_toward(R, 1, s - 2, k, vL.p);
+                fL = mat_eval(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
+                pLf = mat_pdf(m, gL, wi, dLE, false);
+                pcL = bd_pcomp(m, gL, int(vL.comp), dLE);
+                qEs2 = fabsf(bd_pdfs(R, 1, s - 2, k).y) * (mat_pdf(m, gL, dLE, wi, false) * vL.G);
+            }
+            if (is_zero(fL)) continue;
+            float pEf, pcE = 1.f;
+            if (t == 1) {
+                float rx, ry;
+                if (!raster_pos(S, dEL, rx, ry)) continue;
+                const float J = cam_J(S, dEL);
+                fE = mk(J, J, J);
+                pEf = J;
+                px = pixel_of(P, rx, ry);
+            } else {
+                const DevMaterial m = S.mats[vE.mat];
+                const Geom gE = bd_geom(vE);
+                const f3 wi = bd_toward(R, 0, t - 2, k, vE.p);
+                fE = mat_eval(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
+                pEf = mat_pdf(m, gE, wi, dEL, false);
+                pcE = bd_pcomp(m, gE, int(vE.comp), dEL);
+                qLs1 = fabsf(bd_pdfs(R, 0, t - 2, k).y) * (mat_pdf(m, gE, dEL, wi, false) * vE.G);
+            }
+            Cu = aL * (fL * Gc * fE) * aE;
+            qLs = pcE * (pLf * Gc);
+            qEs1 = pcL * (pEf * Gc);
+        }
+        if (is_zero(Cu)) continue;
+
+        // The ratio sweeps over x_i = L[i] (i < s) and E[n-1-i] (i >= s), one record row (r4:
+        // qf, +-pc_out, prev_rev, G) loaded per step and the neighbours kept in registers.
+        // qL(i): i < s stored (L[i].qf); s, s+1 fresh; beyond, the eye subpath's reverse factors
+        // pc_out(E[e]) * prev_rev(E[e+1]). qE(i): i >= s stored (E[e].qf; x_0 as the endpoint:
+        // qE0); s-1, s-2 fresh; below, pc_out(L[i]) * prev_rev(L[i+1]). Samplable (bidir.h:185-224):
+        // x_{s'-1} and x_{s'} not specular (the sign of pc_out; endpoints never are), an infinite
+        // light endpoint not connected (s' = 1), the camera endpoint degenerate (s' = n).
+        const bool inf0 = s == 0 ? vE.kind == kBdInfinite : env_l0;
+        auto spec_of = [](const float4& q) -> bool { return signbit(q.y); };
+        bool ok = true;
+        float inv = 1.f;
+        {
+            float r = 1.f;
+            float4 prev = make_float4(0.f, 1.f, 0.f, 0.f);
+            float4 cur = bd_pdfs(R, 0, t - 1, k);  // x_s = E[t-1]
+            for (int j = s; j <= n - 2; j++) {     // p_{j+1} / p_s
+                const int e = n - 1 - j;           // x_j = E[e]; x_{j+1} = E[e-1]
+                const float4 nxt = bd_pdfs(R, 0, e - 1, k);
+                const float den = (j == 0) ? qE0 : cur.x;
+                if (den == 0.f) { ok = false; break; }
+                const float num = j == s ? qLs : (j == s + 1 ? qLs1 : fabsf(cur.y) * prev.z);
+                r *= num / den;
+                const bool spec_j = j != 0 && spec_of(cur);
+                const bool spec_j1 = (j + 1 != n - 1) && spec_of(nxt);
+                if (r != 0.f && j + 1 < n && !(j + 1 == 1 && inf0) && !spec_j && !spec_j1) inv += r * r;
+                prev = cur;
+                cur = nxt;
             }
         }
+        if (ok && s > 0) {
+            float r = 1.f;
+            float4 above = make_float4(0.f, 1.f, 0.f, 0.f);
+            float4 cur = bd_pdfs(R, 1, s - 1, k);  // x_{s-1} = L[s-1]
+            for (int j = s - 1; j >= 0; j--) {     // p_j / p_s
+                const float4 below = j > 0 ? bd_pdfs(R, 1, j - 1, k) : make_float4(0.f, 1.f, 0.f, 0.f);
+                const float den = cur.x;
+                if (den == 0.f) { ok = false; break; }
+                const float num = j == s - 1 ? qEs1 : (j == s - 2 ? qEs2 : fabsf(cur.y) * above.z);
+                r *= num / den;
+                // samplable(j): x_{j-1} (L[j-1]) and x_j (L[j]) not specular; x_0 an endpoint
+                const bool samp = j == 0 || (!(j == 1 && inf0) && !(j - 1 != 0 && spec_of(below)) && !spec_of(cur));
+                if (r != 0.f && samp) inv += r * r;
+                above = cur;
+                cur = below;
+            }
+        }
+        if (!ok) continue;
+        const f3 C = Cu * (1.f / inv);
+        if (is_zero(C)) continue;
+        if (s == 0) {
+            splat(film, px, C);
+            continue;
+        }
+        const int slot = queue_slot(scount);
+        if (slot >= scap) {
+            atomicOr(err, 2);
+            continue;
+        }
+        // Scene::visible from the light vertex (include/lm/scene.h:343-364)
+        const f3 dv = vE.p - vL.p;
+        const f3 dn = normalize(dv);
+        sq.o[slot] = make_float4(vL.p.x, vL.p.y, vL.p.z, length(dv) * (1.f - kEps));
+        sq.d[slot] = make_float4(dn.x, dn.y, dn.z, 0.f);
+        sq.c[slot] = make_float4(C.x, C.y, C.z, __uint_as_float(px));
     }
 }
 
@@ -1713,7 +1753,7 @@ struct Workspace {
     DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
     lmgpu_batch* batch = nullptr;  // the regenerating wavefront lmgpu_render_pt runs its job on
     int64_t batch_cap = 0;
-    DevBuf bd_rec, bd_nv, bd_s_o, bd_s_d, bd_s_c;  // lmgpu_render_bdpt: subpath records, connection rays
+    DevBuf bd_rec, bd_nv, bd_s_o, bd_s_d, bd_s_c, bd_items;  // lmgpu_render_bdpt: subpath records, connection rays, strategies
 };
 
 Workspace& workspace(int device) {
@@ -2504,6 +2544,8 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         ws.bd_s_o.alloc(size_t(scap) * 16);
         ws.bd_s_d.alloc(size_t(scap) * 16);
         ws.bd_s_c.alloc(size_t(scap) * 16);
+        const int64_t icap = wave * (int64_t(mv) * (mv + 1) / 2);  // strategies with t >= 1, s + t <= max_verts
+        ws.bd_items.alloc(size_t(icap) * 8);
 
         PtConst P{};
         P.seed = prm->seed;
@@ -2517,7 +2559,7 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
             q[b] = ExtQ{ws.q_o[b].as<float4>(), ws.q_d[b].as<float4>(), ws.q_thr[b].as<float4>(), ws.q_nrm[b].as<float4>(),
                         ws.q_ids[b].as<uint2>()};
         ShadowQ sq{ws.bd_s_o.as<float4>(), ws.bd_s_d.as<float4>(), ws.bd_s_c.as<float4>()};
-        // [0],[1] extension queues, [2] connection rays, [3] error, [4],[5] ray fetch
+        // [0],[1] extension queues, [2] connection rays, [3] error, [4],[5] ray fetch, [6] strategies
         int* cnt = ws.counters.as<int>();
         const int refill = tuning().trace_refill;
         const Fetch f_ext{cnt + 4, cnt + 5, refill}, f_sh{cnt + 5, cnt + 4, refill};
@@ -2533,7 +2575,10 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
         const int g_shade = grid_for(shade_k, kBlock, 0);
-        const int g_con = grid_for(k_bd_connect<2>, kBlock, 0);
+        const int g_items = grid_for(k_bd_items, kBlock, 0);
+        // the "shade_minblocks" tuning key: 2 gives connect its full register budget, more gives 3 blocks
+        auto con_k = tuning().shade_minblocks <= 2 ? k_bd_connect<2> : k_bd_connect<3>;
+        const int g_con = grid_for(con_k, kBlock, 0);
 
         enum { K_GEN = 0, K_EXT = 1, K_SHADE = 2, K_SHADOW = 3 };
         std::vector<std::pair<int, cudaEvent_t>> marks;
@@ -2586,8 +2631,10 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
                 cur = 1 - cur;
             }
             mark(K_SHADE);
-            k_bd_connect<2><<<int(std::min<int64_t>(g_con, (n + kBlock - 1) / kBlock)), kBlock, 0, st>>>(
-                s->dev, P, R, n, prm->min_verts, sq, cnt + 2, scap, film, cnt + 3);
+            LMGPU_CUDA(cudaMemsetAsync(cnt + 6, 0, 4, st));
+            k_bd_items<<<int(std::min<int64_t>(g_items, (n + kBlock - 1) / kBlock)), kBlock, 0, st>>>(
+                R, n, prm->min_verts, mv, ws.bd_items.as<uint2>(), cnt + 6, icap, cnt + 3);
+            con_k<<<g_con, kBlock, 0, st>>>(s->dev, P, R, ws.bd_items.as<uint2>(), cnt + 6, sq, cnt + 2, scap, film, cnt + 3);
             mark(-1);
             mark(K_SHADOW);
             sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, nullptr, 0, nullptr, f_sh, nullptr, nullptr);
@@ -2619,7 +2666,7 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         for (auto& e : marks) cudaEventDestroy(e.second);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        if (herr & 2) throw Error(LMGPU_ERR_INTERNAL, "connection queue overflow");
+        if (herr & 6) throw Error(LMGPU_ERR_INTERNAL, "connection or strategy queue overflow");
         if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed");
         if (stats) {
             *stats = lmgpu_render_stats{};
