@@ -335,6 +335,14 @@ int lmgpu_render_lt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_lt_params*
  * random numbers are the Philox stream keyed by (seed, p, subpath vertex), so consecutive calls
  * with first_path and accumulate add up to one render. A strategy whose own pdf is 0 contributes
  * nothing (the reference asserts it is not 0). */
+#define LMGPU_BDPT_ALL 0      /* renderer::bdpt: every strategy, power heuristic (bidir.h:460-479) */
+#define LMGPU_BDPT_PT_NAIVE 1 /* renderer::pt_naive_path (renderer_bdpt.cpp:63-124): s = 0 only, no light
+                                 subpath, unweighted */
+#define LMGPU_BDPT_PT_NEE 2   /* renderer::pt_nee_path (renderer_bdpt.cpp:129-200): per length the strategy
+                                 s = 1, or s = 0 when the eye vertex it connects is specular; unweighted */
+#define LMGPU_BDPT_LT_NEE 3   /* renderer::lt_nee_path (renderer_bdpt.cpp:205-288): t = 1 only, unweighted */
+#define LMGPU_BDPT_OPT 4      /* renderer::bdptopt (renderer_bdptopt.cpp:315-400, 419-535): every strategy,
+                                 balance heuristic over pdfs without component pdfs */
 typedef struct lmgpu_bdpt_params {
     int64_t num_samples;
     int64_t first_path;
@@ -345,6 +353,8 @@ typedef struct lmgpu_bdpt_params {
     int64_t wave_paths;         /* samples per wave; 0 = 2^20, or fewer so that the connection queue holds
                                    at most 2^28 rays. Each sample of a wave takes 2 * max_verts * 64 bytes of
                                    vertex records and max_verts * (max_verts - 1) / 2 * 48 bytes of queue. */
+    int32_t strategy;           /* LMGPU_BDPT_* */
+    int32_t reserved;
 } lmgpu_bdpt_params;
 
 int lmgpu_render_bdpt(lmgpu_scene* scene, lmgpu_film* film, const lmgpu_bdpt_params* params, void* stream,

@@ -1149,13 +1149,15 @@ struct BdVtx {
     bool spec;
 };
 // Records: 5 float4 per vertex, [subpath][vertex][sample] so that consecutive samples read
-// consecutive records. r4 alone carries what the weight sweep reads (the sign of pc_out marks a
-// specular vertex). nv: vertices per subpath, [subpath][sample].
+// consecutive records. r4 = (qf, +-pc_out, prev_rev, pc) alone carries what the weight sweep
+// reads (the sign of pc_out marks a specular vertex). nv: vertices per subpath, [subpath][sample].
 struct BdRec {
     float4* r;
     int32_t* nv;
     int64_t W;
-    int32_t mv;
+    int32_t mv;          // record rows per subpath
+    int32_t max_e, max_l;  // vertices the eye / light subpath may reach (0: not sampled)
+    int32_t mode;        // LMGPU_BDPT_*
 };
 constexpr int kBdRecWords = 5;
 __device__ inline size_t bd_at(const BdRec& R, int sub, int j, int64_t k) {
@@ -1167,12 +1169,12 @@ __device__ inline void bd_store(const BdRec& R, int sub, int j, int64_t k, const
     q[0] = make_float4(v.p.x, v.p.y, v.p.z, __uint_as_float(word));
     q[1] = make_float4(v.n.x, v.n.y, v.n.z, __int_as_float(v.mat));
     q[2] = make_float4(v.gn.x, v.gn.y, v.gn.z, v.pc);
-    q[3] = make_float4(v.a.x, v.a.y, v.a.z, 0.f);
-    q[4] = make_float4(v.qf, v.spec ? -v.pc_out : v.pc_out, v.prev_rev, v.G);
+    q[3] = make_float4(v.a.x, v.a.y, v.a.z, v.G);
+    q[4] = make_float4(v.qf, v.spec ? -v.pc_out : v.pc_out, v.prev_rev, v.pc);
 }
 // the direction-sampling part of a vertex, written once its next direction is known
 __device__ inline void bd_store_out(const BdRec& R, int sub, int j, int64_t k, const BdVtx& v) {
-    R.r[bd_at(R, sub, j, k) + 4] = make_float4(v.qf, v.spec ? -v.pc_out : v.pc_out, v.prev_rev, v.G);
+    R.r[bd_at(R, sub, j, k) + 4] = make_float4(v.qf, v.spec ? -v.pc_out : v.pc_out, v.prev_rev, v.pc);
 }
 __device__ inline BdVtx bd_load(const BdRec& R, int sub, int j, int64_t k) {
     const float4* q = R.r + bd_at(R, sub, j, k);
@@ -1188,11 +1190,11 @@ __device__ inline BdVtx bd_load(const BdRec& R, int sub, int j, int64_t k) {
     v.gn = mk(r2.x, r2.y, r2.z);
     v.pc = r2.w;
     v.a = mk(r3.x, r3.y, r3.z);
+    v.G = r3.w;
     v.qf = r4.x;
     v.pc_out = fabsf(r4.y);
     v.spec = signbit(r4.y);
     v.prev_rev = r4.z;
-    v.G = r4.w;
     return v;
 }
 __device__ inline float4 bd_pdfs(const BdRec& R, int sub, int j, int64_t k) { return R.r[bd_at(R, sub, j, k) + 4]; }
@@ -1234,7 +1236,13 @@ __global__ void __launch_bounds__(kBlock) k_bd_generate(const __grid_constant__ 
         bd_store(R, 0, 0, i, c);
         R.nv[i] = 1;
         const f3 de = primary_dir(S, u[4], u[5]);
-        push_ext<false>(q, qcount, S.cam_p, de, mk(1, 1, 1), cam_pdf(S, de), mk(0, 0, 0), kBdDegOrigin, uint32_t(path), uint32_t(i), 0u);
+        if (R.max_e >= 2)
+            push_ext<false>(q, qcount, S.cam_p, de, mk(1, 1, 1), cam_pdf(S, de), mk(0, 0, 0), kBdDegOrigin, uint32_t(path), uint32_t(i),
+                            0u);
+        if (R.max_l == 0) {  // renderer::pt_naive_path samples no light subpath
+            R.nv[R.W + i] = 0;
+            continue;
+        }
         rng_slots(P.seed, path, kBdLightBase, 0, 2, u);
         f3 o, d, w, ln = mk(0, 0, 0);
         int li = 0;
@@ -1258,7 +1266,7 @@ __global__ void __launch_bounds__(kBlock) k_bd_generate(const __grid_constant__ 
         }
         bd_store(R, 1, 0, i, l);
         R.nv[R.W + i] = 1;
-        if (is_zero(w)) continue;
+        if (is_zero(w) || R.max_l < 2) continue;
         push_ext<false>(q, qcount, o, d, w, pdir, l.n, kBdLightSub | (l.kind == kBdInfinite ? kBdInfOrigin : 0u), uint32_t(path),
                         uint32_t(i), 0u);
     }
@@ -1323,7 +1331,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_co
         v.spec = mat_specular(m);
         bd_store(R, sub, j + 1, slot, v);
         R.nv[sub * R.W + slot] = j + 2;
-        if (j + 2 >= P.max_verts) continue;
+        if (j + 2 >= (sub ? R.max_l : R.max_e)) continue;
         rng_slots(P.seed, ids.x, base + uint32_t(j + 1), 2, 1, u + 8);
         // toward the previous vertex (bidir.h:530): from the positions, or back along an
         // infinite origin's direction
@@ -1353,7 +1361,10 @@ __global__ void __launch_bounds__(kBlock) k_bd_items(BdRec R, int64_t count, int
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
     for (int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w * 32 < count; w += nwarps) {
         const int64_t k = w * 32 + lane;
-        const int nE = k < count ? R.nv[k] : 0, nL = k < count ? R.nv[R.W + k] : 0;
+        // strategy bounds of the mode: lt_nee_path connects only to the camera (t = 1),
+        // pt_nee_path only the light endpoint or nothing (s <= 1)
+        const int nE = k < count ? (R.mode == LMGPU_BDPT_LT_NEE ? min(R.nv[k], 1) : R.nv[k]) : 0;
+        const int nL = k < count ? (R.mode == LMGPU_BDPT_PT_NEE ? min(R.nv[R.W + k], 1) : R.nv[R.W + k]) : 0;
         int mine = 0;
         for (int t = 1; t <= nE; t++) mine += max(0, min(nL, max_verts - t) - max(0, min_verts - t) + 1);
         int tot = mine, tmax = nE, smax = nL;
@@ -1396,6 +1407,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
         const int s = int(item.y & 0xffu), t = int(item.y >> 8);
         const int n = s + t;
         const int nL = R.nv[R.W + k];
+        const bool opt = R.mode == LMGPU_BDPT_OPT;
+        const bool weighted = opt || R.mode == LMGPU_BDPT_ALL;  // the path-structure renderers take one strategy per length
         uint32_t eye_px = 0;
         if (t >= 2) {  // bidir.h:167-171: the raster position of the camera's first edge
             const float4 r0 = R.r[bd_at(R, 0, 1, k)];
@@ -1415,8 +1428,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
         if (s == 0) {
             // the eye subpath ends on a light, which becomes the light endpoint x_0
             if (t < 2 || vE.light < 0) continue;
-            const DevLight L = S.lights[vE.light];
             const float4 e2 = bd_pdfs(R, 0, t - 2, k);
+            // renderer::pt_nee_path takes s = 0 only in place of s = 1 when the eye vertex that
+            // s = 1 would connect is specular (renderer_bdpt.cpp:160-172)
+            if (R.mode == LMGPU_BDPT_PT_NEE && (nL < 1 || !signbit(e2.y))) continue;
+            const DevLight L = S.lights[vE.light];
             f3 Le;
             float pdir;
             if (vE.kind == kBdInfinite) {
@@ -1430,12 +1446,15 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 pdir = front ? 1.f / kPi : 0.f;
                 qLs = bd_area_pa(S, vE.light);
             }
-            Cu = Le * vE.a;  // alpha_L(0) = 1; alpha_E ends on the light endpoint (component pdf 1)
-            qLs1 = fabsf(e2.y) * (pdir * vE.G);
+            // alpha_L(0) = 1; alpha_E ends on the light endpoint, component pdf 1 (bidir.h); bdptopt
+            // keeps the vertex's own component weight (renderer_bdptopt.cpp:265-270)
+            Cu = opt ? Le * (vE.a / vE.pc) : Le * vE.a;
+            qLs1 = (opt ? 1.f : fabsf(e2.y)) * (pdir * vE.G);
             qE0 = vE.qf / vE.pc;
         } else {
             vL = bd_load(R, 1, s - 1, k);
             if (vL.kind == kBdInfinite || vE.kind == kBdInfinite) continue;
+            if (R.mode == LMGPU_BDPT_PT_NEE && vE.spec) continue;  // replaced by s = 0 (above)
             const f3 aL = vL.a / vL.pc, aE = vE.a / vE.pc;
             if (is_zero(aL) || is_zero(aE)) continue;
             const f3 dLE = normalize(vE.p - vL.p), dEL = -dLE;
@@ -1460,7 +1479,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 fL = mat_eval(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
                 pLf = mat_pdf(m, gL, wi, dLE, false);
                 pcL = bd_pcomp(m, gL, int(vL.comp), dLE);
-                qEs2 = fabsf(bd_pdfs(R, 1, s - 2, k).y) * (mat_pdf(m, gL, dLE, wi, false) * vL.G);
+                qEs2 = (opt ? 1.f : fabsf(bd_pdfs(R, 1, s - 2, k).y)) * (mat_pdf(m, gL, dLE, wi, false) * vL.G);
             }
             if (is_zero(fL)) continue;
             float pEf, pcE = 1.f;
@@ -1478,11 +1497,11 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 fE = mat_eval(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
                 pEf = mat_pdf(m, gE, wi, dEL, false);
                 pcE = bd_pcomp(m, gE, int(vE.comp), dEL);
-                qLs1 = fabsf(bd_pdfs(R, 0, t - 2, k).y) * (mat_pdf(m, gE, dEL, wi, false) * vE.G);
+                qLs1 = (opt ? 1.f : fabsf(bd_pdfs(R, 0, t - 2, k).y)) * (mat_pdf(m, gE, dEL, wi, false) * vE.G);
             }
             Cu = aL * (fL * Gc * fE) * aE;
-            qLs = pcE * (pLf * Gc);
-            qEs1 = pcL * (pEf * Gc);
+            qLs = (opt ? 1.f : pcE) * (pLf * Gc);
+            qEs1 = (opt ? 1.f : pcL) * (pEf * Gc);
         }
         if (is_zero(Cu)) continue;
 
@@ -1495,39 +1514,42 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
         // light endpoint not connected (s' = 1), the camera endpoint degenerate (s' = n).
         const bool inf0 = s == 0 ? vE.kind == kBdInfinite : env_l0;
         auto spec_of = [](const float4& q) -> bool { return signbit(q.y); };
+        // bdptopt's cached pdfs leave out the component pdfs (renderer_bdptopt.cpp:145-215)
+        auto fwd = [&](const float4& q) -> float { return opt ? q.x / q.w : q.x; };
+        auto cout = [&](const float4& q) -> float { return opt ? 1.f : fabsf(q.y); };
         bool ok = true;
         float inv = 1.f;
-        {
+        if (weighted) {
             float r = 1.f;
             float4 prev = make_float4(0.f, 1.f, 0.f, 0.f);
             float4 cur = bd_pdfs(R, 0, t - 1, k);  // x_s = E[t-1]
             for (int j = s; j <= n - 2; j++) {     // p_{j+1} / p_s
                 const int e = n - 1 - j;           // x_j = E[e]; x_{j+1} = E[e-1]
                 const float4 nxt = bd_pdfs(R, 0, e - 1, k);
-                const float den = (j == 0) ? qE0 : cur.x;
+                const float den = (j == 0) ? qE0 : fwd(cur);
                 if (den == 0.f) { ok = false; break; }
-                const float num = j == s ? qLs : (j == s + 1 ? qLs1 : fabsf(cur.y) * prev.z);
+                const float num = j == s ? qLs : (j == s + 1 ? qLs1 : cout(cur) * prev.z);
                 r *= num / den;
                 const bool spec_j = j != 0 && spec_of(cur);
                 const bool spec_j1 = (j + 1 != n - 1) && spec_of(nxt);
-                if (r != 0.f && j + 1 < n && !(j + 1 == 1 && inf0) && !spec_j && !spec_j1) inv += r * r;
+                if (r != 0.f && j + 1 < n && !(j + 1 == 1 && inf0) && !spec_j && !spec_j1) inv += opt ? r : r * r;
                 prev = cur;
                 cur = nxt;
             }
         }
-        if (ok && s > 0) {
+        if (weighted && ok && s > 0) {
             float r = 1.f;
             float4 above = make_float4(0.f, 1.f, 0.f, 0.f);
             float4 cur = bd_pdfs(R, 1, s - 1, k);  // x_{s-1} = L[s-1]
             for (int j = s - 1; j >= 0; j--) {     // p_j / p_s
                 const float4 below = j > 0 ? bd_pdfs(R, 1, j - 1, k) : make_float4(0.f, 1.f, 0.f, 0.f);
-                const float den = cur.x;
+                const float den = fwd(cur);
                 if (den == 0.f) { ok = false; break; }
-                const float num = j == s - 1 ? qEs1 : (j == s - 2 ? qEs2 : fabsf(cur.y) * above.z);
+                const float num = j == s - 1 ? qEs1 : (j == s - 2 ? qEs2 : cout(cur) * above.z);
                 r *= num / den;
                 // samplable(j): x_{j-1} (L[j-1]) and x_j (L[j]) not specular; x_0 an endpoint
                 const bool samp = j == 0 || (!(j == 1 && inf0) && !(j - 1 != 0 && spec_of(below)) && !spec_of(cur));
-                if (r != 0.f && samp) inv += r * r;
+                if (r != 0.f && samp) inv += opt ? r : r * r;
                 above = cur;
                 cur = below;
             }
@@ -2523,6 +2545,7 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         if (prm->num_samples <= 0 || prm->first_path < 0 || prm->max_verts < 2 || prm->min_verts < 0)
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "num_samples must be > 0, first_path >= 0, max_verts >= 2 and min_verts >= 0");
         if (prm->max_verts > kBdMaxVerts) throw Error(LMGPU_ERR_UNSUPPORTED, "max_verts above 64");
+        if (prm->strategy < LMGPU_BDPT_ALL || prm->strategy > LMGPU_BDPT_OPT) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown strategy");
         if (prm->first_path + prm->num_samples > (int64_t(1) << 32)) throw Error(LMGPU_ERR_UNSUPPORTED, "sample index above 2^32");
         if (prm->accumulate && f->split) throw Error(LMGPU_ERR_UNSUPPORTED, "film holds split passes");
         ensure_film(f);
@@ -2553,7 +2576,11 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         P.spp = 1;
         P.w = f->w;
         P.h = f->h;
-        const BdRec R{ws.bd_rec.as<float4>(), ws.bd_nv.as<int32_t>(), wave, mv};
+        // subpath lengths of the mode (the reference samples a 1-vertex-limited subpath up to its
+        // first hit; that hit is never connected, so it is not traced here)
+        const int max_e = prm->strategy == LMGPU_BDPT_LT_NEE ? 1 : mv;
+        const int max_l = prm->strategy == LMGPU_BDPT_PT_NAIVE ? 0 : (prm->strategy == LMGPU_BDPT_PT_NEE ? 1 : mv);
+        const BdRec R{ws.bd_rec.as<float4>(), ws.bd_nv.as<int32_t>(), wave, mv, max_e, max_l, prm->strategy};
         ExtQ q[2];
         for (int b = 0; b < 2; b++)
             q[b] = ExtQ{ws.q_o[b].as<float4>(), ws.q_d[b].as<float4>(), ws.q_thr[b].as<float4>(), ws.q_nrm[b].as<float4>(),

@@ -20,7 +20,8 @@ functests use to build scenes and render them:
 
 Every accel key the reference registers (accel::sahbvh, accel::nanort, accel::embree,
 accel::embreeinstanced) and accel::gpu resolve to the GB300 8-wide BVH; renderer::pt,
-renderer::lt, renderer::bdpt and renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a
+renderer::lt, renderer::bdpt (and the path-structure renderers of renderer_bdpt.cpp,
+renderer::bdptopt) and renderer::raycast resolve to the CUDA renderers. There is no CPU fallback: a
 missing liblmgpu.so raises at the first render or build.
 """
 from __future__ import annotations
@@ -1317,6 +1318,8 @@ class RendererBDPT(_SpiRenderer):
     reference: scene, output, min_verts (default 2), max_verts, seed, scheduler ('sample' with
     num_samples, or 'time'). GPU extra: wave_paths (samples per wave)."""
 
+    strategy = 0  # LMGPU_BDPT_ALL
+
     def construct(self, prop):
         self._spi_construct(prop)
         self.min_verts = int(prop.get("min_verts", 2))
@@ -1325,7 +1328,37 @@ class RendererBDPT(_SpiRenderer):
         p = N.BDPTParams()
         p.num_samples, p.first_path, p.min_verts, p.max_verts = n, first, self.min_verts, self.max_verts
         p.seed, p.accumulate, p.wave_paths = self.seed & 0xFFFFFFFF, int(accumulate), self.wave_paths
+        p.strategy = self.strategy
         N.check(N.lib().lmgpu_render_bdpt(self.scene._h, self.film._h, C.byref(p), None, C.byref(st)))
+
+
+@_reg("renderer::pt_naive_path")
+class RendererPTNaivePath(RendererBDPT):
+    """renderer::pt_naive_path (renderer_bdpt.cpp:63-124): path tracing through the path
+    structure, the eye subpath's hits on lights only (s = 0), unweighted."""
+    strategy = 1
+
+
+@_reg("renderer::pt_nee_path")
+class RendererPTNEEPath(RendererBDPT):
+    """renderer::pt_nee_path (renderer_bdpt.cpp:129-200): per path length the light endpoint
+    connected to the eye subpath (s = 1), or the eye subpath's own hit on a light when that eye
+    vertex is specular (s = 0), unweighted."""
+    strategy = 2
+
+
+@_reg("renderer::lt_nee_path")
+class RendererLTNEEPath(RendererBDPT):
+    """renderer::lt_nee_path (renderer_bdpt.cpp:205-288): light subpath vertices connected to the
+    camera (t = 1), unweighted."""
+    strategy = 3
+
+
+@_reg("renderer::bdptopt")
+class RendererBDPTOpt(RendererBDPT):
+    """renderer::bdptopt (renderer_bdptopt.cpp:419-535): every strategy, weighted by the balance
+    heuristic over pdfs without component pdfs (renderer_bdptopt.cpp:315-400)."""
+    strategy = 4
 
 
 @_reg("renderer::lt", "renderer::lt_gpu")

@@ -72,7 +72,8 @@ class LTParams(C.Structure):
 
 class BDPTParams(C.Structure):
     _fields_ = [("num_samples", C.c_int64), ("first_path", C.c_int64), ("min_verts", C.c_int32), ("max_verts", C.c_int32),
-                ("seed", C.c_uint32), ("accumulate", C.c_int32), ("wave_paths", C.c_int64)]
+                ("seed", C.c_uint32), ("accumulate", C.c_int32), ("wave_paths", C.c_int64), ("strategy", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class RenderStats(C.Structure):

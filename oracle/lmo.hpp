@@ -1517,8 +1517,10 @@ template <typename F> struct Bidir {
         return aL * connection(P, s) * aE;
     }
 
-    // bidir.h:397-449 (pdf_bidir)
-    F pdf(const FullPath& P, int s) const {
+    // bidir.h:397-449 (pdf_bidir). with_comp = false leaves out the component pdfs, as the
+    // cached pdfs of renderer::bdptopt do (renderer_bdptopt.cpp:145-215).
+    F pdf(const FullPath& P, int s, bool with_comp = true) const {
+        auto pcomp = [&](const SceneInteraction<F>& sp, V3F wi, int comp) { return with_comp ? pdf_comp(sp, wi, comp) : F(1); };
         if (!samplable(P, s)) return F(0);
         auto sub = [&](int l, TransDir td) -> F {
             if (l == 0) return F(1);
@@ -1526,12 +1528,12 @@ template <typename F> struct Bidir {
             F p = F(0);
             const auto* v0 = P.at(0, td);
             if (is_connectable(v0->sp)) {
-                p = pdf_position(v0->sp) * pdf_comp(v0->sp, V3F(), v0->comp);
+                p = pdf_position(v0->sp) * pcomp(v0->sp, V3F(), v0->comp);
             } else {
                 const auto* v1 = P.at(1, td);
                 const auto d01 = direction(v0, v1);
-                p = pdf_primary_ray(v0->sp, d01) * geometry_term(v0->sp.geom, v1->sp.geom) * pdf_comp(v0->sp, V3F(), v0->comp) *
-                    pdf_comp(v1->sp, -d01, v1->comp);
+                p = pdf_primary_ray(v0->sp, d01) * geometry_term(v0->sp.geom, v1->sp.geom) * pcomp(v0->sp, V3F(), v0->comp) *
+                    pcomp(v1->sp, -d01, v1->comp);
                 i++;
             }
             for (; i < l - 1; i++) {
@@ -1539,7 +1541,7 @@ template <typename F> struct Bidir {
                 const auto* vn = P.at(i + 1, td);
                 const auto wi = direction(v, P.at(i - 1, td));
                 const auto wo = direction(v, vn);
-                p *= pdf_comp(vn->sp, -wo, vn->comp) * (pdf_dir(v->sp, wi, wo, v->comp) * geometry_term(v->sp.geom, vn->sp.geom));
+                p *= pcomp(vn->sp, -wo, vn->comp) * (pdf_dir(v->sp, wi, wo, v->comp) * geometry_term(v->sp.geom, vn->sp.geom));
             }
             return p;
         };
@@ -1548,20 +1550,25 @@ template <typename F> struct Bidir {
 
     // bidir.h:460-479 (power heuristic over every strategy of the path). The reference asserts a
     // nonzero pdf of the strategy that sampled the path; a zero one contributes nothing here.
-    F mis(const FullPath& P, int s) const {
-        const F ps = pdf(P, s);
+    // balance: renderer_bdptopt.cpp:315-400, the balance heuristic over pdfs without component
+    // pdfs (the same ratios as its cached forward / reverse pdfs).
+    F mis(const FullPath& P, int s, bool balance = false) const {
+        const F ps = pdf(P, s, !balance);
         if (ps == F(0)) return F(0);
         F inv = F(0);
         for (int s2 = 0; s2 <= P.n(); s2++) {
-            const F pi = pdf(P, s2);
+            const F pi = pdf(P, s2, !balance);
             if (pi == F(0)) continue;
             const F r = pi / ps;
-            inv += r * r;
+            inv += balance ? r : r * r;
         }
         return F(1) / inv;
     }
 };
 
+// mode: 0 renderer::bdpt, 1 renderer::pt_naive_path, 2 renderer::pt_nee_path,
+// 3 renderer::lt_nee_path, 4 renderer::bdptopt
+enum BdMode { BD_ALL = 0, BD_PT_NAIVE = 1, BD_PT_NEE = 2, BD_LT_NEE = 3, BD_OPT = 4 };
 struct BDPTParams {
     int w, h;
     long long num_samples;
@@ -1569,6 +1576,7 @@ struct BDPTParams {
     int min_verts, max_verts;
     unsigned int seed;
     int rng_mode;
+    int mode;
 };
 
 template <typename F>
@@ -1590,23 +1598,54 @@ void render_bdpt(const Scene<F>& scene, const BDPTParams& P, double* out, long l
         PathRng rng; rng.mode = P.rng_mode; rng.mt = rngs[tid]; rng.seed = P.seed; rng.path = (uint64_t)(P.first_path + index);
         auto U = [&](int nv, int s) -> double { return rng.mode == 0 ? rng.seq() : rng.slot(nv, s); };
         long long& nrays = rays[tid];
-        const auto E = B.sample_subpath(U, kBdEye, P.max_verts, TransDir::EL, nrays);
-        const auto L = B.sample_subpath(U, kBdLight, P.max_verts, TransDir::LE, nrays);
+        // subpath lengths: renderer_bdpt.cpp:72, 143-144, 219-220; renderer_bdptopt.cpp:487-488
+        const int maxE = P.mode == BD_LT_NEE ? 1 : P.max_verts;
+        const int maxL = P.mode == BD_PT_NEE ? 1 : P.max_verts;
+        const auto E = B.sample_subpath(U, kBdEye, maxE, TransDir::EL, nrays);
+        const auto L = P.mode == BD_PT_NAIVE ? std::vector<BdVert<F>>() : B.sample_subpath(U, kBdLight, maxL, TransDir::LE, nrays);
         const int nE = int(E.size()), nL = int(L.size());
-        for (int s = 0; s <= nL; s++) {
-            for (int t = 0; t <= nE; t++) {
-                const int k = s + t;
+        auto contribute = [&](int s, int t, bool weighted) {
+            const auto path = B.connect(L, E, s, t, nrays);
+            if (!path) return;
+            auto Cu = B.weight(*path, s);
+            if (P.mode == BD_OPT && s == 0 && path->vs.front().sp.type == SI_Light && E[t - 1].sp.type == SI_Surface) {
+                // bdptopt's eye alpha keeps the last vertex's component weight (renderer_bdptopt.cpp:265-270)
+                const auto& v = E[t - 1];
+                Cu = Cu / B.pdf_comp(v.sp, Bidir<F>::direction(&v, &E[t - 2]), v.comp);
+            }
+            if (is_zero(Cu)) return;
+            const F w = weighted ? B.mis(*path, s, P.mode == BD_OPT) : F(1);
+            // bidir.h:167-171: the raster position of the camera's first edge
+            const auto* vE = path->at(0, TransDir::EL);
+            const auto rp = scene.camera().raster_position(Bidir<F>::direction(vE, path->at(1, TransDir::EL)));
+            if (!rp) return;  // the reference dereferences it unchecked; only rounding reaches here
+            film.splat(*rp, w * Cu);
+        };
+        if (P.mode == BD_ALL || P.mode == BD_OPT) {
+            for (int s = 0; s <= nL; s++) {
+                for (int t = 0; t <= nE; t++) {
+                    const int k = s + t;
+                    if (k < P.min_verts || P.max_verts < k) continue;
+                    contribute(s, t, true);
+                }
+            }
+        } else if (P.mode == BD_PT_NAIVE) {  // renderer_bdpt.cpp:77-105
+            for (int t = 2; t <= nE; t++) {
+                if (t < P.min_verts || P.max_verts < t) continue;
+                contribute(0, t, false);
+            }
+        } else {  // renderer_bdpt.cpp:149-186 (pt_nee_path) and 228-278 (lt_nee_path)
+            for (int k = 2; k <= nL + nE; k++) {
                 if (k < P.min_verts || P.max_verts < k) continue;
-                const auto path = B.connect(L, E, s, t, nrays);
-                if (!path) continue;
-                const auto Cu = B.weight(*path, s);
-                if (is_zero(Cu)) continue;
-                const F w = B.mis(*path, s);
-                // bidir.h:167-171: the raster position of the camera's first edge
-                const auto* vE = path->at(0, TransDir::EL);
-                const auto rp = scene.camera().raster_position(Bidir<F>::direction(vE, path->at(1, TransDir::EL)));
-                if (!rp) continue;  // the reference dereferences it unchecked; only rounding reaches here
-                film.splat(*rp, w * Cu);
+                int s = P.mode == BD_PT_NEE ? 1 : k - 1;
+                int t = k - s;
+                if (s > nL || t > nE) continue;
+                if (P.mode == BD_PT_NEE && B.is_specular(E[t - 1].sp, E[t - 1].comp)) {
+                    s = 0;
+                    t = k;
+                    if (s > nL || t > nE) continue;
+                }
+                contribute(s, t, false);
             }
         }
     }

@@ -274,12 +274,12 @@ int lmo_render_lt(void* p, int w, int hgt, long long num_samples, long long firs
 }
 
 int lmo_render_bdpt(void* p, int w, int hgt, long long num_samples, long long first_path, int min_verts, int max_verts,
-                    unsigned int seed, int rng_mode, double* out, long long* rays, int nthreads, double* secs) {
+                    unsigned int seed, int rng_mode, int mode, double* out, long long* rays, int nthreads, double* secs) {
     auto* h = static_cast<Handle*>(p);
     return dispatch(h, [&](auto& S) -> int {
         using F = typename std::decay_t<decltype(S)>::Float;
         const auto t0 = std::chrono::steady_clock::now();
-        BDPTParams P{w, hgt, num_samples, first_path, min_verts, max_verts, seed, rng_mode};
+        BDPTParams P{w, hgt, num_samples, first_path, min_verts, max_verts, seed, rng_mode, mode};
         render_bdpt<F>(S, P, out, rays, nthreads > 0 ? nthreads : omp_get_max_threads());
         if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return 0;

@@ -57,7 +57,7 @@ def lib() -> C.CDLL:
         L.lmo_render_lt.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int, C.c_uint, C.c_int, dp,
                                     C.POINTER(C.c_longlong), C.c_int, dp]
         L.lmo_render_bdpt.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_longlong, C.c_int, C.c_int, C.c_uint, C.c_int,
-                                      dp, C.POINTER(C.c_longlong), C.c_int, dp]
+                                      C.c_int, dp, C.POINTER(C.c_longlong), C.c_int, dp]
         L.lmo_philox_uniform.restype = C.c_float
         L.lmo_philox_uniform.argtypes = [C.c_uint, C.c_ulonglong, C.c_uint, C.c_uint]
         L.lmo_max_threads.restype = C.c_int
@@ -209,15 +209,20 @@ class OracleScene:
         return out, rays.value, s.value
 
 
-    def render_bdpt(self, w, h, num_samples, max_verts, seed=0, min_verts=2, first_path=0, rng="philox", nthreads: int = 0):
-        """renderer::bdpt: returns (image (h,w,3) scaled by w*h / num_samples, rays, seconds) for samples
+    BDPT_MODES = {"bdpt": 0, "pt_naive_path": 1, "pt_nee_path": 2, "lt_nee_path": 3, "bdptopt": 4}
+
+    def render_bdpt(self, w, h, num_samples, max_verts, seed=0, min_verts=2, first_path=0, rng="philox", nthreads: int = 0,
+                    mode: str = "bdpt"):
+        """renderer::bdpt (or, by mode, renderer::pt_naive_path / pt_nee_path / lt_nee_path / bdptopt):
+        returns (image (h,w,3) scaled by w*h / num_samples, rays, seconds) for samples
         [first_path, first_path + num_samples), each one eye and one light subpath."""
         out = np.zeros((h, w, 3))
         rays = C.c_longlong()
         s = C.c_double()
         rm = {"mt19937": 0, "philox": 1}[rng]
         _chk(lib().lmo_render_bdpt(self.h, w, h, num_samples, first_path, min_verts, max_verts, seed & 0xFFFFFFFF, rm,
-                                   out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(rays), nthreads, C.byref(s)))
+                                   self.BDPT_MODES[mode], out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(rays), nthreads,
+                                   C.byref(s)))
         return out, rays.value, s.value
 
 

@@ -62,6 +62,21 @@ def test_oracle_bdpt_white_furnace(lm, oracle_mod):
     assert direct[bg.max(axis=2) == 0].mean() < 0.01   # silhouette pixels may see some environment
 
 
+@pytest.mark.parametrize("mode,n", [("bdptopt", 200_000), ("pt_naive_path", 2_000_000), ("pt_nee_path", 400_000),
+                                    ("lt_nee_path", 1_000_000)])
+def test_oracle_bidir_renderers_match_pt_box(lm, oracle_mod, mode, n):
+    """The path-structure renderers (renderer_bdpt.cpp:63-288) and renderer::bdptopt estimate the
+    path tracer's image where their strategies cover all transport: the closed box, one area
+    light not seen directly, diffuse walls."""
+    from lightmetrica import synthetic as syn
+    scene, _ = syn.box_scene(w=16, h=16, prefix="bdm_")
+    S = oracle_mod.from_lm_scene(scene, double=True)
+    S.build()
+    pt, _, _, _ = S.render_pt(16, 16, 2048, 6, seed=1)
+    img, _, _ = S.render_bdpt(16, 16, n, 6, seed=3, mode=mode)
+    assert abs(img.mean() / pt.mean() - 1) < 0.02, img.mean() / pt.mean()
+
+
 def test_renderer_bdpt_props(lm):
     from lightmetrica import synthetic as syn
     scene, film = syn.box_scene(w=8, h=8, prefix="bdp_")
@@ -115,6 +130,25 @@ def test_bdpt_spheres_env_glass_matches_oracle(lm, oracle_mod):
     S = oracle_mod.from_lm_scene(scene, double=True)
     S.build()
     ref, _, _ = S.render_bdpt(32, 24, 1 << 18, 8, seed=9)
+    assert ref.sum() > 0
+    assert _rel_l1(gpu, ref) < 2e-3, _rel_l1(gpu, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["bdptopt", "pt_naive_path", "pt_nee_path", "lt_nee_path"])
+def test_bidir_renderers_match_oracle(lm, oracle_mod, mode):
+    """Each strategy mode against the oracle with matched streams on the spheres scene (glass
+    vertices trigger pt_nee_path's s = 0 replacement; the environment and the glass are what
+    pt_nee_path and lt_nee_path cannot reach, identically on both sides)."""
+    from lightmetrica import synthetic as syn
+    scene, film, _ = syn.spheres_scene(n_spheres=10, subdiv=3, ground_quads=8, w=32, h=24, prefix="bdmg_")
+    scene.build()
+    lm.load_renderer("bdmg_" + mode, mode, scene=scene, output=film, max_verts=8, seed=9, scheduler="sample",
+                     num_samples=1 << 18).render()
+    gpu = film.buffer().astype(np.float64)
+    S = oracle_mod.from_lm_scene(scene, double=True)
+    S.build()
+    ref, _, _ = S.render_bdpt(32, 24, 1 << 18, 8, seed=9, mode=mode)
     assert ref.sum() > 0
     assert _rel_l1(gpu, ref) < 2e-3, _rel_l1(gpu, ref)
 
