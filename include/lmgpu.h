@@ -222,6 +222,9 @@ int lmgpu_film_create(lmgpu_film** out, int32_t w, int32_t h);
 int lmgpu_film_destroy(lmgpu_film* film);
 int lmgpu_film_clear(lmgpu_film* film);
 /* Film::buffer (film_bitmap.cpp:202-208): copies h x w x 3 floats to host memory. */
+/* Every pixel set to rgb (3 floats): renderer::blank's Film::clear + set_pixel loop
+ * (src/renderer/renderer_blank.cpp:36-45). */
+int lmgpu_film_fill(lmgpu_film* film, const float* rgb);
 int lmgpu_film_read(lmgpu_film* film, float* out_rgb);
 /* Device pointer to the h x w x 3 fp32 pixels (valid until the film is destroyed). */
 int lmgpu_film_device_ptr(lmgpu_film* film, void** out);

@@ -2134,6 +2134,27 @@ int lmgpu_film_rel_mse(lmgpu_film* f, double eps, double* rel_mse) {
     });
 }
 
+int lmgpu_film_fill(lmgpu_film* f, const float* rgb) {
+    return guarded([&] {
+        if (!f || !rgb) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        ensure_film(f);
+        const size_t n = size_t(f->w) * f->h;
+        std::vector<float> px(n * 3);
+        for (size_t i = 0; i < n; i++) {
+            px[3 * i] = rgb[0];
+            px[3 * i + 1] = rgb[1];
+            px[3 * i + 2] = rgb[2];
+        }
+        LMGPU_CUDA(cudaMemcpy(f->sum.p, px.data(), n * 3 * 4, cudaMemcpyHostToDevice));
+        LMGPU_CUDA(cudaMemcpy(f->out.p, px.data(), n * 3 * 4, cudaMemcpyHostToDevice));
+        if (f->sum_odd.p) LMGPU_CUDA(cudaMemset(f->sum_odd.p, 0, n * 3 * 4));
+        f->accumulated_spp = 0;
+        f->scale = 1.0;
+        f->split = false;
+        f->passes_even = f->passes_odd = 0;
+    });
+}
+
 int lmgpu_film_read(lmgpu_film* f, float* out_rgb) {
     return guarded([&] {
         if (!f || !out_rgb) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");

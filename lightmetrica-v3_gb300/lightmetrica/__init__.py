@@ -1151,6 +1151,20 @@ _SAMPLING = {"naive": 0, "nee": 1, "mis": 2}
 _PRIMARY = {"pixel": 0, "image": 1}
 
 
+@_reg("renderer::blank")
+class RendererBlank(Component):
+    """renderer::blank (src/renderer/renderer_blank.cpp:14-47): every pixel of the output film
+    set to `color`."""
+
+    def construct(self, prop):
+        self.color = [float(x) for x in _vec3(_req(prop, "color"))]
+        self.film = _resolve(_req(prop, "output"))
+
+    def render(self) -> dict:
+        N.check(N.lib().lmgpu_film_fill(self.film._h, (C.c_float * 3)(*self.color)))
+        return {}
+
+
 @_reg("renderer::raycast", "renderer::raycast_gpu")
 class RendererRaycast(Component):
     """renderer::raycast (src/renderer/renderer_raycast.cpp:48-101)."""

@@ -9,7 +9,7 @@ def test_registered_keys(lm):
     for k in ["accel::sahbvh", "accel::nanort", "accel::embree", "accel::embreeinstanced", "accel::gpu",
               "renderer::pt", "renderer::lt", "renderer::raycast", "film::bitmap", "camera::pinhole", "mesh::raw",
               "model::wavefrontobj", "material::mixture_wavefrontobj", "renderer::bdpt", "renderer::bdptopt",
-              "renderer::pt_naive_path", "renderer::pt_nee_path", "renderer::lt_nee_path",
+              "renderer::pt_naive_path", "renderer::pt_nee_path", "renderer::lt_nee_path", "renderer::blank",
               "material::diffuse", "material::glossy", "material::glass", "material::mirror",
               "light::area", "light::envconst", "light::env", "scene::default"]:
         assert k in keys
