@@ -122,6 +122,14 @@ __device__ inline uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 
 
 // Three-input min / max (one instruction each on sm_100 and later; exact, like the two-input
 // forms, so the slab test's result does not change).
+#ifndef LMGPU_TRAV_SPLIT
+// persistent traversal steps: 0 = a node and all its entered leaf triangles per step (trav_step);
+// 1 = a node or one triangle per step (trav_step_split); 2 = as 1, and a closest-hit step that
+// tests a node's last pending triangle goes on to the next node (measured on the displaced-sphere
+// frame: extension 70.7 -> 64.5 ms, shadow 27.5 -> 27.2 ms per 64-spp frame)
+#define LMGPU_TRAV_SPLIT 2
+#endif
+
 #ifndef LMGPU_NO_MINMAX3
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
     float d;
@@ -177,6 +185,10 @@ struct Trav {
     f3 wo, wd;
     int inst_sp;
     int32_t id_base;
+#if LMGPU_TRAV_SPLIT
+    // split steps: the entered leaf triangles of the last node, tested one per step
+    uint32_t tri_base, tri_mask;
+#endif
 };
 
 __device__ inline void trav_set_ray(Trav& s, f3 o, f3 d) {
@@ -203,6 +215,9 @@ __device__ inline void trav_init(Trav& s, f3 o, f3 d, float tmin, float tmax) {
     s.ntri = 0;
     s.inst_sp = -1;
     s.id_base = 0;
+#if LMGPU_TRAV_SPLIT
+    s.tri_mask = 0u;
+#endif
 }
 
 // Visits s.node (testing the triangles of every leaf child the ray enters) and moves to the next
@@ -328,6 +343,153 @@ __device__ __forceinline__ bool trav_step(const Bvh8& bvh, Trav& s, uint32_t* st
     return false;
 }
 
+#if LMGPU_TRAV_SPLIT
+// trav_step with finer steps (after the triangle-postponing traversal of Ylitie et al., HPG 2017):
+// a node step records the triangles of the leaf children the ray enters as a mask; each later
+// step tests one of them; the next node is visited once the mask is empty. The order of tests is
+// trav_step's, so the result is the same; a warp's lanes now diverge between a node step and
+// one triangle test instead of waiting for the lane with the most triangles.
+template <bool kAnyHit, bool kCount, bool kTwoLevel = false>
+__device__ __forceinline__ bool trav_step_split(const Bvh8& bvh, Trav& s, uint32_t* stk_base, uint32_t* stk_bits, int stride,
+                                                int* err) {
+    if (s.tri_mask) {
+        const int j = __ffs(s.tri_mask) - 1;
+        s.tri_mask &= s.tri_mask - 1u;
+        const float4* tp = bvh.tris + size_t(s.tri_base + uint32_t(j)) * 3;
+        const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        if (kCount) s.ntri++;
+        float t, u, v;
+        if (tri_test(s.o, s.d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), s.tmin, s.best.t, t, u, v)) {
+            const int32_t id = (kTwoLevel ? s.id_base : 0) + int32_t(__float_as_uint(c.y));
+            if (kAnyHit) {
+                s.best = TraceHit{t, u, v, id};
+                return true;
+            }
+            if (t < s.best.t || s.best.id < 0 || id < s.best.id) s.best = TraceHit{t, u, v, id};
+        }
+        // closest hit (mode 2): after the last pending triangle go on to the next node in the same
+        // step; any hit keeps one triangle per step (measured faster for shadow rays)
+        if (kAnyHit || LMGPU_TRAV_SPLIT != 2) return s.tri_mask == 0u && s.node == 0xffffffffu;
+        if (s.tri_mask != 0u) return false;
+    }
+    if (s.node == 0xffffffffu) return true;
+    if (s.node >= bvh.num_nodes || s.nvis >= bvh.max_visits) { *err = 2; return true; }
+    const uint4* np = bvh.nodes + size_t(s.node) * 5;
+    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1);
+    s.nvis++;
+    if (kTwoLevel && (w0.w & 0xffu) == 0xffu) {
+        const float4* ip = bvh.inst + size_t(w1.x) * 4;
+        const float4 r0 = __ldg(ip), r1 = __ldg(ip + 1), r2 = __ldg(ip + 2);
+        const uint4 m = __ldg(reinterpret_cast<const uint4*>(ip + 3));
+        s.wo = s.o;
+        s.wd = s.d;
+        const f3 lo = {r0.x * s.o.x + r0.y * s.o.y + r0.z * s.o.z + r0.w, r1.x * s.o.x + r1.y * s.o.y + r1.z * s.o.z + r1.w,
+                       r2.x * s.o.x + r2.y * s.o.y + r2.z * s.o.z + r2.w};
+        const f3 ld = {r0.x * s.d.x + r0.y * s.d.y + r0.z * s.d.z, r1.x * s.d.x + r1.y * s.d.y + r1.z * s.d.z,
+                       r2.x * s.d.x + r2.y * s.d.y + r2.z * s.d.z};
+        trav_set_ray(s, lo, ld);
+        s.inst_sp = s.sp;
+        s.id_base = int32_t(m.y);
+        s.node = m.x;
+        return false;
+    }
+    const uint4 w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+    const uint32_t oct = s.oct;
+    const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+    const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+    const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+    const uint32_t imask = w0.w >> 24;
+    const float ax = sx * s.inv.x, ay = sy * s.inv.y, az = sz * s.inv.z;
+    const float bx = (__uint_as_float(w0.x) - s.o.x) * s.inv.x;
+    const float by = (__uint_as_float(w0.y) - s.o.y) * s.inv.y;
+    const float bz = (__uint_as_float(w0.z) - s.o.z) * s.inv.z;
+    const float ax8 = ax * 0.00390625f, ay8 = ay * 0.00390625f, az8 = az * 0.00390625f;
+    const float bx8 = fmaf(-32768.0f, ax, bx), by8 = fmaf(-32768.0f, ay, by), bz8 = fmaf(-32768.0f, az, bz);
+    const uint32_t lx0 = w2.x, lx1 = w2.y, ly0 = w2.z, ly1 = w2.w, lz0 = w3.x, lz1 = w3.y;
+    const uint32_t hx0 = w3.z, hx1 = w3.w, hy0 = w4.x, hy1 = w4.y, hz0 = w4.z, hz1 = w4.w;
+    const uint32_t nx0 = (oct & 1u) ? hx0 : lx0, nx1 = (oct & 1u) ? hx1 : lx1;
+    const uint32_t fx0 = (oct & 1u) ? lx0 : hx0, fx1 = (oct & 1u) ? lx1 : hx1;
+    const uint32_t ny0 = (oct & 2u) ? hy0 : ly0, ny1 = (oct & 2u) ? hy1 : ly1;
+    const uint32_t fy0 = (oct & 2u) ? ly0 : hy0, fy1 = (oct & 2u) ? ly1 : hy1;
+    const uint32_t nz0 = (oct & 4u) ? hz0 : lz0, nz1 = (oct & 4u) ? hz1 : lz1;
+    const uint32_t fz0 = (oct & 4u) ? lz0 : hz0, fz1 = (oct & 4u) ? lz1 : hz1;
+    uint32_t hitmask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint32_t sel = 0x5404u | (uint32_t(k & 3) << 4);
+        const float qnx = __uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x4B00u, sel));
+        const float qfx = __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x4B00u, sel));
+        const float qny = __uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x4B00u, sel));
+        const float qfy = __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x4B00u, sel));
+        const float qnz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x4B00u, sel));
+        const float qfz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B00u, sel));
+        const float tn = fmax3(fmaf(qnx, ax8, bx8), fmaf(qny, ay8, by8), fmaxf(fmaf(qnz, az8, bz8), s.tmin));
+        const float tf0 = fmin3(fmaf(qfx, ax8, bx8), fmaf(qfy, ay8, by8), fminf(fmaf(qfz, az8, bz8), s.best.t));
+        if (tn <= tf0 * 1.0000038f) hitmask |= 1u << k;
+    }
+    // the entered leaf children's triangles, in trav_step's order (children ascending, then the
+    // triangles of each): one mask bit per triangle slot after the node's first triangle
+    uint32_t leaves = hitmask & ~imask, tmask = 0u;
+    while (leaves) {
+        const int k = __ffs(leaves) - 1;
+        leaves &= leaves - 1;
+        const uint32_t meta = byte_of(k < 4 ? w1.z : w1.w, k & 3);
+        const uint32_t cnt = meta >> 5, off = meta & 31u;
+        tmask |= ((1u << cnt) - 1u) << off;
+    }
+    s.tri_base = w1.y;
+    s.tri_mask = tmask;
+    // next node (visited after these triangles)
+    uint32_t inner = oct_permute(hitmask & imask, oct);
+    uint32_t g_base = w1.x, g_imask = imask;
+    if (inner == 0u) {
+        if (kTwoLevel && s.sp == s.inst_sp) {
+            // the instance is done once its last node's triangles are: test them in this frame
+            // first (a node sentinel would lose the frame switch), so finish them here
+            while (s.tri_mask) {
+                const int j = __ffs(s.tri_mask) - 1;
+                s.tri_mask &= s.tri_mask - 1u;
+                const float4* tp = bvh.tris + size_t(s.tri_base + uint32_t(j)) * 3;
+                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+                if (kCount) s.ntri++;
+                float t, u, v;
+                if (tri_test(s.o, s.d, mk(a.x, a.y, a.z), mk(a.w, b.x, b.y), mk(b.z, b.w, c.x), s.tmin, s.best.t, t, u, v)) {
+                    const int32_t id = s.id_base + int32_t(__float_as_uint(c.y));
+                    if (kAnyHit) {
+                        s.best = TraceHit{t, u, v, id};
+                        return true;
+                    }
+                    if (t < s.best.t || s.best.id < 0 || id < s.best.id) s.best = TraceHit{t, u, v, id};
+                }
+            }
+            trav_set_ray(s, s.wo, s.wd);
+            s.inst_sp = -1;
+            s.id_base = 0;
+        }
+        if (s.sp == 0) {
+            s.node = 0xffffffffu;  // no node left: done after the pending triangles
+            return s.tri_mask == 0u;
+        }
+        s.sp--;
+        g_base = stk_base[s.sp * stride];
+        const uint32_t bits = stk_bits[s.sp * stride];
+        g_imask = bits >> 8;
+        inner = bits & 0xffu;
+    }
+    const int k = __ffs(inner) - 1;
+    inner &= inner - 1;
+    const uint32_t slot = uint32_t(k) ^ s.oct;
+    s.node = g_base + __popc(g_imask & ((1u << slot) - 1u));
+    if (inner != 0u) {
+        if (s.sp >= bvh.depth) { *err = 1; return true; }
+        stk_base[s.sp * stride] = g_base;
+        stk_bits[s.sp * stride] = (g_imask << 8) | inner;
+        s.sp++;
+    }
+    return false;
+}
+#endif
+
 // One ray to the end. Adds the node visits and triangle tests to *nodes_visited / *tris_tested
 // when kCount.
 template <bool kAnyHit, bool kCount, bool kTwoLevel = false>
@@ -387,7 +549,11 @@ __device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bv
         if (__ballot_sync(0xffffffffu, active) == 0u) break;
         const int keep = exhausted ? 1 : f.refill;
         do {
+#if LMGPU_TRAV_SPLIT
+            if (active && trav_step_split<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr)) {
+#else
             if (active && trav_step<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr)) {
+#endif
                 end(k, s);
                 active = false;
             }
