@@ -550,7 +550,9 @@ __device__ __forceinline__ void fetch_loop(int n, const Fetch& f, const Bvh8& bv
         const int keep = exhausted ? 1 : f.refill;
         do {
 #if LMGPU_TRAV_SPLIT
-            if (active && trav_step_split<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr)) {
+            // two-level trees keep whole-node steps (measured faster on the instanced frame)
+            if (active && (kTwoLevel ? trav_step<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr)
+                                     : trav_step_split<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr))) {
 #else
             if (active && trav_step<kAnyHit, kCount, kTwoLevel>(B, s, sb, sbits, stride, lerr)) {
 #endif
