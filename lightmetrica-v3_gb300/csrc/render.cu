@@ -37,6 +37,13 @@ struct DevLight {
     int32_t env_w, env_h, tex_off, marg_off, cond_off;
     float rot, scale;
 };
+// Scene features that select a specialised shade kernel: code for a feature the scene lacks is
+// left out of it (the shade kernels are bound by instruction fetch)
+constexpr uint32_t kFeatEnvTex = 1u;    // a textured environment light (light::env)
+constexpr uint32_t kFeatMixture = 2u;   // material::mixture_wavefrontobj
+constexpr uint32_t kFeatTwoLevel = 4u;  // a two-level (instanced) tree
+constexpr uint32_t kFeatAll = 7u;
+
 struct DevScene {
     Bvh8 bvh;
     const float4* shade;   // 6 words per triangle: p1 p2 p3 n1 n2 n3 gn prim
@@ -59,6 +66,7 @@ struct DevScene {
     // light tracing starts the rays of an environment light; radius 0 without triangles
     f3 bound_c;
     float bound_r;
+    uint32_t feat;  // kFeat* bits present in the scene
 };
 
 }  // namespace lmgpu
@@ -153,8 +161,9 @@ __device__ inline float sn_correction_le(const Geom& g, f3 wi, f3 wo) {
     return wi_ns * wo_ng / (wo_ns * wi_ng);
 }
 
+template <uint32_t kF = kFeatAll>
 __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float v, int32_t& prim) {
-    if (S.num_inst > 0) {
+    if ((kF & kFeatTwoLevel) && S.num_inst > 0) {
         // instance holding hit index id (the last whose first hit index is <= id), then the local
         // surface point moved to world space as scene.cpp:335-343 does with the hit's transform
         int lo = 0, hi = S.num_inst;
@@ -308,6 +317,7 @@ __device__ inline float mixture_w(const DevMaterial& m) {
 }
 
 // le: transport direction LE (light tracing): refraction carries no eta^2 (material_glass.cpp:85-87)
+template <uint32_t kF = kFeatAll>
 __device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, int comp, bool eval_delta, bool le = false) {
     switch (m.type) {
     case LMGPU_MAT_DIFFUSE:
@@ -316,6 +326,7 @@ __device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo,
     case LMGPU_MAT_GLOSSY:
         return glossy_eval(m, mk(m.c[0], m.c[1], m.c[2]), g, wi, wo);
     case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507 with alpha 1: the two lobes summed
+        if (!(kF & kFeatMixture)) return mk(0, 0, 0);  // not in this scene
         const f3 fd = opposite(g, wi, wo) ? mk(0, 0, 0) : mk(m.c[0], m.c[1], m.c[2]) / kPi;
         return fd + glossy_eval(m, mk(m.ks[0], m.ks[1], m.ks[2]), g, wi, wo);
     }
@@ -331,6 +342,7 @@ __device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo,
         return eval_delta ? mk(0, 0, 0) : mk(1, 1, 1);
     }
 }
+template <uint32_t kF = kFeatAll>
 __device__ inline float mat_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 wo, bool eval_delta) {
     switch (m.type) {
     case LMGPU_MAT_DIFFUSE:
@@ -338,6 +350,7 @@ __device__ inline float mat_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 w
     case LMGPU_MAT_GLOSSY:
         return glossy_pdf(m, g, wi, wo);
     case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:484-494: the lobes' pdfs by selection probability
+        if (!(kF & kFeatMixture)) return 0.f;
         const float w = mixture_w(m);
         const float pd = opposite(g, wi, wo) ? 0.f : 1.f / kPi;
         return w * pd + (1.f - w) * glossy_pdf(m, g, wi, wo);
@@ -348,6 +361,7 @@ __device__ inline float mat_pdf(const DevMaterial& m, const Geom& g, f3 wi, f3 w
 }
 // Returns false when no direction is produced (glossy below the surface). uc: the component
 // random number of the direction sample (DirectionSampleU::udc.x), used by the mixture.
+template <uint32_t kF = kFeatAll>
 __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, int comp, float u0, float u1, float uc, f3& wo,
                                   f3& w, bool le = false) {
     switch (m.type) {
@@ -357,16 +371,17 @@ __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, in
         return true;
     case LMGPU_MAT_GLOSSY: {
         if (!glossy_dir(m, g, wi, u0, u1, wo)) return false;
-        const f3 f = mat_eval(m, g, wi, wo, 0, false);
-        const float p = mat_pdf(m, g, wi, wo, false);
+        const f3 f = mat_eval<kF>(m, g, wi, wo, 0, false);
+        const float p = mat_pdf<kF>(m, g, wi, wo, false);
         w = f / p;
         return true;
     }
     case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:437-461: one lobe sampled, weight f / p of the sum
+        if (!(kF & kFeatMixture)) return false;
         if (uc < mixture_w(m)) wo = diffuse_dir(g, wi, u0, u1);
         else if (!glossy_dir(m, g, wi, u0, u1, wo)) return false;
-        const f3 f = mat_eval(m, g, wi, wo, 0, false);
-        const float p = mat_pdf(m, g, wi, wo, false);
+        const f3 f = mat_eval<kF>(m, g, wi, wo, 0, false);
+        const float p = mat_pdf<kF>(m, g, wi, wo, false);
         w = f / p;
         return true;
     }
@@ -378,7 +393,7 @@ __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, in
             glass_fresnel(m, g, wi, wt, total, eta, Fr);
             wo = wt;
         }
-        w = mat_eval(m, g, wi, wo, comp, false, le);  // pdf of a component direction is 1
+        w = mat_eval<kF>(m, g, wi, wo, comp, false, le);  // pdf of a component direction is 1
         return true;
     }
     default:
@@ -409,8 +424,9 @@ __device__ inline void env_uv(const DevLight& L, f3 d, float& u, float& v) {
     u = t - floorf(t);
     v = acosf(fminf(1.f, fmaxf(-1.f, d.y))) / kPi;
 }
+template <uint32_t kF = kFeatAll>
 __device__ inline f3 env_eval(const DevScene& S, const DevLight& L, f3 gwo) {
-    if (L.type == LMGPU_LIGHT_ENVCONST) return mk(L.ke[0], L.ke[1], L.ke[2]);
+    if (!(kF & kFeatEnvTex) || L.type == LMGPU_LIGHT_ENVCONST) return mk(L.ke[0], L.ke[1], L.ke[2]);
     const f3 d = -gwo;
     float u, v;
     env_uv(L, d, u, v);
@@ -420,9 +436,10 @@ __device__ inline f3 env_eval(const DevScene& S, const DevLight& L, f3 gwo) {
     return mk(__ldg(t), __ldg(t + 1), __ldg(t + 2)) * L.scale;
 }
 // pdf_direct of an infinite light endpoint with direction gwo, seen from g (projected solid angle)
+template <uint32_t kF = kFeatAll>
 __device__ inline float env_pdf_direct(const DevScene& S, const DevLight& L, const Geom& g, f3 gwo) {
     const f3 d = -gwo;
-    if (L.type == LMGPU_LIGHT_ENVCONST) return pdf_sa_to_projsa(1.f / (4.f * kPi), g, d);
+    if (!(kF & kFeatEnvTex) || L.type == LMGPU_LIGHT_ENVCONST) return pdf_sa_to_projsa(1.f / (4.f * kPi), g, d);
     float u, v;
     env_uv(L, d, u, v);
     const float st = sqrtf(fmaxf(0.f, 1.f - d.y * d.y));
@@ -447,6 +464,7 @@ struct LightSample {
 };
 
 // path::sample_direct(LE), path.h:493-530, with u = {up(0,1), upc(2,3), ud(4,5), udc(6,7)}
+template <uint32_t kF = kFeatAll>
 __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const float* u, LightSample& out) {
     const int n = S.num_lights;
     const int li = min(max(int(u[2] * float(n)), 0), n - 1);
@@ -470,7 +488,7 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
         return true;
     }
     f3 wo;
-    if (L.type == LMGPU_LIGHT_ENVCONST) {
+    if (!(kF & kFeatEnvTex) || L.type == LMGPU_LIGHT_ENVCONST) {
         const float z = 1.f - 2.f * u[4];
         const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
         float st, ct;
@@ -488,9 +506,9 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
     }
     out.gL = infinite_point(wo);
     out.wo = wo;
-    const float pL = env_pdf_direct(S, L, g, wo);
+    const float pL = env_pdf_direct<kF>(S, L, g, wo);
     if (pL == 0.f) return false;
-    out.weight = env_eval(S, L, wo) / pL / p_sel;
+    out.weight = env_eval<kF>(S, L, wo) / pL / p_sel;
     return true;
 }
 
@@ -649,11 +667,11 @@ __device__ inline uint32_t pixel_of(const PtConst& P, float rx, float ry) {
 
 // NEE connection from vertex g (material m, or the camera if m == nullptr); pushes a shadow ray
 // with the contribution it carries when the connection is nonzero (renderer_pt.cpp:142-192).
-template <bool kBatched>
+template <bool kBatched, uint32_t kF = kFeatAll>
 __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, const DevMaterial* m, f3 wi, int comp, f3 thr,
                            const float* u8, uint32_t pixel, const ShadowQ& sq, int* scount, uint32_t job) {
     LightSample sL;
-    if (!sample_direct(S, g, u8, sL)) return;
+    if (!sample_direct<kF>(S, g, u8, sL)) return;
     const f3 wo = -sL.wo;
     uint32_t px = pixel;
     f3 fs;
@@ -663,15 +681,15 @@ __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, c
         px = pixel_of(P, rx, ry) | (pixel & kOddPass);  // the camera vertex keeps the pass bit
         fs = mk(cam_J(S, wo), cam_J(S, wo), cam_J(S, wo));
     } else {
-        fs = mat_eval(*m, g, wi, wo, comp, true) * sn_correction(g, wi, wo);
+        fs = mat_eval<kF>(*m, g, wi, wo, comp, true) * sn_correction(g, wi, wo);
     }
     if (is_zero(fs)) return;
     float mis = 1.f;
     if (P.mode == LMGPU_SAMPLING_MIS) {
         const DevLight L = S.lights[sL.light];
         const float pl = (1.f / float(S.num_lights)) *
-                         (L.type == LMGPU_LIGHT_AREA ? area_pdf_direct(L, g, sL.gL, sL.wo) : env_pdf_direct(S, L, g, sL.gL.wo));
-        const float pb = m == nullptr ? cam_pdf(S, wo) : mat_pdf(*m, g, wi, wo, true);
+                         (L.type == LMGPU_LIGHT_AREA ? area_pdf_direct(L, g, sL.gL, sL.wo) : env_pdf_direct<kF>(S, L, g, sL.gL.wo));
+        const float pb = m == nullptr ? cam_pdf(S, wo) : mat_pdf<kF>(*m, g, wi, wo, true);
         mis = (pl == 0.f && pb == 0.f) ? 0.f : pl / (pl + pb);
     }
     const f3 C = thr * fs * sL.weight * mis;
@@ -929,7 +947,7 @@ __global__ void __launch_bounds__(kBlock, LMGPU_TRACE_MINBLOCKS) k_pt_shadow(Bvh
 // One pass of the loop body after the intersection (renderer_pt.cpp:221-300) for one path whose
 // ray left vertex nv (flags bits 8-15), then NEE and direction sampling at the new vertex nv+1.
 // Returns false when the path ends here.
-template <bool kBatched>
+template <bool kBatched, uint32_t kF = kFeatAll>
 __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, float* film, float* film_odd, uint32_t parity0,
                                            uint32_t job, float4 o4, float4 d4, float4 t4, float4 n4, float4 h4, uint2 ids,
                                            const ExtQ& qo, int* qocount, const ShadowQ& sq, int* scount) {
@@ -961,16 +979,16 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
             const f3 gwo = -d;
             float mis = 1.f;
             if (use_mis) {
-                const float pl = (1.f / float(S.num_lights)) * env_pdf_direct(S, L, gp, gwo);
+                const float pl = (1.f / float(S.num_lights)) * env_pdf_direct<kF>(S, L, gp, gwo);
                 mis = (prev_pdf == 0.f && pl == 0.f) ? 0.f : prev_pdf / (prev_pdf + pl);
             }
-            const f3 C = thr * env_eval(S, L, gwo) * mis;
+            const f3 C = thr * env_eval<kF>(S, L, gwo) * mis;
             if (!is_zero(C)) splat(film, ids.y, C);
         }
         return false;
     }
     int32_t prim;
-    const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+    const Geom g = surface_at<kF>(S, id, h4.y, h4.z, prim);
     const int2 ml = __ldg(S.prim_ml + prim);
     const f3 wi = -d;
     if (ml.y >= 0 && direct_ok) {
@@ -1006,11 +1024,11 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
     const bool spec = mat_specular(m);
     const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && !spec;
     rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
-    if (nee_ok) nee<kBatched>(S, P, g, &m, wi, comp, thr, u, ids.y | odd_bit, sq, scount, job);
+    if (nee_ok) nee<kBatched, kF>(S, P, g, &m, wi, comp, thr, u, ids.y | odd_bit, sq, scount, job);
     f3 wo, w;
-    if (!mat_sample(m, g, wi, comp, u[8], u[9], u[10], wo, w)) return false;
+    if (!mat_sample<kF>(m, g, wi, comp, u[8], u[9], u[10], wo, w)) return false;
     w = w * sn_correction(g, wi, wo);
-    const float pdf = (P.mode == LMGPU_SAMPLING_MIS && nee_ok) ? mat_pdf(m, g, wi, wo, true) : 0.f;
+    const float pdf = (P.mode == LMGPU_SAMPLING_MIS && nee_ok) ? mat_pdf<kF>(m, g, wi, wo, true) : 0.f;
     thr = thr * w;
     push_ext<kBatched>(qo, qocount, g.p, wo, thr, pdf, g.n, (nee_ok ? 1u : 0u) | (uint32_t(nv) << 8), ids.x, ids.y, job);
     return true;
@@ -1577,7 +1595,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
 
 // Job table: as k_pt_shade with each entry's own job; a path that ends adds one to its job's pass
 // counter (warp-aggregated per pass).
-template <int kMinBlocks, bool kSingle>
+template <int kMinBlocks, bool kSingle, uint32_t kF = kFeatAll>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* __restrict__ jobs, ExtQ qi, const float4* __restrict__ hits,
                                                      const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
                                                      int* scount, unsigned int* pass_done) {
@@ -1587,7 +1605,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* _
         const uint32_t job = kSingle ? 0u : qi.job[k];
         const JobDev& J = jobs[job];
         const uint2 ids = qi.ids[k];
-        const bool alive = shade_path<true>(J.S, J.P, J.film, J.film_odd, J.parity0, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
+        const bool alive = shade_path<true, kF>(J.S, J.P, J.film, J.film_odd, J.parity0, job, qi.o[k], qi.d[k], qi.thr[k], qi.nrm[k], hits[k], ids, qo,
                                             qocount, sq, scount);
         if (!alive) {
             const uint32_t key = J.pass_off + ids.x % uint32_t(J.P.spp);
@@ -2042,6 +2060,11 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         ds.bvh = device_view(accel);
         ds.bound_c = bound_c;
         ds.bound_r = bound_r;
+        ds.feat = two_level ? kFeatTwoLevel : 0u;
+        for (int32_t i = 0; i < D->num_lights; i++)
+            if (D->lights[i].type == LMGPU_LIGHT_ENV) ds.feat |= kFeatEnvTex;
+        for (int32_t i = 0; i < D->num_materials; i++)
+            if (D->materials[i].type == LMGPU_MAT_MIXTURE) ds.feat |= kFeatMixture;
         ds.shade = s->shade.as<const float4>();
         ds.prim_ml = s->prim_ml.as<const int2>();
         ds.mats = s->mats.as<const DevMaterial>();
@@ -2913,6 +2936,7 @@ struct lmgpu_batch {
         int refill = -1, shade = -1, first_pass = -1;
         bool two_level = false;
         bool single = false;      // captured for a one-job table
+        uint32_t feat = 0;        // that job's scene features (the shade kernel specialised for them)
         lmgpu::Bvh8 bvh{};        // that job's tree and films, passed by value to the trace kernels
         float* film = nullptr;
         float* film_odd = nullptr;
@@ -2981,6 +3005,26 @@ __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
     ctl[5] = njobs;
 }
 
+// The one-job shade kernel specialised for the job scene's features (default register budget).
+using WfShadeK = decltype(&k_wf_shade<4, true, kFeatAll>);
+WfShadeK wf_shade_single(uint32_t feat) {
+    switch (feat & kFeatAll) {
+    case 0: return k_wf_shade<4, true, 0u>;
+    case 1: return k_wf_shade<4, true, 1u>;
+    case 2: return k_wf_shade<4, true, 2u>;
+    case 3: return k_wf_shade<4, true, 3u>;
+    case 4: return k_wf_shade<4, true, 4u>;
+    case 5: return k_wf_shade<4, true, 5u>;
+    case 6: return k_wf_shade<4, true, 6u>;
+    default: return k_wf_shade<4, true, 7u>;
+    }
+}
+WfShadeK wf_shade_kernel(const lmgpu_batch* b, bool single, uint32_t feat) {
+    if (single && b->shade_minblocks >= 4) return wf_shade_single(feat);
+    return single ? pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks)
+                  : pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks);
+}
+
 // Stream-ordered view of one chunk of iterations; captured into a graph.
 void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
     const size_t tsmem = size_t(2) * 4 * kBlock * size_t(b->max_depth);
@@ -2997,8 +3041,7 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
                        : (b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>);
     const int g_ext = grid_for(ext_k, kBlock, tsmem);
     const int g_sh = grid_for(sh_k, kBlock, tsmem);
-    auto shade_k = single ? pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks)
-                          : pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks);
+    auto shade_k = wf_shade_kernel(b, single, single ? J0.S.feat : kFeatAll);
     const int g_shade = grid_for(shade_k, kBlock, 0);
     const int g_gen = grid_for(k_wf_generate, kBlock, 0);
     Bvh8 tb = bmax;  // stack sized by the deepest tree seen; single job: its own tree
@@ -3059,8 +3102,10 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     }
     auto& g = b->slot[b->timed ? 1 : 0];
     const bool single = b->host_jobs.size() == 1;
+    const uint32_t feat = single ? b->host_jobs[0].S.feat : kFeatAll;
     const bool same_shape = g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
-                            g.two_level == b->two_level && g.first_pass == b->first_pass && g.single == single;
+                            g.two_level == b->two_level && g.first_pass == b->first_pass && g.single == single &&
+                            g.feat == feat;
     auto same_job = [&] {
         const JobDev& J = b->host_jobs[0];
         return std::memcmp(&g.bvh, &J.S.bvh, sizeof(Bvh8)) == 0 && g.film == J.film && g.film_odd == J.film_odd;
@@ -3077,8 +3122,8 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     (void)grid_for(b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>, kBlock, tsmem);
     (void)grid_for(b->two_level ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>, kBlock, tsmem);
     (void)grid_for(b->two_level ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>, kBlock, tsmem);
-    (void)grid_for(pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks), kBlock, 0);
-    (void)grid_for(pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks), kBlock, 0);
+    (void)grid_for(wf_shade_kernel(b, false, kFeatAll), kBlock, 0);
+    (void)grid_for(wf_shade_kernel(b, single, feat), kBlock, 0);
     (void)grid_for(k_wf_generate, kBlock, 0);
     cudaGraph_t ng = nullptr;
     LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
@@ -3115,6 +3160,7 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     g.first_pass = b->first_pass;
     g.shade = b->shade_minblocks;
     g.single = single;
+    g.feat = feat;
     if (single) {
         g.bvh = b->host_jobs[0].S.bvh;
         g.film = b->host_jobs[0].film;
