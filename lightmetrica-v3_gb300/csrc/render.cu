@@ -3019,10 +3019,19 @@ WfShadeK wf_shade_single(uint32_t feat) {
     default: return k_wf_shade<4, true, 7u>;
     }
 }
+// feat: the job's features (one job) or the union over the table's jobs. Several jobs: a kernel
+// without the textured environment and the mixture when no job has them.
 WfShadeK wf_shade_kernel(const lmgpu_batch* b, bool single, uint32_t feat) {
     if (single && b->shade_minblocks >= 4) return wf_shade_single(feat);
+    if (!single && b->shade_minblocks >= 4 && (feat & ~kFeatTwoLevel) == 0u)
+        return (feat & kFeatTwoLevel) ? k_wf_shade<4, false, kFeatTwoLevel> : k_wf_shade<4, false, 0u>;
     return single ? pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks)
                   : pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks);
+}
+uint32_t table_features(const lmgpu_batch* b) {
+    uint32_t f = 0u;
+    for (const auto& J : b->host_jobs) f |= J.S.feat;
+    return f;
 }
 
 // Stream-ordered view of one chunk of iterations; captured into a graph.
@@ -3041,7 +3050,7 @@ void enqueue_chunk(lmgpu_batch* b, cudaStream_t st, bool timed) {
                        : (b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>);
     const int g_ext = grid_for(ext_k, kBlock, tsmem);
     const int g_sh = grid_for(sh_k, kBlock, tsmem);
-    auto shade_k = wf_shade_kernel(b, single, single ? J0.S.feat : kFeatAll);
+    auto shade_k = wf_shade_kernel(b, single, table_features(b));
     const int g_shade = grid_for(shade_k, kBlock, 0);
     const int g_gen = grid_for(k_wf_generate, kBlock, 0);
     Bvh8 tb = bmax;  // stack sized by the deepest tree seen; single job: its own tree
@@ -3102,7 +3111,7 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     }
     auto& g = b->slot[b->timed ? 1 : 0];
     const bool single = b->host_jobs.size() == 1;
-    const uint32_t feat = single ? b->host_jobs[0].S.feat : kFeatAll;
+    const uint32_t feat = table_features(b);
     const bool same_shape = g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
                             g.two_level == b->two_level && g.first_pass == b->first_pass && g.single == single &&
                             g.feat == feat;
@@ -3122,7 +3131,6 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     (void)grid_for(b->two_level ? k_pt_shadow<false, true, true> : k_pt_shadow<false, true, false>, kBlock, tsmem);
     (void)grid_for(b->two_level ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>, kBlock, tsmem);
     (void)grid_for(b->two_level ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>, kBlock, tsmem);
-    (void)grid_for(wf_shade_kernel(b, false, kFeatAll), kBlock, 0);
     (void)grid_for(wf_shade_kernel(b, single, feat), kBlock, 0);
     (void)grid_for(k_wf_generate, kBlock, 0);
     cudaGraph_t ng = nullptr;
