@@ -295,6 +295,9 @@ def run_gpu(args) -> None:
         # shadow ray written 48 B
         bytes_total, launches = tot["ext"] * (88 + 88 + 96 + 48), tot["ext_launches"]
     achieved = bytes_total / (kern[dom] / 1e3) / 1e9
+    # L2 read bandwidth (64 MB buffer, below the 129 MB L2): the node arrays of this scene fit in L2
+    l2 = C.c_double()
+    N.check(L.lmgpu_probe_l2_bandwidth(64 << 20, 20, C.byref(l2)))
     # DRAM traffic per launch of the dominant kernel: bytes per traced ray from an ncu capture of
     # every launch of that kernel in one step (profiles/traffic_per_ray.json) times the rays one
     # launch of this run traces on average
@@ -335,6 +338,7 @@ def run_gpu(args) -> None:
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                         "l2_peak_gbs": l2.value, "frac_l2": achieved / l2.value,
                          "traffic": traffic, "bytes_per_ray": {"extend": b_ext, "shadow": b_sh},
                          "launches": launches, **counts},
             "cpu_baseline": cpu,

@@ -222,6 +222,11 @@ int lmgpu_film_create(lmgpu_film** out, int32_t w, int32_t h);
 int lmgpu_film_destroy(lmgpu_film* film);
 int lmgpu_film_clear(lmgpu_film* film);
 /* Film::buffer (film_bitmap.cpp:202-208): copies h x w x 3 floats to host memory. */
+/* Measurement helper (no reference counterpart): L2 read bandwidth in GB/s, from `iters` streaming
+ * passes over a `bytes`-sized buffer (>= 1 MB; below the L2 size) with L1-bypassing loads. The
+ * roofline of the trace kernels quotes it beside HBM, as their node arrays fit in L2. */
+int lmgpu_probe_l2_bandwidth(int64_t bytes, int32_t iters, double* gbs);
+
 /* Every pixel set to rgb (3 floats): renderer::blank's Film::clear + set_pixel loop
  * (src/renderer/renderer_blank.cpp:36-45). */
 int lmgpu_film_fill(lmgpu_film* film, const float* rgb);

@@ -1716,6 +1716,18 @@ __global__ void k_rel_mse(const float* __restrict__ a, const float* __restrict__
     if ((threadIdx.x & 31) == 0) atomicAdd(acc, s);
 }
 
+// L2 read bandwidth probe: every thread streams float4s of an L2-resident buffer with loads that
+// bypass L1 (ld.global.cg); the sum only keeps the loads alive.
+__global__ void k_l2_probe(const float4* __restrict__ buf, int64_t n, int iters, float* out) {
+    float acc = 0.f;
+    for (int it = 0; it < iters; it++)
+        for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+            const float4 v = __ldcg(buf + i);
+            acc += (v.x + v.y) + (v.z + v.w);
+        }
+    if (acc == 1234.5f) out[0] = acc;
+}
+
 __global__ void k_scale(const float* __restrict__ in, float* __restrict__ out, int64_t n, float s) {
     for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
         out[i] = in[i] * s;
@@ -2153,6 +2165,33 @@ int lmgpu_film_rel_mse(lmgpu_film* f, double eps, double* rel_mse) {
         double h = 0.0;
         LMGPU_CUDA(cudaMemcpy(&h, acc.p, sizeof(double), cudaMemcpyDeviceToHost));
         *rel_mse = h / double(n);
+    });
+}
+
+int lmgpu_probe_l2_bandwidth(int64_t bytes, int32_t iters, double* gbs) {
+    return guarded([&] {
+        if (!gbs || bytes < (int64_t(1) << 20) || iters < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid probe size");
+        DevBuf buf, out;
+        const int64_t n = bytes / 16;
+        buf.alloc(size_t(n) * 16);
+        out.alloc(16);
+        LMGPU_CUDA(cudaMemset(buf.p, 0, size_t(n) * 16));
+        const int grid = 8 * current_device().num_sms;
+        k_l2_probe<<<grid, 256>>>(buf.as<float4>(), n, 1, out.as<float>());  // brings the buffer into L2
+        LMGPU_CUDA(cudaGetLastError());
+        cudaEvent_t e0, e1;
+        LMGPU_CUDA(cudaEventCreate(&e0));
+        LMGPU_CUDA(cudaEventCreate(&e1));
+        LMGPU_CUDA(cudaEventRecord(e0));
+        k_l2_probe<<<grid, 256>>>(buf.as<float4>(), n, iters, out.as<float>());
+        LMGPU_CUDA(cudaEventRecord(e1));
+        LMGPU_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        LMGPU_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        LMGPU_CUDA(cudaGetLastError());
+        *gbs = double(n) * 16.0 * iters / (double(ms) * 1e-3) / 1e9;
     });
 }
 

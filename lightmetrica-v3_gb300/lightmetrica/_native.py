@@ -112,6 +112,7 @@ SIGNATURES = [
     ("lmgpu_film_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.c_int32]),
     ("lmgpu_film_destroy", C.c_int, [C.c_void_p]),
     ("lmgpu_film_clear", C.c_int, [C.c_void_p]),
+    ("lmgpu_probe_l2_bandwidth", C.c_int, [C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
     ("lmgpu_film_fill", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
     ("lmgpu_film_read", C.c_int, [C.c_void_p, c_float_p]),
     ("lmgpu_film_device_ptr", C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
