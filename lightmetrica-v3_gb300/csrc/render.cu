@@ -3044,17 +3044,21 @@ __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
 }
 
 // The one-job shade kernel specialised for the job scene's features (default register budget).
+#ifndef LMGPU_SHADE_SINGLE_MINBLOCKS
+#define LMGPU_SHADE_SINGLE_MINBLOCKS 4  // blocks per SM of the specialised kernels (3: 41.0 ms, 5: 39.5 ms, 4: 37.1 ms per frame)
+#endif
 using WfShadeK = decltype(&k_wf_shade<4, true, kFeatAll>);
 WfShadeK wf_shade_single(uint32_t feat) {
+    constexpr int mb = LMGPU_SHADE_SINGLE_MINBLOCKS;
     switch (feat & kFeatAll) {
-    case 0: return k_wf_shade<4, true, 0u>;
-    case 1: return k_wf_shade<4, true, 1u>;
-    case 2: return k_wf_shade<4, true, 2u>;
-    case 3: return k_wf_shade<4, true, 3u>;
-    case 4: return k_wf_shade<4, true, 4u>;
-    case 5: return k_wf_shade<4, true, 5u>;
-    case 6: return k_wf_shade<4, true, 6u>;
-    default: return k_wf_shade<4, true, 7u>;
+    case 0: return k_wf_shade<mb, true, 0u>;
+    case 1: return k_wf_shade<mb, true, 1u>;
+    case 2: return k_wf_shade<mb, true, 2u>;
+    case 3: return k_wf_shade<mb, true, 3u>;
+    case 4: return k_wf_shade<mb, true, 4u>;
+    case 5: return k_wf_shade<mb, true, 5u>;
+    case 6: return k_wf_shade<mb, true, 6u>;
+    default: return k_wf_shade<mb, true, 7u>;
     }
 }
 // feat: the job's features (one job) or the union over the table's jobs. Several jobs: a kernel
