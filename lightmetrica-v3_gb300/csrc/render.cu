@@ -1069,7 +1069,7 @@ __global__ void __launch_bounds__(kBlock) k_lt_generate(const __grid_constant__ 
 // One light path after its extension ray: roulette and component at the hit (vertex k + 1), the
 // camera connection of that vertex (camera_pinhole.cpp:178-203: weight J(wo) G; the raster
 // position is tested before the shadow ray is queued), and the next direction.
-template <int kMinBlocks>
+template <int kMinBlocks, uint32_t kF = kFeatAll>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
                                                      ExtQ qi, const float4* __restrict__ hits, const int* __restrict__ qicount,
                                                      ExtQ qo, int* qocount, ShadowQ sq, int* scount) {
@@ -1090,7 +1090,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_co
             thr = thr / (1.f - qrr);
         }
         int32_t prim;
-        const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+        const Geom g = surface_at<kF>(S, id, h4.y, h4.z, prim);
         const DevMaterial m = S.mats[__ldg(S.prim_ml + prim).x];
         const f3 wi = -mk(d4.x, d4.y, d4.z);
         int comp = 0;
@@ -1112,7 +1112,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_co
                 const float G = fabsf(dot(g.n, dc / len)) / L2;
                 if (G != 0.f) {
                     const f3 wo = -wE;
-                    const f3 fs = mat_eval(m, g, wi, wo, comp, true, true) * sn_correction_le(g, wi, wo);
+                    const f3 fs = mat_eval<kF>(m, g, wi, wo, comp, true, true) * sn_correction_le(g, wi, wo);
                     const f3 C = thr * fs * (cam_J(S, wE) * G);
                     if (!is_zero(C)) push_shadow<false>(sq, scount, g.p, normalize(dc), len * (1.f - kEps), C, pixel_of(P, rx, ry), 0u);
                 }
@@ -1121,7 +1121,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_co
         if (nv + 1 >= P.max_verts) continue;  // the next vertex would not connect
         rng_slots(P.seed, ids.x, uint32_t(nv), 2, 1, u + 8);
         f3 wo, w;
-        if (!mat_sample(m, g, wi, comp, u[8], u[9], u[10], wo, w, true)) continue;
+        if (!mat_sample<kF>(m, g, wi, comp, u[8], u[9], u[10], wo, w, true)) continue;
         thr = thr * (w * sn_correction_le(g, wi, wo));
         if (is_zero(thr)) continue;
         push_ext<false>(qo, qocount, g.p, wo, thr, 0.f, g.n, uint32_t(nv) << 8, ids.x, 0u, 0u);
@@ -1290,7 +1290,7 @@ __global__ void __launch_bounds__(kBlock) k_bd_generate(const __grid_constant__ 
 // One subpath step (bidir.h:507-569): the hit becomes vertex j + 1 with the component sampled
 // there; then, while the subpath has fewer than max_verts vertices, the next direction in the
 // subpath's transport direction. The queue carries the subpath weight up to the hit.
-template <int kMinBlocks>
+template <int kMinBlocks, uint32_t kF = kFeatAll>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
                                                      BdRec R, ExtQ qi, const float4* __restrict__ hits, const int* __restrict__ qicount,
                                                      ExtQ qo, int* qocount) {
@@ -1318,7 +1318,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_co
             continue;
         }
         int32_t prim;
-        const Geom g = surface_at(S, id, h4.y, h4.z, prim);
+        const Geom g = surface_at<kF>(S, id, h4.y, h4.z, prim);
         const int2 ml = __ldg(S.prim_ml + prim);
         const DevMaterial m = S.mats[ml.x];
         float u[16];
@@ -1352,14 +1352,14 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_co
         // infinite origin's direction
         const f3 wi = (flags & kBdInfOrigin) ? -d : normalize(o - g.p);
         f3 wo, w;
-        if (!mat_sample(m, g, wi, int(v.comp), u[8], u[9], u[10], wo, w, sub == 1)) continue;
+        if (!mat_sample<kF>(m, g, wi, int(v.comp), u[8], u[9], u[10], wo, w, sub == 1)) continue;
         w = w * (sub ? sn_correction_le(g, wi, wo) : sn_correction(g, wi, wo));
         const f3 next = (thr / v.pc) * w;
         if (is_zero(next)) continue;  // every strategy through the next vertex weighs 0
         v.pc_out = bd_pcomp(m, g, int(v.comp), wo);
-        v.prev_rev = mat_pdf(m, g, wo, wi, false) * v.G;
+        v.prev_rev = mat_pdf<kF>(m, g, wo, wi, false) * v.G;
         bd_store_out(R, sub, j + 1, slot, v);
-        push_ext<false>(qo, qocount, g.p, wo, next, mat_pdf(m, g, wi, wo, false), g.n, (uint32_t(j + 1) << 8) | (sub ? kBdLightSub : 0u),
+        push_ext<false>(qo, qocount, g.p, wo, next, mat_pdf<kF>(m, g, wi, wo, false), g.n, (uint32_t(j + 1) << 8) | (sub ? kBdLightSub : 0u),
                         ids.x, ids.y, 0u);
     }
 }
@@ -1411,7 +1411,7 @@ __global__ void __launch_bounds__(kBlock) k_bd_items(BdRec R, int64_t count, int
 // contribution alpha_L * c_st * alpha_E (bidir.h:325-343) and the weight. s = 0 splats at the
 // eye's raster position; s, t >= 1 queue a visibility ray from the light vertex to the eye
 // vertex. Strategies whose own pdf is 0 contribute nothing.
-template <int kMinBlocks>
+template <int kMinBlocks, uint32_t kF = kFeatAll>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_constant__ DevScene S, const __grid_constant__ PtConst P,
                                                        BdRec R, const uint2* __restrict__ items, const int* __restrict__ icount,
                                                        ShadowQ sq, int* scount, int64_t scap, float* film, int* err) {
@@ -1451,7 +1451,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
             f3 Le;
             float pdir;
             if (vE.kind == kBdInfinite) {
-                Le = env_eval(S, L, vE.p);
+                Le = env_eval<kF>(S, L, vE.p);
                 pdir = bd_env_pray(S);
                 qLs = 1.f;
             } else {
@@ -1491,10 +1491,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 const DevMaterial m = S.mats[vL.mat];
                 const Geom gL = bd_geom(vL);
                 const f3 wi = bd_toward(R, 1, s - 2, k, vL.p);
-                fL = mat_eval(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
-                pLf = mat_pdf(m, gL, wi, dLE, false);
+                fL = mat_eval<kF>(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
+                pLf = mat_pdf<kF>(m, gL, wi, dLE, false);
                 pcL = bd_pcomp(m, gL, int(vL.comp), dLE);
-                qEs2 = (opt ? 1.f : fabsf(bd_pdfs(R, 1, s - 2, k).y)) * (mat_pdf(m, gL, dLE, wi, false) * vL.G);
+                qEs2 = (opt ? 1.f : fabsf(bd_pdfs(R, 1, s - 2, k).y)) * (mat_pdf<kF>(m, gL, dLE, wi, false) * vL.G);
             }
             if (is_zero(fL)) continue;
             float pEf, pcE = 1.f;
@@ -1509,10 +1509,10 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 const DevMaterial m = S.mats[vE.mat];
                 const Geom gE = bd_geom(vE);
                 const f3 wi = bd_toward(R, 0, t - 2, k, vE.p);
-                fE = mat_eval(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
-                pEf = mat_pdf(m, gE, wi, dEL, false);
+                fE = mat_eval<kF>(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
+                pEf = mat_pdf<kF>(m, gE, wi, dEL, false);
                 pcE = bd_pcomp(m, gE, int(vE.comp), dEL);
-                qLs1 = (opt ? 1.f : fabsf(bd_pdfs(R, 0, t - 2, k).y)) * (mat_pdf(m, gE, dEL, wi, false) * vE.G);
+                qLs1 = (opt ? 1.f : fabsf(bd_pdfs(R, 0, t - 2, k).y)) * (mat_pdf<kF>(m, gE, dEL, wi, false) * vE.G);
             }
             Cu = aL * (fL * Gc * fE) * aE;
             qLs = (opt ? 1.f : pcE) * (pLf * Gc);
@@ -1814,6 +1814,36 @@ Workspace& workspace(int device) {
     std::lock_guard<std::mutex> lk(reg_m);
     if (!reg[device]) reg[device] = new Workspace();  // never freed: outlives the CUDA runtime's teardown order
     return *reg[device];
+}
+
+// Light-tracing and BDPT kernels specialised on the features they use: instances and mixture
+// materials (shade), the textured environment and mixture materials (connect).
+using LtShadeK = decltype(&k_lt_shade<4, kFeatAll>);
+LtShadeK lt_shade_for(uint32_t feat) {
+    switch (feat & (kFeatMixture | kFeatTwoLevel)) {
+    case 0: return k_lt_shade<4, 0u>;
+    case kFeatMixture: return k_lt_shade<4, kFeatMixture>;
+    case kFeatTwoLevel: return k_lt_shade<4, kFeatTwoLevel>;
+    default: return k_lt_shade<4, kFeatMixture | kFeatTwoLevel>;
+    }
+}
+using BdShadeK = decltype(&k_bd_shade<4, kFeatAll>);
+BdShadeK bd_shade_for(uint32_t feat) {
+    switch (feat & (kFeatMixture | kFeatTwoLevel)) {
+    case 0: return k_bd_shade<4, 0u>;
+    case kFeatMixture: return k_bd_shade<4, kFeatMixture>;
+    case kFeatTwoLevel: return k_bd_shade<4, kFeatTwoLevel>;
+    default: return k_bd_shade<4, kFeatMixture | kFeatTwoLevel>;
+    }
+}
+using BdConnectK = decltype(&k_bd_connect<3, kFeatAll>);
+BdConnectK bd_connect_for(uint32_t feat) {
+    switch (feat & (kFeatEnvTex | kFeatMixture)) {
+    case 0: return k_bd_connect<3, 0u>;
+    case kFeatEnvTex: return k_bd_connect<3, kFeatEnvTex>;
+    case kFeatMixture: return k_bd_connect<3, kFeatMixture>;
+    default: return k_bd_connect<3, kFeatEnvTex | kFeatMixture>;
+    }
 }
 
 void ensure_queues(Workspace& w, int64_t cap) {
@@ -2515,7 +2545,9 @@ int lmgpu_render_lt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_lt_params* prm, v
         const bool two = s->dev.num_inst > 0;
         auto ext_k = two ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>;
         auto sh_k = two ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>;
-        auto shade_k = pick_shade(k_lt_shade<2>, k_lt_shade<3>, k_lt_shade<4>, tuning().shade_minblocks);
+        // the default register budget runs a kernel specialised on the scene's features
+        auto shade_k = tuning().shade_minblocks >= 4 ? lt_shade_for(s->dev.feat)
+                                                      : pick_shade(k_lt_shade<2>, k_lt_shade<3>, k_lt_shade<4>, tuning().shade_minblocks);
         const int g_gen = grid_for(k_lt_generate, kBlock, 0);
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
@@ -2679,14 +2711,15 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         const bool two = s->dev.num_inst > 0;
         auto ext_k = two ? k_pt_extend<false, false, true> : k_pt_extend<false, false, false>;
         auto sh_k = two ? k_pt_shadow<false, false, true> : k_pt_shadow<false, false, false>;
-        auto shade_k = pick_shade(k_bd_shade<2>, k_bd_shade<3>, k_bd_shade<4>, tuning().shade_minblocks);
+        auto shade_k = tuning().shade_minblocks >= 4 ? bd_shade_for(s->dev.feat)
+                                                      : pick_shade(k_bd_shade<2>, k_bd_shade<3>, k_bd_shade<4>, tuning().shade_minblocks);
         const int g_gen = grid_for(k_bd_generate, kBlock, 0);
         const int g_ext = grid_for(ext_k, kBlock, tsmem);
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
         const int g_shade = grid_for(shade_k, kBlock, 0);
         const int g_items = grid_for(k_bd_items, kBlock, 0);
         // the "shade_minblocks" tuning key: 2 gives connect its full register budget, more gives 3 blocks
-        auto con_k = tuning().shade_minblocks <= 2 ? k_bd_connect<2> : k_bd_connect<3>;
+        auto con_k = tuning().shade_minblocks <= 2 ? k_bd_connect<2> : bd_connect_for(s->dev.feat);
         const int g_con = grid_for(con_k, kBlock, 0);
 
         enum { K_GEN = 0, K_EXT = 1, K_SHADE = 2, K_SHADOW = 3 };
