@@ -160,10 +160,12 @@ typedef struct lmgpu_material {
 #define LMGPU_LIGHT_AREA 0
 #define LMGPU_LIGHT_ENVCONST 1
 #define LMGPU_LIGHT_ENV 2
+#define LMGPU_LIGHT_POINT 3        /* light::point (src/light/light_point.cpp) */
+#define LMGPU_LIGHT_DIRECTIONAL 4  /* light::directional (src/light/light_directional.cpp) */
 
 typedef struct lmgpu_light {
     int32_t type;       /* LMGPU_LIGHT_* */
-    float ke[3];        /* area: Ke; envconst: Le */
+    float ke[3];        /* area: Ke; envconst, point, directional: Le */
     /* area: a range of the light-triangle arrays below. The sampling CDF is built from the
      * untransformed (mesh-local) triangle areas, as light_area.cpp:68-80 does. */
     int64_t tri_offset, tri_count;
@@ -172,6 +174,10 @@ typedef struct lmgpu_light {
     int32_t env_w, env_h;
     int64_t env_offset;
     float rot_deg, scale;
+    /* point: the world-space position (the primitive's transform is not applied,
+     * light_point.cpp:84-88); directional: the direction the light travels, normalized here
+     * (light_directional.cpp:34-37). Unused by the other types. */
+    float vec[3];
 } lmgpu_light;
 
 typedef struct lmgpu_camera {

@@ -36,13 +36,15 @@ struct DevLight {
     float invA_J;  // (1 / mesh-local area) / |det M|, light_area.cpp:41-46
     int32_t env_w, env_h, tex_off, marg_off, cond_off;
     float rot, scale;
+    float v[3];    // point: position; directional: the normalized direction it travels
 };
 // Scene features that select a specialised shade kernel: code for a feature the scene lacks is
 // left out of it (the shade kernels are bound by instruction fetch)
 constexpr uint32_t kFeatEnvTex = 1u;    // a textured environment light (light::env)
 constexpr uint32_t kFeatMixture = 2u;   // material::mixture_wavefrontobj
 constexpr uint32_t kFeatTwoLevel = 4u;  // a two-level (instanced) tree
-constexpr uint32_t kFeatAll = 7u;
+constexpr uint32_t kFeatDelta = 8u;     // light::point or light::directional
+constexpr uint32_t kFeatAll = 15u;
 
 struct DevScene {
     Bvh8 bvh;
@@ -120,6 +122,12 @@ __device__ inline Geom infinite_point(f3 wo) {
     Geom g;
     g.p = mk(0, 0, 0); g.n = mk(0, 0, 0); g.gn = g.n; g.u = g.n; g.v = g.n;
     g.wo = wo; g.degenerated = false; g.infinite = true;
+    return g;
+}
+__device__ inline Geom degenerate_point(f3 p) {
+    Geom g;
+    g.p = p; g.n = mk(0, 0, 0); g.gn = g.n; g.u = g.n; g.v = g.n; g.wo = g.n;
+    g.degenerated = true; g.infinite = false;
     return g;
 }
 __device__ inline bool opposite(const Geom& g, f3 a, f3 b) { return dot(a, g.n) * dot(b, g.n) <= 0.f; }
@@ -487,6 +495,23 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
         out.weight = Le / pL / p_sel;
         return true;
     }
+    if ((kF & kFeatDelta) && L.type == LMGPU_LIGHT_POINT) {  // light_point.cpp:84-100: pdf 1 / G
+        const f3 pl = mk(L.v[0], L.v[1], L.v[2]);
+        out.gL = degenerate_point(pl);
+        out.wo = normalize(g.p - pl);
+        const float G = geometry_term(g, out.gL);
+        if (G == 0.f) return false;
+        out.weight = mk(L.ke[0], L.ke[1], L.ke[2]) / (1.f / G) / p_sel;
+        return true;
+    }
+    if ((kF & kFeatDelta) && L.type == LMGPU_LIGHT_DIRECTIONAL) {  // light_directional.cpp:109-124
+        out.wo = mk(L.v[0], L.v[1], L.v[2]);
+        out.gL = infinite_point(out.wo);
+        const float pL = pdf_sa_to_projsa(1.f, g, -out.wo);
+        if (pL == 0.f) return false;
+        out.weight = mk(L.ke[0], L.ke[1], L.ke[2]) / pL / p_sel;
+        return true;
+    }
     f3 wo;
     if (!(kF & kFeatEnvTex) || L.type == LMGPU_LIGHT_ENVCONST) {
         const float z = 1.f - 2.f * u[4];
@@ -516,9 +541,12 @@ __device__ inline bool sample_direct(const DevScene& S, const Geom& g, const flo
 // u = {up(0,1), upc(2,3), ud(4,5), udc(6,7)}. Area lights (light_area.cpp:78-100): a point as in
 // sample_direct, a cosine-weighted direction about its normal, weight Le / (pA / pi). Environment
 // lights (light_envconst.cpp:47-68, light_env.cpp:86-107): a uniform direction d, a point on the
-// disk of the scene's bounding sphere facing d, weight Le(-d) / (1 / (4 pi) / (pi R^2)). Returns
-// false when nothing can be hit (an environment light in a scene without triangles). li_out: the
-// light chosen; n_out: an area light's normal at the sampled point.
+// disk of the scene's bounding sphere facing d, weight Le(-d) / (1 / (4 pi) / (pi R^2)). Point
+// lights (light_point.cpp:39-49): a uniform direction from the position, weight Le / (1 / (4 pi)).
+// Directional lights (light_directional.cpp:49-70): the light's direction from a point of that
+// disk, weight Le / (1 / (pi R^2)). Returns false when nothing can be hit (an environment or
+// directional light in a scene without triangles). li_out: the light chosen; n_out: an area
+// light's normal at the sampled point.
 __device__ inline bool sample_light_ray(const DevScene& S, const float* u, f3& o, f3& d, f3& w, int* li_out = nullptr,
                                         f3* n_out = nullptr) {
     const int n = S.num_lights;
@@ -547,7 +575,28 @@ __device__ inline bool sample_light_ray(const DevScene& S, const float* u, f3& o
         w = Le / (L.invA_J * (1.f / kPi)) / p_sel;
         return true;
     }
+    if (L.type == LMGPU_LIGHT_POINT) {
+        o = mk(L.v[0], L.v[1], L.v[2]);
+        const float z = 1.f - 2.f * u[4];
+        const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+        float st, ct;
+        sincosf(2.f * kPi * u[5], &st, &ct);
+        d = mk(r * ct, r * st, z);
+        w = mk(L.ke[0], L.ke[1], L.ke[2]) / (1.f / (4.f * kPi)) / p_sel;
+        return true;
+    }
     if (!(S.bound_r > 0.f)) return false;
+    if (L.type == LMGPU_LIGHT_DIRECTIONAL) {
+        d = mk(L.v[0], L.v[1], L.v[2]);
+        const float rd = sqrtf(fmaxf(0.f, u[0]));
+        float sd, cd;
+        sincosf(2.f * kPi * u[1], &sd, &cd);
+        f3 tu, tv;
+        onb(d, tu, tv);
+        o = S.bound_c + (-d) * S.bound_r + (tu * (rd * cd * S.bound_r) + tv * (rd * sd * S.bound_r));
+        w = mk(L.ke[0], L.ke[1], L.ke[2]) / (1.f / (kPi * S.bound_r * S.bound_r)) / p_sel;
+        return true;
+    }
     const float z = 1.f - 2.f * u[4];
     const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
     float st, ct;
@@ -682,7 +731,9 @@ __device__ inline void nee(const DevScene& S, const PtConst& P, const Geom& g, c
     }
     if (is_zero(fs)) return;
     float mis = 1.f;
-    if (P.mode == LMGPU_SAMPLING_MIS) {
+    // renderer_pt.cpp:172-179: a light BSDF sampling cannot reach (point, directional) keeps weight 1
+    const bool delta = (kF & kFeatDelta) && (sL.gL.degenerated || S.lights[sL.light].type == LMGPU_LIGHT_DIRECTIONAL);
+    if (P.mode == LMGPU_SAMPLING_MIS && !delta) {
         const DevLight L = S.lights[sL.light];
         const float pl = (1.f / float(S.num_lights)) *
                          (L.type == LMGPU_LIGHT_AREA ? area_pdf_direct(L, g, sL.gL, sL.wo) : env_pdf_direct<kF>(S, L, g, sL.gL.wo));
@@ -1146,7 +1197,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_lt_shade(const __grid_co
 // 13-14 the component of the vertex the ray that leaves it hits.
 constexpr uint32_t kBdEyeBase = 1, kBdLightBase = 129;
 constexpr int kBdMaxVerts = 64;
+// kinds (2 bits): kBdArea a light endpoint at a finite position (light::area, light::point),
+// kBdInfinite an environment or directional light endpoint, or the environment hit by a subpath.
+// kBdDelta marks a point or directional light endpoint: degenerate or specular, so the strategy
+// that would reach it by tracing (s = 0) does not exist (bidir.h:187-191).
 enum : uint32_t { kBdSurface = 0, kBdCamera = 1, kBdArea = 2, kBdInfinite = 3 };
+constexpr uint32_t kBdDelta = 4u;
 // ext-queue flags of the BDPT subpaths: bits 8-15 the vertex the ray leaves, then these
 constexpr uint32_t kBdLightSub = 1u << 16, kBdInfOrigin = 1u << 17, kBdDegOrigin = 1u << 18;
 
@@ -1162,6 +1218,7 @@ struct BdVtx {
     int32_t light, mat;
     float pc, qf, pc_out, prev_rev, G;
     bool spec;
+    bool delta;  // a point or directional light endpoint
 };
 // Records: 5 float4 per vertex, [subpath][vertex][sample] so that consecutive samples read
 // consecutive records. r4 = (qf, +-pc_out, prev_rev, pc) alone carries what the weight sweep
@@ -1180,7 +1237,7 @@ __device__ inline size_t bd_at(const BdRec& R, int sub, int j, int64_t k) {
 }
 __device__ inline void bd_store(const BdRec& R, int sub, int j, int64_t k, const BdVtx& v) {
     float4* q = R.r + bd_at(R, sub, j, k);
-    const uint32_t word = v.kind | (v.comp << 4) | (uint32_t(v.light + 1) << 8);
+    const uint32_t word = v.kind | (v.delta ? kBdDelta : 0u) | (v.comp << 4) | (uint32_t(v.light + 1) << 8);
     q[0] = make_float4(v.p.x, v.p.y, v.p.z, __uint_as_float(word));
     q[1] = make_float4(v.n.x, v.n.y, v.n.z, __int_as_float(v.mat));
     q[2] = make_float4(v.gn.x, v.gn.y, v.gn.z, v.pc);
@@ -1198,6 +1255,7 @@ __device__ inline BdVtx bd_load(const BdRec& R, int sub, int j, int64_t k) {
     const uint32_t word = __float_as_uint(r0.w);
     v.p = mk(r0.x, r0.y, r0.z);
     v.kind = word & 3u;
+    v.delta = (word & kBdDelta) != 0u;
     v.comp = (word >> 4) & 15u;
     v.light = int32_t(word >> 8) - 1;
     v.n = mk(r1.x, r1.y, r1.z);
@@ -1247,7 +1305,7 @@ __global__ void __launch_bounds__(kBlock) k_bd_generate(const __grid_constant__ 
         BdVtx c;
         c.p = S.cam_p; c.n = c.gn = mk(0, 0, 0); c.a = mk(1, 1, 1);
         c.kind = kBdCamera; c.comp = 0; c.light = -1; c.mat = -1; c.pc = 1.f;
-        c.qf = 1.f; c.pc_out = 1.f; c.prev_rev = 0.f; c.G = 0.f; c.spec = false;
+        c.qf = 1.f; c.pc_out = 1.f; c.prev_rev = 0.f; c.G = 0.f; c.spec = false; c.delta = false;
         bd_store(R, 0, 0, i, c);
         R.nv[i] = 1;
         const f3 de = primary_dir(S, u[4], u[5]);
@@ -1268,22 +1326,27 @@ __global__ void __launch_bounds__(kBlock) k_bd_generate(const __grid_constant__ 
         BdVtx l;
         l.comp = 0; l.light = li; l.mat = -1; l.pc = 1.f; l.pc_out = 1.f; l.prev_rev = 0.f; l.G = 0.f; l.spec = false;
         float pdir;
-        if (S.lights[li].type == LMGPU_LIGHT_AREA) {
+        const int32_t ltype = S.lights[li].type;
+        l.delta = ltype == LMGPU_LIGHT_POINT || ltype == LMGPU_LIGHT_DIRECTIONAL;
+        if (ltype == LMGPU_LIGHT_AREA || ltype == LMGPU_LIGHT_POINT) {
+            // connectable endpoints: qf = pdf_position (light_area.cpp:142; light_point.cpp:78-80: 1),
+            // the first direction's pdf cosine-weighted, or uniform from a point (light_point.cpp:64-66)
             l.kind = kBdArea; l.p = o; l.n = l.gn = ln;
-            l.qf = bd_area_pa(S, li);
+            l.qf = ltype == LMGPU_LIGHT_AREA ? bd_area_pa(S, li) : 1.f / float(S.num_lights);
             const float ia = 1.f / l.qf;
             l.a = mk(ia, ia, ia);
-            pdir = dot(d, ln) <= 0.f ? 0.f : 1.f / kPi;
+            pdir = ltype == LMGPU_LIGHT_POINT ? 1.f / (4.f * kPi) : (dot(d, ln) <= 0.f ? 0.f : 1.f / kPi);
         } else {
+            // pdf_primary_ray of the endpoint (light_directional.cpp:72-75 without eval_delta)
             l.kind = kBdInfinite; l.p = d; l.n = l.gn = mk(0, 0, 0); l.a = mk(0, 0, 0);
             l.qf = 1.f;
-            pdir = bd_env_pray(S);
+            pdir = ltype == LMGPU_LIGHT_DIRECTIONAL ? (1.f / float(S.num_lights)) * (1.f / (kPi * S.bound_r * S.bound_r)) : bd_env_pray(S);
         }
         bd_store(R, 1, 0, i, l);
         R.nv[R.W + i] = 1;
         if (is_zero(w) || R.max_l < 2) continue;
-        push_ext<false>(q, qcount, o, d, w, pdir, l.n, kBdLightSub | (l.kind == kBdInfinite ? kBdInfOrigin : 0u), uint32_t(path),
-                        uint32_t(i), 0u);
+        const uint32_t oflag = l.kind == kBdInfinite ? kBdInfOrigin : (ltype == LMGPU_LIGHT_POINT ? kBdDegOrigin : 0u);
+        push_ext<false>(q, qcount, o, d, w, pdir, l.n, kBdLightSub | oflag, uint32_t(path), uint32_t(i), 0u);
     }
 }
 
@@ -1306,7 +1369,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_shade(const __grid_co
         const f3 o = mk(o4.x, o4.y, o4.z), d = mk(d4.x, d4.y, d4.z), thr = mk(t4.x, t4.y, t4.z), no = mk(n4.x, n4.y, n4.z);
         const int32_t id = __float_as_int(h4.w);
         BdVtx v;
-        v.a = thr; v.pc = 1.f; v.comp = 0; v.pc_out = 1.f; v.prev_rev = 0.f; v.spec = false;
+        v.a = thr; v.pc = 1.f; v.comp = 0; v.pc_out = 1.f; v.prev_rev = 0.f; v.spec = false; v.delta = false;
         if (id < 0) {
             if (S.env_light < 0) continue;  // nothing hit: the subpath ends
             // the environment as a vertex (scene.cpp:321-331); G with an infinite end: |n_o . d|
@@ -1433,7 +1496,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
             raster_pos(S, de, rx, ry);
             eye_px = pixel_of(P, rx, ry);
         }
-        const bool env_l0 = nL > 0 && (__float_as_uint(R.r[bd_at(R, 1, 0, k)].w) & 3u) == kBdInfinite;
+        const uint32_t w0 = nL > 0 ? __float_as_uint(R.r[bd_at(R, 1, 0, k)].w) : 0u;
+        const bool env_l0 = nL > 0 && (w0 & 3u) == kBdInfinite;
+        const bool delta_l0 = (w0 & kBdDelta) != 0u;  // x_0 = L[0] cannot be reached by tracing
         const BdVtx vE = bd_load(R, 0, t - 1, k);
         f3 Cu;
         uint32_t px = eye_px;
@@ -1478,11 +1543,17 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 const float L2 = dot(dv, dv);
                 const f3 dn = dv / sqrtf(L2);
                 const float c2 = vE.kind == kBdCamera ? 1.f : fabsf(dot(vE.n, -dn));
-                return fabsf(dot(vL.n, dn)) * c2 / L2;
+                const float c1 = vL.delta ? 1.f : fabsf(dot(vL.n, dn));  // a point light is degenerate
+                return c1 * c2 / L2;
             }();
             f3 fL, fE;
             float pLf, pcL = 1.f;
-            if (s == 1) {
+            if (s == 1 && vL.delta) {
+                // light::point: Le toward every direction, pdf_direction 1 / (4 pi) (light_point.cpp:64-66, 117-119)
+                const DevLight L = S.lights[vL.light];
+                fL = mk(L.ke[0], L.ke[1], L.ke[2]);
+                pLf = 1.f / (4.f * kPi);
+            } else if (s == 1) {
                 const DevLight L = S.lights[vL.light];
                 const bool front = dot(dLE, vL.n) > 0.f;
                 fL = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
@@ -1562,8 +1633,9 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 if (den == 0.f) { ok = false; break; }
                 const float num = j == s - 1 ? qEs1 : (j == s - 2 ? qEs2 : cout(cur) * above.z);
                 r *= num / den;
-                // samplable(j): x_{j-1} (L[j-1]) and x_j (L[j]) not specular; x_0 an endpoint
-                const bool samp = j == 0 || (!(j == 1 && inf0) && !(j - 1 != 0 && spec_of(below)) && !spec_of(cur));
+                // samplable(j): x_{j-1} (L[j-1]) and x_j (L[j]) not specular; x_0 an endpoint that
+                // tracing reaches (not a point or directional light)
+                const bool samp = j == 0 ? !delta_l0 : (!(j == 1 && inf0) && !(j - 1 != 0 && spec_of(below)) && !spec_of(cur));
                 if (r != 0.f && samp) inv += opt ? r : r * r;
                 above = cur;
                 cur = below;
@@ -1996,6 +2068,7 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         std::vector<DevLight> lights(D->num_lights);
         std::vector<float> cdf, ltri, env;
         int32_t env_light = -1;
+        bool has_directional = false;
         for (int32_t i = 0; i < D->num_lights; i++) {
             const lmgpu_light& L = D->lights[i];
             DevLight& dl = lights[i];
@@ -2059,6 +2132,17 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
                     dl.cond_off = int32_t(env.size());
                     for (double v : cond) env.push_back(float(v));
                 }
+            } else if (L.type == LMGPU_LIGHT_POINT) {
+                dl.v[0] = L.vec[0]; dl.v[1] = L.vec[1]; dl.v[2] = L.vec[2];
+                if (!std::isfinite(dl.v[0]) || !std::isfinite(dl.v[1]) || !std::isfinite(dl.v[2]))
+                    throw Error(LMGPU_ERR_INVALID_ARGUMENT, "point light position is not finite");
+            } else if (L.type == LMGPU_LIGHT_DIRECTIONAL) {
+                // light_directional.cpp:36: the direction normalized (in double)
+                const double x = L.vec[0], y = L.vec[1], z = L.vec[2];
+                const double len = std::sqrt(x * x + y * y + z * z);
+                if (!(len > 0) || !std::isfinite(len)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "directional light needs a nonzero direction");
+                dl.v[0] = float(x / len); dl.v[1] = float(y / len); dl.v[2] = float(z / len);
+                has_directional = true;
             } else {
                 throw Error(LMGPU_ERR_UNSUPPORTED, "unknown light type");
             }
@@ -2070,15 +2154,17 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
 
         // scene.cpp:288-311 and light_envconst.cpp:38-43: the bound of every triangle in world space
         // (two-level scenes: each instance's BLAS triangles moved by its transform), as a sphere
-        // of radius 1.01 |max - center|; only environment lights use it
+        // of radius 1.01 |max - center| (light_directional.cpp:40-45 alike); environment and
+        // directional lights use it
+        const bool need_bound = env_light >= 0 || has_directional;
         double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
         auto grow = [&](double x, double y, double z) {
             lo[0] = std::min(lo[0], x); lo[1] = std::min(lo[1], y); lo[2] = std::min(lo[2], z);
             hi[0] = std::max(hi[0], x); hi[1] = std::max(hi[1], y); hi[2] = std::max(hi[2], z);
         };
-        if (env_light >= 0 && !two_level) {
+        if (need_bound && !two_level) {
             for (int64_t k = 0; k < 3 * nt; k++) grow(D->positions[3 * k], D->positions[3 * k + 1], D->positions[3 * k + 2]);
-        } else if (env_light >= 0) {
+        } else if (need_bound) {
             for (int32_t i = 0; i < accel->num_instances; i++) {
                 const double* M = &accel->inst_xform[size_t(12) * i];
                 const int b = accel->inst_blas[i];
@@ -2104,6 +2190,7 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         ds.feat = two_level ? kFeatTwoLevel : 0u;
         for (int32_t i = 0; i < D->num_lights; i++)
             if (D->lights[i].type == LMGPU_LIGHT_ENV) ds.feat |= kFeatEnvTex;
+            else if (D->lights[i].type == LMGPU_LIGHT_POINT || D->lights[i].type == LMGPU_LIGHT_DIRECTIONAL) ds.feat |= kFeatDelta;
         for (int32_t i = 0; i < D->num_materials; i++)
             if (D->materials[i].type == LMGPU_MAT_MIXTURE) ds.feat |= kFeatMixture;
         ds.shade = s->shade.as<const float4>();
@@ -3083,7 +3170,8 @@ __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
 using WfShadeK = decltype(&k_wf_shade<4, true, kFeatAll>);
 WfShadeK wf_shade_single(uint32_t feat) {
     constexpr int mb = LMGPU_SHADE_SINGLE_MINBLOCKS;
-    switch (feat & kFeatAll) {
+    if (feat & kFeatDelta) return k_wf_shade<mb, true, kFeatAll>;
+    switch (feat & 7u) {
     case 0: return k_wf_shade<mb, true, 0u>;
     case 1: return k_wf_shade<mb, true, 1u>;
     case 2: return k_wf_shade<mb, true, 2u>;

@@ -596,6 +596,30 @@ class LightEnvConst(_Light):
         self.Le = _vec3(_req(prop, "Le"))
 
 
+@_reg("light::point")
+class LightPoint(_Light):
+    """light::point (light_point.cpp:34-37): Le and a world-space position; the transform of the
+    primitive node that holds it is not applied, as in the reference."""
+
+    def construct(self, prop):
+        self.Le = _vec3(_req(prop, "Le"))
+        self.position = _vec3(_req(prop, "position"))
+
+
+@_reg("light::directional")
+class LightDirectional(_Light):
+    """light::directional (light_directional.cpp:34-37): Le and the direction the light travels,
+    normalized."""
+
+    def construct(self, prop):
+        self.Le = _vec3(_req(prop, "Le"))
+        d = _vec3(_req(prop, "direction"))
+        n = float(np.linalg.norm(d))
+        if not n > 0:
+            raise LmGpuError(1, f"Invalid direction {prop['direction']!r}")
+        self.direction = d / n
+
+
 @_reg("light::env")
 class LightEnv(_Light):
     """light::env. The reference loads envmap_path through texture::bitmap; here 'envmap_path'
@@ -1031,6 +1055,14 @@ class SceneDefault(Component):
             elif isinstance(comp_, LightEnvConst):
                 L.type = 1
                 L.ke[:] = [float(x) for x in comp_.Le]
+            elif isinstance(comp_, LightPoint):
+                L.type = 3
+                L.ke[:] = [float(x) for x in comp_.Le]
+                L.vec[:] = [float(x) for x in comp_.position]
+            elif isinstance(comp_, LightDirectional):
+                L.type = 4
+                L.ke[:] = [float(x) for x in comp_.Le]
+                L.vec[:] = [float(x) for x in comp_.direction]
             elif isinstance(comp_, LightEnv):
                 L.type = 2
                 L.env_w, L.env_h = comp_.data.shape[1], comp_.data.shape[0]

@@ -36,7 +36,7 @@ class Material(C.Structure):
 class Light(C.Structure):
     _fields_ = [("type", C.c_int32), ("ke", C.c_float * 3), ("tri_offset", C.c_int64), ("tri_count", C.c_int64),
                 ("transform_j", C.c_float), ("env_w", C.c_int32), ("env_h", C.c_int32), ("env_offset", C.c_int64),
-                ("rot_deg", C.c_float), ("scale", C.c_float)]
+                ("rot_deg", C.c_float), ("scale", C.c_float), ("vec", C.c_float * 3)]
 
 
 class Camera(C.Structure):

@@ -11,7 +11,7 @@
 //   src/mesh/mesh_raw.cpp                 -> Mesh
 //   src/camera/camera_pinhole.cpp         -> Camera
 //   src/material/material_{diffuse,glossy,glass,mirror}.cpp -> Material
-//   src/light/light_{area,envconst,env}.cpp, src/texture/texture_bitmap.cpp -> Light
+//   src/light/light_{area,envconst,env,point,directional}.cpp, src/texture/texture_bitmap.cpp -> Light
 //   src/renderer/renderer_{raycast,pt}.cpp, src/scheduler.cpp, src/parallel/parallel_openmp.cpp
 //   src/film/film_bitmap.cpp, include/lm/film.h -> Film
 // Templated on Float: double is the faithful mode (the reference's Float), float is the fp32
@@ -384,14 +384,16 @@ template <typename F> struct Material {
 };
 
 // ------------------------------------------------------------------------------------------------
-// Lights: src/light/light_area.cpp, light_envconst.cpp, light_env.cpp
-enum LightType { LIGHT_AREA = 0, LIGHT_ENVCONST = 1, LIGHT_ENV = 2 };
+// Lights: src/light/light_area.cpp, light_envconst.cpp, light_env.cpp, light_point.cpp,
+// light_directional.cpp
+enum LightType { LIGHT_AREA = 0, LIGHT_ENVCONST = 1, LIGHT_ENV = 2, LIGHT_POINT = 3, LIGHT_DIRECTIONAL = 4 };
 
 template <typename F> struct LightSample { PointGeometry<F> geom; V3<F> wo; V3<F> weight; };
 
 template <typename F> struct Light {
     int type = LIGHT_AREA;
-    V3<F> Ke;            // area: Ke; envconst: Le
+    V3<F> Ke;            // area: Ke; envconst, point, directional: Le
+    V3<F> pos;           // point: its world position; directional: its normalized direction
     int mesh = -1;       // area
     Dist<F> dist;        // area: triangle-area CDF
     F invA = 0;          // area
@@ -401,8 +403,11 @@ template <typename F> struct Light {
     F rot = 0, scale = 1;
     Dist2<F> dist2;
 
-    bool is_env() const { return type != LIGHT_AREA; }
-    bool is_infinite() const { return type != LIGHT_AREA; }
+    bool is_env() const { return type == LIGHT_ENVCONST || type == LIGHT_ENV; }
+    bool is_infinite() const { return is_env() || type == LIGHT_DIRECTIONAL; }
+    // light_directional.cpp:131-133 (the others: false)
+    bool is_specular() const { return type == LIGHT_DIRECTIONAL; }
+    bool is_delta() const { return type == LIGHT_POINT || type == LIGHT_DIRECTIONAL; }
 
     // texture_bitmap.cpp:68-75
     V3<F> tex_eval(V2<F> t) const {
@@ -429,6 +434,8 @@ template <typename F> struct Light {
         switch (type) {
         case LIGHT_AREA: return dot(wo, g.n) <= F(0) ? V3<F>(F(0)) : Ke;
         case LIGHT_ENVCONST: return Ke;
+        case LIGHT_POINT: return Ke;        // light_point.cpp:117-119
+        case LIGHT_DIRECTIONAL: return Ke;  // light_directional.cpp:143-145 without eval_delta
         case LIGHT_ENV: {
             const auto d = -g.wo;
             auto at = std::atan2(d.x, d.z);
@@ -463,6 +470,12 @@ template <typename F> struct Light {
             const auto pdfSA = dist2.pdf(u, v) / (F(2) * C<F>::Pi * C<F>::Pi * st);
             return convert_pdf_SA_to_projSA(pdfSA, g, d);
         }
+        case LIGHT_POINT: {  // light_point.cpp:97-100
+            const auto G = geometry_term(g, gL);
+            return G == F(0) ? F(0) : F(1) / G;
+        }
+        case LIGHT_DIRECTIONAL:  // light_directional.cpp:121-124 without eval_delta
+            return convert_pdf_SA_to_projSA(F(1), g, -gL.wo);
         }
         return F(0);
     }
@@ -843,6 +856,21 @@ template <typename F> struct Scene {
             s = LightSample<F>{gL, wo, Le / pL};
             break;
         }
+        case LIGHT_POINT: {  // light_point.cpp:84-95
+            const auto wo = normalize(g.p - L.pos);
+            const auto gL = PointGeometry<F>::make_degenerated(L.pos);
+            const auto pL = L.pdf_direct(g, gL, lpi.tr, wo);
+            if (pL == F(0)) return {};
+            s = LightSample<F>{gL, wo, L.Ke / pL};
+            break;
+        }
+        case LIGHT_DIRECTIONAL: {  // light_directional.cpp:109-119
+            const auto gL = PointGeometry<F>::make_infinite(L.pos);
+            const auto pL = L.pdf_direct(g, gL, lpi.tr, L.pos);
+            if (pL == F(0)) return {};
+            s = LightSample<F>{gL, L.pos, L.Ke / pL};
+            break;
+        }
         }
         if (s) s->weight = s->weight / p_sel;
         return s;
@@ -866,6 +894,21 @@ template <typename F> struct Scene {
             const auto Le = L.eval(gL, wo);
             const auto p = pA * (F(1) / C<F>::Pi);
             s = LightSample<F>{gL, wo, Le / p};
+        } else if (L.type == LIGHT_POINT) {
+            // light_point.cpp:39-49: a uniform direction from the light's position
+            const auto d = sample_uniform_sphere(ud);
+            s = LightSample<F>{PointGeometry<F>::make_degenerated(L.pos), d, L.Ke / pdf_uniform_sphere<F>()};
+        } else if (L.type == LIGHT_DIRECTIONAL) {
+            // light_directional.cpp:49-70: the light's direction from a point on the disk of the
+            // scene's bounding sphere facing it
+            const auto d = L.pos;
+            const auto pl = sample_uniform_disk(up) * sphere_radius;
+            V3<F> u, v;
+            orthonormal_basis(d, u, v);
+            auto gL = PointGeometry<F>::make_infinite(d);
+            gL.p = sphere_center + sphere_radius * (-d) + (u * pl.x + v * pl.y);
+            const auto p = F(1) / (C<F>::Pi * sphere_radius * sphere_radius);
+            s = LightSample<F>{gL, d, L.eval(gL, d) / p};
         } else {
             // a uniform direction, then a point on the disk of the scene's bounding sphere facing it
             const auto d = sample_uniform_sphere(ud);
@@ -1060,7 +1103,10 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
                           shading_normal_correction(sp.geom, wi, wo, TransDir::EL);
                 if (is_zero(fs)) return;
                 F mis_w = F(1);
-                if (P.sampling_mode == 2) {
+                // renderer_pt.cpp:166-180: a light that BSDF sampling cannot reach (a specular
+                // light, or a degenerate light position) keeps weight 1
+                const bool samplable_by_bsdf = !scene.light_of(light_node).is_specular() && !sL->geom.degenerated;
+                if (P.sampling_mode == 2 && samplable_by_bsdf) {
                     const F p_light = scene.pdf_direct_light(sp, spL, sL->wo);
                     const F p_bsdf = sp.type == SI_Camera ? cam.pdf_direction(wo)
                                                           : scene.material_of(sp.primitive).pdf_direction(sp.geom, wi, wo, comp, true);
@@ -1304,11 +1350,13 @@ template <typename F> struct Bidir {
     // path.h:695-725
     bool is_specular(const SceneInteraction<F>& sp, int comp) const {
         if (sp.type == SI_Surface) return scene.material_of(sp.primitive).is_specular_component(comp);
-        return false;  // lights and the pinhole camera are not specular
+        if (sp.type == SI_Light) return light(sp).is_specular();  // light::directional
+        return false;  // the pinhole camera is not specular
     }
     bool is_connectable(const SceneInteraction<F>& sp) const {
         if (sp.type == SI_Camera) return true;                   // camera_pinhole.cpp:228-230
-        return light(sp).type == LIGHT_AREA;                     // light_area.cpp:181 / light_env*.cpp
+        // light_area.cpp:181, light_point.cpp:113; light_env*.cpp and light_directional.cpp: false
+        return light(sp).type == LIGHT_AREA || light(sp).type == LIGHT_POINT;
     }
     // path.h:761-775 (eval_contrb_direction)
     V3F eval_dir(const SceneInteraction<F>& sp, V3F wi, V3F wo, int comp, TransDir td, bool eval_delta) const {
@@ -1321,6 +1369,7 @@ template <typename F> struct Bidir {
     F pdf_dir(const SceneInteraction<F>& sp, V3F wi, V3F wo, int comp) const {
         if (sp.type == SI_Camera) return cam().pdf_direction(wo);
         if (sp.type == SI_Light) {
+            if (light(sp).type == LIGHT_POINT) return pdf_uniform_sphere<F>();  // light_point.cpp:64-66
             if (light(sp).type != LIGHT_AREA) throw std::runtime_error("pdf_direction of an infinite light");
             return dot(wo, sp.geom.n) <= F(0) ? F(0) : F(1) / C<F>::Pi;
         }
@@ -1334,17 +1383,23 @@ template <typename F> struct Bidir {
     F pdf_position(const SceneInteraction<F>& sp) const {
         if (sp.type == SI_Camera) return F(1);
         const auto& L = light(sp);
+        if (L.type == LIGHT_POINT) return scene.pdf_light_selection();  // light_point.cpp:78-80
         if (L.type != LIGHT_AREA) throw std::runtime_error("pdf_position of an infinite light");
         return scene.pdf_light_selection() * (L.invA / light_tr(sp).J);
     }
     // path.h:149-162 with camera_pinhole.cpp:142-146, light_area.cpp:102-106,
-    // light_envconst.cpp:70-74 and light_env.cpp:109-113
+    // light_envconst.cpp:70-74, light_env.cpp:109-113, light_point.cpp:51-53 and
+    // light_directional.cpp:72-75 (eval_delta false)
     F pdf_primary_ray(const SceneInteraction<F>& sp, V3F wo) const {
         if (sp.type == SI_Camera) return cam().pdf_direction(wo) * F(1);
         const auto& L = light(sp);
         F p;
         if (L.type == LIGHT_AREA) {
             p = (L.invA / light_tr(sp).J) * (dot(wo, sp.geom.n) <= F(0) ? F(0) : F(1) / C<F>::Pi);
+        } else if (L.type == LIGHT_POINT) {
+            p = pdf_uniform_sphere<F>();  // light_point.cpp:51-53
+        } else if (L.type == LIGHT_DIRECTIONAL) {
+            p = F(1) / (C<F>::Pi * scene.sphere_radius * scene.sphere_radius);  // light_directional.cpp:72-75
         } else {
             p = pdf_uniform_sphere<F>() * (F(1) / (C<F>::Pi * scene.sphere_radius * scene.sphere_radius));
         }

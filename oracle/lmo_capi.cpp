@@ -116,6 +116,34 @@ int lmo_add_light_envconst(void* p, const double* Le) {
     });
 }
 
+// light::point (src/light/light_point.cpp:34-37): Le and a world-space position.
+int lmo_add_light_point(void* p, const double* Le, const double* position) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Light<F> L;
+        L.type = LIGHT_POINT;
+        L.Ke = V3<F>(F(Le[0]), F(Le[1]), F(Le[2]));
+        L.pos = V3<F>(F(position[0]), F(position[1]), F(position[2]));
+        S.lights_assets.push_back(std::move(L));
+        return int(S.lights_assets.size()) - 1;
+    });
+}
+
+// light::directional (src/light/light_directional.cpp:34-37): Le and the normalized direction.
+int lmo_add_light_directional(void* p, const double* Le, const double* direction) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        Light<F> L;
+        L.type = LIGHT_DIRECTIONAL;
+        L.Ke = V3<F>(F(Le[0]), F(Le[1]), F(Le[2]));
+        L.pos = normalize(V3<F>(F(direction[0]), F(direction[1]), F(direction[2])));
+        S.lights_assets.push_back(std::move(L));
+        return int(S.lights_assets.size()) - 1;
+    });
+}
+
 // light::env with an in-memory texture (row 0 = first row of `texels`, c channels, fp32).
 int lmo_add_light_env(void* p, const float* texels, int w, int hgt, int c, double rot_deg, double scale) {
     auto* h = static_cast<Handle*>(p);

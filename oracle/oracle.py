@@ -41,6 +41,8 @@ def lib() -> C.CDLL:
         L.lmo_add_material.argtypes = [vp, C.c_int, dp]
         L.lmo_add_light_area.argtypes = [vp, dp, C.c_int]
         L.lmo_add_light_envconst.argtypes = [vp, dp]
+        L.lmo_add_light_point.argtypes = [vp, dp, dp]
+        L.lmo_add_light_directional.argtypes = [vp, dp, dp]
         L.lmo_add_light_env.argtypes = [vp, fp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double]
         L.lmo_add_camera.argtypes = [vp, dp, dp, dp, C.c_double, C.c_double]
         L.lmo_create_primitive_node.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
@@ -120,6 +122,12 @@ class OracleScene:
 
     def add_envconst(self, Le) -> int:
         return _chk(lib().lmo_add_light_envconst(self.h, _dp(Le)))
+
+    def add_point(self, Le, position) -> int:
+        return _chk(lib().lmo_add_light_point(self.h, _dp(Le), _dp(position)))
+
+    def add_directional(self, Le, direction) -> int:
+        return _chk(lib().lmo_add_light_directional(self.h, _dp(Le), _dp(direction)))
 
     def add_env(self, texels: np.ndarray, rot: float = 0.0, scale: float = 1.0) -> int:
         t = np.ascontiguousarray(texels, np.float32)
@@ -269,6 +277,10 @@ def from_lm_scene(scene, double: bool = True) -> OracleScene:
                     light_id[id(L)] = O.add_area_light(L.Ke, mesh_of(L.mesh))
                 elif L.key_name == "light::envconst":
                     light_id[id(L)] = O.add_envconst(L.Le)
+                elif L.key_name == "light::point":
+                    light_id[id(L)] = O.add_point(L.Le, L.position)
+                elif L.key_name == "light::directional":
+                    light_id[id(L)] = O.add_directional(L.Le, L.direction)
                 else:
                     light_id[id(L)] = O.add_env(L.data, L.rot, L.scale)
             li = light_id[id(L)]
