@@ -29,6 +29,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 import time
+import zlib
 from typing import Any
 
 import numpy as np
@@ -564,8 +565,9 @@ class TextureBitmap(Component):
 
 
 def _read_image(path: str, flip: bool = True) -> np.ndarray:
-    """texture::bitmap's image (texture_bitmap.cpp:49-66), row 0 at the bottom: .hdr (flipped on
-    load unless flip=False), .pfm (stored bottom row first), .npy (as stored)."""
+    """texture::bitmap's image (texture_bitmap.cpp:49-66), row 0 at the bottom: .hdr and .png
+    (flipped on load unless flip=False; a .png becomes linear as stbi_loadf makes it), .pfm
+    (stored bottom row first), .npy (as stored). Three channels are kept."""
     from . import imageio
     try:
         if path.endswith(".npy"):
@@ -574,9 +576,11 @@ def _read_image(path: str, flip: bool = True) -> np.ndarray:
             return imageio.read_pfm(path)
         if path.endswith(".hdr"):
             return imageio.read_hdr(path, flip=flip)
-    except (OSError, ValueError) as e:
+        if path.endswith(".png"):
+            return np.ascontiguousarray(imageio.read_png(path, flip=flip)[..., :3])
+    except (OSError, ValueError, zlib.error) as e:
         raise LmGpuError(4, f"Failed to load image [path='{path}']: {e}") from None
-    raise LmGpuError(2, f"Unsupported image format [path='{path}'] (use .hdr, .pfm or .npy)")
+    raise LmGpuError(2, f"Unsupported image format [path='{path}'] (use .hdr, .png, .pfm or .npy)")
 
 
 class _Light(Component):
