@@ -364,8 +364,8 @@ typedef struct lmgpu_bdpt_params {
     int32_t max_verts;          /* 2..64 */
     uint32_t seed;
     int32_t accumulate;
-    int64_t wave_paths;         /* samples per wave; 0 = 2^20, or fewer so that the connection queue holds
-                                   at most 2^28 rays. Each sample of a wave takes 2 * max_verts * 64 bytes of
+    int64_t wave_paths;         /* samples per wave; 0 = 2^22, or fewer so that the connection queue holds
+                                   at most 2^28 rays. Each sample of a wave takes 2 * max_verts * 80 bytes of
                                    vertex records and max_verts * (max_verts - 1) / 2 * 48 bytes of queue. */
     int32_t strategy;           /* LMGPU_BDPT_* */
     int32_t reserved;

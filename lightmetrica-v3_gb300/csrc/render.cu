@@ -1546,45 +1546,56 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_bd_connect(const __grid_
                 const float c1 = vL.delta ? 1.f : fabsf(dot(vL.n, dn));  // a point light is degenerate
                 return c1 * c2 / L2;
             }();
-            f3 fL, fE;
-            float pLf, pcL = 1.f;
-            if (s == 1 && vL.delta) {
-                // light::point: Le toward every direction, pdf_direction 1 / (4 pi) (light_point.cpp:64-66, 117-119)
+            f3 fL = mk(0, 0, 0), fE = mk(0, 0, 0);
+            float pLf = 0.f, pcL = 1.f, pEf = 0.f, pcE = 1.f;
+            if (s == 1) {
+                // the light endpoint: Le toward the front of an area light (pdf_direction 1 / pi),
+                // toward every direction from a point light (1 / (4 pi), light_point.cpp:64-66, 117-119)
                 const DevLight L = S.lights[vL.light];
-                fL = mk(L.ke[0], L.ke[1], L.ke[2]);
-                pLf = 1.f / (4.f * kPi);
-            } else if (s == 1) {
-                const DevLight L = S.lights[vL.light];
-                const bool front = dot(dLE, vL.n) > 0.f;
+                const bool front = vL.delta || dot(dLE, vL.n) > 0.f;
                 fL = front ? mk(L.ke[0], L.ke[1], L.ke[2]) : mk(0, 0, 0);
-                pLf = front ? 1.f / kPi : 0.f;
-            } else {
-                const DevMaterial m = S.mats[vL.mat];
-                const Geom gL = bd_geom(vL);
-                const f3 wi = bd_toward(R, 1, s - 2, k, vL.p);
-                fL = mat_eval<kF>(m, gL, wi, dLE, int(vL.comp), true, true) * sn_correction_le(gL, wi, dLE);
-                pLf = mat_pdf<kF>(m, gL, wi, dLE, false);
-                pcL = bd_pcomp(m, gL, int(vL.comp), dLE);
-                qEs2 = (opt ? 1.f : fabsf(bd_pdfs(R, 1, s - 2, k).y)) * (mat_pdf<kF>(m, gL, dLE, wi, false) * vL.G);
+                pLf = vL.delta ? 1.f / (4.f * kPi) : (front ? 1.f / kPi : 0.f);
+                if (is_zero(fL)) continue;
             }
-            if (is_zero(fL)) continue;
-            float pEf, pcE = 1.f;
-            if (t == 1) {
+            if (t == 1) {  // the camera endpoint
                 float rx, ry;
                 if (!raster_pos(S, dEL, rx, ry)) continue;
                 const float J = cam_J(S, dEL);
                 fE = mk(J, J, J);
                 pEf = J;
                 px = pixel_of(P, rx, ry);
-            } else {
-                const DevMaterial m = S.mats[vE.mat];
-                const Geom gE = bd_geom(vE);
-                const f3 wi = bd_toward(R, 0, t - 2, k, vE.p);
-                fE = mat_eval<kF>(m, gE, wi, dEL, int(vE.comp), true) * sn_correction(gE, wi, dEL);
-                pEf = mat_pdf<kF>(m, gE, wi, dEL, false);
-                pcE = bd_pcomp(m, gE, int(vE.comp), dEL);
-                qLs1 = (opt ? 1.f : fabsf(bd_pdfs(R, 0, t - 2, k).y)) * (mat_pdf<kF>(m, gE, dEL, wi, false) * vE.G);
             }
+            // Surface connection vertices: the light side (transport LE) and the eye side (EL) run
+            // through one code path, so the material code is emitted once (the kernel is bound by
+            // instruction fetch). Per side: f, the pdf toward the other vertex, the component pdf
+            // there, and the reverse pdf toward the subpath's previous vertex.
+            bool dead = false;
+#pragma unroll 1
+            for (int side = s == 1 ? 1 : 0; side < (t == 1 ? 1 : 2); side++) {
+                const bool le = side == 0;
+                const f3 vp = le ? vL.p : vE.p, vn = le ? vL.n : vE.n, vgn = le ? vL.gn : vE.gn;
+                const int comp = int(le ? vL.comp : vE.comp);
+                const float vG = le ? vL.G : vE.G;
+                const int sub = le ? 1 : 0, prev = (le ? s : t) - 2;
+                const f3 wo = le ? dLE : dEL;
+                const DevMaterial m = S.mats[le ? vL.mat : vE.mat];
+                const Geom g = on_surface(vp, vn, vgn);
+                const f3 wi = bd_toward(R, sub, prev, k, vp);
+                const f3 f = mat_eval<kF>(m, g, wi, wo, comp, true, le) * (le ? sn_correction_le(g, wi, wo) : sn_correction(g, wi, wo));
+                if (is_zero(f)) {
+                    dead = true;
+                    break;
+                }
+                const float pf = mat_pdf<kF>(m, g, wi, wo, false);
+                const float pc = bd_pcomp(m, g, comp, wo);
+                const float qrev = (opt ? 1.f : fabsf(bd_pdfs(R, sub, prev, k).y)) * (mat_pdf<kF>(m, g, wo, wi, false) * vG);
+                if (le) {
+                    fL = f; pLf = pf; pcL = pc; qEs2 = qrev;
+                } else {
+                    fE = f; pEf = pf; pcE = pc; qLs1 = qrev;
+                }
+            }
+            if (dead) continue;
             Cu = aL * (fL * Gc * fE) * aE;
             qLs = (opt ? 1.f : pcE) * (pLf * Gc);
             qEs1 = (opt ? 1.f : pcL) * (pEf * Gc);
@@ -2755,8 +2766,10 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         const int64_t total = prm->num_samples;
         const int mv = prm->max_verts;
         const int64_t pairs = int64_t(mv) * (mv - 1) / 2;  // strategies with s, t >= 1 and s + t <= max_verts
-        // default: 2^20 samples, fewer for long paths so the connection queue stays within 2^28 rays
-        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : std::min<int64_t>(int64_t(1) << 20, (int64_t(1) << 28) / pairs),
+        // default: 2^22 samples (about 21 GB of records and queues at max_verts 11; per bounce the
+        // extend launch then stays full: 2^20 measured 20.3 ms per 2^22-sample frame, 2^21 17.5 ms,
+        // 2^22 16.3 ms), fewer for long paths so the connection queue stays within 2^28 rays
+        const int64_t wave = std::min(prm->wave_paths > 0 ? prm->wave_paths : std::min<int64_t>(int64_t(1) << 22, (int64_t(1) << 28) / pairs),
                                       total);
         const int64_t scap = wave * pairs;
         if (scap > (int64_t(1) << 31) - 1) throw Error(LMGPU_ERR_UNSUPPORTED, "wave_paths too large for max_verts");
