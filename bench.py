@@ -151,6 +151,24 @@ def cpu_port(scene, spp: int, threads: int = 0):
     return S
 
 
+def aggregate_ranks(dist, seconds: float, rays: int, device: str = "cuda") -> tuple[float, int]:
+    """Replicas (one job per GPU, no data-path collective): the job's time is the slowest rank's
+    and its work the rays of every rank. dist None: one process."""
+    if dist is None:
+        return seconds, rays
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    n = torch.tensor([rays], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(n.item())
+
+
+def replica_seed(rank: int, k: int) -> int:
+    """Render seed of step k on a rank: each replica renders its own samples."""
+    return SEED_RENDER + k + 100_003 * rank
+
+
 def run_reference(args) -> None:
     ws, rank, _ = _dist()
     if rank != 0:
@@ -239,7 +257,7 @@ def run_gpu(args) -> None:
             flush_l2()
             cudart.cudaDeviceSynchronize()
             s = N.RenderStats()
-            N.check(L.lmgpu_render_pt(scene._h, film._h, C.byref(params(SPP, SEED_RENDER + k)), None, C.byref(s)))
+            N.check(L.lmgpu_render_pt(scene._h, film._h, C.byref(params(SPP, replica_seed(rank, k))), None, C.byref(s)))
             tot["rays"] += s.rays
             tot["ext"] += s.extension_rays
             tot["sh"] += s.shadow_rays
@@ -272,13 +290,8 @@ def run_gpu(args) -> None:
     d2h = img.nbytes
     h2d = C.sizeof(N.PTParams)
 
-    sec = tot["ms"] / 1e3
-    if dist:
-        import torch
-        t = torch.tensor([sec], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec = float(t.item())
-    value = tot["rays"] * ws / sec / 1e6
+    sec, rays_all = aggregate_ranks(dist, tot["ms"] / 1e3, tot["rays"])
+    value = rays_all / sec / 1e6
 
     # roofline of the dominant kernel
     peaks = _peaks()
@@ -323,7 +336,7 @@ def run_gpu(args) -> None:
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": tot["ms"] / max(1, args.steps), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sec / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"renderer::pt, displaced spheres ({info['triangles']} tris), {W_PX}x{H_PX}, "
                                    f"{SPP} spp, max path length {MAX_VERTS - 1}, MIS",
