@@ -392,10 +392,17 @@ class _Material(Component):
 
 @_reg("material::diffuse")
 class MaterialDiffuse(_Material):
+    """material::diffuse (material_diffuse.cpp:55-95): Kd, or mapKd, which has priority. A mapKd
+    that is a texture::constant evaluates to its color everywhere, so it becomes Kd; image
+    textures are not on the GPU path."""
+
     def construct(self, prop):
-        if "mapKd" in prop:
-            raise LmGpuError(2, "material::diffuse mapKd textures are not supported on the GPU path")
         self.Kd = _vec3(prop.get("Kd", [1, 1, 1]))
+        if prop.get("mapKd") is not None:
+            tex = _resolve(prop["mapKd"])
+            if not isinstance(tex, TextureConstant):
+                raise LmGpuError(2, "material::diffuse mapKd image textures are not supported on the GPU path")
+            self.Kd = np.asarray(tex.color, np.float64)
 
     def native(self):
         m = super().native()
@@ -431,6 +438,26 @@ class MaterialGlass(_Material):
 @_reg("material::mirror")
 class MaterialMirror(_Material):
     pass
+
+
+@_reg("material::proxy")
+class MaterialProxy(_Material):
+    """material::proxy (material_proxy.cpp:25-76): every query goes to the material 'ref' names,
+    so it renders as that material."""
+
+    def construct(self, prop):
+        self.ref = _resolve(_req(prop, "ref"))
+        if not isinstance(self.ref, _Material):
+            raise LmGpuError(1, f"Invalid material reference {prop['ref']!r}")
+
+    def underlying(self) -> "_Material":
+        m = self.ref
+        while isinstance(m, MaterialProxy):
+            m = m.ref
+        return m
+
+    def native(self):
+        return self.underlying().native()
 
 
 @_reg("material::mixture_wavefrontobj")
@@ -549,6 +576,21 @@ class ModelWavefrontObj(Component):
         """Model::create_primitives: fn(mesh, material, light) per group, in file order."""
         for mesh, mat, light in self.groups:
             fn(mesh, mat, light)
+
+
+@_reg("texture::constant")
+class TextureConstant(Component):
+    """texture::constant (texture_constant.cpp:22-56): one color (and an optional alpha) for
+    every texture coordinate; a 1 x 1 image where an image is needed (light::env's envmap)."""
+
+    def construct(self, prop):
+        self.color = _vec3(_req(prop, "color"))
+        self.alpha = float(prop["alpha"]) if prop.get("alpha") is not None else None
+        self.data = np.asarray(self.color, np.float32).reshape(1, 1, 3)
+        self.h, self.w = 1, 1
+
+    def has_alpha(self) -> bool:
+        return self.alpha is not None
 
 
 @_reg("texture::bitmap")

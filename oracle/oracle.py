@@ -263,6 +263,8 @@ def from_lm_scene(scene, double: bool = True) -> OracleScene:
         ma = -1
         if n["material"] is not None:
             m = n["material"]
+            while m.key_name == "material::proxy":   # material_proxy.cpp: every query goes to 'ref'
+                m = m.ref
             if id(m) not in mat_id:
                 k = MAT[m.key_name]
                 params = {0: lambda: list(m.Kd), 1: lambda: list(m.Ks) + [m.ax, m.ay], 2: lambda: [m.Ni], 3: lambda: [],

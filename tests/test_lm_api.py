@@ -246,3 +246,40 @@ def test_time_to_rel_mse():
     q.rel_mse = 0.02 * 8 / 24
     assert RenderServer.time_to_rel_mse(q, 0.02) == 0.0   # k = 8: the base image already had it
     assert RenderServer.time_to_rel_mse(q, 0.01) == 20.0 + 0.25 * 8 - 20.0  # k = 16: 8th own pass
+
+
+def test_material_proxy_and_constant_texture(lm, oracle_mod):
+    """material::proxy renders as the material it refers to (material_proxy.cpp); a diffuse
+    mapKd that is a texture::constant is its color (texture_constant.cpp); a constant texture is
+    a 1 x 1 environment map."""
+    from lightmetrica import synthetic as syn
+    base, _ = syn.box_scene(w=8, h=8, prefix="px0_")
+    S0 = oracle_mod.from_lm_scene(base, double=True)
+    S0.build()
+    ref, _, _, _ = S0.render_pt(8, 8, 8, 5, seed=2)
+    # the same box with its grey walls through a proxy, and a red wall Kd given as a constant texture
+    scene, _ = syn.box_scene(w=8, h=8, prefix="px1_")
+    proxy = lm.load_material("px1_proxy", "proxy", ref="px1_grey")
+    tex = lm.load_texture("px1_tex", "constant", color=[0.75, 0.25, 0.25])
+    red = lm.load_material("px1_red_tex", "diffuse", mapKd=tex, Kd=[0, 1, 0])
+    for n in scene.nodes:
+        if n["type"] == "primitive" and n["material"] is not None:
+            if n["material"].key_name == "material::diffuse" and np.allclose(n["material"].Kd, [0.75, 0.75, 0.75]):
+                n["material"] = proxy
+            elif np.allclose(getattr(n["material"], "Kd", [0, 0, 0]), [0.75, 0.25, 0.25]):
+                n["material"] = red
+    rows = [m.native() for m in scene._flatten()["materials"]]
+    assert any(r.type == 0 and np.allclose(list(r.color), [0.75, 0.75, 0.75]) for r in rows)
+    assert any(r.type == 0 and np.allclose(list(r.color), [0.75, 0.25, 0.25]) for r in rows)
+    S1 = oracle_mod.from_lm_scene(scene, double=True)
+    S1.build()
+    img, _, _, _ = S1.render_pt(8, 8, 8, 5, seed=2)
+    assert np.allclose(img, ref, rtol=1e-12, atol=1e-15)
+    assert np.array_equal(tex.data, np.array([[[0.75, 0.25, 0.25]]], np.float32)) and not tex.has_alpha()
+    env = lm.load_light("px1_env", "env", envmap=tex)
+    assert env.data.shape == (1, 1, 3)
+    with pytest.raises(lm.LmGpuError):
+        lm.load_material("px1_bad", "proxy", ref="px1_tex")    # not a material
+    bmp = lm.load_texture("px1_bmp", "bitmap", data=np.ones((2, 2, 3)))
+    with pytest.raises(lm.LmGpuError):
+        lm.load_material("px1_img", "diffuse", mapKd=bmp)     # image textures stay off the GPU path
