@@ -253,3 +253,17 @@ def test_delta_lights_plane_known_answer_gpu(lm):
     lm.load_renderer("gdp_l", "lt", scene=scene, output=film, max_verts=3, seed=1, scheduler="sample",
                      num_samples=1 << 22).render()
     assert abs(film.buffer().mean() / (0.8 / np.pi * 2 / np.linalg.norm(d)) - 1) < 0.01
+
+
+@pytest.mark.gpu
+def test_scene_create_refuses_bad_delta_lights(lm):
+    """lmgpu_scene_create checks the rows it receives: a directional light needs a nonzero
+    direction, a point light a finite position (the Python components check their props too)."""
+    scene, _ = _plane_scene(lm, "gbd_", "directional", Le=[1, 1, 1], direction=[0, 0, -1])
+    scene.nodes[-1]["light"].direction = np.zeros(3)
+    with pytest.raises(lm.LmGpuError):
+        scene.build()
+    scene, _ = _plane_scene(lm, "gbp_", "point", Le=[1, 1, 1], position=[0, 0, 1])
+    scene.nodes[-1]["light"].position = np.array([0.0, np.nan, 1.0])
+    with pytest.raises(lm.LmGpuError):
+        scene.build()
