@@ -79,3 +79,39 @@ def test_tuning_keys(native_lib):
         assert L.lmgpu_tune_set(b"shade_minblocks", 5) == 1
     finally:
         assert L.lmgpu_tune_set(b"trace_refill", old) == 0
+
+
+_STRUCTS = {"Hit": "lmgpu_hit", "Instance": "lmgpu_instance", "AccelStats": "lmgpu_accel_stats", "Material": "lmgpu_material",
+            "Light": "lmgpu_light", "Camera": "lmgpu_camera", "SceneDesc": "lmgpu_scene_desc",
+            "RaycastParams": "lmgpu_raycast_params", "PTParams": "lmgpu_pt_params", "LTParams": "lmgpu_lt_params",
+            "BDPTParams": "lmgpu_bdpt_params", "RenderStats": "lmgpu_render_stats"}
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every ctypes mirror of a header struct has the C compiler's size and field offsets (the
+    layout a binding in another language must reproduce)."""
+    import shutil
+    import subprocess
+    from lightmetrica import _native as N
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lmgpu.h"', "int main(void) {"]
+    for py, c in _STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for name, _ in getattr(N, py)._fields_:
+            lines.append(f'  printf("{py} {name} %zu\\n", offsetof({c}, {name}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for row in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        py, field, v = row.split()
+        got[(py, field)] = int(v)
+    for py in _STRUCTS:
+        cls = getattr(N, py)
+        assert got[(py, "size")] == C.sizeof(cls), py
+        for name, _ in cls._fields_:
+            assert got[(py, name)] == getattr(cls, name).offset, (py, name)
