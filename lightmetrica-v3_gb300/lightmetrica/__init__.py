@@ -35,6 +35,7 @@ from typing import Any
 import numpy as np
 
 from . import _native as N
+from . import objloader  # lm.objloader.init / shutdown, and the OBJ/MTL parser
 from ._native import LmGpuError
 
 Release = True
@@ -177,6 +178,40 @@ def load(name: str, impl_key: str, prop: dict | None = None, **kw) -> Component:
     return _load(iface, name, impl_key, prop, kw)
 
 
+@_reg("asset_group::default")
+class AssetGroup(Component):
+    """asset_group::default (src/assetgroup.cpp): a named subtree of the asset tree. Assets loaded
+    through it get the locator $.assets.<group>.<name>; groups nest. Serialization of a subtree
+    (save_to_file) is not part of the GPU path."""
+
+    def _child(self, iface: str, name: str, impl: str, prop: dict | None, kw: dict) -> Component:
+        return _load(iface, f"{self._name}.{name}", impl, prop, kw)
+
+    def load_film(self, name, impl, prop=None, **kw): return self._child("film", name, impl, prop, kw)
+    def load_camera(self, name, impl, prop=None, **kw): return self._child("camera", name, impl, prop, kw)
+    def load_mesh(self, name, impl, prop=None, **kw): return self._child("mesh", name, impl, prop, kw)
+    def load_material(self, name, impl, prop=None, **kw): return self._child("material", name, impl, prop, kw)
+    def load_light(self, name, impl, prop=None, **kw): return self._child("light", name, impl, prop, kw)
+    def load_texture(self, name, impl, prop=None, **kw): return self._child("texture", name, impl, prop, kw)
+    def load_model(self, name, impl, prop=None, **kw): return self._child("model", name, impl, prop, kw)
+    def load_accel(self, name, impl, prop=None, **kw): return self._child("accel", name, impl, prop, kw)
+    def load_scene(self, name, impl, prop=None, **kw): return self._child("scene", name, impl, prop, kw)
+    def load_renderer(self, name, impl, prop=None, **kw): return self._child("renderer", name, impl, prop, kw)
+    def load_asset_group(self, name, impl="default", prop=None, **kw): return self._child("asset_group", name, impl, prop, kw)
+
+    def save_to_file(self, path: str) -> None:
+        raise LmGpuError(2, "serialization of assets is not part of the GPU path")
+
+
+def load_asset_group(name, impl="default", prop=None, **kw): return _load("asset_group", name, impl, prop, kw)
+
+
+def get_film(loc: str) -> Component: return _resolve(loc)
+def get_renderer(loc: str) -> Component: return _resolve(loc)
+def get_scene(loc: str) -> Component: return _resolve(loc)
+def get_accel(loc: str) -> Component: return _resolve(loc)
+
+
 class _Namespace:
     pass
 
@@ -202,6 +237,22 @@ parallel.shutdown = lambda: None
 debug = _Namespace()
 debug.attach_to_debugger = lambda: None
 debug.print_asset_tree = lambda *a, **k: None
+attach_to_debugger = debug.attach_to_debugger
+
+
+class _Enum:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+
+log.LogLevel = _Enum(Debug=-10, Info=10, Warn=20, Err=30, Progress=100, ProgressEnd=101)
+log.LoggerContext = type("LoggerContext", (), {})
+progress.ProgressMode = _Enum(Samples=0, Time=1)
+progress.ProgressContext = type("ProgressContext", (), {})
+# Floating-point type of the reference's build (lm::Float, double by default); the GPU path
+# computes in fp32 (FloatT says so, for scripts that pick tolerances by it)
+Float32, Float64 = "float32", "float64"
+FloatT = Float32
 
 
 def registered_components() -> list[str]:

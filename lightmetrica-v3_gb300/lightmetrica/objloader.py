@@ -167,3 +167,12 @@ def load_obj(path: str) -> OBJModel:
         materials.append(MTLMaterial("default", illum=-1, Kd=(1.0, 1.0, 1.0)))
     return OBJModel(np.asarray(ps, np.float64).reshape(-1, 3), np.asarray(ns, np.float64).reshape(-1, 3),
                     np.asarray(ts, np.float64).reshape(-1, 2), prims, materials)
+
+
+def init(name: str = "simple", prop: dict | None = None) -> None:
+    """lm.objloader.init: the reference selects objloader::simple or objloader::tinyobjloader; the
+    GPU path's model::wavefrontobj always parses with this module (the objloader::simple rules)."""
+
+
+def shutdown() -> None:
+    """lm.objloader.shutdown: nothing to release."""

@@ -283,3 +283,26 @@ def test_material_proxy_and_constant_texture(lm, oracle_mod):
     bmp = lm.load_texture("px1_bmp", "bitmap", data=np.ones((2, 2, 3)))
     with pytest.raises(lm.LmGpuError):
         lm.load_material("px1_img", "diffuse", mapKd=bmp)     # image textures stay off the GPU path
+
+
+def test_asset_group_and_script_stubs(lm):
+    """lm.load_asset_group (src/assetgroup.cpp): children under $.assets.<group>.<name>, usable as
+    references; the subsystem calls example scripts make (log, progress, objloader, debug) exist."""
+    g = lm.load_asset_group("ag_room", "default")
+    cam = g.load_camera("camera1", "pinhole", position=[0, 0, 5], center=[0, 0, 0], up=[0, 1, 0], vfov=30, aspect=1)
+    assert cam.loc() == "$.assets.ag_room.camera1"
+    assert lm.get("$.assets.ag_room.camera1") is cam
+    sub = g.load_asset_group("sub")
+    mat = sub.load_material("m", "diffuse", Kd=[0.5, 0.5, 0.5])
+    assert mat.loc() == "$.assets.ag_room.sub.m"
+    proxy = lm.load_material("ag_proxy", "proxy", ref="$.assets.ag_room.sub.m")
+    assert proxy.underlying() is mat
+    film = g.load_film("film", "bitmap", w=4, h=4)
+    assert lm.get_film("$.assets.ag_room.film") is film
+    with pytest.raises(lm.LmGpuError):
+        g.save_to_file("x.serialized")
+    lm.log.init("logger::default")
+    lm.progress.init("progress::default")
+    lm.objloader.init("tinyobjloader")
+    lm.debug.print_asset_tree()
+    assert lm.log.LogLevel.Warn > lm.log.LogLevel.Info and lm.FloatT in (lm.Float32, lm.Float64)
