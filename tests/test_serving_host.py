@@ -1,0 +1,142 @@
+"""RenderServer's host logic (admission by measured HBM footprint, least-recently-used eviction of
+idle scenes, the in-flight limit, refinements on a finished film, film release) on the CPU: the
+shared wavefront is replaced by a fake that finishes one sample pass per step, and scenes and
+films by objects with a byte size. The GPU tests run the same server on the real wavefront."""
+import pytest
+
+
+class FakeBatch:
+    def __init__(self, queue_paths=0):
+        self.jobs = {}
+
+    def submit(self, scene, film, *, max_verts, spp, seed=0, accumulate=False, split=False, **kw):
+        j = len(self.jobs)
+        self.jobs[j] = {"spp": spp, "passes": 0, "film": film, "accumulate": accumulate}
+        return j
+
+    def run(self, chunks=0):
+        for j in self.jobs.values():
+            j["passes"] = min(j["spp"], j["passes"] + 1)
+
+    def status(self, job):
+        j = self.jobs[job]
+        return j["passes"], j["passes"] >= j["spp"]
+
+    def resolve(self, job):
+        pass
+
+    def close(self):
+        pass
+
+
+class FakeScene:
+    def __init__(self, key, nbytes):
+        self.key, self.nbytes, self.released = key, nbytes, False
+
+
+class FakeFilm:
+    def __init__(self):
+        self.released = False
+
+    def _release(self):
+        self.released = True
+
+
+@pytest.fixture
+def server(monkeypatch):
+    from lightmetrica import serving
+    import lightmetrica as lm
+    monkeypatch.setattr(serving, "BatchRenderer", FakeBatch)
+    monkeypatch.setattr(serving, "scene_footprint", lambda s: s.nbytes)
+    released = []
+    monkeypatch.setattr(serving, "_release_scene", lambda s: released.append(s.key))
+    monkeypatch.setattr(lm, "load_film", lambda *a, **k: FakeFilm())
+    sizes = {"A": 400, "B": 400, "C": 400, "huge": 5000}
+    t = [0.0]
+
+    def clock():
+        t[0] += 1.0
+        return t[0]
+    srv = serving.RenderServer(lambda key: FakeScene(key, sizes[key]), hbm_budget=1000, max_inflight=3, clock=clock,
+                               build_threads=0)
+    srv.track_error = False
+    srv.released = released
+    yield srv
+    srv.close()
+
+
+def _req(rid, key, spp=2, w=2, h=2, refine=None):
+    from lightmetrica.serving import Request
+    return Request(rid=rid, arrival=0.0, scene_key=key, w=w, h=h, spp=spp, max_verts=5, seed=rid, refine=refine)
+
+
+FILM = 2 * 2 * 3 * 4 * 2   # a 2x2 film: sum and split-pass buffers, fp32
+
+
+def test_admission_waits_for_budget_then_evicts_lru(server):
+    server.submit(_req(0, "A", spp=1))
+    server.submit(_req(1, "B", spp=3))
+    server.step()                       # both admitted; A finishes its one pass in this step
+    assert [r.rid for r in server.inflight] == [1] and server.by_id[0].done is not None
+    assert set(server.scenes) == {"A", "B"} and server.resident_bytes == 800 + 2 * FILM
+    server.submit(_req(2, "C"))
+    server.step()                       # C does not fit while A and B render
+    assert [r.rid for r in server.pending] == [2]
+    while server.inflight:
+        server.step()
+    server.release(0)
+    server.release(1)
+    server.step()                       # A and B idle: C evicts the least recently used (A)
+    assert [r.rid for r in server.inflight] == [2]
+    # C was built once to measure it and released (no room); then A, idle longest, was evicted
+    assert server.released == ["C", "A"] and server.evictions == 1 and server.scene_builds == 4
+    assert set(server.scenes) == {"B", "C"}
+    assert server.peak_resident_bytes <= server.budget
+
+
+def test_scene_larger_than_budget_is_never_admitted(server):
+    server.submit(_req(0, "huge"))
+    for _ in range(3):
+        server.step()
+    assert [r.rid for r in server.pending] == [0] and not server.scenes
+    assert server.released == ["huge"] * 3 or server.released[:1] == ["huge"]
+    assert server.footprints["huge"] == 5000
+
+
+def test_inflight_limit(server):
+    for i in range(5):
+        server.submit(_req(i, "A", spp=4))
+    server.step()
+    assert len(server.inflight) == 3 and len(server.pending) == 2
+    assert server.scene_users["A"] == 3
+
+
+def test_refinement_reuses_the_finished_film(server):
+    server.submit(_req(0, "A", spp=2))
+    server.submit(_req(1, "A", spp=3, refine=0))
+    server.step()
+    assert [r.rid for r in server.pending] == [1]      # waits for its base to finish
+    while not server.idle():
+        server.step()
+    base, ref = server.by_id[0], server.by_id[1]
+    assert ref.film is base.film and ref.base_passes == 2
+    assert server.batch.jobs[ref.job]["accumulate"]
+    assert server.resident_bytes == 400 + FILM          # the refinement adds no film
+    assert ref.first_image is not None and ref.done >= ref.first_image >= ref.admitted
+
+
+def test_release_frees_film_and_guards_refinements(server):
+    server.submit(_req(0, "A"))
+    while not server.idle():
+        server.step()
+    film = server.by_id[0].film
+    server.submit(_req(1, "A", refine=0))
+    with pytest.raises(ValueError):
+        server.release(0)                              # a refinement still waits for this film
+    while not server.idle():
+        server.step()
+    server.release(0)
+    assert film.released and server.resident_bytes == 400
+    server.submit(_req(2, "A", refine=0))
+    with pytest.raises(ValueError):
+        server.step()                                  # refining a released film
