@@ -12,7 +12,7 @@ import time
 
 from .serving import BatchRenderer
 
-DEFAULT_CANDIDATES = (1 << 22, 1 << 23, 1 << 24)
+DEFAULT_CANDIDATES = (1 << 22, 1 << 23, 1 << 24, 1 << 25)
 
 
 def tune_queue(jobs: list[dict], candidates=DEFAULT_CANDIDATES, repeats: int = 1) -> tuple[int, dict]:
