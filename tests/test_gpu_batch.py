@@ -35,11 +35,13 @@ def _scenes(lm):
     return out
 
 
-def test_each_job_same_alone_and_in_mix(lm):
+@pytest.mark.parametrize("queue", [1000, 1 << 25])
+def test_each_job_same_alone_and_in_mix(lm, queue):
+    """A small queue (paths of several jobs share it) and the largest size the autotuner tries."""
     from lightmetrica.serving import BatchRenderer
     jobs = _scenes(lm)
     alone = [_alone(lm, s, f, **kw) for s, f, kw in jobs]
-    b = BatchRenderer(queue_paths=1000)  # a small queue: paths of several jobs share it
+    b = BatchRenderer(queue_paths=queue)
     ids = b.render([dict(scene=s, film=f, **kw) for s, f, kw in jobs])
     for (s, f, kw), a, j in zip(jobs, alone, ids):
         np.testing.assert_allclose(f.buffer_f32(), a, **TOL)
