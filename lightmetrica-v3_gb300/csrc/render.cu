@@ -667,7 +667,7 @@ struct JobDev {
 constexpr int kBlock = 256;
 // Shadow-queue pixel word: bit 31 marks an odd pass of a split-pass film (pixels stay below 2^31).
 constexpr uint32_t kOddPass = 0x80000000u;
-constexpr int64_t kRenderQueue = int64_t(1) << 25;  // paths in flight of lmgpu_render_pt by default (2^24: 1.2 % slower)
+constexpr int64_t kRenderQueue = int64_t(1) << 25;  // paths in flight of lmgpu_render_pt by default (2^24: 1.2 % slower; 2^26: no faster)
 #ifndef LMGPU_TRACE_MINBLOCKS
 #define LMGPU_TRACE_MINBLOCKS 4  // resident 256-thread blocks per SM of the closest-hit kernel (3 and 5 measured slower)
 #endif
