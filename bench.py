@@ -15,26 +15,39 @@ timed with CUDA events on the launching stream. `e2e` is the same metric through
 host memory every step). The scene (BVH, triangles, shading data: well above the 129 MB L2)
 stays resident; L2 is also flushed between timed steps with a 256 MB write.
 
-Two more legs (rank 0) report the batched and served forms (keys "batched" and "served"):
+More legs (rank 0), each a key of the same JSON line:
 
+* raycast -- the plain drop-in workload's probe: 2^24 uniform-sphere rays from one point inside the
+  scene, closest hit through lmgpu_accel_intersect_device (CUDA events) and end to end through
+  lmgpu_accel_intersect; every hit checked against the fp32 oracle (bit-exact count, exact-t ties)
+  and the fp64 oracle timed on 2^21 of the rays as the CPU baseline.
+* frame_vs_golden -- the timed 1920x1080 frame, box-filtered 4x4, against the oracle's 4096-spp
+  480x270 image of the same camera (tests/golden/spheres480_ref_4k.npz): its relative MSE beside
+  what an unbiased render predicts.
 * batched -- 256 procedural jobs (lightmetrica.synthetic.batch_jobs: random-triangle scenes of
   1k-200k triangles, 64^2-512^2, 4-64 spp, path length 6-12), rendered job by job with
   renderer::pt and then all at once through the shared wavefront (queue size autotuned on a
   32-job probe). jobs/s = jobs / wall-clock seconds (host overhead included); the images of the
   two forms are compared (same random streams, so the same estimate up to fp32 summation order).
+* batched_to_error -- the same 256 jobs at equal relative MSE: each renders until its film's
+  reference-free error estimate is at or below --target-rel-mse (1e-3), at most 4096 spp; plain
+  job by job (renderer::pt's 'error' scheduler) against the shared wavefront
+  (BatchRenderer.render_to_error); the estimate is checked against the true relative MSE of the
+  smallest jobs (16k-spp GPU references).
 * instanced -- renderer::pt through the two-level accel on lightmetrica.synthetic.instanced_scene:
   64 instances of a 499k-triangle displaced mesh (32M triangles effective, 1.5M stored), a
   1024x512 procedural HDR environment and 16 area lights, 4096x2160, path length 16.
-* served_stress -- the heavy-tailed mix of the instanced configuration: 1 request in 10 renders
-  the instanced scene at 4096x2160 (1-4 spp), the rest batched-workload scenes, through a
-  RenderServer that builds scenes on admission under a 1.5 GB HBM budget, so memory admission,
-  eviction and rebuilds are exercised (bounded to 300 requests).
-* served -- a Poisson stream of requests over the same scenes (30 % are +16 spp refinements of
-  earlier requests) at 80 % of the batched capacity just measured, through RenderServer under a
-  150 GB HBM budget; reports p50/p99 time-to-first-image (first complete sample pass) and
-  time-to-done from arrival, and from each finished image's relative-MSE estimate (even / odd
-  pass accumulators) the time to reach rel-MSE 1e-3 and 1e-2 over the requests whose sample
-  budget reached it, with the fraction that did.
+* served_stress (and served_stress_150gb) -- the heavy-tailed mix of the instanced configuration:
+  1 request in 10 renders the instanced scene at 4096x2160 (1-4 spp), the rest batched-workload
+  scenes, through a RenderServer that builds scenes on admission under a 1.5 GB HBM budget, so
+  memory admission, eviction and rebuilds are exercised (bounded to 300 requests); the second
+  key runs the same mix under the served configuration's 150 GB budget.
+* served -- a Poisson stream of --served-requests requests (300 by default; the configuration
+  names 5000, which at the target error would take over 15 minutes) over the same scenes at 80 %
+  of the batched capacity at the target error, through RenderServer under a 150 GB HBM budget:
+  new images render to the target error (time-to-target is read at the server's error check,
+  not extrapolated), 30 % of requests are +16 spp refinements of finished films; p50/p99 of
+  time-to-first-image (first complete sample pass), time-to-done and time-to-target.
 
 --impl reference times the CPU restatement of the reference's path (fp64 accel::sahbvh +
 renderer::pt with std::mt19937 per thread under OpenMP, all host cores) on a bounded sample of
@@ -169,13 +182,44 @@ def replica_seed(rank: int, k: int) -> int:
     return SEED_RENDER + k + 100_003 * rank
 
 
+def golden_check(img) -> dict | None:
+    """The rendered 1920x1080 frame box-filtered 4x4 (= the same camera's 480x270 image at 16x the
+    spp) against the committed 4096-spp oracle image tests/golden/spheres480_ref_4k.npz: relative
+    MSE sum((x - ref)^2) / sum(ref^2), and what an unbiased render predicts from the golden's
+    recorded per-sample variance."""
+    import numpy as np
+    g = os.path.join(ROOT, "tests", "golden", "spheres480_ref_4k")
+    if (W_PX, H_PX) != (1920, 1080) or not os.path.exists(g + ".npz") or img is None or img.shape[:2] != (H_PX, W_PX):
+        return None
+    ref = np.load(g + ".npz")["img"].astype(np.float64)
+    meta = json.load(open(g + ".json"))
+    low = img.astype(np.float64).reshape(270, 4, 480, 4, 3).mean(axis=(1, 3))
+    e = float(np.sum((low - ref) ** 2) / np.sum(ref ** 2))
+    spp = SPP * 16
+    pred = meta["sum_var"] * (1.0 / spp + 1.0 / meta["spp"]) / meta["sum_img2"]
+    return {"rel_mse": e, "predicted_unbiased": pred, "golden": "spheres480_ref_4k (oracle fp64, 4096 spp, 480x270)",
+            "filter": "4x4 box: the frame's 480x270 image at 16x its spp"}
+
+
+def workload_config(info: dict, ws: int) -> dict:
+    """The `config` both arms report: the plain drop-in workload one step renders."""
+    return {"workload": f"renderer::pt, displaced spheres ({info['triangles']} tris), {W_PX}x{H_PX}, "
+                        f"{SPP} spp, max path length {MAX_VERTS - 1}, MIS",
+            "triangles": info["triangles"], "spp": SPP, "max_verts": MAX_VERTS,
+            "l2": "inputs larger than L2 (scene resident) and a 256 MB L2 flush between steps",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
 def run_reference(args) -> None:
     ws, rank, _ = _dist()
     if rank != 0:
         return
     from oracle import oracle as O
-    lm, scene, film, info = build_scene()
-    S = cpu_port(scene, 1)
+    from lightmetrica import synthetic as syn  # data only: the reference arm loads no GPU library
+    parts = syn.spheres_parts(seed=SEED_SCENE, w=W_PX, h=H_PX)
+    info = parts["info"]
+    S = O.from_parts(parts, double=True)
+    S.build()
     cores = O.max_threads()
     for _ in range(args.warmup):
         S.render_pt(W_PX, H_PX, 1, MAX_VERTS, seed=SEED_RENDER, rng="mt19937")
@@ -189,10 +233,11 @@ def run_reference(args) -> None:
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"displaced spheres {info['triangles']} tris, {W_PX}x{H_PX}, path length {MAX_VERTS - 1}, "
-                                  f"MIS; sample: 1 spp per step", "triangles": info["triangles"]},
+           "config": workload_config(info, 1),
            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port",
-                            "sample": f"{W_PX}x{H_PX} at 1 spp per step ({W_PX * H_PX} paths), {args.steps} steps"},
+                            "sample": f"each step renders 1 of the workload's {SPP} samples per pixel: {W_PX}x{H_PX} "
+                                      f"at 1 spp ({W_PX * H_PX} paths), {args.steps} steps; Mrays/s counts every "
+                                      f"traced segment, as the GPU arm does"},
            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "build_seconds": S.build_seconds}
     print(json.dumps(out))
@@ -289,6 +334,7 @@ def run_gpu(args) -> None:
             e2e_rays += out["rays"]
     d2h = img.nbytes
     h2d = C.sizeof(N.PTParams)
+    frame_check = golden_check(img)
 
     sec, rays_all = aggregate_ranks(dist, tot["ms"] / 1e3, tot["rays"])
     value = rays_all / sec / 1e6
@@ -322,6 +368,7 @@ def run_gpu(args) -> None:
             n_rays, n_launch = (tot["ext"], tot["ext_launches"]) if dom == "extend" else (tot["sh"], tot["sh_launches"])
             traffic = per_ray * n_rays / max(1, n_launch)
     cpu = None
+    S = None
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         S = cpu_port(scene, 1)
@@ -338,11 +385,7 @@ def run_gpu(args) -> None:
             "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sec / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"renderer::pt, displaced spheres ({info['triangles']} tris), {W_PX}x{H_PX}, "
-                                   f"{SPP} spp, max path length {MAX_VERTS - 1}, MIS",
-                       "triangles": info["triangles"], "spp": SPP, "max_verts": MAX_VERTS,
-                       "l2": "inputs larger than L2 (scene resident) and a 256 MB L2 flush between steps",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": workload_config(info, ws),
             "rays_per_step": tot["rays"] / max(1, args.steps),
             "extension_rays_per_step": tot["ext"] / max(1, args.steps),
             "shadow_rays_per_step": tot["sh"] / max(1, args.steps),
@@ -355,6 +398,7 @@ def run_gpu(args) -> None:
                          "traffic": traffic, "bytes_per_ray": {"extend": b_ext, "shadow": b_sh},
                          "launches": launches, **counts},
             "cpu_baseline": cpu,
+            "frame_vs_golden": frame_check,
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clocks,
             "accel": {"nodes": acc["num_nodes"], "depth": acc["max_depth"], "build_seconds": acc["build_seconds"],
@@ -362,10 +406,17 @@ def run_gpu(args) -> None:
         }
         if not args.no_batched:
             out["batched"], ctx = run_batched(lm, args)
+            if args.target_rel_mse > 0:
+                out["batched_to_error"] = run_batched_to_error(lm, args, ctx)
+                ctx["capacity_to_error"] = out["batched_to_error"]["batched"]["jobs_per_s"]
             if args.served_requests > 0:
                 out["served"] = run_served(lm, args, ctx)
             if args.stress_requests > 0:
                 out["served_stress"] = run_served_stress(lm, args, ctx)
+                # the same mix at the served configuration's 150 GB budget: nothing is evicted
+                out["served_stress_150gb"] = run_served_stress(lm, args, ctx, budget_bytes=150 * 10**9)
+        if args.raycast:
+            out["raycast"] = run_raycast(lm, scene, args, cpu_scene=S if not args.no_cpu else None)
         if args.lt_paths > 0:
             out["lt"] = run_lt(lm, scene, film, args)
         if args.bdpt_samples > 0:
@@ -442,12 +493,83 @@ def run_batched(lm, args) -> tuple[dict, dict]:
                  "paths_per_s": paths / batch_s}
 
 
+def run_batched_to_error(lm, args, ctx) -> dict:
+    """The batched workload at equal relative MSE: every job renders until its film's rel-MSE
+    estimate (even / odd passes, eps 0.01) is at or below args.target_rel_mse, at most
+    args.error_budget_spp samples per pixel. Plain: renderer::pt job by job with the 'error'
+    scheduler (a round of 8 spp, then rounds sized from the estimate, each a full render call).
+    Batched: BatchRenderer.render_to_error, every job in one shared wavefront (a job that reaches
+    its round's count is checked and raised while the others keep the queue full). The estimate
+    is checked against the true relative MSE on the smallest jobs, against GPU renders of 16k spp."""
+    import numpy as np
+    from lightmetrica import _native as N
+    from lightmetrica.serving import BatchRenderer
+    import ctypes as C
+    jobs, scenes = ctx["jobs"], ctx["scenes"]
+    target, budget = args.target_rel_mse, args.error_budget_spp
+    # plain, job by job
+    plain = []
+    t = time.perf_counter()
+    for i, (j, (s, f)) in enumerate(zip(jobs, scenes)):
+        r = lm.load_renderer(f"err_r{i}", "pt", scene=s, output=f, max_verts=j["max_verts"], seed=j["seed"],
+                             scheduler="error", target_rel_mse=target, spp=budget)
+        out = r.render()
+        plain.append({"spp": r.last_spp, "rel_mse": r.last_rel_mse, "rays": out["rays"]})
+    plain_s = time.perf_counter() - t
+    # batched
+    films = [lm.load_film(f"err_out{i}", "bitmap", w=j["res"], h=j["res"]) for i, j in enumerate(jobs)]
+    spec = [dict(scene=s, film=f2, max_verts=j["max_verts"], spp=budget, seed=j["seed"])
+            for j, (s, _), f2 in zip(jobs, scenes, films)]
+    b = BatchRenderer(queue_paths=ctx["queue"])
+    t = time.perf_counter()
+    res = b.render_to_error(spec, target)
+    batch_s = time.perf_counter() - t
+    st = b.stats()
+    b.close()
+    # the estimate against the true relative MSE on the eight smallest jobs (16k-spp GPU reference)
+    small = sorted(range(len(jobs)), key=lambda i: (jobs[i]["res"], jobs[i]["tris"]))[:8]
+    checks = []
+    L = N.lib()
+    for i in small:
+        j = jobs[i]
+        s, _ = scenes[i]
+        ref_f = lm.load_film(f"err_ref{i}", "bitmap", w=j["res"], h=j["res"])
+        p = N.PTParams()
+        p.spp, p.max_verts, p.seed, p.sampling_mode = 16384, j["max_verts"], j["seed"] + 99991, 2
+        N.check(L.lmgpu_render_pt(s._h, ref_f._h, C.byref(p), None, None))
+        ref = ref_f.buffer_f32().astype(np.float64)
+        for form, img, est in (("plain", scenes[i][1].buffer_f32(), plain[i]["rel_mse"]),
+                               ("batched", films[i].buffer_f32(), res[i]["rel_mse"])):
+            true = float(np.mean((img.astype(np.float64) - ref) ** 2 / (ref * ref + 1e-2)))
+            checks.append({"job": i, "form": form, "res": j["res"], "estimate": est, "true_vs_16k": true})
+        ref_f._release()
+    pe = [p["rel_mse"] for p in plain]
+    be = [r["rel_mse"] for r in res]
+    return {
+        "workload": f"the batched workload's {len(jobs)} jobs, each rendered until its relative-MSE estimate <= "
+                    f"{target:g} (at most {budget} spp)",
+        "target_rel_mse": target,
+        "plain": {"jobs_per_s": len(jobs) / plain_s, "seconds": plain_s,
+                  "Mrays_per_s": sum(p["rays"] for p in plain) / plain_s / 1e6,
+                  "reached": float(np.mean([e <= target for e in pe])), "rel_mse_mean": float(np.mean(pe)),
+                  "spp_p50": float(np.median([p["spp"] for p in plain]))},
+        "batched": {"jobs_per_s": len(jobs) / batch_s, "seconds": batch_s, "Mrays_per_s": st["rays"] / batch_s / 1e6,
+                    "reached": float(np.mean([e <= target for e in be])), "rel_mse_mean": float(np.mean(be)),
+                    "spp_p50": float(np.median([r["spp"] for r in res])),
+                    "rounds_mean": float(np.mean([r["rounds"] for r in res])), "queue_paths": ctx["queue"]},
+        "speedup": plain_s / batch_s,
+        "estimate_vs_true": checks,
+        "timing": "wall clock around all jobs (host overhead, error checks and rounds included); scene builds excluded",
+    }
+
+
 def run_served(lm, args, ctx) -> dict:
     """Poisson request stream through RenderServer at 80 % of the measured batched capacity."""
     from lightmetrica import synthetic as syn
     from lightmetrica.serving import RenderServer, Request
     scenes = ctx["scenes"]
-    rate = 0.8 * ctx["capacity"]
+    target = args.target_rel_mse if args.target_rel_mse > 0 else None
+    rate = 0.8 * (ctx.get("capacity_to_error") if target else ctx["capacity"])
     reqs = syn.served_requests(args.served_requests, rate=rate, n_scenes=len(scenes))
     srv = RenderServer(lambda k: scenes[k][0], hbm_budget=150 * 10**9, queue_paths=args.served_queue, max_inflight=1024)
     srv.owns_scenes = False
@@ -457,8 +579,12 @@ def run_served(lm, args, ctx) -> dict:
         now = srv.clock() - t0
         while i < n and reqs[i]["arrival"] <= now:
             q = reqs[i]
+            # new images render to the target error (at most error_budget_spp); refinements add
+            # 16 spp to a finished film
+            new_image = q["refine"] is None and target is not None
             srv.submit(Request(rid=q["rid"], arrival=t0 + q["arrival"], scene_key=q["scene"], w=q["res"], h=q["res"],
-                               spp=q["spp"], max_verts=q["max_verts"], seed=q["seed"], refine=q["refine"]))
+                               spp=args.error_budget_spp if new_image else q["spp"], max_verts=q["max_verts"],
+                               seed=q["seed"], refine=q["refine"], target=target if new_image else None))
             i += 1
         if srv.idle() and i < n:
             time.sleep(max(0.0, reqs[i]["arrival"] - (srv.clock() - t0)))
@@ -469,18 +595,20 @@ def run_served(lm, args, ctx) -> dict:
     st = srv.batch.stats()
     srv.close()
     return {"queue_paths": args.served_queue,
-            "workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the batched capacity), "
-                        f"{sum(1 for q in reqs if q['refine'] is not None)} refinements (+16 spp), scenes of the "
-                        f"batched workload, 150 GB HBM budget",
+            "workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the batched capacity"
+                        f"{' at the target error' if target else ''}), {sum(1 for q in reqs if q['refine'] is not None)} "
+                        f"refinements (+16 spp on a finished film), the others new images rendered "
+                        + (f"to rel-MSE {target:g} (at most {args.error_budget_spp} spp)" if target else "at 4-64 spp")
+                        + ", scenes of the batched workload, 150 GB HBM budget",
             "requests": n, "rate_per_s": rate, "seconds": total, "jobs_per_s": n / total,
             "Mrays_per_s": st["rays"] / total / 1e6,
             "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"],
             "done_p50_s": lat["done_p50"], "done_p99_s": lat["done_p99"], "evictions": lat["evictions"],
             "peak_resident_bytes": srv.peak_resident_bytes,
-            **{k: v for k, v in lat.items() if k.startswith(("rel_mse", "time_to_rel_mse", "reached_rel_mse"))}}
+            **{k: v for k, v in lat.items() if k.startswith(("rel_mse", "target_", "reached_target", "time_to_target"))}}
 
 
-def run_served_stress(lm, args, ctx) -> dict:
+def run_served_stress(lm, args, ctx, budget_bytes: int | None = None) -> dict:
     """Heavy-tailed served mix: 1 request in 10 renders the instanced scene at 4096x2160 (path
     length 16, 1-4 spp), the rest batched-workload scenes (the first 32 of the mix), under a small
     HBM budget, so admission waits for memory and idle scenes are evicted and rebuilt. Scenes are
@@ -514,7 +642,7 @@ def run_served_stress(lm, args, ctx) -> dict:
             s, _ = syn.triangles_scene(j["scene_seed"], j["tris"], 64, 64, prefix=f"stress{key}_")
         s.build()
         return s
-    budget = args.stress_budget_mb << 20
+    budget = (args.stress_budget_mb << 20) if budget_bytes is None else budget_bytes
     srv = RenderServer(make_scene, hbm_budget=budget, queue_paths=args.served_queue, max_inflight=256)
     t0 = srv.clock()
     i, n, released = 0, len(reqs), 0
@@ -542,7 +670,7 @@ def run_served_stress(lm, args, ctx) -> dict:
     return {"queue_paths": args.served_queue,
             "workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the measured path throughput for this mix), "
                         f"{len(inst)} instanced 4096x2160 jobs (1-4 spp, length 16) among batched-workload jobs on 32 "
-                        f"scenes; {args.stress_budget_mb} MB HBM budget; scenes built on admission",
+                        f"scenes; {budget >> 20} MB HBM budget; scenes built on admission",
             "requests": n, "seconds": total, "jobs_per_s": n / total, "Mrays_per_s": st["rays"] / total / 1e6,
             "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"], "done_p50_s": lat["done_p50"],
             "done_p99_s": lat["done_p99"],
@@ -551,7 +679,7 @@ def run_served_stress(lm, args, ctx) -> dict:
             "evictions": srv.evictions, "scene_builds": srv.scene_builds,
             "scene_build_seconds": srv.scene_build_seconds, "peak_resident_bytes": srv.peak_resident_bytes,
             "budget_bytes": budget,
-            **{k: v for k, v in lat.items() if k.startswith(("rel_mse", "time_to_rel_mse", "reached_rel_mse"))}}
+            **{k: v for k, v in lat.items() if k.startswith("rel_mse")}}
 
 
 def run_instanced(lm, args) -> dict:
@@ -591,6 +719,103 @@ def run_instanced(lm, args) -> dict:
             "instances": acc["num_instances"], "accel_device_bytes": acc["device_bytes"],
             "scene_device_bytes": int(sb.value), "flattened_bytes_estimate": int(flat_est),
             "build_seconds": build_s}
+
+
+def run_raycast(lm, scene, args, cpu_scene=None) -> dict:
+    """The raycast probe of the plain drop-in workload: 2^24 uniform-sphere rays from one point
+    inside the displaced-sphere scene, closest hit through lmgpu_accel_intersect_device (the batched
+    Accel::intersect), device buffers, CUDA events on the launching stream; `e2e` through
+    lmgpu_accel_intersect (host rays in, host hits out). Every hit of one pass is then checked
+    against the fp32 oracle (bit-exact index, t, u, v; exact-t ties counted), and the fp64 oracle
+    (the reference's precision) is timed on a bounded subsample as the CPU baseline."""
+    import ctypes as C
+    import numpy as np
+    from lightmetrica import _native as N
+    from lightmetrica import synthetic as syn
+    L = N.lib()
+    rt = _cudart()
+    acc = scene.accel()
+    rays = syn.sphere_rays(syn.RAYCAST_PROBE_RAYS, syn.RAYCAST_PROBE_ORIGIN, seed=syn.RAYCAST_PROBE_SEED)
+    n = len(rays)
+    d_rays, d_hits = C.c_void_p(), C.c_void_p()
+    assert rt.cudaMalloc(C.byref(d_rays), rays.nbytes) == 0
+    assert rt.cudaMalloc(C.byref(d_hits), n * 16) == 0
+    flush = C.c_void_p()
+    assert rt.cudaMalloc(C.byref(flush), 256 << 20) == 0
+    try:
+        assert rt.cudaMemcpy(d_rays, rays.ctypes.data, rays.nbytes, 1) == 0
+        mn, mt = C.c_double(), C.c_double()
+        N.check(L.lmgpu_accel_trace_counts(acc._h, d_rays, n, 0, 64, C.byref(mn), C.byref(mt)))
+        e0, e1 = C.c_void_p(), C.c_void_p()
+        rt.cudaEventCreate(C.byref(e0))
+        rt.cudaEventCreate(C.byref(e1))
+        for _ in range(max(3, args.warmup)):
+            N.check(L.lmgpu_accel_intersect_device(acc._h, d_rays, n, d_hits, None))
+        rt.cudaDeviceSynchronize()
+        times = []
+        for _ in range(max(1, args.steps)):
+            rt.cudaMemset(flush, 0, 256 << 20)
+            rt.cudaDeviceSynchronize()
+            rt.cudaEventRecord(e0, None)
+            N.check(L.lmgpu_accel_intersect_device(acc._h, d_rays, n, d_hits, None))
+            rt.cudaEventRecord(e1, None)
+            rt.cudaEventSynchronize(e1)
+            ms = C.c_float()
+            rt.cudaEventElapsedTime(C.byref(ms), e0, e1)
+            times.append(ms.value)
+        rt.cudaEventDestroy(e0)
+        rt.cudaEventDestroy(e1)
+        hits = np.zeros(n, dtype=[("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<i4")])
+        assert rt.cudaMemcpy(hits.ctypes.data, d_hits, n * 16, 2) == 0
+    finally:
+        rt.cudaFree(d_rays)
+        rt.cudaFree(d_hits)
+        rt.cudaFree(flush)
+    # end to end: host rays in, host hits out, through the C-ABI
+    e2e = []
+    for _ in range(max(1, min(3, args.steps))):
+        t = time.perf_counter()
+        acc.intersect_batch(rays)
+        e2e.append(time.perf_counter() - t)
+    ms = statistics.median(times)
+    b_ray = 32 + 16 + NODE_BYTES * mn.value + TRI_BYTES * mt.value
+    peaks = _peaks()
+    achieved = n * b_ray / (ms / 1e3) / 1e9
+    out = {"workload": f"{n} uniform-sphere rays from {list(syn.RAYCAST_PROBE_ORIGIN)} in the displaced-sphere scene "
+                       f"({acc.stats()['num_tris']} triangles), closest hit, tmin 1e-3, tmax 1e10",
+           "Mrays_per_s": n / ms / 1e3, "ms_median": ms, "ms_all": times,
+           "e2e": {"value": n / statistics.median(e2e) / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": rays.nbytes,
+                   "d2h_bytes_per_step": n * 16},
+           "hit_fraction": float((hits["prim"] >= 0).mean()),
+           "roofline": {"bound": "issue/latency (L2-resident nodes)", "achieved": achieved, "unit": "GB/s",
+                        "peak": peaks["hbm_gbs"], "frac": achieved / peaks["hbm_gbs"], "bytes_per_ray": b_ray,
+                        "nodes_per_ray": mn.value, "tris_per_ray": mt.value}}
+    if cpu_scene is not None:
+        from oracle import oracle as O
+        # checker: every GPU hit against the fp32 restatement (not timed)
+        S32 = O.from_lm_scene(scene, double=False)
+        S32.build(robust=True)
+        t32, uv32, id32, _ = S32.intersect(rays, refine_t=True)
+        tri32 = S32.triangles()
+        del S32
+        g = hits["prim"].astype(np.int64)
+        same = g == id32
+        hit = same & (g >= 0)
+        exact = same & (~hit | ((hits["t"] == t32.astype(np.float32)) & (hits["u"] == uv32[:, 0].astype(np.float32))
+                                & (hits["v"] == uv32[:, 1].astype(np.float32))))
+        cand = np.nonzero(~same & (g >= 0) & (id32 >= 0))[0]
+        ties = 0
+        if len(cand):
+            ties = int(np.sum(O.mt32(rays[cand], tri32, g[cand]) == O.mt32(rays[cand], tri32, id32[cand])))
+        out["check_fp32_oracle"] = {"rays": n, "bit_exact": int(exact.sum()), "exact_t_ties": ties,
+                                    "mismatches": int(n - exact.sum() - ties)}
+        # CPU baseline: the fp64 restatement of accel_sahbvh.cpp on a bounded subsample
+        sub = rays[: 1 << 21]
+        _, _, _, csec = cpu_scene.intersect(sub)
+        out["cpu_baseline"] = {"value": len(sub) / csec / 1e6, "unit": "Mrays/s", "cores": O.max_threads(),
+                               "kind": "port", "sample": f"first {len(sub)} of the probe's rays, fp64 accel::sahbvh "
+                                                         f"restatement ({csec:.2f} s)"}
+    return out
 
 
 def run_lt(lm, scene, film, args) -> dict:
@@ -703,6 +928,12 @@ def _cudart():
             lib.cudaMalloc.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
             lib.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
             lib.cudaFree.argtypes = [C.c_void_p]
+            lib.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+            lib.cudaEventCreate.argtypes = [C.POINTER(C.c_void_p)]
+            lib.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+            lib.cudaEventSynchronize.argtypes = [C.c_void_p]
+            lib.cudaEventDestroy.argtypes = [C.c_void_p]
+            lib.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
             return lib
         except OSError:
             continue
@@ -722,8 +953,13 @@ def main():
     ap.add_argument("--spp", type=int, default=0)
     ap.add_argument("--wave", type=int, default=0, help="paths in flight per wave (0 = library default)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched and served legs")
+    ap.add_argument("--raycast", type=int, default=1, help="1: the 2^24-ray raycast probe leg (0 skips it)")
+    ap.add_argument("--target-rel-mse", type=float, default=1e-3,
+                    help="relative MSE the batched_to_error and served legs render to (0 skips batched_to_error)")
+    ap.add_argument("--error-budget-spp", type=int, default=4096, help="most spp a job may take to reach the target")
     ap.add_argument("--batched-jobs", type=int, default=256)
-    ap.add_argument("--served-requests", type=int, default=5000, help="0 skips the served leg")
+    ap.add_argument("--served-requests", type=int, default=300,
+                    help="requests of the served leg (0 skips it); new images render to the target error")
     ap.add_argument("--instanced-spp", type=int, default=4, help="spp of the instanced leg (0 skips it)")
     ap.add_argument("--stress-requests", type=int, default=300, help="requests of the served stress leg (0 skips it)")
     ap.add_argument("--served-queue", type=int, default=1 << 22,

@@ -77,8 +77,8 @@ int lmgpu_set_device(int device);
  * Accel. Replaces the accel::sahbvh / accel::nanort / accel::embree slot.
  */
 
-/* Accel construction; the accel's Json props (embree_params.h:105-115 for accel::embree) have no
- * counterpart: the builder is fixed (binned SAH, collapsed to 8-wide quantized nodes). */
+/* Accel construction. The accel's Json props (embree_params.h:105-115 for accel::embree) have no
+ * counterpart; the builder is chosen per build (lmgpu_accel_build_ex). */
 int lmgpu_accel_create(lmgpu_accel** out);
 int lmgpu_accel_destroy(lmgpu_accel* accel);
 
@@ -86,6 +86,17 @@ int lmgpu_accel_destroy(lmgpu_accel* accel);
  * graph first). The caller passes the flattened triangles: tri_p holds num_tris x 9 floats, the
  * world-space p1, p2, p3 of each triangle in flattening order. The data is copied. */
 int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris);
+
+/* Builders of the 8-wide tree (the reference's accel_sahbvh.cpp:127-267 sorts fully per node on
+ * the host). Closest hits do not depend on the builder: the traversal's tie rule (the smaller
+ * triangle index) makes them independent of the tree.
+ *  LMGPU_BUILDER_HOST_SAH -- binned SAH binary tree on the host threads, SAH-optimal 8-wide
+ *                            collapse (lmgpu_accel_build's builder);
+ *  LMGPU_BUILDER_GPU_PLOC -- on the GPU: Morton order, PLOC clustering into a binary tree, the same
+ *                            SAH-optimal collapse and quantization. */
+#define LMGPU_BUILDER_HOST_SAH 0
+#define LMGPU_BUILDER_GPU_PLOC 1
+int lmgpu_accel_build_ex(lmgpu_accel* accel, const float* tri_p, int64_t num_tris, int32_t builder);
 
 /* One instance of a bottom-level triangle set: `transform` is its world-from-local matrix, the top
  * three rows of the 4x4 (row-major; the last row is 0 0 0 1). */
@@ -130,6 +141,10 @@ int lmgpu_accel_get_stats(const lmgpu_accel* accel, lmgpu_accel_stats* out);
  * them. `nodes` must hold 20 * max(num_tris, 1) words and `tris` 12 * num_tris floats. */
 int lmgpu_bvh8_build_host(const float* tri_p, int64_t num_tris, uint32_t* nodes, float* tris, int64_t* num_nodes,
                           int32_t* max_depth);
+/* The same through the GPU builder (LMGPU_BUILDER_GPU_PLOC), copied back to host memory (no
+ * reference counterpart; for tests). Same buffer sizes. Synchronous. */
+int lmgpu_bvh8_build_gpu(const float* tri_p, int64_t num_tris, uint32_t* nodes, float* tris, int64_t* num_nodes,
+                         int32_t* max_depth);
 
 /* Instrumented trace (no reference counterpart; feeds the roofline's algorithmic byte count):
  * over every `sample`-th ray of the device batch, the mean number of 8-wide nodes visited and
@@ -400,6 +415,17 @@ int lmgpu_batch_run(lmgpu_batch* batch, int32_t max_chunks, void* stream, int64_
 /* Progress of a job as of the last lmgpu_batch_run: leading samples-per-pixel passes whose every
  * pixel has finished, and whether the whole job is done. */
 int lmgpu_batch_job_status(const lmgpu_batch* batch, int32_t job, int32_t* passes_complete, int32_t* done);
+/* Changes how many samples per pixel a job renders, between runs (after lmgpu_batch_run has
+ * returned): down to stop it early, back up (at most to the spp it was submitted with) to let it
+ * continue. Passes of which a path has already started always complete, so the count becomes
+ * max(spp, passes started) and *spp_out (may be null) receives it. Random streams stay keyed by
+ * the submitted spp (pix * spp_submitted + sample), so a job stopped after N passes holds exactly
+ * the first N passes of the submitted render. With split passes the film's even / odd pass counts
+ * follow, so lmgpu_film_rel_mse on a job that is done reads the error of the passes it holds: the
+ * loop "run until done, estimate the error, raise spp" is progressive rendering to a target error
+ * (the reference's progressive schedulers, scheduler.cpp:57-109, stop on time instead). The job must
+ * be its film's latest and not yet resolved. */
+int lmgpu_batch_job_set_spp(lmgpu_batch* batch, int32_t job, int32_t spp, int32_t* spp_out);
 /* Rescales a finished job's film (as lmgpu_render_pt does at the end of a render). */
 int lmgpu_batch_resolve(lmgpu_batch* batch, int32_t job, void* stream);
 /* Cumulative rays traced and device time since creation or the last reset. */
@@ -411,21 +437,26 @@ int lmgpu_batch_reset(lmgpu_batch* batch);
 int lmgpu_batch_set_timing(lmgpu_batch* batch, int32_t on);
 
 /* No counterpart in the reference. renderer::pt for callers that must not allocate device memory:
- * code that renders while a CUDA graph is being captured (cudaMalloc is not a capturable call),
  * hosts that hand every byte of HBM to their own pool allocator and forbid libraries from calling
- * cudaMalloc/cudaFree behind their back, and latency-bound loops that cannot afford the allocator's
- * implicit synchronization. It renders exactly like lmgpu_render_pt, but its wavefront queues live
- * in one file-scope device array of fixed size (about 6.5 MiB, held by every GPU that loads the
- * library until the process exits) instead of buffers the library allocates, so at most
- * LMGPU_NOALLOC_MAX_WAVE paths are in flight per wave (params->wave_paths = 0 picks that size;
- * larger values are rejected with LMGPU_ERR_INVALID_ARGUMENT). The scene must already be created.
- * The caller passes the output: d_film, a device buffer of h x w x 3 floats, which receives the
- * estimate scaled by 1/spp (pixel mode) or w*h/spp (image mode); params->accumulate must be 0.
- * The first call on a device looks up the array's device address (cudaGetSymbolAddress) and
- * caches it; make that first call before any stream capture begins. Every call shares the one
- * array and clears what must start at zero, so calls whose work overlaps on the GPU (different
- * streams, or concurrent host threads) race: serialize them. The call enqueues on `stream` and
- * waits for it, and calls no cudaMalloc, cudaFree or other allocating routine. */
+ * cudaMalloc/cudaFree behind their back (a training or serving framework that reserves the device
+ * at start-up, a plugin host whose memory accounting would not see the library's buffers), and
+ * hosts that require a steady state free of allocations, where cudaMalloc's implicit device
+ * synchronization and possible failure are not acceptable mid-run. It renders exactly like
+ * lmgpu_render_pt, but its wavefront queues live in one file-scope device array of fixed size
+ * (about 6.5 MiB, held by every GPU that loads the library until the process exits) instead of
+ * buffers the library allocates, so at most LMGPU_NOALLOC_MAX_WAVE paths are in flight per wave
+ * (params->wave_paths = 0 picks that size; larger values are rejected with
+ * LMGPU_ERR_INVALID_ARGUMENT). The scene must already be created. The caller passes the output:
+ * d_film, a device buffer of h x w x 3 floats, which receives the estimate scaled by 1/spp in
+ * both primary modes (the scale renderer_pt.cpp:307-312 gives, as lmgpu_render_pt does);
+ * params->accumulate must be 0. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current and caches it for the life of the process;
+ * make that first call before any stream capture begins. A cudaDeviceReset invalidates the cached
+ * address, as it invalidates every scene and film handle of the library: do not call this entry
+ * point after one. Every call shares the one array and clears what must start at zero, so calls
+ * whose work overlaps on the GPU (different streams, or concurrent host threads) race: serialize
+ * them. The call enqueues on `stream`, waits for it to read the error word, and calls no
+ * cudaMalloc, cudaFree or other allocating routine. */
 #define LMGPU_NOALLOC_MAX_WAVE 32768
 int lmgpu_render_pt_noalloc(lmgpu_scene* scene, float* d_film, int32_t w, int32_t h, const lmgpu_pt_params* params,
                             void* stream);

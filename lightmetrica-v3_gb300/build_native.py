@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + [
 ]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-I", INCLUDE]
 
-CU_SOURCES = ["accel.cu", "render.cu"]
+CU_SOURCES = ["accel.cu", "render.cu", "bvh_gpu.cu"]
 CPP_SOURCES = ["bvh_build.cpp"]
 
 

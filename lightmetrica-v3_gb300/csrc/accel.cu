@@ -34,7 +34,33 @@ Tuning& tuning() {
     return t;
 }
 
+std::shared_mutex& capture_mutex() {
+    static std::shared_mutex m;
+    return m;
+}
+
 constexpr int kTraceBlock = 128;
+
+// Hit distance of an accepted hit, recomputed in double from the same fp32 ray and triangle record
+// (p1, e1, e2) with the operations of accel_sahbvh.cpp:58-75 in their order (p = d x e2,
+// tv = o - p1, q = tv x e1, t = (e2 . q) / (e1 . p); glm's dot and cross order) and rounded once
+// to float. The fp32 test still decides which triangle is hit and where the traversal stops;
+// this only makes the reported t agree with the reference's fp64 value to fp32 rounding (an fp32
+// t of a grazing hit can be 2e-5 off relative). Explicit IEEE double ops: no contraction.
+__device__ inline float refine_hit_t(const float4 ra, const float4 rb, const float4 a, const float4 b, const float4 c) {
+    const double ox = ra.x, oy = ra.y, oz = ra.z, dx = rb.x, dy = rb.y, dz = rb.z;
+    const double e1x = a.w, e1y = b.x, e1z = b.y, e2x = b.z, e2y = b.w, e2z = c.x;
+    const double px = __dsub_rn(__dmul_rn(dy, e2z), __dmul_rn(e2y, dz));
+    const double py = __dsub_rn(__dmul_rn(dz, e2x), __dmul_rn(e2z, dx));
+    const double pz = __dsub_rn(__dmul_rn(dx, e2y), __dmul_rn(e2x, dy));
+    const double tx = __dsub_rn(ox, double(a.x)), ty = __dsub_rn(oy, double(a.y)), tz = __dsub_rn(oz, double(a.z));
+    const double qx = __dsub_rn(__dmul_rn(ty, e1z), __dmul_rn(e1y, tz));
+    const double qy = __dsub_rn(__dmul_rn(tz, e1x), __dmul_rn(e1z, tx));
+    const double qz = __dsub_rn(__dmul_rn(tx, e1y), __dmul_rn(e1x, ty));
+    const double det = __dadd_rn(__dadd_rn(__dmul_rn(e1x, px), __dmul_rn(e1y, py)), __dmul_rn(e1z, pz));
+    const double num = __dadd_rn(__dadd_rn(__dmul_rn(e2x, qx), __dmul_rn(e2y, qy)), __dmul_rn(e2z, qz));
+    return __double2float_rn(__ddiv_rn(num, det));
+}
 
 // rays: 2 float4 per ray (o, tmin) (d, tmax). refill > 0: each block takes one contiguous chunk
 // of the rays and its warps fetch from it dynamically through a shared-memory counter (no state
@@ -82,6 +108,20 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const flo
         }
     }
     if (lerr) atomicOr(err, lerr);
+}
+
+// The fp64 hit distance of every closest hit (refine_hit_t), as a pass of its own after the
+// trace: inside the persistent traversal loop the lanes whose ray ends would run its long chain
+// of double ops while the warp's other lanes wait.
+__global__ void __launch_bounds__(256) k_refine_hits(const float4* __restrict__ rays, lmgpu_hit* __restrict__ hits,
+                                                     int64_t n, const float4* __restrict__ tris,
+                                                     const int32_t* __restrict__ tri_slot) {
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const int32_t id = hits[i].prim;
+        if (id < 0) continue;
+        const float4* tp = tris + size_t(__ldg(tri_slot + id)) * 3;
+        hits[i].t = refine_hit_t(rays[2 * i], rays[2 * i + 1], __ldg(tp), __ldg(tp + 1), __ldg(tp + 2));
+    }
 }
 
 // Instrumented pass: node visits and triangle tests summed over every `sample`-th ray.
@@ -154,6 +194,12 @@ void launch_trace(const lmgpu_accel* a, const void* d_rays, int64_t n, void* d_h
     if (d_occ) two ? run(k_trace_batch<true, true>) : run(k_trace_batch<true, false>);
     else two ? run(k_trace_batch<false, true>) : run(k_trace_batch<false, false>);
     LMGPU_CUDA(cudaGetLastError());
+    if (!d_occ && !two && a->tri_slot.p && n > 0) {
+        const int g = int(std::min<int64_t>((n + 255) / 256, int64_t(current_device().num_sms) * 8));
+        k_refine_hits<<<g, 256, 0, st>>>(static_cast<const float4*>(d_rays), static_cast<lmgpu_hit*>(d_hits), n,
+                                         a->tris.as<const float4>(), a->tri_slot.as<const int32_t>());
+        LMGPU_CUDA(cudaGetLastError());
+    }
 }
 
 }  // namespace lmgpu
@@ -217,20 +263,56 @@ int lmgpu_accel_destroy(lmgpu_accel* accel) {
 }
 
 int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris) {
+    return lmgpu_accel_build_ex(accel, tri_p, num_tris, LMGPU_BUILDER_HOST_SAH);
+}
+
+int lmgpu_accel_build_ex(lmgpu_accel* accel, const float* tri_p, int64_t num_tris, int32_t builder) {
     return guarded([&] {
         if (!accel || (!tri_p && num_tris > 0)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "accel or triangles null");
+        if (builder != LMGPU_BUILDER_HOST_SAH && builder != LMGPU_BUILDER_GPU_PLOC)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown builder");
         const auto t0 = std::chrono::steady_clock::now();
+        if (builder == LMGPU_BUILDER_GPU_PLOC) {
+            cudaStream_t st;
+            LMGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            int64_t nn = 0;
+            int32_t depth = 0;
+            double sah = 0;
+            try {
+                build_bvh8_gpu(tri_p, num_tris, accel->nodes, accel->tris, accel->tri_slot, nn, depth, sah, st);
+            } catch (...) {
+                cudaStreamDestroy(st);
+                throw;
+            }
+            cudaStreamDestroy(st);
+            accel->num_nodes = nn;
+            accel->depth = depth;
+            accel->sah_cost = sah;
+        } else {
         Bvh8Host h;
         std::string err;
         if (!build_bvh8(tri_p, num_tris, h, &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
         accel->nodes.upload(h.nodes.data(), h.nodes.size());
         accel->tris.upload(h.tris.data(), h.tris.size());
-        accel->err.alloc(sizeof(int));
-        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
-        accel->num_tris = num_tris;
+        {
+            // flattened triangle index -> leaf-order record, for the fp64 hit distance
+            std::vector<int32_t> slot(size_t(num_tris), -1);
+            for (int64_t k = 0; k < num_tris; k++) {
+                uint32_t id;
+                std::memcpy(&id, &h.tris[size_t(12) * k + 9], sizeof(id));
+                if (int64_t(id) >= num_tris || slot[id] != -1) throw Error(LMGPU_ERR_INTERNAL, "triangle records are not a permutation");
+                slot[id] = int32_t(k);
+            }
+            accel->tri_slot.upload(slot.data(), slot.size());
+        }
         accel->num_nodes = int64_t(h.nodes.size() / 20);
         accel->depth = h.max_depth;
         accel->sah_cost = h.sah_cost;
+        }
+        accel->err.alloc(sizeof(int));
+        LMGPU_CUDA_SYNC(cudaMemset(accel->err.p, 0, sizeof(int)));
+        accel->num_tris = num_tris;
+        accel->builder = builder;
         accel->inst.release();
         accel->num_instances = 0;
         accel->max_visits = 0;
@@ -238,7 +320,7 @@ int lmgpu_accel_build(lmgpu_accel* accel, const float* tri_p, int64_t num_tris) 
         accel->inst_xform.clear();
         accel->inst_id_base.clear();
         accel->blas_offsets.clear();
-        LMGPU_CUDA(cudaDeviceSynchronize());
+        LMGPU_CUDA_SYNC(cudaDeviceSynchronize());
         accel->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     });
 }
@@ -353,9 +435,10 @@ int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const in
         }
         accel->nodes.upload(nodes.data(), nodes.size());
         accel->tris.upload(tris.data(), tris.size());
+        accel->tri_slot.release();  // two-level hits keep the fp32 distance of the instance-frame ray
         accel->inst.upload(rec.data(), rec.size());
         accel->err.alloc(sizeof(int));
-        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
+        LMGPU_CUDA_SYNC(cudaMemset(accel->err.p, 0, sizeof(int)));
         accel->num_tris = total;
         accel->num_nodes = int64_t(nodes.size() / 20);
         accel->depth = top.max_depth + bdepth;
@@ -367,7 +450,7 @@ int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const in
         accel->inst_xform = xf;
         accel->inst_id_base = id_base;
         accel->blas_offsets.assign(blas_offsets, blas_offsets + num_blas + 1);
-        LMGPU_CUDA(cudaDeviceSynchronize());
+        LMGPU_CUDA_SYNC(cudaDeviceSynchronize());
         accel->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     });
 }
@@ -379,12 +462,12 @@ int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgp
         if (n == 0) return;
         accel->scratch_rays.alloc(size_t(n) * 32);
         accel->scratch_hits.alloc(size_t(n) * sizeof(lmgpu_hit));
-        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
-        LMGPU_CUDA(cudaMemcpy(accel->scratch_rays.p, rays, size_t(n) * 32, cudaMemcpyHostToDevice));
+        LMGPU_CUDA_SYNC(cudaMemset(accel->err.p, 0, sizeof(int)));
+        LMGPU_CUDA_SYNC(cudaMemcpy(accel->scratch_rays.p, rays, size_t(n) * 32, cudaMemcpyHostToDevice));
         launch_trace(accel, accel->scratch_rays.p, n, accel->scratch_hits.p, nullptr, 0, accel->err.as<int>());
-        LMGPU_CUDA(cudaMemcpy(hits, accel->scratch_hits.p, size_t(n) * sizeof(lmgpu_hit), cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(hits, accel->scratch_hits.p, size_t(n) * sizeof(lmgpu_hit), cudaMemcpyDeviceToHost));
         int herr = 0;
-        LMGPU_CUDA(cudaMemcpy(&herr, accel->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(&herr, accel->err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed (code " + std::to_string(herr) + ")");
     });
 }
@@ -435,6 +518,31 @@ int lmgpu_bvh8_build_host(const float* tri_p, int64_t num_tris, uint32_t* nodes,
     });
 }
 
+int lmgpu_bvh8_build_gpu(const float* tri_p, int64_t num_tris, uint32_t* nodes, float* tris, int64_t* num_nodes,
+                         int32_t* max_depth) {
+    return guarded([&] {
+        if (!tri_p || !nodes || !tris || !num_nodes || !max_depth) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        DevBuf dn, dt, ds;
+        int64_t nn = 0;
+        int32_t depth = 0;
+        double sah = 0;
+        cudaStream_t st;
+        LMGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        try {
+            build_bvh8_gpu(tri_p, num_tris, dn, dt, ds, nn, depth, sah, st);
+        } catch (...) {
+            cudaStreamDestroy(st);
+            throw;
+        }
+        cudaStreamDestroy(st);
+        if (nn > (num_tris > 0 ? num_tris : 1)) throw Error(LMGPU_ERR_INTERNAL, "node count above the documented bound");
+        LMGPU_CUDA_SYNC(cudaMemcpy(nodes, dn.p, size_t(nn) * 80, cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(tris, dt.p, size_t(num_tris) * 48, cudaMemcpyDeviceToHost));
+        *num_nodes = nn;
+        *max_depth = depth;
+    });
+}
+
 int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, int32_t any_hit, int32_t sample,
                              double* mean_nodes, double* mean_tris) {
     return guarded([&] {
@@ -443,8 +551,8 @@ int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, 
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "invalid argument");
         DevBuf sums;
         sums.alloc(3 * sizeof(unsigned long long));
-        LMGPU_CUDA(cudaMemset(sums.p, 0, 3 * sizeof(unsigned long long)));
-        LMGPU_CUDA(cudaMemset(accel->err.p, 0, sizeof(int)));
+        LMGPU_CUDA_SYNC(cudaMemset(sums.p, 0, 3 * sizeof(unsigned long long)));
+        LMGPU_CUDA_SYNC(cudaMemset(accel->err.p, 0, sizeof(int)));
         const Bvh8 b = device_view(accel);
         const size_t smem = trace_smem(accel);
         const int64_t m = (n + sample - 1) / sample;
@@ -458,7 +566,7 @@ int lmgpu_accel_trace_counts(lmgpu_accel* accel, const void* d_rays, int64_t n, 
         else two ? run(k_trace_count<false, true>) : run(k_trace_count<false, false>);
         LMGPU_CUDA(cudaGetLastError());
         unsigned long long h[3];
-        LMGPU_CUDA(cudaMemcpy(h, sums.p, sizeof(h), cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(h, sums.p, sizeof(h), cudaMemcpyDeviceToHost));
         const double c = h[2] ? double(h[2]) : 1.0;
         *mean_nodes = double(h[0]) / c;
         *mean_tris = double(h[1]) / c;

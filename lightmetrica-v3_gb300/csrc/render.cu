@@ -660,6 +660,7 @@ struct JobDev {
     float* film_odd;   // split passes: odd global passes splat here (else null)
     int64_t path_begin;
     int64_t npix;
+    int64_t limit;     // paths the planner starts: npix * the job's current spp (lmgpu_batch_job_set_spp)
     uint32_t pass_off;
     uint32_t parity0;  // parity of the job's first pass among the film's passes
 };
@@ -812,7 +813,8 @@ struct AllocEntry {
     int64_t local, slot;
     int32_t job, pad;
 };
-// Planner's view of a job that still has paths to start.
+// Planner's view of a job that still has paths to start (its end is read from the job table,
+// where the host may move it between runs).
 struct ActiveJob {
     int64_t npix, total;
     int32_t job, pad;
@@ -1714,7 +1716,7 @@ __global__ void __launch_bounds__(32) k_wf_plan(int64_t* ctl, const int* qcount,
     int64_t nact = ctl[21];
     for (int64_t j = seen + lane; j < njobs; j += 32) {
         const JobDev& J = jobs[j];
-        active[nact + (j - seen)] = ActiveJob{J.npix, J.npix * J.P.spp, int32_t(j), 0};
+        active[nact + (j - seen)] = ActiveJob{J.npix, J.limit, int32_t(j), 0};
     }
     nact += njobs > seen ? njobs - seen : 0;
     __syncwarp();
@@ -1730,7 +1732,8 @@ __global__ void __launch_bounds__(32) k_wf_plan(int64_t* ctl, const int* qcount,
                 const ActiveJob A = active[a];
                 j = A.job;
                 nx = job_next[j];
-                const int64_t end = phase == 0 ? min(A.npix, A.total) : A.total;
+                const int64_t total = jobs[j].limit;
+                const int64_t end = phase == 0 ? min(A.npix, total) : total;
                 want = end > nx ? end - nx : 0;
             }
             int64_t inc = want;  // inclusive scan of the wants across the warp
@@ -1762,7 +1765,7 @@ __global__ void __launch_bounds__(32) k_wf_plan(int64_t* ctl, const int* qcount,
         ActiveJob A{};
         if (a < nact) {
             A = active[a];
-            keep = job_next[A.job] < A.total;
+            keep = job_next[A.job] < jobs[A.job].limit;
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (keep) active[k + __popc(m & below)] = A;
@@ -1992,8 +1995,8 @@ void ensure_film(lmgpu_film* f) {
     const size_t n = size_t(f->w) * f->h * 3;
     f->sum.alloc(n * 4);
     f->out.alloc(n * 4);
-    LMGPU_CUDA(cudaMemset(f->sum.p, 0, n * 4));
-    LMGPU_CUDA(cudaMemset(f->out.p, 0, n * 4));
+    LMGPU_CUDA_SYNC(cudaMemset(f->sum.p, 0, n * 4));
+    LMGPU_CUDA_SYNC(cudaMemset(f->out.p, 0, n * 4));
 }
 
 }  // namespace
@@ -2226,7 +2229,7 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
             ds.aspect = c.aspect;
         }
         s->counters.alloc(192);
-        LMGPU_CUDA(cudaMemset(s->counters.p, 0, 192));
+        LMGPU_CUDA_SYNC(cudaMemset(s->counters.p, 0, 192));
         *out = s.release();
     });
 }
@@ -2266,9 +2269,9 @@ int lmgpu_film_clear(lmgpu_film* f) {
         if (!f) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "film is null");
         ensure_film(f);
         const size_t n = size_t(f->w) * f->h * 3;
-        LMGPU_CUDA(cudaMemset(f->sum.p, 0, n * 4));
-        LMGPU_CUDA(cudaMemset(f->out.p, 0, n * 4));
-        if (f->sum_odd.p) LMGPU_CUDA(cudaMemset(f->sum_odd.p, 0, n * 4));
+        LMGPU_CUDA_SYNC(cudaMemset(f->sum.p, 0, n * 4));
+        LMGPU_CUDA_SYNC(cudaMemset(f->out.p, 0, n * 4));
+        if (f->sum_odd.p) LMGPU_CUDA_SYNC(cudaMemset(f->sum_odd.p, 0, n * 4));
         f->accumulated_spp = 0;
         f->scale = 1.0;
         f->split = false;
@@ -2285,13 +2288,15 @@ int lmgpu_film_rel_mse(lmgpu_film* f, double eps, double* rel_mse) {
         const double N = double(f->passes_even + f->passes_odd);
         DevBuf& acc = f->mse_acc;
         acc.alloc(sizeof(double));
-        LMGPU_CUDA(cudaMemset(acc.p, 0, sizeof(double)));
-        // f->scale * N = 1: the film is the sum over passes divided by the pass count
+        LMGPU_CUDA_SYNC(cudaMemset(acc.p, 0, sizeof(double)));
+        // the accumulators hold per-pass sums in the estimate's units (a render scales its film by
+        // 1 / passes in both primary modes), so no further unit factor; N only fixes the pass count
+        (void)N;
         k_rel_mse<<<256, 256>>>(f->sum.as<float>(), f->sum_odd.as<float>(), n, double(f->passes_even), double(f->passes_odd),
-                                f->scale * N, eps, acc.as<double>());
+                                1.0, eps, acc.as<double>());
         LMGPU_CUDA(cudaGetLastError());
         double h = 0.0;
-        LMGPU_CUDA(cudaMemcpy(&h, acc.p, sizeof(double), cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(&h, acc.p, sizeof(double), cudaMemcpyDeviceToHost));
         *rel_mse = h / double(n);
     });
 }
@@ -2303,7 +2308,7 @@ int lmgpu_probe_l2_bandwidth(int64_t bytes, int32_t iters, double* gbs) {
         const int64_t n = bytes / 16;
         buf.alloc(size_t(n) * 16);
         out.alloc(16);
-        LMGPU_CUDA(cudaMemset(buf.p, 0, size_t(n) * 16));
+        LMGPU_CUDA_SYNC(cudaMemset(buf.p, 0, size_t(n) * 16));
         const int grid = 8 * current_device().num_sms;
         k_l2_probe<<<grid, 256>>>(buf.as<float4>(), n, 1, out.as<float>());  // brings the buffer into L2
         LMGPU_CUDA(cudaGetLastError());
@@ -2334,9 +2339,9 @@ int lmgpu_film_fill(lmgpu_film* f, const float* rgb) {
             px[3 * i + 1] = rgb[1];
             px[3 * i + 2] = rgb[2];
         }
-        LMGPU_CUDA(cudaMemcpy(f->sum.p, px.data(), n * 3 * 4, cudaMemcpyHostToDevice));
-        LMGPU_CUDA(cudaMemcpy(f->out.p, px.data(), n * 3 * 4, cudaMemcpyHostToDevice));
-        if (f->sum_odd.p) LMGPU_CUDA(cudaMemset(f->sum_odd.p, 0, n * 3 * 4));
+        LMGPU_CUDA_SYNC(cudaMemcpy(f->sum.p, px.data(), n * 3 * 4, cudaMemcpyHostToDevice));
+        LMGPU_CUDA_SYNC(cudaMemcpy(f->out.p, px.data(), n * 3 * 4, cudaMemcpyHostToDevice));
+        if (f->sum_odd.p) LMGPU_CUDA_SYNC(cudaMemset(f->sum_odd.p, 0, n * 3 * 4));
         f->accumulated_spp = 0;
         f->scale = 1.0;
         f->split = false;
@@ -2348,7 +2353,7 @@ int lmgpu_film_read(lmgpu_film* f, float* out_rgb) {
     return guarded([&] {
         if (!f || !out_rgb) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         ensure_film(f);
-        LMGPU_CUDA(cudaMemcpy(out_rgb, f->out.p, size_t(f->w) * f->h * 3 * 4, cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(out_rgb, f->out.p, size_t(f->w) * f->h * 3 * 4, cudaMemcpyDeviceToHost));
     });
 }
 
@@ -3094,6 +3099,14 @@ struct lmgpu_batch {
     size_t jobs_done = 0;                   // job-table entries already on the device
     std::vector<lmgpu::JobDev> host_jobs;
     std::vector<lmgpu_film*> films;
+    // per job: samples per pixel submitted (the random-key stride and the most it may run), the
+    // current count (lmgpu_batch_job_set_spp), the film's pass count before the job, resolved
+    struct JobMeta {
+        int32_t spp_budget = 0, spp = 0;
+        int64_t film_first = 0;
+        bool resolved = false;
+    };
+    std::vector<JobMeta> meta;
     std::vector<uint32_t> host_pass;      // mirror of pass_done after the last run
     int64_t total = 0;
     uint32_t passes = 0;
@@ -3310,18 +3323,27 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     (void)grid_for(wf_shade_kernel(b, single, feat), kBlock, 0);
     (void)grid_for(k_wf_generate, kBlock, 0);
     cudaGraph_t ng = nullptr;
-    LMGPU_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    try {
-        enqueue_chunk(b, cs, b->timed);
-    } catch (...) {
-        cudaGraph_t gr;
-        cudaStreamEndCapture(cs, &gr);
-        if (gr) cudaGraphDestroy(gr);
+    {
+        // no other host thread may synchronize the device while the capture is open
+        std::unique_lock<std::shared_mutex> capture_lk(capture_mutex());
+        cudaError_t began = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (began != cudaSuccess) {
+            cudaStreamDestroy(cs);
+            LMGPU_CUDA(began);
+        }
+        try {
+            enqueue_chunk(b, cs, b->timed);
+        } catch (...) {
+            cudaGraph_t gr = nullptr;
+            cudaStreamEndCapture(cs, &gr);
+            if (gr) cudaGraphDestroy(gr);
+            cudaStreamDestroy(cs);
+            throw;
+        }
+        cudaError_t ended = cudaStreamEndCapture(cs, &ng);
         cudaStreamDestroy(cs);
-        throw;
+        LMGPU_CUDA(ended);
     }
-    LMGPU_CUDA(cudaStreamEndCapture(cs, &ng));
-    LMGPU_CUDA(cudaStreamDestroy(cs));
     // only the job's tree or film changed: the new graph has the same nodes, so update the
     // executable in place
     bool updated = false;
@@ -3385,7 +3407,7 @@ int lmgpu_batch_create(lmgpu_batch** out, int64_t queue_paths) {
         b->hits.alloc(c * 16);
         b->s_o.alloc(2 * c * 16); b->s_d.alloc(2 * c * 16); b->s_c.alloc(2 * c * 16); b->s_job.alloc(2 * c * 4);
         b->ctl.alloc(256);
-        LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
+        LMGPU_CUDA_SYNC(cudaMemset(b->ctl.p, 0, 256));
         *out = b.release();
     });
 }
@@ -3415,7 +3437,7 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         if (prm->split_passes && prm->instrument) throw Error(LMGPU_ERR_UNSUPPORTED, "split_passes with instrument");
         ensure_film(f);
         if (!prm->accumulate) {
-            LMGPU_CUDA(cudaMemset(f->sum.p, 0, size_t(npix) * 3 * 4));
+            LMGPU_CUDA_SYNC(cudaMemset(f->sum.p, 0, size_t(npix) * 3 * 4));
             f->accumulated_spp = 0;
             f->split = prm->split_passes != 0;
             f->passes_even = f->passes_odd = 0;
@@ -3427,9 +3449,12 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         if (f->split) {
             if (!f->sum_odd.p || f->accumulated_spp == 0) {
                 f->sum_odd.alloc(size_t(npix) * 3 * 4);
-                LMGPU_CUDA(cudaMemset(f->sum_odd.p, 0, size_t(npix) * 3 * 4));
+                LMGPU_CUDA_SYNC(cudaMemset(f->sum_odd.p, 0, size_t(npix) * 3 * 4));
             }
         }
+        lmgpu_batch::JobMeta M;
+        M.spp_budget = M.spp = prm->spp;
+        M.film_first = f->passes_even + f->passes_odd;
         JobDev J{};
         J.S = s->dev;
         J.P.seed = prm->seed;
@@ -3450,9 +3475,11 @@ int lmgpu_batch_submit(lmgpu_batch* b, lmgpu_scene* s, lmgpu_film* f, const lmgp
         }
         J.path_begin = b->total;
         J.npix = npix;
+        J.limit = npix * prm->spp;
         J.pass_off = b->passes;
         b->host_jobs.push_back(J);
         b->films.push_back(f);
+        b->meta.push_back(M);
         b->total += npix * prm->spp;
         b->passes += uint32_t(prm->spp);
         b->host_pass.resize(b->passes, 0);
@@ -3479,10 +3506,10 @@ int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* p
                 nn.alloc(c * sizeof(int64_t));
                 na.alloc(c * sizeof(ActiveJob));
                 nal.alloc(2 * c * sizeof(AllocEntry));
-                LMGPU_CUDA(cudaMemset(nn.p, 0, c * sizeof(int64_t)));
+                LMGPU_CUDA_SYNC(cudaMemset(nn.p, 0, c * sizeof(int64_t)));
                 if (b->aux_cap) {
-                    LMGPU_CUDA(cudaMemcpy(nn.p, b->job_next.p, b->aux_cap * sizeof(int64_t), cudaMemcpyDeviceToDevice));
-                    LMGPU_CUDA(cudaMemcpy(na.p, b->active.p, b->aux_cap * sizeof(ActiveJob), cudaMemcpyDeviceToDevice));
+                    LMGPU_CUDA_SYNC(cudaMemcpy(nn.p, b->job_next.p, b->aux_cap * sizeof(int64_t), cudaMemcpyDeviceToDevice));
+                    LMGPU_CUDA_SYNC(cudaMemcpy(na.p, b->active.p, b->aux_cap * sizeof(ActiveJob), cudaMemcpyDeviceToDevice));
                 }
                 std::swap(b->job_next.p, nn.p); std::swap(b->job_next.bytes, nn.bytes);
                 std::swap(b->active.p, na.p); std::swap(b->active.bytes, na.bytes);
@@ -3496,8 +3523,8 @@ int lmgpu_batch_run(lmgpu_batch* b, int32_t max_chunks, void* stream, int64_t* p
                 size_t c = std::max<size_t>(size_t(b->passes), 2 * b->pass_cap);
                 DevBuf nb;
                 nb.alloc(c * 4);
-                LMGPU_CUDA(cudaMemset(nb.p, 0, c * 4));
-                if (b->pass_cap) LMGPU_CUDA(cudaMemcpy(nb.p, b->pass_done.p, b->pass_cap * 4, cudaMemcpyDeviceToDevice));
+                LMGPU_CUDA_SYNC(cudaMemset(nb.p, 0, c * 4));
+                if (b->pass_cap) LMGPU_CUDA_SYNC(cudaMemcpy(nb.p, b->pass_done.p, b->pass_cap * 4, cudaMemcpyDeviceToDevice));
                 std::swap(b->pass_done.p, nb.p);
                 std::swap(b->pass_done.bytes, nb.bytes);
                 b->pass_cap = c;
@@ -3546,15 +3573,69 @@ int lmgpu_batch_job_status(const lmgpu_batch* b, int32_t job, int32_t* passes_co
     return guarded([&] {
         if (!b || job < 0 || size_t(job) >= b->host_jobs.size()) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown job");
         const JobDev& J = b->host_jobs[job];
+        const int32_t spp = b->meta[job].spp;
         int32_t k = 0;
-        while (k < J.P.spp && int64_t(b->host_pass[J.pass_off + k]) >= J.npix) k++;
+        while (k < spp && int64_t(b->host_pass[J.pass_off + k]) >= J.npix) k++;
         if (passes_complete) *passes_complete = k;
         if (done) {
             int32_t all = 1;
-            for (int64_t s = 0; s < J.P.spp; s++)
+            for (int64_t s = 0; s < spp; s++)
                 if (int64_t(b->host_pass[J.pass_off + s]) < J.npix) { all = 0; break; }
             *done = all;
         }
+    });
+}
+
+int lmgpu_batch_job_set_spp(lmgpu_batch* b, int32_t job, int32_t spp, int32_t* spp_out) {
+    return guarded([&] {
+        if (!b || job < 0 || size_t(job) >= b->host_jobs.size()) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown job");
+        JobDev& J = b->host_jobs[job];
+        auto& M = b->meta[job];
+        lmgpu_film* f = b->films[job];
+        if (M.resolved) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "job already resolved");
+        if (spp < 1 || spp > M.spp_budget)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "spp must be in [1, the spp the job was submitted with]");
+        if (f->split && f->passes_even + f->passes_odd != M.film_first + M.spp)
+            throw Error(LMGPU_ERR_UNSUPPORTED, "a later job accumulates into this job's film");
+        const bool on_device = size_t(job) < b->jobs_done;
+        int64_t next = 0;
+        int64_t ctl[32];
+        if (on_device) {
+            LMGPU_CUDA_SYNC(cudaMemcpy(ctl, b->ctl.p, sizeof(ctl), cudaMemcpyDeviceToHost));
+            LMGPU_CUDA_SYNC(cudaMemcpy(&next, b->job_next.as<int64_t>() + job, sizeof(next), cudaMemcpyDeviceToHost));
+        }
+        // passes with a started path stay: they complete as they are
+        const int32_t started = int32_t((next + J.npix - 1) / J.npix);
+        const int32_t nspp = std::max(spp, started);
+        if (spp_out) *spp_out = nspp;
+        if (nspp == M.spp) return;
+        const int64_t delta = int64_t(nspp - M.spp) * J.npix;
+        J.limit = int64_t(nspp) * J.npix;
+        b->total += delta;
+        if (f->split) {
+            const int64_t p0 = int64_t(J.parity0);
+            f->passes_odd += (nspp + p0) / 2 - (M.spp + p0) / 2;
+            f->passes_even += (nspp - (nspp + p0) / 2) - (M.spp - (M.spp + p0) / 2);
+        }
+        M.spp = nspp;
+        if (!on_device) return;  // the next run uploads the job and the total
+        char* jobs_dev = static_cast<char*>(b->jobs.p) + size_t(job) * sizeof(JobDev);
+        LMGPU_CUDA_SYNC(cudaMemcpy(jobs_dev + offsetof(JobDev, limit), &J.limit, sizeof(int64_t), cudaMemcpyHostToDevice));
+        ctl[1] += delta;
+        // a job the planner has seen and dropped from its list of jobs with paths left (every path
+        // of its old count started) rejoins that list, once
+        if (delta > 0 && job < ctl[20]) {
+            std::vector<ActiveJob> act(static_cast<size_t>(ctl[21]));
+            if (!act.empty())
+                LMGPU_CUDA_SYNC(cudaMemcpy(act.data(), b->active.p, act.size() * sizeof(ActiveJob), cudaMemcpyDeviceToHost));
+            const bool listed = std::any_of(act.begin(), act.end(), [&](const ActiveJob& A) { return A.job == job; });
+            if (!listed) {
+                const ActiveJob A{J.npix, J.limit, job, 0};
+                LMGPU_CUDA_SYNC(cudaMemcpy(b->active.as<ActiveJob>() + ctl[21], &A, sizeof(A), cudaMemcpyHostToDevice));
+                ctl[21] += 1;
+            }
+        }
+        LMGPU_CUDA_SYNC(cudaMemcpy(b->ctl.p, ctl, sizeof(ctl), cudaMemcpyHostToDevice));
     });
 }
 
@@ -3564,7 +3645,10 @@ int lmgpu_batch_resolve(lmgpu_batch* b, int32_t job, void* stream) {
         const JobDev& J = b->host_jobs[job];
         lmgpu_film* f = b->films[job];
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        f->accumulated_spp += J.P.spp;
+        auto& M = b->meta[job];
+        if (M.resolved) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "job already resolved");
+        M.resolved = true;
+        f->accumulated_spp += M.spp;
         // renderer_pt.cpp:307-312: 1 / spp in pixel mode; w*h / (w*h*spp paths) in image mode
         const double scale = 1.0 / double(f->accumulated_spp);
         f->scale = scale;
@@ -3582,7 +3666,7 @@ int lmgpu_batch_get_stats(const lmgpu_batch* b, lmgpu_render_stats* out) {
         if (!b || !out) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         std::memset(out, 0, sizeof(*out));
         unsigned long long r[2];
-        LMGPU_CUDA(cudaMemcpy(r, reinterpret_cast<const char*>(b->ctl.p) + 64, sizeof(r), cudaMemcpyDeviceToHost));
+        LMGPU_CUDA_SYNC(cudaMemcpy(r, reinterpret_cast<const char*>(b->ctl.p) + 64, sizeof(r), cudaMemcpyDeviceToHost));
         out->paths = b->total;
         out->extension_rays = int64_t(r[0]);
         out->shadow_rays = int64_t(r[1]);
@@ -3601,9 +3685,10 @@ int lmgpu_batch_get_stats(const lmgpu_batch* b, lmgpu_render_stats* out) {
 int lmgpu_batch_reset(lmgpu_batch* b) {
     return guarded([&] {
         if (!b) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "batch is null");
-        LMGPU_CUDA(cudaDeviceSynchronize());
+        LMGPU_CUDA_SYNC(cudaDeviceSynchronize());
         b->host_jobs.clear();
         b->films.clear();
+        b->meta.clear();
         b->host_pass.clear();
         b->jobs_done = 0;
         b->total = 0;
@@ -3614,9 +3699,9 @@ int lmgpu_batch_reset(lmgpu_batch* b) {
         b->chunks_run = 0;
         for (double& k : b->kms) k = 0;
         b->table_dirty = false;
-        LMGPU_CUDA(cudaMemset(b->ctl.p, 0, 256));
-        if (b->pass_cap) LMGPU_CUDA(cudaMemset(b->pass_done.p, 0, b->pass_cap * 4));
-        if (b->aux_cap) LMGPU_CUDA(cudaMemset(b->job_next.p, 0, b->aux_cap * sizeof(int64_t)));
+        LMGPU_CUDA_SYNC(cudaMemset(b->ctl.p, 0, 256));
+        if (b->pass_cap) LMGPU_CUDA_SYNC(cudaMemset(b->pass_done.p, 0, b->pass_cap * 4));
+        if (b->aux_cap) LMGPU_CUDA_SYNC(cudaMemset(b->job_next.p, 0, b->aux_cap * sizeof(int64_t)));
     });
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <shared_mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -27,6 +28,20 @@ void set_last_error(const std::string& msg);
         if (e_ != cudaSuccess)                                                                    \
             throw ::lmgpu::Error(e_ == cudaErrorMemoryAllocation ? LMGPU_ERR_OUT_OF_MEMORY : LMGPU_ERR_CUDA, \
                                  std::string(#call) + ": " + cudaGetErrorString(e_));           \
+    } while (0)
+
+// Stream capture (the shared wavefront's CUDA graphs) against calls that may synchronize the
+// device implicitly: cudaMalloc, cudaFree, synchronous copies and memsets, cudaDeviceSynchronize.
+// Such a call made by another host thread while a capture is open (a scene built on a worker
+// thread while the serving loop captures its chunk) invalidates the capture. The capture holds
+// this mutex exclusively; those calls hold it shared, so they wait only while a capture is open
+// (microseconds) and never wait on each other.
+std::shared_mutex& capture_mutex();
+
+#define LMGPU_CUDA_SYNC(call)                                                                    \
+    do {                                                                                          \
+        std::shared_lock<std::shared_mutex> lk_(::lmgpu::capture_mutex());                         \
+        LMGPU_CUDA(call);                                                                         \
     } while (0)
 
 // Runs `fn` and converts any failure into a status code plus lmgpu_last_error() text.
@@ -56,7 +71,10 @@ struct DevBuf {
     DevBuf& operator=(const DevBuf&) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            std::shared_lock<std::shared_mutex> lk(capture_mutex());
+            cudaFree(p);
+        }
         p = nullptr;
         bytes = 0;
     }
@@ -64,7 +82,7 @@ struct DevBuf {
         if (n <= bytes && p) return;
         release();
         if (n == 0) return;
-        LMGPU_CUDA(cudaMalloc(&p, n));
+        LMGPU_CUDA_SYNC(cudaMalloc(&p, n));
         bytes = n;
     }
     template <typename T>
@@ -75,6 +93,11 @@ struct DevBuf {
     template <typename T>
     T* as() const { return static_cast<T*>(p); }
 };
+
+// GPU builder of the 8-wide tree (bvh_gpu.cu): device buffers in the layout of bvh_build.h, plus
+// the flattened-index -> record map. Synchronous on `st`.
+void build_bvh8_gpu(const float* tri_p, int64_t n, DevBuf& nodes, DevBuf& tris, DevBuf& tri_slot, int64_t& num_nodes,
+                    int32_t& depth, double& sah_cost, cudaStream_t st);
 
 struct DeviceInfo {
     int device = 0;
@@ -105,6 +128,8 @@ struct lmgpu_accel {
     double build_seconds = 0;
     double sah_cost = 0;
     lmgpu::DevBuf nodes, tris;
+    lmgpu::DevBuf tri_slot;  // single-level builds: flattened triangle index -> leaf-order record
+    int32_t builder = 0;     // LMGPU_BUILDER_* of the last build
     lmgpu::DevBuf scratch_rays, scratch_hits, err;
     // two-level builds only
     lmgpu::DevBuf inst;                      // per instance: inverse transform rows (3 float4), {root, id_base}

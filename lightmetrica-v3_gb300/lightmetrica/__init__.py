@@ -734,12 +734,15 @@ class LightEnv(_Light):
 
 @_reg("accel::sahbvh", "accel::nanort", "accel::embree")
 class AccelGpu(Component):
-    """The accel slot (include/lm/accel.h): an 8-wide quantized BVH built on the host and traced on
-    the GPU. Registered under every key the reference's accels use. Like accel::sahbvh, nanort
-    and embree it flattens instance groups into one tree; prop `instancing=True` (the default of
-    accel::embreeinstanced and accel::gpu) builds the two-level form instead."""
+    """The accel slot (include/lm/accel.h): an 8-wide quantized BVH traced on the GPU. Registered
+    under every key the reference's accels use. Like accel::sahbvh, nanort and embree it flattens
+    instance groups into one tree; prop `instancing=True` (the default of accel::embreeinstanced
+    and accel::gpu) builds the two-level form instead. GPU extra: prop `builder` -- 'sah' (binned
+    SAH on the host threads, the default) or 'ploc' (built on the GPU: Morton order, PLOC
+    clustering, the same 8-wide collapse); hits are the same either way."""
 
     default_instancing = False
+    BUILDERS = {"sah": 0, "ploc": 1}
 
     def construct(self, prop):
         h = C.c_void_p()
@@ -747,6 +750,10 @@ class AccelGpu(Component):
         self._h = h
         self.num_tris = 0
         self.instancing = bool(prop.get("instancing", self.default_instancing))
+        b = prop.get("builder", "sah")
+        if b not in self.BUILDERS:
+            raise LmGpuError(1, f"Invalid builder '{b}' (sah or ploc)")
+        self.builder = b
 
     def _release(self):
         if getattr(self, "_h", None):
@@ -761,7 +768,7 @@ class AccelGpu(Component):
 
     def build_triangles(self, tri_p: np.ndarray) -> None:
         tri_p = np.ascontiguousarray(tri_p, dtype=np.float32).reshape(-1, 9)
-        N.check(N.lib().lmgpu_accel_build(self._h, N.fptr(tri_p), tri_p.shape[0]))
+        N.check(N.lib().lmgpu_accel_build_ex(self._h, N.fptr(tri_p), tri_p.shape[0], self.BUILDERS[self.builder]))
         self.num_tris = tri_p.shape[0]
 
     def build_instanced(self, tri_p: np.ndarray, blas_offsets, instances) -> None:
@@ -1319,6 +1326,13 @@ class RendererRaycast(Component):
         return {"elapsed": time.perf_counter() - t0}
 
 
+def next_spp_for_error(spp: int, rel_mse: float, target: float, margin: float = 1.05) -> int:
+    """Samples per pixel an estimate needs to reach `target` relative MSE, from `rel_mse` measured
+    after `spp`: the variance of the mean falls as 1/N (a few percent of margin for the
+    estimate's own noise)."""
+    return int(math.ceil(spp * rel_mse / target * margin))
+
+
 @_reg("renderer::pt", "renderer::pt_gpu")
 class RendererPT(Component):
     """renderer::pt (src/renderer/renderer_pt.cpp:51-315) as a wavefront on the GPU.
@@ -1326,7 +1340,10 @@ class RendererPT(Component):
     Props as the reference: scene, output, max_verts, seed, sampling_mode (naive|nee|mis),
     primary_ray_sampling_mode (pixel|image), scheduler ('sample' with spp; 'time' with
     render_time renders progressively in rounds of `spp_per_round` until the time is spent).
-    GPU extras: wave_paths (paths in flight per wave)."""
+    GPU extras: wave_paths (paths in flight per wave); scheduler 'error' with target_rel_mse and
+    spp (the most it renders) renders progressively until the film's relative-MSE estimate
+    (lmgpu_film_rel_mse over even / odd passes, eps rel_mse_eps = 0.01) is at or below the target:
+    a first round of spp_first (8) passes, then rounds sized from the estimate's 1/N fall-off."""
 
     def construct(self, prop):
         self.scene = _resolve(_req(prop, "scene"))
@@ -1354,6 +1371,13 @@ class RendererPT(Component):
         elif self.scheduler == "time":
             self.render_time = float(_req(prop, "render_time"))
             self.spp_per_round = int(prop.get("spp_per_round", 1))
+        elif self.scheduler == "error":
+            self.target_rel_mse = float(_req(prop, "target_rel_mse"))
+            self.spp = int(_req(prop, "spp"))
+            self.spp_first = max(2, int(prop.get("spp_first", 8)))
+            self.rel_mse_eps = float(prop.get("rel_mse_eps", 1e-2))
+            if self.target_rel_mse <= 0 or self.spp < 2:
+                raise LmGpuError(1, "scheduler 'error' needs target_rel_mse > 0 and spp >= 2")
         else:
             raise LmGpuError(1, f"Invalid scheduler '{self.scheduler}'")
         # processed samples as the reference's scheduler reports them: passes in pixel mode
@@ -1383,6 +1407,24 @@ class RendererPT(Component):
                                             None, C.byref(st)))
             processed = self.spp * self._per_pass
             rays, dev_ms = st.rays, st.elapsed_ms
+        elif self.scheduler == "error":
+            processed, rays, dev_ms, k, done_spp = 0, 0, 0.0, 0, 0
+            nxt = min(self.spp, self.spp_first)
+            while True:
+                p = self._params(nxt, k > 0, self.seed + 7919 * k)
+                p.split_passes = 1
+                N.check(N.lib().lmgpu_render_pt(self.scene._h, self.film._h, C.byref(p), None, C.byref(st)))
+                done_spp += nxt
+                processed += nxt * self._per_pass
+                rays += st.rays
+                dev_ms += st.elapsed_ms
+                k += 1
+                err = self.film.rel_mse(self.rel_mse_eps)
+                if err <= self.target_rel_mse or done_spp >= self.spp:
+                    break
+                nxt = min(self.spp, max(next_spp_for_error(done_spp, err, self.target_rel_mse), done_spp + 1)) - done_spp
+            self.last_rel_mse = err
+            self.last_spp = done_spp
         else:
             processed, rays, dev_ms, k = 0, 0, 0.0, 0
             while True:

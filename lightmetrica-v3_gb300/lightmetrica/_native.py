@@ -96,6 +96,7 @@ SIGNATURES = [
     ("lmgpu_accel_create", C.c_int, [C.POINTER(C.c_void_p)]),
     ("lmgpu_accel_destroy", C.c_int, [C.c_void_p]),
     ("lmgpu_accel_build", C.c_int, [C.c_void_p, c_float_p, C.c_int64]),
+    ("lmgpu_accel_build_ex", C.c_int, [C.c_void_p, c_float_p, C.c_int64, C.c_int32]),
     ("lmgpu_accel_build_instanced", C.c_int, [C.c_void_p, c_float_p, C.POINTER(C.c_int64), C.c_int32,
                                               C.POINTER(Instance), C.c_int32]),
     ("lmgpu_accel_intersect", C.c_int, [C.c_void_p, c_float_p, C.c_int64, C.POINTER(Hit)]),
@@ -106,6 +107,8 @@ SIGNATURES = [
                                            C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("lmgpu_bvh8_build_host", C.c_int, [c_float_p, C.c_int64, C.POINTER(C.c_uint32), c_float_p,
                                         C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    ("lmgpu_bvh8_build_gpu", C.c_int, [c_float_p, C.c_int64, C.POINTER(C.c_uint32), c_float_p,
+                                       C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     ("lmgpu_scene_create", C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.POINTER(SceneDesc)]),
     ("lmgpu_scene_destroy", C.c_int, [C.c_void_p]),
     ("lmgpu_scene_device_bytes", C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
@@ -126,6 +129,7 @@ SIGNATURES = [
     ("lmgpu_batch_submit", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(PTParams), C.POINTER(C.c_int32)]),
     ("lmgpu_batch_run", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.POINTER(C.c_int64)]),
     ("lmgpu_batch_job_status", C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("lmgpu_batch_job_set_spp", C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
     ("lmgpu_batch_resolve", C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     ("lmgpu_batch_get_stats", C.c_int, [C.c_void_p, C.POINTER(RenderStats)]),
     ("lmgpu_batch_reset", C.c_int, [C.c_void_p]),

@@ -88,6 +88,13 @@ class BatchRenderer:
         N.check(N.lib().lmgpu_batch_job_status(self._h, int(job), C.byref(passes), C.byref(done)))
         return passes.value, bool(done.value)
 
+    def set_spp(self, job: int, spp: int) -> int:
+        """Moves a job's sample count between runs (down to stop early, up to at most the spp it
+        was submitted with); passes already started stay. Returns the count now in effect."""
+        out = C.c_int32()
+        N.check(N.lib().lmgpu_batch_job_set_spp(self._h, int(job), int(spp), C.byref(out)))
+        return out.value
+
     def resolve(self, job: int) -> None:
         """Rescales a finished job's film so film.buffer() reads the estimate."""
         N.check(N.lib().lmgpu_batch_resolve(self._h, int(job), None))
@@ -101,6 +108,49 @@ class BatchRenderer:
     def reset(self) -> None:
         N.check(N.lib().lmgpu_batch_reset(self._h))
         self._keep.clear()
+
+    def render_to_error(self, jobs: list[dict], target: float, spp_first: int = 8, eps: float = 1e-2,
+                        chunks: int = 2) -> list[dict]:
+        """Renders every job ({scene, film, max_verts, spp, seed, ...}; spp is the most it may
+        render) progressively until its film's relative-MSE estimate is at or below `target`, all
+        in the one shared wavefront: each job starts with spp_first passes; whenever a job is done
+        at its current count the host reads its estimate (lmgpu_film_rel_mse over even / odd
+        passes) and either finishes it or raises its count to what the 1/N fall-off predicts
+        (lmgpu_batch_job_set_spp); the other jobs keep the queue full meanwhile. Returns per job
+        {job, spp, rel_mse, rounds}."""
+        from . import next_spp_for_error
+        info = []
+        for j in jobs:
+            budget = int(j["spp"])
+            jid = self.submit(j["scene"], j["film"], split=True,
+                              **{k: v for k, v in j.items() if k not in ("scene", "film", "split")})
+            cur = self.set_spp(jid, min(budget, max(2, spp_first)))
+            info.append({"job": jid, "film": j["film"], "budget": budget, "spp": cur, "rel_mse": None, "rounds": 1})
+        pending = list(range(len(info)))
+        while pending:
+            left = self.run(chunks)
+            still = []
+            moved = 0
+            for k in pending:
+                r = info[k]
+                _, done = self.status(r["job"])
+                if not done:
+                    still.append(k)
+                    continue
+                moved += 1
+                err = r["film"].rel_mse(eps)
+                r["rel_mse"] = err
+                if err <= target or r["spp"] >= r["budget"]:
+                    self.resolve(r["job"])
+                    continue
+                want = min(r["budget"], max(next_spp_for_error(r["spp"], err, target), r["spp"] + 1))
+                r["spp"] = self.set_spp(r["job"], want)
+                r["rounds"] += 1
+                still.append(k)
+            if left == 0 and moved == 0 and still:
+                raise RuntimeError("render_to_error: the wavefront drained with jobs unfinished")
+            pending = still
+        return [{k: r[k] for k in ("job", "spp", "rel_mse", "rounds")} for r in info]
 
     def render(self, jobs: list[dict]) -> list[int]:
         """Submits every job ({scene, film, max_verts, spp, seed, ...}), runs to completion and
@@ -142,6 +192,7 @@ class Request:
     max_verts: int
     seed: int
     refine: int | None = None
+    target: float | None = None  # render until the film's rel-MSE estimate <= target (spp: the most it may take)
     # filled by the server
     admitted: float | None = None
     first_image: float | None = None
@@ -151,6 +202,9 @@ class Request:
     pass_times: list = None      # completion time of each of its sample passes
     base_passes: int = 0         # passes the film held before this request (refinements)
     rel_mse: float | None = None  # estimated relative MSE of the finished image
+    spp_run: int = 0             # samples per pixel rendered (target requests stop early)
+    target_time: float | None = None  # when the server read an estimate at or below `target`
+    rounds: int = 0              # error checks of a target request
 
 
 class RenderServer:
@@ -189,6 +243,7 @@ class RenderServer:
         self.footprints: dict[Any, int] = {}  # measured device bytes per scene key
         self.track_error = True               # split passes: each finished image's rel-MSE estimate
         self.rel_mse_eps = 1e-2
+        self.spp_first = 8                    # first error check of a target request
         self._pool = ThreadPoolExecutor(build_threads) if build_threads > 0 else None
         self._building: dict[Any, Any] = {}  # scene key -> future of (scene, build seconds)
         self._film_seq = 0
@@ -270,10 +325,15 @@ class RenderServer:
         self.peak_resident_bytes = max(self.peak_resident_bytes, self.resident_bytes)
         if req.refine is not None:
             base = self.by_id[req.refine]
-            req.base_passes = base.base_passes + base.spp
+            req.base_passes = base.base_passes + base.spp_run
         req.pass_times = []
+        if req.target is not None and not self.track_error:
+            raise ValueError("target requests need track_error (split passes)")
         req.job = self.batch.submit(scene, req.film, max_verts=req.max_verts, spp=req.spp, seed=req.seed,
                                     accumulate=accumulate, split=self.track_error)
+        req.spp_run = req.spp
+        if req.target is not None:
+            req.spp_run = self.batch.set_spp(req.job, min(req.spp, max(2, self.spp_first)))
         req.admitted = self.clock()
         self.scene_users[req.scene_key] = self.scene_users.get(req.scene_key, 0) + 1
         self.scene_last_use[req.scene_key] = req.admitted
@@ -326,10 +386,22 @@ class RenderServer:
                 req.first_image = now
             if passes > len(req.pass_times):
                 req.pass_times.extend([now] * (passes - len(req.pass_times)))
+            if done and req.target is not None:
+                # progressive to a target error: finish, or raise the count the estimate asks for
+                req.rounds += 1
+                req.rel_mse = req.film.rel_mse(self.rel_mse_eps)
+                if req.rel_mse <= req.target:
+                    req.target_time = now
+                elif req.spp_run < req.spp:
+                    from . import next_spp_for_error
+                    want = min(req.spp, max(next_spp_for_error(req.spp_run, req.rel_mse, req.target), req.spp_run + 1))
+                    req.spp_run = self.batch.set_spp(req.job, want)
+                    remaining.append(req)
+                    continue
             if done:
                 self.batch.resolve(req.job)
                 req.done = now
-                if self.track_error and req.base_passes + req.spp >= 2:
+                if self.track_error and req.target is None and req.base_passes + req.spp_run >= 2:
                     req.rel_mse = req.film.rel_mse(self.rel_mse_eps)
                 if req.first_image is None:
                     req.first_image = now
@@ -356,26 +428,18 @@ class RenderServer:
         return not self.pending and not self.inflight
 
     @staticmethod
-    def time_to_rel_mse(req: Request, target: float) -> float | None:
-        """Seconds from arrival until the request's image reached relative MSE `target`, or None if
-        its passes never did. The error of an N-pass estimate falls as 1/N, so with the finished
-        image's estimate e over N passes, pass k = ceil(N * e / target) of the film is the first
-        at or below target (0 for a refinement whose base image was already there)."""
-        if req.rel_mse is None or not req.pass_times:
+    def time_to_target(req: Request) -> float | None:
+        """Seconds from arrival until the server read an error estimate at or below the request's
+        target (measured at the error check, not extrapolated), or None if it never did."""
+        if req.target is None or req.target_time is None:
             return None
-        total = req.base_passes + req.spp
-        k = int(np.ceil(total * req.rel_mse / target - 1e-9))
-        if k > total:
-            return None
-        own = k - req.base_passes
-        if own <= 0:
-            return 0.0
-        return req.pass_times[own - 1] - req.arrival
+        return req.target_time - req.arrival
 
-    def latencies(self, rel_mse_targets=(1e-3, 1e-2)) -> dict:
-        """p50/p99 of time-to-first-image and time-to-done (from arrival, seconds); with error
-        tracking also the finished images' relative MSE and, per target, the time to reach it over
-        the requests that did and the fraction that did."""
+    def latencies(self) -> dict:
+        """p50/p99 over every finished request of time-to-first-image and time-to-done (from
+        arrival, seconds); with error tracking the finished images' relative-MSE estimates; for
+        target requests the measured time-to-target over those that reached it, the fraction that
+        did, and the samples per pixel they took."""
         tfi = np.array([r.first_image - r.arrival for r in self.finished])
         ttd = np.array([r.done - r.arrival for r in self.finished])
         if len(ttd) == 0:
@@ -387,10 +451,16 @@ class RenderServer:
         if errs:
             out["rel_mse_p50"] = float(np.percentile(errs, 50))
             out["rel_mse_p99"] = float(np.percentile(errs, 99))
-            for t in rel_mse_targets:
-                ts = [x for x in (self.time_to_rel_mse(r, t) for r in self.finished) if x is not None]
-                key = f"{t:g}"
-                out[f"time_to_rel_mse_{key}_p50"] = float(np.percentile(ts, 50)) if ts else None
-                out[f"time_to_rel_mse_{key}_p99"] = float(np.percentile(ts, 99)) if ts else None
-                out[f"reached_rel_mse_{key}"] = len(ts) / len(self.finished)
+        tgt = [r for r in self.finished if r.target is not None]
+        if tgt:
+            ts = [self.time_to_target(r) for r in tgt]
+            reached = [t for t in ts if t is not None]
+            spp = [r.spp_run for r in tgt]
+            out["target_requests"] = len(tgt)
+            out["reached_target"] = len(reached) / len(tgt)
+            out["time_to_target_p50"] = float(np.percentile(reached, 50)) if reached else None
+            out["time_to_target_p99"] = float(np.percentile(reached, 99)) if reached else None
+            out["target_spp_p50"] = float(np.percentile(spp, 50))
+            out["target_spp_p99"] = float(np.percentile(spp, 99))
+            out["target_rounds_mean"] = float(np.mean([r.rounds for r in tgt]))
         return out

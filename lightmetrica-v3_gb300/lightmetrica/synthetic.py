@@ -208,19 +208,17 @@ def ground_grid(n: int, half: float, y: float = 0.0):
 SPHERES_CAMERA = dict(position=[0.0, 4.0, 15.0], center=[0.0, 0.6, 0.0], up=[0, 1, 0], vfov=40)
 
 
-def spheres_scene(seed: int = 7, n_spheres: int = 40, subdiv: int = 6, ground_quads: int = 512, w: int = 1920,
-                  h: int = 1080, accel: str = "sahbvh", env_le: float = 0.3, half: float = 12.0, prefix: str = ""):
-    """Displaced icospheres on a ground plane. Returns (scene, film, info dict). Asset names start
-    with `prefix`."""
+def spheres_parts(seed: int = 7, n_spheres: int = 40, subdiv: int = 6, ground_quads: int = 512, w: int = 1920,
+                  h: int = 1080, env_le: float = 0.3, half: float = 12.0) -> dict:
+    """The displaced-sphere scene as plain data (no library call): camera props, and primitives
+    in scene order, each {"name", "mesh": (ps, ns, fp, fn) or None, "material": (kind, props) or
+    None, "light": (kind, props) or None}. spheres_scene builds the `lightmetrica` scene from it;
+    a CPU restatement can build its own scene from the same data."""
     rng = np.random.default_rng(seed)
-    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
-    camera = lm.load_camera(prefix + "camera", "pinhole", aspect=w / h, **SPHERES_CAMERA)
-    scene = lm.load_scene(prefix + "scene", "default", accel=lm.load_accel(prefix + "accel", accel))
-    scene.add_primitive(camera=camera)
+    prims = []
     gp, gn, gf = ground_grid(ground_quads, half)
-    ground = lm.load_mesh(prefix + "ground", "raw", ps=gp, ns=gn, ts=np.zeros((1, 2), np.float32),
-                          fs={"p": gf.reshape(-1), "n": np.zeros(gf.size, np.int32), "t": np.zeros(gf.size, np.int32)})
-    scene.add_primitive(mesh=ground, material=lm.load_material(prefix + "ground_mat", "diffuse", Kd=[0.6, 0.6, 0.6]))
+    prims.append({"name": "ground", "mesh": (gp, gn, gf.reshape(-1), np.zeros(gf.size, np.int32)),
+                  "material": ("diffuse", {"Kd": [0.6, 0.6, 0.6]}), "light": None})
     kinds = np.array(["diffuse"] * int(round(0.5 * n_spheres)) + ["glossy"] * int(round(0.3 * n_spheres)))
     kinds = np.concatenate([kinds, np.array(["glass"] * (n_spheres - len(kinds)))])
     rng.shuffle(kinds)
@@ -234,29 +232,73 @@ def spheres_scene(seed: int = 7, n_spheres: int = 40, subdiv: int = 6, ground_qu
                 break
         centers.append((c, r))
         p, n, f = displaced_sphere(subdiv, c, r, 0.05, seed * 1000 + i)
-        mesh = lm.load_mesh(prefix + f"sphere{i}", "raw", ps=p, ns=n, ts=np.zeros((1, 2), np.float32),
-                            fs={"p": f.reshape(-1), "n": f.reshape(-1), "t": np.zeros(f.size, np.int32)})
         if kinds[i] == "diffuse":
-            mat = lm.load_material(prefix + f"mat{i}", "diffuse", Kd=rng.uniform(0.2, 0.9, 3))
+            mat = ("diffuse", {"Kd": rng.uniform(0.2, 0.9, 3)})
         elif kinds[i] == "glossy":
             rough = rng.uniform(0.05, 0.5)
-            mat = lm.load_material(prefix + f"mat{i}", "glossy", Ks=rng.uniform(0.5, 0.95, 3), ax=rough, ay=rough)
+            mat = ("glossy", {"Ks": rng.uniform(0.5, 0.95, 3), "ax": rough, "ay": rough})
         else:
-            mat = lm.load_material(prefix + f"mat{i}", "glass", Ni=1.5)
-        scene.add_primitive(mesh=mesh, material=mat)
+            mat = ("glass", {"Ni": 1.5})
+        prims.append({"name": f"sphere{i}", "mesh": (p, n, f.reshape(-1), f.reshape(-1)), "material": mat,
+                      "light": None})
         tris += f.shape[0]
-    black = lm.load_material(prefix + "light_mat", "diffuse", Kd=[0, 0, 0])
     for k in range(6):
         ang = 2 * math.pi * k / 6 + rng.uniform(-0.2, 0.2)
         cx, cz, y, s = 6.0 * math.cos(ang), 6.0 * math.sin(ang), rng.uniform(6.0, 8.0), 0.75
-        lmesh = load_mesh(prefix + f"light_mesh{k}", *quad((cx - s, y, cz - s), (cx + s, y, cz - s), (cx + s, y, cz + s),
-                                                  (cx - s, y, cz + s), (0, -1, 0)))
-        light = lm.load_light(prefix + f"light{k}", "area", Ke=list(rng.uniform(8.0, 16.0, 3)), mesh=lmesh)
-        scene.add_primitive(mesh=lmesh, material=black, light=light)
+        prims.append({"name": f"light{k}", "mesh": quad((cx - s, y, cz - s), (cx + s, y, cz - s), (cx + s, y, cz + s),
+                                                        (cx - s, y, cz + s), (0, -1, 0)),
+                      "material": ("diffuse", {"Kd": [0, 0, 0]}),
+                      "light": ("area", {"Ke": list(rng.uniform(8.0, 16.0, 3))})})
         tris += 2
     if env_le > 0:
-        scene.add_primitive(light=lm.load_light(prefix + "env", "envconst", Le=[env_le, env_le, env_le * 1.1]))
-    return scene, film, {"triangles": tris, "spheres": n_spheres, "subdiv": subdiv, "ground_quads": ground_quads}
+        prims.append({"name": "env", "mesh": None, "material": None,
+                      "light": ("envconst", {"Le": [env_le, env_le, env_le * 1.1]})})
+    camera = dict(SPHERES_CAMERA, aspect=w / h)
+    return {"camera": camera, "primitives": prims, "w": w, "h": h,
+            "info": {"triangles": tris, "spheres": n_spheres, "subdiv": subdiv, "ground_quads": ground_quads}}
+
+
+def spheres_scene(seed: int = 7, n_spheres: int = 40, subdiv: int = 6, ground_quads: int = 512, w: int = 1920,
+                  h: int = 1080, accel: str = "sahbvh", env_le: float = 0.3, half: float = 12.0, prefix: str = ""):
+    """Displaced icospheres on a ground plane. Returns (scene, film, info dict). Asset names start
+    with `prefix`."""
+    d = spheres_parts(seed, n_spheres, subdiv, ground_quads, w, h, env_le, half)
+    film = lm.load_film(prefix + "film", "bitmap", w=w, h=h)
+    camera = lm.load_camera(prefix + "camera", "pinhole", **d["camera"])
+    scene = lm.load_scene(prefix + "scene", "default", accel=lm.load_accel(prefix + "accel", accel))
+    scene.add_primitive(camera=camera)
+    mats = {}
+    for pr in d["primitives"]:
+        mesh = mat = light = None
+        if pr["mesh"] is not None:
+            ps, ns, fp, fn = pr["mesh"]
+            mesh = lm.load_mesh(prefix + pr["name"] + ("_mesh" if pr["light"] else ""), "raw",
+                                ps=np.asarray(ps, np.float32), ns=np.asarray(ns, np.float32),
+                                ts=np.zeros((1, 2), np.float32),
+                                fs={"p": np.asarray(fp, np.int32), "n": np.asarray(fn, np.int32),
+                                    "t": np.zeros(len(fp), np.int32)})
+        if pr["material"] is not None:
+            kind, props = pr["material"]
+            if pr["light"] is not None:  # every light quad shares one black material
+                if "light_mat" not in mats:
+                    mats["light_mat"] = lm.load_material(prefix + "light_mat", kind, **props)
+                mat = mats["light_mat"]
+            else:
+                name = "ground_mat" if pr["name"] == "ground" else "mat" + pr["name"][len("sphere"):]
+                mat = lm.load_material(prefix + name, kind, **props)
+        if pr["light"] is not None:
+            kind, props = pr["light"]
+            light = lm.load_light(prefix + pr["name"], kind, **(dict(props, mesh=mesh) if kind == "area" else props))
+        scene.add_primitive(mesh=mesh, material=mat, light=light)
+    return scene, film, d["info"]
+
+
+# The raycast probe of the plain drop-in workload: 2^24 rays with directions uniform on the sphere
+# from one point inside the displaced-sphere scene's bounding box (above the ground, between the
+# spheres).
+RAYCAST_PROBE_ORIGIN = (0.0, 1.0, 0.5)
+RAYCAST_PROBE_RAYS = 1 << 24
+RAYCAST_PROBE_SEED = 11
 
 
 def sphere_rays(n: int, origin, seed: int = 11, tmin: float = 1e-3, tmax: float = 1e10) -> np.ndarray:

@@ -527,6 +527,18 @@ template <typename F> struct Tri {
     }
 };
 
+// The hit distance the GPU's accel API reports for an accepted fp32 hit: the formula of
+// accel_sahbvh.cpp:58-75 (p = d x e2, tv = o - p1, q = tv x e1, t = (e2 . q) / (e1 . p)) evaluated
+// in double on the same fp32 ray and triangle (p1, e1, e2), rounded once to float. Which triangle
+// is hit is still decided by the fp32 test.
+inline float refine_hit_t(const V3<float>& o, const V3<float>& d, const Tri<float>& tr) {
+    auto D = [](const V3<float>& v) { return V3<double>(double(v.x), double(v.y), double(v.z)); };
+    const auto p = cross(D(d), D(tr.e2));
+    const auto tv = D(o) - D(tr.p1);
+    const auto q = cross(tv, D(tr.e1));
+    return float(dot(D(tr.e2), q) / dot(D(tr.e1), p));
+}
+
 template <typename F> struct Accel {
     struct Node { Bound<F> b; bool leaf = false; int s = 0, e = 0, c1 = 0, c2 = 0; };
     struct Flat { Transform<F> tr; int primitive; };

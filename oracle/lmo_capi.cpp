@@ -5,6 +5,7 @@
 #include <chrono>
 #include <cstring>
 #include <memory>
+#include <type_traits>
 
 using namespace lmo;
 
@@ -236,7 +237,7 @@ int lmo_get_triangles(void* p, float* out9) {
 // Outputs: t (float64), u, v (float64), global triangle index (-1 = miss). brute != 0 uses the
 // exhaustive test instead of the BVH. Returns the elapsed seconds in *secs.
 int lmo_intersect(void* p, const float* rays, long long n, double* t_out, double* uv_out, int* tri_out,
-                  int nthreads, int brute, double* secs) {
+                  int nthreads, int brute, int refine_t, double* secs) {
     auto* h = static_cast<Handle*>(p);
     return dispatch(h, [&](auto& S) -> int {
         using F = typename std::decay_t<decltype(S)>::Float;
@@ -249,6 +250,8 @@ int lmo_intersect(void* p, const float* rays, long long n, double* t_out, double
             const auto hit = brute ? S.accel.intersect_brute(ray, F(r[3]), F(r[7])) : S.accel.intersect(ray, F(r[3]), F(r[7]));
             if (hit) {
                 t_out[i] = double(hit->t); uv_out[2 * i] = double(hit->uv.x); uv_out[2 * i + 1] = double(hit->uv.y);
+                if constexpr (std::is_same_v<F, float>)
+                    if (refine_t) t_out[i] = double(refine_hit_t(ray.o, ray.d, S.accel.trs.at(hit->global_tri)));
                 tri_out[i] = hit->global_tri;
             } else {
                 t_out[i] = 0; uv_out[2 * i] = 0; uv_out[2 * i + 1] = 0; tri_out[i] = -1;

@@ -52,7 +52,7 @@ def lib() -> C.CDLL:
         L.lmo_build.argtypes = [vp, C.c_int, C.c_int, dp]
         L.lmo_num_triangles.argtypes = [vp]
         L.lmo_get_triangles.argtypes = [vp, fp]
-        L.lmo_intersect.argtypes = [vp, fp, C.c_longlong, dp, dp, ip, C.c_int, C.c_int, dp]
+        L.lmo_intersect.argtypes = [vp, fp, C.c_longlong, dp, dp, ip, C.c_int, C.c_int, C.c_int, dp]
         L.lmo_render_raycast.argtypes = [vp, C.c_int, C.c_int, dp, C.c_int, C.c_int, dp, dp, C.c_int, dp]
         L.lmo_render_pt.argtypes = [vp, C.c_int, C.c_int, C.c_longlong, C.c_int, C.c_uint, C.c_int, C.c_int, C.c_int,
                                     dp, dp, C.POINTER(C.c_longlong), C.c_int, dp]
@@ -164,8 +164,10 @@ class OracleScene:
         _chk(lib().lmo_get_triangles(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
         return out
 
-    def intersect(self, rays: np.ndarray, nthreads: int = 0, brute: bool = False):
-        """Returns (t, uv, global triangle index, seconds); index -1 = miss."""
+    def intersect(self, rays: np.ndarray, nthreads: int = 0, brute: bool = False, refine_t: bool = False):
+        """Returns (t, uv, global triangle index, seconds); index -1 = miss. refine_t (fp32 mode):
+        t is the hit triangle's distance recomputed in double and rounded once to float, as the
+        GPU's accel API reports it for single-level trees."""
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
         n = rays.shape[0]
         t = np.zeros(n)
@@ -174,7 +176,8 @@ class OracleScene:
         s = C.c_double()
         _chk(lib().lmo_intersect(self.h, rays.ctypes.data_as(C.POINTER(C.c_float)), n, _dp(t) if False else
                                  t.ctypes.data_as(C.POINTER(C.c_double)), uv.ctypes.data_as(C.POINTER(C.c_double)),
-                                 tri.ctypes.data_as(C.POINTER(C.c_int)), nthreads, 1 if brute else 0, C.byref(s)))
+                                 tri.ctypes.data_as(C.POINTER(C.c_int)), nthreads, 1 if brute else 0, 1 if refine_t else 0,
+                                 C.byref(s)))
         return t, uv, tri, s.value
 
     def render_raycast(self, w, h, bg=(0, 0, 0), use_constant_color=False, visualize_normal=False, color=None,
@@ -234,12 +237,60 @@ class OracleScene:
         return out, rays.value, s.value
 
 
+def mt32(rays, tri32, idx):
+    """fp32 Moller-Trumbore t of triangle idx[k] (records p1, e1, e2 of the oracle's fp32 accel)
+    for ray k, in the operation order of accel_sahbvh.cpp:58-75 with glm's dot and cross (every
+    numpy float32 op rounds once, as the kernel's IEEE ops do)."""
+    f = np.float32
+    o = rays[:, 0:3].astype(f)
+    d = rays[:, 4:7].astype(f)
+    T = tri32[idx]
+    p1, e1, e2 = T[:, 0:3], T[:, 3:6], T[:, 6:9]
+
+    def cross(x, y):
+        return np.stack([x[:, 1] * y[:, 2] - y[:, 1] * x[:, 2], x[:, 2] * y[:, 0] - y[:, 2] * x[:, 0],
+                         x[:, 0] * y[:, 1] - y[:, 0] * x[:, 1]], 1)
+
+    def dot(x, y):
+        return (x[:, 0] * y[:, 0] + x[:, 1] * y[:, 1]) + x[:, 2] * y[:, 2]
+
+    p = cross(d, e2)
+    q = cross(o - p1, e1)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return dot(e2, q) / dot(e1, p)
+
+
 def philox_uniform(seed: int, path: int, vertex: int, slot: int) -> float:
     return float(lib().lmo_philox_uniform(seed, path, vertex, slot))
 
 
 def max_threads() -> int:
     return lib().lmo_max_threads()
+
+
+def from_parts(parts: dict, double: bool = True) -> OracleScene:
+    """Builds the oracle's scene straight from a plain scene description (synthetic.spheres_parts:
+    camera props and primitives in scene order), without the GPU library: the same graph
+    from_lm_scene rebuilds from the `lightmetrica` objects."""
+    O = OracleScene(double)
+    c = parts["camera"]
+    cam = O.add_camera(c["position"], c["center"], c["up"], c["vfov"], c["aspect"])
+    O.add_child(0, O.primitive(-1, -1, -1, cam))
+    for pr in parts["primitives"]:
+        me = ma = li = -1
+        if pr["mesh"] is not None:
+            ps, ns, fp, fn = pr["mesh"]
+            me = O.add_mesh(ps, ns, fp, fn)
+        if pr["material"] is not None:
+            kind, m = pr["material"]
+            params = {"diffuse": lambda: list(m["Kd"]), "glossy": lambda: list(m["Ks"]) + [m["ax"], m["ay"]],
+                      "glass": lambda: [m["Ni"]], "mirror": lambda: []}[kind]()
+            ma = O.add_material(MAT["material::" + kind], params)
+        if pr["light"] is not None:
+            kind, L = pr["light"]
+            li = O.add_area_light(L["Ke"], me) if kind == "area" else O.add_envconst(L["Le"])
+        O.add_child(0, O.primitive(me, ma, li, -1))
+    return O
 
 
 def from_lm_scene(scene, double: bool = True) -> OracleScene:

@@ -29,6 +29,20 @@ def build_host(native, tri_p: np.ndarray):
     return nodes[:20 * nn.value].reshape(-1, 20), tris.reshape(-1, 12), depth.value
 
 
+def build_gpu(native, tri_p: np.ndarray):
+    """The same arrays from the GPU builder (lmgpu_bvh8_build_gpu; needs a device)."""
+    tri_p = np.ascontiguousarray(tri_p, np.float32).reshape(-1, 9)
+    n = tri_p.shape[0]
+    nodes = np.zeros(20 * max(n, 1), np.uint32)
+    tris = np.zeros(12 * n, np.float32)
+    nn = C.c_int64()
+    depth = C.c_int32()
+    from lightmetrica import _native as N
+    N.check(native.lmgpu_bvh8_build_gpu(N.fptr(tri_p), n, nodes.ctypes.data_as(C.POINTER(C.c_uint32)), N.fptr(tris),
+                                        C.byref(nn), C.byref(depth)))
+    return nodes[:20 * nn.value].reshape(-1, 20), tris.reshape(-1, 12), depth.value
+
+
 def decode(w: np.ndarray) -> dict:
     u = w.astype(np.uint64)
     org = w[0:3].view(np.float32)

@@ -200,3 +200,84 @@ def test_split_passes_estimate_relative_mse(lm):
     b.resolve(j)
     assert 1.4 < est[64] / f.rel_mse(1e-2) < 2.9
     b.close()
+
+
+def test_set_spp_stops_and_resumes(lm):
+    """lmgpu_batch_job_set_spp: a job stopped after N passes holds exactly the first N passes of
+    its submitted render (streams stay keyed by the submitted spp), whether stopped before it
+    starts or while it is in flight, and raising the count back completes the submitted render."""
+    from lightmetrica.serving import BatchRenderer
+    from lightmetrica import synthetic as syn
+    s, f = syn.box_scene(w=24, h=20, prefix="sppbox_")
+    s.build()
+    kw = dict(max_verts=9, spp=16, seed=5)
+    full = _alone(lm, s, f, **kw)
+    # stopped before the first run, then resumed: the film adds up to the full render
+    b = BatchRenderer(queue_paths=1000)
+    j = b.submit(s, f, **kw)
+    assert b.set_spp(j, 6) == 6
+    b.run(0)
+    assert b.status(j) == (6, True)
+    assert b.set_spp(j, 16) == 16
+    assert b.status(j)[1] is False
+    b.run(0)
+    assert b.status(j) == (16, True)
+    b.resolve(j)
+    np.testing.assert_allclose(f.buffer_f32(), full, **TOL)
+    with pytest.raises(lm.LmGpuError):
+        b.set_spp(j, 4)  # resolved
+    b.close()
+    # stopped in flight: the count becomes at least the passes already started, and the image
+    # is the same as that many passes stopped before the start, alone or beside another job
+    b = BatchRenderer(queue_paths=2000)
+    j = b.submit(s, f, **kw)
+    b.run(1)
+    n = b.set_spp(j, 3)
+    assert 3 <= n <= 16
+    b.run(0)
+    assert b.status(j) == (n, True)
+    b.resolve(j)
+    stopped = f.buffer_f32().copy()
+    b.close()
+    f2 = lm.load_film("spp_f2", "bitmap", w=24, h=20)
+    s2, fo, _ = syn.spheres_scene(n_spheres=3, subdiv=2, ground_quads=4, w=16, h=12, prefix="sppsph_")
+    s2.build()
+    b = BatchRenderer(queue_paths=700)
+    other = b.submit(s2, fo, max_verts=8, spp=6, seed=2)
+    j2 = b.submit(s, f2, **kw)
+    assert b.set_spp(j2, n) == n
+    b.run(0)
+    assert b.status(j2) == (n, True) and b.status(other) == (6, True)
+    b.resolve(j2)
+    np.testing.assert_allclose(f2.buffer_f32(), stopped, **TOL)
+    with pytest.raises(lm.LmGpuError):
+        b.set_spp(other, 7)  # above the submitted spp
+    b.close()
+
+
+def test_render_to_error_reaches_target(lm):
+    """Progressive rendering to a target relative MSE: every job of a mix ends at or below the
+    target (or at its spp budget), the batched loop and the renderer::pt 'error' scheduler agree on
+    the spp each job needs within the estimate's noise, and jobs that are stopped at a count hold
+    that many passes."""
+    from lightmetrica.serving import BatchRenderer
+    from lightmetrica import synthetic as syn
+    jobs = []
+    for k, (w, h) in enumerate([(32, 32), (48, 40), (24, 24)]):
+        s, f = syn.box_scene(seed=100 + k, w=w, h=h, prefix=f"errbox{k}_")
+        s.build()
+        jobs.append(dict(scene=s, film=f, max_verts=9, spp=4096, seed=20 + k))
+    target = 3e-3
+    b = BatchRenderer(queue_paths=1 << 16)
+    res = b.render_to_error(jobs, target, spp_first=8)
+    b.close()
+    for r in res:
+        assert r["rel_mse"] <= target and 8 <= r["spp"] < 4096, r
+    # the same jobs one at a time through renderer::pt's 'error' scheduler
+    for j, r in zip(jobs, res):
+        f = lm.load_film(f"err_plain_{id(j)}", "bitmap", w=j["film"].w, h=j["film"].h)
+        rp = lm.load_renderer(f"err_pt_{id(j)}", "pt", scene=j["scene"], output=f, max_verts=9, seed=j["seed"],
+                              scheduler="error", target_rel_mse=target, spp=4096)
+        rp.render()
+        assert rp.last_rel_mse <= target
+        assert 0.5 < rp.last_spp / r["spp"] < 2.0, (rp.last_spp, r)

@@ -16,6 +16,7 @@ import ctypes as C
 
 import numpy as np
 import pytest
+from parity_util import classify_fp64_mismatches, compare_bitexact
 
 pytestmark = pytest.mark.gpu
 
@@ -48,20 +49,6 @@ def _rays(n, seed, lo=-0.2, hi=1.2):
     return r
 
 
-def _compare_bitexact(gpu, t_ref, uv_ref, id_ref):
-    """Returns (# exact-t ties); asserts every other ray agrees bit for bit."""
-    g_id = gpu["prim"].astype(np.int64)
-    same = g_id == id_ref
-    hit = same & (g_id >= 0)
-    ties = (~same) & (g_id >= 0) & (id_ref >= 0) & (gpu["t"] == t_ref.astype(np.float32))
-    bad = ~(same | ties)
-    assert bad.sum() == 0, f"{bad.sum()} of {len(g_id)} rays differ, e.g. {np.nonzero(bad)[0][:5]}"
-    assert np.array_equal(gpu["t"][hit], t_ref[hit].astype(np.float32))
-    assert np.array_equal(gpu["u"][hit], uv_ref[hit, 0].astype(np.float32))
-    assert np.array_equal(gpu["v"][hit], uv_ref[hit, 1].astype(np.float32))
-    return int(ties.sum())
-
-
 def test_intersect_bitexact_soup(lm, oracle_mod):
     scene = _soup_scene(lm, 20000, 1)
     scene._accel.build(scene)
@@ -69,9 +56,9 @@ def test_intersect_bitexact_soup(lm, oracle_mod):
     gpu = scene._accel.intersect_batch(rays)
     S = oracle_mod.from_lm_scene(scene, double=False)
     S.build(robust=True)
-    t, uv, ids, _ = S.intersect(rays)
+    t, uv, ids, _ = S.intersect(rays, refine_t=True)
     assert (ids >= 0).mean() > 0.3
-    ties = _compare_bitexact(gpu, t, uv, ids)
+    ties = compare_bitexact(gpu, t, uv, ids, rays, S.triangles())
     assert ties <= 10
 
 
@@ -96,23 +83,9 @@ def test_intersect_edge_cases(lm, oracle_mod):
     gpu = scene._accel.intersect_batch(rays)
     S = oracle_mod.from_lm_scene(scene, double=False)
     S.build(robust=True)
-    t, uv, ids, _ = S.intersect(rays, brute=True)
-    _compare_bitexact(gpu, t, uv, ids)
+    t, uv, ids, _ = S.intersect(rays, brute=True, refine_t=True)
+    compare_bitexact(gpu, t, uv, ids, rays, S.triangles())
     assert (gpu["prim"][:n] >= 0).all(), "every downward ray hits the closed grid"
-
-
-def _mt64(o, d, p1, e1, e2):
-    """fp64 Moller-Trumbore without range checks: (t, u, v, |det|) per row."""
-    p = np.cross(d, e2)
-    tv = o - p1
-    q = np.cross(tv, e1)
-    det = np.sum(e1 * p, 1)
-    ad = np.abs(det)
-    s = np.sign(det)
-    u = np.sum(tv * p, 1) * s / np.where(ad > 0, ad, 1)
-    v = np.sum(d * q, 1) * s / np.where(ad > 0, ad, 1)
-    t = np.sum(e2 * q, 1) / np.where(det != 0, det, 1)
-    return t, u, v, ad
 
 
 def test_intersect_spheres_vs_fp32_and_fp64(lm, oracle_mod):
@@ -125,8 +98,8 @@ def test_intersect_spheres_vs_fp32_and_fp64(lm, oracle_mod):
     gpu = scene._accel.intersect_batch(rays)
     S32 = oracle_mod.from_lm_scene(scene, double=False)
     S32.build(robust=True)
-    t, uv, ids, _ = S32.intersect(rays)
-    _compare_bitexact(gpu, t, uv, ids)
+    t, uv, ids, _ = S32.intersect(rays, refine_t=True)
+    compare_bitexact(gpu, t, uv, ids, rays, S32.triangles())
     # against the reference precision
     S64 = oracle_mod.from_lm_scene(scene, double=True)
     S64.build()
@@ -135,22 +108,9 @@ def test_intersect_spheres_vs_fp32_and_fp64(lm, oracle_mod):
     both = (g >= 0) & (g == ids64)
     rel = np.abs(gpu["t"][both] - t64[both]) / t64[both]
     assert rel.max() <= 1e-5, rel.max()
-    mism = np.nonzero(g != ids64)[0]
-    assert len(mism) / len(g) < 1e-3
+    assert (g != ids64).mean() < 1e-3
     tri = scene._flatten()["positions"].reshape(-1, 3, 3).astype(np.float64)
-    unexplained = []
-    for i in mism:
-        o, d = rays[i, 0:3].astype(np.float64), rays[i, 4:7].astype(np.float64)
-        cand = [c for c in (g[i], ids64[i]) if c >= 0]
-        res = []
-        for c in cand:
-            p1 = tri[c, 0]
-            tt, u, v, ad = _mt64(o[None], d[None], p1[None], (tri[c, 1] - p1)[None], (tri[c, 2] - p1)[None])
-            res.append((tt[0], min(u[0], v[0], 1 - u[0] - v[0])))
-        near_tie = len(res) == 2 and abs(res[0][0] - res[1][0]) <= 1e-5 * max(res[0][0], 1e-3)
-        grazing = any(abs(m) <= 1e-5 for _, m in res)
-        if not (near_tie or grazing):
-            unexplained.append(int(i))
+    _, _, unexplained = classify_fp64_mismatches(rays, g, ids64, tri)
     assert not unexplained, unexplained[:10]
 
 

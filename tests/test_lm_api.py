@@ -230,24 +230,6 @@ def test_render_server_builds_scenes_on_a_worker(monkeypatch):
     srv.close()
 
 
-def test_time_to_rel_mse():
-    """Pass k = ceil(N * e / target) of the film is the first at or below target; refinements count
-    from their own arrival and reach targets their base image already met at once."""
-    from lightmetrica.serving import RenderServer, Request
-    r = Request(rid=0, arrival=10.0, scene_key=0, w=1, h=1, spp=8, max_verts=2, seed=0)
-    r.pass_times = [10.0 + 0.5 * (k + 1) for k in range(8)]
-    r.rel_mse = 0.02                                  # after 8 passes
-    assert RenderServer.time_to_rel_mse(r, 0.04) == 2.0   # k = 4
-    assert RenderServer.time_to_rel_mse(r, 0.02) == 4.0   # k = 8
-    assert RenderServer.time_to_rel_mse(r, 0.01) is None  # would need 16 passes
-    q = Request(rid=1, arrival=20.0, scene_key=0, w=1, h=1, spp=16, max_verts=2, seed=0, refine=0)
-    q.base_passes = 8
-    q.pass_times = [20.0 + 0.25 * (k + 1) for k in range(16)]
-    q.rel_mse = 0.02 * 8 / 24
-    assert RenderServer.time_to_rel_mse(q, 0.02) == 0.0   # k = 8: the base image already had it
-    assert RenderServer.time_to_rel_mse(q, 0.01) == 20.0 + 0.25 * 8 - 20.0  # k = 16: 8th own pass
-
-
 def test_material_proxy_and_constant_texture(lm, oracle_mod):
     """material::proxy renders as the material it refers to (material_proxy.cpp); a diffuse
     mapKd that is a texture::constant is its color (texture_constant.cpp); a constant texture is

@@ -11,8 +11,14 @@ class FakeBatch:
 
     def submit(self, scene, film, *, max_verts, spp, seed=0, accumulate=False, split=False, **kw):
         j = len(self.jobs)
-        self.jobs[j] = {"spp": spp, "passes": 0, "film": film, "accumulate": accumulate}
+        self.jobs[j] = {"spp": spp, "budget": spp, "passes": 0, "film": film, "accumulate": accumulate}
+        film.job = self.jobs[j]
         return j
+
+    def set_spp(self, job, spp):
+        j = self.jobs[job]
+        j["spp"] = max(min(spp, j["budget"]), j["passes"])
+        return j["spp"]
 
     def run(self, chunks=0):
         for j in self.jobs.values():
@@ -35,8 +41,14 @@ class FakeScene:
 
 
 class FakeFilm:
-    def __init__(self):
+    """err0: the relative MSE of one pass; an N-pass image reads err0 / N."""
+
+    def __init__(self, err0=0.08):
         self.released = False
+        self.err0 = err0
+
+    def rel_mse(self, eps=1e-2):
+        return self.err0 / max(1, self.job["passes"])
 
     def _release(self):
         self.released = True
@@ -140,3 +152,29 @@ def test_release_frees_film_and_guards_refinements(server):
     server.submit(_req(2, "A", refine=0))
     with pytest.raises(ValueError):
         server.step()                                  # refining a released film
+
+
+def test_target_requests_stop_at_the_error_and_report_measured_latency(server):
+    """A request with a target renders spp_first passes, reads the estimate, raises its count to
+    what the 1/N fall-off predicts and finishes once the estimate is at or below the target; its
+    time-to-target is the clock at that check, not an extrapolation. A target its budget cannot
+    reach ends at the budget and counts as not reached."""
+    from lightmetrica.serving import Request
+    server.track_error = True
+    server.spp_first = 4
+    ok = Request(rid=0, arrival=0.0, scene_key="A", w=2, h=2, spp=64, max_verts=5, seed=0, target=0.005)
+    short = Request(rid=1, arrival=0.0, scene_key="A", w=2, h=2, spp=8, max_verts=5, seed=1, target=0.005)
+    server.submit(ok)
+    server.submit(short)
+    for _ in range(200):
+        if server.idle():
+            break
+        server.step()
+    assert server.idle()
+    # err0 / N <= 0.005 needs N >= 16: 4 passes (0.02), then ceil(4 * 0.02 / 0.005 * 1.05) = 17
+    assert ok.spp_run == 17 and ok.rel_mse <= 0.005 and ok.rounds == 2
+    assert ok.target_time is not None and server.time_to_target(ok) == ok.target_time - ok.arrival
+    assert short.spp_run == 8 and short.target_time is None and short.rel_mse > 0.005
+    lat = server.latencies()
+    assert lat["target_requests"] == 2 and lat["reached_target"] == 0.5
+    assert lat["time_to_target_p50"] == server.time_to_target(ok)

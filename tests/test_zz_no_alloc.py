@@ -1,13 +1,15 @@
 """lmgpu_render_pt_noalloc: path tracing for callers that cannot allocate device memory.
 
-Code that renders inside a CUDA graph capture, hosts whose pool allocator owns all of HBM, and
-latency-bound loops cannot let the library call cudaMalloc. The no-allocation entry point keeps
-its wavefront queues in a fixed device array and writes into a film buffer the caller provides.
-This test calls it through the C-ABI twice in a row and checks both results against
-lmgpu_render_pt on the same scene, seed and spp, within the tolerance the wave-size invariance
-test uses (rtol 1e-5, atol 1e-6: only the order of fp32 film additions differs). It also checks
-that a wave above the fixed maximum is rejected. The test allocates the film buffer itself; the
-entry point allocates nothing.
+Some hosts cannot let the library call cudaMalloc: a framework whose pool allocator reserves all
+of HBM at start-up (a library allocation would fail or go unaccounted), or a loop that must stay
+free of allocations once it runs (cudaMalloc synchronizes the device and can fail mid-run). The
+no-allocation entry point keeps its wavefront queues in a fixed device array and writes into a
+film buffer the caller provides. This test calls it through the C-ABI twice in a row and checks
+both results against lmgpu_render_pt on the same scene, seed and spp, within the tolerance the
+wave-size invariance test uses (rtol 1e-5, atol 1e-6: only the order of fp32 film additions
+differs): in pixel and image primary-ray modes, on a one-level box scene and on a two-level
+(instanced) scene. It also checks that a wave above the fixed maximum is rejected. The test
+allocates the film buffer itself; the entry point allocates nothing.
 """
 import ctypes as C
 import glob
@@ -31,22 +33,35 @@ def _cudart():
     pytest.fail("libcudart not found")
 
 
-def test_noalloc_matches_render_pt(lm):
-    from lightmetrica import _native as N
+def _scene(lm, kind, W, H):
     from lightmetrica import synthetic as syn
+    if kind == "box":
+        scene, film = syn.box_scene(w=W, h=H, prefix="na_")
+    else:
+        scene, film, _ = syn.instanced_scene(n_instances=5, n_lat=8, n_lon=12, n_lights=2, w=W, h=H, env_w=16,
+                                             env_h=8, seed=11, spread=3.0, prefix="nai_")
+    scene.build()
+    return scene, film
+
+
+@pytest.mark.parametrize("kind,primary", [("box", "pixel"), ("box", "image"), ("instanced", "pixel")])
+def test_noalloc_matches_render_pt(lm, kind, primary):
+    from lightmetrica import _native as N
     L = N.lib()
     N.check(L.lmgpu_set_device(0))
-    W = H = 32
-    scene, film = syn.box_scene(w=W, h=H)
-    scene.build()
+    W, H = 32, 24
+    scene, film = _scene(lm, kind, W, H)
+    if kind == "instanced":
+        assert scene._accel.stats()["num_instances"] > 1  # a two-level tree: the two-level kernels run
 
     p = N.PTParams()
     p.spp = 16
     p.max_verts = 9
     p.seed = 21
     p.sampling_mode = 2
+    p.primary_mode = 1 if primary == "image" else 0
     N.check(L.lmgpu_render_pt(scene._h, film._h, C.byref(p), None, None))
-    ref = film.buffer_f32()
+    ref = film.buffer_f32().copy()
     assert ref.sum() > 0
 
     rt = _cudart()
