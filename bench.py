@@ -640,6 +640,7 @@ def run_served_stress(lm, args, ctx, budget_bytes: int | None = None) -> dict:
         else:
             j = jobs[key]
             s, _ = syn.triangles_scene(j["scene_seed"], j["tris"], 64, 64, prefix=f"stress{key}_")
+        s._accel.builder = args.served_builder  # built on admission: the GPU builder by default
         s.build()
         return s
     budget = (args.stress_budget_mb << 20) if budget_bytes is None else budget_bytes
@@ -670,7 +671,8 @@ def run_served_stress(lm, args, ctx, budget_bytes: int | None = None) -> dict:
     return {"queue_paths": args.served_queue,
             "workload": f"{n} requests, Poisson at {rate:.1f}/s (80 % of the measured path throughput for this mix), "
                         f"{len(inst)} instanced 4096x2160 jobs (1-4 spp, length 16) among batched-workload jobs on 32 "
-                        f"scenes; {budget >> 20} MB HBM budget; scenes built on admission",
+                        f"scenes; {budget >> 20} MB HBM budget; scenes built on admission "
+                        f"({'GPU PLOC' if args.served_builder == 'ploc' else 'host SAH'} builder)",
             "requests": n, "seconds": total, "jobs_per_s": n / total, "Mrays_per_s": st["rays"] / total / 1e6,
             "ttfi_p50_s": lat["ttfi_p50"], "ttfi_p99_s": lat["ttfi_p99"], "done_p50_s": lat["done_p50"],
             "done_p99_s": lat["done_p99"],
@@ -957,6 +959,8 @@ def main():
     ap.add_argument("--target-rel-mse", type=float, default=1e-3,
                     help="relative MSE the batched_to_error and served legs render to (0 skips batched_to_error)")
     ap.add_argument("--error-budget-spp", type=int, default=4096, help="most spp a job may take to reach the target")
+    ap.add_argument("--served-builder", default="ploc", choices=["sah", "ploc"],
+                    help="BVH builder of the scenes the served_stress legs build on admission")
     ap.add_argument("--batched-jobs", type=int, default=256)
     ap.add_argument("--served-requests", type=int, default=300,
                     help="requests of the served leg (0 skips it); new images render to the target error")

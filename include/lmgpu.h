@@ -118,6 +118,10 @@ typedef struct lmgpu_instance {
  * build up to that rounding. The data is copied. */
 int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const int64_t* blas_offsets, int32_t num_blas,
                                 const lmgpu_instance* instances, int32_t num_instances);
+/* The same with the bottom-level trees built by `builder` (LMGPU_BUILDER_*); the top level over the
+ * instance boxes is always built on the host (one leaf per instance). */
+int lmgpu_accel_build_instanced_ex(lmgpu_accel* accel, const float* tri_p, const int64_t* blas_offsets, int32_t num_blas,
+                                   const lmgpu_instance* instances, int32_t num_instances, int32_t builder);
 
 /* Accel::intersect(Ray, tmin, tmax) (include/lm/accel.h:70; accel_sahbvh.cpp:269-299) over a
  * batch. Host buffers: rays is n x 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax); hits receives n
@@ -170,7 +174,18 @@ typedef struct lmgpu_material {
     float ax, ay;       /* glossy and mixture: GGX roughness */
     float ni;           /* glass index of refraction */
     float ks[3];        /* mixture: Ks of its glossy lobe */
+    int32_t map_kd;     /* diffuse and mixture: texture whose texel replaces Kd (material_diffuse.cpp:36-40), or -1 */
+    int32_t mask;       /* mixture: alpha-mask texture, 4 channels (model_wavefrontobj.cpp:403-410), or -1 */
 } lmgpu_material;
+
+/* texture::bitmap (src/texture/texture_bitmap.cpp): w x h texels of c floats (3 = RGB, 4 = RGBA) at
+ * lmgpu_scene_desc::texels + offset, row-major with row 0 at the bottom (stbi's flip on load).
+ * Looked up at the nearest texel of the wrapped coordinate (texture_bitmap.cpp:68-85). Image
+ * textures are supported by renderer::pt and renderer::raycast. */
+typedef struct lmgpu_texture {
+    int32_t w, h, c, reserved;
+    int64_t offset;
+} lmgpu_texture;
 
 #define LMGPU_LIGHT_AREA 0
 #define LMGPU_LIGHT_ENVCONST 1
@@ -225,6 +240,14 @@ typedef struct lmgpu_scene_desc {
     const float* env_texels;
     int32_t has_camera;
     lmgpu_camera camera;
+    /* Image textures (needed when a material has map_kd or mask >= 0): per triangle the three
+     * corners' texture coordinates (num_tris x 6 floats, u v per corner, in the shading records'
+     * order), the texture table and the texels. */
+    const float* texcoords;
+    int32_t num_textures;
+    const lmgpu_texture* textures;
+    int64_t num_texels;
+    const float* texels;
 } lmgpu_scene_desc;
 
 /* Scene::build (src/scene.cpp:274-317) for the GPU renderers: uploads the description and binds

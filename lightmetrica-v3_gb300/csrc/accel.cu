@@ -327,7 +327,15 @@ int lmgpu_accel_build_ex(lmgpu_accel* accel, const float* tri_p, int64_t num_tri
 
 int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const int64_t* blas_offsets, int32_t num_blas,
                                 const lmgpu_instance* instances, int32_t num_instances) {
+    return lmgpu_accel_build_instanced_ex(accel, tri_p, blas_offsets, num_blas, instances, num_instances,
+                                          LMGPU_BUILDER_HOST_SAH);
+}
+
+int lmgpu_accel_build_instanced_ex(lmgpu_accel* accel, const float* tri_p, const int64_t* blas_offsets, int32_t num_blas,
+                                   const lmgpu_instance* instances, int32_t num_instances, int32_t builder) {
     return guarded([&] {
+        if (builder != LMGPU_BUILDER_HOST_SAH && builder != LMGPU_BUILDER_GPU_PLOC)
+            throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown builder");
         if (!accel || !tri_p || !blas_offsets || !instances) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         if (num_blas < 1 || num_instances < 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "need at least one BLAS and one instance");
         if (blas_offsets[0] != 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "blas_offsets[0] must be 0");
@@ -339,8 +347,31 @@ int lmgpu_accel_build_instanced(lmgpu_accel* accel, const float* tri_p, const in
         std::vector<std::array<double, 6>> lbox(static_cast<size_t>(num_blas));
         for (int32_t b = 0; b < num_blas; b++) {
             const int64_t off = blas_offsets[b], cnt = blas_offsets[b + 1] - off;
-            std::string err;
-            if (!build_bvh8(tri_p + 9 * off, cnt, bl[b], &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+            if (builder == LMGPU_BUILDER_GPU_PLOC) {
+                // the BLAS built on the GPU, brought back for the merge into one node array
+                DevBuf dn, dt, ds;
+                int64_t nn = 0;
+                int32_t depth = 0;
+                double sah = 0;
+                cudaStream_t st;
+                LMGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+                try {
+                    build_bvh8_gpu(tri_p + 9 * off, cnt, dn, dt, ds, nn, depth, sah, st);
+                } catch (...) {
+                    cudaStreamDestroy(st);
+                    throw;
+                }
+                cudaStreamDestroy(st);
+                bl[b].nodes.resize(size_t(nn) * 20);
+                bl[b].tris.resize(size_t(cnt) * 12);
+                LMGPU_CUDA_SYNC(cudaMemcpy(bl[b].nodes.data(), dn.p, size_t(nn) * 80, cudaMemcpyDeviceToHost));
+                LMGPU_CUDA_SYNC(cudaMemcpy(bl[b].tris.data(), dt.p, size_t(cnt) * 48, cudaMemcpyDeviceToHost));
+                bl[b].max_depth = depth;
+                bl[b].sah_cost = sah;
+            } else {
+                std::string err;
+                if (!build_bvh8(tri_p + 9 * off, cnt, bl[b], &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+            }
             std::array<double, 6> bx{1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
             for (int64_t i = 9 * off; i < 9 * (off + cnt); i += 3)
                 for (int a = 0; a < 3; a++) {

@@ -28,6 +28,14 @@ struct DevMaterial {
     float c[3];
     float ax, ay, ni;
     float ks[3];  // mixture: the glossy lobe's Ks
+    int32_t map_kd, mask;  // texture indices or -1 (diffuse / mixture mapKd; mixture alpha mask)
+    float alpha;           // mixture: the alpha mask's value at the shaded point (1 without a mask)
+};
+// texture::bitmap (texture_bitmap.cpp): w x h texels of c (3 or 4) floats at texels + off, row 0
+// at the bottom
+struct DevTexture {
+    int32_t w, h, c, pad;
+    int64_t off;
 };
 struct DevLight {
     int32_t type;
@@ -44,7 +52,8 @@ constexpr uint32_t kFeatEnvTex = 1u;    // a textured environment light (light::
 constexpr uint32_t kFeatMixture = 2u;   // material::mixture_wavefrontobj
 constexpr uint32_t kFeatTwoLevel = 4u;  // a two-level (instanced) tree
 constexpr uint32_t kFeatDelta = 8u;     // light::point or light::directional
-constexpr uint32_t kFeatAll = 15u;
+constexpr uint32_t kFeatTexture = 16u;  // an image texture on a material (mapKd, alpha mask)
+constexpr uint32_t kFeatAll = 31u;
 
 struct DevScene {
     Bvh8 bvh;
@@ -69,6 +78,10 @@ struct DevScene {
     f3 bound_c;
     float bound_r;
     uint32_t feat;  // kFeat* bits present in the scene
+    // image textures (kFeatTexture): per shading record the three corners' texture coordinates
+    const float* uv;
+    const DevTexture* tex;
+    const float* texels;
 };
 
 }  // namespace lmgpu
@@ -76,7 +89,7 @@ struct DevScene {
 struct lmgpu_scene {
     lmgpu_accel* accel = nullptr;
     lmgpu::DevScene dev{};
-    lmgpu::DevBuf shade, prim_ml, mats, lights, ltri, cdf, env;
+    lmgpu::DevBuf shade, prim_ml, mats, lights, ltri, cdf, env, uv, tex, texels;
     lmgpu::DevBuf inst;      // two-level scenes: per-instance shading transforms
     lmgpu::DevBuf counters;  // raycast error flag
 };
@@ -170,7 +183,7 @@ __device__ inline float sn_correction_le(const Geom& g, f3 wi, f3 wo) {
 }
 
 template <uint32_t kF = kFeatAll>
-__device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float v, int32_t& prim) {
+__device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float v, int32_t& prim, int64_t* rec_out = nullptr) {
     if ((kF & kFeatTwoLevel) && S.num_inst > 0) {
         // instance holding hit index id (the last whose first hit index is <= id), then the local
         // surface point moved to world space as scene.cpp:335-343 does with the hit's transform
@@ -183,6 +196,7 @@ __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float 
         const float4 m0 = __ldg(ip), m1 = __ldg(ip + 1), m2 = __ldg(ip + 2);
         const float4 q0 = __ldg(ip + 3), q1 = __ldg(ip + 4), q2 = __ldg(ip + 5), mt = __ldg(ip + 6);
         const int64_t rec = int64_t(__float_as_uint(mt.y)) + (id - int32_t(__float_as_uint(mt.x)));
+        if (rec_out) *rec_out = rec;
         const float4* sp = S.shade + size_t(rec) * 6;
         const float4 s0 = __ldg(sp), s1 = __ldg(sp + 1), s2 = __ldg(sp + 2), s3 = __ldg(sp + 3), s4 = __ldg(sp + 4),
                      s5 = __ldg(sp + 5);
@@ -199,6 +213,7 @@ __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float 
         const f3 gn = normalize(mk(dot(mk(q0.x, q0.y, q0.z), gl), dot(mk(q1.x, q1.y, q1.z), gl), dot(mk(q2.x, q2.y, q2.z), gl)));
         return on_surface(p, n, gn);
     }
+    if (rec_out) *rec_out = id;
     const float4* sp = S.shade + size_t(id) * 6;
     const float4 s0 = __ldg(sp), s1 = __ldg(sp + 1), s2 = __ldg(sp + 2), s3 = __ldg(sp + 3), s4 = __ldg(sp + 4),
                  s5 = __ldg(sp + 5);
@@ -210,6 +225,31 @@ __device__ inline Geom surface_at(const DevScene& S, int32_t id, float u, float 
     const f3 p = mix3(p1, b0, p2, u, p3, v);
     const f3 n = normalize(mix3(n1, b0, n2, u, n3, v));
     return on_surface(p, n, gn);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Image textures (texture_bitmap.cpp:68-85): the nearest texel of the wrapped coordinate.
+__device__ inline int64_t tex_index(const DevTexture& T, float tu, float tv) {
+    const float uu = tu - floorf(tu), vv = tv - floorf(tv);
+    const int x = min(max(int(uu * float(T.w)), 0), T.w - 1);
+    const int y = min(max(int(vv * float(T.h)), 0), T.h - 1);
+    return T.off + int64_t(T.c) * (int64_t(T.w) * y + x);
+}
+// The material at a shaded point: mapKd's texel becomes Kd (material_diffuse.cpp:70, 79, 88; the
+// mixture's diffuse lobe), the alpha mask's value its alpha (model_wavefrontobj.cpp:365-368).
+// Texture coordinates: mix_barycentric of the record's corners (mesh_raw.cpp:97).
+__device__ inline void resolve_textures(const DevScene& S, DevMaterial& m, int64_t rec, float u, float v) {
+    const float* t = S.uv + size_t(rec) * 6;
+    const float b0 = 1.f - u - v;
+    const float tu = fmaf(__ldg(t + 4), v, fmaf(__ldg(t + 2), u, __ldg(t) * b0));
+    const float tv = fmaf(__ldg(t + 5), v, fmaf(__ldg(t + 3), u, __ldg(t + 1) * b0));
+    if (m.map_kd >= 0) {
+        const int64_t i = tex_index(S.tex[m.map_kd], tu, tv);
+        m.c[0] = __ldg(S.texels + i);
+        m.c[1] = __ldg(S.texels + i + 1);
+        m.c[2] = __ldg(S.texels + i + 2);
+    }
+    if (m.mask >= 0) m.alpha = __ldg(S.texels + tex_index(S.tex[m.mask], tu, tv) + 3);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -276,7 +316,10 @@ __device__ inline void glass_fresnel(const DevMaterial& m, const Geom& g, f3 wi,
     const float r2 = r * r;
     Fr = r2 + (1.f - r2) * powf(1.f - cs, 5.f);
 }
-__device__ inline bool mat_specular(const DevMaterial& m) { return m.type == LMGPU_MAT_GLASS || m.type == LMGPU_MAT_MIRROR; }
+__device__ inline bool mat_specular(const DevMaterial& m, int comp = 0) {
+    // the mixture's component 1 is the alpha mask's pass-through (model_wavefrontobj.cpp:513-515)
+    return m.type == LMGPU_MAT_GLASS || m.type == LMGPU_MAT_MIRROR || (m.type == LMGPU_MAT_MIXTURE && comp != 0);
+}
 
 // Lobes shared by the glossy and mixture materials (material_glossy.cpp:35-113) and the diffuse
 // and mixture materials (material_diffuse.cpp:55-95).
@@ -333,10 +376,15 @@ __device__ inline f3 mat_eval(const DevMaterial& m, const Geom& g, f3 wi, f3 wo,
         return mk(m.c[0], m.c[1], m.c[2]) / kPi;
     case LMGPU_MAT_GLOSSY:
         return glossy_eval(m, mk(m.c[0], m.c[1], m.c[2]), g, wi, wo);
-    case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507 with alpha 1: the two lobes summed
+    case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507: the two lobes summed, times alpha
         if (!(kF & kFeatMixture)) return mk(0, 0, 0);  // not in this scene
+        if ((kF & kFeatTexture) && comp != 0) {
+            const float r = eval_delta ? 0.f : 1.f - m.alpha;
+            return mk(r, r, r);
+        }
         const f3 fd = opposite(g, wi, wo) ? mk(0, 0, 0) : mk(m.c[0], m.c[1], m.c[2]) / kPi;
-        return fd + glossy_eval(m, mk(m.ks[0], m.ks[1], m.ks[2]), g, wi, wo);
+        const f3 f = fd + glossy_eval(m, mk(m.ks[0], m.ks[1], m.ks[2]), g, wi, wo);
+        return (kF & kFeatTexture) ? f * m.alpha : f;
     }
     case LMGPU_MAT_GLASS: {
         if (eval_delta) return mk(0, 0, 0);
@@ -386,6 +434,13 @@ __device__ inline bool mat_sample(const DevMaterial& m, const Geom& g, f3 wi, in
     }
     case LMGPU_MAT_MIXTURE: {  // model_wavefrontobj.cpp:437-461: one lobe sampled, weight f / p of the sum
         if (!(kF & kFeatMixture)) return false;
+        if ((kF & kFeatTexture) && comp != 0) {
+            // the alpha mask's pass-through (model_wavefrontobj.cpp:462-471): the reference returns
+            // weight 1, not its f / p, so the path keeps only the component weight 1 / (1 - alpha)
+            wo = -wi;
+            w = mk(1, 1, 1);
+            return true;
+        }
         if (uc < mixture_w(m)) wo = diffuse_dir(g, wi, u0, u1);
         else if (!glossy_dir(m, g, wi, u0, u1, wo)) return false;
         const f3 f = mat_eval<kF>(m, g, wi, wo, 0, false);
@@ -1038,7 +1093,8 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
         return false;
     }
     int32_t prim;
-    const Geom g = surface_at<kF>(S, id, h4.y, h4.z, prim);
+    int64_t rec = 0;
+    const Geom g = surface_at<kF>(S, id, h4.y, h4.z, prim, (kF & kFeatTexture) ? &rec : nullptr);
     const int2 ml = __ldg(S.prim_ml + prim);
     const f3 wi = -d;
     if (ml.y >= 0 && direct_ok) {
@@ -1061,17 +1117,22 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
         if (u[12] < qrr) return false;
         thr = thr / (1.f - qrr);
     }
-    const DevMaterial m = S.mats[ml.x];
+    DevMaterial m = S.mats[ml.x];
+    if ((kF & kFeatTexture) && (m.map_kd >= 0 || m.mask >= 0)) resolve_textures(S, m, rec, h4.y, h4.z);
     int comp = 0;
     if (m.type == LMGPU_MAT_GLASS) {
         f3 wt; bool total; float eta, Fr;
         glass_fresnel(m, g, wi, wt, total, eta, Fr);
         comp = u[13] < Fr ? 0 : 1;
         thr = thr * (1.f / (comp == 0 ? Fr : 1.f - Fr));
+    } else if ((kF & kFeatTexture) && m.type == LMGPU_MAT_MIXTURE && m.mask >= 0) {
+        // model_wavefrontobj.cpp:413-420: the surface with probability alpha, else the pass-through
+        comp = u[13] < m.alpha ? 0 : 1;
+        thr = thr * (1.f / (comp == 0 ? m.alpha : 1.f - m.alpha));
     }
     const int nv = it + 1;
     if (nv >= P.max_verts) return false;
-    const bool spec = mat_specular(m);
+    const bool spec = mat_specular(m, comp);
     const bool nee_ok = P.mode != LMGPU_SAMPLING_NAIVE && !spec;
     rng_slots(P.seed, ids.x, uint32_t(nv), 0, 3, u);
     if (nee_ok) nee<kBatched, kF>(S, P, g, &m, wi, comp, thr, u, ids.y | odd_bit, sq, scount, job);
@@ -1843,7 +1904,8 @@ __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lm
             }
         } else {
             int32_t prim;
-            const Geom g = surface_at(S, hit.id, hit.u, hit.v, prim);
+            int64_t rec = 0;
+            const Geom g = surface_at(S, hit.id, hit.u, hit.v, prim, &rec);
             if (prm.visualize_normal) {
                 c = mk(fabsf(g.n.x), fabsf(g.n.y), fabsf(g.n.z));
             } else {
@@ -1851,7 +1913,8 @@ __global__ void __launch_bounds__(kBlock) k_raycast(DevScene S, int w, int h, lm
                 if (prm.has_color) {
                     R = mk(prm.color[0], prm.color[1], prm.color[2]);
                 } else {
-                    const DevMaterial m = S.mats[__ldg(S.prim_ml + prim).x];
+                    DevMaterial m = S.mats[__ldg(S.prim_ml + prim).x];
+                    if ((S.feat & kFeatTexture) && m.map_kd >= 0) resolve_textures(S, m, rec, hit.u, hit.v);
                     // Material::reflectance: Kd (diffuse, mixture), Ks (glossy), none for the specular ones
                     R = (m.type == LMGPU_MAT_DIFFUSE || m.type == LMGPU_MAT_GLOSSY || m.type == LMGPU_MAT_MIXTURE)
                             ? mk(m.c[0], m.c[1], m.c[2])
@@ -2074,9 +2137,41 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
             if (m.type == LMGPU_MAT_MIXTURE && !(m.ax > 0.f && m.ay > 0.f))
                 throw Error(LMGPU_ERR_INVALID_ARGUMENT, "mixture roughness must be > 0");
             if (m.type == LMGPU_MAT_GLOSSY && !(m.ax > 0.f && m.ay > 0.f)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "glossy roughness must be > 0");
-            mats[i] = DevMaterial{m.type, {m.color[0], m.color[1], m.color[2]}, m.ax, m.ay, m.ni, {m.ks[0], m.ks[1], m.ks[2]}};
+            const bool takes_kd = m.type == LMGPU_MAT_DIFFUSE || m.type == LMGPU_MAT_MIXTURE;
+            if (m.map_kd < -1 || m.map_kd >= D->num_textures || m.mask < -1 || m.mask >= D->num_textures ||
+                (!takes_kd && m.map_kd >= 0) || (m.type != LMGPU_MAT_MIXTURE && m.mask >= 0))
+                throw Error(LMGPU_ERR_INVALID_ARGUMENT, "material texture index out of range or on a material without one");
+            if (m.mask >= 0 && D->textures[m.mask].c != 4)
+                throw Error(LMGPU_ERR_INVALID_ARGUMENT, "alpha mask texture without an alpha channel");
+            mats[i] = DevMaterial{m.type, {m.color[0], m.color[1], m.color[2]}, m.ax, m.ay, m.ni, {m.ks[0], m.ks[1], m.ks[2]},
+                                  m.map_kd, m.mask, 1.f};
         }
         s->mats.upload(mats.data(), mats.size());
+
+        // image textures: the table, the texels and per shading record the corners' coordinates
+        bool textured = false;
+        for (int32_t i = 0; i < D->num_materials; i++)
+            textured = textured || D->materials[i].map_kd >= 0 || D->materials[i].mask >= 0;
+        if (D->num_textures < 0 || D->num_texels < 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "negative texture table size");
+        if (D->num_textures > 0 && (!D->textures || !D->texels)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "missing texture table");
+        if (textured && nt > 0 && !D->texcoords) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "textured materials need texcoords");
+        if (D->num_textures > 0) {
+            std::vector<DevTexture> tex(D->num_textures);
+            for (int32_t i = 0; i < D->num_textures; i++) {
+                const lmgpu_texture& t = D->textures[i];
+                if (t.w <= 0 || t.h <= 0 || (t.c != 3 && t.c != 4) || t.offset < 0 ||
+                    t.offset + int64_t(t.w) * t.h * t.c > D->num_texels)
+                    throw Error(LMGPU_ERR_INVALID_ARGUMENT, "texture size or offset out of range");
+                tex[i] = DevTexture{t.w, t.h, t.c, 0, t.offset};
+            }
+            s->tex.upload(tex.data(), tex.size());
+            s->texels.upload(D->texels, size_t(D->num_texels));
+        }
+        if (textured && nt > 0) {
+            for (int64_t k = 0; k < 6 * nt; k++)
+                if (!std::isfinite(D->texcoords[k])) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "non-finite texture coordinate");
+            s->uv.upload(D->texcoords, size_t(nt) * 6);
+        }
 
         // lights: area CDFs and env tables are built here in double precision, then stored fp32
         std::vector<DevLight> lights(D->num_lights);
@@ -2205,8 +2300,13 @@ int lmgpu_scene_create(lmgpu_scene** out, lmgpu_accel* accel, const lmgpu_scene_
         for (int32_t i = 0; i < D->num_lights; i++)
             if (D->lights[i].type == LMGPU_LIGHT_ENV) ds.feat |= kFeatEnvTex;
             else if (D->lights[i].type == LMGPU_LIGHT_POINT || D->lights[i].type == LMGPU_LIGHT_DIRECTIONAL) ds.feat |= kFeatDelta;
-        for (int32_t i = 0; i < D->num_materials; i++)
+        for (int32_t i = 0; i < D->num_materials; i++) {
             if (D->materials[i].type == LMGPU_MAT_MIXTURE) ds.feat |= kFeatMixture;
+            if (D->materials[i].map_kd >= 0 || D->materials[i].mask >= 0) ds.feat |= kFeatTexture;
+        }
+        ds.uv = s->uv.as<const float>();
+        ds.tex = s->tex.as<const DevTexture>();
+        ds.texels = s->texels.as<const float>();
         ds.shade = s->shade.as<const float4>();
         ds.prim_ml = s->prim_ml.as<const int2>();
         ds.mats = s->mats.as<const DevMaterial>();
@@ -2609,6 +2709,8 @@ int lmgpu_render_pt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_pt_params* prm, v
 int lmgpu_render_lt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_lt_params* prm, void* stream, lmgpu_render_stats* stats) {
     return guarded([&] {
         if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (s->dev.feat & kFeatTexture)
+            throw Error(LMGPU_ERR_UNSUPPORTED, "image textures are supported by renderer::pt and renderer::raycast");
         if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
         if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
         if (prm->num_samples <= 0 || prm->max_verts < 1 || prm->first_path < 0)
@@ -2757,6 +2859,8 @@ int lmgpu_render_lt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_lt_params* prm, v
 int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* prm, void* stream, lmgpu_render_stats* stats) {
     return guarded([&] {
         if (!s || !f || !prm) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
+        if (s->dev.feat & kFeatTexture)
+            throw Error(LMGPU_ERR_UNSUPPORTED, "image textures are supported by renderer::pt and renderer::raycast");
         if (!s->dev.has_camera) throw Error(LMGPU_ERR_UNSUPPORTED, "Missing camera primitive.");
         if (s->dev.num_lights == 0) throw Error(LMGPU_ERR_UNSUPPORTED, "No light in the scene.");
         if (prm->num_samples <= 0 || prm->first_path < 0 || prm->max_verts < 2 || prm->min_verts < 0)
@@ -3196,7 +3300,7 @@ __global__ void k_wf_set_total(int64_t* ctl, int64_t total, int64_t njobs) {
 using WfShadeK = decltype(&k_wf_shade<4, true, kFeatAll>);
 WfShadeK wf_shade_single(uint32_t feat) {
     constexpr int mb = LMGPU_SHADE_SINGLE_MINBLOCKS;
-    if (feat & kFeatDelta) return k_wf_shade<mb, true, kFeatAll>;
+    if (feat & (kFeatDelta | kFeatTexture)) return k_wf_shade<mb, true, kFeatAll>;
     switch (feat & 7u) {
     case 0: return k_wf_shade<mb, true, 0u>;
     case 1: return k_wf_shade<mb, true, 1u>;

@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 import time
 import zlib
 from typing import Any
@@ -417,6 +418,11 @@ class MeshRaw(Component):
             raise LmGpuError(1, "mesh::raw: position index out of range")
         if self.ns.size == 0:
             raise LmGpuError(1, "mesh::raw: normals are required")
+        if self.ts.size == 0:  # no texture coordinates: every corner at (0, 0)
+            self.ts = np.zeros((1, 2), np.float32)
+            self.ft = np.zeros_like(self.fp)
+        if self.ft.size != self.fp.size or (self.ft.size and (self.ft.min() < 0 or self.ft.max() >= len(self.ts))):
+            raise LmGpuError(1, "mesh::raw: texture coordinate index out of range")
         if self.fn.size and (self.fn.min() < 0 or self.fn.max() >= len(self.ns)):
             raise LmGpuError(1, "mesh::raw: normal index out of range")
 
@@ -444,16 +450,21 @@ class _Material(Component):
 @_reg("material::diffuse")
 class MaterialDiffuse(_Material):
     """material::diffuse (material_diffuse.cpp:55-95): Kd, or mapKd, which has priority. A mapKd
-    that is a texture::constant evaluates to its color everywhere, so it becomes Kd; image
-    textures are not on the GPU path."""
+    that is a texture::constant evaluates to its color everywhere, so it becomes Kd; a
+    texture::bitmap is looked up at the shaded point's texture coordinate (renderer::pt and
+    renderer::raycast)."""
 
     def construct(self, prop):
         self.Kd = _vec3(prop.get("Kd", [1, 1, 1]))
-        if prop.get("mapKd") is not None:
+        self.mapKd = None
+        if prop.get("mapKd"):
             tex = _resolve(prop["mapKd"])
-            if not isinstance(tex, TextureConstant):
-                raise LmGpuError(2, "material::diffuse mapKd image textures are not supported on the GPU path")
-            self.Kd = np.asarray(tex.color, np.float64)
+            if isinstance(tex, TextureConstant):
+                self.Kd = np.asarray(tex.color, np.float64)
+            elif isinstance(tex, TextureBitmap):
+                self.mapKd = tex
+            else:
+                raise LmGpuError(1, f"material::diffuse: mapKd is not a texture [{prop['mapKd']!r}]")
 
     def native(self):
         m = super().native()
@@ -514,13 +525,20 @@ class MaterialProxy(_Material):
 @_reg("material::mixture_wavefrontobj")
 class MaterialMixtureWavefrontObj(_Material):
     """material::mixture_wavefrontobj (src/model/model_wavefrontobj.cpp:361-517): the sum of a
-    diffuse (Kd) and a GGX glossy (Ks, ax, ay) lobe, one lobe sampled with probability
-    max(Kd) / (max(Kd) + max(Ks)). Textures (mapKd, and the alpha mask taken from them) are not
-    on the GPU path."""
+    diffuse (Kd, or the texel of mapKd) and a GGX glossy (Ks, ax, ay) lobe, one lobe sampled with
+    probability max(Kd) / (max(Kd) + max(Ks)); when mapKd has an alpha channel (and no_alpha_mask
+    is false) it is also the alpha mask: the surface with probability alpha, else a pass-through."""
 
     def construct(self, prop):
+        self.mapKd = None
+        self.mask = None
         if prop.get("mapKd"):
-            raise LmGpuError(2, "material::mixture_wavefrontobj mapKd textures are not supported on the GPU path")
+            tex = _resolve(prop["mapKd"])
+            if not isinstance(tex, (TextureBitmap, TextureConstant)):
+                raise LmGpuError(1, f"material::mixture_wavefrontobj: mapKd is not a texture [{prop['mapKd']!r}]")
+            self.mapKd = tex
+            if not bool(prop.get("no_alpha_mask", False)) and tex.has_alpha():
+                self.mask = tex
         self.Kd = _vec3(_req(prop, "Kd"))
         self.Ks = _vec3(_req(prop, "Ks"))
         self.ax = float(_req(prop, "ax"))
@@ -561,7 +579,19 @@ class ModelWavefrontObj(Component):
         skip_spec = bool(prop.get("skip_specular_mat", False))
         base = _resolve(prop["base_material"]) if prop.get("base_material") is not None else None
         mat_of: list[Component] = []
+        tex_key = prop.get("texture", "texture::bitmap")
         for m in obj.materials:
+            # map_Kd: one texture per file stem, texture_<stem>, path relative to the OBJ
+            # (model_wavefrontobj.cpp:133-154)
+            tex = None
+            if m.map_Kd and base is None:
+                tid = "texture_" + os.path.splitext(os.path.basename(m.map_Kd))[0]
+                if tid not in self.assets:
+                    cls = _registry.get(tex_key if "::" in tex_key else f"texture::{tex_key}")
+                    if cls is None:
+                        raise LmGpuError(1, f"Missing component [key='{tex_key}']")
+                    self.assets[tid] = cls(tid, {"path": os.path.join(os.path.dirname(path), m.map_Kd)})
+                tex = self.assets[tid]
             if base is not None:
                 mat = base
             elif m.illum in (5, 7):
@@ -572,14 +602,13 @@ class ModelWavefrontObj(Component):
                 else:
                     mat = MaterialMirror(m.name, {})
             else:
-                if m.map_Kd:
-                    raise LmGpuError(2, f"map_Kd textures are not supported on the GPU path [material='{m.name}']")
                 r = 2.0 / (2.0 + m.Ns)
                 a = math.sqrt(max(0.0, 1.0 - m.an * 0.9))
                 if a == 0.0:
                     raise LmGpuError(1, f"aniso >= 1/0.9 gives an infinite roughness [material='{m.name}']")
                 mat = MaterialMixtureWavefrontObj(m.name, {"Kd": list(m.Kd), "Ks": list(m.Ks), "ax": max(1e-3, r / a),
-                                                          "ay": max(1e-3, r * a)})
+                                                          "ay": max(1e-3, r * a), "mapKd": tex,
+                                                          "no_alpha_mask": skip_spec})
             self.assets[m.name] = mat
             mat_of.append(mat)
         n_ps, n_ns = len(obj.ps), len(obj.ns)
@@ -604,9 +633,19 @@ class ModelWavefrontObj(Component):
                 idx = n_ns + np.arange(len(g))
                 fn.reshape(-1, 3)[~has_n] = idx[:, None]
             ns = np.concatenate([obj.ns, extra]) if len(extra) else obj.ns
+            # texture coordinates: a face whose first corner has none reads (0, 0) everywhere
+            # (model_wavefrontobj.cpp:318-320); the entry after the file's vt lines is that (0, 0)
+            n_ts = len(obj.ts)
+            ft = faces[:, 1].copy()
+            no_t = (ft.reshape(-1, 3)[:, 0] < 0) if ft.size else np.zeros(0, bool)
+            ft.reshape(-1, 3)[no_t] = n_ts
+            ft[ft < 0] = n_ts
+            if ft.size and ft.max() > n_ts:
+                raise LmGpuError(1, f"OBJ face refers to a missing texture coordinate [{name}]")
+            ts = np.concatenate([np.asarray(obj.ts, np.float32).reshape(-1, 2), np.zeros((1, 2), np.float32)])
             mesh = MeshRaw(name, {"ps": obj.ps.astype(np.float32), "ns": (ns if len(ns) else np.zeros((1, 3))).astype(np.float32),
-                                  "ts": np.zeros((1, 2), np.float32),
-                                  "fs": {"p": fp.astype(np.int32), "n": fn.astype(np.int32), "t": np.zeros(fp.size, np.int32)}})
+                                  "ts": ts,
+                                  "fs": {"p": fp.astype(np.int32), "n": fn.astype(np.int32), "t": ft.astype(np.int32)}})
             self.assets[name] = mesh
             mtl = obj.materials[prim.material]
             light = None
@@ -643,34 +682,56 @@ class TextureConstant(Component):
     def has_alpha(self) -> bool:
         return self.alpha is not None
 
+    def texels(self) -> np.ndarray:
+        """1 x 1 x (3 or 4) texels for a material's texture table."""
+        c = list(self.color) + ([self.alpha] if self.alpha is not None else [])
+        return np.asarray(c, np.float32).reshape(1, 1, -1)
+
 
 @_reg("texture::bitmap")
 class TextureBitmap(Component):
-    """texture::bitmap with an in-memory array ('data': h x w x 3) or a .pfm/.npy 'path'."""
+    """texture::bitmap (texture_bitmap.cpp:40-85) with an in-memory array ('data': h x w x 3 or 4,
+    row 0 at the bottom) or an image 'path' (.png, .hdr, .pfm, .npy; flipped on load unless
+    flip=False). Three channels serve light::env; a fourth is the alpha has_alpha() reports."""
 
     def construct(self, prop):
         if "data" in prop:
-            self.data = np.ascontiguousarray(np.asarray(prop["data"], dtype=np.float32)[..., :3])
+            full = np.asarray(prop["data"], dtype=np.float32)
         else:
             path = _req(prop, "path")
-            self.data = _read_image(path, flip=bool(prop.get("flip", True)))
+            full = _read_image(path, flip=bool(prop.get("flip", True)), keep_alpha=True)
+        if full.ndim == 2:
+            full = full[..., None]
+        if full.shape[2] == 1:      # gray: widened to RGB
+            full = np.repeat(full, 3, axis=2)
+        elif full.shape[2] == 2:    # gray + alpha
+            full = np.concatenate([np.repeat(full[..., :1], 3, axis=2), full[..., 1:2]], axis=2)
+        self.rgba = np.ascontiguousarray(full[..., :4])
+        self.data = np.ascontiguousarray(self.rgba[..., :3])
         self.h, self.w = self.data.shape[:2]
 
+    def has_alpha(self) -> bool:
+        return self.rgba.shape[2] == 4
 
-def _read_image(path: str, flip: bool = True) -> np.ndarray:
+    def texels(self) -> np.ndarray:
+        return self.rgba
+
+
+def _read_image(path: str, flip: bool = True, keep_alpha: bool = False) -> np.ndarray:
     """texture::bitmap's image (texture_bitmap.cpp:49-66), row 0 at the bottom: .hdr and .png
     (flipped on load unless flip=False; a .png becomes linear as stbi_loadf makes it), .pfm
     (stored bottom row first), .npy (as stored). Three channels are kept."""
     from . import imageio
     try:
+        nc = 4 if keep_alpha else 3
         if path.endswith(".npy"):
-            return np.ascontiguousarray(np.load(path).astype(np.float32)[..., :3])
+            return np.ascontiguousarray(np.load(path).astype(np.float32)[..., :nc])
         if path.endswith(".pfm"):
             return imageio.read_pfm(path)
         if path.endswith(".hdr"):
             return imageio.read_hdr(path, flip=flip)
         if path.endswith(".png"):
-            return np.ascontiguousarray(imageio.read_png(path, flip=flip)[..., :3])
+            return np.ascontiguousarray(imageio.read_png(path, flip=flip)[..., :nc])
     except (OSError, ValueError, zlib.error) as e:
         raise LmGpuError(4, f"Failed to load image [path='{path}']: {e}") from None
     raise LmGpuError(2, f"Unsupported image format [path='{path}'] (use .hdr, .png, .pfm or .npy)")
@@ -781,8 +842,8 @@ class AccelGpu(Component):
         for k, (b, m) in enumerate(instances):
             arr[k].blas = int(b)
             arr[k].transform[:] = [float(x) for x in np.asarray(m, np.float64)[:3, :4].reshape(-1)]
-        N.check(N.lib().lmgpu_accel_build_instanced(self._h, N.fptr(tri_p), offs.ctypes.data_as(C.POINTER(C.c_int64)),
-                                                     len(offs) - 1, arr, len(instances)))
+        N.check(N.lib().lmgpu_accel_build_instanced_ex(self._h, N.fptr(tri_p), offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                        len(offs) - 1, arr, len(instances), self.BUILDERS[self.builder]))
         self.num_tris = self.stats()["num_tris"]
 
     def build(self, scene: "SceneDefault") -> None:
@@ -845,6 +906,16 @@ def _f32_xform(m: np.ndarray, p: np.ndarray) -> np.ndarray:
     for i in range(3):
         out[..., i] = (m[i, 0] * x + m[i, 1] * y) + (m[i, 2] * z + m[i, 3] * one)
     return out
+
+
+def _tri_texcoords(mesh) -> np.ndarray:
+    """Per triangle the three corners' texture coordinates (k, 6), in the mesh's face order."""
+    ts = getattr(mesh, "ts", None)
+    ft = getattr(mesh, "ft", None)
+    n = mesh.num_triangles()
+    if ts is None or ft is None or len(ts) == 0:
+        return np.zeros((n, 6), np.float32)
+    return np.asarray(ts, np.float32)[np.asarray(ft)].reshape(n, 6)
 
 
 def _is_identity(m: np.ndarray) -> bool:
@@ -1014,7 +1085,7 @@ class SceneDefault(Component):
                 light_index_of_node[i] = nl[0]
                 nl[0] += 1
         self.traverse_primitive_nodes(collect_lights)
-        blas: list[dict] = [{"pos": [], "nrm": [], "gn": [], "prim": []}]
+        blas: list[dict] = [{"pos": [], "nrm": [], "gn": [], "prim": [], "tc": []}]
         blas_of_group: dict[int, int] = {}
         instances: list = []
 
@@ -1031,6 +1102,7 @@ class SceneDefault(Component):
             blas[b]["nrm"].append(wn)
             blas[b]["gn"].append(g)
             blas[b]["prim"].append(np.full(wp.shape[0], pi, dtype=np.int32))
+            blas[b]["tc"].append(_tri_texcoords(n["mesh"]))
 
         def visit_local(i, m, b):  # inside an instance group: plain flattening into BLAS b
             n = self.nodes[i]
@@ -1051,7 +1123,7 @@ class SceneDefault(Component):
             if n["instanced"]:
                 if i not in blas_of_group:
                     blas_of_group[i] = len(blas)
-                    blas.append({"pos": [], "nrm": [], "gn": [], "prim": []})
+                    blas.append({"pos": [], "nrm": [], "gn": [], "prim": [], "tc": []})
                     visit_local(i, np.eye(4, dtype=np.float32), blas_of_group[i])
                 instances.append((blas_of_group[i], m.astype(np.float64)))
                 return
@@ -1077,12 +1149,13 @@ class SceneDefault(Component):
                 "geo_normals": cat("gn", 3, np.float32), "tri_prim": cat("prim", 1, np.int32).reshape(-1),
                 "blas_offsets": offs, "instances": instances,
                 "prim_material": np.asarray(prim_mat, np.int32), "prim_light": np.asarray(prim_light, np.int32),
-                "prim_node": np.asarray(prim_node, np.int32), "materials": mats}
+                "prim_node": np.asarray(prim_node, np.int32), "materials": mats,
+                "texcoords": cat("tc", 6, np.float32)}
 
     def _flatten(self, geometry: bool = True) -> dict:
         """Flattened scene: world-space triangles with shading data (unless geometry=False, which
         gives the light tables alone), primitive and material tables, lights in traversal order."""
-        pos, nrm, gns, tri_prim = [], [], [], []
+        pos, nrm, gns, tri_prim, tcs = [], [], [], [], []
         prim_mat, prim_light, prim_node = [], [], []
         mats: list[_Material] = []
         lights: list[tuple] = []        # (light component, global transform, node index)
@@ -1109,6 +1182,7 @@ class SceneDefault(Component):
             nrm.append(wn)
             gns.append(g)
             tri_prim.append(np.full(wp.shape[0], pi, dtype=np.int32))
+            tcs.append(_tri_texcoords(n["mesh"]))
         if geometry:
             self.traverse_primitive_nodes(collect_geometry)
 
@@ -1117,7 +1191,9 @@ class SceneDefault(Component):
             normals = np.ascontiguousarray(np.concatenate(nrm), dtype=np.float32)
             geo = np.ascontiguousarray(np.concatenate(gns), dtype=np.float32)
             tprim = np.ascontiguousarray(np.concatenate(tri_prim), dtype=np.int32)
+            texcoords = np.ascontiguousarray(np.concatenate(tcs), dtype=np.float32)
         else:
+            texcoords = np.zeros((0, 6), np.float32)
             positions = np.zeros((0, 9), np.float32)
             normals = np.zeros((0, 9), np.float32)
             geo = np.zeros((0, 3), np.float32)
@@ -1186,6 +1262,7 @@ class SceneDefault(Component):
             "light_tri_gn": np.concatenate(ltg) if ltg else np.zeros((0, 3), np.float32),
             "light_tri_area": np.concatenate(lta) if lta else np.zeros(0, np.float32),
             "env_texels": np.concatenate(env_tex) if env_tex else np.zeros(0, np.float32),
+            "texcoords": texcoords,
         }
 
     def build(self) -> None:
@@ -1199,7 +1276,7 @@ class SceneDefault(Component):
             # shading data per BLAS in its own frame; lights stay as flattened in world space
             g = self._flatten_instanced()
             for k in ("positions", "normals", "geo_normals", "tri_prim", "prim_material", "prim_light", "prim_node",
-                      "materials", "blas_offsets", "instances"):
+                      "materials", "blas_offsets", "instances", "texcoords"):
                 flat[k] = g[k]
         if flat["positions"].shape[0] == 0:
             raise LmGpuError(2, "Missing primitives. Use lm::primitive() function to add primitives.")
@@ -1222,8 +1299,40 @@ class SceneDefault(Component):
         d.num_prims = len(flat["prim_material"])
         d.prim_material = N.iptr(arr(flat["prim_material"], np.int32))
         d.prim_light = N.iptr(arr(flat["prim_light"], np.int32))
-        mats = (N.Material * max(1, len(flat["materials"])))(*[m.native() for m in flat["materials"]])
+        # image textures: each distinct texture once; materials refer to them by index
+        textures, tex_index = [], {}
+
+        def tex_of(t):
+            if t is None:
+                return -1
+            if id(t) not in tex_index:
+                tex_index[id(t)] = len(textures)
+                textures.append(t)
+            return tex_index[id(t)]
+        natives = []
+        for m in flat["materials"]:
+            nm = m.native()
+            u = m.underlying() if hasattr(m, "underlying") else m
+            nm.map_kd = tex_of(getattr(u, "mapKd", None))
+            nm.mask = tex_of(getattr(u, "mask", None))
+            natives.append(nm)
+        mats = (N.Material * max(1, len(natives)))(*natives)
         d.num_materials = len(flat["materials"])
+        if textures:
+            tables = (N.Texture * len(textures))()
+            parts, off = [], 0
+            for k, t in enumerate(textures):
+                tx = t.texels()
+                tables[k].w, tables[k].h, tables[k].c, tables[k].offset = tx.shape[1], tx.shape[0], tx.shape[2], off
+                parts.append(tx.reshape(-1))
+                off += tx.size
+            texels = arr(np.concatenate(parts), np.float32)
+            keep.append(tables)
+            d.num_textures = len(textures)
+            d.textures = C.cast(tables, C.POINTER(N.Texture))
+            d.num_texels = texels.size
+            d.texels = N.fptr(texels)
+            d.texcoords = N.fptr(arr(flat["texcoords"], np.float32))
         d.materials = C.cast(mats, C.POINTER(N.Material))
         lights = (N.Light * max(1, len(flat["lights"])))(*flat["lights"])
         d.num_lights = len(flat["lights"])

@@ -30,7 +30,18 @@ class AccelStats(C.Structure):
 
 class Material(C.Structure):
     _fields_ = [("type", C.c_int32), ("color", C.c_float * 3), ("ax", C.c_float), ("ay", C.c_float), ("ni", C.c_float),
-                ("ks", C.c_float * 3)]
+                ("ks", C.c_float * 3), ("map_kd", C.c_int32), ("mask", C.c_int32)]
+
+    def __init__(self, *a, **kw):
+        super().__init__(*a, **kw)
+        if "map_kd" not in kw:
+            self.map_kd = -1
+        if "mask" not in kw:
+            self.mask = -1
+
+
+class Texture(C.Structure):
+    _fields_ = [("w", C.c_int32), ("h", C.c_int32), ("c", C.c_int32), ("reserved", C.c_int32), ("offset", C.c_int64)]
 
 
 class Light(C.Structure):
@@ -51,7 +62,8 @@ class SceneDesc(C.Structure):
                 ("num_lights", C.c_int32), ("lights", C.POINTER(Light)), ("num_light_tris", C.c_int64),
                 ("light_tri_p", c_float_p), ("light_tri_gn", c_float_p), ("light_tri_area", c_float_p),
                 ("num_env_texels", C.c_int64), ("env_texels", c_float_p), ("has_camera", C.c_int32),
-                ("camera", Camera)]
+                ("camera", Camera), ("texcoords", c_float_p), ("num_textures", C.c_int32),
+                ("textures", C.POINTER(Texture)), ("num_texels", C.c_int64), ("texels", c_float_p)]
 
 
 class RaycastParams(C.Structure):
@@ -99,6 +111,8 @@ SIGNATURES = [
     ("lmgpu_accel_build_ex", C.c_int, [C.c_void_p, c_float_p, C.c_int64, C.c_int32]),
     ("lmgpu_accel_build_instanced", C.c_int, [C.c_void_p, c_float_p, C.POINTER(C.c_int64), C.c_int32,
                                               C.POINTER(Instance), C.c_int32]),
+    ("lmgpu_accel_build_instanced_ex", C.c_int, [C.c_void_p, c_float_p, C.POINTER(C.c_int64), C.c_int32,
+                                                 C.POINTER(Instance), C.c_int32, C.c_int32]),
     ("lmgpu_accel_intersect", C.c_int, [C.c_void_p, c_float_p, C.c_int64, C.POINTER(Hit)]),
     ("lmgpu_accel_intersect_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     ("lmgpu_accel_occluded_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),

@@ -22,6 +22,7 @@
 #include <atomic>
 #include <condition_variable>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <optional>
@@ -136,7 +137,7 @@ template <typename F> struct Mesh {
         return {mix_barycentric(ps[i1.p], ps[i2.p], ps[i3.p], uv),
                 normalize(mix_barycentric(ns[i1.n], ns[i2.n], ns[i3.n], uv)),
                 geometry_normal(ps[i1.p], ps[i2.p], ps[i3.p]),
-                V2<F>()};
+                mix_barycentric2(ts[i1.t], ts[i2.t], ts[i3.t], uv)};
     }
 };
 
@@ -192,6 +193,26 @@ template <typename F> struct Camera {
 // alpha mask: diffuse (Kd) + GGX glossy (Ks, ax, ay) summed, one lobe sampled
 enum MatType { MAT_DIFFUSE = 0, MAT_GLOSSY = 1, MAT_GLASS = 2, MAT_MIRROR = 3, MAT_MIXTURE = 4 };
 
+// src/texture/texture_bitmap.cpp:68-85: nearest texel of the wrapped texture coordinate, row 0 at
+// the bottom (stbi's vertical flip on load); texels stored row-major with c channels (3 or 4).
+template <typename F> struct Texture {
+    int w = 0, h = 0, c = 3;
+    std::vector<float> data;
+    int index(V2<F> t) const {
+        const auto u = t.x - std::floor(t.x);
+        const auto v = t.y - std::floor(t.y);
+        const int x = std::clamp(int(u * F(w)), 0, w - 1);
+        const int y = std::clamp(int(v * F(h)), 0, h - 1);
+        return w * y + x;
+    }
+    V3<F> eval(V2<F> t) const {
+        const int i = index(t);
+        return V3<F>(F(data[c * i]), F(data[c * i + 1]), F(data[c * i + 2]));
+    }
+    F eval_alpha(V2<F> t) const { return F(data[c * index(t) + 3]); }
+    bool has_alpha() const { return c == 4; }
+};
+
 template <typename F> struct DirectionSample { V3<F> wo; V3<F> weight; };
 template <typename F> struct ComponentSample { int comp; F weight; };
 
@@ -199,6 +220,12 @@ template <typename F> struct Material {
     int type = MAT_DIFFUSE;
     V3<F> Kd = V3<F>(F(1)), Ks;
     F ax = 0, ay = 0, Ni = 1;
+    // material_diffuse.cpp:36-40 (mapKd has priority over Kd); model_wavefrontobj.cpp:403-410 (the
+    // mixture's alpha mask: its mapKd texture when that has an alpha channel)
+    std::shared_ptr<const Texture<F>> mapKd, mask;
+
+    V3<F> kd_at(const PointGeometry<F>& g) const { return mapKd ? mapKd->eval(g.t) : Kd; }
+    F alpha_at(const PointGeometry<F>& g) const { return mask ? mask->eval_alpha(g.t) : F(1); }
 
     // material_glossy.cpp:43-59
     F normal_dist(V3<F> wh, V3<F> u, V3<F> v, V3<F> n) const {
@@ -232,10 +259,18 @@ template <typename F> struct Material {
         Fr = total ? F(1) : fresnel(wi, wt, g);
     }
 
-    bool is_specular_component(int) const { return type == MAT_GLASS || type == MAT_MIRROR; }
+    // the mixture's component 1 is the alpha mask's pass-through (model_wavefrontobj.cpp:513-515)
+    bool is_specular_component(int comp) const {
+        return type == MAT_GLASS || type == MAT_MIRROR || (type == MAT_MIXTURE && comp != 0);
+    }
 
-    // material_glass.cpp:143-158 (component sampling on); a single component elsewhere
+    // material_glass.cpp:143-158 (component sampling on); model_wavefrontobj.cpp:422-425 (alpha);
+    // a single component elsewhere
     F pdf_component(int comp, const PointGeometry<F>& g, V3<F> wi) const {
+        if (type == MAT_MIXTURE) {
+            const F a = alpha_at(g);
+            return comp == 0 ? a : F(1) - a;
+        }
         if (type != MAT_GLASS) return F(1);
         V3<F> wt; bool total; F eta, Fr;
         glass_refr(g, wi, wt, total, eta, Fr);
@@ -250,12 +285,19 @@ template <typename F> struct Material {
             const auto pdf = comp == 0 ? Fr : F(1) - Fr;
             return {comp, F(1) / pdf};
         }
+        if (type == MAT_MIXTURE) {  // model_wavefrontobj.cpp:413-420
+            const F a = alpha_at(g);
+            if (uc.x < a) return {0, F(1) / a};
+            return {1, F(1) / (F(1) - a)};
+        }
         return {0, F(1)};
     }
 
-    // model_wavefrontobj.cpp:427-435: probability of sampling the diffuse lobe
-    F diffuse_selection_prob() const {
-        const F wd = std::max(Kd.x, std::max(Kd.y, Kd.z)), wg = std::max(Ks.x, std::max(Ks.y, Ks.z));
+    // model_wavefrontobj.cpp:427-435: probability of sampling the diffuse lobe (the diffuse lobe's
+    // reflectance is its texel where it has a texture)
+    F diffuse_selection_prob(const PointGeometry<F>& g) const {
+        const auto kd = kd_at(g);
+        const F wd = std::max(kd.x, std::max(kd.y, kd.z)), wg = std::max(Ks.x, std::max(Ks.y, Ks.z));
         if (wd == F(0) && wg == F(0)) return F(1);
         return wd / (wd + wg);
     }
@@ -292,7 +334,7 @@ template <typename F> struct Material {
     std::optional<DirectionSample<F>> sample_direction(V2<F> ud, V2<F> udc, const PointGeometry<F>& g, V3<F> wi, int comp, TransDir td) const {
         switch (type) {
         case MAT_DIFFUSE:  // material_diffuse.cpp:63-71
-            return DirectionSample<F>{diffuse_dir(ud, g, wi), Kd};
+            return DirectionSample<F>{diffuse_dir(ud, g, wi), kd_at(g)};
         case MAT_GLOSSY: {  // material_glossy.cpp:70-86
             const auto wo = glossy_dir(ud, g, wi);
             if (!wo) return {};
@@ -300,9 +342,14 @@ template <typename F> struct Material {
             const auto p = pdf_direction(g, wi, *wo, 0, false);
             return DirectionSample<F>{*wo, f / p};
         }
-        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:437-461, component 0 (no alpha mask)
+        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:437-471
+            if (comp != 0) {
+                // the alpha mask's pass-through: the reference returns weight 1 (its f / p, computed
+                // beside it, is unused), so the path carries the component weight 1 / (1 - alpha)
+                return DirectionSample<F>{-wi, V3<F>(F(1))};
+            }
             V3<F> wo;
-            if (udc.x < diffuse_selection_prob()) {
+            if (udc.x < diffuse_selection_prob(g)) {
                 wo = diffuse_dir(ud, g, wi);
             } else {
                 const auto w = glossy_dir(ud, g, wi);
@@ -334,12 +381,13 @@ template <typename F> struct Material {
         return {};
     }
 
-    F pdf_direction(const PointGeometry<F>& g, V3<F> wi, V3<F> wo, int, bool eval_delta) const {
+    F pdf_direction(const PointGeometry<F>& g, V3<F> wi, V3<F> wo, int comp, bool eval_delta) const {
         switch (type) {
         case MAT_DIFFUSE: return g.opposite(wi, wo) ? F(0) : F(1) / C<F>::Pi;
         case MAT_GLOSSY: return glossy_pdf(g, wi, wo);
         case MAT_MIXTURE: {  // model_wavefrontobj.cpp:484-494
-            const F w = diffuse_selection_prob();
+            if (comp != 0) return eval_delta ? F(0) : F(1);
+            const F w = diffuse_selection_prob(g);
             const F pd = g.opposite(wi, wo) ? F(0) : F(1) / C<F>::Pi;
             return w * pd + (F(1) - w) * glossy_pdf(g, wi, wo);
         }
@@ -353,11 +401,13 @@ template <typename F> struct Material {
         switch (type) {
         case MAT_DIFFUSE:
             if (g.opposite(wi, wo)) return V3<F>();
-            return Kd / C<F>::Pi;
+            return kd_at(g) / C<F>::Pi;
         case MAT_GLOSSY: return glossy_eval(g, wi, wo);
-        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507, alpha = 1
-            const V3<F> fd = g.opposite(wi, wo) ? V3<F>() : Kd / C<F>::Pi;
-            return fd + glossy_eval(g, wi, wo);
+        case MAT_MIXTURE: {  // model_wavefrontobj.cpp:496-507
+            const F a = alpha_at(g);
+            if (comp != 0) return eval_delta ? V3<F>(F(0)) : V3<F>(F(1) - a);
+            const V3<F> fd = g.opposite(wi, wo) ? V3<F>() : kd_at(g) / C<F>::Pi;
+            return (fd + glossy_eval(g, wi, wo)) * a;
         }
         case MAT_GLASS: {
             if (eval_delta) return V3<F>(F(0));
@@ -373,11 +423,11 @@ template <typename F> struct Material {
         return V3<F>();
     }
 
-    std::optional<V3<F>> reflectance() const {
+    std::optional<V3<F>> reflectance(const PointGeometry<F>& g) const {
         switch (type) {
-        case MAT_DIFFUSE: return Kd;
+        case MAT_DIFFUSE: return kd_at(g);
         case MAT_GLOSSY: return Ks;
-        case MAT_MIXTURE: return Kd;
+        case MAT_MIXTURE: return kd_at(g);
         default: return V3<F>(F(0));
         }
     }
@@ -670,6 +720,7 @@ template <typename F> struct Scene {
     std::vector<SceneNode<F>> nodes;
     std::vector<Mesh<F>> meshes;
     std::vector<Material<F>> materials;
+    std::vector<std::shared_ptr<const Texture<F>>> textures;
     std::vector<Light<F>> lights_assets;
     std::vector<Camera<F>> cameras;
     std::optional<int> camera_;
@@ -1023,7 +1074,7 @@ void render_raycast(const Scene<F>& scene, int w, int h, V3<F> bg, bool use_cons
         else if (visualize_normal) c = vabs(sp->geom.n);
         else if (sp->geom.infinite) c = scene.light_of(sp->primitive).eval(sp->geom, sp->geom.wo);
         else {
-            const auto R = color ? std::optional<V3<F>>(*color) : scene.material_of(sp->primitive).reflectance();
+            const auto R = color ? std::optional<V3<F>>(*color) : scene.material_of(sp->primitive).reflectance(sp->geom);
             c = R ? *R : V3<F>();
             if (!use_constant_color) c *= F(.2) + F(.8) * std::abs(dot(sp->geom.n, -ray.d));
         }

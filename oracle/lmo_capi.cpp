@@ -29,6 +29,11 @@ int dispatch(Handle* h, Fn&& fn) {
     }
 }
 
+int fail(const char* msg) {
+    g_err = msg;
+    return -1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -56,7 +61,11 @@ int lmo_add_mesh(void* p, const float* ps, int nps, const float* ns, int nns, co
         for (int i = 0; i < nns; i++) m.ns.push_back(V3<F>(F(ns[3 * i]), F(ns[3 * i + 1]), F(ns[3 * i + 2])));
         for (int i = 0; i < nts; i++) m.ts.push_back(V2<F>(F(ts[2 * i]), F(ts[2 * i + 1])));
         if (m.ts.empty()) m.ts.push_back(V2<F>());
-        for (int i = 0; i < ncorners; i++) m.fs.push_back({fp[i], ft ? ft[i] : 0, fn[i]});
+        for (int i = 0; i < ncorners; i++) {
+            const int t = ft && nts > 0 ? ft[i] : 0;
+            if (t < 0 || t >= int(m.ts.size())) return fail("texture coordinate index out of range");
+            m.fs.push_back({fp[i], t, fn[i]});
+        }
         S.meshes.push_back(std::move(m));
         return int(S.meshes.size()) - 1;
     });
@@ -80,6 +89,35 @@ int lmo_add_material(void* p, int type, const double* prm) {
         }
         S.materials.push_back(m);
         return int(S.materials.size()) - 1;
+    });
+}
+
+// texture::bitmap (texture_bitmap.cpp:40-85): w x h texels of c (3 or 4) floats, row 0 at the bottom.
+int lmo_add_texture(void* p, const float* data, int w, int hgt, int c) {
+    auto* h = static_cast<Handle*>(p);
+    if (!data || w <= 0 || hgt <= 0 || (c != 3 && c != 4)) return fail("texture: invalid size or channel count");
+    return dispatch(h, [&](auto& S) -> int {
+        using F = typename std::decay_t<decltype(S)>::Float;
+        auto t = std::make_shared<Texture<F>>();
+        t->w = w; t->h = hgt; t->c = c;
+        t->data.assign(data, data + size_t(w) * hgt * c);
+        S.textures.push_back(t);
+        return int(S.textures.size()) - 1;
+    });
+}
+
+// material::diffuse's mapKd (and the mixture's diffuse lobe), and the mixture's alpha mask: texture
+// indices or -1.
+int lmo_set_material_textures(void* p, int mat, int mapKd, int mask) {
+    auto* h = static_cast<Handle*>(p);
+    return dispatch(h, [&](auto& S) -> int {
+        if (mat < 0 || mat >= int(S.materials.size())) return fail("material index out of range");
+        const int nt = int(S.textures.size());
+        if (mapKd >= nt || mask >= nt) return fail("texture index out of range");
+        if (mask >= 0 && !S.textures[mask]->has_alpha()) return fail("alpha mask texture without an alpha channel");
+        S.materials[mat].mapKd = mapKd >= 0 ? S.textures[mapKd] : nullptr;
+        S.materials[mat].mask = mask >= 0 ? S.textures[mask] : nullptr;
+        return 0;
     });
 }
 

@@ -308,6 +308,11 @@ template <typename F> inline V3<F> geometry_normal(V3<F> p1, V3<F> p2, V3<F> p3)
 template <typename F> inline V3<F> mix_barycentric(V3<F> a, V3<F> b, V3<F> c, V2<F> uv) {
     return a * (F(1) - uv.x - uv.y) + b * uv.x + c * uv.y;
 }
+// the same for texture coordinates (mesh_raw.cpp:97: math::mix_barycentric on Vec2)
+template <typename F> inline V2<F> mix_barycentric2(V2<F> a, V2<F> b, V2<F> c, V2<F> uv) {
+    const F w = F(1) - uv.x - uv.y;
+    return V2<F>(a.x * w + b.x * uv.x + c.x * uv.y, a.y * w + b.y * uv.x + c.y * uv.y);
+}
 template <typename F> inline V2<F> sample_uniform_disk(V2<F> u) {
     const auto r = safe_sqrt(u.x);
     const auto t = F(2) * C<F>::Pi * u.y;

@@ -39,6 +39,8 @@ def lib() -> C.CDLL:
         L.lmo_destroy.argtypes = [vp]
         L.lmo_add_mesh.argtypes = [vp, fp, C.c_int, fp, C.c_int, fp, C.c_int, ip, ip, ip, C.c_int]
         L.lmo_add_material.argtypes = [vp, C.c_int, dp]
+        L.lmo_add_texture.argtypes = [vp, fp, C.c_int, C.c_int, C.c_int]
+        L.lmo_set_material_textures.argtypes = [vp, C.c_int, C.c_int, C.c_int]
         L.lmo_add_light_area.argtypes = [vp, dp, C.c_int]
         L.lmo_add_light_envconst.argtypes = [vp, dp]
         L.lmo_add_light_point.argtypes = [vp, dp, dp]
@@ -116,6 +118,16 @@ class OracleScene:
         p = np.zeros(8)
         p[:len(params)] = params
         return _chk(lib().lmo_add_material(self.h, kind, _dp(p)))
+
+    def add_texture(self, data) -> int:
+        """texture::bitmap texels (h, w, 3 or 4), row 0 at the bottom."""
+        t = np.ascontiguousarray(data, np.float32)
+        self._keep.append(t)
+        h, w, c = t.shape
+        return _chk(lib().lmo_add_texture(self.h, t.ctypes.data_as(C.POINTER(C.c_float)), w, h, c))
+
+    def set_material_textures(self, mat: int, mapKd: int = -1, mask: int = -1) -> None:
+        _chk(lib().lmo_set_material_textures(self.h, mat, mapKd, mask))
 
     def add_area_light(self, Ke, mesh: int) -> int:
         return _chk(lib().lmo_add_light_area(self.h, _dp(Ke), mesh))
@@ -298,10 +310,21 @@ def from_lm_scene(scene, double: bool = True) -> OracleScene:
     O = OracleScene(double)
     mesh_id, mat_id, light_id, cam_id = {}, {}, {}, {}
 
+    tex_id = {}
+
     def mesh_of(m):
         if id(m) not in mesh_id:
-            mesh_id[id(m)] = O.add_mesh(m.ps, m.ns, m.fp, m.fn)
+            ts = getattr(m, "ts", None)
+            ft = getattr(m, "ft", None)
+            mesh_id[id(m)] = O.add_mesh(m.ps, m.ns, m.fp, m.fn, ts, ft)
         return mesh_id[id(m)]
+
+    def tex_of(t):
+        if t is None:
+            return -1
+        if id(t) not in tex_id:
+            tex_id[id(t)] = O.add_texture(t.texels())
+        return tex_id[id(t)]
 
     node_map = {0: 0}
     for i, n in enumerate(scene.nodes):
@@ -321,6 +344,9 @@ def from_lm_scene(scene, double: bool = True) -> OracleScene:
                 params = {0: lambda: list(m.Kd), 1: lambda: list(m.Ks) + [m.ax, m.ay], 2: lambda: [m.Ni], 3: lambda: [],
                           4: lambda: list(m.Kd) + list(m.Ks) + [m.ax, m.ay]}[k]()
                 mat_id[id(m)] = O.add_material(k, params)
+                mk, mm = tex_of(getattr(m, "mapKd", None)), tex_of(getattr(m, "mask", None))
+                if mk >= 0 or mm >= 0:
+                    O.set_material_textures(mat_id[id(m)], mk, mm)
             ma = mat_id[id(m)]
         li = -1
         if n["light"] is not None:

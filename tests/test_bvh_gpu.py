@@ -121,3 +121,20 @@ def test_gpu_builder_plain_drop_in_scene(lm):
         acc._release()
     for k in ("prim", "t", "u", "v"):
         assert np.array_equal(hits["sah"][k], hits["ploc"][k]), k
+
+
+def test_gpu_builder_instanced_same_hits(lm):
+    """Two-level trees whose bottom levels come from either builder give bit-identical hits."""
+    from lightmetrica import synthetic as syn
+    rays = syn.sphere_rays(100000, [0.0, 2.0, 0.0], seed=8)
+    hits = []
+    for b in ("sah", "ploc"):
+        scene, _, _ = syn.instanced_scene(n_instances=6, n_lat=10, n_lon=14, n_lights=2, w=16, h=12, env_w=16, env_h=8,
+                                          seed=11, spread=3.0, prefix=f"ib_{b}_")
+        scene._accel.builder = b
+        scene._accel.build(scene)
+        assert scene._accel.stats()["num_instances"] > 1
+        hits.append(scene._accel.intersect_batch(rays))
+    assert (hits[0]["prim"] >= 0).mean() > 0.05
+    for k in ("prim", "t", "u", "v"):
+        assert np.array_equal(hits[0][k], hits[1][k]), k

@@ -82,7 +82,7 @@ def test_tuning_keys(native_lib):
 
 
 _STRUCTS = {"Hit": "lmgpu_hit", "Instance": "lmgpu_instance", "AccelStats": "lmgpu_accel_stats", "Material": "lmgpu_material",
-            "Light": "lmgpu_light", "Camera": "lmgpu_camera", "SceneDesc": "lmgpu_scene_desc",
+            "Light": "lmgpu_light", "Camera": "lmgpu_camera", "SceneDesc": "lmgpu_scene_desc", "Texture": "lmgpu_texture",
             "RaycastParams": "lmgpu_raycast_params", "PTParams": "lmgpu_pt_params", "LTParams": "lmgpu_lt_params",
             "BDPTParams": "lmgpu_bdpt_params", "RenderStats": "lmgpu_render_stats"}
 

@@ -263,8 +263,10 @@ def test_material_proxy_and_constant_texture(lm, oracle_mod):
     with pytest.raises(lm.LmGpuError):
         lm.load_material("px1_bad", "proxy", ref="px1_tex")    # not a material
     bmp = lm.load_texture("px1_bmp", "bitmap", data=np.ones((2, 2, 3)))
+    img_mat = lm.load_material("px1_img", "diffuse", mapKd=bmp)   # an image texture, looked up per point
+    assert img_mat.mapKd is bmp and bmp.texels().shape == (2, 2, 3)
     with pytest.raises(lm.LmGpuError):
-        lm.load_material("px1_img", "diffuse", mapKd=bmp)     # image textures stay off the GPU path
+        lm.load_material("px1_notex", "diffuse", mapKd="px1_red_tex")  # a material is not a texture
 
 
 def test_asset_group_and_script_stubs(lm):
