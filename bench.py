@@ -394,6 +394,12 @@ def run_gpu(args) -> None:
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                         # what limits it: the counters (profiles/k_pt_extend_small.md) show issue slots
+                         # busy and node reads served by L2, not DRAM bandwidth
+                         "limiter": "instruction issue and latency; nodes and triangles L2-resident" if dom in (
+                             "extend", "shadow") else "dependent gathers (latency)",
+                         "frac_dram": (traffic * launches / (kern[dom] / 1e3) / 1e9 / peaks["hbm_gbs"]
+                                       if traffic else None),
                          "l2_peak_gbs": l2.value, "frac_l2": achieved / l2.value,
                          "traffic": traffic, "bytes_per_ray": {"extend": b_ext, "shadow": b_sh},
                          "launches": launches, **counts},
