@@ -205,6 +205,17 @@ class Request:
     spp_run: int = 0             # samples per pixel rendered (target requests stop early)
     target_time: float | None = None  # when the server read an estimate at or below `target`
     rounds: int = 0              # error checks of a target request
+    cancelled: bool = False      # RenderServer.cancel: stopped at the passes it had started
+    error: str | None = None     # why the request failed (its scene build raised or timed out)
+
+
+class RequestFailed(RuntimeError):
+    """A request the server cannot serve; it is recorded in RenderServer.failed with the reason."""
+
+
+class SceneBuildError(RequestFailed):
+    """A scene build for a request failed (make_scene raised, e.g. out of device memory) or did
+    not finish within the server's build_timeout."""
 
 
 class RenderServer:
@@ -246,6 +257,10 @@ class RenderServer:
         self.spp_first = 8                    # first error check of a target request
         self._pool = ThreadPoolExecutor(build_threads) if build_threads > 0 else None
         self._building: dict[Any, Any] = {}  # scene key -> future of (scene, build seconds)
+        self._build_started: dict[Any, float] = {}
+        self.build_timeout: float | None = None  # seconds a scene build may take before its requests fail
+        self.failed: list[Request] = []           # requests whose scene build failed
+        self.cancelled: list[Request] = []
         self._film_seq = 0
 
     # -- admission -------------------------------------------------------------------------------
@@ -285,6 +300,9 @@ class RenderServer:
             return False
         if req.refine is not None:
             base = self.by_id[req.refine]
+            if base.error is not None or base.cancelled:
+                raise RequestFailed(f"request {req.rid} refines request {base.rid}, which "
+                                    + ("failed" if base.error is not None else "was cancelled"))
             if base.done is None:
                 return False  # refine a finished image only
             if base.film is None:
@@ -347,17 +365,29 @@ class RenderServer:
 
     def _scene_ready(self, key):
         """(scene, build seconds) once the scene for `key` is built, else None (a build is started
-        on the worker threads, or runs here when there are none)."""
+        on the worker threads, or runs here when there are none). Raises SceneBuildError when the
+        build raised, or ran longer than build_timeout (the worker is then abandoned: a Python
+        thread cannot be stopped, its late result is dropped)."""
         if self._pool is None:
-            return self._build(key)
+            try:
+                return self._build(key)
+            except Exception as e:
+                raise SceneBuildError(f"scene {key!r}: {e}") from e
         fut = self._building.get(key)
         if fut is None:
             self._building[key] = self._pool.submit(self._build, key)
+            self._build_started[key] = self.clock()
             return None
         if not fut.done():
+            if self.build_timeout is not None and self.clock() - self._build_started[key] > self.build_timeout:
+                del self._building[key]
+                raise SceneBuildError(f"scene {key!r}: build did not finish within {self.build_timeout} s")
             return None
         del self._building[key]
-        return fut.result()
+        try:
+            return fut.result()
+        except Exception as e:
+            raise SceneBuildError(f"scene {key!r}: {e}") from e
 
     def close(self) -> None:
         if self._pool is not None:
@@ -370,7 +400,15 @@ class RenderServer:
         """Admits what fits, advances the wavefront one step, and records progress."""
         still = []
         for req in self.pending:
-            if not self._try_admit(req):
+            try:
+                admitted = self._try_admit(req)
+            except RequestFailed as e:
+                # the request fails; the others go on, and a later request for the key builds again
+                req.error = str(e)
+                req.done = self.clock()
+                self.failed.append(req)
+                continue
+            if not admitted:
                 still.append(req)
         self.pending = still
         if not self.inflight:
@@ -407,10 +445,28 @@ class RenderServer:
                     req.first_image = now
                 self.scene_users[req.scene_key] -= 1
                 self.scene_last_use[req.scene_key] = now
-                self.finished.append(req)
+                (self.cancelled if req.cancelled else self.finished).append(req)
             else:
                 remaining.append(req)
         self.inflight = remaining
+
+    def cancel(self, rid: int) -> bool:
+        """Cancels a request. Waiting: it is dropped. In flight: its job stops at the sample passes
+        it has already started (lmgpu_batch_job_set_spp; paths on the device are not aborted), and
+        it leaves the loop when those are done, apart from the finished requests. Returns False
+        for a request that has already finished or failed."""
+        req = self.by_id[rid]
+        if req.done is not None or req.cancelled:
+            return False
+        req.cancelled = True
+        if req in self.pending:
+            self.pending.remove(req)
+            req.done = self.clock()
+            self.cancelled.append(req)
+            return True
+        req.target = None
+        req.spp_run = self.batch.set_spp(req.job, 1)
+        return True
 
     def release(self, rid: int) -> None:
         """Frees a finished request's film (no later request may refine it)."""

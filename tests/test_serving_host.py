@@ -178,3 +178,93 @@ def test_target_requests_stop_at_the_error_and_report_measured_latency(server):
     lat = server.latencies()
     assert lat["target_requests"] == 2 and lat["reached_target"] == 0.5
     assert lat["time_to_target_p50"] == server.time_to_target(ok)
+
+
+def test_cancel_waiting_and_in_flight_requests(server):
+    """A waiting request is dropped; one in flight stops at the passes it has started and leaves
+    the loop apart from the finished requests (the reference's parallel loop stops on an
+    exception and rethrows it, parallel_openmp.cpp:41-99; here one request stops, the rest go on)."""
+    server.submit(_req(0, "A", spp=6))
+    server.submit(_req(1, "A", spp=6))
+    server.step()                      # both admitted, one pass each
+    server.submit(_req(2, "B", spp=3))
+    assert server.cancel(2)            # still waiting: dropped
+    assert server.cancel(0)            # in flight: stops at the started pass
+    while not server.idle():
+        server.step()
+    r0, r1, r2 = (server.by_id[i] for i in range(3))
+    assert r0.cancelled and r0.spp_run == 1 and r0 in server.cancelled
+    assert r2.cancelled and r2.job is None and r2 in server.cancelled
+    assert [r.rid for r in server.finished] == [1] and r1.spp_run == 6
+    assert server.latencies()["requests"] == 1
+    assert not server.cancel(1)        # already finished
+    assert server.scene_users["A"] == 0
+
+
+def test_failed_scene_build_fails_its_request_only(server, monkeypatch):
+    """A scene build that raises (here the fake allocator's out-of-memory on the second build)
+    fails the requests that needed it; the others are served, a refinement of a failed request
+    fails too, and a later request for the same scene builds it again."""
+    from lightmetrica import _native as N
+    calls = []
+    make = server.make_scene
+
+    def flaky(key):
+        calls.append(key)
+        if len(calls) == 2:
+            raise N.LmGpuError(5, "cudaMalloc: out of memory")
+        return make(key)
+    server.make_scene = flaky
+    server.submit(_req(0, "A", spp=2))
+    server.submit(_req(1, "B", spp=2))
+    server.submit(_req(2, "A", spp=1))
+    for _ in range(20):
+        server.step()
+    assert server.by_id[1].error and "out of memory" in server.by_id[1].error
+    assert [r.rid for r in server.failed] == [1]
+    assert sorted(r.rid for r in server.finished) == [0, 2]
+    server.submit(_req(3, "B", spp=2, refine=1))
+    server.submit(_req(4, "B", spp=2))
+    for _ in range(20):
+        server.step()
+    assert "refines request 1" in server.by_id[3].error
+    assert server.by_id[4].done is not None and server.by_id[4].error is None and calls.count("B") == 2
+
+
+def test_stuck_scene_build_times_out(monkeypatch):
+    """A build worker that never returns: its request fails after build_timeout seconds and the
+    server keeps serving; the worker's late result is dropped."""
+    import threading
+    from lightmetrica import serving
+    import lightmetrica as lm
+    monkeypatch.setattr(serving, "BatchRenderer", FakeBatch)
+    monkeypatch.setattr(serving, "scene_footprint", lambda s: s.nbytes)
+    monkeypatch.setattr(serving, "_release_scene", lambda s: None)
+    monkeypatch.setattr(lm, "load_film", lambda *a, **k: FakeFilm())
+    gate = threading.Event()
+    t = [0.0]
+
+    def clock():
+        t[0] += 0.05
+        return t[0]
+
+    def make(key):
+        if key == "stuck":
+            gate.wait(10.0)
+        return FakeScene(key, 100)
+    srv = serving.RenderServer(make, hbm_budget=10**6, clock=clock, build_threads=2)
+    srv.track_error = False
+    srv.build_timeout = 1.0
+    srv.submit(_req(0, "stuck", spp=2))
+    srv.submit(_req(1, "ok", spp=2))
+    for _ in range(400):
+        if srv.idle():
+            break
+        srv.step()
+        import time
+        time.sleep(0.001)
+    assert srv.idle()
+    assert "did not finish within 1.0 s" in srv.by_id[0].error
+    assert srv.by_id[1].done is not None and srv.by_id[1].error is None
+    gate.set()
+    srv.close()
