@@ -448,15 +448,26 @@ def _batched_scenes(lm, n_jobs: int):
 
 
 def run_batched(lm, args) -> tuple[dict, dict]:
-    """Plain job-by-job renderer::pt vs the shared wavefront on the batched workload."""
+    """Plain job-by-job renderer::pt vs the shared wavefront on the batched workload, after the
+    autotuner has chosen queue size, launch shape, shade-kernel split and node width on a 32-job
+    probe (both forms then run with its choices)."""
     import numpy as np
-    from lightmetrica.autotune import tune_queue
+    from lightmetrica.autotune import tune
     from lightmetrica.serving import BatchRenderer
     jobs, scenes, build_s = _batched_scenes(lm, args.batched_jobs)
     paths = sum(j["res"] ** 2 * j["spp"] for j in jobs)
-    # warm-up of both forms
     s0, f0 = scenes[0]
     lm.load_renderer("batch_warm", "pt", scene=s0, output=f0, max_verts=7, seed=1, spp=2, scheduler="sample").render()
+    probe_films = [lm.load_film(f"batch_probe{i}", "bitmap", w=j["res"], h=j["res"]) for i, j in enumerate(jobs[:32])]
+    probe = [dict(scene=s, film=f2, max_verts=j["max_verts"], spp=j["spp"], seed=j["seed"])
+             for j, (s, _), f2 in zip(jobs, scenes, probe_films)]
+    t = time.perf_counter()
+    chosen, tune_times = tune(probe, rebuild=lambda: [s.build() for s, _ in scenes[:len(probe)]])
+    tune_s = time.perf_counter() - t
+    if chosen.get("node_width", 8) != 8:
+        for s, _ in scenes[len(probe):]:
+            s.build()
+    queue = chosen["queue_paths"]
     # plain: one renderer::pt per job, in order
     t = time.perf_counter()
     plain_rays = 0
@@ -469,7 +480,6 @@ def run_batched(lm, args) -> tuple[dict, dict]:
     films = [lm.load_film(f"batch_out{i}", "bitmap", w=j["res"], h=j["res"]) for i, j in enumerate(jobs)]
     spec = [dict(scene=s, film=f2, max_verts=j["max_verts"], spp=j["spp"], seed=j["seed"])
             for j, (s, _), f2 in zip(jobs, scenes, films)]
-    queue, tune = tune_queue(spec[: min(32, len(spec))])
     b = BatchRenderer(queue_paths=queue)
     b.submit(s0, films[0], max_verts=7, spp=1, seed=0)
     b.run(0)
@@ -490,7 +500,9 @@ def run_batched(lm, args) -> tuple[dict, dict]:
         "batched": {"jobs_per_s": len(jobs) / batch_s, "seconds": batch_s, "Mrays_per_s": st["rays"] / batch_s / 1e6,
                     "device_ms": st["device_ms"], "queue_paths": queue},
         "speedup": plain_s / batch_s,
-        "autotune_seconds": {str(k): v for k, v in tune.items()},
+        "autotune": {"chosen": chosen, "seconds_per_candidate": {k: {str(c): v for c, v in d.items()}
+                                                                 for k, d in tune_times.items()},
+                     "tuning_seconds": tune_s, "probe": f"the first {len(probe)} jobs, wall clock per render"},
         "max_rel_image_diff": diff,
         "timing": "wall clock around all jobs (host overhead included); scene builds excluded",
         "scene_build_seconds": build_s,

@@ -66,6 +66,10 @@ int lmgpu_version(void);
  *   "batch_first_pass" shared wavefront: start the sample-0 paths of every job before any other
  *                   path (1, the default: a newly admitted job's first image does not wait behind
  *                   older jobs' later samples) or start paths in submission order (0).
+ *   "node_width"     BVH builds (both builders): children per node the collapse may use (2..8,
+ *                   default 8; the 80-byte node keeps 8 slots, a narrower tree leaves some empty).
+ *   "shade_specialize" path-tracing shade kernels: 1 (default) runs the kernel specialised for the
+ *                   scene's features, 0 the full-feature kernel.
  * Tuning changes speed only, never results. Process-wide; set it between renders. */
 int lmgpu_tune_set(const char* key, int64_t value);
 int lmgpu_tune_get(const char* key, int64_t* value);

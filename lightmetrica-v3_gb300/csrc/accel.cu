@@ -34,6 +34,13 @@ Tuning& tuning() {
     return t;
 }
 
+// The builders' options from the process-wide tuning (node width).
+BuildOptions tuned_build_options() {
+    BuildOptions o;
+    o.max_width = tuning().node_width;
+    return o;
+}
+
 std::shared_mutex& capture_mutex() {
     static std::shared_mutex m;
     return m;
@@ -225,6 +232,12 @@ int lmgpu_tune_set(const char* key, int64_t value) {
         } else if (k == "shade_minblocks") {
             if (value < 2 || value > 4) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "shade_minblocks must be 2, 3 or 4");
             tuning().shade_minblocks = int(value);
+        } else if (k == "node_width") {
+            if (value < 2 || value > 8) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "node_width must be in [2, 8]");
+            tuning().node_width = int(value);
+        } else if (k == "shade_specialize") {
+            if (value != 0 && value != 1) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "shade_specialize must be 0 or 1");
+            tuning().shade_specialize = int(value);
         } else {
             throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
         }
@@ -238,6 +251,8 @@ int lmgpu_tune_get(const char* key, int64_t* value) {
         if (k == "trace_refill") *value = tuning().trace_refill;
         else if (k == "shade_minblocks") *value = tuning().shade_minblocks;
         else if (k == "batch_first_pass") *value = tuning().batch_first_pass;
+        else if (k == "node_width") *value = tuning().node_width;
+        else if (k == "shade_specialize") *value = tuning().shade_specialize;
         else throw Error(LMGPU_ERR_INVALID_ARGUMENT, "unknown tuning key: " + k);
     });
 }
@@ -291,7 +306,7 @@ int lmgpu_accel_build_ex(lmgpu_accel* accel, const float* tri_p, int64_t num_tri
         } else {
         Bvh8Host h;
         std::string err;
-        if (!build_bvh8(tri_p, num_tris, h, &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+        if (!build_bvh8(tri_p, num_tris, h, &err, tuned_build_options())) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
         accel->nodes.upload(h.nodes.data(), h.nodes.size());
         accel->tris.upload(h.tris.data(), h.tris.size());
         {
@@ -370,7 +385,8 @@ int lmgpu_accel_build_instanced_ex(lmgpu_accel* accel, const float* tri_p, const
                 bl[b].sah_cost = sah;
             } else {
                 std::string err;
-                if (!build_bvh8(tri_p + 9 * off, cnt, bl[b], &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+                if (!build_bvh8(tri_p + 9 * off, cnt, bl[b], &err, tuned_build_options()))
+                    throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
             }
             std::array<double, 6> bx{1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
             for (int64_t i = 9 * off; i < 9 * (off + cnt); i += 3)
@@ -539,7 +555,7 @@ int lmgpu_bvh8_build_host(const float* tri_p, int64_t num_tris, uint32_t* nodes,
         if (!tri_p || !nodes || !tris || !num_nodes || !max_depth) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "null argument");
         Bvh8Host h;
         std::string err;
-        if (!build_bvh8(tri_p, num_tris, h, &err)) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
+        if (!build_bvh8(tri_p, num_tris, h, &err, tuned_build_options())) throw Error(LMGPU_ERR_INVALID_ARGUMENT, err);
         if (h.nodes.size() > size_t(20) * size_t(num_tris > 0 ? num_tris : 1))
             throw Error(LMGPU_ERR_INTERNAL, "node count above the documented bound");
         std::memcpy(nodes, h.nodes.data(), h.nodes.size() * 4);

@@ -244,6 +244,7 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err, 
     //          (A * c_node + the best split of its two children over 8 slots);
     //   i > 1: the i-1 option, or the subtree's two children placed directly with k and i-k slots.
     constexpr float kCNode = 1.0f, kCPrim = 0.3f;
+    const int W = opt.leaf_nodes ? 8 : std::min(8, std::max(2, opt.max_width));
     const float inf = std::numeric_limits<float>::infinity();
     std::vector<float> cost(size_t(nb) * 8);
     std::vector<int8_t> dec(size_t(nb) * 8);  // i=1: 0 leaf / 1 node; i>1: 0 = as i-1, k = split
@@ -271,10 +272,10 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err, 
                 if (v < dist[j]) { dist[j] = v; dk[j] = int8_t(k); }
             }
         }
-        const float cnode = A * kCNode + dist[8];
+        const float cnode = A * kCNode + dist[W];
         c[0] = std::min(cleaf, cnode);
         d[0] = cleaf <= cnode ? 0 : 1;
-        dnode[ni] = dk[8];
+        dnode[ni] = dk[W];
         for (int i = 2; i <= 8; i++) {
             if (c[i - 2] <= dist[i]) { c[i - 1] = c[i - 2]; d[i - 1] = 0; }
             else { c[i - 1] = dist[i]; d[i - 1] = dk[i]; }
@@ -316,7 +317,7 @@ bool build_bvh8(const float* tri_p, int64_t n, Bvh8Host& out, std::string* err, 
             kids.push_back({pd.bin, true});  // the whole tree is one leaf
         } else {
             emit(root.left, dnode[pd.bin], kids);
-            emit(root.right, 8 - dnode[pd.bin], kids);
+            emit(root.right, W - dnode[pd.bin], kids);
         }
         const int nch = int(kids.size());
         if (nch < 1 || nch > 8) {

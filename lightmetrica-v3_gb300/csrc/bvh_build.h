@@ -44,6 +44,9 @@ constexpr uint32_t kInstanceMarker = 0xFFu;
 
 struct BuildOptions {
     bool leaf_nodes = false;  // top-level mode (see above); tris stays empty
+    // children per node the collapse may use (2..8): the node layout keeps 8 slots, a narrower
+    // tree leaves the rest empty (the autotuner compares widths)
+    int max_width = 8;
 };
 
 // tri_p: n x 9 floats (p1, p2, p3); in top-level mode each "triangle" is (lo, hi, lo) of one

@@ -139,7 +139,8 @@ __global__ void k_morton(const float4* __restrict__ cen, int64_t n, const uint32
 }
 
 // Collapse cost of node `id` from its children's (their costs are final).
-__device__ void collapse_cost(const Nodes& N, int32_t id, int32_t l, int32_t r, float4 lo, float4 hi, int32_t count) {
+__device__ void collapse_cost(const Nodes& N, int32_t id, int32_t l, int32_t r, float4 lo, float4 hi, int32_t count,
+                              int W) {
     const float A = box_area(lo, hi);
     const float cleaf = count <= kMaxLeaf ? A * kCPrim * float(count) : INFINITY;
     float* c = N.cost + size_t(id) * 8;
@@ -161,11 +162,11 @@ __device__ void collapse_cost(const Nodes& N, int32_t id, int32_t l, int32_t r, 
             if (v < dist[j]) { dist[j] = v; dk[j] = int8_t(k); }
         }
     }
-    const float cnode = A * kCNode + dist[8];
+    const float cnode = A * kCNode + dist[W];
     float c0 = fminf(cleaf, cnode);
     c[0] = c0;
     d[0] = cleaf <= cnode ? 0 : 1;
-    N.dnode[id] = dk[8];
+    N.dnode[id] = dk[W];
     float prev = c0;
     for (int i = 2; i <= 8; i++) {
         if (prev <= dist[i]) { c[i - 1] = prev; d[i - 1] = 0; }
@@ -184,7 +185,7 @@ __global__ void k_leaves(const int32_t* __restrict__ vals, int64_t n, const floa
         N.left[k] = -1;
         N.right[k] = t;
         N.count[k] = 1;
-        collapse_cost(N, int32_t(k), -1, -1, lo, hi, 1);
+        collapse_cost(N, int32_t(k), -1, -1, lo, hi, 1, 8);
         clusters[k] = int32_t(k);
     }
 }
@@ -238,7 +239,7 @@ __global__ void k_merge_flags(const int32_t* __restrict__ nn, int32_t m, unsigne
 
 __global__ void k_merge(const int32_t* __restrict__ cin, int32_t m, const int32_t* __restrict__ nn,
                         const unsigned long long* __restrict__ flags, const unsigned long long* __restrict__ scan,
-                        int32_t next_id, Nodes N, int32_t* __restrict__ cout, unsigned long long* totals) {
+                        int32_t next_id, Nodes N, int32_t* __restrict__ cout, unsigned long long* totals, int W) {
     const int32_t i = int32_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= m) return;
     const unsigned long long f = flags[i], s = scan[i];
@@ -257,7 +258,7 @@ __global__ void k_merge(const int32_t* __restrict__ cin, int32_t m, const int32_
         N.left[id] = a;
         N.right[id] = b;
         N.count[id] = cnt;
-        collapse_cost(N, id, a, b, lo, hi, cnt);
+        collapse_cost(N, id, a, b, lo, hi, cnt, W);
         cout[slot] = id;
     } else {
         cout[slot] = cin[i];
@@ -278,6 +279,7 @@ struct Emit {
     int32_t root;
     int32_t wide_cap;
     int* err;
+    int width;               // children per node (2..8)
 };
 
 __device__ inline uint32_t fbits(float f) { return __float_as_uint(f); }
@@ -337,7 +339,7 @@ __global__ void k_emit(Emit E, int32_t w0, int32_t w1) {
         int si[16];
         int sp = 0;
         const int k0 = N.dnode[bin];
-        sm[sp] = N.right[bin]; si[sp++] = 8 - k0;
+        sm[sp] = N.right[bin]; si[sp++] = E.width - k0;
         sm[sp] = N.left[bin]; si[sp++] = k0;
         while (sp > 0) {
             const int32_t m = sm[--sp];
@@ -484,6 +486,7 @@ void build_bvh8_gpu(const float* tri_p, int64_t n, DevBuf& nodes, DevBuf& tris, 
     if (n <= 0) throw Error(LMGPU_ERR_INVALID_ARGUMENT, "accel build: no triangles");
     if (n > (int64_t(1) << 30)) throw Error(LMGPU_ERR_UNSUPPORTED, "accel build: more than 2^30 triangles on the GPU builder");
     const size_t nn = size_t(2) * size_t(n);
+    const int width = std::min(8, std::max(2, tuning().node_width));
     DevBuf P, tlo, thi, cen, cb, err, keys[2], vals[2], blo, bhi, bl, br, bc, cost, dec, dnode, cl[2], nnb, flags, scan,
         totals, q, wide_count, tri_count, tmp;
     P.alloc(size_t(n) * 36);
@@ -538,7 +541,7 @@ void build_bvh8_gpu(const float* tri_p, int64_t n, DevBuf& nodes, DevBuf& tris, 
                                                  m, st));
         k_merge<<<gm, kBlock, 0, st>>>(cl[cur].as<int32_t>(), m, nnb.as<int32_t>(), flags.as<unsigned long long>(),
                                        scan.as<unsigned long long>(), next_id, N, cl[1 - cur].as<int32_t>(),
-                                       totals.as<unsigned long long>());
+                                       totals.as<unsigned long long>(), width);
         LMGPU_CUDA(cudaGetLastError());
         unsigned long long tot = 0;
         LMGPU_CUDA(cudaMemcpyAsync(&tot, totals.p, 8, cudaMemcpyDeviceToHost, st));
@@ -577,7 +580,7 @@ void build_bvh8_gpu(const float* tri_p, int64_t n, DevBuf& nodes, DevBuf& tris, 
     LMGPU_CUDA(cudaMemcpyAsync(wide_count.p, &one, 4, cudaMemcpyHostToDevice, st));
     LMGPU_CUDA(cudaMemsetAsync(tri_count.p, 0, 4, st));
     Emit E{N, P.as<float>(), nodes.as<uint32_t>(), tris.as<float4>(), tri_slot.as<int32_t>(), q.as<int32_t>(),
-           wide_count.as<int32_t>(), tri_count.as<int32_t>(), root, cap, err.as<int>()};
+           wide_count.as<int32_t>(), tri_count.as<int32_t>(), root, cap, err.as<int>(), width};
     int32_t w0 = 0, w1 = 1, levels = 0;
     while (w0 < w1) {
         k_emit<<<int((w1 - w0 + 127) / 128), 128, 0, st>>>(E, w0, w1);

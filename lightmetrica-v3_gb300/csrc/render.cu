@@ -3221,7 +3221,7 @@ struct lmgpu_batch {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         int32_t depth = 0;
-        int refill = -1, shade = -1, first_pass = -1;
+        int refill = -1, shade = -1, first_pass = -1, specialize = -1;
         bool two_level = false;
         bool single = false;      // captured for a one-job table
         uint32_t feat = 0;        // that job's scene features (the shade kernel specialised for them)
@@ -3235,7 +3235,7 @@ struct lmgpu_batch {
             graph = nullptr;
         }
     } slot[2];
-    int refill = 0, shade_minblocks = 3, first_pass = 1;
+    int refill = 0, shade_minblocks = 3, first_pass = 1, specialize = 1;
     bool two_level = false;  // some job's scene is instanced
     bool timed = false;      // per-kernel device time (lmgpu_batch_set_timing)
     cudaEvent_t ev[6 * 8] = {};
@@ -3315,8 +3315,8 @@ WfShadeK wf_shade_single(uint32_t feat) {
 // feat: the job's features (one job) or the union over the table's jobs. Several jobs: a kernel
 // without the textured environment and the mixture when no job has them.
 WfShadeK wf_shade_kernel(const lmgpu_batch* b, bool single, uint32_t feat) {
-    if (single && b->shade_minblocks >= 4) return wf_shade_single(feat);
-    if (!single && b->shade_minblocks >= 4 && (feat & ~kFeatTwoLevel) == 0u)
+    if (single && b->shade_minblocks >= 4 && b->specialize) return wf_shade_single(feat);
+    if (!single && b->shade_minblocks >= 4 && b->specialize && (feat & ~kFeatTwoLevel) == 0u)
         return (feat & kFeatTwoLevel) ? k_wf_shade<4, false, kFeatTwoLevel> : k_wf_shade<4, false, 0u>;
     return single ? pick_shade(k_wf_shade<2, true>, k_wf_shade<3, true>, k_wf_shade<4, true>, b->shade_minblocks)
                   : pick_shade(k_wf_shade<2, false>, k_wf_shade<3, false>, k_wf_shade<4, false>, b->shade_minblocks);
@@ -3398,6 +3398,7 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     b->refill = tuning().trace_refill;
     b->shade_minblocks = tuning().shade_minblocks;
     b->first_pass = tuning().batch_first_pass;
+    b->specialize = tuning().shade_specialize;
     if (realloc) {
         b->slot[0].clear();
         b->slot[1].clear();
@@ -3407,7 +3408,7 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     const uint32_t feat = table_features(b);
     const bool same_shape = g.exec && g.depth == b->max_depth && g.refill == b->refill && g.shade == b->shade_minblocks &&
                             g.two_level == b->two_level && g.first_pass == b->first_pass && g.single == single &&
-                            g.feat == feat;
+                            g.feat == feat && g.specialize == b->specialize;
     auto same_job = [&] {
         const JobDev& J = b->host_jobs[0];
         return std::memcmp(&g.bvh, &J.S.bvh, sizeof(Bvh8)) == 0 && g.film == J.film && g.film_odd == J.film_odd;
@@ -3469,6 +3470,7 @@ cudaGraphExec_t ensure_graph(lmgpu_batch* b, bool realloc) {
     g.two_level = b->two_level;
     g.first_pass = b->first_pass;
     g.shade = b->shade_minblocks;
+    g.specialize = b->specialize;
     g.single = single;
     g.feat = feat;
     if (single) {

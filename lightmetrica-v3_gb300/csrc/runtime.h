@@ -115,6 +115,10 @@ struct Tuning {
     // Shared wavefront: start every job's sample-0 paths before other paths (1) or start paths
     // strictly in submission order (0).
     int batch_first_pass = 1;
+    // BVH builds: children per node the 8-wide collapse may use (2..8; the layout keeps 8 slots)
+    int node_width = 8;
+    // Shade kernels: 1 = the kernel specialised for the scene's features, 0 = the full-feature one
+    int shade_specialize = 1;
 };
 Tuning& tuning();
 

@@ -146,3 +146,34 @@ def test_axis_aligned_rays_stay_cheap(native_lib):
             ray = np.array([*o, 1e-3, *d, 1e10], np.float32)
             t, u, v, tid, visited = sim.trace(nodes, tris, depth, ray)
             assert visited <= 4 * depth + 16, (d, visited, len(nodes))
+
+
+@pytest.mark.parametrize("width", [2, 4, 6])
+def test_narrower_trees(native_lib, oracle_mod, width):
+    """The "node_width" tuning key: the collapse uses at most `width` of a node's 8 slots; the
+    layout's invariants hold and the traversal (replayed in Python) still returns the exhaustive
+    closest hit."""
+    from lightmetrica import _native as N
+    N.check(native_lib.lmgpu_tune_set(b"node_width", width))
+    try:
+        tri_p = _soup(600, 21)
+        nodes, tris, depth = sim.build_host(native_lib, tri_p)
+    finally:
+        N.check(native_lib.lmgpu_tune_set(b"node_width", 8))
+    used = [sum(1 for m in sim.decode(w)["meta"] if m) for w in nodes]
+    assert max(used) <= width and max(used) == width
+    _check_structure(nodes, tris, tri_p)
+    S = oracle_mod.OracleScene(False)
+    n = len(tri_p)
+    m = S.add_mesh(tri_p.reshape(-1, 3), [[0, 0, 1]], np.arange(3 * n, dtype=np.int32), np.zeros(3 * n, np.int32))
+    S.add_child(0, S.primitive(m, S.add_material(0, [1, 1, 1])))
+    S.build(robust=True)
+    rays = _rays(150, 12)
+    t_ref, _, id_ref, _ = S.intersect(rays, brute=True)
+    for i, r in enumerate(rays):
+        t, u, v, tid, _ = sim.trace(nodes, tris, depth, r)
+        assert tid == id_ref[i]
+        if tid >= 0:
+            assert np.float32(t) == np.float32(t_ref[i])
+    with pytest.raises(Exception):
+        N.check(native_lib.lmgpu_tune_set(b"node_width", 9))
