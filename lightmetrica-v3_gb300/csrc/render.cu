@@ -1145,19 +1145,6 @@ __device__ __forceinline__ bool shade_path(const DevScene& S, const PtConst& P, 
     return true;
 }
 
-// The shading record of the hit in queue slot k, prefetched into L2: its address depends on the
-// hit, so without this the shade kernels wait on one dependent gather per path (the records of a
-// large scene are mostly not in L2). One-level trees only: a two-level record needs the instance
-// lookup first.
-__device__ __forceinline__ void prefetch_record(const DevScene& S, const float4* hits, int k) {
-    if (S.num_inst > 0) return;
-    const int32_t id = __ldg(reinterpret_cast<const int32_t*>(hits + k) + 3);
-    if (id < 0) return;
-    const char* p = reinterpret_cast<const char*>(S.shade + size_t(id) * 6);
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 95));
-}
-
 // kMinBlocks: resident 256-thread blocks per SM the register allocation must allow (2: up to 128
 // registers; 3: 80; 4: 64), selected at run time by the "shade_minblocks" tuning key.
 template <int kMinBlocks>
@@ -1756,10 +1743,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_wf_shade(const JobDev* _
                                                      const int* __restrict__ qicount, ExtQ qo, int* qocount, ShadowQ sq,
                                                      int* scount, unsigned int* pass_done) {
     const int n = *qicount;
-    const int stride = gridDim.x * blockDim.x;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
-        // the next iteration's shading record starts on its way to L2 while this one shades
-        if (k + stride < n) prefetch_record(jobs[kSingle ? 0u : qi.job[k + stride]].S, hits, k + stride);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         // kSingle: the batch holds one job, so no per-path job id is read
         const uint32_t job = kSingle ? 0u : qi.job[k];
         const JobDev& J = jobs[job];
