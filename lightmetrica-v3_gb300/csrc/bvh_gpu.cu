@@ -36,10 +36,11 @@ namespace lmgpu {
 namespace gpubuild {
 
 constexpr int kMaxLeaf = 3;      // triangles per leaf child (3 bits of meta hold the count)
-// PLOC neighbourhood: kRadius clusters on either side. Measured on the 3.8M-triangle headline
-// scene (trace speed of the resulting tree, SAH cost): 8 -> 2,586 Mrays/s, 8.83; 16 -> 2,497,
-// 8.94; 32 -> 2,540, 9.14.
-constexpr int kRadius = 8;
+// PLOC neighbourhood: kRadius clusters on either side. Trace speed of the resulting trees on
+// the 3.8M-triangle headline scene (64 spp, Mrays/s; the host SAH builder's tree: 2,680):
+// radius 4 -> 2,594, 6 -> 2,684, 8 -> 2,636, 16 -> 2,497, 32 -> 2,540. On random-triangle soups of
+// 1.5k-160k triangles every radius from 4 to 8 stays within 1-7 % of the host builder's trees.
+constexpr int kRadius = 6;
 constexpr int kBlock = 256;
 constexpr float kCNode = 1.0f, kCPrim = 0.3f;
 
