@@ -262,6 +262,11 @@ def run_gpu(args) -> None:
     scene.build()
     build_s = time.perf_counter() - t0
     acc = scene.accel().stats()
+    # the same triangles through the GPU builder (timed apart; the frame renders on the host tree)
+    gpu_acc = lm.load_accel("bench_ploc_accel", "sahbvh", builder="ploc")
+    gpu_acc.build_triangles(scene.flattened()["positions"])
+    gpu_build = gpu_acc.stats()
+    gpu_acc._release()
     L = N.lib()
 
     def params(spp, seed, instrument=0):
@@ -408,7 +413,9 @@ def run_gpu(args) -> None:
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clocks,
             "accel": {"nodes": acc["num_nodes"], "depth": acc["max_depth"], "build_seconds": acc["build_seconds"],
-                      "scene_build_seconds": build_s, "sah_cost": acc["sah_cost"]},
+                      "scene_build_seconds": build_s, "sah_cost": acc["sah_cost"], "builder": "host SAH",
+                      "gpu_builder": {"build_seconds": gpu_build["build_seconds"], "nodes": gpu_build["num_nodes"],
+                                      "depth": gpu_build["max_depth"], "sah_cost": gpu_build["sah_cost"]}},
         }
         if not args.no_batched:
             out["batched"], ctx = run_batched(lm, args)
@@ -440,10 +447,17 @@ def _batched_scenes(lm, n_jobs: int):
     jobs = syn.batch_jobs(n_jobs)
     scenes = []
     t = time.perf_counter()
+    accel_s = {"sah": 0.0, "ploc": 0.0}
     for i, j in enumerate(jobs):
         s, f = syn.triangles_scene(j["scene_seed"], j["tris"], j["res"], j["res"], prefix=f"batch{i}_")
         s.build()
+        accel_s["sah"] += s.accel().stats()["build_seconds"]
+        g = lm.load_accel(f"batch{i}_ploc", "sahbvh", builder="ploc")
+        g.build_triangles(s.flattened()["positions"])
+        accel_s["ploc"] += g.stats()["build_seconds"]
+        g._release()
         scenes.append((s, f))
+    _batched_scenes.accel_seconds = accel_s
     return jobs, scenes, time.perf_counter() - t
 
 
@@ -506,6 +520,9 @@ def run_batched(lm, args) -> tuple[dict, dict]:
         "max_rel_image_diff": diff,
         "timing": "wall clock around all jobs (host overhead included); scene builds excluded",
         "scene_build_seconds": build_s,
+        "accel_build_seconds": {"host_sah": _batched_scenes.accel_seconds["sah"],
+                                "gpu_ploc": _batched_scenes.accel_seconds["ploc"],
+                                "note": "all 256 scenes' trees (the timed renders use the host builder's)"},
     }
     return out, {"jobs": jobs, "scenes": scenes, "queue": queue, "capacity": len(jobs) / batch_s,
                  "paths_per_s": paths / batch_s}
