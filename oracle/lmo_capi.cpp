@@ -361,6 +361,165 @@ float lmo_philox_uniform(unsigned int seed, unsigned long long path, unsigned in
 
 int lmo_max_threads() { return omp_get_max_threads(); }
 
+// The restated math.h helpers in double precision over n records, with the same record layout as
+// the reference library's lmref_math_eval, so that tests can compare the two bit for bit.
+int lmo_math_eval(const char* fn, const double* in, long long n, double* out) {
+    using V = V3<double>;
+    auto v3 = [](const double* p) { return V(p[0], p[1], p[2]); };
+    auto put3 = [](double* o, V v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; };
+    const std::string f(fn);
+    for (long long i = 0; i < n; i++) {
+        if (f == "reflection") {
+            const double* a = in + 6 * i;
+            put3(out + 3 * i, reflection(v3(a), v3(a + 3)));
+        } else if (f == "refraction") {
+            const double* a = in + 7 * i;
+            const auto r = refraction(v3(a), v3(a + 3), a[6]);
+            put3(out + 4 * i, r.wt);
+            out[4 * i + 3] = r.total ? 1 : 0;
+        } else if (f == "orthonormal_basis") {
+            V u, v;
+            orthonormal_basis(v3(in + 3 * i), u, v);
+            put3(out + 6 * i, u);
+            put3(out + 6 * i + 3, v);
+        } else if (f == "geometry_normal") {
+            const double* a = in + 9 * i;
+            put3(out + 3 * i, geometry_normal(v3(a), v3(a + 3), v3(a + 6)));
+        } else if (f == "sample_uniform_disk") {
+            const auto d = sample_uniform_disk(V2<double>(in[2 * i], in[2 * i + 1]));
+            out[2 * i] = d.x; out[2 * i + 1] = d.y;
+        } else if (f == "sample_cosine_weighted") {
+            put3(out + 3 * i, sample_cosine_weighted(V2<double>(in[2 * i], in[2 * i + 1])));
+        } else if (f == "sample_uniform_sphere") {
+            put3(out + 3 * i, sample_uniform_sphere(V2<double>(in[2 * i], in[2 * i + 1])));
+        } else if (f == "balance_heuristic") {
+            out[i] = balance_heuristic(in[2 * i], in[2 * i + 1]);
+        } else if (f == "safe_sqrt") {
+            out[i] = safe_sqrt(in[i]);
+        } else if (f == "transform_J") {
+            out[i] = Transform<double>(M4<double>::from_colmajor(in + 16 * i)).J;
+        } else if (f == "bound_isect") {
+            const double* a = in + 14 * i;
+            Bound<double> b;
+            b.min = v3(a);
+            b.max = v3(a + 3);
+            const Ray<double> r{v3(a + 6), v3(a + 9)};
+            // Bound::isect with the range it narrowed (math.h:143-158 isect_range)
+            double tmin = a[12], tmax = a[13];
+            bool hit = true;
+            for (int k = 0; k < 3 && hit; k++) {
+                const double vd = 1.0 / r.d[k];
+                double t1 = (b.min[k] - r.o[k]) * vd, t2 = (b.max[k] - r.o[k]) * vd;
+                if (vd < 0) std::swap(t1, t2);
+                tmin = t1 < tmin ? tmin : t1;
+                tmax = tmax < t2 ? tmax : t2;
+                if (tmax < tmin) hit = false;
+            }
+            if (hit != b.isect(r, a[12], a[13], false)) return fail("isect and isect_range disagree");
+            out[3 * i] = hit ? 1 : 0; out[3 * i + 1] = tmin; out[3 * i + 2] = tmax;
+        } else {
+            return fail("unknown function");
+        }
+    }
+    return 0;
+}
+
+int lmo_dist2_eval(const double* v, int cols, int rows, long long n, const double* uvq, const double* u4,
+                   double* pdf_out, double* sample_out) {
+    Dist2<double> d;
+    d.init(std::vector<double>(v, v + size_t(cols) * rows), cols, rows);
+    for (long long i = 0; i < n; i++) {
+        pdf_out[i] = d.pdf(uvq[2 * i], uvq[2 * i + 1]);
+        const auto s = d.sample(u4[4 * i], u4[4 * i + 1], u4[4 * i + 2], u4[4 * i + 3]);
+        sample_out[2 * i] = s.x; sample_out[2 * i + 1] = s.y;
+    }
+    return 0;
+}
+
+// Every Material query of the restated material `type` (parameters as lmo_add_material) in double,
+// over n records with the layout of the reference library's lmref_material_query.
+int lmo_material_query(int type, const double* prm, const double* rec, long long n, double* out) {
+    using V = V3<double>;
+    auto v3 = [](const double* p) { return V(p[0], p[1], p[2]); };
+    auto put3 = [](double* o, V v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; };
+    Material<double> m;
+    m.type = type;
+    if (type == MAT_DIFFUSE) m.Kd = v3(prm);
+    if (type == MAT_GLOSSY) { m.Ks = v3(prm); m.ax = prm[3]; m.ay = prm[4]; }
+    if (type == MAT_GLASS) m.Ni = prm[0];
+    for (long long i = 0; i < n; i++) {
+        const double* r = rec + 26 * i;
+        double* o = out + 18 * i;
+        const auto g = PointGeometry<double>::make_on_surface(v3(r), v3(r + 3), v3(r + 6), V2<double>(r[9], r[10]));
+        const V wi = v3(r + 11), wo = v3(r + 14);
+        const int comp = int(r[17]);
+        const auto td = r[18] != 0 ? TransDir::EL : TransDir::LE;
+        const bool ed = r[19] != 0;
+        put3(o, m.eval(g, wi, wo, comp, td, ed));
+        o[3] = m.pdf_direction(g, wi, wo, comp, ed);
+        const auto s = m.sample_direction(V2<double>(r[20], r[21]), V2<double>(r[22], r[23]), g, wi, comp, td);
+        o[4] = s ? 1 : 0;
+        put3(o + 5, s ? s->wo : V());
+        put3(o + 8, s ? s->weight : V());
+        const auto cs = m.sample_component(V2<double>(r[24], r[25]), g, wi);
+        o[11] = cs.comp;
+        o[12] = cs.weight;
+        o[13] = m.pdf_component(comp, g, wi);
+        put3(o + 14, m.reflectance(g).value_or(V()));
+        o[17] = m.is_specular_component(comp) ? 1 : 0;
+    }
+    return 0;
+}
+
+// Light queries of a built double-precision scene that holds exactly one light, over records with
+// the layout of the reference library's lmref_light_query: direct sampling toward a shading point
+// (with its pdf and the emitted radiance) and emission sampling, as path.h's sample_direct and
+// sample_primary_ray call them for that light.
+int lmo_light_query(void* p, const double* rec, long long n, double* out) {
+    auto* h = static_cast<Handle*>(p);
+    if (!h->dbl) return fail("light queries need a double-precision scene");
+    auto& S = *h->sd;
+    if (!S.built || S.num_lights() != 1) return fail("light queries need a built scene with one light");
+    using V = V3<double>;
+    auto v3 = [](const double* q) { return V(q[0], q[1], q[2]); };
+    auto put3 = [](double* o, V v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; };
+    const auto& lpi = S.lights_.at(0);
+    const auto& L = S.light_of(lpi.index);
+    try {
+        for (long long i = 0; i < n; i++) {
+            const double* r = rec + 14 * i;
+            double* o = out + 33 * i;
+            std::fill(o, o + 33, 0.0);
+            SceneInteraction<double> sp;
+            sp.type = SI_Surface;
+            sp.geom = PointGeometry<double>::make_on_surface(v3(r), v3(r + 3), v3(r + 6), V2<double>());
+            const double u8[8] = {r[9], r[10], 0.0, r[11], r[12], r[13], 0.0, 0.0};
+            int node = -1;
+            if (const auto sd = S.sample_direct_light(u8, sp, node)) {
+                o[0] = 1;
+                put3(o + 1, sd->geom.p); put3(o + 4, sd->geom.n); put3(o + 7, sd->geom.wo);
+                put3(o + 10, sd->wo); put3(o + 13, sd->weight);
+                o[16] = L.pdf_direct(sp.geom, sd->geom, lpi.tr, sd->wo);
+                put3(o + 17, L.eval(sd->geom, sd->wo));
+            }
+            if (const auto sr = S.sample_primary_ray_light(u8)) {
+                o[20] = 1;
+                put3(o + 21, sr->geom.p); put3(o + 24, sr->geom.n); put3(o + 27, sr->wo); put3(o + 30, sr->weight);
+            }
+        }
+    } catch (const std::exception& e) {
+        return fail(e.what());
+    }
+    return 0;
+}
+
+// n uniforms of the restated reference Rng (RngMT), double or float flavour.
+int lmo_rng_mt(unsigned int seed, int as_float, long long n, double* out) {
+    RngMT r(seed, as_float != 0);
+    for (long long i = 0; i < n; i++) out[i] = r.u();
+    return 0;
+}
+
 }  // extern "C"
 
 extern "C" void lmo_philox4x32(unsigned int c0, unsigned int c1, unsigned int c2, unsigned int c3, unsigned int k0,

@@ -65,6 +65,11 @@ def lib() -> C.CDLL:
         L.lmo_philox_uniform.restype = C.c_float
         L.lmo_philox_uniform.argtypes = [C.c_uint, C.c_ulonglong, C.c_uint, C.c_uint]
         L.lmo_max_threads.restype = C.c_int
+        L.lmo_math_eval.argtypes = [C.c_char_p, dp, C.c_longlong, dp]
+        L.lmo_dist2_eval.argtypes = [dp, C.c_int, C.c_int, C.c_longlong, dp, dp, dp, dp]
+        L.lmo_rng_mt.argtypes = [C.c_uint, C.c_int, C.c_longlong, dp]
+        L.lmo_material_query.argtypes = [C.c_int, dp, dp, C.c_longlong, dp]
+        L.lmo_light_query.argtypes = [vp, dp, C.c_longlong, dp]
         _lib = L
     return _lib
 
@@ -170,6 +175,15 @@ class OracleScene:
         self.num_tris = lib().lmo_num_triangles(self.h)
 
     # -- queries ----------------------------------------------------------------------------------
+    def light_query(self, rec: np.ndarray) -> np.ndarray:
+        """Direct and emission sampling of the scene's only light over records of 14 doubles
+        (layout as oracle/ref.py's light_query); returns n x 33. Double-precision scenes."""
+        rec = np.ascontiguousarray(rec, np.float64)
+        out = np.zeros((rec.shape[0], 33))
+        dp = C.POINTER(C.c_double)
+        _chk(lib().lmo_light_query(self.h, rec.ctypes.data_as(dp), rec.shape[0], out.ctypes.data_as(dp)))
+        return out
+
     def triangles(self) -> np.ndarray:
         """(n, 9): p1, e1, e2 of every flattened triangle, as the accel stores them."""
         out = np.empty((self.num_tris, 9), np.float32)
@@ -278,6 +292,50 @@ def philox_uniform(seed: int, path: int, vertex: int, slot: int) -> float:
 
 def max_threads() -> int:
     return lib().lmo_max_threads()
+
+
+def math_eval(fn: str, inp: np.ndarray, out_width: int) -> np.ndarray:
+    """The restated math.h helper `fn` in double over the rows of `inp` (record layouts as
+    oracle/ref.py's math_eval, so the two compare bit for bit)."""
+    inp = np.ascontiguousarray(inp, np.float64)
+    out = np.zeros((inp.shape[0], out_width))
+    _chk(lib().lmo_math_eval(fn.encode(), inp.ctypes.data_as(C.POINTER(C.c_double)), inp.shape[0],
+                             out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+def dist2_eval(v: np.ndarray, uvq: np.ndarray, u4: np.ndarray):
+    """Restated Dist2 over the rows x cols table v: pdf at uvq (n x 2), samples from u4 (n x 4)."""
+    v = np.ascontiguousarray(v, np.float64)
+    rows, cols = v.shape
+    uvq = np.ascontiguousarray(uvq, np.float64)
+    u4 = np.ascontiguousarray(u4, np.float64)
+    n = uvq.shape[0]
+    pdf, smp = np.zeros(n), np.zeros((n, 2))
+    dp = C.POINTER(C.c_double)
+    _chk(lib().lmo_dist2_eval(v.ctypes.data_as(dp), cols, rows, n, uvq.ctypes.data_as(dp), u4.ctypes.data_as(dp),
+                              pdf.ctypes.data_as(dp), smp.ctypes.data_as(dp)))
+    return pdf, smp
+
+
+def material_query(key: str, params, rec: np.ndarray) -> np.ndarray:
+    """Every query of the restated material `key` over records of 26 doubles (layout as
+    oracle/ref.py's material_query); returns n x 18."""
+    prm = np.zeros(8)
+    prm[:len(params)] = params
+    rec = np.ascontiguousarray(rec, np.float64)
+    out = np.zeros((rec.shape[0], 18))
+    dp = C.POINTER(C.c_double)
+    _chk(lib().lmo_material_query(MAT[key], prm.ctypes.data_as(dp), rec.ctypes.data_as(dp), rec.shape[0],
+                                  out.ctypes.data_as(dp)))
+    return out
+
+
+def rng_mt(seed: int, n: int, as_float: bool = False) -> np.ndarray:
+    """n uniforms of the restated reference Rng (mt19937, double or the float flavour)."""
+    out = np.zeros(n)
+    _chk(lib().lmo_rng_mt(seed, 1 if as_float else 0, n, out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
 
 
 def from_parts(parts: dict, double: bool = True) -> OracleScene:

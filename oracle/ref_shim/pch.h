@@ -1,0 +1,22 @@
+// Oracle (test infrastructure only): stand-in for the reference's precompiled header, which
+// gathers the standard headers its sources use.
+#pragma once
+#include <algorithm>
+#include <atomic>
+#include <cassert>
+#include <cmath>
+#include <condition_variable>
+#include <functional>
+#include <limits>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <numeric>
+#include <optional>
+#include <queue>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <tuple>
+#include <vector>

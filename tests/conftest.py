@@ -31,6 +31,16 @@ def oracle_mod():
     return O
 
 
+@pytest.fixture(scope="session")
+def ref_mod():
+    """oracle/_ref/liblmref.so: the reference's own accel and math code, compiled from its sources.
+    Only where those sources are present; elsewhere the tests that need it skip."""
+    from oracle import ref as R
+    if not R.available():
+        pytest.skip("the reference's sources are absent, so oracle/_ref is not built")
+    return R
+
+
 @pytest.fixture
 def lm(native_lib):
     import lightmetrica as lm_

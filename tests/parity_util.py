@@ -47,6 +47,21 @@ def mt64(o, d, p1, e1, e2):
 EPS32 = 2.0 ** -24
 
 
+def fp32_bounds(o, d, tri_rows, k=16.0):
+    """fp64 (t, u, v) of rays (o, d) against triangle rows (m, 3, 3) and the fp32 Moller-Trumbore
+    test's error bounds for them (see classify_fp64_mismatches): (t, u, v, err_t, err_u, err_v)."""
+    nd = np.linalg.norm(d, axis=1)
+    p1 = tri_rows[:, 0]
+    e1, e2 = tri_rows[:, 1] - p1, tri_rows[:, 2] - p1
+    t, u, v, ad = mt64(o, d, p1, e1, e2)
+    ad = np.maximum(ad, 1e-300)
+    ntv, n1, n2 = np.linalg.norm(o - p1, axis=1), np.linalg.norm(e1, axis=1), np.linalg.norm(e2, axis=1)
+    err_u = k * EPS32 * ntv * nd * n2 / ad
+    err_v = k * EPS32 * nd * ntv * n1 / ad
+    err_t = k * EPS32 * (n2 * ntv * n1 / ad + np.abs(t))
+    return t, u, v, err_t, err_u, err_v
+
+
 def classify_fp64_mismatches(rays, g, ids64, tri, k=16.0):
     """Rays whose GPU (fp32) triangle differs from the fp64 restatement's. Each must be one the
     fp32 test cannot decide within its rounding error: a near-tie (the two triangles' fp64 t
@@ -64,19 +79,10 @@ def classify_fp64_mismatches(rays, g, ids64, tri, k=16.0):
         return 0, 0, []
     o = rays[mism, 0:3].astype(np.float64)
     d = rays[mism, 4:7].astype(np.float64)
-    nd = np.linalg.norm(d, axis=1)
 
     def test(c):
         valid = c >= 0
-        cc = np.where(valid, c, 0)
-        p1 = tri[cc, 0]
-        e1, e2 = tri[cc, 1] - p1, tri[cc, 2] - p1
-        t, u, v, ad = mt64(o, d, p1, e1, e2)
-        ad = np.maximum(ad, 1e-300)
-        ntv, n1, n2 = np.linalg.norm(o - p1, axis=1), np.linalg.norm(e1, axis=1), np.linalg.norm(e2, axis=1)
-        err_u = k * EPS32 * ntv * nd * n2 / ad
-        err_v = k * EPS32 * nd * ntv * n1 / ad
-        err_t = k * EPS32 * (n2 * ntv * n1 / ad + np.abs(t))
+        t, u, v, err_t, err_u, err_v = fp32_bounds(o, d, tri[np.where(valid, c, 0)], k)
         margins = np.stack([u, v, 1 - u - v], 1)
         errs = np.stack([err_u, err_v, err_u + err_v], 1)
         graze = np.any(np.abs(margins) <= errs, axis=1)
@@ -88,6 +94,32 @@ def classify_fp64_mismatches(rays, g, ids64, tri, k=16.0):
     grazing = (va & ga) | (vb & gb)
     ok = near_tie | grazing
     return int(near_tie.sum()), int((grazing & ~near_tie).sum()), [int(i) for i in mism[~ok]]
+
+
+def check_against_fp64(gpu, t64, uv64, ids64, rays, tri, label):
+    """GPU (fp32) hits against fp64 hits of the same rays (the reference's own, or the fp64
+    restatement's). Where both pick the same triangle, t agrees within 1e-5 relative and u, v
+    within 1e-5 absolute, or within the fp32 test's error bounds where those are larger (far,
+    grazing hits). Every differing triangle choice is a near-tie or a grazing hit (see
+    classify_fp64_mismatches). `tri` is the world-space triangles (n, 3, 3) in flattened order.
+    Returns (fp64 hits, index mismatches, near-ties, grazing)."""
+    g = gpu["prim"].astype(np.int64)
+    ids64 = np.asarray(ids64, np.int64)
+    both = np.nonzero((g >= 0) & (g == ids64))[0]
+    if both.size:
+        o = rays[both, 0:3].astype(np.float64)
+        d = rays[both, 4:7].astype(np.float64)
+        _, _, _, err_t, err_u, err_v = fp32_bounds(o, d, tri[g[both]])
+        dt = np.abs(gpu["t"][both].astype(np.float64) - t64[both])
+        du = np.abs(gpu["u"][both].astype(np.float64) - uv64[both, 0])
+        dv = np.abs(gpu["v"][both].astype(np.float64) - uv64[both, 1])
+        bad_t = dt > np.maximum(1e-5 * np.abs(t64[both]), err_t)
+        bad_uv = (du > np.maximum(1e-5, err_u)) | (dv > np.maximum(1e-5, err_v))
+        assert not bad_t.any(), f"{label}: t outside its bound at rays {both[bad_t][:10]}"
+        assert not bad_uv.any(), f"{label}: u, v outside their bounds at rays {both[bad_uv][:10]}"
+    near, graze, unexplained = classify_fp64_mismatches(rays, g, ids64, tri)
+    assert not unexplained, f"{label}: unexplained index mismatches at rays {unexplained[:10]}"
+    return int((ids64 >= 0).sum()), int((g != ids64).sum()), near, graze
 
 
 def nmse(img, ref):

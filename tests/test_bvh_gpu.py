@@ -138,3 +138,34 @@ def test_gpu_builder_instanced_same_hits(lm):
     assert (hits[0]["prim"] >= 0).mean() > 0.05
     for k in ("prim", "t", "u", "v"):
         assert np.array_equal(hits[0][k], hits[1][k]), k
+
+
+def test_transformed_scene_against_reference_fixture(lm, oracle_mod):
+    """Nested group transforms, shared edges, duplicated and degenerate triangles, axis-parallel
+    and vertex-aimed rays (tests/ref_scenes.py): the hits of trees from either builder against the
+    reference's own hits (accel_sahbvh.cpp compiled from its sources, committed as
+    tests/golden/ref_transformed_hits.npz) within fp32's error bounds, and bit for bit against the
+    fp32 restatement's exhaustive test (exact-t ties exempt). Exhaustive, because rays aimed exactly
+    at a triangle's corner can be accepted by the fp32 Moller-Trumbore test a rounding error outside
+    the triangle's bounding box: the restated binary BVH's slab test culls some of those hits, the
+    kernel's outward-rounded boxes do not."""
+    import os
+
+    import ref_scenes as RS
+    from parity_util import check_against_fp64, compare_bitexact
+    desc = RS.transformed_scene()
+    scene = RS.to_lm(lm, desc, "rfx_")
+    rays = RS.pin_rays(desc)
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_transformed_hits.npz"))
+    S32 = RS.to_oracle(oracle_mod, desc, double=False)
+    S32.build(robust=True)
+    t32, uv32, ids32, _ = S32.intersect(rays, brute=True, refine_t=True)
+    tri32 = S32.triangles()
+    tri = scene._flatten()["positions"].reshape(-1, 3, 3).astype(np.float64)
+    h = _hits_both(lm, scene, rays)
+    for b in ("sah", "ploc"):
+        hits, mism, near, graze = check_against_fp64(h[b], fx["t"], fx["uv"], fx["tri"], rays, tri, b)
+        ties = compare_bitexact(h[b], t32, uv32, ids32, rays, tri32)
+        print(f"{b}: {hits} reference hits, {mism} index mismatches ({near} near-ties, {graze} grazing); "
+              f"{ties} exact-t ties against fp32")
+        assert hits > 8000

@@ -24,7 +24,7 @@ import os
 
 import numpy as np
 import pytest
-from parity_util import classify_fp64_mismatches, compare_bitexact, downsample, nmse
+from parity_util import check_against_fp64, classify_fp64_mismatches, compare_bitexact, downsample, nmse
 
 pytestmark = pytest.mark.gpu
 
@@ -60,7 +60,7 @@ def test_c2_raycast_probe_16m_rays(lm, oracle_mod):
 
     S64 = oracle_mod.from_lm_scene(scene, double=True)
     S64.build()
-    t64, _, ids64, _ = S64.intersect(rays)
+    t64, uv64, ids64, _ = S64.intersect(rays)
     del S64
     g = gpu["prim"].astype(np.int64)
     both = (g >= 0) & (g == ids64)
@@ -72,6 +72,18 @@ def test_c2_raycast_probe_16m_rays(lm, oracle_mod):
           f"mismatches ({near} near-ties, {graze} grazing)")
     assert (g != ids64).mean() < 1e-4
     assert not unexplained, unexplained[:10]
+
+    # The reference's own hits (accel_sahbvh.cpp compiled from its sources; every 1024th probe
+    # ray, tests/golden/make_ref_fixtures.py): the fp64 restatement on this machine reproduces
+    # them bit for bit, and the GPU's hits agree with them within fp32's error bounds.
+    fx = np.load(os.path.join(GOLDEN, "ref_c2_probe_hits.npz"))
+    sel = fx["ray"]
+    assert np.array_equal(ids64[sel], fx["tri"])
+    assert np.array_equal(t64[sel], fx["t"]) and np.array_equal(uv64[sel], fx["uv"])
+    sub = {k: gpu[k][sel] for k in ("prim", "t", "u", "v")}
+    hits, mism, near, graze = check_against_fp64(sub, fx["t"], fx["uv"], fx["tri"], rays[sel], tri, "C2 vs reference")
+    print(f"C2 raycast probe vs the reference's own hits: {len(sel)} rays, {hits} hits, {mism} index mismatches "
+          f"({near} near-ties, {graze} grazing)")
 
 
 def _golden(name):

@@ -1,0 +1,316 @@
+"""The oracle pinned to the reference's own code (CPU).
+
+oracle/_ref/liblmref.so is the reference's src/accel/accel_sahbvh.cpp,
+src/material/material_{diffuse,glossy,glass,mirror}.cpp, src/light/light_{area,envconst,point,
+directional}.cpp, include/lm/math.h and include/lm/surface.h, compiled unmodified from its sources
+(oracle/Makefile `ref`, oracle/ref.py) against stand-in headers for glm's arithmetic and the few
+lm core names they use. Where those sources are present the tests compare the oracle's fp64
+restatement with that library directly; everywhere, they compare it with the hit fixtures the
+library produced (tests/golden/make_ref_fixtures.py).
+
+Bit-exact means equal float64 bit patterns (NaNs equal to NaNs), equal triangle indices and equal
+hit/miss decisions: the restatement must reproduce the reference's Möller–Trumbore test
+(accel_sahbvh.cpp:58-75), its full-sort SAH build (:127-267, including the split chosen among
+equal costs), its traversal order and "later triangle wins" ties (:269-299), the slab test
+(math.h:143-158), the scene flattening with group transforms, the math helpers, Dist2 and the
+Rng, every material query and the lights' direct and emission sampling.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import ref_scenes as RS
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _same_bits(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    if a.shape != b.shape:
+        return False
+    nan = np.isnan(a)
+    if not np.array_equal(nan, np.isnan(b)):
+        return False
+    return np.array_equal(a[~nan].view(np.uint64), b[~nan].view(np.uint64))
+
+
+def _assert_hits_equal(ref_hits, orc_hits, label):
+    (t1, uv1, i1), (t2, uv2, i2) = ref_hits, orc_hits
+    i1 = np.asarray(i1, np.int64)
+    i2 = np.asarray(i2, np.int64)
+    bad = np.flatnonzero(i1 != i2)
+    assert bad.size == 0, f"{label}: {bad.size} index mismatches, first {bad[:5]}"
+    assert _same_bits(t1, t2), f"{label}: t differs"
+    assert _same_bits(uv1, uv2), f"{label}: uv differs"
+
+
+def _soup(seed, n=4000):
+    rng = np.random.default_rng(seed)
+    from lightmetrica import synthetic as syn
+    p, _ = syn.random_triangles(n, rng)
+    p = p.reshape(n, 3, 3)
+    p[n - n // 10:] = p[: n // 10]                  # exact duplicates
+    p[: n // 20, :, 1] = np.float32(0.5)           # a plane of coplanar triangles at y = 0.5
+    return {"meshes": [(p.reshape(-1, 3), np.arange(3 * n, dtype=np.int32).reshape(-1, 3))],
+            "nodes": [("prim", 0, 0)]}
+
+
+def _soup_rays(seed, n=40000):
+    rng = np.random.default_rng(seed + 100)
+    o = rng.uniform(-0.5, 1.5, (n, 3))
+    d = rng.normal(size=(n, 3))
+    d[: n // 8, rng.integers(0, 3)] = 0.0              # a zero direction component
+    d[n // 8: n // 4, 1] = 0.0
+    o[n // 8: n // 4, 1] = 0.5                         # in the coplanar triangles' plane
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = np.empty((n, 8), np.float32)
+    r[:, 0:3], r[:, 3], r[:, 4:7], r[:, 7] = o, 0.0, d, 1e10
+    return r
+
+
+# -- against the reference library ----------------------------------------------------------------
+
+def test_transformed_scene_hits_match_reference(ref_mod, oracle_mod):
+    desc = RS.transformed_scene()
+    S = RS.to_ref(desc)
+    S.build()
+    O = RS.to_oracle(oracle_mod, desc)
+    O.build()
+    rays = RS.pin_rays(desc)
+    ref = S.intersect(rays)
+    t, uv, ids, _ = O.intersect(rays)
+    assert (ref[2] >= 0).sum() > 5000
+    _assert_hits_equal(ref, (t, uv, ids), "transformed scene")
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_triangle_soup_hits_match_reference(ref_mod, oracle_mod, seed):
+    desc = _soup(seed)
+    S = RS.to_ref(desc)
+    S.build()
+    O = RS.to_oracle(oracle_mod, desc)
+    O.build()
+    rays = _soup_rays(seed)
+    ref = S.intersect(rays)
+    t, uv, ids, _ = O.intersect(rays)
+    assert (ref[2] >= 0).sum() > 1000
+    _assert_hits_equal(ref, (t, uv, ids), f"soup {seed}")
+
+
+def test_small_spheres_probe_matches_reference(ref_mod, oracle_mod):
+    """The displaced-sphere scene's generator at a reduced size, probed from the raycast probe's
+    origin."""
+    from lightmetrica import synthetic as syn
+    parts = syn.spheres_parts(seed=7, n_spheres=8, subdiv=4, ground_quads=32)
+    S = ref_mod.from_parts(parts)
+    S.build()
+    O = oracle_mod.from_parts(parts, double=True)
+    O.build()
+    rays = syn.sphere_rays(1 << 16, syn.RAYCAST_PROBE_ORIGIN, seed=3)
+    ref = S.intersect(rays)
+    t, uv, ids, _ = O.intersect(rays)
+    _assert_hits_equal(ref, (t, uv, ids), "small spheres")
+
+
+def _math_inputs(rng, n=4000):
+    u2 = rng.random((n, 2))
+    u2[:8] = [[0, 0], [0, 1], [1, 0], [1, 1], [0.5, 0.25], [1e-300, 0.5], [0.999999999, 0.0], [0.25, 0.999999999]]
+    v3 = rng.normal(size=(n, 3))
+    v3 /= np.linalg.norm(v3, axis=1, keepdims=True)
+    v3[:6] = [[0, 0, 1], [0, 0, -1], [0, 0, 0.0], [0, 0, -0.0], [1, 0, 0], [0, 1, 0]]
+    w3 = rng.normal(size=(n, 3))
+    w3 /= np.linalg.norm(w3, axis=1, keepdims=True)
+    eta = rng.choice([1 / 1.5, 1.5, 1.0, 2.4], n)[:, None]
+    tri = rng.normal(size=(n, 9))
+    tri[:4, 6:9] = tri[:4, 3:6]                    # degenerate: two equal corners
+    p2 = rng.random((n, 2)) * rng.choice([0.0, 1.0, 1e-300], (n, 2))
+    s1 = rng.normal(size=(n, 1))
+    m = rng.normal(size=(n, 16))
+    box = np.concatenate([rng.uniform(-1, 0, (n, 3)), rng.uniform(0, 1, (n, 3)), rng.uniform(-2, 2, (n, 3)),
+                          rng.normal(size=(n, 3)), np.zeros((n, 1)), np.full((n, 1), 1e10)], 1)
+    box[: n // 4, 9 + 0] = 0.0                     # direction component 0 ...
+    box[: n // 8, 6 + 0] = box[: n // 8, 0]        # ... from an origin on the slab plane: 0 * inf
+    box[n // 4: n // 2, 12] = rng.uniform(0, 3, n // 4)
+    box[n // 4: n // 2, 13] = box[n // 4: n // 2, 12] + rng.uniform(0, 1, n // 4)
+    return {
+        "reflection": (np.c_[w3, v3], 3),
+        "refraction": (np.c_[w3, v3, eta], 4),
+        "orthonormal_basis": (v3, 6),
+        "geometry_normal": (tri, 3),
+        "sample_uniform_disk": (u2, 2),
+        "sample_cosine_weighted": (u2, 3),
+        "sample_uniform_sphere": (u2, 3),
+        "balance_heuristic": (p2, 1),
+        "safe_sqrt": (s1, 1),
+        "transform_J": (m, 1),
+        "bound_isect": (box, 3),
+    }
+
+
+def test_math_helpers_match_reference(ref_mod, oracle_mod):
+    """math.h's helpers (reflection, refraction, orthonormal_basis, geometry_normal, the disk /
+    cosine / sphere samplers, balance_heuristic, safe_sqrt, Transform's Jacobian, the slab test's
+    narrowed range) against the restatement, bit for bit, edge inputs included."""
+    for fn, (inp, width) in _math_inputs(np.random.default_rng(9)).items():
+        a = ref_mod.math_eval(fn, inp, width)
+        b = oracle_mod.math_eval(fn, inp, width)
+        assert _same_bits(a, b), fn
+
+
+def test_dist2_matches_reference(ref_mod, oracle_mod):
+    """Dist2 (math.h:378-432): pdf and sampling over a table with zero rows and columns."""
+    rng = np.random.default_rng(4)
+    v = rng.random((24, 40)) ** 3
+    v[5] = 0.0
+    v[:, 7] = 0.0
+    uvq = rng.random((5000, 2))
+    u4 = rng.random((5000, 4))
+    u4[:4, :2] = [[0, 0], [1 - 1e-16, 1 - 1e-16], [0.5, 0.5], [0.2083333333333333, 0.175]]
+    p1, s1 = ref_mod.dist2_eval(v, uvq, u4)
+    p2, s2 = oracle_mod.dist2_eval(v, uvq, u4)
+    assert _same_bits(p1, p2) and _same_bits(s1, s2)
+
+
+@pytest.mark.parametrize("as_float", [False, True])
+def test_rng_matches_reference(ref_mod, oracle_mod, as_float):
+    """The reference's Rng (std::mt19937 + uniform_real_distribution<double>; the float flavour
+    rounds toward -inf) against the oracle's, for the seeds renderer_pt uses (seed + thread)."""
+    for seed in (0, 1, 42, 1234 + 7):
+        assert _same_bits(ref_mod.rng(seed, 20000, as_float), oracle_mod.rng_mt(seed, 20000, as_float))
+
+
+def test_fixtures_reproduce(ref_mod):
+    """The committed transformed-scene fixture is what the reference library gives now."""
+    desc = RS.transformed_scene()
+    S = RS.to_ref(desc)
+    S.build()
+    t, uv, tri = S.intersect(RS.pin_rays(desc))
+    fx = np.load(os.path.join(GOLDEN, "ref_transformed_hits.npz"))
+    assert np.array_equal(tri, fx["tri"]) and _same_bits(t, fx["t"]) and _same_bits(uv, fx["uv"])
+
+
+# -- against the committed reference fixtures (no reference sources needed) -----------------------
+
+def test_oracle_matches_reference_fixture_transformed(oracle_mod):
+    desc = RS.transformed_scene()
+    O = RS.to_oracle(oracle_mod, desc)
+    O.build()
+    t, uv, ids, _ = O.intersect(RS.pin_rays(desc))
+    fx = np.load(os.path.join(GOLDEN, "ref_transformed_hits.npz"))
+    _assert_hits_equal((fx["t"], fx["uv"], fx["tri"]), (t, uv, ids), "transformed fixture")
+
+
+def test_oracle_matches_reference_fixture_c2_probe(oracle_mod):
+    """The benchmark's 3,801,100-triangle scene: every 1024th ray of the 16,777,216-ray probe,
+    the fp64 oracle against the reference's own hits."""
+    from lightmetrica import synthetic as syn
+    fx = np.load(os.path.join(GOLDEN, "ref_c2_probe_hits.npz"))
+    parts = syn.spheres_parts(seed=7)
+    O = oracle_mod.from_parts(parts, double=True)
+    O.build()
+    assert O.num_tris == 3801100
+    rays = syn.sphere_rays(syn.RAYCAST_PROBE_RAYS, syn.RAYCAST_PROBE_ORIGIN, seed=syn.RAYCAST_PROBE_SEED)[fx["ray"]]
+    t, uv, ids, _ = O.intersect(rays)
+    assert (fx["tri"] >= 0).sum() > 8000
+    _assert_hits_equal((fx["t"], fx["uv"], fx["tri"]), (t, uv, ids), "C2 probe fixture")
+
+
+def _material_records(rng, n=20000):
+    def unit(x):
+        return x / np.linalg.norm(x, axis=1, keepdims=True)
+    nn = unit(rng.normal(size=(n, 3)))
+    rec = np.zeros((n, 26))
+    rec[:, 0:3] = rng.normal(size=(n, 3))
+    rec[:, 3:6] = nn
+    rec[:, 6:9] = nn
+    rec[:, 9:11] = rng.random((n, 2))
+    rec[:, 11:14] = unit(rng.normal(size=(n, 3)))
+    rec[:, 14:17] = unit(rng.normal(size=(n, 3)))
+    rec[: n // 10, 14:17] = -rec[: n // 10, 11:14]       # straight through
+    rec[n // 10: n // 5, 14:17] = 2 * np.sum(rec[n // 10: n // 5, 11:14] * nn[n // 10: n // 5], 1)[:, None] * \
+        nn[n // 10: n // 5] - rec[n // 10: n // 5, 11:14]  # mirror direction
+    rec[:, 17] = rng.integers(0, 2, n)
+    rec[:, 18] = rng.integers(0, 2, n)
+    rec[:, 19] = rng.integers(0, 2, n)
+    rec[:, 20:26] = rng.random((n, 6))
+    rec[:8, 20:22] = [[0, 0], [1 - 1e-16, 0], [0, 1 - 1e-16], [0.5, 0.5], [1e-300, 0.3], [0.3, 1e-300], [1, 1], [0, 1]]
+    return rec
+
+
+@pytest.mark.parametrize("key,params", [
+    ("material::diffuse", [0.6, 0.5, 0.4]),
+    ("material::glossy", [0.7, 0.6, 0.5, 0.2, 0.35]),
+    ("material::glossy", [0.95, 0.9, 0.8, 0.02, 0.6]),
+    ("material::glass", [1.5]),
+    ("material::glass", [1.0 / 1.33]),
+    ("material::mirror", []),
+])
+def test_materials_match_reference(ref_mod, oracle_mod, key, params):
+    """Every Material query (eval, pdf_direction, sample_direction, sample_component,
+    pdf_component, reflectance, is_specular_component; both transport directions, both
+    components, eval_delta on and off) of material_{diffuse,glossy,glass,mirror}.cpp against the
+    restatement, bit for bit, on random and edge geometry."""
+    rec = _material_records(np.random.default_rng(11))
+    a = ref_mod.material_query(key, params, rec)
+    b = oracle_mod.material_query(key, params, rec)
+    assert _same_bits(a, b), f"{key}: rows {np.nonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).all(1))[0][:5]}"
+
+
+_LIGHT_MESH = (np.array([[0, 0, 0], [1, 0, 0], [1, 0, 1], [0, 0, 1], [0.5, 0.2, 0.5]], np.float32),
+               np.array([[0, 1, 2], [0, 2, 3], [0, 4, 1]], np.int32))
+# an axis permutation, a scale by 2 (Jacobian 8) and a translation: exact in any inverse
+_LIGHT_M = np.array([[0, 0, 2, 1.5], [2, 0, 0, 3.0], [0, 2, 0, -0.5], [0, 0, 0, 1]], np.float64)
+
+
+@pytest.mark.parametrize("key,params", [
+    ("light::area", [4.0, 5.0, 6.0]),
+    ("light::envconst", [0.3, 0.4, 0.5]),
+    ("light::point", [3.0, 2.0, 1.0, 0.2, 4.0, -1.0]),
+    ("light::directional", [1.0, 2.0, 3.0, 0.3, -1.0, 0.2]),
+])
+def test_lights_match_reference(ref_mod, oracle_mod, key, params):
+    """light_{area,envconst,point,directional}.cpp: sample_direct toward random shading points with
+    its pdf_direct and eval, and sample_ray, under a transform (area) and with the scene bound the
+    scene's transformed triangles give (envconst, directional), against the restatement's
+    path-level light sampling with one light, bit for bit."""
+    from lightmetrica import synthetic as syn
+    gp, _, gf = syn.ground_grid(4, 3.0)
+    lp, lf = _LIGHT_MESH
+    S = ref_mod.RefScene()
+    m0, m1 = S.add_mesh(gp, gf), S.add_mesh(lp, lf)
+    S.add_child(0, S.primitive(m0))
+    g = S.group(_LIGHT_M)
+    S.add_child(0, g)
+    S.add_child(g, S.primitive(m1))
+    O = oracle_mod.OracleScene(True)
+    mat = O.add_material(oracle_mod.MAT["material::diffuse"], [0.5, 0.5, 0.5])
+    nrm = np.array([[0, 1, 0]], np.float32)
+    o0 = O.add_mesh(gp, nrm, gf.reshape(-1), np.zeros(gf.size, np.int32))
+    o1 = O.add_mesh(lp, nrm, lf.reshape(-1), np.zeros(lf.size, np.int32))
+    O.add_child(0, O.primitive(o0, mat, -1, -1))
+    og = O.group(_LIGHT_M)
+    O.add_child(0, og)
+    if key == "light::area":
+        O.add_child(og, O.primitive(o1, mat, O.add_area_light(params[:3], o1), -1))
+    else:
+        O.add_child(og, O.primitive(o1, mat, -1, -1))
+        li = {"light::envconst": lambda: O.add_envconst(params[:3]),
+              "light::point": lambda: O.add_point(params[:3], params[3:6]),
+              "light::directional": lambda: O.add_directional(params[:3], params[3:6])}[key]()
+        O.add_child(0, O.primitive(-1, -1, li, -1))
+    O.build()
+    rng = np.random.default_rng(13)
+    n = 5000
+    rec = np.zeros((n, 14))
+    rec[:, 0:3] = rng.uniform(-3, 3, (n, 3))
+    nn = rng.normal(size=(n, 3))
+    nn /= np.linalg.norm(nn, axis=1, keepdims=True)
+    rec[:, 3:6] = nn
+    rec[:, 6:9] = nn
+    rec[:, 9:14] = rng.random((n, 5))
+    a = ref_mod.light_query(S, key, params, m1, _LIGHT_M, rec)
+    b = O.light_query(rec)
+    assert a[:, 0].sum() > 1000 and a[:, 20].sum() == n
+    assert _same_bits(a, b), f"{key}: rows {np.nonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).all(1))[0][:5]}"
