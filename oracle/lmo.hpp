@@ -185,6 +185,23 @@ template <typename F> struct Camera {
         if (!raster_position(wo)) return V3<F>(F(0));
         return V3<F>(J(wo));
     }
+    // camera_pinhole.cpp:178-203: the connection from a scene point to the camera: the camera
+    // point, wo from it toward the scene point, weight J(wo) / (1 / G)
+    struct DirectSample { PointGeometry<F> geom; V3<F> wo; V3<F> weight; };
+    F pdf_direct(const PointGeometry<F>& g, const PointGeometry<F>& gE) const {
+        if (g.infinite) return F(0);
+        const F G = geometry_term(g, gE);
+        return G == F(0) ? F(0) : F(1) / G;
+    }
+    std::optional<DirectSample> sample_direct(const PointGeometry<F>& g) const {
+        if (g.infinite) return {};
+        const auto gE = PointGeometry<F>::make_degenerated(position);
+        const auto wo = normalize(g.p - position);
+        const auto We = V3<F>(J(wo));
+        const auto p = pdf_direct(g, gE);
+        if (p == F(0)) return {};
+        return DirectSample{gE, wo, We / p};
+    }
 };
 
 // ------------------------------------------------------------------------------------------------
@@ -1328,12 +1345,11 @@ void render_lt(const Scene<F>& scene, const LTParams& P, double* out, long long*
             // weight J(wo) / (1 / G)
             [&] {
                 for (int k = 0; k < 8; k++) U(nv, k);
-                const auto gE = PointGeometry<F>::make_degenerated(cam.position);
-                const auto wE = normalize(sp.geom.p - cam.position);
-                const F G = geometry_term(sp.geom, gE);
-                const F pE = G == F(0) ? F(0) : F(1) / G;
-                if (pE == F(0)) return;
-                const auto weightE = V3F(cam.J(wE)) / pE;
+                const auto sE = cam.sample_direct(sp.geom);
+                if (!sE) return;
+                const auto gE = sE->geom;
+                const auto wE = sE->wo;
+                const auto weightE = sE->weight;
                 SceneInteraction<F> spE; spE.type = SI_Camera; spE.primitive = *scene.camera_; spE.geom = gE;
                 nrays++;
                 if (!scene.visible(sp, spE)) return;

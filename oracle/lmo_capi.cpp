@@ -513,6 +513,38 @@ int lmo_light_query(void* p, const double* rec, long long n, double* out) {
     return 0;
 }
 
+// The restated camera::pinhole in double over records with the layout of the reference library's
+// lmref_camera_query.
+int lmo_camera_query(const double* prm, const double* rec, long long n, double* out) {
+    using V = V3<double>;
+    auto v3 = [](const double* q) { return V(q[0], q[1], q[2]); };
+    auto put3 = [](double* o, V v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; };
+    Camera<double> cam;
+    cam.construct(v3(prm), v3(prm + 3), v3(prm + 6), prm[9], prm[10]);
+    for (long long i = 0; i < n; i++) {
+        const double* r = rec + 11 * i;
+        double* o = out + 21 * i;
+        std::fill(o, o + 21, 0.0);
+        const auto ray = cam.primary_ray(V2<double>(r[0], r[1]));
+        put3(o, ray.o);
+        put3(o + 3, ray.d);
+        const V wo = v3(r + 2);
+        if (const auto rp = cam.raster_position(wo)) {
+            o[6] = 1; o[7] = rp->x; o[8] = rp->y;
+        }
+        o[9] = cam.pdf_direction(wo);
+        put3(o + 10, cam.eval(wo));
+        const auto g = PointGeometry<double>::make_on_surface(v3(r + 5), v3(r + 8));
+        if (const auto sd = cam.sample_direct(g)) {
+            o[13] = 1;
+            put3(o + 14, sd->wo);
+            put3(o + 17, sd->weight);
+            o[20] = cam.pdf_direct(g, sd->geom);
+        }
+    }
+    return 0;
+}
+
 // n uniforms of the restated reference Rng (RngMT), double or float flavour.
 int lmo_rng_mt(unsigned int seed, int as_float, long long n, double* out) {
     RngMT r(seed, as_float != 0);

@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
         L.lmo_rng_mt.argtypes = [C.c_uint, C.c_int, C.c_longlong, dp]
         L.lmo_material_query.argtypes = [C.c_int, dp, dp, C.c_longlong, dp]
         L.lmo_light_query.argtypes = [vp, dp, C.c_longlong, dp]
+        L.lmo_camera_query.argtypes = [dp, dp, C.c_longlong, dp]
         _lib = L
     return _lib
 
@@ -328,6 +329,17 @@ def material_query(key: str, params, rec: np.ndarray) -> np.ndarray:
     dp = C.POINTER(C.c_double)
     _chk(lib().lmo_material_query(MAT[key], prm.ctypes.data_as(dp), rec.ctypes.data_as(dp), rec.shape[0],
                                   out.ctypes.data_as(dp)))
+    return out
+
+
+def camera_query(params, rec: np.ndarray) -> np.ndarray:
+    """The restated camera::pinhole (position, center, up, vfov, aspect) over records of 11
+    doubles (layout as oracle/ref.py's camera_query); returns n x 21."""
+    prm = np.ascontiguousarray(params, np.float64)
+    rec = np.ascontiguousarray(rec, np.float64)
+    out = np.zeros((rec.shape[0], 21))
+    dp = C.POINTER(C.c_double)
+    _chk(lib().lmo_camera_query(prm.ctypes.data_as(dp), rec.ctypes.data_as(dp), rec.shape[0], out.ctypes.data_as(dp)))
     return out
 
 

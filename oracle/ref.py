@@ -1,7 +1,8 @@
 """Oracle (test infrastructure only): ctypes wrapper of oracle/_ref/liblmref.so, the reference's
-own accel, material, light and math code (src/accel/accel_sahbvh.cpp,
+own accel, material, light, camera and math code (src/accel/accel_sahbvh.cpp,
 src/material/material_{diffuse,glossy,glass,mirror}.cpp, src/light/light_{area,envconst,point,
-directional}.cpp, include/lm/math.h, include/lm/surface.h) compiled unmodified by
+directional}.cpp, src/camera/camera_pinhole.cpp, include/lm/math.h, include/lm/surface.h)
+compiled unmodified by
 `make -C oracle ref`.
 
 Only tests/ and tests/golden/make_ref_fixtures.py use it, to pin the CPU restatement (and,
@@ -73,6 +74,7 @@ def lib() -> C.CDLL:
         L.lmref_light_create.argtypes = [vp, C.c_char_p, dp, C.c_int]
         L.lmref_light_destroy.argtypes = [vp]
         L.lmref_light_query.argtypes = [vp, dp, dp, C.c_longlong, dp]
+        L.lmref_camera_query.argtypes = [dp, dp, C.c_longlong, dp]
         _lib = L
     return _lib
 
@@ -206,6 +208,18 @@ def light_query(scene: RefScene, key: str, params, mesh: int, m4, rec: np.ndarra
         return out
     finally:
         lib().lmref_light_destroy(h)
+
+
+def camera_query(params, rec: np.ndarray) -> np.ndarray:
+    """The reference's camera::pinhole (position, center, up, vfov, aspect) over records of 11
+    doubles: rp[2], wo[3], a scene point p[3] n[3]. Returns n x 21: primary_ray(rp) (o, d),
+    raster_position(wo) (valid, rp), pdf_direction(wo), eval(wo), sample_direct toward the point
+    (valid, wo, weight) and its pdf_direct."""
+    prm = np.ascontiguousarray(params, np.float64)
+    rec = np.ascontiguousarray(rec, np.float64)
+    out = np.zeros((rec.shape[0], 21))
+    _chk(lib().lmref_camera_query(_p(prm, C.c_double), _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
+    return out
 
 
 def rng(seed: int, n: int, as_float: bool = False) -> np.ndarray:

@@ -1,6 +1,7 @@
 // Oracle (test infrastructure only): C entry points into the reference's own code, compiled from
 // its sources (src/accel/accel_sahbvh.cpp, src/material/material_{diffuse,glossy,glass,mirror}.cpp,
-// src/light/light_{area,envconst,point,directional}.cpp, include/lm/math.h and
+// src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
+// include/lm/math.h and
 // include/lm/surface.h, unmodified) into
 // oracle/_ref/liblmref.so by oracle/Makefile's `ref` target. Tests call them through ctypes to
 // check the CPU restatement (liblmoracle.so) against the reference itself, and
@@ -17,6 +18,7 @@
 #include <lm/mesh.h>
 #include <lm/material.h>
 #include <lm/light.h>
+#include <lm/camera.h>
 
 #include <chrono>
 #include <cstring>
@@ -378,6 +380,48 @@ int lmref_light_query(void* lp, const double* m16, const double* rec, long long 
             if (const auto sr = L->sample_ray(u, tr)) {
                 o[20] = 1;
                 put3(o + 21, sr->geom.p); put3(o + 24, sr->geom.n); put3(o + 27, sr->wo); put3(o + 30, sr->weight);
+            }
+        }
+        return 0;
+    });
+}
+
+// camera::pinhole from position[3], center[3], up[3], vfov, aspect, over n records of 11 doubles:
+// a raster position rp[2], a direction wo[3], a scene point p[3] n[3]. Out, 21 per record:
+// primary_ray(rp) (o[3], d[3]); raster_position(wo) (valid, rp[2]); pdf_direction(wo); eval(wo)[3];
+// sample_direct toward the point (valid, wo[3], weight[3]) and its pdf_direct.
+int lmref_camera_query(const double* prm, const double* rec, long long n, double* out) {
+    return guarded([&] {
+        Json j;
+        j.set("position", {prm[0], prm[1], prm[2]});
+        j.set("center", {prm[3], prm[4], prm[5]});
+        j.set("up", {prm[6], prm[7], prm[8]});
+        j.set("vfov", {prm[9]});
+        j.set("aspect", {prm[10]});
+        std::unique_ptr<Component> c(refshim::create("camera::pinhole"));
+        auto* cam = dynamic_cast<Camera*>(c.get());
+        if (!cam) throw std::invalid_argument("no camera::pinhole registered");
+        c->construct(j);
+        for (long long i = 0; i < n; i++) {
+            const double* r = rec + 11 * i;
+            double* o = out + 21 * i;
+            std::fill(o, o + 21, 0.0);
+            const auto ray = cam->primary_ray(Vec2(r[0], r[1]));
+            put3(o, ray.o);
+            put3(o + 3, ray.d);
+            const Vec3 wo = v3(r + 2);
+            if (const auto rp = cam->raster_position(wo)) {
+                o[6] = 1; o[7] = rp->x; o[8] = rp->y;
+            }
+            const auto g0 = PointGeometry::make_degenerated(Vec3());
+            o[9] = cam->pdf_direction(g0, wo);
+            put3(o + 10, cam->eval(wo));
+            const auto g = PointGeometry::make_on_surface(v3(r + 5), v3(r + 8));
+            if (const auto sd = cam->sample_direct({Vec2()}, g)) {
+                o[13] = 1;
+                put3(o + 14, sd->wo);
+                put3(o + 17, sd->weight);
+                o[20] = cam->pdf_direct(g, sd->geom, sd->wo);
             }
         }
         return 0;

@@ -1,6 +1,6 @@
 // Oracle (test infrastructure only): stand-in for the part of glm that the reference's
-// include/lm/math.h and src/accel/accel_sahbvh.cpp use, so that those two reference files compile
-// unmodified into oracle/_ref. glm itself (a third-party header library; the reference's
+// include/lm/math.h, include/lm/surface.h and the accel, material, light and camera sources
+// compiled into oracle/_ref use, so that they compile unmodified. glm itself (a third-party header library; the reference's
 // environment.yml and conda/meta.yaml list it without a version, the 0.9.9 series at the time) is
 // absent here.
 //
@@ -212,6 +212,31 @@ template <typename T> inline tmat4x4<T> inverse(const tmat4x4<T>& m) {
         }
     for (int i = 0; i < 4; i++) adj[i] = adj[i] / det;
     return adj;
+}
+
+// Camera matrices (right-handed, clip depth in [-1, 1]); no pinned output depends on them.
+template <typename T> inline T radians(T degrees) { return degrees * T(0.01745329251994329576923690768489); }
+template <typename T> inline T tan(T x) { return std::tan(x); }
+template <typename T> inline tmat4x4<T> lookAt(const tvec3<T>& eye, const tvec3<T>& center, const tvec3<T>& up) {
+    const tvec3<T> f = normalize(center - eye);
+    const tvec3<T> s = normalize(cross(f, up));
+    const tvec3<T> u = cross(s, f);
+    tmat4x4<T> r(T(1));
+    r[0][0] = s.x; r[1][0] = s.y; r[2][0] = s.z;
+    r[0][1] = u.x; r[1][1] = u.y; r[2][1] = u.z;
+    r[0][2] = -f.x; r[1][2] = -f.y; r[2][2] = -f.z;
+    r[3][0] = -dot(s, eye); r[3][1] = -dot(u, eye); r[3][2] = dot(f, eye);
+    return r;
+}
+template <typename T> inline tmat4x4<T> perspective(T fovy, T aspect, T znear, T zfar) {
+    const T th = std::tan(fovy / T(2));
+    tmat4x4<T> r(T(0));
+    r[0][0] = T(1) / (aspect * th);
+    r[1][1] = T(1) / th;
+    r[2][2] = -(zfar + znear) / (zfar - znear);
+    r[2][3] = -T(1);
+    r[3][2] = -(T(2) * zfar * znear) / (zfar - znear);
+    return r;
 }
 
 template <typename T> inline T* value_ptr(tvec3<T>& v) { return &v.x; }

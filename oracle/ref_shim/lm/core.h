@@ -28,14 +28,40 @@ public:
         std::vector<double> nums;
         std::string str;
         bool is_str = false;
+        // a value read as a 4x4 matrix (16 numbers, column-major)
+        operator Mat4() const {
+            Mat4 m;
+            for (int c = 0; c < 4; c++) m[c] = Vec4(nums.at(4 * c), nums.at(4 * c + 1), nums.at(4 * c + 2), nums.at(4 * c + 3));
+            return m;
+        }
+    };
+    // one name-value pair of a brace-initialised object ({"eye", position_}, {"vfov", vfov_})
+    struct Item {
+        std::string name;
+        Entry e;
+        Item(const char* n, double v) : name(n), e{{v}, {}, false} {}
+        Item(const char* n, const Vec3& v) : name(n), e{{v.x, v.y, v.z}, {}, false} {}
     };
     std::map<std::string, Entry> entries;
+    Json() = default;
+    Json(std::initializer_list<Item> items) {
+        for (const auto& it : items) entries[it.name] = it.e;
+    }
     void set(const std::string& name, std::vector<double> v) { entries[name] = Entry{std::move(v), {}, false}; }
     void set_str(const std::string& name, const std::string& v) { entries[name] = Entry{{}, v, true}; }
     const Entry* find_entry(const std::string& name) const {
         auto it = entries.find(name);
         return it == entries.end() ? nullptr : &it->second;
     }
+    // lookup as the compiled sources write it: `auto it = prop.find(name); it != prop.end(); *it`
+    struct ConstIter {
+        std::map<std::string, Entry>::const_iterator it;
+        const Entry& operator*() const { return it->second; }
+        bool operator==(const ConstIter& o) const { return it == o.it; }
+        bool operator!=(const ConstIter& o) const { return it != o.it; }
+    };
+    ConstIter find(const std::string& name) const { return {entries.find(name)}; }
+    ConstIter end() const { return {entries.end()}; }
 };
 
 class Component {
@@ -45,6 +71,7 @@ public:
     virtual void construct(const Json& prop) { (void)prop; }
     virtual Component* underlying(const std::string& name) const { (void)name; return nullptr; }
     virtual void foreach_underlying(const ComponentVisitor& visitor) { (void)visitor; }
+    virtual Json underlying_value(const std::string& query = "") const { (void)query; return {}; }
 };
 
 LM_NAMESPACE_BEGIN(comp)

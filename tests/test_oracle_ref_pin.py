@@ -2,7 +2,8 @@
 
 oracle/_ref/liblmref.so is the reference's src/accel/accel_sahbvh.cpp,
 src/material/material_{diffuse,glossy,glass,mirror}.cpp, src/light/light_{area,envconst,point,
-directional}.cpp, include/lm/math.h and include/lm/surface.h, compiled unmodified from its sources
+directional}.cpp, src/camera/camera_pinhole.cpp, include/lm/math.h and include/lm/surface.h,
+compiled unmodified from its sources
 (oracle/Makefile `ref`, oracle/ref.py) against stand-in headers for glm's arithmetic and the few
 lm core names they use. Where those sources are present the tests compare the oracle's fp64
 restatement with that library directly; everywhere, they compare it with the hit fixtures the
@@ -13,7 +14,7 @@ hit/miss decisions: the restatement must reproduce the reference's Möller–Tru
 (accel_sahbvh.cpp:58-75), its full-sort SAH build (:127-267, including the split chosen among
 equal costs), its traversal order and "later triangle wins" ties (:269-299), the slab test
 (math.h:143-158), the scene flattening with group transforms, the math helpers, Dist2 and the
-Rng, every material query and the lights' direct and emission sampling.
+Rng, every material query, the lights' direct and emission sampling and the pinhole camera.
 """
 import os
 
@@ -314,3 +315,28 @@ def test_lights_match_reference(ref_mod, oracle_mod, key, params):
     b = O.light_query(rec)
     assert a[:, 0].sum() > 1000 and a[:, 20].sum() == n
     assert _same_bits(a, b), f"{key}: rows {np.nonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).all(1))[0][:5]}"
+
+
+@pytest.mark.parametrize("params", [
+    [0.0, 4.0, 15.0, 0.0, 0.6, 0.0, 0, 1, 0, 40.0, 16 / 9],
+    [0.5, 0.5, 2.6, 0.5, 0.5, 0.0, 0, 1, 0, 30.0, 1.0],
+    [1.0, -2.0, 0.5, -0.3, 0.4, 0.2, 0.1, 0.2, 1.0, 75.0, 0.5],
+])
+def test_camera_matches_reference(ref_mod, oracle_mod, params):
+    """camera_pinhole.cpp: primary_ray, raster_position (inside, outside and behind the frustum),
+    pdf_direction, eval, and the connection toward a scene point (sample_direct with its
+    pdf_direct), bit for bit."""
+    rng = np.random.default_rng(17)
+    n = 20000
+    rec = np.zeros((n, 11))
+    rec[:, 0:2] = rng.random((n, 2))
+    rec[:8, 0:2] = [[0, 0], [1, 1], [0, 1], [1, 0], [0.5, 0.5], [1e-300, 0.5], [0.5, 1 - 1e-16], [0.25, 0.75]]
+    wo = rng.normal(size=(n, 3))
+    rec[:, 2:5] = wo / np.linalg.norm(wo, axis=1, keepdims=True)
+    rec[:, 5:8] = rng.uniform(-5, 5, (n, 3))
+    nn = rng.normal(size=(n, 3))
+    rec[:, 8:11] = nn / np.linalg.norm(nn, axis=1, keepdims=True)
+    a = ref_mod.camera_query(params, rec)
+    b = oracle_mod.camera_query(params, rec)
+    assert a[:, 6].sum() > 100 and a[:, 13].sum() > 1000
+    assert _same_bits(a, b), f"rows {np.nonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).all(1))[0][:5]}"
