@@ -1066,11 +1066,11 @@ struct Film {
         int x, y; raster_to_pixel(rp, x, y);
         add(data[size_t(y) * w + x], Px{double(c.x), double(c.y), double(c.z)});
     }
-    template <typename F> void splat_path(V2<F> rp, V3<F> c) {
+    // a path's total contribution c, squared into the second moment (the per-sample variance)
+    template <typename F> void add_m2(V2<F> rp, V3<F> c) {
+        if (!with_m2) return;
         int x, y; raster_to_pixel(rp, x, y);
-        const size_t i = size_t(y) * w + x;
-        add(data[i], Px{double(c.x), double(c.y), double(c.z)});
-        if (with_m2) add(m2[i], Px{double(c.x) * double(c.x), double(c.y) * double(c.y), double(c.z) * double(c.z)});
+        add(m2[size_t(y) * w + x], Px{double(c.x) * double(c.x), double(c.y) * double(c.y), double(c.z) * double(c.z)});
     }
 };
 
@@ -1154,7 +1154,7 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
         V3F throughput(F(1));
         V3F wi{};
         V2<F> raster_pos{};
-        V3F L(F(0));  // path contribution (pixel mode: every splat of a path lands on raster_pos)
+        V3F L(F(0));  // the path's total (pixel mode: every splat of a path lands on raster_pos), for m2
         bool have_rp = false;
 
         for (int nv = 1; nv < P.max_verts; nv++) {
@@ -1193,15 +1193,18 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
                     mis_w = balance_heuristic(p_light, p_bsdf);
                 }
                 const auto Cc = throughput * fs * sL->weight * mis_w;
-                if (pixel_mode) L += Cc; else film.splat(rp, Cc);
+                film.splat(rp, Cc);  // each contribution as it comes, as renderer_pt.cpp:190-191 does
+                L += Cc;
             }();
 
             // Direction sampling
             std::optional<DirectionSample<F>> s;
             if (nv == 1) {
-                // camera_pinhole.cpp:143-148 with the pixel-window jitter of renderer_pt.cpp:199-201
-                const double j0 = U(nv, 8);
+                // camera_pinhole.cpp:143-148 with the pixel-window jitter of renderer_pt.cpp:199-201.
+                // `Vec2(x+w*rng.u(), y+h*rng.u())` leaves the order of its two draws to the compiler;
+                // GCC (and MSVC) evaluate the arguments right to left, so y takes the first number.
                 const double j1 = U(nv, 9);
+                const double j0 = U(nv, 8);
                 const V2<F> ud(wx + ww * F(j0), wy + wh * F(j1));
                 U(nv, 10); U(nv, 11);
                 s = DirectionSample<F>{cam.primary_ray(ud).d, V3F(F(1))};
@@ -1239,7 +1242,8 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
                     mis_w = balance_heuristic(pdf_bsdf, pdf_light);
                 }
                 const auto Cc = throughput * fs * mis_w;
-                if (pixel_mode) L += Cc; else film.splat(raster_pos, Cc);
+                film.splat(raster_pos, Cc);
+                L += Cc;
             }();
 
             if (hit->geom.infinite) break;
@@ -1261,7 +1265,7 @@ void render_pt(const Scene<F>& scene, const PTParams& P, double* out, double* ou
             sp = *hit;
             comp = sc.comp;
         }
-        if (pixel_mode && have_rp) film.splat_path(raster_pos, L);
+        if (pixel_mode && have_rp) film.add_m2(raster_pos, L);
     }
 
     for (auto* r : rngs) delete r;

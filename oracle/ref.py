@@ -1,9 +1,9 @@
 """Oracle (test infrastructure only): ctypes wrapper of oracle/_ref/liblmref.so, the reference's
-own accel, material, light, camera and math code (src/accel/accel_sahbvh.cpp,
-src/material/material_{diffuse,glossy,glass,mirror}.cpp, src/light/light_{area,envconst,point,
-directional}.cpp, src/camera/camera_pinhole.cpp, include/lm/math.h, include/lm/surface.h)
-compiled unmodified by
-`make -C oracle ref`.
+own code compiled unmodified by `make -C oracle ref`: src/scene.cpp, src/accel/accel_sahbvh.cpp,
+src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,mirror}.cpp,
+src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
+src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_pt.cpp and the headers they
+include (math.h, surface.h, scene.h, path.h, ...).
 
 Only tests/ and tests/golden/make_ref_fixtures.py use it, to pin the CPU restatement (and,
 through committed fixtures, the CUDA path) to the reference itself. The library can be built only
@@ -25,7 +25,7 @@ _lib = None
 
 
 def sources_present() -> bool:
-    return os.path.exists(os.path.join(REF_ROOT, "src", "accel", "accel_sahbvh.cpp"))
+    return os.path.exists(os.path.join(REF_ROOT, "src", "renderer", "renderer_pt.cpp"))
 
 
 def build() -> str | None:
@@ -58,23 +58,26 @@ def lib() -> C.CDLL:
         L.lmref_scene_create.restype = vp
         L.lmref_scene_destroy.argtypes = [vp]
         L.lmref_scene_add_mesh.argtypes = [vp, fp, C.c_int, ip, C.c_int]
-        L.lmref_scene_primitive.argtypes = [vp, C.c_int]
+        L.lmref_scene_add_mesh_raw.argtypes = [vp, fp, C.c_int, fp, C.c_int, fp, C.c_int, ip, ip, ip, C.c_int]
+        L.lmref_scene_add_material.argtypes = [vp, C.c_char_p, dp]
+        L.lmref_scene_add_light.argtypes = [vp, C.c_char_p, dp, C.c_int]
+        L.lmref_scene_add_camera.argtypes = [vp, dp]
+        L.lmref_scene_add_film.argtypes = [vp, C.c_int, C.c_int]
+        L.lmref_scene_primitive_ex.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.lmref_scene_group.argtypes = [vp, dp]
         L.lmref_scene_add_child.argtypes = [vp, C.c_int, C.c_int]
-        L.lmref_accel_build.argtypes = [vp, C.c_char_p, dp]
+        L.lmref_scene_build.argtypes = [vp, dp]
         L.lmref_accel_intersect.argtypes = [vp, fp, C.c_longlong, dp, dp, ip, ip, lp, C.c_int]
-        L.lmref_math_eval.argtypes = [C.c_char_p, dp, C.c_longlong, dp]
-        L.lmref_dist2_eval.argtypes = [dp, C.c_int, C.c_int, C.c_longlong, dp, dp, dp, dp]
-        L.lmref_rng.argtypes = [C.c_int, C.c_int, C.c_longlong, dp]
+        L.lmref_render_pt.argtypes = [vp, C.c_int, C.c_longlong, C.c_int, C.c_uint, C.c_int, C.c_int, dp]
+        L.lmref_light_query.argtypes = [vp, C.c_int, dp, dp, C.c_longlong, dp]
         L.lmref_material_create.restype = vp
         L.lmref_material_create.argtypes = [C.c_char_p, dp]
         L.lmref_material_destroy.argtypes = [vp]
         L.lmref_material_query.argtypes = [vp, dp, C.c_longlong, dp]
-        L.lmref_light_create.restype = vp
-        L.lmref_light_create.argtypes = [vp, C.c_char_p, dp, C.c_int]
-        L.lmref_light_destroy.argtypes = [vp]
-        L.lmref_light_query.argtypes = [vp, dp, dp, C.c_longlong, dp]
         L.lmref_camera_query.argtypes = [dp, dp, C.c_longlong, dp]
+        L.lmref_math_eval.argtypes = [C.c_char_p, dp, C.c_longlong, dp]
+        L.lmref_dist2_eval.argtypes = [dp, C.c_int, C.c_int, C.c_longlong, dp, dp, dp, dp]
+        L.lmref_rng.argtypes = [C.c_int, C.c_int, C.c_longlong, dp]
         _lib = L
     return _lib
 
@@ -89,11 +92,21 @@ def _p(a, t):
     return a.ctypes.data_as(C.POINTER(t))
 
 
+def _prm(params, n=11):
+    prm = np.zeros(n)
+    prm[:len(params)] = params
+    return prm
+
+
 class RefScene:
-    """A scene graph for the reference's accel: node 0 is the root group."""
+    """One reference scene (scene::default over accel::sahbvh) with its assets; node 0 is the root
+    group. Mesh, material, light, camera and film methods return ids that primitive() takes."""
 
     def __init__(self):
         self.h = lib().lmref_scene_create()
+        if not self.h:
+            raise RuntimeError("reference: " + lib().lmref_last_error().decode())
+        self.films = {}
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -101,12 +114,40 @@ class RefScene:
             self.h = None
 
     def add_mesh(self, ps, fp) -> int:
+        """Positions and triangle indices only, for intersection (any size)."""
         ps = np.ascontiguousarray(ps, np.float32).reshape(-1, 3)
         fp = np.ascontiguousarray(fp, np.int32).reshape(-1, 3)
         return _chk(lib().lmref_scene_add_mesh(self.h, _p(ps, C.c_float), ps.shape[0], _p(fp, C.c_int), fp.shape[0]))
 
-    def primitive(self, mesh: int = -1) -> int:
-        return _chk(lib().lmref_scene_primitive(self.h, mesh))
+    def add_mesh_raw(self, ps, ns, fp, fn, ts=None, ft=None) -> int:
+        """mesh::raw with normals and texture coordinates, for rendering."""
+        ps = np.ascontiguousarray(ps, np.float32).reshape(-1, 3)
+        ns = np.ascontiguousarray(ns, np.float32).reshape(-1, 3)
+        ts = np.ascontiguousarray(ts if ts is not None else np.zeros((1, 2)), np.float32).reshape(-1, 2)
+        fp = np.ascontiguousarray(fp, np.int32).reshape(-1)
+        fn = np.ascontiguousarray(fn, np.int32).reshape(-1)
+        ft = np.ascontiguousarray(ft if ft is not None else np.zeros_like(fp), np.int32).reshape(-1)
+        return _chk(lib().lmref_scene_add_mesh_raw(self.h, _p(ps, C.c_float), ps.shape[0], _p(ns, C.c_float), ns.shape[0],
+                                                   _p(ts, C.c_float), ts.shape[0], _p(fp, C.c_int), _p(ft, C.c_int),
+                                                   _p(fn, C.c_int), fp.size))
+
+    def material(self, key: str, params) -> int:
+        return _chk(lib().lmref_scene_add_material(self.h, key.encode(), _p(_prm(params), C.c_double)))
+
+    def light(self, key: str, params, mesh: int = -1) -> int:
+        return _chk(lib().lmref_scene_add_light(self.h, key.encode(), _p(_prm(params), C.c_double), mesh))
+
+    def camera(self, position, center, up, vfov, aspect) -> int:
+        prm = _prm(list(position) + list(center) + list(up) + [vfov, aspect])
+        return _chk(lib().lmref_scene_add_camera(self.h, _p(prm, C.c_double)))
+
+    def film(self, w: int, h: int) -> int:
+        f = _chk(lib().lmref_scene_add_film(self.h, w, h))
+        self.films[f] = (w, h)
+        return f
+
+    def primitive(self, mesh: int = -1, material: int = -1, light: int = -1, camera: int = -1) -> int:
+        return _chk(lib().lmref_scene_primitive_ex(self.h, mesh, material, light, camera))
 
     def group(self, m4=None) -> int:
         """m4: 4x4 (row-major numpy, as the lightmetrica API takes it) or None."""
@@ -118,9 +159,9 @@ class RefScene:
     def add_child(self, parent: int, child: int) -> None:
         _chk(lib().lmref_scene_add_child(self.h, parent, child))
 
-    def build(self, key: str = "accel::sahbvh") -> float:
+    def build(self) -> float:
         s = C.c_double()
-        _chk(lib().lmref_accel_build(self.h, key.encode(), C.byref(s)))
+        _chk(lib().lmref_scene_build(self.h, C.byref(s)))
         return s.value
 
     def intersect(self, rays: np.ndarray, nthreads: int = 0):
@@ -134,19 +175,87 @@ class RefScene:
                                          _p(prim, C.c_int), _p(face, C.c_int), _p(tri, C.c_longlong), nthreads))
         return t, uv, tri
 
+    def render_pt(self, film: int, samples: int, max_verts: int, seed: int = 0, sampling_mode: str = "mis",
+                  primary_mode: str = "pixel") -> np.ndarray:
+        """The reference's renderer::pt on one thread (Rng seeded `seed`), scheduler::spp::sample
+        (pixel: `samples` spp) or scheduler::spi::sample (image: `samples` samples). Returns the
+        film, (h, w, 3), row 0 at the bottom, as film_bitmap holds it."""
+        w, h = self.films[film]
+        out = np.zeros((h, w, 3))
+        sm = {"naive": 0, "nee": 1, "mis": 2}[sampling_mode]
+        pm = {"pixel": 0, "image": 1}[primary_mode]
+        _chk(lib().lmref_render_pt(self.h, film, samples, max_verts, seed & 0xFFFFFFFF, sm, pm, _p(out, C.c_double)))
+        return out
 
-def from_parts(parts: dict) -> RefScene:
-    """The reference accel's scene from a plain scene description (synthetic.spheres_parts), with
-    the node order oracle.from_parts uses (camera primitive first, then the primitives)."""
+    def light_query(self, light: int, m4, rec: np.ndarray) -> np.ndarray:
+        """Light asset `light` (built scene: it holds the scene bound) under the 4x4 transform m4
+        (row-major), over records of 14 doubles: p n gn of the shading point, up upc ud. Returns
+        n x 33: sample_direct (valid, geomL p n wo, wo, weight), its pdf_direct, eval, sample_ray
+        (valid, geomL p n, wo, weight)."""
+        cm = np.ascontiguousarray(np.asarray(m4, np.float64).T).reshape(16)
+        rec = np.ascontiguousarray(rec, np.float64)
+        out = np.zeros((rec.shape[0], 33))
+        _chk(lib().lmref_light_query(self.h, light, _p(cm, C.c_double), _p(rec, C.c_double), rec.shape[0],
+                                     _p(out, C.c_double)))
+        return out
+
+
+def from_parts(parts: dict, renderable: bool = False) -> RefScene:
+    """The reference's scene from a plain scene description (synthetic.spheres_parts), with the node
+    order oracle.from_parts uses (camera primitive first, then the primitives). renderable=False
+    keeps positions only (any size, intersection only); True builds mesh::raw meshes, materials,
+    lights and the camera, for renderer::pt."""
     S = RefScene()
-    S.add_child(0, S.primitive(-1))
+    c = parts["camera"]
+    cam = S.camera(c["position"], c["center"], c["up"], c["vfov"], c["aspect"]) if renderable else -1
+    S.add_child(0, S.primitive(camera=cam))
     for pr in parts["primitives"]:
-        me = -1
+        me = ma = li = -1
         if pr["mesh"] is not None:
-            ps, _, fp, _ = pr["mesh"]
-            me = S.add_mesh(ps, fp)
-        S.add_child(0, S.primitive(me))
+            ps, ns, fp, fn = pr["mesh"]
+            me = S.add_mesh_raw(ps, ns, fp, fn) if renderable else S.add_mesh(ps, np.asarray(fp).reshape(-1, 3))
+        if renderable and pr["material"] is not None:
+            kind, m = pr["material"]
+            params = {"diffuse": lambda: list(m["Kd"]), "glossy": lambda: list(m["Ks"]) + [m["ax"], m["ay"]],
+                      "glass": lambda: [m["Ni"]], "mirror": lambda: []}[kind]()
+            ma = S.material("material::" + kind, params)
+        if renderable and pr["light"] is not None:
+            kind, L = pr["light"]
+            li = S.light("light::area", L["Ke"], me) if kind == "area" else S.light("light::envconst", L["Le"])
+        if me < 0 and ma < 0 and li < 0:
+            continue
+        S.add_child(0, S.primitive(me, ma, li, -1))
     return S
+
+
+def material_query(key: str, params, rec: np.ndarray) -> np.ndarray:
+    """Every Material query of the reference's `key` component (diffuse Kd; glossy Ks, ax, ay;
+    glass Ni; mirror none) over records of 26 doubles: p n gn t wi wo comp trans_dir(0 LE, 1 EL)
+    eval_delta ud udc uc. Returns n x 18: eval[3], pdf_direction, sample_direction (valid, wo[3],
+    weight[3]), sample_component (comp, weight), pdf_component, reflectance[3],
+    is_specular_component."""
+    m = lib().lmref_material_create(key.encode(), _p(_prm(params), C.c_double))
+    if not m:
+        raise RuntimeError("reference: " + lib().lmref_last_error().decode())
+    try:
+        rec = np.ascontiguousarray(rec, np.float64)
+        out = np.zeros((rec.shape[0], 18))
+        _chk(lib().lmref_material_query(m, _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
+        return out
+    finally:
+        lib().lmref_material_destroy(m)
+
+
+def camera_query(params, rec: np.ndarray) -> np.ndarray:
+    """The reference's camera::pinhole (position, center, up, vfov, aspect) over records of 11
+    doubles: rp[2], wo[3], a scene point p[3] n[3]. Returns n x 21: primary_ray(rp) (o, d),
+    raster_position(wo) (valid, rp), pdf_direction(wo), eval(wo), sample_direct toward the point
+    (valid, wo, weight) and its pdf_direct."""
+    prm = np.ascontiguousarray(params, np.float64)
+    rec = np.ascontiguousarray(rec, np.float64)
+    out = np.zeros((rec.shape[0], 21))
+    _chk(lib().lmref_camera_query(_p(prm, C.c_double), _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
+    return out
 
 
 def math_eval(fn: str, inp: np.ndarray, out_width: int) -> np.ndarray:
@@ -169,60 +278,69 @@ def dist2_eval(v: np.ndarray, uvq: np.ndarray, u4: np.ndarray):
     return pdf, smp
 
 
-def material_query(key: str, params, rec: np.ndarray) -> np.ndarray:
-    """Every Material query of the reference's `key` component (diffuse Kd; glossy Ks, ax, ay;
-    glass Ni; mirror none) over records of 26 doubles: p n gn t wi wo comp trans_dir(0 LE, 1 EL)
-    eval_delta ud udc uc. Returns n x 18: eval[3], pdf_direction, sample_direction (valid, wo[3],
-    weight[3]), sample_component (comp, weight), pdf_component, reflectance[3],
-    is_specular_component."""
-    prm = np.zeros(8)
-    prm[:len(params)] = params
-    m = lib().lmref_material_create(key.encode(), _p(prm, C.c_double))
-    if not m:
-        raise RuntimeError("reference: " + lib().lmref_last_error().decode())
-    try:
-        rec = np.ascontiguousarray(rec, np.float64)
-        out = np.zeros((rec.shape[0], 18))
-        _chk(lib().lmref_material_query(m, _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
-        return out
-    finally:
-        lib().lmref_material_destroy(m)
-
-
-def light_query(scene: RefScene, key: str, params, mesh: int, m4, rec: np.ndarray) -> np.ndarray:
-    """The reference's `key` light (area: Ke over the scene's mesh `mesh`; envconst: Le; point:
-    Le, position; directional: Le, direction), bounded by the scene's transformed triangles, under
-    the 4x4 transform m4 (row-major), over records of 14 doubles: p n gn of the shading point, up
-    upc ud. Returns n x 33: sample_direct (valid, geomL p n wo, wo, weight), its pdf_direct, eval,
-    sample_ray (valid, geomL p n, wo, weight)."""
-    prm = np.zeros(8)
-    prm[:len(params)] = params
-    h = lib().lmref_light_create(scene.h, key.encode(), _p(prm, C.c_double), mesh)
-    if not h:
-        raise RuntimeError("reference: " + lib().lmref_last_error().decode())
-    try:
-        cm = np.ascontiguousarray(np.asarray(m4, np.float64).T).reshape(16)
-        rec = np.ascontiguousarray(rec, np.float64)
-        out = np.zeros((rec.shape[0], 33))
-        _chk(lib().lmref_light_query(h, _p(cm, C.c_double), _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
-        return out
-    finally:
-        lib().lmref_light_destroy(h)
-
-
-def camera_query(params, rec: np.ndarray) -> np.ndarray:
-    """The reference's camera::pinhole (position, center, up, vfov, aspect) over records of 11
-    doubles: rp[2], wo[3], a scene point p[3] n[3]. Returns n x 21: primary_ray(rp) (o, d),
-    raster_position(wo) (valid, rp), pdf_direction(wo), eval(wo), sample_direct toward the point
-    (valid, wo, weight) and its pdf_direct."""
-    prm = np.ascontiguousarray(params, np.float64)
-    rec = np.ascontiguousarray(rec, np.float64)
-    out = np.zeros((rec.shape[0], 21))
-    _chk(lib().lmref_camera_query(_p(prm, C.c_double), _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
-    return out
-
-
 def rng(seed: int, n: int, as_float: bool = False) -> np.ndarray:
     out = np.zeros(n)
     _chk(lib().lmref_rng(seed, 1 if as_float else 0, n, _p(out, C.c_double)))
     return out
+
+
+def from_lm_scene(scene) -> RefScene:
+    """The reference's scene from a `lightmetrica` scene graph (the GPU mirror's SceneDefault), node
+    for node as oracle.from_lm_scene rebuilds it, for the components compiled into the library
+    (mesh::raw, diffuse / glossy / glass / mirror, area / envconst / point / directional lights,
+    the pinhole camera). Anything else raises NotImplementedError."""
+    S = RefScene()
+    mesh_id, mat_id, light_id, cam_id = {}, {}, {}, {}
+
+    def mesh_of(m):
+        if id(m) not in mesh_id:
+            mesh_id[id(m)] = S.add_mesh_raw(m.ps, m.ns, m.fp, m.fn, getattr(m, "ts", None), getattr(m, "ft", None))
+        return mesh_id[id(m)]
+
+    node_map = {0: 0}
+    for i, n in enumerate(scene.nodes):
+        if i == 0:
+            continue
+        if n["type"] == "group":
+            if n["instanced"]:
+                raise NotImplementedError("instance groups")
+            node_map[i] = S.group(n["transform"])
+            continue
+        me = mesh_of(n["mesh"]) if n["mesh"] is not None else -1
+        ma = -1
+        if n["material"] is not None:
+            m = n["material"]
+            if id(m) not in mat_id:
+                params = {"material::diffuse": lambda: list(m.Kd), "material::glossy": lambda: list(m.Ks) + [m.ax, m.ay],
+                          "material::glass": lambda: [m.Ni], "material::mirror": lambda: []}
+                if m.key_name not in params or getattr(m, "mapKd", None) is not None:
+                    raise NotImplementedError(m.key_name)
+                mat_id[id(m)] = S.material(m.key_name, params[m.key_name]())
+            ma = mat_id[id(m)]
+        li = -1
+        if n["light"] is not None:
+            L = n["light"]
+            if id(L) not in light_id:
+                if L.key_name == "light::area":
+                    light_id[id(L)] = S.light("light::area", L.Ke, mesh_of(L.mesh))
+                elif L.key_name == "light::envconst":
+                    light_id[id(L)] = S.light("light::envconst", L.Le)
+                elif L.key_name == "light::point":
+                    light_id[id(L)] = S.light("light::point", list(L.Le) + list(L.position))
+                elif L.key_name == "light::directional":
+                    light_id[id(L)] = S.light("light::directional", list(L.Le) + list(L.direction))
+                else:
+                    raise NotImplementedError(L.key_name)
+            li = light_id[id(L)]
+        ca = -1
+        if n["camera"] is not None:
+            c = n["camera"]
+            if id(c) not in cam_id:
+                cam_id[id(c)] = S.camera(c.position, c.center, c.up, c.vfov, c.aspect)
+            ca = cam_id[id(c)]
+        node_map[i] = S.primitive(me, ma, li, ca)
+    for i, n in enumerate(scene.nodes):
+        if n["type"] == "group":
+            for c in n["children"]:
+                S.add_child(node_map[i], node_map[c])
+    return S

@@ -1,16 +1,17 @@
 // Oracle (test infrastructure only): C entry points into the reference's own code, compiled from
-// its sources (src/accel/accel_sahbvh.cpp, src/material/material_{diffuse,glossy,glass,mirror}.cpp,
+// its sources, unmodified, into oracle/_ref/liblmref.so by oracle/Makefile's `ref` target:
+// src/scene.cpp, src/accel/accel_sahbvh.cpp, src/mesh/mesh_raw.cpp,
+// src/material/material_{diffuse,glossy,glass,mirror}.cpp,
 // src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
-// include/lm/math.h and
-// include/lm/surface.h, unmodified) into
-// oracle/_ref/liblmref.so by oracle/Makefile's `ref` target. Tests call them through ctypes to
-// check the CPU restatement (liblmoracle.so) against the reference itself, and
-// tests/golden/make_ref_fixtures.py records reference hits that the GPU tests compare with.
+// src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_pt.cpp, and the headers they
+// include (math.h, surface.h, scene.h, path.h, ...). Tests call them through ctypes
+// (oracle/ref.py) to check the CPU restatement (liblmoracle.so) against the reference itself, and
+// tests/golden/make_ref_fixtures.py records reference outputs that the GPU tests compare with.
 //
-// The scene here is the part of the reference's Scene_ that an accel's build sees: a node graph
-// whose node 0 is the root group, group nodes with optional local transforms, and primitive nodes
-// holding a mesh::raw-style indexed triangle mesh. Traversal follows src/scene.cpp:216-230
-// (depth first, children in insertion order, global = parent global * local).
+// A handle owns one reference scene (scene::default over accel::sahbvh) and the assets its nodes
+// refer to, created through the component factories under locators "$.h<handle>.<name>", as the
+// reference's user API does. The parallel loop the schedulers and the film call is the
+// reference's OpenMP loop with one thread: indices in order, thread id 0.
 #include <pch.h>
 #include <lm/core.h>
 #include <lm/accel.h>
@@ -19,6 +20,10 @@
 #include <lm/material.h>
 #include <lm/light.h>
 #include <lm/camera.h>
+#include <lm/film.h>
+#include <lm/renderer.h>
+#include <lm/parallel.h>
+#include <lm/progress.h>
 
 #include <chrono>
 #include <cstring>
@@ -26,11 +31,37 @@
 
 using namespace lm;
 
+// ------------------------------------------------------------------------------------------------
+// The reference's parallel and progress entry points (src/parallel.cpp, src/progress.cpp dispatch
+// to configurable backends): a sequential loop with thread id 0, and no progress reports.
+
+LM_NAMESPACE_BEGIN(LM_NAMESPACE)
+LM_NAMESPACE_BEGIN(parallel)
+void init(const std::string&, const Json&) {}
+void shutdown() {}
+int num_threads() { return 1; }
+bool main_thread() { return true; }
+void foreach(long long num_samples, const ParallelProcessFunc& process_func, const ProgressUpdateFunc& progress_func) {
+    for (long long i = 0; i < num_samples; i++) process_func(i, 0);
+    if (progress_func) progress_func(num_samples);
+}
+LM_NAMESPACE_END(parallel)
+LM_NAMESPACE_BEGIN(progress)
+void init(const std::string&, const Json&) {}
+void shutdown() {}
+void start(ProgressMode, long long, double) {}
+void end() {}
+void update(long long) {}
+void update_time(Float) {}
+LM_NAMESPACE_END(progress)
+LM_NAMESPACE_END(LM_NAMESPACE)
+
 namespace {
 
 thread_local std::string g_err;
 
-// src/mesh/mesh_raw.cpp:70-85: triangles are three indexed positions per face.
+// An indexed triangle mesh for scenes too large for a JSON property list (the accel's build reads
+// triangles only): the triangle iteration of src/mesh/mesh_raw.cpp:70-85.
 class RawMesh final : public Mesh {
 public:
     std::vector<Vec3> ps;
@@ -39,45 +70,53 @@ public:
         for (int fi = 0; fi < int(fs.size()) / 3; fi++) f(fi, triangle_at(fi));
     }
     Tri triangle_at(int face) const override {
-        Tri t;
+        Tri t{};
         t.p1.p = ps.at(fs.at(3 * face));
         t.p2.p = ps.at(fs.at(3 * face + 1));
         t.p3.p = ps.at(fs.at(3 * face + 2));
         return t;
     }
+    InterpolatedPoint surface_point(int, Vec2) const override {
+        throw std::runtime_error("RawMesh holds positions only; render with mesh::raw meshes");
+    }
     int num_triangles() const override { return int(fs.size()) / 3; }
 };
 
-class GraphScene final : public Scene {
-public:
-    std::vector<SceneNode> nodes;
-    std::vector<std::unique_ptr<RawMesh>> meshes;
-    std::vector<int> parents;  // each node is attached at most once
-    std::unique_ptr<Accel> accel;
-    std::vector<long long> tri_offset;  // per node: first flattened triangle, -1 for non-meshes
+struct Handle {
+    int id = 0;
+    std::vector<std::unique_ptr<Component>> assets;  // owned; registered by locator
+    std::vector<std::string> locs;
+    std::vector<int> mesh_assets;                    // mesh id -> asset index
+    Scene* scene = nullptr;
+    Accel* accel = nullptr;
+    int scene_asset = -1;
+    std::string default_material;
+    std::vector<long long> tri_offset;               // per node: first flattened triangle
 
-    GraphScene() {
-        SceneNode root{};
-        root.type = SceneNodeType::Group;
-        root.index = 0;
-        nodes.push_back(root);
-        parents.push_back(-1);
+    ~Handle() {
+        for (const auto& l : locs) refshim::remove_named(l);
     }
-    void traverse_primitive_nodes(const NodeTraverseFunc& traverse_func) const override {
-        std::function<void(int, Mat4)> visit = [&](int index, Mat4 global_transform) {
-            const auto& node = nodes.at(index);
-            traverse_func(node, global_transform);
-            if (node.type == SceneNodeType::Group) {
-                const auto M = node.group.local_transform ? global_transform * *node.group.local_transform
-                                                          : global_transform;
-                for (int child : node.group.children) visit(child, M);
-            }
-        };
-        visit(0, Mat4(1_f));
+    std::string loc(const std::string& name) const { return "$.h" + std::to_string(id) + "." + name; }
+    int add(const std::string& name, std::unique_ptr<Component> c) {
+        if (!c) throw std::invalid_argument("no component registered for " + name);
+        const auto l = loc(name);
+        refshim::add_named(l, c.get());
+        locs.push_back(l);
+        assets.push_back(std::move(c));
+        return int(assets.size()) - 1;
     }
+    template <typename T> int create(const std::string& key, const std::string& name, const Json& prop) {
+        auto c = comp::create<Component>(key, loc(name), prop);
+        if (!c || !dynamic_cast<T*>(c.get())) throw std::invalid_argument("cannot create " + key);
+        return add(name, std::move(c));
+    }
+    std::string next_name() const { return "asset" + std::to_string(assets.size()); }
+    const std::string& asset_loc(int i) const { return locs.at(size_t(i)); }
 };
 
-GraphScene* S(void* p) { return static_cast<GraphScene*>(p); }
+int g_next_handle = 0;
+
+Handle* H(void* p) { return static_cast<Handle*>(p); }
 
 template <typename Fn> int guarded(Fn&& fn) {
     try {
@@ -90,6 +129,24 @@ template <typename Fn> int guarded(Fn&& fn) {
 
 Vec3 v3(const double* p) { return Vec3(p[0], p[1], p[2]); }
 void put3(double* o, Vec3 v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; }
+Json arr(const float* v, long long n) {
+    Json j = Json::array();
+    for (long long i = 0; i < n; i++) j.push_back(Json(double(v[i])));
+    return j;
+}
+Json arr(const int* v, long long n) {
+    Json j = Json::array();
+    for (long long i = 0; i < n; i++) j.push_back(Json(v[i]));
+    return j;
+}
+Mat4 mat4(const double* m16) {
+    Mat4 M;
+    for (int c = 0; c < 4; c++) M[c] = Vec4(m16[4 * c], m16[4 * c + 1], m16[4 * c + 2], m16[4 * c + 3]);
+    return M;
+}
+Json camera_prop(const double* prm) {
+    return Json{{"position", v3(prm)}, {"center", v3(prm + 3)}, {"up", v3(prm + 6)}, {"vfov", prm[9]}, {"aspect", prm[10]}};
+}
 
 }  // namespace
 
@@ -97,83 +154,160 @@ extern "C" {
 
 const char* lmref_last_error() { return g_err.c_str(); }
 
-void* lmref_scene_create() { return new GraphScene(); }
-void lmref_scene_destroy(void* p) { delete S(p); }
+// ------------------------------------------------------------------------------------------------
+// Scene and assets
 
-// Mesh from float positions (nps x 3) and position indices (nf x 3); returns its id.
+void* lmref_scene_create() {
+    try {
+        auto h = std::make_unique<Handle>();
+        h->id = g_next_handle++;
+        const int a = h->create<Accel>("accel::sahbvh", "accel", Json::object());
+        h->accel = dynamic_cast<Accel*>(h->assets[a].get());
+        h->scene_asset = h->create<Scene>("scene::default", "scene", Json{{"accel", h->asset_loc(a)}});
+        h->scene = dynamic_cast<Scene*>(h->assets[h->scene_asset].get());
+        const int m = h->create<Material>("material::diffuse", "default_material", Json{{"Kd", Vec3(1_f)}});
+        h->default_material = h->asset_loc(m);
+        return h.release();
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return nullptr;
+    }
+}
+void lmref_scene_destroy(void* p) { delete H(p); }
+
+// Mesh from float positions (nps x 3) and position indices (nf x 3), for the accel only.
 int lmref_scene_add_mesh(void* p, const float* ps, int nps, const int* fp, int nf) {
     return guarded([&] {
+        auto* h = H(p);
         auto m = std::make_unique<RawMesh>();
-        m->ps.reserve(nps);
+        m->ps.reserve(size_t(nps));
         for (int i = 0; i < nps; i++) m->ps.emplace_back(Float(ps[3 * i]), Float(ps[3 * i + 1]), Float(ps[3 * i + 2]));
         m->fs.assign(fp, fp + 3 * size_t(nf));
         for (int i : m->fs)
             if (i < 0 || i >= nps) throw std::out_of_range("face index out of range");
-        S(p)->meshes.push_back(std::move(m));
-        return int(S(p)->meshes.size()) - 1;
+        const int id = int(h->mesh_assets.size());
+        const auto name = "mesh" + std::to_string(id);
+        m->lmref_set_ids("mesh::positions", h->loc(name));
+        h->mesh_assets.push_back(h->add(name, std::move(m)));
+        return id;
     });
 }
 
-int lmref_scene_primitive(void* p, int mesh) {
+// mesh::raw (src/mesh/mesh_raw.cpp) from its properties: ps, ns, ts and per-corner indices.
+int lmref_scene_add_mesh_raw(void* p, const float* ps, int nps, const float* ns, int nns, const float* ts, int nts,
+                             const int* fp, const int* ft, const int* fn, int ncorners) {
     return guarded([&] {
-        auto* s = S(p);
-        SceneNode n{};
-        n.type = SceneNodeType::Primitive;
-        n.index = int(s->nodes.size());
-        n.primitive.mesh = mesh >= 0 ? s->meshes.at(mesh).get() : nullptr;
-        s->nodes.push_back(n);
-        s->parents.push_back(-1);
-        return n.index;
+        auto* h = H(p);
+        Json fs = Json::object();
+        fs["p"] = arr(fp, ncorners);
+        fs["t"] = arr(ft, ncorners);
+        fs["n"] = arr(fn, ncorners);
+        Json prop = Json::object();
+        prop["ps"] = arr(ps, 3LL * nps);
+        prop["ns"] = arr(ns, 3LL * nns);
+        prop["ts"] = arr(ts, 2LL * nts);
+        prop["fs"] = fs;
+        const int id = int(h->mesh_assets.size());
+        h->mesh_assets.push_back(h->create<Mesh>("mesh::raw", "mesh" + std::to_string(id), prop));
+        return id;
     });
 }
 
-// Group node; m16 (column-major) or null for a group without a local transform.
-int lmref_scene_group(void* p, const double* m16) {
+// Materials: diffuse Kd[3]; glossy Ks[3], ax, ay; glass Ni; mirror none. Returns an asset id.
+int lmref_scene_add_material(void* p, const char* key, const double* prm) {
     return guarded([&] {
-        auto* s = S(p);
-        SceneNode n{};
-        n.type = SceneNodeType::Group;
-        n.index = int(s->nodes.size());
-        if (m16) {
-            Mat4 M;
-            for (int c = 0; c < 4; c++) M[c] = Vec4(m16[4 * c], m16[4 * c + 1], m16[4 * c + 2], m16[4 * c + 3]);
-            n.group.local_transform = M;
+        auto* h = H(p);
+        const std::string k(key);
+        Json j = Json::object();
+        if (k == "material::diffuse") j["Kd"] = Vec3(prm[0], prm[1], prm[2]);
+        else if (k == "material::glossy") { j["Ks"] = Vec3(prm[0], prm[1], prm[2]); j["ax"] = prm[3]; j["ay"] = prm[4]; }
+        else if (k == "material::glass") j["Ni"] = prm[0];
+        return h->create<Material>(k, h->next_name(), j);
+    });
+}
+
+// Lights: area Ke[3] over mesh `mesh`; envconst Le[3]; point Le[3], position[3]; directional
+// Le[3], direction[3]. Returns an asset id.
+int lmref_scene_add_light(void* p, const char* key, const double* prm, int mesh) {
+    return guarded([&] {
+        auto* h = H(p);
+        const std::string k(key);
+        Json j = Json::object();
+        if (k == "light::area") {
+            j["Ke"] = Vec3(prm[0], prm[1], prm[2]);
+            j["mesh"] = h->asset_loc(h->mesh_assets.at(size_t(mesh)));
+        } else {
+            j["Le"] = Vec3(prm[0], prm[1], prm[2]);
+            if (k == "light::point") j["position"] = Vec3(prm[3], prm[4], prm[5]);
+            if (k == "light::directional") j["direction"] = Vec3(prm[3], prm[4], prm[5]);
         }
-        s->nodes.push_back(n);
-        s->parents.push_back(-1);
-        return n.index;
+        return h->create<Light>(k, h->next_name(), j);
     });
+}
+
+// camera::pinhole: position[3], center[3], up[3], vfov, aspect. Returns an asset id.
+int lmref_scene_add_camera(void* p, const double* prm) {
+    return guarded([&] { return H(p)->create<Camera>("camera::pinhole", H(p)->next_name(), camera_prop(prm)); });
+}
+
+// film::bitmap of w x h. Returns an asset id.
+int lmref_scene_add_film(void* p, int w, int hgt) {
+    return guarded([&] { return H(p)->create<Film>("film::bitmap", H(p)->next_name(), Json{{"w", w}, {"h", hgt}}); });
+}
+
+// Primitive node (Scene::create_primitive_node, scene.cpp:71-126) over a mesh id and material,
+// light and camera asset ids (-1 = none). A mesh without a material gets a white diffuse one; a
+// node with nothing gets a camera (the node a scene's camera primitive takes).
+int lmref_scene_primitive_ex(void* p, int mesh, int material, int light, int camera) {
+    return guarded([&] {
+        auto* h = H(p);
+        Json j = Json::object();
+        if (mesh >= 0) {
+            j["mesh"] = h->asset_loc(h->mesh_assets.at(size_t(mesh)));
+            j["material"] = material >= 0 ? h->asset_loc(material) : h->default_material;
+        } else if (material >= 0) {
+            j["material"] = h->asset_loc(material);
+        }
+        if (light >= 0) j["light"] = h->asset_loc(light);
+        if (camera >= 0) j["camera"] = h->asset_loc(camera);
+        if (mesh < 0 && material < 0 && light < 0 && camera < 0) {
+            static const double cam[11] = {0, 0, 1, 0, 0, 0, 0, 1, 0, 30, 1};
+            j["camera"] = h->asset_loc(h->create<Camera>("camera::pinhole", h->next_name(), camera_prop(cam)));
+        }
+        return h->scene->create_primitive_node(j);
+    });
+}
+int lmref_scene_primitive(void* p, int mesh) { return lmref_scene_primitive_ex(p, mesh, -1, -1, -1); }
+
+// Group node; m16 (column-major) or null for an identity transform.
+int lmref_scene_group(void* p, const double* m16) {
+    return guarded([&] { return H(p)->scene->create_group_node(m16 ? mat4(m16) : Mat4(1_f)); });
 }
 
 int lmref_scene_add_child(void* p, int parent, int child) {
     return guarded([&] {
-        auto* s = S(p);
-        if (s->nodes.at(parent).type != SceneNodeType::Group) throw std::invalid_argument("parent is not a group");
-        if (child <= 0 || s->parents.at(child) >= 0) throw std::invalid_argument("node already attached");
-        s->parents[child] = parent;
-        s->nodes[parent].group.children.push_back(child);
+        auto* h = H(p);
+        if (parent < 0 || parent >= h->scene->num_nodes() || child <= 0 || child >= h->scene->num_nodes())
+            throw std::out_of_range("node index out of range");
+        h->scene->add_child(parent, child);
         return 0;
     });
 }
 
-// Builds the accel registered under `key` (e.g. "accel::sahbvh") over the scene.
-int lmref_accel_build(void* p, const char* key, double* secs) {
+// Scene::build (scene.cpp:274-316): light transforms, the scene bound handed to the lights, the
+// accel's build. Records each mesh node's first flattened triangle (traversal order).
+int lmref_scene_build(void* p, double* secs) {
     return guarded([&] {
-        auto* s = S(p);
-        std::unique_ptr<Component> c(refshim::create(key));
-        auto* a = dynamic_cast<Accel*>(c.get());
-        if (!a) throw std::invalid_argument(std::string("no accel registered as ") + key);
-        c.release();
-        s->accel.reset(a);
-        s->tri_offset.assign(s->nodes.size(), -1);
+        auto* h = H(p);
+        h->tri_offset.assign(size_t(h->scene->num_nodes()), -1);
         long long off = 0;
-        s->traverse_primitive_nodes([&](const SceneNode& n, Mat4) {
+        h->scene->traverse_primitive_nodes([&](const SceneNode& n, Mat4) {
             if (n.type != SceneNodeType::Primitive || !n.primitive.mesh) return;
-            s->tri_offset[n.index] = off;
+            h->tri_offset[size_t(n.index)] = off;
             off += n.primitive.mesh->num_triangles();
         });
         const auto t0 = std::chrono::steady_clock::now();
-        s->accel->build(*s);
+        h->scene->build();
         if (secs) *secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return 0;
     });
@@ -183,8 +317,7 @@ int lmref_accel_build(void* p, const char* key, double* secs) {
 // v, the primitive node, the face and the flattened triangle index (traversal order; -1 = miss).
 int lmref_accel_intersect(void* p, const float* rays, long long n, double* t, double* uv, int* prim, int* face,
                           long long* tri, int nthreads) {
-    auto* s = S(p);
-    if (!s->accel) { g_err = "accel not built"; return -1; }
+    auto* h = H(p);
     int rc = 0;
     const int nth = nthreads > 0 ? nthreads : omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nth)
@@ -192,11 +325,11 @@ int lmref_accel_intersect(void* p, const float* rays, long long n, double* t, do
         const float* r = rays + 8 * i;
         const Ray ray{Vec3(r[0], r[1], r[2]), Vec3(r[4], r[5], r[6])};
         try {
-            const auto h = s->accel->intersect(ray, Float(r[3]), Float(r[7]));
-            if (h) {
-                t[i] = h->t; uv[2 * i] = h->uv.x; uv[2 * i + 1] = h->uv.y;
-                prim[i] = h->primitive; face[i] = h->face;
-                tri[i] = s->tri_offset.at(h->primitive) + h->face;
+            const auto hit = h->accel->intersect(ray, Float(r[3]), Float(r[7]));
+            if (hit) {
+                t[i] = hit->t; uv[2 * i] = hit->uv.x; uv[2 * i + 1] = hit->uv.y;
+                prim[i] = hit->primitive; face[i] = hit->face;
+                tri[i] = h->tri_offset.at(size_t(hit->primitive)) + hit->face;
             } else {
                 t[i] = 0; uv[2 * i] = 0; uv[2 * i + 1] = 0; prim[i] = -1; face[i] = -1; tri[i] = -1;
             }
@@ -208,71 +341,59 @@ int lmref_accel_intersect(void* p, const float* rays, long long n, double* t, do
     return rc;
 }
 
-// math.h helpers over n records of fixed width (see the table in tests/test_oracle_ref_pin.py).
-int lmref_math_eval(const char* fn, const double* in, long long n, double* out) {
+// renderer::pt (src/renderer/renderer_pt.cpp) over the scene into film asset `film`: max_verts,
+// seed, sampling_mode (0 naive, 1 nee, 2 mis), primary mode (0 pixel with `samples` spp, 1 image
+// with `samples` samples), scheduler::{spp,spi}::sample. The render runs on a new thread, so the
+// renderer's per-thread Rng starts from seed + 0. out: the film's h x w x 3 after its rescale.
+int lmref_render_pt(void* p, int film, long long samples, int max_verts, unsigned int seed, int sampling_mode,
+                    int primary_mode, double* out) {
     return guarded([&] {
-        const std::string f(fn);
-        for (long long i = 0; i < n; i++) {
-            if (f == "reflection") {
-                const double* a = in + 6 * i;
-                put3(out + 3 * i, math::reflection(v3(a), v3(a + 3)));
-            } else if (f == "refraction") {
-                const double* a = in + 7 * i;
-                const auto r = math::refraction(v3(a), v3(a + 3), a[6]);
-                put3(out + 4 * i, r.wt);
-                out[4 * i + 3] = r.total ? 1 : 0;
-            } else if (f == "orthonormal_basis") {
-                const auto [u, v] = math::orthonormal_basis(v3(in + 3 * i));
-                put3(out + 6 * i, u);
-                put3(out + 6 * i + 3, v);
-            } else if (f == "geometry_normal") {
-                const double* a = in + 9 * i;
-                put3(out + 3 * i, math::geometry_normal(v3(a), v3(a + 3), v3(a + 6)));
-            } else if (f == "sample_uniform_disk") {
-                const auto d = math::sample_uniform_disk(Vec2(in[2 * i], in[2 * i + 1]));
-                out[2 * i] = d.x; out[2 * i + 1] = d.y;
-            } else if (f == "sample_cosine_weighted") {
-                put3(out + 3 * i, math::sample_cosine_weighted(Vec2(in[2 * i], in[2 * i + 1])));
-            } else if (f == "sample_uniform_sphere") {
-                put3(out + 3 * i, math::sample_uniform_sphere(Vec2(in[2 * i], in[2 * i + 1])));
-            } else if (f == "balance_heuristic") {
-                out[i] = math::balance_heuristic(in[2 * i], in[2 * i + 1]);
-            } else if (f == "safe_sqrt") {
-                out[i] = math::safe_sqrt(in[i]);
-            } else if (f == "transform_J") {
-                Mat4 M;
-                for (int c = 0; c < 4; c++)
-                    M[c] = Vec4(in[16 * i + 4 * c], in[16 * i + 4 * c + 1], in[16 * i + 4 * c + 2], in[16 * i + 4 * c + 3]);
-                out[i] = Transform(M).J;
-            } else if (f == "bound_isect") {
-                // min3 max3 o3 d3 tmin tmax -> hit, tmin', tmax' (Bound::isect_range)
-                const double* a = in + 14 * i;
-                Bound b;
-                b.min = v3(a);
-                b.max = v3(a + 3);
-                Float tmin = a[12], tmax = a[13];
-                const bool hit = b.isect_range(Ray{v3(a + 6), v3(a + 9)}, tmin, tmax);
-                out[3 * i] = hit ? 1 : 0; out[3 * i + 1] = tmin; out[3 * i + 2] = tmax;
-            } else {
-                throw std::invalid_argument("unknown function " + f);
+        auto* h = H(p);
+        static const char* modes[] = {"naive", "nee", "mis"};
+        if (sampling_mode < 0 || sampling_mode > 2) throw std::invalid_argument("sampling mode");
+        Json prop = Json::object();
+        prop["scene"] = h->asset_loc(h->scene_asset);
+        prop["output"] = h->asset_loc(film);
+        prop["max_verts"] = max_verts;
+        prop["seed"] = seed;
+        prop["sampling_mode"] = modes[sampling_mode];
+        prop["scheduler"] = "sample";
+        prop["primary_ray_sampling_mode"] = primary_mode == 0 ? "pixel" : "image";
+        if (primary_mode == 0) prop["spp"] = samples;
+        else prop["num_samples"] = samples;
+        auto r = comp::create<Renderer>("renderer::pt", h->loc("renderer"), prop);
+        if (!r) throw std::invalid_argument("cannot create renderer::pt");
+        std::string err;
+        std::thread th([&] {
+            try {
+                r->render();
+            } catch (const std::exception& e) {
+                err = e.what();
             }
-        }
+        });
+        th.join();
+        if (!err.empty()) throw std::runtime_error(err);
+        auto* f = dynamic_cast<Film*>(h->assets.at(size_t(film)).get());
+        const auto b = f->buffer();
+        std::memcpy(out, b.data, sizeof(double) * 3 * size_t(b.w) * size_t(b.h));
         return 0;
     });
 }
+
+// ------------------------------------------------------------------------------------------------
+// Components on their own
 
 // A material component created under its key with its properties: diffuse Kd[3]; glossy Ks[3],
 // ax, ay; glass Ni; mirror none. Returns a handle for lmref_material_query.
 void* lmref_material_create(const char* key, const double* prm) {
     try {
         const std::string k(key);
-        Json j;
-        if (k == "material::diffuse") j.set("Kd", {prm[0], prm[1], prm[2]});
-        else if (k == "material::glossy") { j.set("Ks", {prm[0], prm[1], prm[2]}); j.set("ax", {prm[3]}); j.set("ay", {prm[4]}); }
-        else if (k == "material::glass") j.set("Ni", {prm[0]});
-        std::unique_ptr<Component> c(refshim::create(k));
-        if (!dynamic_cast<Material*>(c.get())) throw std::invalid_argument("no material registered as " + k);
-        c->construct(j);
+        Json j = Json::object();
+        if (k == "material::diffuse") j["Kd"] = Vec3(prm[0], prm[1], prm[2]);
+        else if (k == "material::glossy") { j["Ks"] = Vec3(prm[0], prm[1], prm[2]); j["ax"] = prm[3]; j["ay"] = prm[4]; }
+        else if (k == "material::glass") j["Ni"] = prm[0];
+        auto c = comp::create<Material>(k, "$.lmref_material", j);
+        if (!c) throw std::invalid_argument("no material registered as " + k);
         return c.release();
     } catch (const std::exception& e) {
         g_err = e.what();
@@ -314,56 +435,16 @@ int lmref_material_query(void* mp, const double* rec, long long n, double* out) 
     });
 }
 
-// A light component under its key: area Ke[3] over mesh `mesh` of the scene; envconst Le[3];
-// point Le[3], position[3]; directional Le[3], direction[3]. Its scene bound is the bound of the
-// scene's transformed triangles (src/scene.cpp:288-311).
-void* lmref_light_create(void* scene, const char* key, const double* prm, int mesh) {
-    try {
-        auto* s = S(scene);
-        const std::string k(key);
-        Json j;
-        if (k == "light::area") {
-            j.set("Ke", {prm[0], prm[1], prm[2]});
-            refshim::add_named("lmref_light_mesh", s->meshes.at(mesh).get());
-            j.set_str("mesh", "lmref_light_mesh");
-        } else {
-            j.set("Le", {prm[0], prm[1], prm[2]});
-            if (k == "light::point") j.set("position", {prm[3], prm[4], prm[5]});
-            if (k == "light::directional") j.set("direction", {prm[3], prm[4], prm[5]});
-        }
-        std::unique_ptr<Component> c(refshim::create(k));
-        auto* L = dynamic_cast<Light*>(c.get());
-        if (!L) throw std::invalid_argument("no light registered as " + k);
-        c->construct(j);
-        Bound bound;
-        s->traverse_primitive_nodes([&](const SceneNode& node, Mat4 global_transform) {
-            if (node.type != SceneNodeType::Primitive || !node.primitive.mesh) return;
-            node.primitive.mesh->foreach_triangle([&](int, const Mesh::Tri& tri) {
-                bound = merge(bound, Vec3(global_transform * Vec4(tri.p1.p, 1_f)));
-                bound = merge(bound, Vec3(global_transform * Vec4(tri.p2.p, 1_f)));
-                bound = merge(bound, Vec3(global_transform * Vec4(tri.p3.p, 1_f)));
-            });
-        });
-        L->set_scene_bound(bound);
-        return c.release();
-    } catch (const std::exception& e) {
-        g_err = e.what();
-        return nullptr;
-    }
-}
-void lmref_light_destroy(void* l) { delete static_cast<Component*>(l); }
-
-// Light queries under the transform m16 (column-major) over n records of 14 doubles: the shading
-// point p[3] n[3] gn[3], then up[2] upc ud[2]. Out, 33 per record: sample_direct (valid, geomL.p[3],
+// Light asset `light` of the scene, after lmref_scene_build handed it the scene bound. Queries
+// under the transform m16 (column-major) over n records of 14 doubles: the shading point p[3]
+// n[3] gn[3], then up[2] upc ud[2]. Out, 33 per record: sample_direct (valid, geomL.p[3],
 // geomL.n[3], geomL.wo[3], wo[3], weight[3]), pdf_direct at that sample, eval(geomL, wo), and
 // sample_ray (valid, geomL.p[3], geomL.n[3], wo[3], weight[3]).
-int lmref_light_query(void* lp, const double* m16, const double* rec, long long n, double* out) {
+int lmref_light_query(void* p, int light, const double* m16, const double* rec, long long n, double* out) {
     return guarded([&] {
-        const auto* L = dynamic_cast<const Light*>(static_cast<Component*>(lp));
+        const auto* L = dynamic_cast<const Light*>(H(p)->assets.at(size_t(light)).get());
         if (!L) throw std::invalid_argument("not a light");
-        Mat4 M;
-        for (int c = 0; c < 4; c++) M[c] = Vec4(m16[4 * c], m16[4 * c + 1], m16[4 * c + 2], m16[4 * c + 3]);
-        const Transform tr(M);
+        const Transform tr(mat4(m16));
         for (long long i = 0; i < n; i++) {
             const double* r = rec + 14 * i;
             double* o = out + 33 * i;
@@ -392,16 +473,8 @@ int lmref_light_query(void* lp, const double* m16, const double* rec, long long 
 // sample_direct toward the point (valid, wo[3], weight[3]) and its pdf_direct.
 int lmref_camera_query(const double* prm, const double* rec, long long n, double* out) {
     return guarded([&] {
-        Json j;
-        j.set("position", {prm[0], prm[1], prm[2]});
-        j.set("center", {prm[3], prm[4], prm[5]});
-        j.set("up", {prm[6], prm[7], prm[8]});
-        j.set("vfov", {prm[9]});
-        j.set("aspect", {prm[10]});
-        std::unique_ptr<Component> c(refshim::create("camera::pinhole"));
-        auto* cam = dynamic_cast<Camera*>(c.get());
+        auto cam = comp::create<Camera>("camera::pinhole", "$.lmref_camera", camera_prop(prm));
         if (!cam) throw std::invalid_argument("no camera::pinhole registered");
-        c->construct(j);
         for (long long i = 0; i < n; i++) {
             const double* r = rec + 11 * i;
             double* o = out + 21 * i;
@@ -422,6 +495,56 @@ int lmref_camera_query(const double* prm, const double* rec, long long n, double
                 put3(o + 14, sd->wo);
                 put3(o + 17, sd->weight);
                 o[20] = cam->pdf_direct(g, sd->geom, sd->wo);
+            }
+        }
+        return 0;
+    });
+}
+
+// math.h helpers over n records of fixed width (record layouts as lmo_math_eval's).
+int lmref_math_eval(const char* fn, const double* in, long long n, double* out) {
+    return guarded([&] {
+        const std::string f(fn);
+        for (long long i = 0; i < n; i++) {
+            if (f == "reflection") {
+                const double* a = in + 6 * i;
+                put3(out + 3 * i, math::reflection(v3(a), v3(a + 3)));
+            } else if (f == "refraction") {
+                const double* a = in + 7 * i;
+                const auto r = math::refraction(v3(a), v3(a + 3), a[6]);
+                put3(out + 4 * i, r.wt);
+                out[4 * i + 3] = r.total ? 1 : 0;
+            } else if (f == "orthonormal_basis") {
+                const auto [u, v] = math::orthonormal_basis(v3(in + 3 * i));
+                put3(out + 6 * i, u);
+                put3(out + 6 * i + 3, v);
+            } else if (f == "geometry_normal") {
+                const double* a = in + 9 * i;
+                put3(out + 3 * i, math::geometry_normal(v3(a), v3(a + 3), v3(a + 6)));
+            } else if (f == "sample_uniform_disk") {
+                const auto d = math::sample_uniform_disk(Vec2(in[2 * i], in[2 * i + 1]));
+                out[2 * i] = d.x; out[2 * i + 1] = d.y;
+            } else if (f == "sample_cosine_weighted") {
+                put3(out + 3 * i, math::sample_cosine_weighted(Vec2(in[2 * i], in[2 * i + 1])));
+            } else if (f == "sample_uniform_sphere") {
+                put3(out + 3 * i, math::sample_uniform_sphere(Vec2(in[2 * i], in[2 * i + 1])));
+            } else if (f == "balance_heuristic") {
+                out[i] = math::balance_heuristic(in[2 * i], in[2 * i + 1]);
+            } else if (f == "safe_sqrt") {
+                out[i] = math::safe_sqrt(in[i]);
+            } else if (f == "transform_J") {
+                out[i] = Transform(mat4(in + 16 * i)).J;
+            } else if (f == "bound_isect") {
+                // min3 max3 o3 d3 tmin tmax -> hit, tmin', tmax' (Bound::isect_range)
+                const double* a = in + 14 * i;
+                Bound b;
+                b.min = v3(a);
+                b.max = v3(a + 3);
+                Float tmin = a[12], tmax = a[13];
+                const bool hit = b.isect_range(Ray{v3(a + 6), v3(a + 9)}, tmin, tmax);
+                out[3 * i] = hit ? 1 : 0; out[3 * i + 1] = tmin; out[3 * i + 2] = tmax;
+            } else {
+                throw std::invalid_argument("unknown function " + f);
             }
         }
         return 0;

@@ -50,13 +50,18 @@ template <typename T> struct tvec3 {
 };
 
 template <typename T> struct tvec4 {
-    T x{}, y{}, z{}, w{};
-    tvec4() = default;
+    // glm's storage: the components alias an array member `data.data`
+    struct Storage { T data[4]; };
+    union {
+        struct { T x, y, z, w; };
+        Storage data;
+    };
+    tvec4() : x(0), y(0), z(0), w(0) {}
     explicit tvec4(T s) : x(s), y(s), z(s), w(s) {}
     tvec4(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
     tvec4(const tvec3<T>& v, T d) : x(v.x), y(v.y), z(v.z), w(d) {}
-    T& operator[](int i) { return (&x)[i]; }
-    const T& operator[](int i) const { return (&x)[i]; }
+    T& operator[](int i) { return data.data[i]; }
+    const T& operator[](int i) const { return data.data[i]; }
 };
 
 template <typename T> inline tvec3<T>::tvec3(const tvec4<T>& v) : x(v.x), y(v.y), z(v.z) {}
@@ -84,9 +89,12 @@ LMREF_GLM_VEC(tvec4, 4)
 #undef LMREF_GLM_VEC
 #undef LMREF_GLM_BINOP
 
+using ivec2 = tvec2<int>;
+
 // -- common functions -----------------------------------------------------------------------------
 template <typename T> inline T min(T x, T y) { return (y < x) ? y : x; }
 template <typename T> inline T max(T x, T y) { return (x < y) ? y : x; }
+template <typename T> inline T clamp(T x, T lo, T hi) { return min(max(x, lo), hi); }
 template <typename T> inline T abs(T x) { return x >= T(0) ? x : -x; }
 template <typename T> inline tvec2<T> min(const tvec2<T>& a, const tvec2<T>& b) { return {min(a.x, b.x), min(a.y, b.y)}; }
 template <typename T> inline tvec2<T> max(const tvec2<T>& a, const tvec2<T>& b) { return {max(a.x, b.x), max(a.y, b.y)}; }

@@ -20,3 +20,12 @@
 #include <thread>
 #include <tuple>
 #include <vector>
+#include <chrono>
+#include <cstring>
+#include <filesystem>
+#include <fstream>
+#include <iostream>
+#include <set>
+#include <sstream>
+#include <unordered_map>
+namespace fs = std::filesystem;

@@ -279,12 +279,23 @@ def test_lights_match_reference(ref_mod, oracle_mod, key, params):
     from lightmetrica import synthetic as syn
     gp, _, gf = syn.ground_grid(4, 3.0)
     lp, lf = _LIGHT_MESH
+    nrm1 = np.array([[0, 1, 0]], np.float32)
     S = ref_mod.RefScene()
-    m0, m1 = S.add_mesh(gp, gf), S.add_mesh(lp, lf)
+    m0 = S.add_mesh_raw(gp, nrm1, gf.reshape(-1), np.zeros(gf.size, np.int32))
+    m1 = S.add_mesh_raw(lp, nrm1, lf.reshape(-1), np.zeros(lf.size, np.int32))
     S.add_child(0, S.primitive(m0))
     g = S.group(_LIGHT_M)
     S.add_child(0, g)
-    S.add_child(g, S.primitive(m1))
+    if key == "light::area":
+        light = S.light(key, params, m1)
+        S.add_child(g, S.primitive(m1, light=light))
+        light_m = _LIGHT_M
+    else:
+        S.add_child(g, S.primitive(m1))
+        light = S.light(key, params)
+        S.add_child(0, S.primitive(light=light))
+        light_m = np.eye(4)
+    S.build()
     O = oracle_mod.OracleScene(True)
     mat = O.add_material(oracle_mod.MAT["material::diffuse"], [0.5, 0.5, 0.5])
     nrm = np.array([[0, 1, 0]], np.float32)
@@ -311,7 +322,7 @@ def test_lights_match_reference(ref_mod, oracle_mod, key, params):
     rec[:, 3:6] = nn
     rec[:, 6:9] = nn
     rec[:, 9:14] = rng.random((n, 5))
-    a = ref_mod.light_query(S, key, params, m1, _LIGHT_M, rec)
+    a = S.light_query(light, light_m, rec)
     b = O.light_query(rec)
     assert a[:, 0].sum() > 1000 and a[:, 20].sum() == n
     assert _same_bits(a, b), f"{key}: rows {np.nonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).all(1))[0][:5]}"
@@ -340,3 +351,48 @@ def test_camera_matches_reference(ref_mod, oracle_mod, params):
     b = oracle_mod.camera_query(params, rec)
     assert a[:, 6].sum() > 100 and a[:, 13].sum() > 1000
     assert _same_bits(a, b), f"rows {np.nonzero(~((a == b) | (np.isnan(a) & np.isnan(b))).all(1))[0][:5]}"
+
+
+# -- the path tracer itself ------------------------------------------------------------------------
+
+def _pt_scene(lm, which, prefix):
+    from lightmetrica import synthetic as syn
+    if which == "box":
+        scene, film = syn.box_scene(w=24, h=24, prefix=prefix)
+    elif which == "box_point":
+        scene, film = syn.box_scene(w=20, h=20, prefix=prefix)
+        scene.add_primitive(light=lm.load_light(prefix + "point", "point", Le=[0.6, 0.5, 0.4], position=[0.8, 0.7, 0.75]))
+    elif which == "spheres_directional":
+        scene, film, _ = syn.spheres_scene(n_spheres=6, subdiv=3, ground_quads=8, w=24, h=14, prefix=prefix)
+        scene.add_primitive(light=lm.load_light(prefix + "sun", "directional", Le=[3, 2.8, 2.5], direction=[0.4, -1, 0.3]))
+    elif which == "spheres_mirror":
+        scene, film, _ = syn.spheres_scene(n_spheres=5, subdiv=3, ground_quads=8, w=24, h=14, prefix=prefix)
+        mir = lm.load_material(prefix + "mir", "mirror")
+        spheres = [n for n in scene.nodes if n["type"] == "primitive" and n["mesh"] is not None and n["light"] is None]
+        spheres[1]["material"] = mir
+    return scene, film
+
+
+@pytest.mark.parametrize("which", ["box", "box_point", "spheres_directional", "spheres_mirror"])
+@pytest.mark.parametrize("sampling_mode,primary_mode", [("naive", "pixel"), ("nee", "pixel"), ("mis", "pixel"),
+                                                        ("mis", "image")])
+def test_pt_images_match_reference_renderer(ref_mod, oracle_mod, lm, which, sampling_mode, primary_mode):
+    """The reference's own renderer::pt (renderer_pt.cpp with path.h, scene.cpp, the film and the
+    scheduler, compiled from its sources) on one thread, Rng seeded `seed`, against the
+    restatement's render_pt with the reference's random stream, every pixel bit for bit: diffuse,
+    glossy, glass and mirror materials, area, envconst, point and directional lights, naive / NEE /
+    MIS, pixel and image sampling, Russian roulette (max_verts 8)."""
+    scene, film = _pt_scene(lm, which, f"rp_{which}_{sampling_mode}_{primary_mode}_")
+    w, h = film.w, film.h
+    samples = 3 if primary_mode == "pixel" else 3 * w * h
+    S = ref_mod.from_lm_scene(scene)
+    f = S.film(w, h)
+    S.build()
+    a = S.render_pt(f, samples, 8, seed=5, sampling_mode=sampling_mode, primary_mode=primary_mode)
+    O = oracle_mod.from_lm_scene(scene, double=True)
+    O.build()
+    b, _, _, _ = O.render_pt(w, h, 3, 8, seed=5, sampling_mode=sampling_mode, primary_mode=primary_mode,
+                             rng="mt19937", nthreads=1)
+    assert a.sum() > 0
+    bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))).all(axis=2))
+    assert bad.size == 0, f"{len(bad)} pixels differ, first {bad[:4].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
