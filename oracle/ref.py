@@ -2,8 +2,8 @@
 own code compiled unmodified by `make -C oracle ref`: src/scene.cpp, src/accel/accel_sahbvh.cpp,
 src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,mirror}.cpp,
 src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
-src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_pt.cpp and the headers they
-include (math.h, surface.h, scene.h, path.h, ...).
+src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_{pt,lt,bdpt}.cpp and the
+headers they include (math.h, surface.h, scene.h, path.h, bidir.h, ...).
 
 Only tests/ and tests/golden/make_ref_fixtures.py use it, to pin the CPU restatement (and,
 through committed fixtures, the CUDA path) to the reference itself. The library can be built only
@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
         L.lmref_scene_build.argtypes = [vp, dp]
         L.lmref_accel_intersect.argtypes = [vp, fp, C.c_longlong, dp, dp, ip, ip, lp, C.c_int]
         L.lmref_render_pt.argtypes = [vp, C.c_int, C.c_longlong, C.c_int, C.c_uint, C.c_int, C.c_int, dp]
+        L.lmref_render_spi.argtypes = [vp, C.c_char_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_uint, dp]
         L.lmref_light_query.argtypes = [vp, C.c_int, dp, dp, C.c_longlong, dp]
         L.lmref_material_create.restype = vp
         L.lmref_material_create.argtypes = [C.c_char_p, dp]
@@ -185,6 +186,18 @@ class RefScene:
         sm = {"naive": 0, "nee": 1, "mis": 2}[sampling_mode]
         pm = {"pixel": 0, "image": 1}[primary_mode]
         _chk(lib().lmref_render_pt(self.h, film, samples, max_verts, seed & 0xFFFFFFFF, sm, pm, _p(out, C.c_double)))
+        return out
+
+    def render_spi(self, key: str, film: int, num_samples: int, max_verts: int, seed: int = 0,
+                   min_verts: int = 2) -> np.ndarray:
+        """The reference's light-tracing renderers on one thread (Rng seeded `seed`) with
+        scheduler::spi::sample over `num_samples` samples: "renderer::lt", "renderer::bdpt" or a
+        strategy renderer ("renderer::pt_naive_path", "renderer::pt_nee_path",
+        "renderer::lt_nee_path"). Returns the film, (h, w, 3), row 0 at the bottom."""
+        w, h = self.films[film]
+        out = np.zeros((h, w, 3))
+        _chk(lib().lmref_render_spi(self.h, key.encode(), film, num_samples, min_verts, max_verts, seed & 0xFFFFFFFF,
+                                    _p(out, C.c_double)))
         return out
 
     def light_query(self, light: int, m4, rec: np.ndarray) -> np.ndarray:

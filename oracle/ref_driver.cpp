@@ -3,10 +3,11 @@
 // src/scene.cpp, src/accel/accel_sahbvh.cpp, src/mesh/mesh_raw.cpp,
 // src/material/material_{diffuse,glossy,glass,mirror}.cpp,
 // src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
-// src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_pt.cpp, and the headers they
-// include (math.h, surface.h, scene.h, path.h, ...). Tests call them through ctypes
-// (oracle/ref.py) to check the CPU restatement (liblmoracle.so) against the reference itself, and
-// tests/golden/make_ref_fixtures.py records reference outputs that the GPU tests compare with.
+// src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_{pt,lt,bdpt}.cpp, and the
+// headers they include (math.h, surface.h, scene.h, path.h, bidir.h, ...). Tests call them through
+// ctypes (oracle/ref.py) to check the CPU restatement (liblmoracle.so) against the reference
+// itself, and tests/golden/make_ref_fixtures.py records reference outputs that the GPU tests
+// compare with.
 //
 // A handle owns one reference scene (scene::default over accel::sahbvh) and the assets its nodes
 // refer to, created through the component factories under locators "$.h<handle>.<name>", as the
@@ -24,6 +25,7 @@
 #include <lm/renderer.h>
 #include <lm/parallel.h>
 #include <lm/progress.h>
+#include <lm/debug.h>
 
 #include <chrono>
 #include <cstring>
@@ -32,8 +34,9 @@
 using namespace lm;
 
 // ------------------------------------------------------------------------------------------------
-// The reference's parallel and progress entry points (src/parallel.cpp, src/progress.cpp dispatch
-// to configurable backends): a sequential loop with thread id 0, and no progress reports.
+// The reference's parallel, progress and debug entry points (src/parallel.cpp, src/progress.cpp
+// and src/debug.cpp dispatch to configurable backends): a sequential loop with thread id 0, no
+// progress reports, no debug polling.
 
 LM_NAMESPACE_BEGIN(LM_NAMESPACE)
 LM_NAMESPACE_BEGIN(parallel)
@@ -46,6 +49,9 @@ void foreach(long long num_samples, const ParallelProcessFunc& process_func, con
     if (progress_func) progress_func(num_samples);
 }
 LM_NAMESPACE_END(parallel)
+LM_NAMESPACE_BEGIN(debug)
+void poll(const Json&) {}
+LM_NAMESPACE_END(debug)
 LM_NAMESPACE_BEGIN(progress)
 void init(const std::string&, const Json&) {}
 void shutdown() {}
@@ -363,6 +369,42 @@ int lmref_render_pt(void* p, int film, long long samples, int max_verts, unsigne
         else prop["num_samples"] = samples;
         auto r = comp::create<Renderer>("renderer::pt", h->loc("renderer"), prop);
         if (!r) throw std::invalid_argument("cannot create renderer::pt");
+        std::string err;
+        std::thread th([&] {
+            try {
+                r->render();
+            } catch (const std::exception& e) {
+                err = e.what();
+            }
+        });
+        th.join();
+        if (!err.empty()) throw std::runtime_error(err);
+        auto* f = dynamic_cast<Film*>(h->assets.at(size_t(film)).get());
+        const auto b = f->buffer();
+        std::memcpy(out, b.data, sizeof(double) * 3 * size_t(b.w) * size_t(b.h));
+        return 0;
+    });
+}
+
+// A light-tracing renderer of the reference over the scene into film asset `film`, scheduled by
+// scheduler::spi::sample over `num_samples` light paths: key "renderer::lt", "renderer::bdpt"
+// (min_verts, max_verts) or one of bdpt's strategy renderers ("renderer::pt_naive_path",
+// "renderer::pt_nee_path", "renderer::lt_nee_path"). One thread, Rng seeded `seed`, as
+// lmref_render_pt. out: the film's h x w x 3 after its rescale.
+int lmref_render_spi(void* p, const char* key, int film, long long num_samples, int min_verts, int max_verts,
+                     unsigned int seed, double* out) {
+    return guarded([&] {
+        auto* h = H(p);
+        Json prop = Json::object();
+        prop["scene"] = h->asset_loc(h->scene_asset);
+        prop["output"] = h->asset_loc(film);
+        prop["min_verts"] = min_verts;
+        prop["max_verts"] = max_verts;
+        prop["seed"] = seed;
+        prop["scheduler"] = "sample";
+        prop["num_samples"] = num_samples;
+        auto r = comp::create<Renderer>(key, h->loc("renderer"), prop);
+        if (!r) throw std::invalid_argument(std::string("cannot create ") + key);
         std::string err;
         std::thread th([&] {
             try {

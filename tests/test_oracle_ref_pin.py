@@ -1,9 +1,10 @@
 """The oracle pinned to the reference's own code (CPU).
 
-oracle/_ref/liblmref.so is the reference's src/accel/accel_sahbvh.cpp,
-src/material/material_{diffuse,glossy,glass,mirror}.cpp, src/light/light_{area,envconst,point,
-directional}.cpp, src/camera/camera_pinhole.cpp, include/lm/math.h and include/lm/surface.h,
-compiled unmodified from its sources
+oracle/_ref/liblmref.so is the reference's src/scene.cpp, src/scheduler.cpp,
+src/accel/accel_sahbvh.cpp, src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,
+mirror}.cpp, src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
+src/film/film_bitmap.cpp and src/renderer/renderer_{pt,lt,bdpt}.cpp with the headers they
+include, compiled unmodified from its sources
 (oracle/Makefile `ref`, oracle/ref.py) against stand-in headers for glm's arithmetic and the few
 lm core names they use. Where those sources are present the tests compare the oracle's fp64
 restatement with that library directly; everywhere, they compare it with the hit fixtures the
@@ -14,7 +15,9 @@ hit/miss decisions: the restatement must reproduce the reference's Möller–Tru
 (accel_sahbvh.cpp:58-75), its full-sort SAH build (:127-267, including the split chosen among
 equal costs), its traversal order and "later triangle wins" ties (:269-299), the slab test
 (math.h:143-158), the scene flattening with group transforms, the math helpers, Dist2 and the
-Rng, every material query, the lights' direct and emission sampling and the pinhole camera.
+Rng, every material query, the lights' direct and emission sampling, the pinhole camera, and the
+whole renderers (renderer::pt, lt, bdpt and bdpt's strategy renderers) pixel for pixel on one
+thread with the reference's random stream.
 """
 import os
 
@@ -393,6 +396,31 @@ def test_pt_images_match_reference_renderer(ref_mod, oracle_mod, lm, which, samp
     O.build()
     b, _, _, _ = O.render_pt(w, h, 3, 8, seed=5, sampling_mode=sampling_mode, primary_mode=primary_mode,
                              rng="mt19937", nthreads=1)
+    assert a.sum() > 0
+    bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))).all(axis=2))
+    assert bad.size == 0, f"{len(bad)} pixels differ, first {bad[:4].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
+
+
+@pytest.mark.parametrize("which", ["box", "box_point", "spheres_directional", "spheres_mirror"])
+@pytest.mark.parametrize("key", ["renderer::lt", "renderer::bdpt", "renderer::pt_naive_path", "renderer::pt_nee_path",
+                                 "renderer::lt_nee_path"])
+def test_light_tracing_images_match_reference_renderers(ref_mod, oracle_mod, lm, which, key):
+    """The reference's own renderer::lt (renderer_lt.cpp) and renderer::bdpt with its strategy
+    renderers (renderer_bdpt.cpp, bidir.h) on one thread against the restatement with the
+    reference's random stream, every pixel bit for bit."""
+    scene, film = _pt_scene(lm, which, f"rl_{which}_{key.split('::')[1]}_")
+    w, h = film.w, film.h
+    n = 4 * w * h
+    S = ref_mod.from_lm_scene(scene)
+    f = S.film(w, h)
+    S.build()
+    a = S.render_spi(key, f, n, 7, seed=9)
+    O = oracle_mod.from_lm_scene(scene, double=True)
+    O.build()
+    if key == "renderer::lt":
+        b, _, _ = O.render_lt(w, h, n, 7, seed=9, rng="mt19937", nthreads=1)
+    else:
+        b, _, _ = O.render_bdpt(w, h, n, 7, seed=9, rng="mt19937", nthreads=1, mode=key.split("::")[1])
     assert a.sum() > 0
     bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))).all(axis=2))
     assert bad.size == 0, f"{len(bad)} pixels differ, first {bad[:4].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
