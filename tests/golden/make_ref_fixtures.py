@@ -1,12 +1,13 @@
 """Generates the committed hit fixtures under tests/golden/ with the reference's own accel code.
 
-    python tests/golden/make_ref_fixtures.py [c2|transformed|all]
+    python tests/golden/make_ref_fixtures.py [c2|transformed|box256|all]
 
-The hits come from oracle/_ref/liblmref.so: src/accel/accel_sahbvh.cpp (Tri::intersect, the
-multithreaded full-sort SAH build, the stack traversal) and include/lm/math.h (Bound, Ray, Float =
-double), compiled unmodified from the reference's sources by `make -C oracle ref`. So these
-fixtures are outputs of the reference itself; machines without the reference's sources (the GPU
-box) compare against them.
+They come from oracle/_ref/liblmref.so, the reference's own sources compiled unmodified by
+`make -C oracle ref` (for hits: src/accel/accel_sahbvh.cpp's Tri::intersect, multithreaded
+full-sort SAH build and stack traversal with include/lm/math.h's Bound, Float = double; for
+images: src/renderer/renderer_pt.cpp with the scene, film and scheduler). So these fixtures are
+outputs of the reference itself; machines without the reference's sources (the GPU machine) compare
+against them.
 
 ref_c2_probe_hits.npz -- the displaced-sphere scene of the plain drop-in benchmark
     (lightmetrica.synthetic.spheres_parts, seed 7, 3,801,100 triangles) and every 1024th ray of the
@@ -16,6 +17,11 @@ ref_c2_probe_hits.npz -- the displaced-sphere scene of the plain drop-in benchma
 ref_transformed_hits.npz -- tests/ref_scenes.transformed_scene() (nested group transforms, shared
     edges, duplicated and degenerate triangles, an axis-aligned cube) with pin_rays(): `tri`, `t`,
     `uv` for every ray.
+ref_box256_pt16.npz -- the reference's own renderer::pt (renderer_pt.cpp, path.h, scene.cpp,
+    film_bitmap.cpp, scheduler::spp::sample) on the benchmark box scene (synthetic.box_scene,
+    seed 1234) at its benchmark configuration: 256 x 256, 16 spp, max_verts 9, MIS, pixel
+    sampling, one thread with Rng seed 77. `img`, float32, as the film holds it (row 0 at the
+    bottom).
 """
 import json
 import os
@@ -63,6 +69,18 @@ def transformed():
     print({"rays": len(rays), "hits": int((tri >= 0).sum())})
 
 
+def box256_pt16():
+    import lightmetrica as lm
+    lm.init()
+    scene, _ = syn.box_scene(seed=1234, w=256, h=256, prefix="fx_")
+    S = R.from_lm_scene(scene)
+    f = S.film(256, 256)
+    S.build()
+    img = S.render_pt(f, 16, 9, seed=77, sampling_mode="mis", primary_mode="pixel")
+    np.savez_compressed(os.path.join(HERE, "ref_box256_pt16.npz"), img=img.astype(np.float32))
+    print({"box256_pt16_mean": float(img.mean())})
+
+
 if __name__ == "__main__":
     which = sys.argv[1] if len(sys.argv) > 1 else "all"
     if not R.available():
@@ -71,3 +89,5 @@ if __name__ == "__main__":
         c2_probe()
     if which in ("transformed", "all"):
         transformed()
+    if which in ("box256", "all"):
+        box256_pt16()

@@ -7,9 +7,9 @@ C-ABI), not at reduced sizes.
   exempt and counted; against the fp64 restatement (the reference's precision) t agrees within
   1e-5 relative and every index mismatch is a near-tie or an edge-grazing hit.
 * The box scene at its benchmark size (256 x 256, 16 spp, max_verts 9): a per-pixel z-test of the
-  GPU image against the oracle with the reference's own random stream (std::mt19937 per thread,
-  renderer_pt.cpp:91) at the same spp, and the relative MSE against the committed 16384-spp
-  golden image (tests/golden/box256_ref_16k.npz).
+  GPU image against the reference's own renderer::pt image at the same spp (compiled from its
+  sources; tests/golden/ref_box256_pt16.npz), and the relative MSE against the committed
+  16384-spp golden image (tests/golden/box256_ref_16k.npz).
 * The displaced-sphere scene at 1/16 of its pixels (480 x 270, the same camera) against the
   committed 4096-spp golden image (tests/golden/spheres480_ref_4k.npz), and the full 1920 x 1080
   x 64 spp benchmark frame box-filtered to 480 x 270 against the same golden.
@@ -114,18 +114,17 @@ def _render_box256(lm, spp, seed, split=False):
     return scene, film, film.buffer_f32().astype(np.float64)
 
 
-def test_c1_ztest_against_reference_stream_at_matched_spp(lm, oracle_mod):
+def test_c1_ztest_against_reference_renderer_at_matched_spp(lm):
     """The box scene exactly as benchmarked (256 x 256, 16 spp, max_verts 9): the GPU image against
-    the oracle's image with the reference's std::mt19937 stream, also at 16 spp. Per pixel and
-    channel z = (gpu - oracle) / sqrt(2 var / 16), var the golden's per-sample variance: z has
-    mean 0 and variance 1 for two unbiased estimates of the same image. Also 16 x 16-pixel blocks
-    (sums of 256 pixels, near normal). Bands calibrated on the oracle's own two streams: |mean| <=
-    0.004, std 0.996, P(|z| > 4) <= 3.4e-4, block max |z| <= 3.1."""
+    the reference's own renderer::pt image at the same spp (tests/golden/ref_box256_pt16.npz,
+    renderer_pt.cpp compiled from its sources, one thread, Rng seed 77). Per pixel and channel
+    z = (gpu - reference) / sqrt(2 var / 16), var the golden's per-sample variance: z has mean 0
+    and variance 1 for two unbiased estimates of the same image. Also 16 x 16-pixel blocks (sums of
+    256 pixels, near normal). Bands calibrated on the oracle's own two streams: |mean| <= 0.004,
+    std 0.996, P(|z| > 4) <= 3.4e-4, block max |z| <= 3.1."""
     ref, var, meta = _golden("box256_ref_16k")
     scene, _, gpu = _render_box256(lm, 16, 31)
-    S = oracle_mod.from_lm_scene(scene, double=True)
-    S.build()
-    orc, _, _, _ = S.render_pt(256, 256, 16, 9, seed=77, rng="mt19937")
+    orc = np.load(os.path.join(GOLDEN, "ref_box256_pt16.npz"))["img"].astype(np.float64)
     m = var > 0
     z = (gpu - orc)[m] / np.sqrt(2 * var[m] / 16)
     k = 16

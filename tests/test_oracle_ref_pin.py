@@ -424,3 +424,16 @@ def test_light_tracing_images_match_reference_renderers(ref_mod, oracle_mod, lm,
     assert a.sum() > 0
     bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))).all(axis=2))
     assert bad.size == 0, f"{len(bad)} pixels differ, first {bad[:4].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
+
+
+def test_oracle_matches_reference_fixture_box256(oracle_mod, lm):
+    """The benchmark box configuration (256 x 256, 16 spp, max_verts 9, MIS): the restatement on
+    one thread with the reference's random stream reproduces the reference renderer's committed
+    image (tests/golden/ref_box256_pt16.npz, float32) exactly."""
+    from lightmetrica import synthetic as syn
+    scene, _ = syn.box_scene(seed=1234, w=256, h=256, prefix="fxo_")
+    O = oracle_mod.from_lm_scene(scene, double=True)
+    O.build()
+    img, _, _, _ = O.render_pt(256, 256, 16, 9, seed=77, sampling_mode="mis", rng="mt19937", nthreads=1)
+    fx = np.load(os.path.join(GOLDEN, "ref_box256_pt16.npz"))["img"]
+    assert np.array_equal(img.astype(np.float32), fx)
