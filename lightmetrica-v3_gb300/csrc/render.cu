@@ -1533,6 +1533,52 @@ __global__ void __launch_bounds__(kBlock) k_bd_items(BdRec R, int64_t count, int
     }
 }
 
+// Strategy-major order of the items: a counting sort by (t, s), so that a warp of k_bd_connect
+// runs one strategy (one path length, one pair of connection vertex roles) instead of a mix.
+// Bucket key t * (max_verts + 1) + s; at most kBdSortBuckets buckets (max_verts <= 31).
+constexpr int kBdSortBuckets = 1024;
+__device__ __forceinline__ int bd_item_key(uint2 item, int32_t max_verts) {
+    return int(item.y >> 8) * (max_verts + 1) + int(item.y & 0xffu);
+}
+__global__ void __launch_bounds__(kBlock) k_bd_sort_count(const uint2* __restrict__ items, const int* __restrict__ icount,
+                                                          int32_t max_verts, int nbuckets, int* __restrict__ hist) {
+    __shared__ int h[kBdSortBuckets];
+    for (int i = threadIdx.x; i < nbuckets; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const int n = *icount;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[bd_item_key(items[i], max_verts)], 1);
+    __syncthreads();
+    for (int i = threadIdx.x; i < nbuckets; i += blockDim.x)
+        if (h[i]) atomicAdd(hist + i, h[i]);
+}
+// One block: exclusive prefix of the bucket counts, in place (the scatter's cursors).
+__global__ void k_bd_sort_scan(int* hist, int nbuckets) {
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int i = 0; i < nbuckets; i++) {
+            const int c = hist[i];
+            hist[i] = run;
+            run += c;
+        }
+    }
+}
+__global__ void __launch_bounds__(kBlock) k_bd_sort_scatter(const uint2* __restrict__ items, const int* __restrict__ icount,
+                                                            int32_t max_verts, int* __restrict__ cursor, uint2* __restrict__ out) {
+    const int n = *icount;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint2 item = items[i];
+        const int key = bd_item_key(item, max_verts);
+        // one atomic per distinct key in the warp
+        cg::coalesced_group g = cg::coalesced_threads();
+        cg::coalesced_group peers = cg::labeled_partition(g, key);
+        int base = 0;
+        if (peers.thread_rank() == 0) base = atomicAdd(cursor + key, int(peers.size()));
+        base = peers.shfl(base, 0);
+        out[base + int(peers.thread_rank())] = item;
+    }
+}
+
 // One strategy of one sample per item: the connection (bidir.h:593-643), the unweighted
 // contribution alpha_L * c_st * alpha_E (bidir.h:325-343) and the weight. s = 0 splats at the
 // eye's raster position; s, t >= 1 queue a visibility ray from the light vertex to the eye
@@ -1953,7 +1999,8 @@ struct Workspace {
     DevBuf q_o[2], q_d[2], q_thr[2], q_nrm[2], q_ids[2], hits, s_o, s_d, s_c, counters;
     lmgpu_batch* batch = nullptr;  // the regenerating wavefront lmgpu_render_pt runs its job on
     int64_t batch_cap = 0;
-    DevBuf bd_rec, bd_nv, bd_s_o, bd_s_d, bd_s_c, bd_items;  // lmgpu_render_bdpt: subpath records, connection rays, strategies
+    DevBuf bd_rec, bd_nv, bd_s_o, bd_s_d, bd_s_c, bd_items, bd_items_sorted, bd_hist;  // lmgpu_render_bdpt: subpath records,
+    // connection rays, strategies (and in strategy-major order), the sort's bucket counts
 };
 
 Workspace& workspace(int device) {
@@ -2892,6 +2939,12 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         ws.bd_s_c.alloc(size_t(scap) * 16);
         const int64_t icap = wave * (int64_t(mv) * (mv + 1) / 2);  // strategies with t >= 1, s + t <= max_verts
         ws.bd_items.alloc(size_t(icap) * 8);
+        const int nbuckets = (mv + 1) * (mv + 1);
+        const bool sort_items = nbuckets <= kBdSortBuckets;
+        if (sort_items) {
+            ws.bd_items_sorted.alloc(size_t(icap) * 8);
+            ws.bd_hist.alloc(size_t(kBdSortBuckets) * 4);
+        }
 
         PtConst P{};
         P.seed = prm->seed;
@@ -2927,6 +2980,7 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
         const int g_sh = grid_for(sh_k, kBlock, tsmem);
         const int g_shade = grid_for(shade_k, kBlock, 0);
         const int g_items = grid_for(k_bd_items, kBlock, 0);
+        const int g_sort = grid_for(k_bd_sort_scatter, kBlock, 0);
         // the "shade_minblocks" tuning key: 2 gives connect its full register budget, more gives 3 blocks
         auto con_k = tuning().shade_minblocks <= 2 ? k_bd_connect<2> : bd_connect_for(s->dev.feat);
         const int g_con = grid_for(con_k, kBlock, 0);
@@ -2985,7 +3039,16 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
             LMGPU_CUDA(cudaMemsetAsync(cnt + 6, 0, 4, st));
             k_bd_items<<<int(std::min<int64_t>(g_items, (n + kBlock - 1) / kBlock)), kBlock, 0, st>>>(
                 R, n, prm->min_verts, mv, ws.bd_items.as<uint2>(), cnt + 6, icap, cnt + 3);
-            con_k<<<g_con, kBlock, 0, st>>>(s->dev, P, R, ws.bd_items.as<uint2>(), cnt + 6, sq, cnt + 2, scap, film, cnt + 3);
+            const uint2* items = ws.bd_items.as<uint2>();
+            if (sort_items) {
+                int* hist = ws.bd_hist.as<int>();
+                LMGPU_CUDA(cudaMemsetAsync(hist, 0, size_t(nbuckets) * 4, st));
+                k_bd_sort_count<<<g_sort, kBlock, 0, st>>>(items, cnt + 6, mv, nbuckets, hist);
+                k_bd_sort_scan<<<1, 32, 0, st>>>(hist, nbuckets);
+                k_bd_sort_scatter<<<g_sort, kBlock, 0, st>>>(items, cnt + 6, mv, hist, ws.bd_items_sorted.as<uint2>());
+                items = ws.bd_items_sorted.as<uint2>();
+            }
+            con_k<<<g_con, kBlock, 0, st>>>(s->dev, P, R, items, cnt + 6, sq, cnt + 2, scap, film, cnt + 3);
             mark(-1);
             mark(K_SHADOW);
             sh_k<<<g_sh, kBlock, tsmem, st>>>(bvh, sq, cnt + 2, film, rays + 1, cnt + 3, nullptr, 0, nullptr, f_sh, nullptr, nullptr);
