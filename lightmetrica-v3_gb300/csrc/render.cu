@@ -1563,19 +1563,28 @@ __global__ void k_bd_sort_scan(int* hist, int nbuckets) {
         }
     }
 }
+// Each block takes one contiguous range of the items: it counts its range per bucket in shared
+// memory, reserves one run per nonempty bucket with one global atomic, then places its items with
+// shared-memory atomics (one global atomic per block and bucket instead of per warp and key).
 __global__ void __launch_bounds__(kBlock) k_bd_sort_scatter(const uint2* __restrict__ items, const int* __restrict__ icount,
-                                                            int32_t max_verts, int* __restrict__ cursor, uint2* __restrict__ out) {
+                                                            int32_t max_verts, int nbuckets, int* __restrict__ cursor,
+                                                            uint2* __restrict__ out) {
+    __shared__ int h[kBdSortBuckets];
     const int n = *icount;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int per = (n + int(gridDim.x) - 1) / int(gridDim.x);
+    const int lo = int(blockIdx.x) * per, hi = min(n, lo + per);
+    for (int b = threadIdx.x; b < nbuckets; b += blockDim.x) h[b] = 0;
+    __syncthreads();
+    for (int i = lo + int(threadIdx.x); i < hi; i += blockDim.x) atomicAdd(&h[bd_item_key(items[i], max_verts)], 1);
+    __syncthreads();
+    for (int b = threadIdx.x; b < nbuckets; b += blockDim.x) {
+        const int c = h[b];
+        h[b] = c ? atomicAdd(cursor + b, c) : 0;
+    }
+    __syncthreads();
+    for (int i = lo + int(threadIdx.x); i < hi; i += blockDim.x) {
         const uint2 item = items[i];
-        const int key = bd_item_key(item, max_verts);
-        // one atomic per distinct key in the warp
-        cg::coalesced_group g = cg::coalesced_threads();
-        cg::coalesced_group peers = cg::labeled_partition(g, key);
-        int base = 0;
-        if (peers.thread_rank() == 0) base = atomicAdd(cursor + key, int(peers.size()));
-        base = peers.shfl(base, 0);
-        out[base + int(peers.thread_rank())] = item;
+        out[atomicAdd(&h[bd_item_key(item, max_verts)], 1)] = item;
     }
 }
 
@@ -3045,7 +3054,7 @@ int lmgpu_render_bdpt(lmgpu_scene* s, lmgpu_film* f, const lmgpu_bdpt_params* pr
                 LMGPU_CUDA(cudaMemsetAsync(hist, 0, size_t(nbuckets) * 4, st));
                 k_bd_sort_count<<<g_sort, kBlock, 0, st>>>(items, cnt + 6, mv, nbuckets, hist);
                 k_bd_sort_scan<<<1, 32, 0, st>>>(hist, nbuckets);
-                k_bd_sort_scatter<<<g_sort, kBlock, 0, st>>>(items, cnt + 6, mv, hist, ws.bd_items_sorted.as<uint2>());
+                k_bd_sort_scatter<<<g_sort, kBlock, 0, st>>>(items, cnt + 6, mv, nbuckets, hist, ws.bd_items_sorted.as<uint2>());
                 items = ws.bd_items_sorted.as<uint2>();
             }
             con_k<<<g_con, kBlock, 0, st>>>(s->dev, P, R, items, cnt + 6, sq, cnt + 2, scap, film, cnt + 3);
