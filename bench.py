@@ -762,7 +762,8 @@ def run_raycast(lm, scene, args, cpu_scene=None) -> dict:
     """The raycast probe of the plain drop-in workload: 2^24 uniform-sphere rays from one point
     inside the displaced-sphere scene, closest hit through lmgpu_accel_intersect_device (the batched
     Accel::intersect), device buffers, CUDA events on the launching stream; `e2e` through
-    lmgpu_accel_intersect (host rays in, host hits out). Every hit of one pass is then checked
+    lmgpu_accel_intersect (host rays in, host hits out) from pinned host memory, with the pageable
+    figure beside it. Every hit of one pass is then checked
     against the fp32 oracle (bit-exact index, t, u, v; exact-t ties counted), and the fp64 oracle
     (the reference's precision) is timed on a bounded subsample as the CPU baseline."""
     import ctypes as C
@@ -808,12 +809,29 @@ def run_raycast(lm, scene, args, cpu_scene=None) -> dict:
         rt.cudaFree(d_rays)
         rt.cudaFree(d_hits)
         rt.cudaFree(flush)
-    # end to end: host rays in, host hits out, through the C-ABI
-    e2e = []
+    # end to end: host rays in, host hits out, through the C-ABI (Accel::intersect over host
+    # buffers): from pinned host memory, as a caller streaming rays would hold them, and, for
+    # comparison, from ordinary (pageable) numpy arrays
+    e2e, e2e_pageable = [], []
+    h_rays, h_hits = C.c_void_p(), C.c_void_p()
+    assert rt.cudaMallocHost(C.byref(h_rays), rays.nbytes) == 0
+    assert rt.cudaMallocHost(C.byref(h_hits), n * 16) == 0
+    try:
+        C.memmove(h_rays, rays.ctypes.data, rays.nbytes)
+        N.check(L.lmgpu_accel_intersect(acc._h, C.cast(h_rays, C.POINTER(C.c_float)), n, C.cast(h_hits, C.POINTER(N.Hit))))
+        for _ in range(max(1, min(3, args.steps))):
+            t = time.perf_counter()
+            N.check(L.lmgpu_accel_intersect(acc._h, C.cast(h_rays, C.POINTER(C.c_float)), n, C.cast(h_hits, C.POINTER(N.Hit))))
+            e2e.append(time.perf_counter() - t)
+        hits_pinned = np.frombuffer((C.c_char * (n * 16)).from_address(h_hits.value), dtype=hits.dtype).copy()
+        assert np.array_equal(hits_pinned, hits), "hits through host buffers differ from the device-buffer pass"
+    finally:
+        rt.cudaFreeHost(h_rays)
+        rt.cudaFreeHost(h_hits)
     for _ in range(max(1, min(3, args.steps))):
         t = time.perf_counter()
         acc.intersect_batch(rays)
-        e2e.append(time.perf_counter() - t)
+        e2e_pageable.append(time.perf_counter() - t)
     ms = statistics.median(times)
     b_ray = 32 + 16 + NODE_BYTES * mn.value + TRI_BYTES * mt.value
     peaks = _peaks()
@@ -822,7 +840,8 @@ def run_raycast(lm, scene, args, cpu_scene=None) -> dict:
                        f"({acc.stats()['num_tris']} triangles), closest hit, tmin 1e-3, tmax 1e10",
            "Mrays_per_s": n / ms / 1e3, "ms_median": ms, "ms_all": times,
            "e2e": {"value": n / statistics.median(e2e) / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": rays.nbytes,
-                   "d2h_bytes_per_step": n * 16},
+                   "d2h_bytes_per_step": n * 16, "host_memory": "pinned",
+                   "pageable_value": n / statistics.median(e2e_pageable) / 1e6},
            "hit_fraction": float((hits["prim"] >= 0).mean()),
            "roofline": {"bound": "issue/latency (L2-resident nodes)", "achieved": achieved, "unit": "GB/s",
                         "peak": peaks["hbm_gbs"], "frac": achieved / peaks["hbm_gbs"], "bytes_per_ray": b_ray,
@@ -971,6 +990,8 @@ def _cudart():
             lib.cudaEventSynchronize.argtypes = [C.c_void_p]
             lib.cudaEventDestroy.argtypes = [C.c_void_p]
             lib.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
+            lib.cudaMallocHost.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+            lib.cudaFreeHost.argtypes = [C.c_void_p]
             return lib
         except OSError:
             continue

@@ -509,10 +509,67 @@ int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgp
         if (n == 0) return;
         accel->scratch_rays.alloc(size_t(n) * 32);
         accel->scratch_hits.alloc(size_t(n) * sizeof(lmgpu_hit));
-        LMGPU_CUDA_SYNC(cudaMemset(accel->err.p, 0, sizeof(int)));
-        LMGPU_CUDA_SYNC(cudaMemcpy(accel->scratch_rays.p, rays, size_t(n) * 32, cudaMemcpyHostToDevice));
-        launch_trace(accel, accel->scratch_rays.p, n, accel->scratch_hits.p, nullptr, 0, accel->err.as<int>());
-        LMGPU_CUDA_SYNC(cudaMemcpy(hits, accel->scratch_hits.p, size_t(n) * sizeof(lmgpu_hit), cudaMemcpyDeviceToHost));
+        // With page-locked host buffers, chunks of 2^21 rays alternate between two streams, so that
+        // one chunk's copies run beside the next chunk's trace. Pageable buffers go in one copy each
+        // way (chunked copies from pageable memory measured slower: 1,102 -> 775 Mrays/s).
+        constexpr int64_t kChunk = int64_t(1) << 21;
+        auto page_locked = [](const void* p) {
+            cudaPointerAttributes a{};
+            if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+                cudaGetLastError();  // clear the (non-sticky) error an unknown pointer may leave
+                return false;
+            }
+            return a.type == cudaMemoryTypeHost;
+        };
+        if (n <= kChunk || !page_locked(rays) || !page_locked(hits)) {
+            LMGPU_CUDA_SYNC(cudaMemset(accel->err.p, 0, sizeof(int)));
+            LMGPU_CUDA_SYNC(cudaMemcpy(accel->scratch_rays.p, rays, size_t(n) * 32, cudaMemcpyHostToDevice));
+            launch_trace(accel, accel->scratch_rays.p, n, accel->scratch_hits.p, nullptr, 0, accel->err.as<int>());
+            LMGPU_CUDA_SYNC(cudaMemcpy(hits, accel->scratch_hits.p, size_t(n) * sizeof(lmgpu_hit), cudaMemcpyDeviceToHost));
+        } else {
+            std::shared_lock<std::shared_mutex> lk(capture_mutex());
+            cudaStream_t sts[2] = {nullptr, nullptr};
+            cudaEvent_t cleared = nullptr;
+            LMGPU_CUDA(cudaStreamCreateWithFlags(&sts[0], cudaStreamNonBlocking));
+            cudaError_t e1 = cudaStreamCreateWithFlags(&sts[1], cudaStreamNonBlocking);
+            if (e1 == cudaSuccess) e1 = cudaEventCreateWithFlags(&cleared, cudaEventDisableTiming);
+            if (e1 != cudaSuccess) {
+                cudaStreamDestroy(sts[0]);
+                if (sts[1]) cudaStreamDestroy(sts[1]);
+                LMGPU_CUDA(e1);
+            }
+            try {
+                // the error flag is cleared on the first stream before either stream's first trace
+                LMGPU_CUDA(cudaMemsetAsync(accel->err.p, 0, sizeof(int), sts[0]));
+                LMGPU_CUDA(cudaEventRecord(cleared, sts[0]));
+                LMGPU_CUDA(cudaStreamWaitEvent(sts[1], cleared, 0));
+                char* d_r = static_cast<char*>(accel->scratch_rays.p);
+                char* d_h = static_cast<char*>(accel->scratch_hits.p);
+                for (int64_t off = 0, c = 0; off < n; off += kChunk, c++) {
+                    const int64_t m = std::min(kChunk, n - off);
+                    cudaStream_t st = sts[c & 1];
+                    LMGPU_CUDA(cudaMemcpyAsync(d_r + off * 32, rays + off * 8, size_t(m) * 32, cudaMemcpyHostToDevice, st));
+                    launch_trace(accel, d_r + off * 32, m, d_h + off * int64_t(sizeof(lmgpu_hit)), nullptr, st, accel->err.as<int>());
+                    LMGPU_CUDA(cudaMemcpyAsync(hits + off, d_h + off * int64_t(sizeof(lmgpu_hit)), size_t(m) * sizeof(lmgpu_hit),
+                                               cudaMemcpyDeviceToHost, st));
+                }
+            } catch (...) {
+                for (auto st : sts) {
+                    cudaStreamSynchronize(st);
+                    cudaStreamDestroy(st);
+                }
+                cudaEventDestroy(cleared);
+                throw;
+            }
+            cudaError_t first_err = cudaSuccess;
+            for (auto st : sts) {
+                const cudaError_t e = cudaStreamSynchronize(st);
+                if (first_err == cudaSuccess) first_err = e;
+                cudaStreamDestroy(st);
+            }
+            cudaEventDestroy(cleared);
+            LMGPU_CUDA(first_err);
+        }
         int herr = 0;
         LMGPU_CUDA_SYNC(cudaMemcpy(&herr, accel->err.p, sizeof(int), cudaMemcpyDeviceToHost));
         if (herr) throw Error(LMGPU_ERR_INTERNAL, "traversal consistency check failed (code " + std::to_string(herr) + ")");

@@ -37,7 +37,9 @@ public:
     Json(float v) : type_(Type::Number), num_(v) {}
     Json(int v) : type_(Type::Number), num_(v) {}
     Json(unsigned int v) : type_(Type::Number), num_(v) {}
+    Json(long v) : type_(Type::Number), num_(double(v)) {}
     Json(long long v) : type_(Type::Number), num_(double(v)) {}
+    Json(unsigned long v) : type_(Type::Number), num_(double(v)) {}
     Json(bool v) : type_(Type::Number), num_(v ? 1 : 0) {}
     Json(const char* s) : type_(Type::String), str_(s) {}
     Json(const std::string& s) : type_(Type::String), str_(s) {}
@@ -102,6 +104,15 @@ public:
         return str_;
     }
     template <typename T> T get() const;
+    // nlohmann's j.value(key, default)
+    template <typename T> T value(const std::string& k, const T& def) const {
+        auto it = obj_.find(k);
+        return it == obj_.end() ? def : it->second.template get<T>();
+    }
+    std::string value(const std::string& k, const char* def) const {
+        auto it = obj_.find(k);
+        return it == obj_.end() ? std::string(def) : it->second.string();
+    }
 
     operator double() const { return number(); }
     operator float() const { return float(number()); }
@@ -171,6 +182,7 @@ public:
     virtual Component* underlying(const std::string& name) const { (void)name; return nullptr; }
     virtual void foreach_underlying(const ComponentVisitor& visitor) { (void)visitor; }
     virtual Json underlying_value(const std::string& query = "") const { (void)query; return {}; }
+    virtual void* underlying_raw_pointer(const std::string& query = "") const { (void)query; return nullptr; }
 
     void lmref_set_ids(const std::string& key, const std::string& loc) {
         key_ = key;
