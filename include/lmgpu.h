@@ -479,10 +479,9 @@ int lmgpu_batch_set_timing(lmgpu_batch* batch, int32_t on);
  * d_film, a device buffer of h x w x 3 floats, which receives the estimate scaled by 1/spp in
  * both primary modes (the scale renderer_pt.cpp:307-312 gives, as lmgpu_render_pt does);
  * params->accumulate must be 0. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current and caches it for the life of the process;
- * make that first call before any stream capture begins. A cudaDeviceReset invalidates the cached
- * address, as it invalidates every scene and film handle of the library: do not call this entry
- * point after one. Every call shares the one array and clears what must start at zero, so calls
+ * (cudaGetSymbolAddress) with that device current and caches it for the life of the process. A
+ * cudaDeviceReset invalidates the cached address, as it invalidates every scene and film handle of
+ * the library: do not call this entry point after one. Every call shares the one array and clears what must start at zero, so calls
  * whose work overlaps on the GPU (different streams, or concurrent host threads) race: serialize
  * them. The call enqueues on `stream`, waits for it to read the error word, and calls no
  * cudaMalloc, cudaFree or other allocating routine. */
