@@ -400,3 +400,45 @@ def test_axis_aligned_rays_visit_few_nodes(lm):
     assert mn.value < 40, (mn.value, st["num_nodes"])
     hits = scene._accel.intersect_batch(rays)
     assert (hits["prim"][: n // 2] >= 0).all()  # every downward ray hits the ground
+
+
+def test_intersect_host_buffers_pinned_and_pageable(lm):
+    """Accel::intersect over host buffers (lmgpu_accel_intersect): page-locked buffers of more
+    than 2^21 rays go in chunks over two streams (the last one short), pageable ones in one copy
+    each way; both give the device-buffer call's hits exactly."""
+    import numpy as np
+    from lightmetrica import _native as N
+    from lightmetrica import synthetic as syn
+    scene, _, _ = syn.spheres_scene(n_spheres=8, subdiv=5, ground_quads=64, w=32, h=18, prefix="hb_")
+    scene.build()
+    acc = scene.accel()
+    n = 5 * (1 << 20) + 12345
+    rays = syn.sphere_rays(n, [0.0, 1.0, 0.5], seed=21)
+    L = N.lib()
+    rt = _cudart()
+    rt.cudaMallocHost.argtypes = [C.POINTER(C.c_void_p), C.c_size_t]
+    rt.cudaFreeHost.argtypes = [C.c_void_p]
+    d_rays = _dev_alloc(rt, rays.nbytes)
+    d_hits = _dev_alloc(rt, n * 16)
+    h_rays, h_hits = C.c_void_p(), C.c_void_p()
+    assert rt.cudaMallocHost(C.byref(h_rays), rays.nbytes) == 0
+    assert rt.cudaMallocHost(C.byref(h_hits), n * 16) == 0
+    try:
+        _h2d(rt, d_rays, rays)
+        N.check(L.lmgpu_accel_intersect_device(acc._h, d_rays, n, d_hits, None))
+        dev = np.zeros(n * 4, np.float32)
+        _d2h(rt, dev, d_hits)
+        C.memmove(h_rays, rays.ctypes.data, rays.nbytes)
+        N.check(L.lmgpu_accel_intersect(acc._h, C.cast(h_rays, C.POINTER(C.c_float)), n, C.cast(h_hits, C.POINTER(N.Hit))))
+        pinned = np.frombuffer((C.c_char * (n * 16)).from_address(h_hits.value), dtype=np.float32).copy()
+        pageable = np.zeros(n * 4, np.float32)
+        N.check(L.lmgpu_accel_intersect(acc._h, rays.ctypes.data_as(C.POINTER(C.c_float)), n,
+                                        pageable.ctypes.data_as(C.POINTER(N.Hit))))
+        assert (dev.view(np.int32)[3::4] >= 0).mean() > 0.2
+        assert np.array_equal(pinned.view(np.uint32), dev.view(np.uint32))
+        assert np.array_equal(pageable.view(np.uint32), dev.view(np.uint32))
+    finally:
+        rt.cudaFreeHost(h_rays)
+        rt.cudaFreeHost(h_hits)
+        rt.cudaFree(d_rays)
+        rt.cudaFree(d_hits)
