@@ -646,6 +646,9 @@ class ModelWavefrontObj(Component):
             mesh = MeshRaw(name, {"ps": obj.ps.astype(np.float32), "ns": (ns if len(ns) else np.zeros((1, 3))).astype(np.float32),
                                   "ts": ts,
                                   "fs": {"p": fp.astype(np.int32), "n": fn.astype(np.int32), "t": ft.astype(np.int32)}})
+            # the faces whose shading normal is the geometric one, computed exactly by the
+            # reference; the float32 copy above serves the GPU
+            mesh.geo_normal_faces = ~has_n
             self.assets[name] = mesh
             mtl = obj.materials[prim.material]
             light = None

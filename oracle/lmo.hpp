@@ -128,15 +128,20 @@ template <typename F> struct Mesh {
     struct Tri { Point p1, p2, p3; };
     struct InterpolatedPoint { V3<F> p, n, gn; V2<F> t; };
     int num_triangles() const { return int(fs.size()) / 3; }
+    // A face whose first corner has no normal index (n < 0) takes the geometric normal as its
+    // shading normal, as an OBJ model's mesh does (model_wavefrontobj.cpp:285-321).
+    V3<F> normal_at(int n) const { return n < 0 ? V3<F>() : ns[n]; }
     Tri triangle_at(int face) const {
         const auto f1 = fs[3 * face], f2 = fs[3 * face + 1], f3 = fs[3 * face + 2];
-        return {{ps[f1.p], ns[f1.n], ts[f1.t]}, {ps[f2.p], ns[f2.n], ts[f2.t]}, {ps[f3.p], ns[f3.n], ts[f3.t]}};
+        return {{ps[f1.p], normal_at(f1.n), ts[f1.t]}, {ps[f2.p], normal_at(f2.n), ts[f2.t]},
+                {ps[f3.p], normal_at(f3.n), ts[f3.t]}};
     }
     InterpolatedPoint surface_point(int face, V2<F> uv) const {
         const auto i1 = fs[3 * face], i2 = fs[3 * face + 1], i3 = fs[3 * face + 2];
+        const auto gn = geometry_normal(ps[i1.p], ps[i2.p], ps[i3.p]);
         return {mix_barycentric(ps[i1.p], ps[i2.p], ps[i3.p], uv),
-                normalize(mix_barycentric(ns[i1.n], ns[i2.n], ns[i3.n], uv)),
-                geometry_normal(ps[i1.p], ps[i2.p], ps[i3.p]),
+                i1.n < 0 ? gn : normalize(mix_barycentric(ns[i1.n], ns[i2.n], ns[i3.n], uv)),
+                gn,
                 mix_barycentric2(ts[i1.t], ts[i2.t], ts[i3.t], uv)};
     }
 };

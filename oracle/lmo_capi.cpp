@@ -64,6 +64,7 @@ int lmo_add_mesh(void* p, const float* ps, int nps, const float* ns, int nns, co
         for (int i = 0; i < ncorners; i++) {
             const int t = ft && nts > 0 ? ft[i] : 0;
             if (t < 0 || t >= int(m.ts.size())) return fail("texture coordinate index out of range");
+            if (fn[i] >= nns || (fn[i] < 0 && fn[i - i % 3] >= 0)) return fail("normal index out of range");
             m.fs.push_back({fp[i], t, fn[i]});
         }
         S.meshes.push_back(std::move(m));
@@ -436,17 +437,13 @@ int lmo_dist2_eval(const double* v, int cols, int rows, long long n, const doubl
     return 0;
 }
 
-// Every Material query of the restated material `type` (parameters as lmo_add_material) in double,
-// over n records with the layout of the reference library's lmref_material_query.
-int lmo_material_query(int type, const double* prm, const double* rec, long long n, double* out) {
+namespace {
+// Every Material query of m over n records with the layout of the reference library's
+// lmref_material_query.
+void material_records(const Material<double>& m, const double* rec, long long n, double* out) {
     using V = V3<double>;
     auto v3 = [](const double* p) { return V(p[0], p[1], p[2]); };
     auto put3 = [](double* o, V v) { o[0] = v.x; o[1] = v.y; o[2] = v.z; };
-    Material<double> m;
-    m.type = type;
-    if (type == MAT_DIFFUSE) m.Kd = v3(prm);
-    if (type == MAT_GLOSSY) { m.Ks = v3(prm); m.ax = prm[3]; m.ay = prm[4]; }
-    if (type == MAT_GLASS) m.Ni = prm[0];
     for (long long i = 0; i < n; i++) {
         const double* r = rec + 26 * i;
         double* o = out + 18 * i;
@@ -467,6 +464,47 @@ int lmo_material_query(int type, const double* prm, const double* rec, long long
         o[13] = m.pdf_component(comp, g, wi);
         put3(o + 14, m.reflectance(g).value_or(V()));
         o[17] = m.is_specular_component(comp) ? 1 : 0;
+    }
+}
+}  // namespace
+
+// Every Material query of the restated material `type` (parameters as lmo_add_material) in double,
+// over n records with the layout of the reference library's lmref_material_query.
+int lmo_material_query(int type, const double* prm, const double* rec, long long n, double* out) {
+    using V = V3<double>;
+    auto v3 = [](const double* p) { return V(p[0], p[1], p[2]); };
+    Material<double> m;
+    m.type = type;
+    if (type == MAT_DIFFUSE) m.Kd = v3(prm);
+    if (type == MAT_GLOSSY) { m.Ks = v3(prm); m.ax = prm[3]; m.ay = prm[4]; }
+    if (type == MAT_GLASS) m.Ni = prm[0];
+    material_records(m, rec, n, out);
+    return 0;
+}
+
+// The same queries on material `mat` of a double-precision scene, with the textures bound to it.
+int lmo_scene_material_query(void* p, int mat, const double* rec, long long n, double* out) {
+    auto* h = static_cast<Handle*>(p);
+    if (!h->dbl) return fail("material queries need a double-precision scene");
+    if (mat < 0 || mat >= int(h->sd->materials.size())) return fail("material index out of range");
+    material_records(h->sd->materials[size_t(mat)], rec, n, out);
+    return 0;
+}
+
+// Texture `tex` of a double-precision scene at n texture coordinates (uv[2] each). Out, 5 per
+// point: eval[3], eval_alpha (0 without alpha), has_alpha.
+int lmo_texture_query(void* p, int tex, const double* uv, long long n, double* out) {
+    auto* h = static_cast<Handle*>(p);
+    if (!h->dbl) return fail("texture queries need a double-precision scene");
+    if (tex < 0 || tex >= int(h->sd->textures.size())) return fail("texture index out of range");
+    const auto& t = *h->sd->textures[size_t(tex)];
+    const bool a = t.has_alpha();
+    for (long long i = 0; i < n; i++) {
+        const V2<double> q(uv[2 * i], uv[2 * i + 1]);
+        const auto v = t.eval(q);
+        out[5 * i] = v.x; out[5 * i + 1] = v.y; out[5 * i + 2] = v.z;
+        out[5 * i + 3] = a ? t.eval_alpha(q) : 0;
+        out[5 * i + 4] = a ? 1 : 0;
     }
     return 0;
 }

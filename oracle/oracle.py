@@ -70,6 +70,8 @@ def lib() -> C.CDLL:
         L.lmo_rng_mt.argtypes = [C.c_uint, C.c_int, C.c_longlong, dp]
         L.lmo_material_query.argtypes = [C.c_int, dp, dp, C.c_longlong, dp]
         L.lmo_light_query.argtypes = [vp, dp, C.c_longlong, dp]
+        L.lmo_scene_material_query.argtypes = [vp, C.c_int, dp, C.c_longlong, dp]
+        L.lmo_texture_query.argtypes = [vp, C.c_int, dp, C.c_longlong, dp]
         L.lmo_camera_query.argtypes = [dp, dp, C.c_longlong, dp]
         _lib = L
     return _lib
@@ -183,6 +185,24 @@ class OracleScene:
         out = np.zeros((rec.shape[0], 33))
         dp = C.POINTER(C.c_double)
         _chk(lib().lmo_light_query(self.h, rec.ctypes.data_as(dp), rec.shape[0], out.ctypes.data_as(dp)))
+        return out
+
+    def material_query(self, mat: int, rec: np.ndarray) -> np.ndarray:
+        """Every query of material `mat` with its textures over records of 26 doubles (layout as
+        oracle/ref.py's material_query); returns n x 18. Double-precision scenes."""
+        rec = np.ascontiguousarray(rec, np.float64)
+        out = np.zeros((rec.shape[0], 18))
+        dp = C.POINTER(C.c_double)
+        _chk(lib().lmo_scene_material_query(self.h, mat, rec.ctypes.data_as(dp), rec.shape[0], out.ctypes.data_as(dp)))
+        return out
+
+    def texture_query(self, tex: int, uv: np.ndarray) -> np.ndarray:
+        """Texture `tex` at texture coordinates uv (n x 2): n x 5 (eval[3], eval_alpha,
+        has_alpha). Double-precision scenes."""
+        uv = np.ascontiguousarray(uv, np.float64)
+        out = np.zeros((uv.shape[0], 5))
+        dp = C.POINTER(C.c_double)
+        _chk(lib().lmo_texture_query(self.h, tex, uv.ctypes.data_as(dp), uv.shape[0], out.ctypes.data_as(dp)))
         return out
 
     def triangles(self) -> np.ndarray:
@@ -386,7 +406,13 @@ def from_lm_scene(scene, double: bool = True) -> OracleScene:
         if id(m) not in mesh_id:
             ts = getattr(m, "ts", None)
             ft = getattr(m, "ft", None)
-            mesh_id[id(m)] = O.add_mesh(m.ps, m.ns, m.fp, m.fn, ts, ft)
+            fn = m.fn
+            geo = getattr(m, "geo_normal_faces", None)
+            if double and geo is not None and np.any(geo):
+                # faces an OBJ gave no normals: the exact geometric normal, not its float32 copy
+                fn = np.array(fn, np.int32).reshape(-1, 3)
+                fn[np.asarray(geo, bool)] = -1
+            mesh_id[id(m)] = O.add_mesh(m.ps, m.ns, m.fp, fn, ts, ft)
         return mesh_id[id(m)]
 
     def tex_of(t):

@@ -1,9 +1,12 @@
 """Oracle (test infrastructure only): ctypes wrapper of oracle/_ref/liblmref.so, the reference's
 own code compiled unmodified by `make -C oracle ref`: src/scene.cpp, src/accel/accel_sahbvh.cpp,
-src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,mirror}.cpp,
-src/light/light_{area,envconst,point,directional}.cpp, src/camera/camera_pinhole.cpp,
-src/film/film_bitmap.cpp, src/scheduler.cpp, src/renderer/renderer_{pt,lt,bdpt}.cpp and the
-headers they include (math.h, surface.h, scene.h, path.h, bidir.h, ...).
+src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,mirror,proxy}.cpp,
+src/light/light_{area,envconst,point,directional,env}.cpp, src/texture/texture_bitmap.cpp,
+src/objloader/objloader{,_simple}.cpp, src/model/model_wavefrontobj.cpp (with
+material::mixture_wavefrontobj), src/camera/camera_pinhole.cpp, src/film/film_bitmap.cpp,
+src/scheduler.cpp, src/renderer/renderer_{pt,lt,bdpt}.cpp and the headers they include (math.h,
+surface.h, scene.h, path.h, bidir.h, ...). stb_image, which texture_bitmap.cpp decodes images
+with, is not among the reference's sources: images reach it decoded, through register_image.
 
 Only tests/ and tests/golden/make_ref_fixtures.py use it, to pin the CPU restatement (and,
 through committed fixtures, the CUDA path) to the reference itself. The library can be built only
@@ -71,6 +74,14 @@ def lib() -> C.CDLL:
         L.lmref_render_pt.argtypes = [vp, C.c_int, C.c_longlong, C.c_int, C.c_uint, C.c_int, C.c_int, dp]
         L.lmref_render_spi.argtypes = [vp, C.c_char_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_uint, dp]
         L.lmref_light_query.argtypes = [vp, C.c_int, dp, dp, C.c_longlong, dp]
+        L.lmref_register_image.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, fp]
+        L.lmref_scene_add_texture.argtypes = [vp, C.c_char_p, C.c_int]
+        L.lmref_scene_add_material_tex.argtypes = [vp, C.c_char_p, dp, C.c_int]
+        L.lmref_scene_add_light_env.argtypes = [vp, C.c_char_p, C.c_double, C.c_double]
+        L.lmref_scene_add_model.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+        L.lmref_scene_add_child_from_model.argtypes = [vp, C.c_int, C.c_int]
+        L.lmref_texture_query.argtypes = [vp, C.c_int, dp, C.c_longlong, dp]
+        L.lmref_scene_material_query.argtypes = [vp, C.c_int, dp, C.c_longlong, dp]
         L.lmref_material_create.restype = vp
         L.lmref_material_create.argtypes = [C.c_char_p, dp]
         L.lmref_material_destroy.argtypes = [vp]
@@ -97,6 +108,16 @@ def _prm(params, n=11):
     prm = np.zeros(n)
     prm[:len(params)] = params
     return prm
+
+
+def register_image(path: str, texels_top_first) -> None:
+    """Hands texture::bitmap's stb_image stand-in the decoded image it loads from `path`: h x w x c
+    (3 or 4) floats, top row first as an image file stores them."""
+    t = np.ascontiguousarray(texels_top_first, np.float32)
+    if t.ndim != 3:
+        raise ValueError("texels must be h x w x c")
+    h, w, c = t.shape
+    _chk(lib().lmref_register_image(str(path).encode(), w, h, c, _p(t, C.c_float)))
 
 
 class RefScene:
@@ -137,6 +158,43 @@ class RefScene:
 
     def light(self, key: str, params, mesh: int = -1) -> int:
         return _chk(lib().lmref_scene_add_light(self.h, key.encode(), _p(_prm(params), C.c_double), mesh))
+
+    def texture(self, path: str, flip: bool = True) -> int:
+        """texture::bitmap of an image given to register_image under `path`."""
+        return _chk(lib().lmref_scene_add_texture(self.h, str(path).encode(), 1 if flip else 0))
+
+    def material_tex(self, key: str, params, map_kd: int = -1) -> int:
+        """material::diffuse (Kd) or material::mixture_wavefrontobj (Kd, Ks, ax, ay,
+        no_alpha_mask) with texture asset map_kd (-1 = none)."""
+        return _chk(lib().lmref_scene_add_material_tex(self.h, key.encode(), _p(_prm(params), C.c_double), map_kd))
+
+    def light_env(self, path: str, rot_deg: float = 0.0, scale: float = 1.0) -> int:
+        """light::env over the image registered under `path` (loaded flipped)."""
+        return _chk(lib().lmref_scene_add_light_env(self.h, str(path).encode(), rot_deg, scale))
+
+    def model(self, path: str, skip_specular_mat: bool = False, base_material: int = -1) -> int:
+        """model::wavefrontobj of an OBJ file (MTL and textures beside it; texture images through
+        register_image)."""
+        return _chk(lib().lmref_scene_add_model(self.h, str(path).encode(), 1 if skip_specular_mat else 0,
+                                                base_material))
+
+    def add_child_from_model(self, parent: int, model: int) -> int:
+        """Scene::add_child_from_model; returns the number of primitive nodes it added."""
+        return _chk(lib().lmref_scene_add_child_from_model(self.h, parent, model))
+
+    def texture_query(self, tex: int, uv: np.ndarray) -> np.ndarray:
+        """n x 5: eval[3], eval_alpha (0 without alpha), has_alpha at texture coordinates uv."""
+        uv = np.ascontiguousarray(uv, np.float64)
+        out = np.zeros((uv.shape[0], 5))
+        _chk(lib().lmref_texture_query(self.h, tex, _p(uv, C.c_double), uv.shape[0], _p(out, C.c_double)))
+        return out
+
+    def material_query(self, mat: int, rec: np.ndarray) -> np.ndarray:
+        """material_query's records on material asset `mat` of this scene (textured ones too)."""
+        rec = np.ascontiguousarray(rec, np.float64)
+        out = np.zeros((rec.shape[0], 18))
+        _chk(lib().lmref_scene_material_query(self.h, mat, _p(rec, C.c_double), rec.shape[0], _p(out, C.c_double)))
+        return out
 
     def camera(self, position, center, up, vfov, aspect) -> int:
         prm = _prm(list(position) + list(center) + list(up) + [vfov, aspect])
@@ -300,10 +358,26 @@ def rng(seed: int, n: int, as_float: bool = False) -> np.ndarray:
 def from_lm_scene(scene) -> RefScene:
     """The reference's scene from a `lightmetrica` scene graph (the GPU mirror's SceneDefault), node
     for node as oracle.from_lm_scene rebuilds it, for the components compiled into the library
-    (mesh::raw, diffuse / glossy / glass / mirror, area / envconst / point / directional lights,
-    the pinhole camera). Anything else raises NotImplementedError."""
+    (mesh::raw, diffuse (textured or not) / glossy / glass / mirror / mixture_wavefrontobj /
+    proxy materials, area / envconst / point / directional / env lights, the pinhole camera).
+    Texture images go to the stb_image stand-in under names of their own, flipped back to file
+    order, and load flipped. Anything else raises NotImplementedError."""
     S = RefScene()
-    mesh_id, mat_id, light_id, cam_id = {}, {}, {}, {}
+    mesh_id, mat_id, light_id, cam_id, tex_id = {}, {}, {}, {}, {}
+    tag = f"lmref_mem/{id(scene):x}"
+
+    def image_of(texels, what):
+        path = f"{tag}/{what}.img"
+        register_image(path, np.ascontiguousarray(np.asarray(texels, np.float32)[::-1]))
+        return path
+
+    def tex_of(t):
+        # texture::constant's eval is its colour everywhere; a 1 x 1 bitmap of it answers the same
+        if t is None:
+            return -1
+        if id(t) not in tex_id:
+            tex_id[id(t)] = S.texture(image_of(t.texels(), f"tex{len(tex_id)}"), flip=True)
+        return tex_id[id(t)]
 
     def mesh_of(m):
         if id(m) not in mesh_id:
@@ -323,12 +397,23 @@ def from_lm_scene(scene) -> RefScene:
         ma = -1
         if n["material"] is not None:
             m = n["material"]
+            while m.key_name == "material::proxy":   # material_proxy.cpp: every query goes to 'ref'
+                m = m.ref
             if id(m) not in mat_id:
                 params = {"material::diffuse": lambda: list(m.Kd), "material::glossy": lambda: list(m.Ks) + [m.ax, m.ay],
                           "material::glass": lambda: [m.Ni], "material::mirror": lambda: []}
-                if m.key_name not in params or getattr(m, "mapKd", None) is not None:
+                mk = getattr(m, "mapKd", None)
+                if m.key_name == "material::mixture_wavefrontobj":
+                    # the mask is mapKd's alpha unless no_alpha_mask (model_wavefrontobj.cpp:403-410)
+                    no_mask = mk is not None and mk.has_alpha() and m.mask is None
+                    mat_id[id(m)] = S.material_tex(m.key_name, list(m.Kd) + list(m.Ks) + [m.ax, m.ay, no_mask],
+                                                   tex_of(mk))
+                elif m.key_name == "material::diffuse" and mk is not None:
+                    mat_id[id(m)] = S.material_tex(m.key_name, list(m.Kd), tex_of(mk))
+                elif m.key_name in params and mk is None:
+                    mat_id[id(m)] = S.material(m.key_name, params[m.key_name]())
+                else:
                     raise NotImplementedError(m.key_name)
-                mat_id[id(m)] = S.material(m.key_name, params[m.key_name]())
             ma = mat_id[id(m)]
         li = -1
         if n["light"] is not None:
@@ -342,6 +427,8 @@ def from_lm_scene(scene) -> RefScene:
                     light_id[id(L)] = S.light("light::point", list(L.Le) + list(L.position))
                 elif L.key_name == "light::directional":
                     light_id[id(L)] = S.light("light::directional", list(L.Le) + list(L.direction))
+                elif L.key_name == "light::env":
+                    light_id[id(L)] = S.light_env(image_of(L.data, f"env{len(light_id)}"), L.rot, L.scale)
                 else:
                     raise NotImplementedError(L.key_name)
             li = light_id[id(L)]

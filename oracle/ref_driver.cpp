@@ -23,6 +23,10 @@
 #include <lm/camera.h>
 #include <lm/film.h>
 #include <lm/renderer.h>
+#include <lm/texture.h>
+#include <lm/model.h>
+#include <lm/objloader.h>
+#include <stb/stb_image.h>
 #include <lm/parallel.h>
 #include <lm/progress.h>
 #include <lm/debug.h>
@@ -111,16 +115,35 @@ struct Handle {
         assets.push_back(std::move(c));
         return int(assets.size()) - 1;
     }
+    // Registered by locator before construct(), as assetgroup.cpp:62-86 does: a model's
+    // construct() hands its own locator's children (meshes, textures) to the lights and
+    // materials it creates.
     template <typename T> int create(const std::string& key, const std::string& name, const Json& prop) {
-        auto c = comp::create<Component>(key, loc(name), prop);
+        std::unique_ptr<Component> c(refshim::make(key));
         if (!c || !dynamic_cast<T*>(c.get())) throw std::invalid_argument("cannot create " + key);
-        return add(name, std::move(c));
+        c->lmref_set_ids(key, loc(name));
+        const int id = add(name, std::move(c));
+        try {
+            assets.back()->construct(prop);
+        } catch (...) {
+            refshim::remove_named(locs.back());
+            locs.pop_back();
+            assets.pop_back();
+            throw;
+        }
+        return id;
     }
     std::string next_name() const { return "asset" + std::to_string(assets.size()); }
     const std::string& asset_loc(int i) const { return locs.at(size_t(i)); }
 };
 
 int g_next_handle = 0;
+
+// objloader::init (objloader.cpp:13-15) runs once, as lm::init does (user.cpp:59).
+bool& objloader_ready() {
+    static bool r = false;
+    return r;
+}
 
 Handle* H(void* p) { return static_cast<Handle*>(p); }
 
@@ -152,6 +175,30 @@ Mat4 mat4(const double* m16) {
 }
 Json camera_prop(const double* prm) {
     return Json{{"position", v3(prm)}, {"center", v3(prm + 3)}, {"up", v3(prm + 6)}, {"vfov", prm[9]}, {"aspect", prm[10]}};
+}
+
+void material_records(const Material* m, const double* rec, long long n, double* out) {
+    for (long long i = 0; i < n; i++) {
+        const double* r = rec + 26 * i;
+        double* o = out + 18 * i;
+        const auto g = PointGeometry::make_on_surface(v3(r), v3(r + 3), v3(r + 6), Vec2(r[9], r[10]));
+        const Vec3 wi = v3(r + 11), wo = v3(r + 14);
+        const int comp = int(r[17]);
+        const auto td = r[18] != 0 ? Material::TransDir::EL : Material::TransDir::LE;
+        const bool ed = r[19] != 0;
+        put3(o, m->eval(g, wi, wo, comp, td, ed));
+        o[3] = m->pdf_direction(g, wi, wo, comp, ed);
+        const auto s = m->sample_direction({Vec2(r[20], r[21]), Vec2(r[22], r[23])}, g, wi, comp, td);
+        o[4] = s ? 1 : 0;
+        put3(o + 5, s ? s->wo : Vec3());
+        put3(o + 8, s ? s->weight : Vec3());
+        const auto cs = m->sample_component({Vec2(r[24], r[25])}, g, wi);
+        o[11] = cs.comp;
+        o[12] = cs.weight;
+        o[13] = m->pdf_component(comp, g, wi);
+        put3(o + 14, m->reflectance(g));
+        o[17] = m->is_specular_component(comp) ? 1 : 0;
+    }
 }
 
 }  // namespace
@@ -259,6 +306,107 @@ int lmref_scene_add_camera(void* p, const double* prm) {
 // film::bitmap of w x h. Returns an asset id.
 int lmref_scene_add_film(void* p, int w, int hgt) {
     return guarded([&] { return H(p)->create<Film>("film::bitmap", H(p)->next_name(), Json{{"w", w}, {"h", hgt}}); });
+}
+
+// An image for texture::bitmap under `path` (the stand-in stb_image's registry): h rows of w x c
+// floats, top row first, as decoded from a file.
+int lmref_register_image(const char* path, int w, int hgt, int c, const float* texels) {
+    return guarded([&] {
+        if (w <= 0 || hgt <= 0 || c < 3 || c > 4) throw std::invalid_argument("image shape");
+        auto& im = lmref_stb::images()[lmref_stb::key(path)];
+        im.w = w;
+        im.h = hgt;
+        im.c = c;
+        im.texels.assign(texels, texels + size_t(w) * size_t(hgt) * size_t(c));
+        return 0;
+    });
+}
+
+// texture::bitmap (src/texture/texture_bitmap.cpp) of a registered image. Returns an asset id.
+int lmref_scene_add_texture(void* p, const char* path, int flip) {
+    return guarded([&] {
+        return H(p)->create<Texture>("texture::bitmap", H(p)->next_name(), Json{{"path", path}, {"flip", flip != 0}});
+    });
+}
+
+// A material whose texture is an asset of the scene (-1 = none): material::diffuse Kd[3] with
+// mapKd; material::mixture_wavefrontobj (model_wavefrontobj.cpp:339-513) Kd[3], Ks[3], ax, ay,
+// no_alpha_mask with mapKd. Returns an asset id.
+int lmref_scene_add_material_tex(void* p, const char* key, const double* prm, int map_kd) {
+    return guarded([&] {
+        auto* h = H(p);
+        const std::string k(key);
+        const std::string tex = map_kd >= 0 ? h->asset_loc(map_kd) : std::string();
+        Json j = Json::object();
+        if (k == "material::diffuse") {
+            j["Kd"] = v3(prm);
+            if (map_kd >= 0) j["mapKd"] = tex;
+        } else if (k == "material::mixture_wavefrontobj") {
+            j["Kd"] = v3(prm);
+            j["Ks"] = v3(prm + 3);
+            j["ax"] = prm[6];
+            j["ay"] = prm[7];
+            j["no_alpha_mask"] = prm[8] != 0;
+            j["mapKd"] = tex;
+        } else {
+            throw std::invalid_argument("no textured form of " + k);
+        }
+        return h->create<Material>(k, h->next_name(), j);
+    });
+}
+
+// light::env (src/light/light_env.cpp) over a registered image `path` (loaded flipped, as
+// texture::bitmap does by default), rot in degrees, scale. Returns an asset id.
+int lmref_scene_add_light_env(void* p, const char* path, double rot, double scale) {
+    return guarded([&] {
+        return H(p)->create<Light>("light::env", H(p)->next_name(),
+                                   Json{{"path", path}, {"rot", rot}, {"scale", scale}});
+    });
+}
+
+// model::wavefrontobj (src/model/model_wavefrontobj.cpp) of an OBJ file, read by the reference's
+// objloader::simple (src/objloader/objloader_simple.cpp); its textures come from the image
+// registry under the paths the model makes of the MTL's map_Kd. skip_specular_mat as the model's
+// property; base_material an asset id or -1. Returns an asset id.
+int lmref_scene_add_model(void* p, const char* path, int skip_specular_mat, int base_material) {
+    return guarded([&] {
+        auto* h = H(p);
+        if (!objloader_ready()) {
+            objloader::init();
+            objloader_ready() = true;
+        }
+        Json j{{"path", path}, {"skip_specular_mat", skip_specular_mat != 0}};
+        if (base_material >= 0) j["base_material"] = h->asset_loc(base_material);
+        return h->create<Model>("model::wavefrontobj", h->next_name(), j);
+    });
+}
+
+// Scene::add_child_from_model (scene.cpp:158-180): one primitive node per group of the model
+// under node `parent`.
+int lmref_scene_add_child_from_model(void* p, int parent, int model) {
+    return guarded([&] {
+        auto* h = H(p);
+        const int before = h->scene->num_nodes();
+        h->scene->add_child_from_model(parent, h->asset_loc(model));
+        return h->scene->num_nodes() - before;
+    });
+}
+
+// Texture asset `tex` at n texture coordinates (uv[2] each). Out, 5 per point: eval[3],
+// eval_alpha (0 without alpha), has_alpha.
+int lmref_texture_query(void* p, int tex, const double* uv, long long n, double* out) {
+    return guarded([&] {
+        const auto* t = dynamic_cast<const Texture*>(H(p)->assets.at(size_t(tex)).get());
+        if (!t) throw std::invalid_argument("not a texture");
+        const bool a = t->has_alpha();
+        for (long long i = 0; i < n; i++) {
+            const Vec2 q(uv[2 * i], uv[2 * i + 1]);
+            put3(out + 5 * i, t->eval(q));
+            out[5 * i + 3] = a ? t->eval_alpha(q) : 0;
+            out[5 * i + 4] = a ? 1 : 0;
+        }
+        return 0;
+    });
 }
 
 // Primitive node (Scene::create_primitive_node, scene.cpp:71-126) over a mesh id and material,
@@ -452,27 +600,17 @@ int lmref_material_query(void* mp, const double* rec, long long n, double* out) 
     return guarded([&] {
         const auto* m = dynamic_cast<const Material*>(static_cast<Component*>(mp));
         if (!m) throw std::invalid_argument("not a material");
-        for (long long i = 0; i < n; i++) {
-            const double* r = rec + 26 * i;
-            double* o = out + 18 * i;
-            const auto g = PointGeometry::make_on_surface(v3(r), v3(r + 3), v3(r + 6), Vec2(r[9], r[10]));
-            const Vec3 wi = v3(r + 11), wo = v3(r + 14);
-            const int comp = int(r[17]);
-            const auto td = r[18] != 0 ? Material::TransDir::EL : Material::TransDir::LE;
-            const bool ed = r[19] != 0;
-            put3(o, m->eval(g, wi, wo, comp, td, ed));
-            o[3] = m->pdf_direction(g, wi, wo, comp, ed);
-            const auto s = m->sample_direction({Vec2(r[20], r[21]), Vec2(r[22], r[23])}, g, wi, comp, td);
-            o[4] = s ? 1 : 0;
-            put3(o + 5, s ? s->wo : Vec3());
-            put3(o + 8, s ? s->weight : Vec3());
-            const auto cs = m->sample_component({Vec2(r[24], r[25])}, g, wi);
-            o[11] = cs.comp;
-            o[12] = cs.weight;
-            o[13] = m->pdf_component(comp, g, wi);
-            put3(o + 14, m->reflectance(g));
-            o[17] = m->is_specular_component(comp) ? 1 : 0;
-        }
+        material_records(m, rec, n, out);
+        return 0;
+    });
+}
+
+// The same queries on material asset `mat` of a scene (a textured one among them).
+int lmref_scene_material_query(void* p, int mat, const double* rec, long long n, double* out) {
+    return guarded([&] {
+        const auto* m = dynamic_cast<const Material*>(H(p)->assets.at(size_t(mat)).get());
+        if (!m) throw std::invalid_argument("not a material");
+        material_records(m, rec, n, out);
         return 0;
     });
 }

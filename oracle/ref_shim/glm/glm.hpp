@@ -34,6 +34,7 @@ template <typename T> struct tvec2 {
     explicit tvec2(T s) : x(s), y(s) {}
     tvec2(T a, T b) : x(a), y(b) {}
     template <typename U> explicit tvec2(const tvec2<U>& v) : x(T(v.x)), y(T(v.y)) {}
+    tvec2(const tvec3<T>& v);  // drops z (implicit, as glm's is by default)
     T& operator[](int i) { return (&x)[i]; }
     const T& operator[](int i) const { return (&x)[i]; }
 };
@@ -60,11 +61,13 @@ template <typename T> struct tvec4 {
     explicit tvec4(T s) : x(s), y(s), z(s), w(s) {}
     tvec4(T a, T b, T c, T d) : x(a), y(b), z(c), w(d) {}
     tvec4(const tvec3<T>& v, T d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    tvec4(const tvec2<T>& a, const tvec2<T>& b) : x(a.x), y(a.y), z(b.x), w(b.y) {}
     T& operator[](int i) { return data.data[i]; }
     const T& operator[](int i) const { return data.data[i]; }
 };
 
 template <typename T> inline tvec3<T>::tvec3(const tvec4<T>& v) : x(v.x), y(v.y), z(v.z) {}
+template <typename T> inline tvec2<T>::tvec2(const tvec3<T>& v) : x(v.x), y(v.y) {}
 
 // -- component-wise arithmetic -------------------------------------------------------------------
 #define LMREF_GLM_BINOP(V, N, OP)                                                                  \

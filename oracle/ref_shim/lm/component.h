@@ -9,10 +9,15 @@
 //   * Json -- a small JSON value (null, number, string, array, object) with the nlohmann-style
 //     access they call: operator[], size(), find() / end() / value(), get<T>() and implicit
 //     conversions to numbers, strings, vectors and 4x4 matrices; brace-initialised objects;
-//   * json::value / value_or_none / comp_ref / comp_ref_or_nullptr -- property reads;
+//     raw pointers held as values (model_wavefrontobj.cpp:83-86 hands its mesh components the
+//     model and a face list that way, read back with get<T*>());
+//   * json::value / value_or_none / comp_ref / comp_ref_or_nullptr / merge -- property reads;
 //   * Component (key, locator, name, make_loc, construct / underlying hooks), Component::Ptr;
-//   * comp::create (factory by key, constructed with its properties), comp::get (lookup by
-//     locator among components registered with refshim::add_named), comp::visit;
+//   * comp::create (factory by key, constructed with its properties), comp::get (a locator
+//     registered with refshim::add_named, or one below it resolved through underlying(), as
+//     component.cpp:322-360 walks the hierarchy), comp::visit, comp::detail::ContextInstance
+//     (the singleton context objloader.cpp keeps);
+//   * fmt::format with positional "{}" fields;
 //   * LM_COMP_REG_IMPL -- factory registration by key;
 //   * LM_SERIALIZE_IMPL -- opens a serialization template that is never instantiated;
 //   * logging macros, dropped; errors thrown as std::runtime_error; the floating-point-exception
@@ -29,7 +34,7 @@ LM_NAMESPACE_BEGIN(LM_NAMESPACE)
 
 class Json {
 public:
-    enum class Type { Null, Number, String, Array, Object };
+    enum class Type { Null, Number, String, Array, Object, Pointer };
 
     Json() = default;
     Json(std::nullptr_t) {}
@@ -43,6 +48,8 @@ public:
     Json(bool v) : type_(Type::Number), num_(v ? 1 : 0) {}
     Json(const char* s) : type_(Type::String), str_(s) {}
     Json(const std::string& s) : type_(Type::String), str_(s) {}
+    Json(char* s) : type_(Type::String), str_(s) {}
+    template <typename T> Json(T* p) : type_(Type::Pointer), ptr_(static_cast<const void*>(p)) {}
     Json(const Vec2& v) : type_(Type::Array) { arr_ = {Json(v.x), Json(v.y)}; }
     Json(const Vec3& v) : type_(Type::Array) { arr_ = {Json(v.x), Json(v.y), Json(v.z)}; }
     Json(const Vec4& v) : type_(Type::Array) { arr_ = {Json(v.x), Json(v.y), Json(v.z), Json(v.w)}; }
@@ -94,6 +101,17 @@ public:
     const_iterator find(const std::string& k) const { return {obj_.find(k)}; }
     const_iterator end() const { return {obj_.end()}; }
     bool contains(const std::string& k) const { return obj_.count(k) > 0; }
+    // nlohmann's merge_patch restricted to one level: o's keys replace this object's.
+    Json merged(const Json& o) const {
+        Json r = *this;
+        r.type_ = Type::Object;
+        for (const auto& [k, v] : o.obj_) r.obj_[k] = v;
+        return r;
+    }
+    const void* pointer() const {
+        if (type_ != Type::Pointer) throw std::invalid_argument("not a pointer");
+        return ptr_;
+    }
 
     double number() const {
         if (type_ != Type::Number) throw std::invalid_argument("not a number");
@@ -138,13 +156,17 @@ private:
     std::string str_;
     std::vector<Json> arr_;
     std::map<std::string, Json> obj_;
+    const void* ptr_ = nullptr;
 };
 
-template <typename T> inline T Json::get() const { return static_cast<T>(*this); }
+template <typename T> inline T Json::get() const {
+    if constexpr (std::is_pointer_v<T>) return static_cast<T>(const_cast<void*>(pointer()));
+    else return static_cast<T>(*this);
+}
 template <> inline std::string Json::get<std::string>() const { return string(); }
 
 // ------------------------------------------------------------------------------------------------
-// Errors and logging
+// Errors, logging and formatting
 
 enum class Error {
     None,
@@ -159,6 +181,27 @@ enum class Error {
 LM_NAMESPACE_BEGIN(exception)
 struct ScopedDisableFPEx {};
 LM_NAMESPACE_END(exception)
+
+LM_NAMESPACE_END(LM_NAMESPACE)
+namespace fmt {
+// Each "{}" of f takes the next argument, written as operator<< writes it.
+template <typename... Args> std::string format(const std::string& f, const Args&... args) {
+    std::vector<std::string> parts;
+    ((parts.push_back((std::ostringstream() << args).str())), ...);
+    std::string out;
+    size_t next = 0;
+    for (size_t i = 0; i < f.size(); i++) {
+        if (f[i] == '{' && i + 1 < f.size() && f[i + 1] == '}' && next < parts.size()) {
+            out += parts[next++];
+            i++;
+        } else {
+            out += f[i];
+        }
+    }
+    return out;
+}
+}  // namespace fmt
+LM_NAMESPACE_BEGIN(LM_NAMESPACE)
 
 // ------------------------------------------------------------------------------------------------
 // Components
@@ -218,9 +261,24 @@ template <typename Impl> struct Registrar {
 LM_NAMESPACE_END(refshim)
 
 LM_NAMESPACE_BEGIN(comp)
+// A registered locator, or one below the longest registered prefix reached through underlying()
+// one dot-separated name at a time.
 template <typename T> T* get(const std::string& locator) {
-    auto it = refshim::named().find(locator);
-    return it == refshim::named().end() ? nullptr : dynamic_cast<T*>(it->second);
+    const auto& n = refshim::named();
+    if (const auto it = n.find(locator); it != n.end()) return dynamic_cast<T*>(it->second);
+    for (size_t i = locator.rfind('.'); i != std::string::npos && i > 0; i = locator.rfind('.', i - 1)) {
+        const auto it = n.find(locator.substr(0, i));
+        if (it == n.end()) continue;
+        Component* c = it->second;
+        std::string rest = locator.substr(i + 1);
+        while (c && !rest.empty()) {
+            const size_t j = rest.find('.');
+            c = c->underlying(rest.substr(0, j));
+            rest = j == std::string::npos ? std::string() : rest.substr(j + 1);
+        }
+        return dynamic_cast<T*>(c);
+    }
+    return nullptr;
 }
 template <typename InterfaceT>
 Component::Ptr<InterfaceT> create(const std::string& key, const std::string& loc, const Json& prop = {}) {
@@ -242,6 +300,28 @@ template <typename T> void visit(const Component::ComponentVisitor& visitor, Com
     Component* c = p.get();
     visitor(c, false);
 }
+LM_NAMESPACE_BEGIN(detail)
+// A process-wide context component created by key (the objloader's).
+template <typename ContextComponentT> class ContextInstance {
+public:
+    static ContextComponentT& get() {
+        if (!ctx()) throw std::runtime_error("lm error: Uninitialized context component");
+        return *ctx();
+    }
+    static void init(const std::string& type, const Json& prop) {
+        ctx() = comp::create<ContextComponentT>(type, "$", prop);
+        if (!ctx()) throw std::invalid_argument("no context component registered as " + type);
+    }
+    static void shutdown() { ctx().reset(); }
+    static bool initialized() { return bool(ctx()); }
+
+private:
+    static Component::Ptr<ContextComponentT>& ctx() {
+        static Component::Ptr<ContextComponentT> p;
+        return p;
+    }
+};
+LM_NAMESPACE_END(detail)
 LM_NAMESPACE_END(comp)
 
 // ------------------------------------------------------------------------------------------------
@@ -277,6 +357,7 @@ template <typename T> T* comp_ref(const Json& j, const std::string& name) {
     if (!p) throw std::invalid_argument("missing component reference " + name);
     return p;
 }
+inline Json merge(const Json& a, const Json& b) { return a.merged(b); }
 LM_NAMESPACE_END(json)
 
 LM_NAMESPACE_END(LM_NAMESPACE)
