@@ -1061,11 +1061,13 @@ class SceneDefault(Component):
             nm = np.linalg.inv(m.astype(np.float64)).T[:3, :3].astype(np.float32)
             wn = (tn @ nm.T).astype(np.float32)
         lp = tp.astype(np.float32)
-        g = np.cross(lp[:, 1] - lp[:, 0], lp[:, 2] - lp[:, 0]).astype(np.float32)
-        g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
-        if not ident:
-            g = (g @ nm.T).astype(np.float32)
+        # a zero-area triangle's normal is NaN, as glm::normalize of a zero vector makes it
+        with np.errstate(invalid="ignore", divide="ignore"):
+            g = np.cross(lp[:, 1] - lp[:, 0], lp[:, 2] - lp[:, 0]).astype(np.float32)
             g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
+            if not ident:
+                g = (g @ nm.T).astype(np.float32)
+                g = g / np.sqrt(np.sum(g * g, axis=1, keepdims=True)).astype(np.float32)
         return wp.reshape(-1, 9), wn.reshape(-1, 9), g.reshape(-1, 3)
 
     def _has_instances(self) -> bool:
