@@ -69,10 +69,13 @@ __device__ inline float refine_hit_t(const float4 ra, const float4 rb, const flo
     return __double2float_rn(__ddiv_rn(num, det));
 }
 
-// rays: 2 float4 per ray (o, tmin) (d, tmax). refill > 0: each block takes one contiguous chunk
-// of the rays and its warps fetch from it dynamically through a shared-memory counter (no state
-// outside the launch, so calls on several streams may overlap); 0: one ray per thread,
-// grid-stride.
+// rays: 2 float4 per ray (o, tmin) (d, tmax). refill > 0: block b of G takes the groups of 32
+// consecutive rays b, b + G, b + 2G, ... and its warps fetch from them dynamically through a
+// shared-memory counter (no state outside the launch, so calls on several streams may overlap).
+// Interleaving the groups gives every block a sample of the whole batch: with one contiguous
+// chunk per block, rays in caller order (camera rays, bounces sorted by origin or direction) left
+// some blocks all the expensive rays, and a batch of diffuse bounces in pixel order traced 11 %
+// slower than the same rays shuffled. refill == 0: one ray per thread, grid-stride.
 template <bool kAnyHit, bool kTwoLevel>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const float4* __restrict__ rays, int64_t n,
                                                             lmgpu_hit* __restrict__ hits, uint8_t* __restrict__ occluded,
@@ -96,17 +99,23 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_batch(Bvh8 bvh, const flo
         }
     };
     if (refill > 0) {
-        const int64_t per = (n + gridDim.x - 1) / gridDim.x;
-        const int64_t b0 = min(n, per * int64_t(blockIdx.x)), b1 = min(n, b0 + per);
+        const int64_t G = gridDim.x, blk = blockIdx.x;
+        const int64_t ngroups = (n + 31) / 32;
+        const int64_t mine = blk < ngroups ? (ngroups - 1 - blk) / G + 1 : 0;
+        // only the batch's last group can be short, and it is this block's last one if it is ours
+        int64_t count = mine * 32;
+        if (mine > 0 && blk + (mine - 1) * G == ngroups - 1) count -= ngroups * 32 - n;
+        auto ray_of = [&](int k) { return (blk + int64_t(k >> 5) * G) * 32 + (k & 31); };
         if (threadIdx.x == 0) s_fetch = 0;
         __syncthreads();
         fetch_loop<kAnyHit, false, kTwoLevel>(
-            int(b1 - b0), Fetch{&s_fetch, nullptr, refill}, bvh, sb, sbits, stride, &lerr,
+            int(count), Fetch{&s_fetch, nullptr, refill}, bvh, sb, sbits, stride, &lerr,
             [&](int k, Trav& s, Bvh8&) {
-                const float4 a = rays[2 * (b0 + k)], b = rays[2 * (b0 + k) + 1];
+                const int64_t i = ray_of(k);
+                const float4 a = rays[2 * i], b = rays[2 * i + 1];
                 trav_init(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), a.w, b.w);
             },
-            [&](int k, const Trav& s) { store(b0 + k, s.best); });
+            [&](int k, const Trav& s) { store(ray_of(k), s.best); });
     } else {
         for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
             const float4 a = rays[2 * i], b = rays[2 * i + 1];
