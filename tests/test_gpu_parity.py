@@ -252,6 +252,37 @@ def test_pt_matched_stream_env_map_and_mirror(lm, oracle_mod):
     assert _rel_l1(gpu, ref) < 3e-3, _rel_l1(gpu, ref)
 
 
+def test_pt_env_map_with_black_rows(lm, oracle_mod):
+    """An env map with rows of zero luminance. The reference's Dist2 normalizes such a row by its
+    zero sum (math.h Dist::init), so a BSDF-sampled direction into it has a NaN pdf_direct and
+    renderer::pt with MIS writes NaN (the fp64 restatement reproduces it, pinned to the
+    reference's own code). The GPU gives those rows zero density: its MIS weight is 1 there and
+    the black texels add nothing. Every GPU pixel is finite, and the pixels the restatement
+    renders finite agree on the matched stream."""
+    from lightmetrica import synthetic as syn
+    film = lm.load_film("film", "bitmap", w=40, h=30)
+    cam = lm.load_camera("cam", "pinhole", position=[0, 1.5, 5], center=[0, 0.5, 0], up=[0, 1, 0], vfov=45, aspect=4 / 3)
+    scene = lm.load_scene("scene", "default", accel=lm.load_accel("accel", "sahbvh"))
+    scene.add_primitive(camera=cam)
+    v, f = syn.icosphere(3)
+    for k, (mat, cx) in enumerate([(lm.load_material("d", "diffuse", Kd=[0.8, 0.6, 0.4]), -1.2),
+                                   (lm.load_material("gl", "glossy", Ks=[0.9, 0.9, 0.9], ax=0.2, ay=0.35), 1.2)]):
+        p = (v * 0.5 + [cx, 0.5, 0]).astype(np.float32)
+        mesh = lm.load_mesh(f"s{k}", "raw", ps=p, ns=v.astype(np.float32), ts=[0, 0],
+                            fs={"p": f.ravel(), "n": f.ravel(), "t": np.zeros(f.size, int)})
+        scene.add_primitive(mesh=mesh, material=mat)
+    env = syn.env_texture().copy()
+    env[: env.shape[0] // 4] = 0.0      # the lowest quarter of the sphere black
+    env[env.shape[0] // 2] = 0.0        # and the row at the horizon
+    scene.add_primitive(light=lm.load_light("env", "env", envmap=env, rot=30, scale=1.5))
+    gpu, ref, _, _ = _pt_pair(lm, oracle_mod, scene, film, 40, 30, 8, 6)
+    nan = np.isnan(ref).any(axis=2)
+    assert nan.sum() > 10                # the case occurs on this scene
+    assert np.isfinite(gpu).all()
+    ok = ~nan
+    assert _rel_l1(gpu[ok], ref[ok]) < 3e-3, _rel_l1(gpu[ok], ref[ok])
+
+
 def test_pt_matched_stream_image_mode(lm, oracle_mod):
     from lightmetrica import synthetic as syn
     scene, film = syn.box_scene(w=24, h=24)
