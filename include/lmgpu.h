@@ -130,8 +130,8 @@ int lmgpu_accel_build_instanced_ex(lmgpu_accel* accel, const float* tri_p, const
 /* Accel::intersect(Ray, tmin, tmax) (include/lm/accel.h:70; accel_sahbvh.cpp:269-299) over a
  * batch. Host buffers: rays is n x 8 floats (ox, oy, oz, tmin, dx, dy, dz, tmax); hits receives n
  * records. Copies in, traces, copies out, and returns when the hits are in `hits`. With page-locked
- * (pinned) host buffers, batches larger than 2^21 rays go in chunks over two streams, so that the
- * copies of one chunk run beside the trace of the next. */
+ * (pinned) host buffers, batches larger than 2^21 rays go in chunks through three streams (copy in,
+ * trace, copy out), so that the copies run beside the trace. */
 int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgpu_hit* hits);
 
 /* Same, device-resident: d_rays (n x 8 floats, 16-byte aligned) and d_hits (n records) are

@@ -6,7 +6,9 @@
 #include <chrono>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
+#include "hit_t.h"
 #include "lmgpu_dev.cuh"
 #include "runtime.h"
 
@@ -48,25 +50,16 @@ std::shared_mutex& capture_mutex() {
 
 constexpr int kTraceBlock = 128;
 
-// Hit distance of an accepted hit, recomputed in double from the same fp32 ray and triangle record
-// (p1, e1, e2) with the operations of accel_sahbvh.cpp:58-75 in their order (p = d x e2,
-// tv = o - p1, q = tv x e1, t = (e2 . q) / (e1 . p); glm's dot and cross order) and rounded once
-// to float. The fp32 test still decides which triangle is hit and where the traversal stops;
-// this only makes the reported t agree with the reference's fp64 value to fp32 rounding (an fp32
-// t of a grazing hit can be 2e-5 off relative). Explicit IEEE double ops: no contraction.
+// Hit distance of an accepted hit: the reference's fp64 distance (accel_sahbvh.cpp:58-75) from the
+// same fp32 ray and triangle record (p1, e1, e2), rounded once to float (hit_t.h: a double-float
+// evaluation that falls back to the fp64 chain when it cannot decide the float). The fp32 test
+// still decides which triangle is hit and where the traversal stops; this only makes the reported
+// t agree with the reference's fp64 value to fp32 rounding (an fp32 t of a grazing hit can be
+// 2e-5 off relative).
 __device__ inline float refine_hit_t(const float4 ra, const float4 rb, const float4 a, const float4 b, const float4 c) {
-    const double ox = ra.x, oy = ra.y, oz = ra.z, dx = rb.x, dy = rb.y, dz = rb.z;
-    const double e1x = a.w, e1y = b.x, e1z = b.y, e2x = b.z, e2y = b.w, e2z = c.x;
-    const double px = __dsub_rn(__dmul_rn(dy, e2z), __dmul_rn(e2y, dz));
-    const double py = __dsub_rn(__dmul_rn(dz, e2x), __dmul_rn(e2z, dx));
-    const double pz = __dsub_rn(__dmul_rn(dx, e2y), __dmul_rn(e2x, dy));
-    const double tx = __dsub_rn(ox, double(a.x)), ty = __dsub_rn(oy, double(a.y)), tz = __dsub_rn(oz, double(a.z));
-    const double qx = __dsub_rn(__dmul_rn(ty, e1z), __dmul_rn(e1y, tz));
-    const double qy = __dsub_rn(__dmul_rn(tz, e1x), __dmul_rn(e1z, tx));
-    const double qz = __dsub_rn(__dmul_rn(tx, e1y), __dmul_rn(e1x, ty));
-    const double det = __dadd_rn(__dadd_rn(__dmul_rn(e1x, px), __dmul_rn(e1y, py)), __dmul_rn(e1z, pz));
-    const double num = __dadd_rn(__dadd_rn(__dmul_rn(e2x, qx), __dmul_rn(e2y, qy)), __dmul_rn(e2z, qz));
-    return __double2float_rn(__ddiv_rn(num, det));
+    const float o[3] = {ra.x, ra.y, ra.z}, d[3] = {rb.x, rb.y, rb.z}, p1[3] = {a.x, a.y, a.z};
+    const float e1[3] = {a.w, b.x, b.y}, e2[3] = {b.z, b.w, c.x};
+    return lmgpu_ht::hit_t(o, d, p1, e1, e2);
 }
 
 // rays: 2 float4 per ray (o, tmin) (d, tmax). refill > 0: block b of G takes the groups of 32
@@ -518,9 +511,13 @@ int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgp
         if (n == 0) return;
         accel->scratch_rays.alloc(size_t(n) * 32);
         accel->scratch_hits.alloc(size_t(n) * sizeof(lmgpu_hit));
-        // With page-locked host buffers, chunks of 2^21 rays alternate between two streams, so that
-        // one chunk's copies run beside the next chunk's trace. Pageable buffers go in one copy each
-        // way (chunked copies from pageable memory measured slower: 1,102 -> 775 Mrays/s).
+        // With page-locked host buffers the batch goes in chunks of 2^21 rays through three streams:
+        // one copies every chunk in back to back, one traces each chunk once its rays are in, one
+        // copies each chunk's hits out once traced, so the copy engines and the trace run side by
+        // side (two streams that each copied in, traced and copied out their own chunks kept the
+        // next copy-in waiting behind a copy-out: 2,914 Mrays/s against 4,178 on the device).
+        // Pageable buffers go in one copy each way (chunked copies from pageable memory measured
+        // slower: 1,102 -> 775 Mrays/s).
         constexpr int64_t kChunk = int64_t(1) << 21;
         auto page_locked = [](const void* p) {
             cudaPointerAttributes a{};
@@ -537,46 +534,53 @@ int lmgpu_accel_intersect(lmgpu_accel* accel, const float* rays, int64_t n, lmgp
             LMGPU_CUDA_SYNC(cudaMemcpy(hits, accel->scratch_hits.p, size_t(n) * sizeof(lmgpu_hit), cudaMemcpyDeviceToHost));
         } else {
             std::shared_lock<std::shared_mutex> lk(capture_mutex());
-            cudaStream_t sts[2] = {nullptr, nullptr};
-            cudaEvent_t cleared = nullptr;
-            LMGPU_CUDA(cudaStreamCreateWithFlags(&sts[0], cudaStreamNonBlocking));
-            cudaError_t e1 = cudaStreamCreateWithFlags(&sts[1], cudaStreamNonBlocking);
-            if (e1 == cudaSuccess) e1 = cudaEventCreateWithFlags(&cleared, cudaEventDisableTiming);
-            if (e1 != cudaSuccess) {
-                cudaStreamDestroy(sts[0]);
-                if (sts[1]) cudaStreamDestroy(sts[1]);
-                LMGPU_CUDA(e1);
-            }
+            const int64_t nchunks = (n + kChunk - 1) / kChunk;
+            cudaStream_t sts[3] = {nullptr, nullptr, nullptr};  // copy in, trace, copy out
+            std::vector<cudaEvent_t> evs(size_t(2 * nchunks), nullptr);
+            auto release = [&] {
+                for (auto st : sts)
+                    if (st) {
+                        cudaStreamSynchronize(st);
+                        cudaStreamDestroy(st);
+                    }
+                for (auto e : evs)
+                    if (e) cudaEventDestroy(e);
+            };
+            cudaError_t first_err = cudaSuccess;
             try {
-                // the error flag is cleared on the first stream before either stream's first trace
-                LMGPU_CUDA(cudaMemsetAsync(accel->err.p, 0, sizeof(int), sts[0]));
-                LMGPU_CUDA(cudaEventRecord(cleared, sts[0]));
-                LMGPU_CUDA(cudaStreamWaitEvent(sts[1], cleared, 0));
+                for (auto& st : sts) LMGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+                for (auto& e : evs) LMGPU_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
                 char* d_r = static_cast<char*>(accel->scratch_rays.p);
                 char* d_h = static_cast<char*>(accel->scratch_hits.p);
-                for (int64_t off = 0, c = 0; off < n; off += kChunk, c++) {
-                    const int64_t m = std::min(kChunk, n - off);
-                    cudaStream_t st = sts[c & 1];
-                    LMGPU_CUDA(cudaMemcpyAsync(d_r + off * 32, rays + off * 8, size_t(m) * 32, cudaMemcpyHostToDevice, st));
-                    launch_trace(accel, d_r + off * 32, m, d_h + off * int64_t(sizeof(lmgpu_hit)), nullptr, st, accel->err.as<int>());
+                // the error flag is cleared on the trace stream before its first trace
+                LMGPU_CUDA(cudaMemsetAsync(accel->err.p, 0, sizeof(int), sts[1]));
+                for (int64_t c = 0; c < nchunks; c++) {
+                    const int64_t off = c * kChunk, m = std::min(kChunk, n - off);
+                    LMGPU_CUDA(cudaMemcpyAsync(d_r + off * 32, rays + off * 8, size_t(m) * 32, cudaMemcpyHostToDevice, sts[0]));
+                    LMGPU_CUDA(cudaEventRecord(evs[size_t(2 * c)], sts[0]));
+                }
+                for (int64_t c = 0; c < nchunks; c++) {
+                    const int64_t off = c * kChunk, m = std::min(kChunk, n - off);
+                    LMGPU_CUDA(cudaStreamWaitEvent(sts[1], evs[size_t(2 * c)], 0));
+                    launch_trace(accel, d_r + off * 32, m, d_h + off * int64_t(sizeof(lmgpu_hit)), nullptr, sts[1],
+                                 accel->err.as<int>());
+                    LMGPU_CUDA(cudaEventRecord(evs[size_t(2 * c + 1)], sts[1]));
+                }
+                for (int64_t c = 0; c < nchunks; c++) {
+                    const int64_t off = c * kChunk, m = std::min(kChunk, n - off);
+                    LMGPU_CUDA(cudaStreamWaitEvent(sts[2], evs[size_t(2 * c + 1)], 0));
                     LMGPU_CUDA(cudaMemcpyAsync(hits + off, d_h + off * int64_t(sizeof(lmgpu_hit)), size_t(m) * sizeof(lmgpu_hit),
-                                               cudaMemcpyDeviceToHost, st));
+                                               cudaMemcpyDeviceToHost, sts[2]));
+                }
+                for (auto st : sts) {
+                    const cudaError_t e = cudaStreamSynchronize(st);
+                    if (first_err == cudaSuccess) first_err = e;
                 }
             } catch (...) {
-                for (auto st : sts) {
-                    cudaStreamSynchronize(st);
-                    cudaStreamDestroy(st);
-                }
-                cudaEventDestroy(cleared);
+                release();
                 throw;
             }
-            cudaError_t first_err = cudaSuccess;
-            for (auto st : sts) {
-                const cudaError_t e = cudaStreamSynchronize(st);
-                if (first_err == cudaSuccess) first_err = e;
-                cudaStreamDestroy(st);
-            }
-            cudaEventDestroy(cleared);
+            release();
             LMGPU_CUDA(first_err);
         }
         int herr = 0;
