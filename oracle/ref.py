@@ -4,7 +4,7 @@ src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,mirror,proxy}
 src/light/light_{area,envconst,point,directional,env}.cpp, src/texture/texture_bitmap.cpp,
 src/objloader/objloader{,_simple}.cpp, src/model/model_wavefrontobj.cpp (with
 material::mixture_wavefrontobj), src/camera/camera_pinhole.cpp, src/film/film_bitmap.cpp,
-src/scheduler.cpp, src/renderer/renderer_{pt,lt,bdpt}.cpp and the headers they include (math.h,
+src/scheduler.cpp, src/renderer/renderer_{raycast,pt,lt,bdpt}.cpp and the headers they include (math.h,
 surface.h, scene.h, path.h, bidir.h, ...). stb_image, which texture_bitmap.cpp decodes images
 with, is not among the reference's sources: images reach it decoded, through register_image.
 
@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
         L.lmref_accel_intersect.argtypes = [vp, fp, C.c_longlong, dp, dp, ip, ip, lp, C.c_int]
         L.lmref_render_pt.argtypes = [vp, C.c_int, C.c_longlong, C.c_int, C.c_uint, C.c_int, C.c_int, dp]
         L.lmref_render_spi.argtypes = [vp, C.c_char_p, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_uint, dp]
+        L.lmref_render_raycast.argtypes = [vp, C.c_int, dp, C.c_int, C.c_int, C.c_int, dp, dp]
         L.lmref_light_query.argtypes = [vp, C.c_int, dp, dp, C.c_longlong, dp]
         L.lmref_register_image.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, fp]
         L.lmref_scene_add_texture.argtypes = [vp, C.c_char_p, C.c_int]
@@ -256,6 +257,17 @@ class RefScene:
         out = np.zeros((h, w, 3))
         _chk(lib().lmref_render_spi(self.h, key.encode(), film, num_samples, min_verts, max_verts, seed & 0xFFFFFFFF,
                                     _p(out, C.c_double)))
+        return out
+
+    def render_raycast(self, film: int, bg=(0, 0, 0), use_constant_color: bool = False, visualize_normal: bool = False,
+                       color=None) -> np.ndarray:
+        """The reference's renderer::raycast into film asset `film`; returns its h x w x 3 buffer."""
+        w, h = self.films[film]
+        out = np.zeros((h, w, 3))
+        bgv = np.asarray(bg, np.float64)
+        col = np.asarray(color if color is not None else (0, 0, 0), np.float64)
+        _chk(lib().lmref_render_raycast(self.h, film, _p(bgv, C.c_double), int(use_constant_color), int(visualize_normal),
+                                        int(color is not None), _p(col, C.c_double), _p(out, C.c_double)))
         return out
 
     def light_query(self, light: int, m4, rec: np.ndarray) -> np.ndarray:

@@ -534,6 +534,30 @@ int lmref_render_pt(void* p, int film, long long samples, int max_verts, unsigne
     });
 }
 
+// renderer::raycast (src/renderer/renderer_raycast.cpp) over the scene into film asset `film`:
+// background bg[3], use_constant_color, visualize_normal, and a constant color[3] when has_color.
+// out: the film's h x w x 3.
+int lmref_render_raycast(void* p, int film, const double* bg, int use_constant_color, int visualize_normal, int has_color,
+                         const double* color, double* out) {
+    return guarded([&] {
+        auto* h = H(p);
+        Json prop = Json::object();
+        prop["scene"] = h->asset_loc(h->scene_asset);
+        prop["output"] = h->asset_loc(film);
+        prop["bg_color"] = v3(bg);
+        prop["use_constant_color"] = use_constant_color != 0;
+        prop["visualize_normal"] = visualize_normal != 0;
+        if (has_color) prop["color"] = v3(color);
+        auto r = comp::create<Renderer>("renderer::raycast", h->loc("renderer_raycast"), prop);
+        if (!r) throw std::invalid_argument("cannot create renderer::raycast");
+        r->render();
+        auto* f = dynamic_cast<Film*>(h->assets.at(size_t(film)).get());
+        const auto b = f->buffer();
+        std::memcpy(out, b.data, sizeof(double) * 3 * size_t(b.w) * size_t(b.h));
+        return 0;
+    });
+}
+
 // A light-tracing renderer of the reference over the scene into film asset `film`, scheduled by
 // scheduler::spi::sample over `num_samples` light paths: key "renderer::lt", "renderer::bdpt"
 // (min_verts, max_verts) or one of bdpt's strategy renderers ("renderer::pt_naive_path",

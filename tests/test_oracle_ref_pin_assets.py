@@ -2,7 +2,8 @@
 
 oracle/_ref/liblmref.so also compiles src/texture/texture_bitmap.cpp, src/light/light_env.cpp,
 src/objloader/objloader{,_simple}.cpp, src/model/model_wavefrontobj.cpp (the model with its OBJ
-mesh and material::mixture_wavefrontobj) and src/material/material_proxy.cpp unmodified.
+mesh and material::mixture_wavefrontobj), src/material/material_proxy.cpp and
+src/renderer/renderer_raycast.cpp unmodified.
 stb_image, which texture_bitmap.cpp decodes image files with, is third-party and not among the
 reference's sources: the library's stand-in takes images already decoded (oracle/ref.py
 register_image), so these tests pin everything after the decode -- texel lookup with wrapping and
@@ -379,3 +380,40 @@ def test_textured_env_scene_from_lm_scene_matches_reference(ref_mod, oracle_mod,
     assert np.nansum(a) > 0
     bad = np.argwhere(~((a == b) | (np.isnan(a) & np.isnan(b))).all(axis=2))
     assert bad.size == 0, f"{len(bad)} pixels differ, first {bad[:4].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
+
+
+@pytest.mark.parametrize("which", ["box", "spheres_env"])
+@pytest.mark.parametrize("mode", ["shaded", "normal", "constant", "color"])
+def test_raycast_images_match_reference_renderer(ref_mod, oracle_mod, lm, which, mode):
+    """renderer_raycast.cpp (primary rays at pixel centres, reflectance times 0.2 + 0.8 |n . d|, the
+    environment's radiance where a ray escapes, the background where nothing is hit): its
+    shaded, normal-visualising, constant-colour and colour-override images against the
+    restatement's, every pixel bit for bit; the spheres carry a textured diffuse and a mixture
+    material under an env map."""
+    from lightmetrica import synthetic as syn
+    p = f"pin_rc_{which}_{mode}_"
+    if which == "box":
+        scene, film = syn.box_scene(w=32, h=24, prefix=p)
+    else:
+        scene, film, _ = syn.spheres_scene(n_spheres=5, subdiv=3, ground_quads=8, w=30, h=18, prefix=p)
+        rng = np.random.default_rng(4)
+        for n in scene.nodes:
+            if n["type"] == "primitive" and n["light"] is not None and n["light"].key_name == "light::envconst":
+                n["light"] = lm.load_light(p + "env", "env", envmap=_env_image(rng)[::-1], rot=15.0, scale=1.2)
+        prims = [n for n in scene.nodes if n["type"] == "primitive" and n["mesh"] is not None and n["light"] is None]
+        prims[0]["material"] = lm.load_material(p + "d", "diffuse", Kd=[0.5, 0.5, 0.5],
+                                                 mapKd=lm.load_texture(p + "t", "bitmap", data=_image(rng, 4, 5, 3)))
+        prims[1]["material"] = lm.load_material(p + "mx", "mixture_wavefrontobj", Kd=[0.4, 0.5, 0.6], Ks=[0.5, 0.5, 0.5],
+                                                ax=0.2, ay=0.3, mapKd="", no_alpha_mask=False)
+    kw = {"shaded": {}, "normal": {"visualize_normal": True}, "constant": {"use_constant_color": True},
+          "color": {"color": (0.25, 0.5, 0.75)}}[mode]
+    bg = (0.1, 0.2, 0.3)
+    S = ref_mod.from_lm_scene(scene)
+    f = S.film(film.w, film.h)
+    S.build()
+    a = S.render_raycast(f, bg=bg, **kw)
+    O = oracle_mod.from_lm_scene(scene, double=True)
+    O.build()
+    b, _ = O.render_raycast(film.w, film.h, bg=bg, nthreads=1, **kw)
+    assert np.abs(a).sum() > 0
+    assert _same_bits(a, b), f"{int((a != b).any(axis=2).sum())} pixels differ"
