@@ -4,7 +4,7 @@ src/mesh/mesh_raw.cpp, src/material/material_{diffuse,glossy,glass,mirror,proxy}
 src/light/light_{area,envconst,point,directional,env}.cpp, src/texture/texture_bitmap.cpp,
 src/objloader/objloader{,_simple}.cpp, src/model/model_wavefrontobj.cpp (with
 material::mixture_wavefrontobj), src/camera/camera_pinhole.cpp, src/film/film_bitmap.cpp,
-src/scheduler.cpp, src/renderer/renderer_{raycast,pt,lt,bdpt}.cpp and the headers they include (math.h,
+src/scheduler.cpp, src/renderer/renderer_{raycast,pt,lt,bdpt,bdptopt}.cpp and the headers they include (math.h,
 surface.h, scene.h, path.h, bidir.h, ...). stb_image, which texture_bitmap.cpp decodes images
 with, is not among the reference's sources: images reach it decoded, through register_image.
 
