@@ -2041,13 +2041,16 @@ BdShadeK bd_shade_for(uint32_t feat) {
     default: return k_bd_shade<4, kFeatMixture | kFeatTwoLevel>;
     }
 }
-using BdConnectK = decltype(&k_bd_connect<3, kFeatAll>);
+// Two resident blocks per SM (up to 128 registers, no spills) rather than three (80 registers,
+// 150-230 bytes of spills per thread): shade + connect 6.12 -> 5.84 ms on the headline BDPT frame
+// (A/B on one GB300, three alternating runs each).
+using BdConnectK = decltype(&k_bd_connect<2, kFeatAll>);
 BdConnectK bd_connect_for(uint32_t feat) {
     switch (feat & (kFeatEnvTex | kFeatMixture)) {
-    case 0: return k_bd_connect<3, 0u>;
-    case kFeatEnvTex: return k_bd_connect<3, kFeatEnvTex>;
-    case kFeatMixture: return k_bd_connect<3, kFeatMixture>;
-    default: return k_bd_connect<3, kFeatEnvTex | kFeatMixture>;
+    case 0: return k_bd_connect<2, 0u>;
+    case kFeatEnvTex: return k_bd_connect<2, kFeatEnvTex>;
+    case kFeatMixture: return k_bd_connect<2, kFeatMixture>;
+    default: return k_bd_connect<2, kFeatEnvTex | kFeatMixture>;
     }
 }
 
