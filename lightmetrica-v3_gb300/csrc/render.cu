@@ -2023,22 +2023,27 @@ Workspace& workspace(int device) {
 
 // Light-tracing and BDPT kernels specialised on the features they use: instances and mixture
 // materials (shade), the textured environment and mixture materials (connect).
-using LtShadeK = decltype(&k_lt_shade<4, kFeatAll>);
+// Three resident blocks per SM (up to 80 registers) rather than four (64 registers, up to 48
+// bytes of stack): the LT frame 16.04 -> 15.72 ms (A/B on one GB300, three alternating runs each).
+using LtShadeK = decltype(&k_lt_shade<3, kFeatAll>);
 LtShadeK lt_shade_for(uint32_t feat) {
     switch (feat & (kFeatMixture | kFeatTwoLevel)) {
-    case 0: return k_lt_shade<4, 0u>;
-    case kFeatMixture: return k_lt_shade<4, kFeatMixture>;
-    case kFeatTwoLevel: return k_lt_shade<4, kFeatTwoLevel>;
-    default: return k_lt_shade<4, kFeatMixture | kFeatTwoLevel>;
+    case 0: return k_lt_shade<3, 0u>;
+    case kFeatMixture: return k_lt_shade<3, kFeatMixture>;
+    case kFeatTwoLevel: return k_lt_shade<3, kFeatTwoLevel>;
+    default: return k_lt_shade<3, kFeatMixture | kFeatTwoLevel>;
     }
 }
-using BdShadeK = decltype(&k_bd_shade<4, kFeatAll>);
+// Three resident blocks per SM (up to 80 registers, no spills) rather than four (64 registers,
+// 80 bytes of stack): shade + connect 5.91 -> 5.48 ms on the headline BDPT frame (A/B on one
+// GB300, three alternating runs each).
+using BdShadeK = decltype(&k_bd_shade<3, kFeatAll>);
 BdShadeK bd_shade_for(uint32_t feat) {
     switch (feat & (kFeatMixture | kFeatTwoLevel)) {
-    case 0: return k_bd_shade<4, 0u>;
-    case kFeatMixture: return k_bd_shade<4, kFeatMixture>;
-    case kFeatTwoLevel: return k_bd_shade<4, kFeatTwoLevel>;
-    default: return k_bd_shade<4, kFeatMixture | kFeatTwoLevel>;
+    case 0: return k_bd_shade<3, 0u>;
+    case kFeatMixture: return k_bd_shade<3, kFeatMixture>;
+    case kFeatTwoLevel: return k_bd_shade<3, kFeatTwoLevel>;
+    default: return k_bd_shade<3, kFeatMixture | kFeatTwoLevel>;
     }
 }
 // Two resident blocks per SM (up to 128 registers, no spills) rather than three (80 registers,
